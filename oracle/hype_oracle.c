@@ -1,0 +1,712 @@
+/*
+ * hype_oracle.c -- CPU restatement of the reference's hot path (the oracle).
+ *
+ * TEST INFRASTRUCTURE ONLY.  tests/, the smoke check and bench.py's CPU
+ * baseline leg use it as the checker; the GPU product never links or calls it.
+ *
+ * Every arithmetic expression keeps the operation order of the reference line
+ * it follows, so that with -ffp-contract=off the restatement reproduces the
+ * reference compiled from its own sources bit for bit (checked by
+ * tests/test_oracle_vs_reference.py).  The loop structure, data layout and
+ * ghost handling are this file's own.
+ *
+ *   CTCS 2D plane-wave form     2d/ctcs/plane_wave/wave.c:161-203 (update :192, alpha :169)
+ *   CTCS point-source form      2d/ctcs/line_source/wave.c:149-173, 3d/ctcs/point_source/wave.c:163-194
+ *   Source() wavelet            3d/ctcs/point_source/wave.c:232-238
+ *   Euler RHS skeleton          3d/weno4/Navier-Stokes-3D/rhs_function.c:12-443 (viscous terms dropped)
+ *   boundary ghost fill         3d/weno4/Navier-Stokes-3D/rhs_function.c:52-181
+ *   CWENO4 weno()               3d/weno4/Viscous-Multiphase-Fourth-Order/reconstruction.c:38-259
+ *   evaluate_polynomial         3d/weno4/Viscous-Multiphase-Fourth-Order/reconstruction.c:12-21
+ *   PDEConsFlux / LLF           3d/weno4/Navier-Stokes-3D/pde.c:40-88, 164-187
+ *   dt = CFL h / (3 s_max)      3d/weno4/Navier-Stokes-3D/rhs_function.c:438-440
+ *   SSPRK(4,3) stage algebra    PETSc TSSSP RKS3 with 4 stages (3d/weno4/Navier-Stokes-3D/hype.c:185-187),
+ *                               restated from Ketcheson 2008 (see oracle/petsc_shim/petsc_shim.c)
+ */
+#include "hype_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+int orc_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ====================================================================== CTCS */
+
+static inline double at2(const double* p, int nx, int ny, int i, int j, int bc) {
+    if (i < 0 || i >= nx || j < 0 || j >= ny) {
+        if (bc == ORC_BC_PERIODIC) {
+            i = (i % nx + nx) % nx;
+            j = (j % ny + ny) % ny;
+        } else {
+            return 0.0; /* zero exterior (DM_BOUNDARY_GHOSTED) */
+        }
+    }
+    return p[(long)j * nx + i];
+}
+
+/* After a three-buffer rotation, leave (older, newest) in (p_old, p). */
+static void rotate_back(double* p_old, double* p, double* a, double* b, size_t bytes) {
+    if (b == p_old) {
+        memcpy(p, b, bytes);
+        memcpy(p_old, a, bytes);
+    } else {
+        if (a != p_old) memcpy(p_old, a, bytes);
+        if (b != p) memcpy(p, b, bytes);
+    }
+}
+
+int orc_ctcs2d_plane(int nx, int ny, double alpha, int bc, int nsteps, double* p_old, double* p, double* scratch) {
+    double* a = p_old;
+    double* b = p;
+    double* c = scratch;
+    const double a2 = alpha * alpha;
+    for (int s = 0; s < nsteps; ++s) {
+#pragma omp parallel for schedule(static)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const double pc = b[(long)j * nx + i];
+                double sum = at2(b, nx, ny, i, j + 1, bc) + at2(b, nx, ny, i, j - 1, bc) + at2(b, nx, ny, i + 1, j, bc) +
+                             at2(b, nx, ny, i - 1, j, bc) - 4.0 * pc;
+                c[(long)j * nx + i] = a2 * sum + 2.0 * pc - a[(long)j * nx + i];
+            }
+        double* t = a;
+        a = b;
+        b = c;
+        c = t;
+    }
+    rotate_back(p_old, p, a, b, sizeof(double) * (size_t)nx * ny);
+    return 0;
+}
+
+static double ricker_src(double t, double f0) {
+    double t0 = 4.0 / f0;
+    return -2.0 * (t - t0) * f0 * f0 * exp(-1.0 * f0 * f0 * (t - t0) * (t - t0));
+}
+
+static inline double at3(const double* p, const orc_ctcs_cfg* g, int i, int j, int k) {
+    if (i < 0 || i >= g->nx || j < 0 || j >= g->ny || k < 0 || k >= g->nz) {
+        if (g->bc != ORC_BC_PERIODIC) return 0.0;
+        i = (i % g->nx + g->nx) % g->nx;
+        j = (j % g->ny + g->ny) % g->ny;
+        k = (k % g->nz + g->nz) % g->nz;
+    }
+    return p[((long)k * g->ny + j) * g->nx + i];
+}
+
+static inline double d2_2(double m1, double c, double p1, double inv) { return (p1 - 2.0 * c + m1) * inv; }
+static inline double d2_4(double m2, double m1, double c, double p1, double p2, double inv) {
+    return (-1.0 / 12 * p2 + 4.0 / 3.0 * p1 - 5.0 / 2.0 * c + 4.0 / 3.0 * m1 - 1.0 / 12.0 * m2) * inv;
+}
+
+int orc_ctcs_pointsrc(const orc_ctcs_cfg* g, const double* cf, int nsteps, double* p_old, double* p, double* scratch,
+                      double* receiver) {
+    const long n = (long)g->nx * g->ny * (g->dim == 3 ? g->nz : 1);
+    orc_ctcs_cfg G = *g;
+    if (G.dim == 2) G.nz = 1;
+    double* a = p_old;
+    double* b = p;
+    double* c = scratch;
+    const double ix2 = 1.0 / (g->dx * g->dx), iy2 = 1.0 / (g->dy * g->dy), iz2 = 1.0 / (g->dz * g->dz);
+    const double dt = g->dt;
+    for (int s = 0; s < nsteps; ++s) {
+        const int it = g->it0 + s;
+        if (receiver) receiver[s] = b[((long)(g->dim == 3 ? g->rec_k : 0) * G.ny + g->rec_j) * G.nx + g->rec_i];
+#pragma omp parallel for schedule(static) collapse(2)
+        for (int k = 0; k < G.nz; ++k)
+            for (int j = 0; j < G.ny; ++j)
+                for (int i = 0; i < G.nx; ++i) {
+                    long o = ((long)k * G.ny + j) * G.nx + i;
+                    double pc = b[o], lap;
+                    if (g->order == 4) {
+                        double pxx = d2_4(at3(b, &G, i - 2, j, k), at3(b, &G, i - 1, j, k), pc, at3(b, &G, i + 1, j, k),
+                                          at3(b, &G, i + 2, j, k), ix2);
+                        double pyy = d2_4(at3(b, &G, i, j - 2, k), at3(b, &G, i, j - 1, k), pc, at3(b, &G, i, j + 1, k),
+                                          at3(b, &G, i, j + 2, k), iy2);
+                        if (g->dim == 3) {
+                            double pzz = d2_4(at3(b, &G, i, j, k - 2), at3(b, &G, i, j, k - 1), pc, at3(b, &G, i, j, k + 1),
+                                              at3(b, &G, i, j, k + 2), iz2);
+                            lap = pxx + pyy + pzz;
+                        } else {
+                            lap = pxx + pyy;
+                        }
+                    } else {
+                        double pxx = d2_2(at3(b, &G, i - 1, j, k), pc, at3(b, &G, i + 1, j, k), ix2);
+                        double pyy = d2_2(at3(b, &G, i, j - 1, k), pc, at3(b, &G, i, j + 1, k), iy2);
+                        if (g->dim == 3) {
+                            double pzz = d2_2(at3(b, &G, i, j, k - 1), pc, at3(b, &G, i, j, k + 1), iz2);
+                            lap = pxx + pyy + pzz;
+                        } else {
+                            lap = pxx + pyy;
+                        }
+                    }
+                    double cc = cf ? cf[o] : g->c0;
+                    double v = 2.0 * pc - a[o] + cc * cc * dt * dt * lap;
+                    if (i == g->src_i && j == g->src_j && (g->dim == 2 || k == g->src_k)) {
+                        double vol = (g->dim == 3) ? g->dx * g->dy * g->dz : g->dx * g->dy;
+                        v += ricker_src(it * dt, g->f0) / vol * dt * dt;
+                    }
+                    c[o] = v;
+                }
+        double* t = a;
+        a = b;
+        b = c;
+        c = t;
+    }
+    rotate_back(p_old, p, a, b, sizeof(double) * (size_t)n);
+    return 0;
+}
+
+int orc_ctcs_monopole(const orc_mono_cfg* g, int nsteps, double* p_old, double* p, double* scratch) {
+    double* a = p_old;
+    double* b = p;
+    double* c = scratch;
+    const int nx = g->nx, ny = g->ny;
+    const double inv = 1.0 / (g->h * g->h);
+    const double k2 = g->c0 * g->c0 * g->dt * g->dt;
+    const double r2s = 1.0 / (2.0 * g->sigma * g->sigma);
+    const double two_pi = 6.283185307179586;
+    for (int s = 0; s < nsteps; ++s) {
+        const double t = (double)(g->it0 + s) * g->dt;
+        const double st = sin(two_pi * g->freq * t);
+#pragma omp parallel for schedule(static)
+        for (int j = 0; j < ny; ++j) {
+            const double y = g->ymin + j * g->h;
+            for (int i = 0; i < nx; ++i) {
+                const double x = g->xmin + i * g->h;
+                long o = (long)j * nx + i;
+                double pc = b[o];
+                double pxx = d2_2(at2(b, nx, ny, i - 1, j, ORC_BC_ZERO), pc, at2(b, nx, ny, i + 1, j, ORC_BC_ZERO), inv);
+                double pyy = d2_2(at2(b, nx, ny, i, j - 1, ORC_BC_ZERO), pc, at2(b, nx, ny, i, j + 1, ORC_BC_ZERO), inv);
+                double dx = x - g->xs, dy = y - g->ys;
+                double src = exp(-(dx * dx + dy * dy) * r2s) * st;
+                c[o] = 2.0 * pc - a[o] + k2 * (pxx + pyy) + k2 * src;
+            }
+        }
+        double* tt = a;
+        a = b;
+        b = c;
+        c = tt;
+    }
+    rotate_back(p_old, p, a, b, sizeof(double) * (size_t)nx * ny);
+    return 0;
+}
+
+/* ============================================================ CWENO4 (3D) */
+
+static const double R1_6 = 1. / 6.;
+static const double R1_12 = 1. / 12.;
+static const double R3_20 = 3. / 20.;
+static const double R1_120 = 1. / 120.;
+static const double R13_3 = 13. / 3.;
+static const double R7_6 = 7. / 6.;
+static const double R61_48 = 61. / 48.;
+static const double SMALL = 1.0e-12;
+
+/* Stencil of one cell and one variable, addressed by direction.
+ *   c         centre
+ *   m2,m1,p1,p2[d]   1D neighbours along d (0=x,1=y,2=z)
+ *   q[a][b][sa][sb]  diagonal neighbour at +/-1 along a and b (s: 0 -> -1, 1 -> +1)
+ *   o[sx][sy][sz]    body-diagonal neighbour */
+typedef struct {
+    double c;
+    double m2[3], m1[3], p1[3], p2[3];
+    double q[3][3][2][2];
+    double o[2][2][2];
+} Stencil;
+
+/* R4 cross derivative, reference pattern 0.25*(mm - mp - pm + pp) (weno() :94-96) */
+static inline double r4_cross(const Stencil* s, int a, int b) {
+    return 0.25 * (s->q[a][b][0][0] - s->q[a][b][0][1] - s->q[a][b][1][0] + s->q[a][b][1][1]);
+}
+/* u_aab (:100,:102,:104): 0.25*(-mm + mp - pm + pp) + 0.5*(u_b-1 - u_b+1) */
+static inline double r4_aab(const Stencil* s, int a, int b) {
+    return 0.25 * (-s->q[a][b][0][0] + s->q[a][b][0][1] - s->q[a][b][1][0] + s->q[a][b][1][1]) + 0.5 * (s->m1[b] - s->p1[b]);
+}
+/* u_abb (:101,:103,:105): 0.5*(u_a-1 - u_a+1) + 0.25*(pp - mm - mp + pm) */
+static inline double r4_abb(const Stencil* s, int a, int b) {
+    return 0.5 * (s->m1[a] - s->p1[a]) + 0.25 * (s->q[a][b][1][1] - s->q[a][b][0][0] - s->q[a][b][0][1] + s->q[a][b][1][0]);
+}
+/* centred R3 cross derivative (:129-131): 0.25*(pp - pm - mp + mm) */
+static inline double r3_cross0(const Stencil* s, int a, int b) {
+    return 0.25 * (s->q[a][b][1][1] - s->q[a][b][1][0] - s->q[a][b][0][1] + s->q[a][b][0][0]);
+}
+
+/* Quantities of one R3 stencil: d[0..2] first derivatives, dd[0..2] second,
+ * x[0..2] cross terms in the order xy, yz, xz. */
+typedef struct {
+    double d[3], dd[3], x[3];
+} R3;
+
+static inline double is3(const R3* r) {
+    return (r->d[0] * r->d[0] + r->d[1] * r->d[1] + r->d[2] * r->d[2]) +
+           R13_3 * (r->dd[0] * r->dd[0] + r->dd[1] * r->dd[1] + r->dd[2] * r->dd[2]) +
+           R7_6 * (r->x[0] * r->x[0] + r->x[1] * r->x[1] + r->x[2] * r->x[2]);
+}
+
+/* cross-term slot for a pair of directions: xy -> 0, yz -> 1, xz -> 2 */
+static inline int xslot(int a, int b) {
+    if ((a == 0 && b == 1) || (a == 1 && b == 0)) return 0;
+    if ((a == 1 && b == 2) || (a == 2 && b == 1)) return 1;
+    return 2;
+}
+
+/* CWENO4 with gammaHi = gammaLo = gam (0.85 in the reference); linear=1 returns
+ * the R4 polynomial itself (the optimal-weight limit). */
+static void cweno4(const Stencil* s, double gam, int linear, double* coef) {
+    const double u0 = s->c;
+    double d4[3], dd4[3], ddd4[3];
+    for (int d = 0; d < 3; ++d) {
+        d4[d] = R1_120 * (11.0 * s->m2[d] - 82.0 * s->m1[d] + 82.0 * s->p1[d] - 11.0 * s->p2[d]);
+        dd4[d] = 0.5 * (s->m1[d] - 2.0 * u0 + s->p1[d]);
+        ddd4[d] = R1_12 * (-s->m2[d] + 2.0 * (s->m1[d] - s->p1[d]) + s->p2[d]);
+    }
+    const double xy4 = r4_cross(s, 0, 1), yz4 = r4_cross(s, 1, 2), xz4 = r4_cross(s, 2, 0);
+    const double xxy = r4_aab(s, 0, 1), xyy = r4_abb(s, 0, 1);
+    const double yyz = r4_aab(s, 1, 2), yzz = r4_abb(s, 1, 2);
+    const double xxz = r4_aab(s, 0, 2), xzz = r4_abb(s, 0, 2);
+    const double xyz = 0.125 * (s->o[1][1][1] - s->o[0][1][1] - s->o[1][0][1] - s->o[1][1][0] + s->o[0][0][1] +
+                                s->o[0][1][0] + s->o[1][0][0] - s->o[0][0][0]);
+    if (linear) {
+        coef[0] = u0;
+        coef[1] = d4[0]; coef[2] = d4[1]; coef[3] = d4[2];
+        coef[4] = dd4[0]; coef[5] = dd4[1]; coef[6] = dd4[2];
+        coef[7] = xy4; coef[8] = yz4; coef[9] = xz4;
+        coef[10] = ddd4[0]; coef[11] = ddd4[1]; coef[12] = ddd4[2];
+        coef[13] = xxy; coef[14] = xyy; coef[15] = yyz; coef[16] = yzz; coef[17] = xxz; coef[18] = xzz; coef[19] = xyz;
+        return;
+    }
+    const double IS4 = d4[0] * d4[0] + d4[1] * d4[1] + d4[2] * d4[2] + R13_3 * (dd4[0] * dd4[0] + dd4[1] * dd4[1] + dd4[2] * dd4[2]) +
+                       R7_6 * (xy4 * xy4 + yz4 * yz4 + xz4 * xz4) + 0.2 * (d4[0] * ddd4[0] + d4[1] * ddd4[1] + d4[2] * ddd4[2]) +
+                       4.7 * (xxy * xxy + xxz * xxz + xyy * xyy + xzz * xzz + yyz * yyz + yzz * yzz) +
+                       39.06 * (ddd4[0] * ddd4[0] + ddd4[1] * ddd4[1] + ddd4[2] * ddd4[2]) + R61_48 * xyz * xyz;
+
+    /* the seven R3 stencils: 0 centred, 1+2d one-sided towards +d, 2+2d towards -d */
+    R3 r[7];
+    for (int d = 0; d < 3; ++d) {
+        r[0].d[d] = 0.5 * (s->p1[d] - s->m1[d]);
+        r[0].dd[d] = 0.5 * (s->m1[d] - 2.0 * u0 + s->p1[d]);
+    }
+    r[0].x[0] = r3_cross0(s, 0, 1);
+    r[0].x[1] = r3_cross0(s, 1, 2);
+    r[0].x[2] = r3_cross0(s, 2, 0);
+    for (int d = 0; d < 3; ++d) {
+        R3* P = &r[1 + 2 * d];
+        R3* M = &r[2 + 2 * d];
+        *P = r[0];
+        *M = r[0];
+        P->d[d] = -1.5 * u0 + 2.0 * s->p1[d] - 0.5 * s->p2[d];
+        P->dd[d] = 0.5 * (u0 - 2.0 * s->p1[d] + s->p2[d]);
+        M->d[d] = -2.0 * s->m1[d] + 0.5 * s->m2[d] + 1.5 * u0;
+        M->dd[d] = 0.5 * (s->m2[d] - 2.0 * s->m1[d] + u0);
+        for (int e = 0; e < 3; ++e) {
+            if (e == d) continue;
+            int k = xslot(d, e);
+            P->x[k] = 0.5 * (s->q[d][e][1][1] - s->q[d][e][1][0]) - r[0].d[e];
+            M->x[k] = 0.5 * (s->q[d][e][0][0] - s->q[d][e][0][1]) + r[0].d[e];
+        }
+    }
+    double g3[7];
+    g3[0] = (1.0 - gam) * gam;
+    for (int i = 1; i < 7; ++i) g3[i] = R1_6 * (1 - gam) * (1 - gam);
+    double w4 = gam / pow((IS4 + SMALL), 4.0);
+    double total = w4;
+    double w3[7];
+    for (int i = 0; i < 7; ++i) {
+        w3[i] = g3[i] / pow((is3(&r[i]) + SMALL), 4.0);
+        total += w3[i];
+    }
+    w4 = w4 / total;
+    for (int i = 0; i < 7; ++i) w3[i] = w3[i] / total;
+    double l[9] = {0}, nl[9] = {0};
+    for (int i = 0; i < 7; ++i) {
+        for (int d = 0; d < 3; ++d) {
+            l[d] += g3[i] * r[i].d[d];
+            nl[d] += w3[i] * r[i].d[d];
+        }
+        for (int d = 0; d < 3; ++d) {
+            l[3 + d] += g3[i] * r[i].dd[d];
+            nl[3 + d] += w3[i] * r[i].dd[d];
+        }
+        for (int d = 0; d < 3; ++d) {
+            l[6 + d] += g3[i] * r[i].x[d];
+            nl[6 + d] += w3[i] * r[i].x[d];
+        }
+    }
+    const double wr = w4 / gam;
+    const double lin4[9] = {d4[0], d4[1], d4[2], dd4[0], dd4[1], dd4[2], xy4, yz4, xz4};
+    coef[0] = u0;
+    for (int q = 0; q < 9; ++q) coef[1 + q] = wr * (lin4[q] - l[q]) + nl[q];
+    coef[10] = wr * ddd4[0];
+    coef[11] = wr * ddd4[1];
+    coef[12] = wr * ddd4[2];
+    coef[13] = wr * xxy;
+    coef[14] = wr * xyy;
+    coef[15] = wr * yyz;
+    coef[16] = wr * yzz;
+    coef[17] = wr * xxz;
+    coef[18] = wr * xzz;
+    coef[19] = wr * xyz;
+}
+
+double orc_eval_poly3(double x, double y, double z, const double* c) {
+    return c[0] + c[1] * x + c[2] * y + c[3] * z + c[4] * (x * x - R1_12) + c[5] * (y * y - R1_12) + c[6] * (z * z - R1_12) +
+           c[7] * x * y + c[8] * y * z + c[9] * z * x + c[10] * x * (x * x - R3_20) + c[11] * y * (y * y - R3_20) +
+           c[12] * z * (z * z - R3_20) + c[13] * (x * x - R1_12) * y + c[14] * x * (y * y - R1_12) +
+           c[15] * (y * y - R1_12) * z + c[16] * y * (z * z - R1_12) + c[17] * (x * x - R1_12) * z +
+           c[18] * x * (z * z - R1_12) + c[19] * x * y * z;
+}
+
+void orc_cweno4_ref_args(const double* Ux, const double* Uy, const double* Uz, const double* Uxy, const double* Uyz,
+                         const double* Uzx, const double* Uxyz, double* coeffs) {
+    Stencil s;
+    memset(&s, 0, sizeof(s));
+    s.c = Uxy[0];
+    const double* U1[3] = {Ux, Uy, Uz};
+    for (int d = 0; d < 3; ++d) {
+        s.m2[d] = U1[d][0]; s.m1[d] = U1[d][1]; s.p1[d] = U1[d][3]; s.p2[d] = U1[d][4];
+    }
+    /* reference argument layout: [1]=(+a,+b) [2]=(+a,-b) [3]=(-a,+b) [4]=(-a,-b) for the
+     * pairs (x,y), (y,z) and, for U_zx, [1]=(+z,+x) [2]=(+z,-x) [3]=(-z,+x) [4]=(-z,-x) */
+    const double* U2[3] = {Uxy, Uyz, Uzx};
+    const int pa[3] = {0, 1, 2}, pb[3] = {1, 2, 0};
+    for (int p = 0; p < 3; ++p) {
+        int a = pa[p], b = pb[p];
+        double pp = U2[p][1], pm = U2[p][2], mp = U2[p][3], mm = U2[p][4];
+        s.q[a][b][1][1] = pp; s.q[a][b][1][0] = pm; s.q[a][b][0][1] = mp; s.q[a][b][0][0] = mm;
+        s.q[b][a][1][1] = pp; s.q[b][a][0][1] = pm; s.q[b][a][1][0] = mp; s.q[b][a][0][0] = mm;
+    }
+    /* U_xyz: (+++),(-++),(+-+),(++-),(--+),(-+-),(+--),(---) */
+    const int sx[8] = {1, 0, 1, 1, 0, 0, 1, 0}, sy[8] = {1, 1, 0, 1, 0, 1, 0, 0}, sz[8] = {1, 1, 1, 0, 1, 0, 0, 0};
+    for (int q = 0; q < 8; ++q) s.o[sx[q]][sy[q]][sz[q]] = Uxyz[q];
+    cweno4(&s, 0.85, 0, coeffs);
+}
+
+/* ============================================================ Rusanov flux */
+
+/* PDEConsFlux for an axis normal dir (pde.c:40-88): flux, max wave speed;
+ * *bad set when rho < 1e-14 or p < 1e-12. */
+static inline double cons_flux(const double* Q, int dir, double gm1, double gamma, double* F, int* bad) {
+    const double rho = Q[0];
+    const double r1_rho = 1.0 / rho;
+    const double u = r1_rho * Q[1], v = r1_rho * Q[2], w = r1_rho * Q[3];
+    const double E = Q[4];
+    const double p = gm1 * (E - 0.5 * rho * (u * u + v * v + w * w));
+    if (rho < 1.0e-14 || p < 1.0e-12) *bad = 1;
+    const double un = dir == 0 ? u : (dir == 1 ? v : w);
+    /* the reference's n-weighted sums with one unit component keep exactly the
+     * product order (rho*u)*v etc. of the term that survives */
+    F[0] = rho * un;
+    if (dir == 0) {
+        F[1] = rho * u * u + p;
+        F[2] = rho * u * v;
+        F[3] = rho * u * w;
+    } else if (dir == 1) {
+        F[1] = rho * u * v;
+        F[2] = rho * v * v + p;
+        F[3] = rho * v * w;
+    } else {
+        F[1] = rho * u * w;
+        F[2] = rho * v * w;
+        F[3] = rho * w * w + p;
+    }
+    F[4] = (E + p) * un;
+    const double a = sqrt(r1_rho * gamma * p);
+    return fabs(un) + a;
+}
+
+double orc_rusanov(const double* QL, const double* QR, int dir, double gamma, double* flux, int* bad) {
+    double FL[5], FR[5];
+    const double gm1 = gamma - 1.0;
+    double sl = cons_flux(QL, dir, gm1, gamma, FL, bad);
+    double sr = cons_flux(QR, dir, gm1, gamma, FR, bad);
+    double s = (sl < sr) ? sr : sl;
+    for (int c = 0; c < 5; ++c) flux[c] = 0.5 * (FR[c] + FL[c] - s * (QR[c] - QL[c]));
+    return s;
+}
+
+/* ============================================================ Euler RHS */
+
+#define NV 5
+#define NTR 24 /* traces per cell and variable: face f (0..5) x Gauss point g (0..3) -> f*4+g */
+
+static const double GP = 0.28867513459481287;
+static const double GPX[4] = {-0.28867513459481287, -0.28867513459481287, 0.28867513459481287, 0.28867513459481287};
+static const double GPY[4] = {-0.28867513459481287, 0.28867513459481287, -0.28867513459481287, 0.28867513459481287};
+
+/* boundary map of one index: returns the source index, *flip set for a reflective ghost */
+static inline int bmap(int i, int n, int blo, int bhi, int* flip) {
+    if (i < 0) {
+        if (blo == ORC_BC_PERIODIC) return i + n;
+        if (blo == ORC_BC_TRANSMISSIVE) return 0;
+        *flip = 1;
+        return -1 - i;
+    }
+    if (i >= n) {
+        if (bhi == ORC_BC_PERIODIC) return i - n;
+        if (bhi == ORC_BC_TRANSMISSIVE) return n - 1;
+        *flip = 1;
+        return 2 * (n - 1) - i + 1;
+    }
+    return i;
+}
+
+typedef struct {
+    const orc_euler_cfg* g;
+    int gx, gy, gz; /* padded dims (n + 6) */
+    double* pad;    /* padded state, ghost width 3, AoS */
+} Padded;
+
+static void build_padded(Padded* P, const orc_euler_cfg* g, const double* U) {
+    const int nx = g->nx, ny = g->ny, nz = g->nz;
+    P->g = g;
+    P->gx = nx + 6; P->gy = ny + 6; P->gz = nz + 6;
+#pragma omp parallel for schedule(static) collapse(2)
+    for (int k = -3; k < nz + 3; ++k)
+        for (int j = -3; j < ny + 3; ++j)
+            for (int i = -3; i < nx + 3; ++i) {
+                int fx = 0, fy = 0, fz = 0;
+                int si = bmap(i, nx, g->bc[0], g->bc[1], &fx);
+                int sj = bmap(j, ny, g->bc[2], g->bc[3], &fy);
+                int sk = bmap(k, nz, g->bc[4], g->bc[5], &fz);
+                const double* q = U + (((long)sk * ny + sj) * nx + si) * NV;
+                double* o = P->pad + (((long)(k + 3) * P->gy + (j + 3)) * P->gx + (i + 3)) * NV;
+                for (int c = 0; c < NV; ++c) o[c] = q[c];
+                if (fx) o[1] = -o[1];
+                if (fy) o[2] = -o[2];
+                if (fz) o[3] = -o[3];
+            }
+}
+
+static inline const double* padp(const Padded* P, int i, int j, int k) {
+    return P->pad + (((long)(k + 3) * P->gy + (j + 3)) * P->gx + (i + 3)) * NV;
+}
+
+static void gather(const Padded* P, int i, int j, int k, int c, Stencil* s) {
+    s->c = padp(P, i, j, k)[c];
+    for (int d = 0; d < 3; ++d) {
+        int ex = d == 0, ey = d == 1, ez = d == 2;
+        s->m2[d] = padp(P, i - 2 * ex, j - 2 * ey, k - 2 * ez)[c];
+        s->m1[d] = padp(P, i - ex, j - ey, k - ez)[c];
+        s->p1[d] = padp(P, i + ex, j + ey, k + ez)[c];
+        s->p2[d] = padp(P, i + 2 * ex, j + 2 * ey, k + 2 * ez)[c];
+    }
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            if (a == b) continue;
+            for (int sa = 0; sa < 2; ++sa)
+                for (int sb = 0; sb < 2; ++sb) {
+                    int off[3] = {0, 0, 0};
+                    off[a] = 2 * sa - 1;
+                    off[b] = 2 * sb - 1;
+                    s->q[a][b][sa][sb] = padp(P, i + off[0], j + off[1], k + off[2])[c];
+                }
+        }
+    for (int sx = 0; sx < 2; ++sx)
+        for (int sy = 0; sy < 2; ++sy)
+            for (int sz = 0; sz < 2; ++sz) s->o[sx][sy][sz] = padp(P, i + 2 * sx - 1, j + 2 * sy - 1, k + 2 * sz - 1)[c];
+}
+
+/* traces of one cell: tr[c*NTR + f*4 + g], faces 0..5 = -x,+x,-y,+y,-z,+z */
+static void cell_traces(const Padded* P, int i, int j, int k, double gam, int linear, double* tr) {
+    Stencil s;
+    double coef[20];
+    for (int c = 0; c < NV; ++c) {
+        gather(P, i, j, k, c, &s);
+        cweno4(&s, gam, linear, coef);
+        double* t = tr + c * NTR;
+        for (int g = 0; g < 4; ++g) {
+            t[0 * 4 + g] = orc_eval_poly3(-0.5, GPX[g], GPY[g], coef);
+            t[1 * 4 + g] = orc_eval_poly3(0.5, GPX[g], GPY[g], coef);
+            t[2 * 4 + g] = orc_eval_poly3(GPX[g], -0.5, GPY[g], coef);
+            t[3 * 4 + g] = orc_eval_poly3(GPX[g], 0.5, GPY[g], coef);
+            t[4 * 4 + g] = orc_eval_poly3(GPX[g], GPY[g], -0.5, coef);
+            t[5 * 4 + g] = orc_eval_poly3(GPX[g], GPY[g], 0.5, coef);
+        }
+    }
+    (void)GP;
+}
+
+/* face flux from the left cell's trace set (face fl) and the right cell's (face fr) */
+static inline double face_flux(const double* trL, int fl, const double* trR, int fr, int dir, double gamma, double* F, int* bad) {
+    double smax = 0.0;
+    for (int c = 0; c < NV; ++c) F[c] = 0.0;
+    for (int g = 0; g < 4; ++g) {
+        double QL[NV], QR[NV], fl5[NV];
+        for (int c = 0; c < NV; ++c) {
+            QL[c] = trL[c * NTR + fl * 4 + g];
+            QR[c] = trR[c * NTR + fr * 4 + g];
+        }
+        double s = orc_rusanov(QL, QR, dir, gamma, fl5, bad);
+        if (s > smax) smax = s;
+        for (int c = 0; c < NV; ++c) F[c] += 0.25 * fl5[c];
+    }
+    return smax;
+}
+
+int orc_euler_rhs(const orc_euler_cfg* g, const double* U, double* RHS, double* smax_out, long* bad_out) {
+    const int nx = g->nx, ny = g->ny, nz = g->nz;
+    const double gam = 0.85;
+    const int linear = g->recon == 1;
+    const double r1_h = 1. / (g->h);
+#ifdef _OPENMP
+    if (g->nthreads > 0) omp_set_num_threads(g->nthreads);
+#endif
+    Padded P;
+    P.pad = (double*)malloc(sizeof(double) * (size_t)(nx + 6) * (ny + 6) * (nz + 6) * NV);
+    if (!P.pad) return 3;
+    build_padded(&P, g, U);
+    /* traces for two planes (k-1, k), cells i,j in [-1, n] */
+    const int tx = nx + 2, ty = ny + 2;
+    const size_t plane = (size_t)tx * ty * NV * NTR;
+    double* T[2];
+    T[0] = (double*)malloc(sizeof(double) * plane);
+    T[1] = (double*)malloc(sizeof(double) * plane);
+    /* z fluxes at the face below the current plane, and the previous one */
+    double* H[2];
+    H[0] = (double*)malloc(sizeof(double) * (size_t)nx * ny * NV);
+    H[1] = (double*)malloc(sizeof(double) * (size_t)nx * ny * NV);
+    double* F = (double*)malloc(sizeof(double) * (size_t)(nx + 1) * ny * NV);
+    double* G = (double*)malloc(sizeof(double) * (size_t)nx * (ny + 1) * NV);
+    if (!T[0] || !T[1] || !H[0] || !H[1] || !F || !G) return 3;
+    double smax = 0.0;
+    long bad = -1;
+#define TR(buf, i, j) ((buf) + ((size_t)((j) + 1) * tx + ((i) + 1)) * NV * NTR)
+    for (int k = -1; k <= nz; ++k) {
+        double* Tk = T[(k + 2) & 1];
+        double* Tkm1 = T[(k + 1) & 1];
+        const int ghostk = (k < 0 || k >= nz);
+        /* reconstruct the cells of plane k that some face of an interior cell needs */
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int j = -1; j <= ny; ++j) {
+            const int ghostj = (j < 0 || j >= ny);
+            if (ghostk && ghostj) continue;
+            for (int i = -1; i <= nx; ++i) {
+                const int ghosti = (i < 0 || i >= nx);
+                if (ghosti + ghostj + ghostk > 1) continue;
+                cell_traces(&P, i, j, k, gam, linear, TR(Tk, i, j));
+            }
+        }
+        if (k < 0) continue;
+        double* Hk = H[k & 1];      /* face k-1/2 */
+        double* Hkm1 = H[(k + 1) & 1]; /* face k-3/2 (from the previous plane) */
+        double smax_k = 0.0;
+        int bad_k = 0;
+        /* z faces between plane k-1 and k (for k == nz: the top face of plane nz-1) */
+#pragma omp parallel for schedule(static) reduction(max : smax_k) reduction(| : bad_k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                int b = 0;
+                double s = face_flux(TR(Tkm1, i, j), 5, TR(Tk, i, j), 4, 2, g->gamma, Hk + ((size_t)j * nx + i) * NV, &b);
+                if (s > smax_k) smax_k = s;
+                bad_k |= b;
+            }
+        if (bad_k && bad < 0) bad = (long)k * nx * ny;
+        if (smax_k > smax) smax = smax_k;
+        if (k == 0) continue;
+        /* plane kk = k-1 is complete: x and y faces, then the divergence */
+        const int kk = k - 1;
+        double* Tc = Tkm1;
+        double smax_p = 0.0;
+        int bad_p = 0;
+#pragma omp parallel for schedule(static) reduction(max : smax_p) reduction(| : bad_p)
+        for (int j = 0; j < ny; ++j) {
+            for (int i = 0; i <= nx; ++i) {
+                int b = 0;
+                double s = face_flux(TR(Tc, i - 1, j), 1, TR(Tc, i, j), 0, 0, g->gamma, F + ((size_t)j * (nx + 1) + i) * NV, &b);
+                if (s > smax_p) smax_p = s;
+                bad_p |= b;
+            }
+        }
+#pragma omp parallel for schedule(static) reduction(max : smax_p) reduction(| : bad_p)
+        for (int j = 0; j <= ny; ++j) {
+            for (int i = 0; i < nx; ++i) {
+                int b = 0;
+                double s = face_flux(TR(Tc, i, j - 1), 3, TR(Tc, i, j), 2, 1, g->gamma, G + ((size_t)j * nx + i) * NV, &b);
+                if (s > smax_p) smax_p = s;
+                bad_p |= b;
+            }
+        }
+        if (bad_p && bad < 0) bad = (long)kk * nx * ny;
+        if (smax_p > smax) smax = smax_p;
+#pragma omp parallel for schedule(static)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                double* r = RHS + (((size_t)kk * ny + j) * nx + i) * NV;
+                const double* Fl = F + ((size_t)j * (nx + 1) + i) * NV;
+                const double* Fr = Fl + NV;
+                const double* Gl = G + ((size_t)j * nx + i) * NV;
+                const double* Gr = G + ((size_t)(j + 1) * nx + i) * NV;
+                const double* Hl = Hkm1 + ((size_t)j * nx + i) * NV;
+                const double* Hr = Hk + ((size_t)j * nx + i) * NV;
+                for (int c = 0; c < NV; ++c)
+                    r[c] = -r1_h * (Fr[c] - Fl[c]) - r1_h * (Gr[c] - Gl[c]) - r1_h * (Hr[c] - Hl[c]);
+            }
+    }
+#undef TR
+    free(P.pad);
+    free(T[0]); free(T[1]); free(H[0]); free(H[1]); free(F); free(G);
+    if (smax_out) *smax_out = smax;
+    if (bad_out) *bad_out = bad;
+    return bad >= 0 ? 2 : 0;
+}
+
+/* dt = CFL*h/(3*s_max), rhs_function.c:438 with the viscous speed zero */
+static inline double euler_dt(const orc_euler_cfg* g, double smax) { return (1.0 / 3.0) * (g->cfl * g->h) / (smax + 0.0); }
+
+int orc_euler_run(const orc_euler_cfg* g, int nsteps, int dt_mode, double* U, double* t_inout, double* dt_inout, long* bad) {
+    const size_t n = (size_t)g->nx * g->ny * g->nz * NV;
+    double* u1 = (double*)malloc(sizeof(double) * n);
+    double* F = (double*)malloc(sizeof(double) * n);
+    double smax;
+    double t = t_inout ? *t_inout : 0.0;
+    double dt = 0.0;
+    int rc = 0;
+    /* initial RHS call that sets the first dt (hype.c:175-180); its result is
+     * also the first stage of the first step (same input) */
+    rc = orc_euler_rhs(g, U, F, &smax, bad);
+    if (rc) goto out;
+    double dt_last = euler_dt(g, smax);
+    dt = (dt_mode == 2) ? *dt_inout : dt_last;
+    for (int s = 0; s < nsteps; ++s) {
+        /* stage 1: u1 = u + dt/2 F(u) */
+        if (s > 0) rc = orc_euler_rhs(g, U, F, &smax, bad);
+        if (rc) goto out;
+        const double dtr = dt / 2;
+#pragma omp parallel for schedule(static)
+        for (size_t q = 0; q < n; ++q) u1[q] = U[q] + dtr * F[q];
+        /* stage 2: u2 = u1 + dt/2 F(u1)  (kept in u1; U still holds u^n) */
+        rc = orc_euler_rhs(g, u1, F, &smax, bad);
+        if (rc) goto out;
+#pragma omp parallel for schedule(static)
+        for (size_t q = 0; q < n; ++q) u1[q] = u1[q] + dtr * F[q];
+        /* stage 3: u3 = 2/3 u + dt/6 F(u2) + 1/3 u2 */
+        rc = orc_euler_rhs(g, u1, F, &smax, bad);
+        if (rc) goto out;
+        const double a3 = 1.0 * 2 / (2 * 2 - 1.0), b3 = (2 - 1.0) * dt / (2 * (2 * 2 - 1)), c3 = (2 - 1.0) / (2 * 2 - 1);
+#pragma omp parallel for schedule(static)
+        for (size_t q = 0; q < n; ++q) u1[q] = a3 * U[q] + b3 * F[q] + c3 * u1[q];
+        /* stage 4: u^{n+1} = u3 + dt/2 F(u3) */
+        rc = orc_euler_rhs(g, u1, F, &smax, bad);
+        if (rc) goto out;
+#pragma omp parallel for schedule(static)
+        for (size_t q = 0; q < n; ++q) U[q] = u1[q] + dtr * F[q];
+        t += dt;
+        dt_last = euler_dt(g, smax);
+        if (dt_mode == 0) dt = dt_last;
+    }
+out:
+    free(u1);
+    free(F);
+    if (t_inout) *t_inout = t;
+    if (dt_inout) *dt_inout = dt;
+    return rc;
+}

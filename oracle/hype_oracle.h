@@ -1,0 +1,80 @@
+/*
+ * hype_oracle.h -- CPU restatement of the reference's hot path.
+ * TEST INFRASTRUCTURE ONLY: used by tests/, the smoke check and the CPU
+ * baseline leg of bench.py as the checker.  The GPU product never calls it.
+ *
+ * Layouts follow the reference's DMDA vectors: AoS doubles [k][j][i][c],
+ * x fastest, no ghosts (ghosts are built internally from the boundary codes).
+ */
+#ifndef HYPE_ORACLE_H
+#define HYPE_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* boundary codes (shared with include/hype_gpu.h) */
+#define ORC_BC_PERIODIC 0
+#define ORC_BC_REFLECTIVE 1
+#define ORC_BC_TRANSMISSIVE 2
+#define ORC_BC_ZERO 3
+
+/* 2D CTCS, reference form of 2d/ctcs/plane_wave/wave.c:192 (5-point, alpha = c dt / h). */
+int orc_ctcs2d_plane(int nx, int ny, double alpha, int bc, int nsteps, double* p_old, double* p, double* scratch);
+
+/* 2D/3D CTCS, reference form of 2d/ctcs/line_source/wave.c:155-173 and
+ * 3d/ctcs/point_source/wave.c:173-194: 2nd (order=2) or 4th (order=4) order
+ * Laplacian, c field (NULL -> constant c0), optional Ricker-type point source
+ * (src_i < 0 -> none) with dominant frequency f0, receiver trace out. */
+typedef struct {
+    int dim, nx, ny, nz, order, bc;
+    double dx, dy, dz, dt, c0, f0;
+    int src_i, src_j, src_k;
+    int rec_i, rec_j, rec_k;
+    int it0; /* step counter of the first update (time = it*dt) */
+} orc_ctcs_cfg;
+int orc_ctcs_pointsrc(const orc_ctcs_cfg* cfg, const double* c, int nsteps, double* p_old, double* p, double* scratch,
+                      double* receiver);
+
+/* Gaussian-monopole CTCS (one batched-acoustics instance): 2nd-order form of
+ * 2d/ctcs/line_source/wave.c with s(x,t)=exp(-|x-xs|^2/(2 sig^2)) sin(2 pi f t)
+ * added as c^2 dt^2 s at node (i,j), x_i = xmin + i h. */
+typedef struct {
+    int nx, ny;
+    double xmin, ymin, h, c0, dt, xs, ys, sigma, freq;
+    int it0;
+} orc_mono_cfg;
+int orc_ctcs_monopole(const orc_mono_cfg* cfg, int nsteps, double* p_old, double* p, double* scratch);
+
+/* 3D Euler RHS: CWENO4 reconstruction + Rusanov flux (see hype_oracle.c for the
+ * reference lines followed).  bc[6] = left,right,bottom,top,back,front.
+ * Returns 0, or 2 for an inadmissible state (then *bad = first offending
+ * linear cell index of the face's right cell). */
+typedef struct {
+    int nx, ny, nz;
+    double xmin, ymin, zmin, h, cfl, gamma;
+    int bc[6];
+    int recon; /* 0 = CWENO4 (gamma 0.85), 1 = linear R4 (the optimal-weight polynomial) */
+    int nthreads;
+} orc_euler_cfg;
+int orc_euler_rhs(const orc_euler_cfg* cfg, const double* U, double* RHS, double* smax_out, long* bad);
+/* SSPRK(4,3) steps with dt semantics: dt_mode 0 -> dt refreshed each step from
+ * the last stage RHS (Navier-Stokes-3D monitor), 1 -> frozen at the initial RHS
+ * value, 2 -> *dt_inout for every step.  Returns 0 or the RHS error. */
+int orc_euler_run(const orc_euler_cfg* cfg, int nsteps, int dt_mode, double* U, double* t_inout, double* dt_inout, long* bad);
+
+/* Single-cell CWENO4 coefficients from the 33-point stencil in the reference's
+ * argument order (U_x[5],U_y[5],U_z[5],U_xy[5],U_yz[5],U_zx[5],U_xyz[8]). */
+void orc_cweno4_ref_args(const double* Ux, const double* Uy, const double* Uz, const double* Uxy, const double* Uyz,
+                         const double* Uzx, const double* Uxyz, double* coeffs);
+double orc_eval_poly3(double x, double y, double z, const double* coeffs);
+double orc_rusanov(const double* QL, const double* QR, int dir, double gamma, double* flux, int* bad);
+
+/* flop tally of one Euler RHS evaluation per interior cell (counted by the
+ * instrumented build of the same arithmetic); -1 when not available */
+int orc_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,212 @@
+"""ctypes bindings of the CPU checker (TEST INFRASTRUCTURE ONLY).
+
+Importable by tests/, the smoke check and bench.py's CPU-baseline leg.  It
+binds two things:
+
+* ``liboracle.so`` -- the C restatement in ``hype_oracle.c`` (always built by
+  ``build()``);
+* ``_ref/*`` -- the reference's own C sources compiled in place through the
+  PETSc shim (only where the reference tree is present when ``build()`` runs).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_lib = None
+_ref_euler = None
+_ref_ctcs2d = None
+
+D = C.POINTER(C.c_double)
+
+
+def _dp(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(D)
+
+
+def build(ref_dir: str | None = None, quiet: bool = True) -> None:
+    """make the restatement; also the reference checker when the tree exists."""
+    out = subprocess.DEVNULL if quiet else None
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle"], check=True, stdout=out)
+    ref_dir = ref_dir or "/root/reference"
+    if os.path.isdir(ref_dir):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={ref_dir}"], check=True, stdout=out)
+
+
+class EulerCfg(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("xmin", C.c_double), ("ymin", C.c_double), ("zmin", C.c_double),
+                ("h", C.c_double), ("cfl", C.c_double), ("gamma", C.c_double),
+                ("bc", C.c_int * 6), ("recon", C.c_int), ("nthreads", C.c_int)]
+
+
+class CtcsCfg(C.Structure):
+    _fields_ = [("dim", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("order", C.c_int), ("bc", C.c_int),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+                ("dt", C.c_double), ("c0", C.c_double), ("f0", C.c_double),
+                ("src_i", C.c_int), ("src_j", C.c_int), ("src_k", C.c_int),
+                ("rec_i", C.c_int), ("rec_j", C.c_int), ("rec_k", C.c_int),
+                ("it0", C.c_int)]
+
+
+class MonoCfg(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int),
+                ("xmin", C.c_double), ("ymin", C.c_double), ("h", C.c_double),
+                ("c0", C.c_double), ("dt", C.c_double), ("xs", C.c_double), ("ys", C.c_double),
+                ("sigma", C.c_double), ("freq", C.c_double), ("it0", C.c_int)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        L.orc_euler_rhs.argtypes = [C.POINTER(EulerCfg), D, D, D, C.POINTER(C.c_long)]
+        L.orc_euler_run.argtypes = [C.POINTER(EulerCfg), C.c_int, C.c_int, D, D, D, C.POINTER(C.c_long)]
+        L.orc_ctcs2d_plane.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, D, D, D]
+        L.orc_ctcs_pointsrc.argtypes = [C.POINTER(CtcsCfg), D, C.c_int, D, D, D, D]
+        L.orc_ctcs_monopole.argtypes = [C.POINTER(MonoCfg), C.c_int, D, D, D]
+        L.orc_cweno4_ref_args.argtypes = [D] * 8
+        L.orc_eval_poly3.argtypes = [C.c_double, C.c_double, C.c_double, D]
+        L.orc_eval_poly3.restype = C.c_double
+        L.orc_rusanov.argtypes = [D, D, C.c_int, C.c_double, D, C.POINTER(C.c_int)]
+        L.orc_rusanov.restype = C.c_double
+        L.orc_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def threads() -> int:
+    return lib().orc_threads()
+
+
+def euler_cfg(n, h, cfl=0.4, gamma=1.4, bc=(0,) * 6, origin=(0.0, 0.0, 0.0), recon=0, nthreads=0):
+    nx, ny, nz = (n, n, n) if isinstance(n, int) else n
+    c = EulerCfg()
+    c.nx, c.ny, c.nz = nx, ny, nz
+    c.xmin, c.ymin, c.zmin = origin
+    c.h, c.cfl, c.gamma = h, cfl, gamma
+    for q in range(6):
+        c.bc[q] = bc[q]
+    c.recon, c.nthreads = recon, nthreads
+    return c
+
+
+def euler_rhs(cfg: EulerCfg, U: np.ndarray):
+    """RHS of an AoS [k][j][i][5] state. Returns (rhs, s_max, status, bad)."""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    smax = C.c_double(0.0)
+    bad = C.c_long(-1)
+    rc = lib().orc_euler_rhs(C.byref(cfg), _dp(U), _dp(R), C.byref(smax), C.byref(bad))
+    return R, smax.value, rc, bad.value
+
+
+def euler_run(cfg: EulerCfg, U: np.ndarray, nsteps: int, dt_mode: int = 0, dt: float = 0.0):
+    """nsteps of SSPRK(4,3). Returns (U_new, t, dt_next, status)."""
+    U = np.array(U, dtype=np.float64, order="C", copy=True)
+    t = C.c_double(0.0)
+    d = C.c_double(dt)
+    bad = C.c_long(-1)
+    rc = lib().orc_euler_run(C.byref(cfg), nsteps, dt_mode, _dp(U), C.byref(t), C.byref(d), C.byref(bad))
+    return U, t.value, d.value, rc
+
+
+def ctcs2d_plane(p_old, p, alpha, bc, nsteps):
+    ny, nx = p.shape
+    a = np.array(p_old, dtype=np.float64, order="C", copy=True)
+    b = np.array(p, dtype=np.float64, order="C", copy=True)
+    s = np.zeros_like(b)
+    lib().orc_ctcs2d_plane(nx, ny, alpha, bc, nsteps, _dp(a), _dp(b), _dp(s))
+    return a, b
+
+
+def ctcs_pointsrc(cfg: CtcsCfg, p_old, p, nsteps, c=None, receiver=False):
+    a = np.array(p_old, dtype=np.float64, order="C", copy=True)
+    b = np.array(p, dtype=np.float64, order="C", copy=True)
+    s = np.zeros_like(b)
+    rec = np.zeros(nsteps) if receiver else None
+    cp = _dp(np.ascontiguousarray(c, dtype=np.float64)) if c is not None else None
+    lib().orc_ctcs_pointsrc(C.byref(cfg), cp, nsteps, _dp(a), _dp(b), _dp(s), _dp(rec) if receiver else None)
+    return a, b, rec
+
+
+def ctcs_monopole(cfg: MonoCfg, p_old, p, nsteps):
+    a = np.array(p_old, dtype=np.float64, order="C", copy=True)
+    b = np.array(p, dtype=np.float64, order="C", copy=True)
+    s = np.zeros_like(b)
+    lib().orc_ctcs_monopole(C.byref(cfg), nsteps, _dp(a), _dp(b), _dp(s))
+    return a, b
+
+
+# ---------------------------------------------------------------- reference
+def ref_available() -> bool:
+    return os.path.exists(os.path.join(HERE, "_ref", "libref_euler.so"))
+
+
+def _ref_euler_lib():
+    global _ref_euler
+    if _ref_euler is None:
+        L = C.CDLL(os.path.join(HERE, "_ref", "libref_euler.so"))
+        IP = C.POINTER(C.c_int)
+        L.ref_euler_rhs.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                    C.c_double, IP, D, D, D]
+        L.ref_euler_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                    C.c_double, IP, C.c_int, C.c_int, D, D, D]
+        _ref_euler = L
+    return _ref_euler
+
+
+def ref_euler_rhs(cfg: EulerCfg, U):
+    L = _ref_euler_lib()
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    dt = C.c_double(0.0)
+    bc = (C.c_int * 6)(*cfg.bc)
+    rc = L.ref_euler_rhs(cfg.nx, cfg.ny, cfg.nz, cfg.xmin, cfg.ymin, cfg.zmin, cfg.h, cfg.cfl, bc, _dp(U), _dp(R),
+                         C.byref(dt))
+    return R, dt.value, rc
+
+
+def ref_euler_run(cfg: EulerCfg, U, nsteps, dt_mode=0, dt=0.0):
+    L = _ref_euler_lib()
+    U = np.array(U, dtype=np.float64, order="C", copy=True)
+    t = C.c_double(0.0)
+    d = C.c_double(dt)
+    bc = (C.c_int * 6)(*cfg.bc)
+    rc = L.ref_euler_run(cfg.nx, cfg.ny, cfg.nz, cfg.xmin, cfg.ymin, cfg.zmin, cfg.h, cfg.cfl, bc, nsteps, dt_mode,
+                         _dp(U), C.byref(t), C.byref(d))
+    return U, t.value, d.value, rc
+
+
+def ref_ctcs2d_run(p_old, p, h, c0, dt, zero_bc, nsteps):
+    global _ref_ctcs2d
+    if _ref_ctcs2d is None:
+        L = C.CDLL(os.path.join(HERE, "_ref", "libref_ctcs2d.so"))
+        L.ref_ctcs2d_run.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, D, D]
+        _ref_ctcs2d = L
+    ny, nx = p.shape
+    a = np.array(p_old, dtype=np.float64, order="C", copy=True)
+    b = np.array(p, dtype=np.float64, order="C", copy=True)
+    rc = _ref_ctcs2d.ref_ctcs2d_run(nx, ny, h, c0, dt, int(zero_bc), nsteps, _dp(a), _dp(b))
+    return a, b, rc
+
+
+def ref_point_source_trace() -> np.ndarray:
+    """Run the reference's 3d/ctcs/point_source program (compiled through the
+    shim) in a scratch directory and return its receiver file as text."""
+    exe = os.path.join(HERE, "_ref", "ref_point_source")
+    with tempfile.TemporaryDirectory() as d:
+        os.makedirs(os.path.join(d, "results"))
+        subprocess.run([exe], cwd=d, check=True, stdout=subprocess.DEVNULL)
+        with open(os.path.join(d, "results", "p.dat")) as f:
+            return f.read()
