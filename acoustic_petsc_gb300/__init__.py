@@ -1,0 +1,17 @@
+"""GB300 (sm_103a) implementation of HyPE's finite-volume RHS, SSP-RK stepper
+and CTCS leapfrog acoustics behind a C ABI (include/hype_gpu.h).
+
+The compute path is ``lib/libhype_gb300.so`` built from ``csrc/*.cu``; this
+package only binds it (``_lib``) and mirrors the reference's operator interface
+(``hype``).  There is no CPU fallback.
+"""
+from . import _build, _lib
+from ._lib import HypeError, lib, launches
+from .hype import AppCtx, BatchLeapfrog, CTCS, EulerSolver, Leapfrog, Monopole
+
+__all__ = ["AppCtx", "BatchLeapfrog", "CTCS", "EulerSolver", "HypeError", "Leapfrog", "Monopole", "lib", "launches",
+           "build"]
+
+
+def build(verbose: bool = False) -> str:
+    return _build.build(verbose=verbose)

@@ -1,0 +1,136 @@
+"""ctypes binding of ``libhype_gb300.so`` (the C ABI of ``include/hype_gpu.h``).
+
+There is no CPU fallback: when the library is missing or cannot be loaded,
+``lib()`` raises.  Structures mirror the header field by field.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _build
+
+_L = None
+
+D = C.POINTER(C.c_double)
+I = C.POINTER(C.c_int)
+
+HYPE_OK, HYPE_ERR_ARG, HYPE_ERR_STATE, HYPE_ERR_CUDA, HYPE_ERR_NOMEM, HYPE_ERR_UNSUPPORTED = range(6)
+BC_PERIODIC, BC_REFLECTIVE, BC_TRANSMISSIVE, BC_ZERO = range(4)
+RECON_CWENO4, RECON_LINEAR4 = 0, 1
+PREC_FP64, PREC_FP32 = 0, 1
+DT_MONITOR, DT_FROZEN, DT_FIXED = 0, 1, 2
+
+# every entry point the header declares (checked by the CPU test suite)
+SYMBOLS = [
+    "hype_euler_create", "hype_euler_destroy", "hype_euler_rhs", "hype_euler_rhs_device", "hype_euler_upload",
+    "hype_euler_download", "hype_euler_state_device", "hype_euler_step", "hype_euler_sync",
+    "hype_ctcs2d_update", "hype_ctcs_create", "hype_ctcs_destroy", "hype_ctcs_set", "hype_ctcs_get",
+    "hype_ctcs_step", "hype_ctcs_level_device", "hype_ctcs_sync",
+    "hype_batch_create", "hype_batch_destroy", "hype_batch_set_tile", "hype_batch_set", "hype_batch_get",
+    "hype_batch_step", "hype_batch_sync",
+    "hype_strerror", "hype_last_error", "hype_launch_count", "hype_version",
+]
+
+
+class HypeError(RuntimeError):
+    def __init__(self, code: int, where: str, detail: str = ""):
+        self.code = code
+        msg = f"{where}: {errstr(code)}"
+        if detail:
+            msg += f" [{detail}]"
+        super().__init__(msg)
+
+
+class EulerParams(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("x_min", C.c_double), ("y_min", C.c_double), ("z_min", C.c_double), ("h", C.c_double),
+                ("cfl", C.c_double), ("gamma", C.c_double), ("bc", C.c_int * 6),
+                ("recon", C.c_int), ("precision", C.c_int), ("dt_mode", C.c_int)]
+
+
+class Status(C.Structure):
+    _fields_ = [("bad_cell", C.c_longlong), ("smax", C.c_double), ("rhs_evals", C.c_longlong)]
+
+
+class CtcsParams(C.Structure):
+    _fields_ = [("dim", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("form", C.c_int), ("order", C.c_int), ("bc", C.c_int),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double), ("dt", C.c_double),
+                ("c0", C.c_double), ("f0", C.c_double), ("src", C.c_int * 3), ("rec", C.c_int * 3)]
+
+
+class MonoInstance(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("xmin", C.c_double), ("ymin", C.c_double),
+                ("h", C.c_double), ("c0", C.c_double), ("dt", C.c_double), ("xs", C.c_double),
+                ("ys", C.c_double), ("sigma", C.c_double), ("freq", C.c_double)]
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Load the library (building it first if only the sources exist)."""
+    global _L
+    if _L is not None:
+        return _L
+    path = _build.LIB
+    if not os.path.exists(path):
+        _build.build()
+    L = C.CDLL(path)
+    V = C.c_void_p
+    P = C.POINTER
+    sig = {
+        "hype_euler_create": ([P(EulerParams), P(V)], C.c_int),
+        "hype_euler_destroy": ([V], None),
+        "hype_euler_rhs": ([V, C.c_double, D, D, D], C.c_int),
+        "hype_euler_rhs_device": ([V, C.c_double, V, V, D], C.c_int),
+        "hype_euler_upload": ([V, D], C.c_int),
+        "hype_euler_download": ([V, D], C.c_int),
+        "hype_euler_state_device": ([V], C.c_void_p),
+        "hype_euler_step": ([V, C.c_int, D, D, P(Status)], C.c_int),
+        "hype_euler_sync": ([V], C.c_int),
+        "hype_ctcs2d_update": ([C.c_int, C.c_int, C.c_double, C.c_int, D, D, D], C.c_int),
+        "hype_ctcs_create": ([P(CtcsParams), P(V)], C.c_int),
+        "hype_ctcs_destroy": ([V], None),
+        "hype_ctcs_set": ([V, D, D], C.c_int),
+        "hype_ctcs_get": ([V, D, D], C.c_int),
+        "hype_ctcs_step": ([V, C.c_int, C.c_int, D], C.c_int),
+        "hype_ctcs_level_device": ([V, C.c_int], C.c_void_p),
+        "hype_ctcs_sync": ([V], C.c_int),
+        "hype_batch_create": ([C.c_int, P(MonoInstance), P(V)], C.c_int),
+        "hype_batch_destroy": ([V], None),
+        "hype_batch_set_tile": ([V, C.c_int, C.c_int], C.c_int),
+        "hype_batch_set": ([V, C.c_int, D, D], C.c_int),
+        "hype_batch_get": ([V, C.c_int, D, D], C.c_int),
+        "hype_batch_step": ([V, C.c_int, C.c_int], C.c_int),
+        "hype_batch_sync": ([V], C.c_int),
+        "hype_strerror": ([C.c_int], C.c_char_p),
+        "hype_last_error": ([], C.c_char_p),
+        "hype_launch_count": ([], C.c_longlong),
+        "hype_version": ([], C.c_char_p),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _L = L
+    return L
+
+
+def errstr(code: int) -> str:
+    try:
+        return lib().hype_strerror(code).decode()
+    except Exception:  # pragma: no cover - message only
+        return f"status {code}"
+
+
+def check(code: int, where: str) -> None:
+    if code != HYPE_OK:
+        detail = lib().hype_last_error().decode() if code == HYPE_ERR_CUDA else ""
+        raise HypeError(code, where, detail)
+
+
+def launches() -> int:
+    return int(lib().hype_launch_count())

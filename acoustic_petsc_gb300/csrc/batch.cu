@@ -1,0 +1,430 @@
+// batch.cu -- many independent 2D CTCS acoustic instances of uneven size in
+// one persistent launch per step over a tile work-list.
+//
+// Each instance is the 2nd-order point-source form of
+// 2d/ctcs/line_source/wave.c:149-173 on a zero-Dirichlet grid, with the point
+// source generalised to a Gaussian monopole s = exp(-|x-xs|^2/(2 sig^2)) sin(2 pi f t)
+// added as c^2 dt^2 s.  The Gaussian is separable, so it is stored as two 1-D
+// factors per instance (nx + ny doubles) instead of a field or an FP64 exp per
+// node per step; sin(2 pi f t) is tabulated per step and instance.
+//
+// Work-list: (instance, tile origin) items; blocks stride over it, so the
+// launch is sized to the GPU (a multiple of the SM count), not to the batch.
+// A chunk of steps is captured once as a CUDA graph and replayed; the tile
+// shape is chosen by timing candidates and cached per grid-shape signature.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "hype_common.cuh"
+
+namespace hype {
+namespace batch {
+
+struct Inst {
+    int nx, ny;
+    long long off;   // offset of the instance in a level pool
+    long long goff;  // offset of its Gaussian factors (gx: nx, then gy: ny)
+    double inv_h2;   // 1/(h*h)
+    double k2;       // c0*c0*dt*dt
+};
+
+struct Work {
+    int q, i0, j0, pad;
+};
+
+template <int TX, int TY>
+__global__ void __launch_bounds__(TX* TY) k_batch(const Inst* __restrict__ inst, const Work* __restrict__ work, int nwork,
+                                                  const double* __restrict__ pold, const double* __restrict__ p,
+                                                  double* __restrict__ pnew, const double* __restrict__ gauss,
+                                                  const double* __restrict__ sinv, int ninst, const int* __restrict__ step) {
+    const int s = *step;
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const Work wk = work[w];
+        const Inst I = inst[wk.q];
+        const int i = wk.i0 + (int)threadIdx.x, j = wk.j0 + (int)threadIdx.y;
+        if (i >= I.nx || j >= I.ny) continue;
+        const double* P = p + I.off;
+        const long long o = (long long)j * I.nx + i;
+        const double c = P[o];
+        const double w_ = i > 0 ? P[o - 1] : 0.0;
+        const double e_ = i < I.nx - 1 ? P[o + 1] : 0.0;
+        const double s_ = j > 0 ? P[o - I.nx] : 0.0;
+        const double n_ = j < I.ny - 1 ? P[o + I.nx] : 0.0;
+        const double pxx = (e_ - 2.0 * c + w_) * I.inv_h2;
+        const double pyy = (n_ - 2.0 * c + s_) * I.inv_h2;
+        const double src = (gauss[I.goff + i] * gauss[I.goff + I.nx + j]) * sinv[(long long)s * ninst + wk.q];
+        pnew[I.off + o] = 2.0 * c - pold[I.off + o] + I.k2 * (pxx + pyy) + I.k2 * src;
+    }
+}
+
+__global__ void k_tick(int* step) { *step += 1; }
+
+}  // namespace batch
+}  // namespace hype
+
+using namespace hype;
+using namespace hype::batch;
+
+struct hype_batch {
+    std::vector<hype_mono_instance> hi;
+    std::vector<Inst> inst;
+    long long pool = 0;  // nodes per level
+    cudaStream_t stream = nullptr;
+    Inst* d_inst = nullptr;
+    double* lv[3] = {nullptr, nullptr, nullptr};
+    int cur = 1;
+    double* gauss = nullptr;
+    double* sinv = nullptr;
+    int sin_cap = 0;
+    long long it = 0;  // global step counter of the instances (time t = it*dt)
+    int* d_step = nullptr;
+    int tx = 0, ty = 0;  // chosen tile
+    Work* d_work = nullptr;
+    int nwork = 0;
+    int grid = 0;
+    cudaGraphExec_t chunk[3] = {nullptr, nullptr, nullptr};
+};
+
+static const int kBatchChunk = 30;
+
+typedef void (*BatchKernel)(const Inst*, const Work*, int, const double*, const double*, double*, const double*,
+                            const double*, int, const int*);
+
+static BatchKernel pick_kernel(int tx, int ty) {
+    if (tx == 32 && ty == 4) return k_batch<32, 4>;
+    if (tx == 32 && ty == 8) return k_batch<32, 8>;
+    if (tx == 32 && ty == 16) return k_batch<32, 16>;
+    if (tx == 64 && ty == 4) return k_batch<64, 4>;
+    if (tx == 64 && ty == 8) return k_batch<64, 8>;
+    if (tx == 128 && ty == 2) return k_batch<128, 2>;
+    if (tx == 128 && ty == 4) return k_batch<128, 4>;
+    if (tx == 256 && ty == 1) return k_batch<256, 1>;
+    return nullptr;
+}
+static const int kTiles[][2] = {{32, 4}, {32, 8}, {32, 16}, {64, 4}, {64, 8}, {128, 2}, {128, 4}, {256, 1}};
+
+static void drop_graphs(hype_batch* b) {
+    for (int q = 0; q < 3; ++q)
+        if (b->chunk[q]) {
+            cudaGraphExecDestroy(b->chunk[q]);
+            b->chunk[q] = nullptr;
+        }
+}
+
+static int build_worklist(hype_batch* b, int tx, int ty) {
+    BatchKernel k = pick_kernel(tx, ty);
+    if (!k) return HYPE_ERR_ARG;
+    std::vector<Work> w;
+    for (size_t q = 0; q < b->inst.size(); ++q)
+        for (int j0 = 0; j0 < b->inst[q].ny; j0 += ty)
+            for (int i0 = 0; i0 < b->inst[q].nx; i0 += tx) w.push_back(Work{(int)q, i0, j0, 0});
+    cudaFree(b->d_work);
+    b->d_work = nullptr;
+    HYPE_CK(cudaMalloc((void**)&b->d_work, sizeof(Work) * w.size()));
+    HYPE_CK(cudaMemcpy(b->d_work, w.data(), sizeof(Work) * w.size(), cudaMemcpyHostToDevice));
+    b->nwork = (int)w.size();
+    int dev = 0, sms = 0, per_sm = 0;
+    HYPE_CK(cudaGetDevice(&dev));
+    HYPE_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    HYPE_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, tx * ty, 0));
+    if (per_sm < 1) per_sm = 1;
+    b->grid = std::min<long long>((long long)sms * per_sm, (long long)b->nwork);
+    b->tx = tx;
+    b->ty = ty;
+    drop_graphs(b);
+    return HYPE_OK;
+}
+
+static int batch_launch(hype_batch* b, int phase) {
+    BatchKernel k = pick_kernel(b->tx, b->ty);
+    double* po = b->lv[(phase + 2) % 3];
+    double* pc = b->lv[phase];
+    double* pn = b->lv[(phase + 1) % 3];
+    k<<<b->grid, dim3(b->tx, b->ty), 0, b->stream>>>(b->d_inst, b->d_work, b->nwork, po, pc, pn, b->gauss, b->sinv,
+                                                     (int)b->inst.size(), b->d_step);
+    k_tick<<<1, 1, 0, b->stream>>>(b->d_step);
+    HYPE_LAUNCHED(2);
+    return HYPE_OK;
+}
+
+static int build_chunk(hype_batch* b, int phase) {
+    cudaGraph_t g;
+    HYPE_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = HYPE_OK;
+    for (int s = 0; s < kBatchChunk && rc == HYPE_OK; ++s) rc = batch_launch(b, (phase + s) % 3);
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (rc) return rc;
+    if (e != cudaSuccess) {
+        set_last_error("cudaStreamEndCapture", e);
+        return HYPE_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&b->chunk[phase], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        set_last_error("cudaGraphInstantiate", e);
+        return HYPE_ERR_CUDA;
+    }
+    return HYPE_OK;
+}
+
+// sin(2 pi f t) per step and instance for the next nsteps steps
+static int fill_sin(hype_batch* b, int nsteps) {
+    const int ni = (int)b->inst.size();
+    if (nsteps > b->sin_cap) {
+        cudaFree(b->sinv);
+        b->sinv = nullptr;
+        HYPE_CK(cudaMalloc((void**)&b->sinv, sizeof(double) * (size_t)nsteps * ni));
+        b->sin_cap = nsteps;
+        drop_graphs(b);
+    }
+    std::vector<double> h((size_t)nsteps * ni);
+    const double two_pi = 6.283185307179586;
+    for (int s = 0; s < nsteps; ++s)
+        for (int q = 0; q < ni; ++q) {
+            const double t = (double)(b->it + s) * b->hi[q].dt;
+            h[(size_t)s * ni + q] = sin(two_pi * b->hi[q].freq * t);
+        }
+    HYPE_CK(cudaMemcpyAsync(b->sinv, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, b->stream));
+    int zero = 0;
+    HYPE_CK(cudaMemcpyAsync(b->d_step, &zero, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    HYPE_CK(cudaStreamSynchronize(b->stream));
+    return HYPE_OK;
+}
+
+static int run_steps(hype_batch* b, int nsteps, int graph) {
+    int rc;
+    if ((rc = fill_sin(b, nsteps))) return rc;
+    int s = 0;
+    if (graph) {
+        while (nsteps - s >= kBatchChunk) {
+            const int phase = b->cur;
+            if (!b->chunk[phase] && (rc = build_chunk(b, phase))) return rc;
+            HYPE_CK(cudaGraphLaunch(b->chunk[phase], b->stream));
+            count_launch(2 * kBatchChunk);
+            b->cur = (b->cur + kBatchChunk) % 3;
+            s += kBatchChunk;
+        }
+    }
+    for (; s < nsteps; ++s) {
+        if ((rc = batch_launch(b, b->cur))) return rc;
+        b->cur = (b->cur + 1) % 3;
+    }
+    b->it += nsteps;
+    return HYPE_OK;
+}
+
+// ------------------------------------------------------------------ autotuner
+static std::string shape_key(const hype_batch* b) {
+    std::vector<std::pair<int, int>> s;
+    for (auto& i : b->inst) s.push_back({i.nx, i.ny});
+    std::sort(s.begin(), s.end());
+    unsigned long long h = 1469598103934665603ull;  // FNV-1a over the sorted shapes
+    for (auto& x : s) {
+        h = (h ^ (unsigned)x.first) * 1099511628211ull;
+        h = (h ^ (unsigned)x.second) * 1099511628211ull;
+    }
+    char buf[64];
+    snprintf(buf, sizeof(buf), "%zu-%016llx", s.size(), h);
+    return buf;
+}
+
+static std::string cache_path() {
+    const char* e = getenv("HYPE_TUNE_CACHE");
+    if (e && *e) return e;
+    const char* home = getenv("HOME");
+    return std::string(home ? home : "/tmp") + "/.cache/hype_gb300_tiles.txt";
+}
+
+static bool cache_lookup(const std::string& key, int* tx, int* ty) {
+    FILE* f = fopen(cache_path().c_str(), "r");
+    if (!f) return false;
+    char k[128];
+    int a, c;
+    bool found = false;
+    while (fscanf(f, "%127s %d %d", k, &a, &c) == 3)
+        if (key == k && pick_kernel(a, c)) {
+            *tx = a;
+            *ty = c;
+            found = true;
+        }
+    fclose(f);
+    return found;
+}
+
+static void cache_store(const std::string& key, int tx, int ty) {
+    const std::string p = cache_path();
+    for (size_t q = 1; q < p.size(); ++q)  // create missing parent directories
+        if (p[q] == '/') mkdir(p.substr(0, q).c_str(), 0755);
+    FILE* f = fopen(p.c_str(), "a");
+    if (!f) return;
+    fprintf(f, "%s %d %d\n", key.c_str(), tx, ty);
+    fclose(f);
+}
+
+static int autotune(hype_batch* b) {
+    int tx = 0, ty = 0;
+    const std::string key = shape_key(b);
+    if (cache_lookup(key, &tx, &ty)) return build_worklist(b, tx, ty);
+    // save levels and step counter: tuning steps are undone afterwards
+    const size_t bytes = sizeof(double) * (size_t)b->pool;
+    double* save[3];
+    for (int q = 0; q < 3; ++q) {
+        HYPE_CK(cudaMalloc((void**)&save[q], bytes));
+        HYPE_CK(cudaMemcpy(save[q], b->lv[q], bytes, cudaMemcpyDeviceToDevice));
+    }
+    const int cur0 = b->cur;
+    const long long it0 = b->it;
+    cudaEvent_t e0, e1;
+    HYPE_CK(cudaEventCreate(&e0));
+    HYPE_CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bx = 32, by = 8;
+    int rc = HYPE_OK;
+    for (auto& t : kTiles) {
+        if ((rc = build_worklist(b, t[0], t[1]))) break;
+        if ((rc = run_steps(b, 3, 0))) break;  // warm-up
+        HYPE_CK(cudaEventRecord(e0, b->stream));
+        if ((rc = run_steps(b, 12, 0))) break;
+        HYPE_CK(cudaEventRecord(e1, b->stream));
+        HYPE_CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        HYPE_CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            bx = t[0];
+            by = t[1];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (int q = 0; q < 3; ++q) {
+        cudaMemcpy(b->lv[q], save[q], bytes, cudaMemcpyDeviceToDevice);
+        cudaFree(save[q]);
+    }
+    b->cur = cur0;
+    b->it = it0;
+    if (rc) return rc;
+    cache_store(key, bx, by);
+    return build_worklist(b, bx, by);
+}
+
+// ------------------------------------------------------------------ C ABI
+extern "C" int hype_batch_create(int ninst, const hype_mono_instance* in, hype_batch** out) {
+    if (ninst < 1 || !in || !out) return HYPE_ERR_ARG;
+    *out = nullptr;
+    hype_batch* b = new hype_batch();
+    b->hi.assign(in, in + ninst);
+    long long off = 0, goff = 0;
+    for (int q = 0; q < ninst; ++q) {
+        const hype_mono_instance& m = in[q];
+        if (m.nx < 3 || m.ny < 3 || !(m.h > 0) || !(m.dt > 0) || !(m.sigma > 0)) {
+            delete b;
+            return HYPE_ERR_ARG;
+        }
+        Inst I;
+        I.nx = m.nx;
+        I.ny = m.ny;
+        I.off = off;
+        I.goff = goff;
+        I.inv_h2 = 1.0 / (m.h * m.h);
+        I.k2 = m.c0 * m.c0 * m.dt * m.dt;
+        b->inst.push_back(I);
+        off += ((long long)m.nx * m.ny + 31) / 32 * 32;  // 256-byte aligned instance starts
+        goff += m.nx + m.ny;
+    }
+    b->pool = off;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    for (int q = 0; q < 3 && e == cudaSuccess; ++q) e = cudaMalloc((void**)&b->lv[q], sizeof(double) * off);
+    for (int q = 0; q < 3 && e == cudaSuccess; ++q) e = cudaMemset(b->lv[q], 0, sizeof(double) * off);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_inst, sizeof(Inst) * ninst);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_inst, b->inst.data(), sizeof(Inst) * ninst, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->gauss, sizeof(double) * goff);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_step, sizeof(int));
+    if (e == cudaSuccess) {
+        // separable Gaussian factors exp(-(x-xs)^2/(2 sig^2)), exp(-(y-ys)^2/(2 sig^2))
+        std::vector<double> g(goff);
+        for (int q = 0; q < ninst; ++q) {
+            const hype_mono_instance& m = in[q];
+            const double r2s = 1.0 / (2.0 * m.sigma * m.sigma);
+            for (int i = 0; i < m.nx; ++i) {
+                const double d = (m.xmin + i * m.h) - m.xs;
+                g[b->inst[q].goff + i] = exp(-(d * d) * r2s);
+            }
+            for (int j = 0; j < m.ny; ++j) {
+                const double d = (m.ymin + j * m.h) - m.ys;
+                g[b->inst[q].goff + m.nx + j] = exp(-(d * d) * r2s);
+            }
+        }
+        e = cudaMemcpy(b->gauss, g.data(), sizeof(double) * goff, cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) {
+        set_last_error("hype_batch_create", e);
+        hype_batch_destroy(b);
+        return e == cudaErrorMemoryAllocation ? HYPE_ERR_NOMEM : HYPE_ERR_CUDA;
+    }
+    int rc = build_worklist(b, 32, 8);
+    if (rc) {
+        hype_batch_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return HYPE_OK;
+}
+
+extern "C" void hype_batch_destroy(hype_batch* b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    drop_graphs(b);
+    for (int q = 0; q < 3; ++q) cudaFree(b->lv[q]);
+    cudaFree(b->d_inst);
+    cudaFree(b->gauss);
+    cudaFree(b->sinv);
+    cudaFree(b->d_step);
+    cudaFree(b->d_work);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+extern "C" int hype_batch_set_tile(hype_batch* b, int tx, int ty) {
+    if (!b) return HYPE_ERR_ARG;
+    if (tx == 0 && ty == 0) return autotune(b);
+    return build_worklist(b, tx, ty);
+}
+
+extern "C" int hype_batch_set(hype_batch* b, int q, const double* p_old, const double* p) {
+    if (!b || q < 0 || q >= (int)b->inst.size() || !p_old || !p) return HYPE_ERR_ARG;
+    const Inst& I = b->inst[q];
+    const size_t bytes = sizeof(double) * (size_t)I.nx * I.ny;
+    HYPE_CK(cudaMemcpyAsync(b->lv[(b->cur + 2) % 3] + I.off, p_old, bytes, cudaMemcpyHostToDevice, b->stream));
+    HYPE_CK(cudaMemcpyAsync(b->lv[b->cur] + I.off, p, bytes, cudaMemcpyHostToDevice, b->stream));
+    HYPE_CK(cudaStreamSynchronize(b->stream));
+    return HYPE_OK;
+}
+
+extern "C" int hype_batch_get(hype_batch* b, int q, double* p_old, double* p) {
+    if (!b || q < 0 || q >= (int)b->inst.size()) return HYPE_ERR_ARG;
+    const Inst& I = b->inst[q];
+    const size_t bytes = sizeof(double) * (size_t)I.nx * I.ny;
+    if (p_old) HYPE_CK(cudaMemcpyAsync(p_old, b->lv[(b->cur + 2) % 3] + I.off, bytes, cudaMemcpyDeviceToHost, b->stream));
+    if (p) HYPE_CK(cudaMemcpyAsync(p, b->lv[b->cur] + I.off, bytes, cudaMemcpyDeviceToHost, b->stream));
+    HYPE_CK(cudaStreamSynchronize(b->stream));
+    return HYPE_OK;
+}
+
+extern "C" int hype_batch_step(hype_batch* b, int nsteps, int graph) {
+    if (!b || nsteps < 0) return HYPE_ERR_ARG;
+    return run_steps(b, nsteps, graph);
+}
+
+extern "C" int hype_batch_sync(hype_batch* b) {
+    if (!b) return HYPE_ERR_ARG;
+    HYPE_CK(cudaStreamSynchronize(b->stream));
+    return HYPE_OK;
+}

@@ -1,0 +1,512 @@
+// euler.cu -- 3D Euler CWENO4 + Rusanov RHS and the SSPRK(4,3) stepper on sm_103a.
+//
+// Per RK stage three kernels run on the context's stream:
+//   recon  : one thread per cell of the extended box [-1,n]^3 that some face of an
+//            owned cell needs; ghost values come from the boundary index map
+//            (replaces DMGlobalToLocal + the BC sweeps of
+//            3d/weno4/Navier-Stokes-3D/rhs_function.c:41-181); writes the 24 face
+//            Gauss-point traces of each variable (rhs_function.c:185-274);
+//   faces  : one thread per face and direction; four Rusanov solves at the 2x2
+//            Gauss points, the weighted flux (rhs_function.c:276-417), the block
+//            max of the wave speed (atomicMax on the bit pattern: speeds are >= 0)
+//            and the admissibility flag (replaces MPI_Abort, pde.c:56-66);
+//   update : flux divergence (rhs_function.c:419-433) fused with the SSP stage
+//            combination; dt comes from device memory, so a whole step needs no
+//            host round trip.
+// State and stage buffers are SoA doubles [c][k][j][i]; traces are stored in the
+// arithmetic type R of the reconstruction ([c][face][gp][extended cell]).
+#include <cuda_runtime.h>
+
+#include <string.h>
+
+#include "euler_kernels.cuh"
+
+namespace hype {
+namespace euler {
+
+struct Geo {
+    int nx, ny, nz;
+    int bc[6];
+    long long N;   // owned cells
+    long long NE;  // extended cells (n+2)^3
+    int ex, ey;    // extended x, y extents
+};
+
+// device scalars of one context
+struct DevScalars {
+    unsigned long long smax_bits[6];  // [0..3] stages, [4] RHS-only calls
+    double dt;
+    double t;
+    unsigned long long bad;  // first inadmissible cell (ULLONG_MAX: none)
+    long long rhs_evals;
+};
+
+__device__ __forceinline__ long long ext_index(const Geo& g, int i, int j, int k) {
+    return ((long long)(k + 1) * (g.ny + 2) + (j + 1)) * (long long)g.ex + (i + 1);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_recon(const double* __restrict__ W, R* __restrict__ T, Geo g, int linear) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+    const int k = blockIdx.z - 1;
+    if (i > g.nx || j > g.ny) return;
+    const int gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny), gk = (k < 0 || k >= g.nz);
+    if (gi + gj + gk > 1) return;  // edge/corner ghosts feed no face of an owned cell
+    // boundary maps of the offsets -2..2 along each direction
+    int mi[5], mj[5], mk[5], fi = 0, fj = 0, fk = 0;
+#pragma unroll
+    for (int o = 0; o < 5; ++o) {
+        int f = 0;
+        mi[o] = bmap(i + o - 2, g.nx, g.bc[0], g.bc[1], &f);
+        fi |= f << o;
+        f = 0;
+        mj[o] = bmap(j + o - 2, g.ny, g.bc[2], g.bc[3], &f);
+        fj |= f << o;
+        f = 0;
+        mk[o] = bmap(k + o - 2, g.nz, g.bc[4], g.bc[5], &f);
+        fk |= f << o;
+    }
+    const long long e = ext_index(g, i, j, k);
+    const long long sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
+    (void)sx;
+#pragma unroll 1
+    for (int c = 0; c < NV; ++c) {
+        const double* Wc = W + (long long)c * g.N;
+        // sign flip of the momentum normal to a reflective boundary
+        const int fm = (c == 1) ? fi : (c == 2) ? fj : (c == 3) ? fk : 0;
+        const int ax = (c == 1) ? 0 : (c == 2) ? 1 : (c == 3) ? 2 : -1;
+        auto ld = [&](int oi, int oj, int ok) -> R {
+            double v = __ldg(Wc + mk[ok + 2] * sz + mj[oj + 2] * sy + mi[oi + 2]);
+            const int o = (ax == 0) ? oi : (ax == 1) ? oj : ok;
+            if (fm && ((fm >> (o + 2)) & 1)) v = -v;
+            return (R)v;
+        };
+        R s[33];
+        s[0] = ld(0, 0, 0);
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+            const int off = (o == 0) ? -2 : (o == 1) ? -1 : (o == 2) ? 1 : 2;
+            s[S1(0, off)] = ld(off, 0, 0);
+            s[S1(1, off)] = ld(0, off, 0);
+            s[S1(2, off)] = ld(0, 0, off);
+        }
+#pragma unroll
+        for (int sa = 0; sa < 2; ++sa)
+#pragma unroll
+            for (int sb = 0; sb < 2; ++sb) {
+                s[SQ(0, sa, 1, sb)] = ld(2 * sa - 1, 2 * sb - 1, 0);
+                s[SQ(1, sa, 2, sb)] = ld(0, 2 * sa - 1, 2 * sb - 1);
+                s[SQ(0, sa, 2, sb)] = ld(2 * sa - 1, 0, 2 * sb - 1);
+            }
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 2; ++b)
+#pragma unroll
+                for (int d = 0; d < 2; ++d) s[SO(a, b, d)] = ld(2 * a - 1, 2 * b - 1, 2 * d - 1);
+        R cf[20];
+        cweno4<R>(s, linear != 0, cf);
+        R tr[8];
+        R* Tc = T + (long long)c * NTR * g.NE + e;
+        face_traces<R, 0>(cf, tr);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) Tc[(long long)q * g.NE] = tr[q];
+        face_traces<R, 1>(cf, tr);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) Tc[(long long)(8 + q) * g.NE] = tr[q];
+        face_traces<R, 2>(cf, tr);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) Tc[(long long)(16 + q) * g.NE] = tr[q];
+    }
+}
+
+__device__ __forceinline__ void atomic_max_pos(unsigned long long* a, double v) {
+    atomicMax(a, (unsigned long long)__double_as_longlong(v));
+}
+
+// Face fluxes of direction D.  Face index (i,j,k) is the face on the low side of
+// cell (i,j,k); along D it runs to n (the high face of the last cell).
+template <typename R, int D>
+__global__ void __launch_bounds__(128) k_faces(const R* __restrict__ T, double* __restrict__ F, Geo g, double gamma,
+                                               DevScalars* __restrict__ ds, int slot) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    const int fx = g.nx + (D == 0), fy = g.ny + (D == 1);
+    double smax = 0.0;
+    bool bad = false;
+    const bool active = (i < fx && j < fy);
+    if (active) {
+        const long long eR = ext_index(g, i, j, k);
+        const long long eL = ext_index(g, i - (D == 0), j - (D == 1), k - (D == 2));
+        R acc[NV];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) acc[c] = R(0);
+        const R gm = (R)gamma, gm1 = (R)(gamma - 1.0);
+#pragma unroll
+        for (int gp = 0; gp < 4; ++gp) {
+            R QL[NV], QR[NV], fl[NV];
+#pragma unroll
+            for (int c = 0; c < NV; ++c) {
+                QL[c] = T[((long long)c * NTR + (2 * D + 1) * 4 + gp) * g.NE + eL];
+                QR[c] = T[((long long)c * NTR + (2 * D) * 4 + gp) * g.NE + eR];
+            }
+            const R s = rusanov<R, D>(QL, QR, gm, gm1, fl, bad);
+            smax = fmax(smax, (double)s);
+#pragma unroll
+            for (int c = 0; c < NV; ++c) acc[c] += R(0.25) * fl[c];
+        }
+        const long long nf = (long long)fx * fy * (g.nz + (D == 2));
+        const long long f = ((long long)k * fy + j) * fx + i;
+#pragma unroll
+        for (int c = 0; c < NV; ++c) F[c * nf + f] = (double)acc[c];
+        if (bad) {
+            const int ci = i < g.nx ? i : g.nx - 1, cj = j < g.ny ? j : g.ny - 1, ck = k < g.nz ? k : g.nz - 1;
+            atomicMin(&ds->bad, (unsigned long long)(((long long)ck * g.ny + cj) * g.nx + ci));
+        }
+    }
+    // warp max, one atomic per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, o));
+    if ((threadIdx.x & 31) == 0 && smax > 0.0) atomic_max_pos(&ds->smax_bits[slot], smax);
+}
+
+// stage combination: out = a*U + b*W + (c*dt)*L   (L = divergence of the face fluxes)
+struct Stage {
+    double a, b, c;
+    int rhs_only;
+};
+
+__global__ void __launch_bounds__(256) k_update(const double* __restrict__ Fx, const double* __restrict__ Fy,
+                                                const double* __restrict__ Fz, const double* __restrict__ U,
+                                                const double* __restrict__ W, double* __restrict__ out, Geo g, double r1_h,
+                                                Stage st, const DevScalars* __restrict__ ds) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= g.nx || j >= g.ny) return;
+    const long long nfx = (long long)(g.nx + 1) * g.ny * g.nz, nfy = (long long)g.nx * (g.ny + 1) * g.nz,
+                    nfz = (long long)g.nx * g.ny * (g.nz + 1);
+    const long long ix = ((long long)k * g.ny + j) * (g.nx + 1) + i;
+    const long long iy = ((long long)k * (g.ny + 1) + j) * g.nx + i;
+    const long long iz = ((long long)k * g.ny + j) * g.nx + i;
+    const long long cell = iz;
+    const double cdt = st.rhs_only ? 0.0 : st.c * ds->dt;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        const double L = -r1_h * (Fx[c * nfx + ix + 1] - Fx[c * nfx + ix]) - r1_h * (Fy[c * nfy + iy + g.nx] - Fy[c * nfy + iy]) -
+                         r1_h * (Fz[c * nfz + iz + (long long)g.nx * g.ny] - Fz[c * nfz + iz]);
+        double v;
+        if (st.rhs_only) {
+            v = L;
+        } else {
+            v = W[c * g.N + cell] + cdt * L;
+            if (st.a != 0.0) v = st.a * U[c * g.N + cell] + st.b * W[c * g.N + cell] + cdt * L;
+        }
+        out[c * g.N + cell] = v;
+    }
+}
+
+// dt of the coming step and the time update (one thread)
+__global__ void k_begin_step(DevScalars* ds, int dt_mode, int src_slot, int use_src, int reset_stages, double cfl_h) {
+    if (use_src && dt_mode != HYPE_DT_FIXED) {
+        const double smax = __longlong_as_double((long long)ds->smax_bits[src_slot]);
+        ds->dt = (1.0 / 3.0) * cfl_h / (smax + 0.0);
+    }
+    if (reset_stages)
+        for (int s = 0; s < 4; ++s) ds->smax_bits[s] = 0ull;
+    ds->t += ds->dt;
+}
+
+__global__ void k_reset_slot(DevScalars* ds, int slot) { ds->smax_bits[slot] = 0ull; }
+
+// AoS [cell][c] <-> SoA [c][cell]
+__global__ void k_aos_to_soa(const double* __restrict__ a, double* __restrict__ s, long long N) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= N * NV) return;
+    const long long cell = q / NV;
+    const int c = (int)(q - cell * NV);
+    s[c * N + cell] = a[q];
+}
+__global__ void k_soa_to_aos(const double* __restrict__ s, double* __restrict__ a, long long N) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= N * NV) return;
+    const long long cell = q / NV;
+    const int c = (int)(q - cell * NV);
+    a[q] = s[c * N + cell];
+}
+
+}  // namespace euler
+}  // namespace hype
+
+using namespace hype;
+using namespace hype::euler;
+
+static inline double bits_to_double(unsigned long long b) {
+    double d;
+    memcpy(&d, &b, sizeof(d));
+    return d;
+}
+
+struct hype_euler {
+    hype_euler_params p;
+    Geo g;
+    cudaStream_t stream = nullptr;
+    double* U = nullptr;   // resident state (SoA)
+    double* W = nullptr;   // stage state
+    double* L = nullptr;   // RHS buffer (rhs-only calls)
+    double* S = nullptr;   // scratch SoA state for host RHS calls
+    void* T = nullptr;     // traces
+    double* Fx = nullptr;
+    double* Fy = nullptr;
+    double* Fz = nullptr;
+    double* stage_aos = nullptr;  // device AoS staging
+    DevScalars* ds = nullptr;
+    DevScalars* hs = nullptr;  // pinned host copy
+    double* pin = nullptr;     // pinned host staging for AoS transfers
+    bool initialized_dt = false;
+};
+
+static int launch_rhs(hype_euler* e, const double* Win, int slot) {
+    const Geo& g = e->g;
+    const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2);
+    const bool f32 = e->p.precision == HYPE_PREC_FP32;
+    const int lin = e->p.recon == HYPE_RECON_LINEAR4;
+    if (f32)
+        k_recon<float><<<gr, br, 0, e->stream>>>(Win, (float*)e->T, g, lin);
+    else
+        k_recon<double><<<gr, br, 0, e->stream>>>(Win, (double*)e->T, g, lin);
+    const dim3 bf(32, 4);
+    const dim3 gx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4), g.nz), gy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4), g.nz),
+        gz(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz + 1);
+    if (f32) {
+        k_faces<float, 0><<<gx, bf, 0, e->stream>>>((const float*)e->T, e->Fx, g, e->p.gamma, e->ds, slot);
+        k_faces<float, 1><<<gy, bf, 0, e->stream>>>((const float*)e->T, e->Fy, g, e->p.gamma, e->ds, slot);
+        k_faces<float, 2><<<gz, bf, 0, e->stream>>>((const float*)e->T, e->Fz, g, e->p.gamma, e->ds, slot);
+    } else {
+        k_faces<double, 0><<<gx, bf, 0, e->stream>>>((const double*)e->T, e->Fx, g, e->p.gamma, e->ds, slot);
+        k_faces<double, 1><<<gy, bf, 0, e->stream>>>((const double*)e->T, e->Fy, g, e->p.gamma, e->ds, slot);
+        k_faces<double, 2><<<gz, bf, 0, e->stream>>>((const double*)e->T, e->Fz, g, e->p.gamma, e->ds, slot);
+    }
+    HYPE_LAUNCHED(4);
+    return HYPE_OK;
+}
+
+static int launch_update(hype_euler* e, const double* U, const double* W, double* out, Stage st) {
+    const Geo& g = e->g;
+    const dim3 b(32, 8), gr(cdiv(g.nx, 32), cdiv(g.ny, 8), g.nz);
+    k_update<<<gr, b, 0, e->stream>>>(e->Fx, e->Fy, e->Fz, U, W, out, g, 1.0 / e->p.h, st, e->ds);
+    HYPE_LAUNCHED(1);
+    return HYPE_OK;
+}
+
+extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
+    if (!p || !out) return HYPE_ERR_ARG;
+    *out = nullptr;
+    if (p->nx < 3 || p->ny < 3 || p->nz < 3 || !(p->h > 0) || !(p->cfl > 0) || !(p->gamma > 1.0)) return HYPE_ERR_ARG;
+    for (int f = 0; f < 6; ++f)
+        if (p->bc[f] < HYPE_BC_PERIODIC || p->bc[f] > HYPE_BC_TRANSMISSIVE) return HYPE_ERR_ARG;
+    for (int d = 0; d < 3; ++d)
+        if ((p->bc[2 * d] == HYPE_BC_PERIODIC) != (p->bc[2 * d + 1] == HYPE_BC_PERIODIC)) return HYPE_ERR_ARG;
+    if (p->recon != HYPE_RECON_CWENO4 && p->recon != HYPE_RECON_LINEAR4) return HYPE_ERR_ARG;
+    if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32) return HYPE_ERR_ARG;
+    if (p->dt_mode < HYPE_DT_MONITOR || p->dt_mode > HYPE_DT_FIXED) return HYPE_ERR_ARG;
+    hype_euler* e = new hype_euler();
+    e->p = *p;
+    Geo& g = e->g;
+    g.nx = p->nx; g.ny = p->ny; g.nz = p->nz;
+    for (int f = 0; f < 6; ++f) g.bc[f] = p->bc[f];
+    g.N = (long long)p->nx * p->ny * p->nz;
+    g.NE = (long long)(p->nx + 2) * (p->ny + 2) * (p->nz + 2);
+    g.ex = p->nx + 2;
+    g.ey = p->ny + 2;
+    const size_t sN = sizeof(double) * NV * (size_t)g.N;
+    const size_t tsz = (p->precision == HYPE_PREC_FP32 ? sizeof(float) : sizeof(double)) * NV * NTR * (size_t)g.NE;
+    int rc = HYPE_OK;
+    auto fail = [&](int code) {
+        hype_euler_destroy(e);
+        return code;
+    };
+    cudaError_t ce;
+#define ALLOC(ptr, bytes)                                  \
+    ce = cudaMalloc((void**)&(ptr), (bytes));              \
+    if (ce != cudaSuccess) {                               \
+        set_last_error("cudaMalloc", ce);                  \
+        return fail(HYPE_ERR_NOMEM);                       \
+    }
+    ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) {
+        set_last_error("cudaStreamCreate", ce);
+        return fail(HYPE_ERR_CUDA);
+    }
+    ALLOC(e->U, sN);
+    ALLOC(e->W, sN);
+    ALLOC(e->L, sN);
+    ALLOC(e->S, sN);
+    ALLOC(e->T, tsz);
+    ALLOC(e->Fx, sizeof(double) * NV * (size_t)(p->nx + 1) * p->ny * p->nz);
+    ALLOC(e->Fy, sizeof(double) * NV * (size_t)p->nx * (p->ny + 1) * p->nz);
+    ALLOC(e->Fz, sizeof(double) * NV * (size_t)p->nx * p->ny * (p->nz + 1));
+    ALLOC(e->stage_aos, sN);
+    ALLOC(e->ds, sizeof(DevScalars));
+#undef ALLOC
+    ce = cudaMallocHost((void**)&e->hs, sizeof(DevScalars));
+    if (ce != cudaSuccess) {
+        set_last_error("cudaMallocHost", ce);
+        return fail(HYPE_ERR_NOMEM);
+    }
+    DevScalars z;
+    memset(&z, 0, sizeof(z));
+    z.bad = ~0ull;
+    ce = cudaMemcpy(e->ds, &z, sizeof(z), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) {
+        set_last_error("cudaMemcpy", ce);
+        return fail(HYPE_ERR_CUDA);
+    }
+    *out = e;
+    return rc;
+}
+
+extern "C" void hype_euler_destroy(hype_euler* e) {
+    if (!e) return;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    cudaFree(e->U); cudaFree(e->W); cudaFree(e->L); cudaFree(e->S); cudaFree(e->T);
+    cudaFree(e->Fx); cudaFree(e->Fy); cudaFree(e->Fz); cudaFree(e->stage_aos); cudaFree(e->ds);
+    if (e->hs) cudaFreeHost(e->hs);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+}
+
+static int h2d_aos(hype_euler* e, const double* aos, double* soa) {
+    const long long n = e->g.N * NV;
+    HYPE_CK(cudaMemcpyAsync(e->stage_aos, aos, sizeof(double) * n, cudaMemcpyHostToDevice, e->stream));
+    k_aos_to_soa<<<cdiv(n, 256), 256, 0, e->stream>>>(e->stage_aos, soa, e->g.N);
+    HYPE_LAUNCHED(1);
+    return HYPE_OK;
+}
+
+static int d2h_aos(hype_euler* e, const double* soa, double* aos) {
+    const long long n = e->g.N * NV;
+    k_soa_to_aos<<<cdiv(n, 256), 256, 0, e->stream>>>(soa, e->stage_aos, e->g.N);
+    HYPE_LAUNCHED(1);
+    HYPE_CK(cudaMemcpyAsync(aos, e->stage_aos, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
+    return HYPE_OK;
+}
+
+static int read_scalars(hype_euler* e) {
+    HYPE_CK(cudaMemcpyAsync(e->hs, e->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, e->stream));
+    HYPE_CK(cudaStreamSynchronize(e->stream));
+    return HYPE_OK;
+}
+
+static int rhs_core(hype_euler* e, const double* dU, double* dRHS, double* dt_out) {
+    int rc;
+    k_reset_slot<<<1, 1, 0, e->stream>>>(e->ds, 4);
+    HYPE_LAUNCHED(1);
+    if ((rc = launch_rhs(e, dU, 4))) return rc;
+    Stage st{0.0, 0.0, 0.0, 1};
+    if ((rc = launch_update(e, nullptr, nullptr, dRHS, st))) return rc;
+    if ((rc = read_scalars(e))) return rc;
+    const double smax = bits_to_double(e->hs->smax_bits[4]);
+    if (dt_out) *dt_out = (1.0 / 3.0) * (e->p.cfl * e->p.h) / (smax + 0.0);
+    if (e->hs->bad != ~0ull) return HYPE_ERR_STATE;
+    return HYPE_OK;
+}
+
+extern "C" int hype_euler_rhs(hype_euler* e, double t, const double* U_aos, double* RHS_aos, double* dt_out) {
+    (void)t;  // the Euler RHS is autonomous
+    if (!e || !U_aos || !RHS_aos) return HYPE_ERR_ARG;
+    int rc;
+    if ((rc = h2d_aos(e, U_aos, e->S))) return rc;
+    rc = rhs_core(e, e->S, e->L, dt_out);
+    if (rc && rc != HYPE_ERR_STATE) return rc;
+    int rc2 = d2h_aos(e, e->L, RHS_aos);
+    if (rc2) return rc2;
+    HYPE_CK(cudaStreamSynchronize(e->stream));
+    return rc;
+}
+
+extern "C" int hype_euler_rhs_device(hype_euler* e, double t, const double* dU, double* dRHS, double* dt_out) {
+    (void)t;
+    if (!e || !dU || !dRHS) return HYPE_ERR_ARG;
+    return rhs_core(e, dU, dRHS, dt_out);
+}
+
+extern "C" int hype_euler_upload(hype_euler* e, const double* U_aos) {
+    if (!e || !U_aos) return HYPE_ERR_ARG;
+    int rc = h2d_aos(e, U_aos, e->U);
+    if (rc) return rc;
+    HYPE_CK(cudaStreamSynchronize(e->stream));
+    return HYPE_OK;
+}
+
+extern "C" int hype_euler_download(hype_euler* e, double* U_aos) {
+    if (!e || !U_aos) return HYPE_ERR_ARG;
+    int rc = d2h_aos(e, e->U, U_aos);
+    if (rc) return rc;
+    HYPE_CK(cudaStreamSynchronize(e->stream));
+    return HYPE_OK;
+}
+
+extern "C" double* hype_euler_state_device(hype_euler* e) { return e ? e->U : nullptr; }
+
+extern "C" int hype_euler_sync(hype_euler* e) {
+    if (!e) return HYPE_ERR_ARG;
+    HYPE_CK(cudaStreamSynchronize(e->stream));
+    return HYPE_OK;
+}
+
+extern "C" int hype_euler_step(hype_euler* e, int nsteps, double* t_inout, double* dt_inout, hype_status* st) {
+    if (!e || nsteps < 0 || !t_inout || !dt_inout) return HYPE_ERR_ARG;
+    const int mode = e->p.dt_mode;
+    if (mode == HYPE_DT_FIXED && !(*dt_inout > 0)) return HYPE_ERR_ARG;
+    const double cfl_h = e->p.cfl * e->p.h;
+    int rc;
+    // host-side initial values of t, dt, flags
+    DevScalars init;
+    memset(&init, 0, sizeof(init));
+    init.t = *t_inout;
+    init.dt = *dt_inout;
+    init.bad = ~0ull;
+    HYPE_CK(cudaMemcpyAsync(e->ds, &init, sizeof(init), cudaMemcpyHostToDevice, e->stream));
+    const bool first_from_rhs = (mode != HYPE_DT_FIXED) && !(*dt_inout > 0);
+    // SSPRK(4,3) (PETSc TSSSP RKS3, 4 stages; Ketcheson 2008):
+    //   u1 = u + dt/2 L(u); u2 = u1 + dt/2 L(u1); u3 = 2/3 u + 1/3 u2 + dt/6 L(u2); u4 = u3 + dt/2 L(u3)
+    const Stage s12{0.0, 1.0, 0.5, 0};
+    const Stage s3{2.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 0};
+    for (int s = 0; s < nsteps; ++s) {
+        if (s == 0 && first_from_rhs) {
+            // the initial RHS call of hype.c:175 is this step's first stage RHS
+            if ((rc = launch_rhs(e, e->U, 0))) return rc;
+            k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 0, 1, 0, cfl_h);
+            HYPE_LAUNCHED(1);
+        } else {
+            // dt: MONITOR refreshes it from the last stage of the previous step
+            const int use_src = (mode == HYPE_DT_MONITOR) && s > 0;
+            k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 3, use_src, 1, cfl_h);
+            HYPE_LAUNCHED(1);
+            if ((rc = launch_rhs(e, e->U, 0))) return rc;
+        }
+        if ((rc = launch_update(e, e->U, e->U, e->W, s12))) return rc;
+        if ((rc = launch_rhs(e, e->W, 1))) return rc;
+        if ((rc = launch_update(e, e->U, e->W, e->W, s12))) return rc;
+        if ((rc = launch_rhs(e, e->W, 2))) return rc;
+        if ((rc = launch_update(e, e->U, e->W, e->W, s3))) return rc;
+        if ((rc = launch_rhs(e, e->W, 3))) return rc;
+        if ((rc = launch_update(e, e->U, e->W, e->U, s12))) return rc;
+    }
+    if ((rc = read_scalars(e))) return rc;
+    *t_inout = e->hs->t;
+    const double smax3 = bits_to_double(e->hs->smax_bits[3]);
+    if (nsteps > 0 && mode == HYPE_DT_MONITOR)
+        *dt_inout = (1.0 / 3.0) * cfl_h / (smax3 + 0.0);
+    else
+        *dt_inout = e->hs->dt;
+    if (st) {
+        st->bad_cell = e->hs->bad == ~0ull ? -1 : (long long)e->hs->bad;
+        st->smax = smax3;
+        st->rhs_evals = 4LL * nsteps;
+    }
+    return e->hs->bad == ~0ull ? HYPE_OK : HYPE_ERR_STATE;
+}

@@ -1,0 +1,312 @@
+// euler_kernels.cuh -- device arithmetic of the 3D Euler CWENO4 + Rusanov RHS.
+//
+// The per-cell mathematics follows the reference:
+//   weno()               3d/weno4/Viscous-Multiphase-Fourth-Order/reconstruction.c:38-259
+//   evaluate_polynomial  3d/weno4/Viscous-Multiphase-Fourth-Order/reconstruction.c:12-21
+//   PDEConsFlux / LLF    3d/weno4/Navier-Stokes-3D/pde.c:40-88, 164-187
+// It is written for the GPU: the 33-point stencil lives in registers, the
+// 24 face-Gauss-point traces per variable come from an even/odd split of the
+// polynomial at the symmetric Gauss points (about 40 operations per direction
+// instead of 8 full 20-term evaluations), and the arithmetic type R is a
+// template parameter (double: the FP64 path; float: the FP32 recon/flux form).
+#pragma once
+
+#include "hype_common.cuh"
+
+namespace hype {
+namespace euler {
+
+constexpr int NV = 5;
+constexpr int NTR = 24;  // traces per cell and variable: face (0..5: -x,+x,-y,+y,-z,+z) x Gauss point (0..3)
+
+// 33-point stencil index map: 0 centre; 1 + 4d + {0:-2,1:-1,2:+1,3:+2} along d;
+// 13 + 4P + 2 s_lo + s_hi for the diagonal pair P (0: xy, 1: yz, 2: xz; s = 0 for -1, 1 for +1);
+// 25 + 4 sx + 2 sy + sz for the body diagonals.
+__host__ __device__ constexpr int S1(int d, int off) { return 1 + 4 * d + (off == -2 ? 0 : off == -1 ? 1 : off == 1 ? 2 : 3); }
+__host__ __device__ constexpr int pair_of(int a, int b) { return (a + b == 1) ? 0 : (a + b == 3) ? 1 : 2; }
+__host__ __device__ constexpr int SQ(int a, int sa, int b, int sb) {
+    return a < b ? 13 + 4 * pair_of(a, b) + 2 * sa + sb : 13 + 4 * pair_of(a, b) + 2 * sb + sa;
+}
+__host__ __device__ constexpr int SO(int sx, int sy, int sz) { return 25 + 4 * sx + 2 * sy + sz; }
+
+// polynomial coefficient indices (evaluate_polynomial term order)
+__host__ __device__ constexpr int CLIN(int d) { return 1 + d; }
+__host__ __device__ constexpr int CSQ(int d) { return 4 + d; }
+__host__ __device__ constexpr int CCUBE(int d) { return 10 + d; }
+__host__ __device__ constexpr int CCROSS(int a, int b) { return (a + b == 1) ? 7 : (a + b == 3) ? 8 : 9; }
+// coefficient of (a^2 - 1/12) * b
+__host__ __device__ constexpr int CM(int a, int b) {
+    return (a == 0 && b == 1) ? 13 : (a == 1 && b == 0) ? 14 : (a == 1 && b == 2) ? 15 : (a == 2 && b == 1) ? 16
+         : (a == 0 && b == 2) ? 17 : 18;
+}
+
+// Gauss point of the 2x2 face rule (hype.h:88-91) and the polynomial's basis
+// values there, evaluated as evaluate_polynomial does.
+constexpr double GPT = 0.28867513459481287;
+constexpr double R1_12 = 1. / 12.;
+constexpr double R3_20 = 3. / 20.;
+constexpr double A_ = GPT * GPT - R1_12;        // (y^2 - 1/12) at y = +/-GPT
+constexpr double B_ = GPT * (GPT * GPT - R3_20); // y (y^2 - 3/20) at y = +GPT
+constexpr double X2 = 0.5 * 0.5 - R1_12;        // (x^2 - 1/12) at x = +/-1/2
+constexpr double X3 = 0.5 * (0.5 * 0.5 - R3_20); // x (x^2 - 3/20) at x = +1/2
+constexpr double G2 = GPT * GPT;
+
+template <typename R>
+struct Weights;
+
+// CWENO4 coefficients (20) of one variable from its 33-point stencil.
+// linear: the R4 polynomial (the limit in which all nonlinear weights equal the linear ones).
+template <typename R>
+__device__ __forceinline__ void cweno4(const R* __restrict__ s, bool linear, R* __restrict__ cf) {
+    const R u0 = s[0];
+    const R h = R(0.5), q = R(0.25);
+    R d4[3], dd4[3], ddd4[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const R m2 = s[S1(d, -2)], m1 = s[S1(d, -1)], p1 = s[S1(d, 1)], p2 = s[S1(d, 2)];
+        d4[d] = R(1. / 120.) * (R(11.0) * m2 - R(82.0) * m1 + R(82.0) * p1 - R(11.0) * p2);
+        dd4[d] = h * (m1 - R(2.0) * u0 + p1);
+        ddd4[d] = R(1. / 12.) * (-m2 + R(2.0) * (m1 - p1) + p2);
+    }
+#define QV(a, sa, b, sb) s[SQ(a, sa, b, sb)]
+    // mixed second derivatives (pairs xy, yz, zx as in the reference)
+    const R xy4 = q * (QV(0, 0, 1, 0) - QV(0, 0, 1, 1) - QV(0, 1, 1, 0) + QV(0, 1, 1, 1));
+    const R yz4 = q * (QV(1, 0, 2, 0) - QV(1, 0, 2, 1) - QV(1, 1, 2, 0) + QV(1, 1, 2, 1));
+    const R xz4 = q * (QV(2, 0, 0, 0) - QV(2, 0, 0, 1) - QV(2, 1, 0, 0) + QV(2, 1, 0, 1));
+    // third derivatives u_aab = 0.25(-mm+mp-pm+pp) + 0.5(u_b- - u_b+), u_abb = 0.5(u_a- - u_a+) + 0.25(pp-mm-mp+pm)
+#define AAB(a, b) (q * (-QV(a, 0, b, 0) + QV(a, 0, b, 1) - QV(a, 1, b, 0) + QV(a, 1, b, 1)) + h * (s[S1(b, -1)] - s[S1(b, 1)]))
+#define ABB(a, b) (h * (s[S1(a, -1)] - s[S1(a, 1)]) + q * (QV(a, 1, b, 1) - QV(a, 0, b, 0) - QV(a, 0, b, 1) + QV(a, 1, b, 0)))
+    const R xxy = AAB(0, 1), xyy = ABB(0, 1);
+    const R yyz = AAB(1, 2), yzz = ABB(1, 2);
+    const R xxz = AAB(0, 2), xzz = ABB(0, 2);
+#undef AAB
+#undef ABB
+    const R xyz = R(0.125) * (s[SO(1, 1, 1)] - s[SO(0, 1, 1)] - s[SO(1, 0, 1)] - s[SO(1, 1, 0)] + s[SO(0, 0, 1)] +
+                              s[SO(0, 1, 0)] + s[SO(1, 0, 0)] - s[SO(0, 0, 0)]);
+    cf[0] = u0;
+    if (linear) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            cf[CLIN(d)] = d4[d];
+            cf[CSQ(d)] = dd4[d];
+            cf[CCUBE(d)] = ddd4[d];
+        }
+        cf[7] = xy4; cf[8] = yz4; cf[9] = xz4;
+        cf[13] = xxy; cf[14] = xyy; cf[15] = yyz; cf[16] = yzz; cf[17] = xxz; cf[18] = xzz; cf[19] = xyz;
+        return;
+    }
+    const R r13_3 = R(13. / 3.), r7_6 = R(7. / 6.);
+    const R IS4 = d4[0] * d4[0] + d4[1] * d4[1] + d4[2] * d4[2] + r13_3 * (dd4[0] * dd4[0] + dd4[1] * dd4[1] + dd4[2] * dd4[2]) +
+                  r7_6 * (xy4 * xy4 + yz4 * yz4 + xz4 * xz4) + R(0.2) * (d4[0] * ddd4[0] + d4[1] * ddd4[1] + d4[2] * ddd4[2]) +
+                  R(4.7) * (xxy * xxy + xxz * xxz + xyy * xyy + xzz * xzz + yyz * yyz + yzz * yzz) +
+                  R(39.06) * (ddd4[0] * ddd4[0] + ddd4[1] * ddd4[1] + ddd4[2] * ddd4[2]) + R(61. / 48.) * xyz * xyz;
+    // centred R3 stencil: first derivatives c1[d], second = dd4[d], cross terms (xy, yz, xz)
+    R c1[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) c1[d] = h * (s[S1(d, 1)] - s[S1(d, -1)]);
+    const R cx[3] = {q * (QV(0, 1, 1, 1) - QV(0, 1, 1, 0) - QV(0, 0, 1, 1) + QV(0, 0, 1, 0)),
+                     q * (QV(1, 1, 2, 1) - QV(1, 1, 2, 0) - QV(1, 0, 2, 1) + QV(1, 0, 2, 0)),
+                     q * (QV(2, 1, 0, 1) - QV(2, 1, 0, 0) - QV(2, 0, 0, 1) + QV(2, 0, 0, 0))};
+    const R IS0 = (c1[0] * c1[0] + c1[1] * c1[1] + c1[2] * c1[2]) + r13_3 * (dd4[0] * dd4[0] + dd4[1] * dd4[1] + dd4[2] * dd4[2]) +
+                  r7_6 * (cx[0] * cx[0] + cx[1] * cx[1] + cx[2] * cx[2]);
+    // one-sided stencils: index 2d (towards +d) and 2d+1 (towards -d): first and second
+    // derivative along d and the two cross terms that involve d
+    R sd1[6], sd2[6], sx1[6], sx2[6], IS3[6];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const int e1 = (d == 0) ? 1 : 0, e2 = (d == 2) ? 1 : 2;
+        const int k1 = (d + e1 == 1) ? 0 : (d + e1 == 3) ? 1 : 2;  // cross slot of (d,e1)
+        const int k2 = (d + e2 == 1) ? 0 : (d + e2 == 3) ? 1 : 2;  // cross slot of (d,e2)
+        const R p1 = s[S1(d, 1)], p2 = s[S1(d, 2)], m1 = s[S1(d, -1)], m2 = s[S1(d, -2)];
+        // towards +d
+        sd1[2 * d] = R(-1.5) * u0 + R(2.0) * p1 - h * p2;
+        sd2[2 * d] = h * (u0 - R(2.0) * p1 + p2);
+        sx1[2 * d] = h * (QV(d, 1, e1, 1) - QV(d, 1, e1, 0)) - c1[e1];
+        sx2[2 * d] = h * (QV(d, 1, e2, 1) - QV(d, 1, e2, 0)) - c1[e2];
+        // towards -d
+        sd1[2 * d + 1] = R(-2.0) * m1 + h * m2 + R(1.5) * u0;
+        sd2[2 * d + 1] = h * (m2 - R(2.0) * m1 + u0);
+        sx1[2 * d + 1] = h * (QV(d, 0, e1, 0) - QV(d, 0, e1, 1)) + c1[e1];
+        sx2[2 * d + 1] = h * (QV(d, 0, e2, 0) - QV(d, 0, e2, 1)) + c1[e2];
+        // the unchanged terms are summed directly (no subtraction from the centred sums:
+        // IS values near zero must keep their relative accuracy)
+        const int k3 = 3 - k1 - k2;
+        const R rest1 = c1[e1] * c1[e1] + c1[e2] * c1[e2];
+        const R rest2 = dd4[e1] * dd4[e1] + dd4[e2] * dd4[e2];
+        const R restx = cx[k3] * cx[k3];
+#pragma unroll
+        for (int sg = 0; sg < 2; ++sg) {
+            const int m = 2 * d + sg;
+            const R a1 = rest1 + sd1[m] * sd1[m];
+            const R a2 = rest2 + sd2[m] * sd2[m];
+            const R a3 = restx + sx1[m] * sx1[m] + sx2[m] * sx2[m];
+            IS3[m] = a1 + r13_3 * a2 + r7_6 * a3;
+        }
+    }
+#undef QV
+    // nonlinear weights: gammaHi = gammaLo = 0.85, p = 4, eps = 1e-12
+    const R gH = R(0.85), g0 = R((1.0 - 0.85) * 0.85), gs = R((1. / 6.) * (1 - 0.85) * (1 - 0.85));
+    R w4, w0, ws[6];
+    Weights<R>::compute(IS4, IS0, IS3, gH, g0, gs, w4, w0, ws);
+    const R wr = w4 / gH;
+    // linear and nonlinear R3 combinations of every quantity; the weight of the
+    // centred value is summed from the stencils that keep it (all weights are positive)
+    const R wx = ws[0] + ws[1], wy = ws[2] + ws[3], wz = ws[4] + ws[5];
+    const R lin_c = g0 + R(4) * gs;  // gamma weight of the centred value for a quantity two sided stencils modify
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const R wkeep = w0 + ((d == 0) ? wy + wz : (d == 1) ? wx + wz : wx + wy);
+        const R nl1 = wkeep * c1[d] + ws[2 * d] * sd1[2 * d] + ws[2 * d + 1] * sd1[2 * d + 1];
+        const R l1 = lin_c * c1[d] + gs * (sd1[2 * d] + sd1[2 * d + 1]);
+        cf[CLIN(d)] = wr * (d4[d] - l1) + nl1;
+        const R nl2 = wkeep * dd4[d] + ws[2 * d] * sd2[2 * d] + ws[2 * d + 1] * sd2[2 * d + 1];
+        const R l2 = lin_c * dd4[d] + gs * (sd2[2 * d] + sd2[2 * d + 1]);
+        cf[CSQ(d)] = wr * (dd4[d] - l2) + nl2;
+    }
+    // cross terms: slot 0 (xy) is modified by the x-sided (via sx1 of d=0) and y-sided (sx1 of d=1) stencils,
+    // slot 1 (yz) by y-sided (sx2 of d=1) and z-sided (sx2 of d=2), slot 2 (xz) by x-sided (sx2 of d=0) and z-sided (sx1 of d=2)
+    {
+        const R lin_x = g0 + R(2) * gs;
+        const R nlxy = (w0 + wz) * cx[0] + ws[0] * sx1[0] + ws[1] * sx1[1] + ws[2] * sx1[2] + ws[3] * sx1[3];
+        const R lxy = lin_x * cx[0] + gs * (sx1[0] + sx1[1] + sx1[2] + sx1[3]);
+        const R nlyz = (w0 + wx) * cx[1] + ws[2] * sx2[2] + ws[3] * sx2[3] + ws[4] * sx2[4] + ws[5] * sx2[5];
+        const R lyz = lin_x * cx[1] + gs * (sx2[2] + sx2[3] + sx2[4] + sx2[5]);
+        const R nlxz = (w0 + wy) * cx[2] + ws[0] * sx2[0] + ws[1] * sx2[1] + ws[4] * sx1[4] + ws[5] * sx1[5];
+        const R lxz = lin_x * cx[2] + gs * (sx2[0] + sx2[1] + sx1[4] + sx1[5]);
+        cf[7] = wr * (xy4 - lxy) + nlxy;
+        cf[8] = wr * (yz4 - lyz) + nlyz;
+        cf[9] = wr * (xz4 - lxz) + nlxz;
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) cf[CCUBE(d)] = wr * ddd4[d];
+    cf[13] = wr * xxy; cf[14] = wr * xyy; cf[15] = wr * yyz; cf[16] = wr * yzz;
+    cf[17] = wr * xxz; cf[18] = wr * xzz; cf[19] = wr * xyz;
+}
+
+// w = gamma / (IS + eps)^4, normalised.  FP64: directly, as the reference does.
+template <>
+struct Weights<double> {
+    __device__ __forceinline__ static void compute(double IS4, double IS0, const double* IS3, double gH, double g0, double gs,
+                                                   double& w4, double& w0, double* ws) {
+        double t = IS4 + 1.0e-12;
+        t *= t;
+        w4 = gH / (t * t);
+        t = IS0 + 1.0e-12;
+        t *= t;
+        w0 = g0 / (t * t);
+        double total = w4 + w0;
+#pragma unroll
+        for (int m = 0; m < 6; ++m) {
+            t = IS3[m] + 1.0e-12;
+            t *= t;
+            ws[m] = gs / (t * t);
+            total += ws[m];
+        }
+        const double r = 1.0 / total;
+        w4 *= r;
+        w0 *= r;
+#pragma unroll
+        for (int m = 0; m < 6; ++m) ws[m] *= r;
+    }
+};
+
+// FP32: (1e-12)^4 underflows, so the weights are formed from ratios to the
+// smallest (IS + eps), which is the same normalised quantity.
+template <>
+struct Weights<float> {
+    __device__ __forceinline__ static void compute(float IS4, float IS0, const float* IS3, float gH, float g0, float gs,
+                                                   float& w4, float& w0, float* ws) {
+        float s4 = IS4 + 1.0e-12f, s0 = IS0 + 1.0e-12f, ss[6];
+        float mn = fminf(s4, s0);
+#pragma unroll
+        for (int m = 0; m < 6; ++m) {
+            ss[m] = IS3[m] + 1.0e-12f;
+            mn = fminf(mn, ss[m]);
+        }
+        float r = mn / s4;
+        r *= r;
+        w4 = gH * r * r;
+        r = mn / s0;
+        r *= r;
+        w0 = g0 * r * r;
+        float total = w4 + w0;
+#pragma unroll
+        for (int m = 0; m < 6; ++m) {
+            r = mn / ss[m];
+            r *= r;
+            ws[m] = gs * r * r;
+            total += ws[m];
+        }
+        const float inv = 1.0f / total;
+        w4 *= inv;
+        w0 *= inv;
+#pragma unroll
+        for (int m = 0; m < 6; ++m) ws[m] *= inv;
+    }
+};
+
+// The 8 traces of the two faces normal to d (4 Gauss points each) from the
+// coefficients: even/odd split of the polynomial in the normal coordinate.
+// out[0..3]: face -d, out[4..7]: face +d; Gauss point g = 2*(t1>0) + (t2>0)
+// with (t1,t2) = (y,z), (x,z), (x,y) for d = x, y, z.
+template <typename R, int D>
+__device__ __forceinline__ void face_traces(const R* __restrict__ c, R* __restrict__ out) {
+    constexpr int T1 = (D == 0) ? 1 : 0;
+    constexpr int T2 = (D == 2) ? 1 : 2;
+    const R G = R(GPT);
+    const R E0 = c[0] + c[CSQ(D)] * R(X2) + (c[CSQ(T1)] + c[CSQ(T2)]) * R(A_);
+    const R E1 = c[CLIN(T1)] * G + c[CCUBE(T1)] * R(B_) + c[CM(D, T1)] * R(X2 * GPT) + c[CM(T2, T1)] * R(A_ * GPT);
+    const R E2 = c[CLIN(T2)] * G + c[CCUBE(T2)] * R(B_) + c[CM(D, T2)] * R(X2 * GPT) + c[CM(T1, T2)] * R(A_ * GPT);
+    const R E12 = c[CCROSS(T1, T2)] * R(G2);
+    const R O0 = R(0.5) * c[CLIN(D)] + R(X3) * c[CCUBE(D)] + R(0.5 * A_) * (c[CM(T1, D)] + c[CM(T2, D)]);
+    const R O1 = R(0.5 * GPT) * c[CCROSS(D, T1)];
+    const R O2 = R(0.5 * GPT) * c[CCROSS(D, T2)];
+    const R O12 = R(0.5 * G2) * c[19];
+#pragma unroll
+    for (int sn = 0; sn < 2; ++sn) {
+        const R A = sn ? E0 + O0 : E0 - O0;
+        const R B1 = sn ? E1 + O1 : E1 - O1;
+        const R B2 = sn ? E2 + O2 : E2 - O2;
+        const R B12 = sn ? E12 + O12 : E12 - O12;
+        const R am = A - B1, ap = A + B1;     // t1 = -, +
+        const R bm = B2 - B12, bp = B2 + B12; // coefficient of s2 for t1 = -, +
+        out[4 * sn + 0] = am - bm;
+        out[4 * sn + 1] = am + bm;
+        out[4 * sn + 2] = ap - bp;
+        out[4 * sn + 3] = ap + bp;
+    }
+}
+
+// Rusanov (LLF) flux across an axis face of normal D; returns the max wave
+// speed and flags an inadmissible state (rho < 1e-14 or p < 1e-12).
+template <typename R, int D>
+__device__ __forceinline__ R rusanov(const R* QL, const R* QR, R gamma, R gm1, R* F, bool& bad) {
+    R FL[NV], FR[NV], sL, sR;
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+        const R* Q = side ? QR : QL;
+        R* Fo = side ? FR : FL;
+        const R rho = Q[0];
+        const R ir = R(1) / rho;
+        const R u = ir * Q[1], v = ir * Q[2], w = ir * Q[3];
+        const R E = Q[4];
+        const R p = gm1 * (E - R(0.5) * rho * (u * u + v * v + w * w));
+        bad |= (rho < R(1.0e-14)) || (p < R(1.0e-12)) || !(rho == rho);
+        const R un = (D == 0) ? u : (D == 1) ? v : w;
+        const R mun = rho * un;
+        Fo[0] = mun;
+        Fo[1] = mun * u + ((D == 0) ? p : R(0));
+        Fo[2] = mun * v + ((D == 1) ? p : R(0));
+        Fo[3] = mun * w + ((D == 2) ? p : R(0));
+        Fo[4] = (E + p) * un;
+        const R a = sqrt(ir * gamma * p);
+        (side ? sR : sL) = fabs(un) + a;
+    }
+    const R s = sL < sR ? sR : sL;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) F[c] = R(0.5) * (FR[c] + FL[c] - s * (QR[c] - QL[c]));
+    return s;
+}
+
+}  // namespace euler
+}  // namespace hype

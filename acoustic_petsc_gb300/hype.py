@@ -1,0 +1,253 @@
+"""Host-side mirror of the reference's operator interface for the hot path.
+
+The reference registers ``RHSFunction(TS ts, PetscReal t, Vec U, Vec RHS, void *ctx)``
+with ``TSSetRHSFunction`` (3d/weno4/Navier-Stokes-3D/hype.c:176) and advances with
+TSSSP RKS3/4 stages; its acoustic codes call ``CTCS(da, Pold, Pcurr, Pnew, &user)``
+(2d/ctcs/plane_wave/wave.c:161) and ``UpdatePressure(...)``
+(3d/ctcs/point_source/wave.c:138).  The classes here keep those names, argument
+meanings and the error behaviour of the C ABI (an inadmissible state raises
+``HypeError`` with code HYPE_ERR_STATE where the reference would MPI_Abort).
+Arrays use the DMDA layout: AoS ``[k][j][i][c]`` for HyPE states, ``[j][i]`` or
+``[k][j][i]`` for CTCS levels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import check
+
+_D = C.POINTER(C.c_double)
+
+
+def _dp(a: np.ndarray):
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise ValueError("arrays must be C-contiguous float64")
+    return a.ctypes.data_as(_D)
+
+
+@dataclass
+class AppCtx:
+    """The fields of the reference's AppCtx (3d/weno4/Navier-Stokes-3D/hype.h:245-276)
+    that the RHS reads, plus the GPU-side options."""
+    N_x: int
+    N_y: int
+    N_z: int
+    h: float
+    x_min: float = 0.0
+    y_min: float = 0.0
+    z_min: float = 0.0
+    CFL: float = 0.4
+    gamma: float = 1.4
+    boundaries: tuple = (L.BC_PERIODIC,) * 6  # left,right,bottom,top,back,front
+    recon: int = L.RECON_CWENO4
+    precision: int = L.PREC_FP64
+    dt_mode: int = L.DT_MONITOR
+    dt: float = 0.0  # the reference's Ctx->dt output of RHSFunction
+
+    def params(self) -> L.EulerParams:
+        p = L.EulerParams()
+        p.nx, p.ny, p.nz = self.N_x, self.N_y, self.N_z
+        p.x_min, p.y_min, p.z_min, p.h = self.x_min, self.y_min, self.z_min, self.h
+        p.cfl, p.gamma = self.CFL, self.gamma
+        for q in range(6):
+            p.bc[q] = int(self.boundaries[q])
+        p.recon, p.precision, p.dt_mode = self.recon, self.precision, self.dt_mode
+        return p
+
+
+class EulerSolver:
+    """3D Euler CWENO4 + Rusanov RHS and SSPRK(4,3) stepper on one GPU."""
+
+    def __init__(self, ctx: AppCtx):
+        self.ctx = ctx
+        self._h = C.c_void_p()
+        check(L.lib().hype_euler_create(C.byref(ctx.params()), C.byref(self._h)), "hype_euler_create")
+        self.shape = (ctx.N_z, ctx.N_y, ctx.N_x, 5)
+        self.t = 0.0
+        self.next_dt = 0.0
+
+    def close(self):
+        if self._h:
+            L.lib().hype_euler_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def RHSFunction(self, t: float, U: np.ndarray, RHS: np.ndarray | None = None) -> np.ndarray:
+        """Drop-in for RHSFunction(ts, t, U, RHS, &Ctx): fills RHS and sets ctx.dt."""
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        if U.shape != self.shape:
+            raise ValueError(f"U must have shape {self.shape}")
+        if RHS is None:
+            RHS = np.empty_like(U)
+        dt = C.c_double(0.0)
+        rc = L.lib().hype_euler_rhs(self._h, t, _dp(U), _dp(RHS), C.byref(dt))
+        self.ctx.dt = dt.value
+        check(rc, "RHSFunction")
+        return RHS
+
+    def set_state(self, U: np.ndarray) -> None:
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        if U.shape != self.shape:
+            raise ValueError(f"U must have shape {self.shape}")
+        check(L.lib().hype_euler_upload(self._h, _dp(U)), "hype_euler_upload")
+
+    def get_state(self) -> np.ndarray:
+        U = np.empty(self.shape)
+        check(L.lib().hype_euler_download(self._h, _dp(U)), "hype_euler_download")
+        return U
+
+    def step(self, nsteps: int, dt: float | None = None) -> L.Status:
+        """nsteps of SSPRK(4,3) on the resident state (TSSolve with TSSSP RKS3, 4 stages)."""
+        t = C.c_double(self.t)
+        d = C.c_double(self.next_dt if dt is None else dt)
+        st = L.Status()
+        rc = L.lib().hype_euler_step(self._h, int(nsteps), C.byref(t), C.byref(d), C.byref(st))
+        self.t, self.next_dt = t.value, d.value
+        check(rc, "hype_euler_step")
+        return st
+
+    def device_state_ptr(self) -> int:
+        return int(L.lib().hype_euler_state_device(self._h))
+
+    def sync(self):
+        check(L.lib().hype_euler_sync(self._h), "hype_euler_sync")
+
+
+def CTCS(p_old: np.ndarray, p: np.ndarray, alpha: float, bc: int = L.BC_PERIODIC) -> np.ndarray:
+    """One leapfrog update of 2d/ctcs/plane_wave/wave.c:161-203 on host arrays; returns p_new."""
+    p_old = np.ascontiguousarray(p_old, dtype=np.float64)
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    ny, nx = p.shape
+    out = np.empty_like(p)
+    check(L.lib().hype_ctcs2d_update(nx, ny, float(alpha), int(bc), _dp(p_old), _dp(p), _dp(out)), "CTCS")
+    return out
+
+
+class Leapfrog:
+    """Resident CTCS solver (plane-wave form or point-source form, 2D/3D)."""
+
+    def __init__(self, shape, dx, dt, c0=1.0, form=0, order=2, bc=L.BC_ZERO, f0=0.0, src=None, rec=None,
+                 dy=None, dz=None):
+        p = L.CtcsParams()
+        p.dim = len(shape)
+        if p.dim == 2:
+            p.ny, p.nx = shape
+            p.nz = 1
+        else:
+            p.nz, p.ny, p.nx = shape
+        p.form, p.order, p.bc = form, order, bc
+        p.dx = dx
+        p.dy = dy if dy is not None else dx
+        p.dz = dz if dz is not None else dx
+        p.dt, p.c0, p.f0 = dt, c0, f0
+        for q in range(3):
+            p.src[q] = src[q] if src is not None and q < len(src) else (-1 if src is None else 0)
+            p.rec[q] = rec[q] if rec is not None and q < len(rec) else (-1 if rec is None else 0)
+        self.shape = tuple(shape)
+        self.has_rec = rec is not None
+        self._h = C.c_void_p()
+        check(L.lib().hype_ctcs_create(C.byref(p), C.byref(self._h)), "hype_ctcs_create")
+        self.it = 0
+
+    def close(self):
+        if self._h:
+            L.lib().hype_ctcs_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set(self, p_old, p):
+        a = np.ascontiguousarray(p_old, dtype=np.float64)
+        b = np.ascontiguousarray(p, dtype=np.float64)
+        check(L.lib().hype_ctcs_set(self._h, _dp(a), _dp(b)), "hype_ctcs_set")
+
+    def get(self):
+        a = np.empty(self.shape)
+        b = np.empty(self.shape)
+        check(L.lib().hype_ctcs_get(self._h, _dp(a), _dp(b)), "hype_ctcs_get")
+        return a, b
+
+    def UpdatePressure(self, nsteps: int = 1):
+        """nsteps updates; returns the receiver samples (p before each update) when a receiver is set."""
+        rec = np.zeros(nsteps) if self.has_rec else None
+        check(L.lib().hype_ctcs_step(self._h, int(nsteps), self.it, _dp(rec) if rec is not None else None),
+              "hype_ctcs_step")
+        self.it += nsteps
+        return rec
+
+    def sync(self):
+        check(L.lib().hype_ctcs_sync(self._h), "hype_ctcs_sync")
+
+
+@dataclass
+class Monopole:
+    nx: int
+    ny: int
+    xmin: float
+    ymin: float
+    h: float
+    c0: float
+    dt: float
+    xs: float
+    ys: float
+    sigma: float
+    freq: float
+
+
+class BatchLeapfrog:
+    """Many independent 2D monopole-forced CTCS instances in one persistent launch per step."""
+
+    def __init__(self, instances: list[Monopole], tile=(0, 0)):
+        arr = (L.MonoInstance * len(instances))()
+        for q, m in enumerate(instances):
+            for f, _ in L.MonoInstance._fields_:
+                setattr(arr[q], f, getattr(m, f))
+        self.instances = list(instances)
+        self._h = C.c_void_p()
+        check(L.lib().hype_batch_create(len(instances), arr, C.byref(self._h)), "hype_batch_create")
+        self.set_tile(*tile)
+
+    def set_tile(self, tx=0, ty=0):
+        check(L.lib().hype_batch_set_tile(self._h, int(tx), int(ty)), "hype_batch_set_tile")
+
+    def close(self):
+        if self._h:
+            L.lib().hype_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set(self, q, p_old, p):
+        a = np.ascontiguousarray(p_old, dtype=np.float64)
+        b = np.ascontiguousarray(p, dtype=np.float64)
+        check(L.lib().hype_batch_set(self._h, int(q), _dp(a), _dp(b)), "hype_batch_set")
+
+    def get(self, q):
+        m = self.instances[q]
+        a = np.empty((m.ny, m.nx))
+        b = np.empty((m.ny, m.nx))
+        check(L.lib().hype_batch_get(self._h, int(q), _dp(a), _dp(b)), "hype_batch_get")
+        return a, b
+
+    def step(self, nsteps: int, graph: bool = True):
+        check(L.lib().hype_batch_step(self._h, int(nsteps), int(bool(graph))), "hype_batch_step")
+
+    def sync(self):
+        check(L.lib().hype_batch_sync(self._h), "hype_batch_sync")

@@ -1,0 +1,87 @@
+"""Seeded synthetic inputs of the benchmark configurations (host side).
+
+The reference ships no datasets; each configuration is generated from its
+description with fixed seeds, identically for the GPU path and the CPU oracle.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+# 5-point Gauss rule on [-1/2, 1/2] (3d/weno4/Navier-Stokes-3D/hype.h:76-78)
+X_GP5 = np.array([0.0, -0.2692346550528416, 0.2692346550528416, -0.4530899229693320, 0.4530899229693320])
+W_GP5 = np.array([0.28444444444444444, 0.23931433524968326, 0.23931433524968326, 0.11846344252809456,
+                  0.11846344252809456])
+
+
+def _avg1d(n: int, h: float, x0: float, centre: float, sigma: float) -> np.ndarray:
+    """Cell averages of exp(-(x-c)^2/(2 sigma^2)) by the 5-point rule at the correct
+    points x_c + x_gp h (the 2D form of 2d/HyPE-2D/initialize_solution.c:58-63)."""
+    xc = x0 + (np.arange(n) + 0.5) * h
+    pts = xc[:, None] + X_GP5[None, :] * h
+    return (np.exp(-((pts - centre) ** 2) / (2.0 * sigma * sigma)) * W_GP5[None, :]).sum(axis=1)
+
+
+def euler_pulse(n: int = 256, gamma: float = 1.4, amp: float = 1e-3, sigma: float = 0.04) -> np.ndarray:
+    """3D Euler acoustic pulse on [0,1]^3, periodic: rho = 1 + dp, u = 0, p = 1/gamma + dp,
+    dp = amp exp(-r^2/(2 sigma^2)) about the centre.  AoS [k][j][i][5] cell averages
+    (the Gaussian is separable, so the tensor 5^3 rule factorises exactly)."""
+    h = 1.0 / n
+    g = _avg1d(n, h, 0.0, 0.5, sigma)
+    dp = amp * (g[:, None, None] * g[None, :, None] * g[None, None, :])
+    U = np.zeros((n, n, n, 5))
+    U[..., 0] = 1.0 + dp
+    U[..., 4] = (1.0 / gamma + dp) / (gamma - 1.0)
+    return U
+
+
+def euler_blast(n: int = 512, gamma: float = 1.4, seed: int = 2024, p_ratio: float = 10.0, rho_ratio: float = 8.0,
+                r0: float = 0.1, pert: float = 1e-3) -> np.ndarray:
+    """Spherical blast on [0,1]^3 (cell-centre values): inside r < r0 p = 10 p0, rho = 8 rho0;
+    rho0 = 1, p0 = 1/gamma; p carries a seeded uniform relative perturbation of +-pert."""
+    h = 1.0 / n
+    x = (np.arange(n) + 0.5) * h - 0.5
+    rng = np.random.default_rng(seed)
+    U = np.zeros((n, n, n, 5))
+    for k in range(n):  # plane by plane keeps the temporaries small at 512^3
+        r2 = x[None, :] ** 2 + x[:, None] ** 2 + x[k] ** 2
+        inside = r2 < r0 * r0
+        rho = np.where(inside, rho_ratio, 1.0)
+        p = np.where(inside, p_ratio / gamma, 1.0 / gamma) * (1.0 + pert * rng.uniform(-1.0, 1.0, size=(n, n)))
+        U[k, :, :, 0] = rho
+        U[k, :, :, 4] = p / (gamma - 1.0)
+    return U
+
+
+def ctcs_gaussian(n: int = 512, sigma: float = 0.05, c: float = 1.0, cfl: float = 0.5):
+    """2D CTCS start: nodes x_i = -1 + i h on [-1,1]^2, h = 2/n, p0 = exp(-r^2/(2 sigma^2)),
+    zero initial p_t: p1 = p0 + 1/2 (c dt)^2 lap_h p0 with zero exterior.
+    Returns (p0, p1, h, dt, alpha)."""
+    h = 2.0 / n
+    dt = cfl * h / c
+    x = -1.0 + np.arange(n) * h
+    X, Y = np.meshgrid(x, x)
+    p0 = np.exp(-(X * X + Y * Y) / (2.0 * sigma * sigma))
+    pad = np.zeros((n + 2, n + 2))
+    pad[1:-1, 1:-1] = p0
+    lap = (pad[2:, 1:-1] + pad[:-2, 1:-1] + pad[1:-1, 2:] + pad[1:-1, :-2] - 4.0 * p0) / (h * h)
+    p1 = p0 + 0.5 * (c * dt) ** 2 * lap
+    return p0, p1, h, dt, c * dt / h
+
+
+def monopole_batch(ninst: int = 256, seed: int = 7, nmin: int = 64, nmax: int = 1024, c: float = 1.0,
+                   cfl: float = 0.5):
+    """Batched-acoustics instances: sides log-uniform in [nmin, nmax], source centre
+    U[-0.8,0.8]^2, sigma U[0.02,0.1], points per wavelength U[8,32] -> f = c/(ppw h)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(ninst):
+        n = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
+        h = 2.0 / n
+        xs, ys = rng.uniform(-0.8, 0.8, size=2)
+        sigma = rng.uniform(0.02, 0.1)
+        ppw = rng.uniform(8.0, 32.0)
+        out.append(dict(nx=n, ny=n, xmin=-1.0, ymin=-1.0, h=h, c0=c, dt=cfl * h / c, xs=float(xs), ys=float(ys),
+                        sigma=float(sigma), freq=c / (ppw * h)))
+    return out

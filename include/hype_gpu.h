@@ -1,0 +1,183 @@
+/*
+ * hype_gpu.h -- C ABI of the GB300 (sm_103a) implementation of HyPE's
+ * finite-volume right-hand side, its SSP Runge-Kutta stepper and the CTCS
+ * leapfrog acoustic update.
+ *
+ * Plain C types only (no CUDA or torch types), so that the reference's PETSc
+ * host code can call it from a thin RHSFunction.  Every entry point returns an
+ * int status (HYPE_OK = 0) instead of aborting: the reference calls MPI_Abort on
+ * an inadmissible state (3d/weno4/Navier-Stokes-3D/pde.c:56-66); here the call
+ * returns HYPE_ERR_STATE and reports the first offending cell.
+ *
+ * State layout at the boundary is the reference's DMDA layout: AoS doubles
+ * [k][j][i][c], x fastest, owned box only (the ghost/boundary fill that
+ * DMGlobalToLocal + the BC sweeps do in the reference happens on the device).
+ * Entry points named *_device take device pointers in the library's SoA
+ * layout [c][k][j][i]; all others take host pointers.
+ *
+ * Threading: one CUDA stream per context; calls on one context are serialised
+ * by the caller (the reference also runs one RHS at a time per AppCtx).
+ */
+#ifndef HYPE_GPU_H
+#define HYPE_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status codes */
+#define HYPE_OK 0
+#define HYPE_ERR_ARG 1         /* bad argument (sizes, codes, null pointers) */
+#define HYPE_ERR_STATE 2       /* inadmissible state: rho < 1e-14 or p < 1e-12 at a face Gauss point */
+#define HYPE_ERR_CUDA 3        /* CUDA runtime error (message via hype_last_error) */
+#define HYPE_ERR_NOMEM 4       /* device allocation failed */
+#define HYPE_ERR_UNSUPPORTED 5 /* option combination not implemented */
+
+/* ------------------------------------------------------------ boundary codes
+ * per face: [0]=left(-x) [1]=right(+x) [2]=bottom(-y) [3]=top(+y) [4]=back(-z) [5]=front(+z)
+ * (enum bndry_type in 3d/weno4/Navier-Stokes-3D/hype.h:124; ZERO is the
+ * DM_BOUNDARY_GHOSTED zero exterior of the CTCS codes, 1d/ctcs/source/source.c:83) */
+#define HYPE_BC_PERIODIC 0
+#define HYPE_BC_REFLECTIVE 1
+#define HYPE_BC_TRANSMISSIVE 2
+#define HYPE_BC_ZERO 3
+
+/* reconstruction */
+#define HYPE_RECON_CWENO4 0  /* nonlinear CWENO4, gammaHi=gammaLo=0.85
+                                (3d/weno4/Viscous-Multiphase-Fourth-Order/reconstruction.c:38-259) */
+#define HYPE_RECON_LINEAR4 1 /* the optimal-weight limit: the 4th-order central polynomial R4 */
+
+/* arithmetic of reconstruction + flux (the state and the RK accumulation are always FP64) */
+#define HYPE_PREC_FP64 0
+#define HYPE_PREC_FP32 1
+
+/* dt semantics */
+#define HYPE_DT_MONITOR 0 /* dt of step n+1 = CFL h / (3 s_max) of the last stage RHS of step n
+                             (3d/weno4/Navier-Stokes-3D/monitor_function.c:31) */
+#define HYPE_DT_FROZEN 1  /* dt fixed by the first RHS evaluation (3d/weno3/Euler/hype.c:188) */
+#define HYPE_DT_FIXED 2   /* caller's dt */
+
+/* ============================================================ 3D Euler */
+typedef struct hype_euler hype_euler;
+
+typedef struct {
+    int nx, ny, nz;                /* cells (DMDACreate3d M,N,P) */
+    double x_min, y_min, z_min, h; /* uniform spacing (AppCtx.h) */
+    double cfl;                    /* AppCtx.CFL */
+    double gamma;                  /* ideal-gas ratio (GAMMA, hype.h:39) */
+    int bc[6];                     /* HYPE_BC_* per face; PERIODIC must be paired */
+    int recon;                     /* HYPE_RECON_* */
+    int precision;                 /* HYPE_PREC_* */
+    int dt_mode;                   /* HYPE_DT_* */
+} hype_euler_params;
+
+typedef struct {
+    long long bad_cell; /* first offending linear cell index (k*ny+j)*nx+i, -1 if none */
+    double smax;        /* max wave speed seen by the last RHS evaluation */
+    long long rhs_evals;
+} hype_status;
+
+/* Create a solver context and its device buffers. */
+int hype_euler_create(const hype_euler_params* p, hype_euler** out);
+void hype_euler_destroy(hype_euler* e);
+
+/* Drop-in for RHSFunction(TS ts, PetscReal t, Vec U, Vec RHS, void* ctx)
+ * (3d/weno3/Euler/hype.h:291 declaration; body 3d/weno4/Navier-Stokes-3D/rhs_function.c:12-443):
+ * U_aos, RHS_aos are host arrays of the DMDA global vectors (VecGetArrayRead / VecGetArray);
+ * *dt_out receives the value the reference stores in Ctx->dt (rhs_function.c:438-440). */
+int hype_euler_rhs(hype_euler* e, double t, const double* U_aos, double* RHS_aos, double* dt_out);
+
+/* Same on device buffers in SoA layout [5][nz][ny][nx]; dt_out may be NULL. */
+int hype_euler_rhs_device(hype_euler* e, double t, const double* dU, double* dRHS, double* dt_out);
+
+/* Resident state: host AoS <-> device. */
+int hype_euler_upload(hype_euler* e, const double* U_aos);
+int hype_euler_download(hype_euler* e, double* U_aos);
+/* Device pointer to the resident SoA state (5*nx*ny*nz doubles). */
+double* hype_euler_state_device(hype_euler* e);
+
+/* nsteps of SSPRK(4,3) on the resident state -- replaces TSSolve with
+ * TSSSP/TSSSPRKS3/4 stages (3d/weno4/Navier-Stokes-3D/hype.c:185-188).  The
+ * whole step (4 fused stages, device-side dt) runs without host round trips.
+ * *t_inout advances by the dts used; *dt_inout is the dt the next step will use
+ * (input for HYPE_DT_FIXED; for the other modes pass the value of a previous
+ * call, or <= 0 to start from the RHS of the current state as hype.c does). */
+int hype_euler_step(hype_euler* e, int nsteps, double* t_inout, double* dt_inout, hype_status* st);
+
+/* Block until all work of the context is done. */
+int hype_euler_sync(hype_euler* e);
+
+/* ============================================================ CTCS acoustics */
+/* Drop-in for CTCS(DM, Vec Pold, Vec Pcurr, Vec Pnew, AppCtx*)
+ * (2d/ctcs/plane_wave/wave.c:161-203): one leapfrog update
+ * pnew = alpha^2 (N + S + E + W - 4 C) + 2 C - pold, alpha = c dt / h, on host
+ * arrays [ny][nx]; bc = HYPE_BC_PERIODIC or HYPE_BC_ZERO. */
+int hype_ctcs2d_update(int nx, int ny, double alpha, int bc, const double* p_old, const double* p, double* p_new);
+
+typedef struct hype_ctcs hype_ctcs;
+
+typedef struct {
+    int dim;            /* 2 or 3 */
+    int nx, ny, nz;     /* nodes */
+    int form;           /* 0: plane-wave form (2d/ctcs/plane_wave/wave.c:192, 2D, 2nd order)
+                           1: point-source form (2d/ctcs/line_source/wave.c:149-173,
+                              3d/ctcs/point_source/wave.c:163-194) */
+    int order;          /* 2 or 4 (form 1) */
+    int bc;             /* HYPE_BC_PERIODIC or HYPE_BC_ZERO */
+    double dx, dy, dz, dt, c0;
+    double f0;          /* Source() dominant frequency (form 1) */
+    int src[3];         /* source node, src[0] < 0: none */
+    int rec[3];         /* receiver node, rec[0] < 0: none */
+} hype_ctcs_params;
+
+int hype_ctcs_create(const hype_ctcs_params* p, hype_ctcs** out);
+void hype_ctcs_destroy(hype_ctcs* c);
+/* Set the two time levels (host arrays, x fastest). */
+int hype_ctcs_set(hype_ctcs* c, const double* p_old, const double* p);
+int hype_ctcs_get(hype_ctcs* c, double* p_old, double* p);
+/* nsteps leapfrog updates with pointer rotation (no VecCopy); it0 = step index of
+ * the first update (source time it*dt).  When a receiver is set, receiver[s]
+ * gets p at the receiver before update s (the reference's p.dat line). */
+int hype_ctcs_step(hype_ctcs* c, int nsteps, int it0, double* receiver);
+/* device pointers of the newest and previous levels */
+double* hype_ctcs_level_device(hype_ctcs* c, int which /* 0 = p, 1 = p_old */);
+int hype_ctcs_sync(hype_ctcs* c);
+
+/* ============================================================ batched CTCS */
+/* Many independent 2D acoustic instances of uneven size in one persistent
+ * launch over a tile work-list.  Each instance: nodes nx x ny on
+ * [xmin, xmin+(nx-1)h] x [ymin, ...], zero-Dirichlet exterior, 2nd-order
+ * CTCS with a Gaussian monopole s = exp(-|x-xs|^2/(2 sigma^2)) sin(2 pi f t)
+ * added as c^2 dt^2 s. */
+typedef struct {
+    int nx, ny;
+    double xmin, ymin, h, c0, dt;
+    double xs, ys, sigma, freq;
+} hype_mono_instance;
+
+typedef struct hype_batch hype_batch;
+
+int hype_batch_create(int ninst, const hype_mono_instance* inst, hype_batch** out);
+void hype_batch_destroy(hype_batch* b);
+/* tile shape (0 = autotuned and cached per grid shape) */
+int hype_batch_set_tile(hype_batch* b, int tile_x, int tile_y);
+/* initial levels of instance q (host arrays ny*nx) */
+int hype_batch_set(hype_batch* b, int q, const double* p_old, const double* p);
+int hype_batch_get(hype_batch* b, int q, double* p_old, double* p);
+/* nsteps of every instance; graph=1 replays a captured CUDA graph of the step */
+int hype_batch_step(hype_batch* b, int nsteps, int graph);
+int hype_batch_sync(hype_batch* b);
+
+/* ============================================================ misc */
+const char* hype_strerror(int code);
+/* message of the last CUDA error seen by the library (thread-local) */
+const char* hype_last_error(void);
+/* number of kernel launches issued by the library so far (process-wide) */
+long long hype_launch_count(void);
+/* library version string */
+const char* hype_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,87 @@
+"""Regenerate the golden fixtures of tests/golden/ (run where the reference
+tree is available; the GPU machine has none, so the fixtures are committed).
+
+* point_source_p.dat    -- the reference's checked-in receiver trace
+                           3d/ctcs/point_source/results/p.dat (251 samples)
+* accuracy_tables.json  -- the reference's published accuracy numbers
+                           (2d/weno4/standing_wave/results/Error.dat,
+                            3d/weno4/plane_wave/results/main.tex:39-42)
+* ref_euler_*.npz       -- inputs and outputs of the reference's own RHSFunction
+                           (3d/weno4/Navier-Stokes-3D/rhs_function.c with the
+                           CWENO4 weno() of Viscous-Multiphase-Fourth-Order,
+                           viscous flux zero) compiled through oracle/petsc_shim,
+                           and of 3 SSP RKS3/4-stage steps of the same
+* ref_ctcs2d.npz        -- the reference's CTCS() (2d/ctcs/plane_wave/wave.c)
+                           on a zero-exterior grid
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import pyoracle as O  # noqa: E402
+
+REF = os.environ.get("HYPE_REF_DIR", "/root/reference")
+
+
+def euler_case(n, seed, bc, amp=0.2, sig=0.15, vel=0.05):
+    """seeded smooth state with a pulse and random momentum (cell-centre values)"""
+    h = 1.0 / n
+    x = (np.arange(n) + 0.5) * h
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    r2 = (X - 0.5) ** 2 + (Y - 0.5) ** 2 + (Z - 0.5) ** 2
+    dp = amp * np.exp(-r2 / (2 * sig**2))
+    rng = np.random.default_rng(seed)
+    U = np.zeros((n, n, n, 5))
+    U[..., 0] = 1.0 + dp
+    U[..., 1:4] = vel * rng.standard_normal((n, n, n, 3))
+    p = 1.0 / 1.4 + dp
+    U[..., 4] = p / 0.4 + 0.5 * (U[..., 1] ** 2 + U[..., 2] ** 2 + U[..., 3] ** 2) / U[..., 0]
+    return U
+
+
+CASES = [("periodic", 8, 11, (0, 0, 0, 0, 0, 0)), ("walls", 8, 12, (1, 1, 2, 2, 1, 2)),
+         ("mixed", 9, 13, (2, 2, 0, 0, 1, 1))]
+
+
+def main():
+    O.build(REF)
+    src = os.path.join(REF, "3d/ctcs/point_source/results/p.dat")
+    with open(src) as f, open(os.path.join(HERE, "point_source_p.dat"), "w") as g:
+        g.write(f.read())
+    tables = {"standing_wave_2d_Error_dat": [], "plane_wave_3d_main_tex": []}
+    with open(os.path.join(REF, "2d/weno4/standing_wave/results/Error.dat")) as f:
+        for line in f:
+            if line.strip():
+                tables["standing_wave_2d_Error_dat"].append([float(v) for v in line.split()])
+    tables["plane_wave_3d_main_tex"] = [[16, 7.23e-03, 6.48e-04], [32, 5.06e-04, 4.54e-05], [64, 3.15e-05, 2.82e-06],
+                                        [128, 1.94e-06, 1.74e-07]]
+    with open(os.path.join(HERE, "accuracy_tables.json"), "w") as f:
+        json.dump(tables, f, indent=1)
+    for name, n, seed, bc in CASES:
+        cfg = O.euler_cfg(n, 1.0 / n, cfl=0.4, bc=bc)
+        U = euler_case(n, seed, bc)
+        R, dt, rc = O.ref_euler_rhs(cfg, U)
+        assert rc == 0
+        U3, t3, dt3, rc3 = O.ref_euler_run(cfg, U, 3)
+        assert rc3 == 0
+        np.savez_compressed(os.path.join(HERE, f"ref_euler_{name}.npz"), U=U, RHS=R, dt=dt, U3=U3, t3=t3, dt3=dt3,
+                            bc=np.array(bc), n=n, cfl=0.4)
+    n = 32
+    x = -1 + np.arange(n) * (2.0 / n)
+    Xg, Yg = np.meshgrid(x, x)
+    p0 = np.exp(-(Xg**2 + Yg**2) / (2 * 0.2**2))
+    a, b, rc = O.ref_ctcs2d_run(p0, 0.999 * p0, 2.0 / n, 1.0, 0.5 * 2.0 / n, 1, 25)
+    assert rc == 0
+    np.savez_compressed(os.path.join(HERE, "ref_ctcs2d.npz"), p0=p0, p1=0.999 * p0, h=2.0 / n, dt=0.5 * 2.0 / n,
+                        steps=25, p_old=a, p=b)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

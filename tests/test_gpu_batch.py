@@ -1,0 +1,49 @@
+"""Batched monopole CTCS instances (persistent launch over a tile work-list)
+against the CPU checker instance by instance."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def _instances(k, seed=3, nmin=40, nmax=150):
+    from acoustic_petsc_gb300 import workloads
+
+    return workloads.monopole_batch(k, seed=seed, nmin=nmin, nmax=nmax)
+
+
+def _oracle_run(oracle, m, nsteps):
+    cfg = oracle.MonoCfg()
+    for f, _ in oracle.MonoCfg._fields_:
+        if f != "it0":
+            setattr(cfg, f, m[f])
+    cfg.it0 = 0
+    z = np.zeros((m["ny"], m["nx"]))
+    return oracle.ctcs_monopole(cfg, z, z, nsteps)
+
+
+def test_batch_vs_oracle(hype, oracle):
+    inst = _instances(7)
+    b = hype.BatchLeapfrog([hype.Monopole(**m) for m in inst], tile=(32, 8))
+    b.step(65)
+    for q, m in enumerate(inst):
+        a, p = b.get(q)
+        ao, po = _oracle_run(oracle, m, 65)
+        assert np.abs(p - po).max() <= TOL * np.abs(po).max()
+        assert np.abs(a - ao).max() <= TOL * np.abs(ao).max()
+
+
+def test_graph_and_tiles_do_not_change_results(hype):
+    inst = _instances(5, seed=11)
+    res = []
+    for tile, graph in [((32, 8), True), ((32, 8), False), ((128, 2), True), ((0, 0), True)]:
+        b = hype.BatchLeapfrog([hype.Monopole(**m) for m in inst], tile=tile)
+        b.step(40, graph=graph)
+        b.step(23, graph=graph)
+        res.append([b.get(q)[1] for q in range(len(inst))])
+        b.close()
+    for r in res[1:]:
+        for x, y in zip(res[0], r):
+            assert np.array_equal(x, y)

@@ -1,0 +1,63 @@
+"""The CPU checker against the reference's own outputs (golden fixtures made by
+tests/golden/make_golden.py from the reference compiled in place)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+
+@pytest.mark.parametrize("name", ["periodic", "walls", "mixed"])
+def test_euler_rhs_matches_reference_bitwise(oracle, name):
+    z = np.load(os.path.join(GOLDEN, f"ref_euler_{name}.npz"))
+    n = int(z["n"])
+    cfg = oracle.euler_cfg(n, 1.0 / n, cfl=float(z["cfl"]), bc=tuple(int(b) for b in z["bc"]))
+    R, smax, rc, bad = oracle.euler_rhs(cfg, z["U"])
+    assert rc == 0 and bad == -1
+    assert np.array_equal(R, z["RHS"])
+    dt = (1.0 / 3.0) * (cfg.cfl * cfg.h) / (smax + 0.0)
+    assert dt == float(z["dt"])
+
+
+@pytest.mark.parametrize("name", ["periodic", "walls", "mixed"])
+def test_euler_ssprk43_matches_reference_bitwise(oracle, name):
+    z = np.load(os.path.join(GOLDEN, f"ref_euler_{name}.npz"))
+    n = int(z["n"])
+    cfg = oracle.euler_cfg(n, 1.0 / n, cfl=float(z["cfl"]), bc=tuple(int(b) for b in z["bc"]))
+    U3, t3, dt3, rc = oracle.euler_run(cfg, z["U"], 3)
+    assert rc == 0
+    assert np.array_equal(U3, z["U3"])
+    assert t3 == float(z["t3"]) and dt3 == float(z["dt3"])
+
+
+def test_ctcs2d_matches_reference_bitwise(oracle):
+    z = np.load(os.path.join(GOLDEN, "ref_ctcs2d.npz"))
+    alpha = 1.0 * float(z["dt"]) / float(z["h"])
+    a, b = oracle.ctcs2d_plane(z["p0"], z["p1"], alpha, 3, int(z["steps"]))
+    assert np.array_equal(a, z["p_old"]) and np.array_equal(b, z["p"])
+
+
+def test_point_source_receiver_trace_is_p_dat(oracle):
+    """3D 4th-order CTCS, 100^3, source (50,50,50), receiver (57,57,57), 251 steps:
+    the oracle's trace printed as the reference prints it (%e) equals p.dat."""
+    cfg = oracle.CtcsCfg()
+    cfg.dim, cfg.nx, cfg.ny, cfg.nz, cfg.order, cfg.bc = 3, 100, 100, 100, 4, 0
+    cfg.dx = cfg.dy = cfg.dz = 0.5
+    cfg.dt, cfg.c0, cfg.f0 = 0.0005, 250.0, 100.0
+    cfg.src_i = cfg.src_j = cfg.src_k = 50
+    cfg.rec_i = cfg.rec_j = cfg.rec_k = 57
+    cfg.it0 = 0
+    z = np.zeros((100, 100, 100))
+    _, _, rec = oracle.ctcs_pointsrc(cfg, z, z, 251, receiver=True)
+    text = "".join("%e\t%e\n" % (it * 0.0005, rec[it]) for it in range(251))
+    with open(os.path.join(GOLDEN, "point_source_p.dat")) as f:
+        assert text == f.read()
+
+
+def test_accuracy_tables_present():
+    with open(os.path.join(GOLDEN, "accuracy_tables.json")) as f:
+        t = json.load(f)
+    assert len(t["standing_wave_2d_Error_dat"]) == 4
+    assert t["plane_wave_3d_main_tex"][0][0] == 16
