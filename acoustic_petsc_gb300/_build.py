@@ -44,7 +44,10 @@ def build(verbose: bool = False) -> str:
     for f in sources():
         obj = os.path.join(OBJDIR, f.replace(".cu", ".o"))
         objs.append(obj)
-        cmd = [cc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills",
+        # host code never contracts a*b+c into an FMA (g++ does by default on aarch64): the
+        # host-side tables (source wavelet, Gaussian factors) must round like the reference
+        cmd = [cc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+               "-Xptxas", "-warn-spills",
                *EXTRA.get(f, []), "-c", os.path.join(CSRC, f), "-o", obj]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)

@@ -30,6 +30,8 @@ SYMBOLS = [
     "hype_batch_create", "hype_batch_destroy", "hype_batch_set_tile", "hype_batch_set", "hype_batch_get",
     "hype_batch_step", "hype_batch_sync",
     "hype_strerror", "hype_last_error", "hype_launch_count", "hype_version",
+    "hype_euler_stream", "hype_euler_profile", "hype_euler_profile_read", "hype_set_device", "hype_device_count",
+    "hype_probe_fma_peak",
 ]
 
 
@@ -110,6 +112,12 @@ def lib():
         "hype_last_error": ([], C.c_char_p),
         "hype_launch_count": ([], C.c_longlong),
         "hype_version": ([], C.c_char_p),
+        "hype_euler_stream": ([V], C.c_void_p),
+        "hype_euler_profile": ([V, C.c_int], C.c_int),
+        "hype_euler_profile_read": ([V, D, P(C.c_longlong)], C.c_int),
+        "hype_set_device": ([C.c_int], C.c_int),
+        "hype_device_count": ([P(C.c_int)], C.c_int),
+        "hype_probe_fma_peak": ([C.c_int, D], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -19,6 +19,8 @@
 
 #include <string.h>
 
+#include <vector>
+
 #include "euler_kernels.cuh"
 
 namespace hype {
@@ -219,7 +221,10 @@ __global__ void k_begin_step(DevScalars* ds, int dt_mode, int src_slot, int use_
     ds->t += ds->dt;
 }
 
-__global__ void k_reset_slot(DevScalars* ds, int slot) { ds->smax_bits[slot] = 0ull; }
+__global__ void k_reset_slot(DevScalars* ds, int slot) {
+    ds->smax_bits[slot] = 0ull;
+    ds->bad = ~0ull;
+}
 
 // AoS [cell][c] <-> SoA [c][cell]
 __global__ void k_aos_to_soa(const double* __restrict__ a, double* __restrict__ s, long long N) {
@@ -265,18 +270,44 @@ struct hype_euler {
     DevScalars* ds = nullptr;
     DevScalars* hs = nullptr;  // pinned host copy
     double* pin = nullptr;     // pinned host staging for AoS transfers
-    bool initialized_dt = false;
+    // per-kernel event timing inside a timed region (hype_euler_profile)
+    bool prof = false;
+    std::vector<cudaEvent_t> ev;  // pairs (start, end)
+    std::vector<int> ev_kind;     // 0 recon, 1 faces (3 directions), 2 update
+    size_t ev_used = 0;
 };
+
+static void prof_mark(hype_euler* e, int kind, bool start) {
+    if (!e->prof) return;
+    if (start) {
+        if (e->ev_used + 2 > e->ev.size()) {
+            for (int q = 0; q < 64; ++q) {
+                cudaEvent_t x;
+                cudaEventCreate(&x);
+                e->ev.push_back(x);
+            }
+            e->ev_kind.resize(e->ev.size() / 2);
+        }
+        e->ev_kind[e->ev_used / 2] = kind;
+        cudaEventRecord(e->ev[e->ev_used], e->stream);
+    } else {
+        cudaEventRecord(e->ev[e->ev_used + 1], e->stream);
+        e->ev_used += 2;
+    }
+}
 
 static int launch_rhs(hype_euler* e, const double* Win, int slot) {
     const Geo& g = e->g;
     const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2);
     const bool f32 = e->p.precision == HYPE_PREC_FP32;
     const int lin = e->p.recon == HYPE_RECON_LINEAR4;
+    prof_mark(e, 0, true);
     if (f32)
         k_recon<float><<<gr, br, 0, e->stream>>>(Win, (float*)e->T, g, lin);
     else
         k_recon<double><<<gr, br, 0, e->stream>>>(Win, (double*)e->T, g, lin);
+    prof_mark(e, 0, false);
+    prof_mark(e, 1, true);
     const dim3 bf(32, 4);
     const dim3 gx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4), g.nz), gy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4), g.nz),
         gz(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz + 1);
@@ -289,6 +320,7 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
         k_faces<double, 1><<<gy, bf, 0, e->stream>>>((const double*)e->T, e->Fy, g, e->p.gamma, e->ds, slot);
         k_faces<double, 2><<<gz, bf, 0, e->stream>>>((const double*)e->T, e->Fz, g, e->p.gamma, e->ds, slot);
     }
+    prof_mark(e, 1, false);
     HYPE_LAUNCHED(4);
     return HYPE_OK;
 }
@@ -296,7 +328,9 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
 static int launch_update(hype_euler* e, const double* U, const double* W, double* out, Stage st) {
     const Geo& g = e->g;
     const dim3 b(32, 8), gr(cdiv(g.nx, 32), cdiv(g.ny, 8), g.nz);
+    prof_mark(e, 2, true);
     k_update<<<gr, b, 0, e->stream>>>(e->Fx, e->Fy, e->Fz, U, W, out, g, 1.0 / e->p.h, st, e->ds);
+    prof_mark(e, 2, false);
     HYPE_LAUNCHED(1);
     return HYPE_OK;
 }
@@ -374,6 +408,7 @@ extern "C" void hype_euler_destroy(hype_euler* e) {
     cudaFree(e->U); cudaFree(e->W); cudaFree(e->L); cudaFree(e->S); cudaFree(e->T);
     cudaFree(e->Fx); cudaFree(e->Fy); cudaFree(e->Fz); cudaFree(e->stage_aos); cudaFree(e->ds);
     if (e->hs) cudaFreeHost(e->hs);
+    for (auto x : e->ev) cudaEventDestroy(x);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
 }
@@ -509,4 +544,30 @@ extern "C" int hype_euler_step(hype_euler* e, int nsteps, double* t_inout, doubl
         st->rhs_evals = 4LL * nsteps;
     }
     return e->hs->bad == ~0ull ? HYPE_OK : HYPE_ERR_STATE;
+}
+
+extern "C" void* hype_euler_stream(hype_euler* e) { return e ? (void*)e->stream : nullptr; }
+
+extern "C" int hype_euler_profile(hype_euler* e, int enable) {
+    if (!e) return HYPE_ERR_ARG;
+    HYPE_CK(cudaStreamSynchronize(e->stream));
+    e->prof = enable != 0;
+    e->ev_used = 0;
+    return HYPE_OK;
+}
+
+extern "C" int hype_euler_profile_read(hype_euler* e, double* ms, long long* count) {
+    if (!e || !ms || !count) return HYPE_ERR_ARG;
+    HYPE_CK(cudaStreamSynchronize(e->stream));
+    for (int k = 0; k < 3; ++k) {
+        ms[k] = 0.0;
+        count[k] = 0;
+    }
+    for (size_t q = 0; q + 1 < e->ev_used + 1 && q < e->ev_used; q += 2) {
+        float t = 0.0f;
+        HYPE_CK(cudaEventElapsedTime(&t, e->ev[q], e->ev[q + 1]));
+        ms[e->ev_kind[q / 2]] += t;
+        count[e->ev_kind[q / 2]] += 1;
+    }
+    return HYPE_OK;
 }

@@ -1,0 +1,456 @@
+"""Benchmark of the hot path: one JSON line per run (rank 0).
+
+Default workload (the configuration the headline metric is quoted on): 3D
+compressible Euler, CWENO4 reconstruction + Rusanov flux + SSPRK(4,3), FP64,
+256^3 cells, periodic, Gaussian acoustic pulse, CFL 0.4.  One "step" is one
+SSPRK(4,3) time step (4 RHS stages) of the whole grid; the metric is
+cell-updates/s (cells x steps / s).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl reference]
+
+Other workloads (--workload): euler256_fp32 (FP32 reconstruction/flux, FP64
+state), euler256_linear (optimal-weight linear reconstruction), ctcs512 (2D
+CTCS 512^2), batch256 (256 batched monopole CTCS instances).
+
+N > 1 (torchrun): replicas only -- each rank runs the same workload on its own
+GPU, no data exchange; value = all ranks' cell-updates / max time.
+``--impl reference`` times the CPU implementation of the path on the host
+cores (the reference compiled in place when present, else its C restatement)
+on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+# algorithmic HBM bytes per unit (FP64 state): Euler SSPRK(4,3), 5 variables:
+# per stage read 40 + write 40 B, plus one extra read of u^n in the stage-3
+# combination -> 4*80 + 40 = 360 B per cell-update, 90 B per cell-stage.
+EULER_BYTES_PER_CELL_STAGE = 90.0
+EULER_BYTES_PER_CELL_UPDATE = 360.0
+# CTCS: read p^n, p^{n-1}, write p^{n+1}: 24 B per cell-update
+CTCS_BYTES_PER_CELL_UPDATE = 24.0
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _profile_figure(name: str, key: str):
+    """a number from a committed ncu summary under profiles/ (line 'key = value')"""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.strip().startswith(key) and "=" in line:
+                    return float(line.split("=", 1)[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+    return ws, rank, local
+
+
+def _barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def _max_over_ranks(ws, x: float) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _gpu_index(local: int) -> int:
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        try:
+            return int(vis.split(",")[local])
+        except Exception:
+            return local
+    return local
+
+
+# ------------------------------------------------------------------ CPU side
+def cpu_euler_rate(n: int, steps: int, use_ref: bool = True):
+    """cell-updates/s of the CPU implementation on an n^3 sample of the pulse workload."""
+    from acoustic_petsc_gb300 import workloads
+    from oracle import pyoracle as O
+
+    O.build(os.environ.get("HYPE_REF_DIR", "/root/reference") if os.path.isdir(
+        os.environ.get("HYPE_REF_DIR", "/root/reference")) else None)
+    U = workloads.euler_pulse(n)
+    cfg = O.euler_cfg(n, 1.0 / n, cfl=0.4, nthreads=os.cpu_count() or 1)
+    kind = "port"
+    if use_ref and O.ref_available():
+        kind = "reference"
+        t0 = time.perf_counter()
+        _, _, _, rc = O.ref_euler_run(cfg, U, steps)
+        dt = time.perf_counter() - t0
+        cores = 1
+    else:
+        O.euler_run(cfg, U, 1)  # warm
+        t0 = time.perf_counter()
+        _, _, _, rc = O.euler_run(cfg, U, steps)
+        dt = time.perf_counter() - t0
+        cores = O.threads()
+    assert rc == 0
+    return n**3 * steps / dt, cores, kind, dt
+
+
+def cpu_ctcs_rate(n: int, steps: int):
+    from acoustic_petsc_gb300 import workloads
+    from oracle import pyoracle as O
+
+    O.build(None)
+    p0, p1, h, dt, alpha = workloads.ctcs_gaussian(n)
+    t0 = time.perf_counter()
+    O.ctcs2d_plane(p0, p1, alpha, 3, steps)
+    d = time.perf_counter() - t0
+    return n * n * steps / d, O.threads(), "port", d
+
+
+# ------------------------------------------------------------------ GPU workloads
+def run_euler(args, ws, rank, local, precision=0, recon=0, n=256):
+    import torch
+
+    import acoustic_petsc_gb300 as H
+    from acoustic_petsc_gb300 import workloads
+
+    L = H.lib()
+    H._lib.check(L.hype_set_device(local), "hype_set_device")
+    torch.cuda.set_device(local)
+    U0 = workloads.euler_pulse(n)
+    ctx = H.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, precision=precision, recon=recon)
+    s = H.EulerSolver(ctx)
+    s.set_state(U0)
+    s.step(max(args.warmup, 3))
+    stream = torch.cuda.ExternalStream(L.hype_euler_stream(s._h))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    H._lib.check(L.hype_euler_profile(s._h, 1), "profile")
+    l0 = H.launches()
+    _barrier(ws)
+    torch.cuda.synchronize()
+    with Clocks(_gpu_index(local)) as clk:
+        e0.record(stream)
+        s.step(args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    torch.cuda.synchronize()
+    _barrier(ws)
+    launches = H.launches() - l0
+    ms = e0.elapsed_time(e1)
+    ms_max = _max_over_ranks(ws, ms)
+    prof_ms = (C.c_double * 3)()
+    prof_n = (C.c_longlong * 3)()
+    H._lib.check(L.hype_euler_profile_read(s._h, prof_ms, prof_n), "profile_read")
+    H._lib.check(L.hype_euler_profile(s._h, 0), "profile")
+    cells = n**3
+    value = ws * cells * args.steps / (ms_max * 1e-3)
+    # ---- the stage (recon + faces + update) as the dominant unit of work
+    stages = max(prof_n[0], 1)
+    t_stage = (prof_ms[0] + prof_ms[1] + prof_ms[2]) / stages * 1e-3
+    achieved_gbs = EULER_BYTES_PER_CELL_STAGE * cells / t_stage / 1e9
+    peak, peak_kind = _peaks()
+    tag = {0: "fp64", 1: "fp32"}[precision] + ("_linear" if recon else "")
+    traffic = _profile_figure(f"euler_stage_{tag}.txt", "dram_bytes_per_cell_stage")
+    flops_cell = _profile_figure(f"euler_stage_{tag}.txt", "fp_flops_per_cell_stage")
+    fpeak = C.c_double()
+    H._lib.check(L.hype_probe_fma_peak(precision, C.byref(fpeak)), "probe")
+    roof = {"kernel": "RK stage = k_recon + k_faces x3 + k_update (per-stage average)", "bound": "hbm",
+            "achieved": achieved_gbs, "peak": peak, "unit": "GB/s", "frac": achieved_gbs / peak,
+            "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+            "traffic": traffic * cells if traffic else None, "algorithmic_bytes": EULER_BYTES_PER_CELL_STAGE * cells,
+            "per_kernel_ms": {"recon": prof_ms[0] / stages, "faces": prof_ms[1] / stages,
+                              "update": prof_ms[2] / stages}}
+    alu = None
+    if flops_cell:
+        ach = flops_cell * cells / t_stage / 1e12
+        alu = {"bound": "fp64" if precision == 0 else "fp32", "achieved": ach, "peak": fpeak.value, "unit": "TFLOP/s",
+               "frac": ach / fpeak.value, "flops_per_cell_stage": flops_cell,
+               "peak_kind": "measured FMA issue ceiling (hype_probe_fma_peak)"}
+    # ---- end to end through the public API with host buffers (pinned)
+    e2e = None
+    if rank == 0 or ws > 1:
+        host = torch.empty((n, n, n, 5), dtype=torch.float64, pin_memory=True)
+        host.numpy()[...] = U0
+        hv = host.numpy()
+        ke = max(1, min(3, args.steps))
+        s.set_state(hv)
+        s.step(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(ke):
+            s.set_state(hv)  # H2D of the step's input from pinned host memory
+            s.step(1)
+            H._lib.check(L.hype_euler_download(s._h, hv.ctypes.data_as(H._lib.D)), "download")  # D2H, pinned
+        e1.record(stream)
+        e1.synchronize()
+        wall = time.perf_counter() - t0
+        ms_e2e = _max_over_ranks(ws, max(e0.elapsed_time(e1), wall * 1e3))
+        nb = cells * 5 * 8
+        e2e = {"value": ws * cells * ke / (ms_e2e * 1e-3), "unit": "cell-updates/s", "h2d_bytes_per_step": nb,
+               "d2h_bytes_per_step": nb, "steps": ke,
+               "path": "EulerSolver.set_state -> step(1) -> get_state (hype_euler_upload/step/download)"}
+    clocks = clk.summary()
+    s.close()
+    out = {
+        "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == 0 else "f64 state / f32 recon+flux",
+        "data": "synthetic: Gaussian acoustic pulse dp = 1e-3 exp(-r^2/(2*0.04^2)), 5^3-Gauss cell averages",
+        "config": {"workload": f"euler3d_cweno4{'_linear' if recon else ''}_rusanov_ssprk43_{n}",
+                   "cells": cells, "grid": [n, n, n], "domain": "[0,1]^3 periodic", "cfl": 0.4, "gamma": 1.4,
+                   "reconstruction": "linear R4" if recon else "CWENO4 (gamma 0.85)", "flux": "Rusanov",
+                   "time": "SSPRK(4,3) (PETSc TSSSP RKS3, 4 stages), dt from the last stage (monitor semantics)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (state 5*8*256^3 B = 671 MB > 129 MB); no flush"},
+        "roofline": roof, "gpu_launches": launches, "clocks": clocks, "e2e": e2e,
+    }
+    if alu:
+        out["roofline_alu"] = alu
+    return out
+
+
+def run_ctcs(args, ws, rank, local, n=512):
+    import torch
+
+    import acoustic_petsc_gb300 as H
+    from acoustic_petsc_gb300 import workloads
+
+    L = H.lib()
+    H._lib.check(L.hype_set_device(local), "hype_set_device")
+    torch.cuda.set_device(local)
+    p0, p1, h, dt, alpha = workloads.ctcs_gaussian(n)
+    lf = H.Leapfrog(p0.shape, dx=h, dt=dt, c0=1.0, form=0, bc=H._lib.BC_ZERO)
+    lf.set(p0, p1)
+    steps_per = 1000  # one "step" of this workload = the 1000-step run
+    lf.UpdatePressure(steps_per * max(args.warmup, 3) // 10)
+    lf.sync()
+    l0 = H.launches()
+    _barrier(ws)
+    torch.cuda.synchronize()
+    with Clocks(_gpu_index(local)) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            lf.UpdatePressure(steps_per)
+        lf.sync()
+        sec = time.perf_counter() - t0
+    launches = H.launches() - l0
+    sec = _max_over_ranks(ws, sec)
+    value = ws * n * n * steps_per * args.steps / sec
+    peak, kind = _peaks()
+    achieved = CTCS_BYTES_PER_CELL_UPDATE * n * n * steps_per * args.steps / sec / 1e9
+    return {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": sec * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic Gaussian pulse",
+            "config": {"workload": "ctcs2d_512_1000steps", "grid": [n, n], "bc": "zero-Dirichlet", "cfl": 0.5,
+                       "l2": "L2-resident working set (2 MB per level): HBM roofline does not bind"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None},
+            "gpu_launches": launches, "clocks": clk.summary()}
+
+
+def run_batch(args, ws, rank, local, ninst=256):
+    import torch
+
+    import acoustic_petsc_gb300 as H
+    from acoustic_petsc_gb300 import workloads
+
+    L = H.lib()
+    H._lib.check(L.hype_set_device(local), "hype_set_device")
+    torch.cuda.set_device(local)
+    inst = workloads.monopole_batch(ninst)
+    b = H.BatchLeapfrog([H.Monopole(**m) for m in inst], tile=(0, 0))
+    nodes = sum(m["nx"] * m["ny"] for m in inst)
+    steps_per = 100
+    b.step(steps_per * max(args.warmup, 3) // 10)
+    b.sync()
+    l0 = H.launches()
+    _barrier(ws)
+    with Clocks(_gpu_index(local)) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            b.step(steps_per)
+        b.sync()
+        sec = time.perf_counter() - t0
+    launches = H.launches() - l0
+    sec = _max_over_ranks(ws, sec)
+    value = ws * nodes * steps_per * args.steps / sec
+    peak, kind = _peaks()
+    achieved = CTCS_BYTES_PER_CELL_UPDATE * nodes * steps_per * args.steps / sec / 1e9
+    return {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": sec * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded monopole instances",
+            "config": {"workload": "batch_ctcs_256_instances", "instances": ninst, "nodes": nodes,
+                       "steps_per_bench_step": steps_per, "sizes": "log-uniform 64^2..1024^2 (seed 7)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None},
+            "gpu_launches": launches, "clocks": clk.summary()}
+
+
+WORKLOADS = {
+    "euler256": lambda a, *r: run_euler(a, *r, precision=0, recon=0),
+    "euler256_fp32": lambda a, *r: run_euler(a, *r, precision=1, recon=0),
+    "euler256_linear": lambda a, *r: run_euler(a, *r, precision=0, recon=1),
+    "euler64": lambda a, *r: run_euler(a, *r, precision=0, recon=0, n=64),
+    "euler128": lambda a, *r: run_euler(a, *r, precision=0, recon=0, n=128),
+    "euler128_fp32": lambda a, *r: run_euler(a, *r, precision=1, recon=0, n=128),
+    "ctcs512": run_ctcs,
+    "batch256": run_batch,
+}
+
+
+def reference_arm(args, ws, rank):
+    """CPU implementation of the path on all host cores, bounded sample per step."""
+    if rank != 0:
+        return None
+    n = int(os.environ.get("HYPE_REF_SAMPLE_N", "64"))
+    if args.workload.startswith("euler"):
+        rates = []
+        for _ in range(max(args.warmup, 0)):
+            cpu_euler_rate(n, 1, use_ref=False)
+        t_all = 0.0
+        for _ in range(args.steps):
+            r, cores, kind, d = cpu_euler_rate(n, 1, use_ref=False)
+            rates.append(r)
+            t_all += d
+        value = n**3 * args.steps / t_all
+        sample = f"1 SSPRK(4,3) step of a {n}^3 periodic pulse grid per bench step (same physics as 256^3)"
+        cfg_w = "euler3d_cweno4_rusanov_ssprk43_256"
+    else:
+        r, cores, kind, d = cpu_ctcs_rate(512, 200)
+        value, sample, cfg_w = r, "200 steps of the 512^2 CTCS run", "ctcs2d_512_1000steps"
+    return {"impl": "reference", "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s",
+            "higher_is_better": True, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "config": {"workload": cfg_w},
+            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": cores, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="euler256", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = _dist()
+    if args.impl == "reference":
+        out = reference_arm(args, ws, rank)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+    out = WORKLOADS[args.workload](args, ws, rank, local)
+    if rank == 0 and not args.no_cpu_baseline:
+        if args.workload.startswith("euler"):
+            n = 96 if args.workload != "euler64" else 48
+            r, cores, kind, d = cpu_euler_rate(n, 2, use_ref=False)
+            out["cpu_baseline"] = {"value": r, "unit": "cell-updates/s", "cores": cores, "kind": kind,
+                                   "sample": f"2 SSPRK(4,3) steps of a {n}^3 periodic pulse grid ({d:.1f} s wall)"}
+        else:
+            r, cores, kind, d = cpu_ctcs_rate(512, 300)
+            out["cpu_baseline"] = {"value": r, "unit": "cell-updates/s", "cores": cores, "kind": kind,
+                                   "sample": f"300 steps of the 512^2 CTCS run ({d:.1f} s wall)"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -107,6 +107,17 @@ int hype_euler_step(hype_euler* e, int nsteps, double* t_inout, double* dt_inout
 /* Block until all work of the context is done. */
 int hype_euler_sync(hype_euler* e);
 
+/* The context's CUDA stream (a cudaStream_t), for callers that record their own
+ * events or order their own work after the solver's. */
+void* hype_euler_stream(hype_euler* e);
+
+/* Per-kernel timing: while enabled, every kernel the context launches is
+ * bracketed by CUDA events on its stream; read returns the summed milliseconds
+ * and launch counts of [0] reconstruction, [1] face fluxes (3 directions),
+ * [2] divergence + stage update since the last enable. */
+int hype_euler_profile(hype_euler* e, int enable);
+int hype_euler_profile_read(hype_euler* e, double* ms, long long* count);
+
 /* ============================================================ CTCS acoustics */
 /* Drop-in for CTCS(DM, Vec Pold, Vec Pcurr, Vec Pnew, AppCtx*)
  * (2d/ctcs/plane_wave/wave.c:161-203): one leapfrog update
@@ -169,6 +180,12 @@ int hype_batch_step(hype_batch* b, int nsteps, int graph);
 int hype_batch_sync(hype_batch* b);
 
 /* ============================================================ misc */
+/* Select the CUDA device that later hype_*_create calls of this thread use. */
+int hype_set_device(int device);
+int hype_device_count(int* n);
+/* Measured FMA issue ceiling of the FP64 (HYPE_PREC_FP64) or FP32 pipe of the
+ * current device, in TFLOP/s (about 20 ms of GPU time). */
+int hype_probe_fma_peak(int precision, double* tflops);
 const char* hype_strerror(int code);
 /* message of the last CUDA error seen by the library (thread-local) */
 const char* hype_last_error(void);
