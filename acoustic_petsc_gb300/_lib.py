@@ -31,7 +31,7 @@ SYMBOLS = [
     "hype_batch_step", "hype_batch_sync",
     "hype_strerror", "hype_last_error", "hype_launch_count", "hype_version",
     "hype_euler_stream", "hype_euler_profile", "hype_euler_profile_read", "hype_set_device", "hype_device_count",
-    "hype_probe_fma_peak",
+    "hype_probe_fma_peak", "hype_euler_rhs_noalloc", "hype_euler_noalloc_max_ext",
 ]
 
 
@@ -118,6 +118,8 @@ def lib():
         "hype_set_device": ([C.c_int], C.c_int),
         "hype_device_count": ([P(C.c_int)], C.c_int),
         "hype_probe_fma_peak": ([C.c_int, D], C.c_int),
+        "hype_euler_rhs_noalloc": ([P(EulerParams), V, V, D, V], C.c_int),
+        "hype_euler_noalloc_max_ext": ([], C.c_longlong),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -571,3 +571,119 @@ extern "C" int hype_euler_profile_read(hype_euler* e, double* ms, long long* cou
     }
     return HYPE_OK;
 }
+
+// ======================================================================
+// Allocation-free RHS evaluation.
+//
+// Some callers cannot let a plugin allocate device memory: hosts that hand the
+// plugin pre-allocated device vectors and own every byte of device memory
+// through their own pool, and latency-critical loops where cudaMalloc's
+// implicit device-wide synchronisation is not acceptable.  For them,
+// hype_euler_rhs_noalloc runs the same three kernels as hype_euler_rhs_device
+// with all of their scratch (face traces, face fluxes, the wave-speed and
+// admissibility words) in the fixed device array below, which every GPU that
+// loads this library holds until the process exits.
+namespace hype {
+namespace euler {
+
+constexpr long long kNoAllocMaxExt = 18LL * 18 * 18;  // (nx+2)(ny+2)(nz+2) <= 5832, e.g. 16^3 cells
+constexpr size_t kAlign = 256;
+constexpr size_t align_up(size_t b) { return (b + kAlign - 1) / kAlign * kAlign; }
+constexpr size_t kNoAllocTraceBytes = align_up(sizeof(double) * NV * NTR * kNoAllocMaxExt);
+constexpr size_t kNoAllocFluxBytes = align_up(sizeof(double) * NV * kNoAllocMaxExt);  // one direction
+constexpr size_t kNoAllocScalarBytes = align_up(sizeof(DevScalars));
+constexpr size_t kNoAllocBytes = kNoAllocTraceBytes + 3 * kNoAllocFluxBytes + kNoAllocScalarBytes;  // ~6.3 MB
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+}  // namespace euler
+}  // namespace hype
+
+#include <mutex>
+
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_base[128] = {nullptr};
+
+extern "C" long long hype_euler_noalloc_max_ext(void) { return kNoAllocMaxExt; }
+
+extern "C" int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* dU, double* dRHS, double* dt_out,
+                                      void* stream) {
+    if (!p || !dU || !dRHS) return HYPE_ERR_ARG;
+    if (p->nx < 3 || p->ny < 3 || p->nz < 3 || !(p->h > 0) || !(p->cfl > 0) || !(p->gamma > 1.0)) return HYPE_ERR_ARG;
+    for (int f = 0; f < 6; ++f)
+        if (p->bc[f] < HYPE_BC_PERIODIC || p->bc[f] > HYPE_BC_TRANSMISSIVE) return HYPE_ERR_ARG;
+    for (int d = 0; d < 3; ++d)
+        if ((p->bc[2 * d] == HYPE_BC_PERIODIC) != (p->bc[2 * d + 1] == HYPE_BC_PERIODIC)) return HYPE_ERR_ARG;
+    if (p->recon != HYPE_RECON_CWENO4 && p->recon != HYPE_RECON_LINEAR4) return HYPE_ERR_ARG;
+    if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32) return HYPE_ERR_ARG;
+    const long long ne = (long long)(p->nx + 2) * (p->ny + 2) * (p->nz + 2);
+    if (ne > kNoAllocMaxExt) {
+        set_last_error("hype_euler_rhs_noalloc: grid exceeds the fixed scratch ((nx+2)(ny+2)(nz+2) > 5832)",
+                       cudaErrorInvalidValue);
+        return HYPE_ERR_ARG;
+    }
+    // one-time set-up per device, with that device current: the device address of the
+    // scratch array (its name is only a host-side stand-in in host code)
+    int dev = 0;
+    HYPE_CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128) return HYPE_ERR_UNSUPPORTED;
+    unsigned char* base;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mutex);
+        if (!g_noalloc_base[dev]) {
+            void* ptr = nullptr;
+            cudaError_t ce = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+            if (ce != cudaSuccess) {
+                set_last_error("cudaGetSymbolAddress", ce);
+                return HYPE_ERR_CUDA;
+            }
+            g_noalloc_base[dev] = ptr;
+        }
+        base = (unsigned char*)g_noalloc_base[dev];
+    }
+    Geo g;
+    g.nx = p->nx; g.ny = p->ny; g.nz = p->nz;
+    for (int f = 0; f < 6; ++f) g.bc[f] = p->bc[f];
+    g.N = (long long)p->nx * p->ny * p->nz;
+    g.NE = ne;
+    g.ex = p->nx + 2;
+    g.ey = p->ny + 2;
+    void* T = base;
+    double* Fx = (double*)(base + kNoAllocTraceBytes);
+    double* Fy = (double*)(base + kNoAllocTraceBytes + kNoAllocFluxBytes);
+    double* Fz = (double*)(base + kNoAllocTraceBytes + 2 * kNoAllocFluxBytes);
+    DevScalars* ds = (DevScalars*)(base + kNoAllocTraceBytes + 3 * kNoAllocFluxBytes);
+    cudaStream_t s = (cudaStream_t)stream;
+    // the scratch keeps the previous call's contents: the wave-speed maximum and the
+    // admissibility word must start cleared; traces and fluxes are fully rewritten
+    k_reset_slot<<<1, 1, 0, s>>>(ds, 4);
+    const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2);
+    const int lin = p->recon == HYPE_RECON_LINEAR4;
+    const dim3 bf(32, 4);
+    const dim3 gx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4), g.nz), gy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4), g.nz),
+        gz(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz + 1);
+    if (p->precision == HYPE_PREC_FP32) {
+        k_recon<float><<<gr, br, 0, s>>>(dU, (float*)T, g, lin);
+        k_faces<float, 0><<<gx, bf, 0, s>>>((const float*)T, Fx, g, p->gamma, ds, 4);
+        k_faces<float, 1><<<gy, bf, 0, s>>>((const float*)T, Fy, g, p->gamma, ds, 4);
+        k_faces<float, 2><<<gz, bf, 0, s>>>((const float*)T, Fz, g, p->gamma, ds, 4);
+    } else {
+        k_recon<double><<<gr, br, 0, s>>>(dU, (double*)T, g, lin);
+        k_faces<double, 0><<<gx, bf, 0, s>>>((const double*)T, Fx, g, p->gamma, ds, 4);
+        k_faces<double, 1><<<gy, bf, 0, s>>>((const double*)T, Fy, g, p->gamma, ds, 4);
+        k_faces<double, 2><<<gz, bf, 0, s>>>((const double*)T, Fz, g, p->gamma, ds, 4);
+    }
+    const Stage st{0.0, 0.0, 0.0, 1};
+    const dim3 bu(32, 8), gu(cdiv(g.nx, 32), cdiv(g.ny, 8), g.nz);
+    k_update<<<gu, bu, 0, s>>>(Fx, Fy, Fz, nullptr, nullptr, dRHS, g, 1.0 / p->h, st, ds);
+    HYPE_LAUNCHED(6);
+    if (dt_out) {
+        unsigned long long w[2];
+        HYPE_CK(cudaMemcpyAsync(&w[0], &ds->smax_bits[4], sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        HYPE_CK(cudaMemcpyAsync(&w[1], &ds->bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        HYPE_CK(cudaStreamSynchronize(s));
+        *dt_out = (1.0 / 3.0) * (p->cfl * p->h) / (bits_to_double(w[0]) + 0.0);
+        if (w[1] != ~0ull) return HYPE_ERR_STATE;
+    }
+    return HYPE_OK;
+}

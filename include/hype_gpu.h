@@ -118,6 +118,32 @@ void* hype_euler_stream(hype_euler* e);
 int hype_euler_profile(hype_euler* e, int enable);
 int hype_euler_profile_read(hype_euler* e, double* ms, long long* count);
 
+/* Allocation-free RHS evaluation.  This entry point has no counterpart in the
+ * reference.  It serves callers that cannot let the library allocate device
+ * memory: a host that owns every byte of device memory through its own pool and
+ * hands over pre-allocated device vectors, or a latency-critical loop where
+ * cudaMalloc's implicit device-wide synchronisation is not acceptable.  It
+ * computes what hype_euler_rhs_device computes (same kernels, same results) on
+ * device buffers dU -> dRHS (SoA [5][nz][ny][nx]) for the grid and options in
+ * *p, without creating a context and without any cudaMalloc / cudaFree: all
+ * scratch (face traces, face fluxes, the wave-speed and admissibility words)
+ * lives in one fixed device array of this library, about 6.3 MB, that every GPU
+ * which loads the library holds until the process exits.
+ *   - Limit: (nx+2)(ny+2)(nz+2) <= 5832 (e.g. 16^3 cells; hype_euler_noalloc_max_ext
+ *     returns the bound); larger grids return HYPE_ERR_ARG.
+ *   - The first call on a device looks up the array's device address (once per
+ *     device, with that device current); make that first call before any stream
+ *     capture.
+ *   - Every call shares the one array: calls that overlap on the GPU (other
+ *     streams, other host threads on the same device) race and corrupt each
+ *     other's results; serialise them.
+ *   - stream: a cudaStream_t, or NULL for the legacy default stream.  When dt_out
+ *     is non-NULL the call waits for the stream and stores CFL h / (3 s_max) there
+ *     (and returns HYPE_ERR_STATE for an inadmissible state); with dt_out NULL it
+ *     returns without waiting. */
+int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* dU, double* dRHS, double* dt_out, void* stream);
+long long hype_euler_noalloc_max_ext(void);
+
 /* ============================================================ CTCS acoustics */
 /* Drop-in for CTCS(DM, Vec Pold, Vec Pcurr, Vec Pnew, AppCtx*)
  * (2d/ctcs/plane_wave/wave.c:161-203): one leapfrog update
