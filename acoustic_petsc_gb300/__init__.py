@@ -7,9 +7,9 @@ package only binds it (``_lib``) and mirrors the reference's operator interface
 """
 from . import _build, _lib
 from ._lib import HypeError, lib, launches
-from .hype import AppCtx, BatchLeapfrog, CTCS, EulerSolver, Leapfrog, Monopole
+from .hype import AppCtx, BatchLeapfrog, CTCS, EulerSolver, Leapfrog, Monopole, Multiphase2D
 
-__all__ = ["AppCtx", "BatchLeapfrog", "CTCS", "EulerSolver", "HypeError", "Leapfrog", "Monopole", "lib", "launches",
+__all__ = ["AppCtx", "BatchLeapfrog", "CTCS", "EulerSolver", "HypeError", "Leapfrog", "Monopole", "Multiphase2D", "lib", "launches",
            "build"]
 
 

@@ -20,6 +20,9 @@ BC_PERIODIC, BC_REFLECTIVE, BC_TRANSMISSIVE, BC_ZERO = range(4)
 RECON_CWENO4, RECON_LINEAR4 = 0, 1
 PREC_FP64, PREC_FP32 = 0, 1
 DT_MONITOR, DT_FROZEN, DT_FIXED = 0, 1, 2
+FLUX_RUSANOV, FLUX_HLLC, FLUX_ROTHLLC = 0, 1, 2
+MP_DI4, MP_KAPILA5 = 0, 1
+STEP_SSPRK43, STEP_SSPRK104 = 0, 1
 
 # every entry point the header declares (checked by the CPU test suite)
 SYMBOLS = [
@@ -32,6 +35,8 @@ SYMBOLS = [
     "hype_strerror", "hype_last_error", "hype_launch_count", "hype_version",
     "hype_euler_stream", "hype_euler_profile", "hype_euler_profile_read", "hype_set_device", "hype_device_count",
     "hype_probe_fma_peak", "hype_euler_rhs_noalloc", "hype_euler_noalloc_max_ext",
+    "hype_mp2d_create", "hype_mp2d_destroy", "hype_mp2d_rhs", "hype_mp2d_upload", "hype_mp2d_download",
+    "hype_mp2d_step", "hype_mp2d_sync", "hype_mp2d_stream",
 ]
 
 
@@ -48,7 +53,14 @@ class EulerParams(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
                 ("x_min", C.c_double), ("y_min", C.c_double), ("z_min", C.c_double), ("h", C.c_double),
                 ("cfl", C.c_double), ("gamma", C.c_double), ("bc", C.c_int * 6),
-                ("recon", C.c_int), ("precision", C.c_int), ("dt_mode", C.c_int)]
+                ("recon", C.c_int), ("precision", C.c_int), ("dt_mode", C.c_int), ("flux", C.c_int)]
+
+
+class Mp2dParams(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("x_min", C.c_double), ("y_min", C.c_double), ("h", C.c_double),
+                ("cfl", C.c_double), ("bc", C.c_int * 4), ("model", C.c_int), ("g1", C.c_double), ("p1", C.c_double),
+                ("g2", C.c_double), ("p2", C.c_double), ("stepper", C.c_int), ("precision", C.c_int),
+                ("dt_mode", C.c_int)]
 
 
 class Status(C.Structure):
@@ -120,6 +132,14 @@ def lib():
         "hype_probe_fma_peak": ([C.c_int, D], C.c_int),
         "hype_euler_rhs_noalloc": ([P(EulerParams), V, V, D, V], C.c_int),
         "hype_euler_noalloc_max_ext": ([], C.c_longlong),
+        "hype_mp2d_create": ([P(Mp2dParams), P(V)], C.c_int),
+        "hype_mp2d_destroy": ([V], None),
+        "hype_mp2d_rhs": ([V, C.c_double, D, D, D], C.c_int),
+        "hype_mp2d_upload": ([V, D], C.c_int),
+        "hype_mp2d_download": ([V, D], C.c_int),
+        "hype_mp2d_step": ([V, C.c_int, D, D, P(C.c_longlong)], C.c_int),
+        "hype_mp2d_sync": ([V], C.c_int),
+        "hype_mp2d_stream": ([V], C.c_void_p),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

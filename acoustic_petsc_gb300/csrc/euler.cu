@@ -129,7 +129,7 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long* a, double v) 
 
 // Face fluxes of direction D.  Face index (i,j,k) is the face on the low side of
 // cell (i,j,k); along D it runs to n (the high face of the last cell).
-template <typename R, int D>
+template <typename R, int D, int FLUX>
 __global__ void __launch_bounds__(128) k_faces(const R* __restrict__ T, double* __restrict__ F, Geo g, double gamma,
                                                DevScalars* __restrict__ ds, int slot) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(128) k_faces(const R* __restrict__ T, double* 
                 QL[c] = T[((long long)c * NTR + (2 * D + 1) * 4 + gp) * g.NE + eL];
                 QR[c] = T[((long long)c * NTR + (2 * D) * 4 + gp) * g.NE + eR];
             }
-            const R s = rusanov<R, D>(QL, QR, gm, gm1, fl, bad);
+            const R s = face_solver<R, D, FLUX>(QL, QR, gm, gm1, fl, bad);
             smax = fmax(smax, (double)s);
 #pragma unroll
             for (int c = 0; c < NV; ++c) acc[c] += R(0.25) * fl[c];
@@ -296,6 +296,31 @@ static void prof_mark(hype_euler* e, int kind, bool start) {
     }
 }
 
+template <typename R, int FLUX>
+static void launch_faces_t(const Geo& g, const void* T, double* Fx, double* Fy, double* Fz, double gamma, DevScalars* ds,
+                           int slot, cudaStream_t st) {
+    const dim3 bf(32, 4);
+    const dim3 gx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4), g.nz), gy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4), g.nz),
+        gz(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz + 1);
+    k_faces<R, 0, FLUX><<<gx, bf, 0, st>>>((const R*)T, Fx, g, gamma, ds, slot);
+    k_faces<R, 1, FLUX><<<gy, bf, 0, st>>>((const R*)T, Fy, g, gamma, ds, slot);
+    k_faces<R, 2, FLUX><<<gz, bf, 0, st>>>((const R*)T, Fz, g, gamma, ds, slot);
+}
+
+// the three face-flux launches of one RHS, for the context's precision and flux
+static void launch_faces(const Geo& g, const void* T, double* Fx, double* Fy, double* Fz, double gamma, DevScalars* ds,
+                         int slot, bool f32, int flux, cudaStream_t st) {
+    if (f32) {
+        if (flux == HYPE_FLUX_HLLC) launch_faces_t<float, HYPE_FLUX_HLLC>(g, T, Fx, Fy, Fz, gamma, ds, slot, st);
+        else if (flux == HYPE_FLUX_ROTHLLC) launch_faces_t<float, HYPE_FLUX_ROTHLLC>(g, T, Fx, Fy, Fz, gamma, ds, slot, st);
+        else launch_faces_t<float, HYPE_FLUX_RUSANOV>(g, T, Fx, Fy, Fz, gamma, ds, slot, st);
+    } else {
+        if (flux == HYPE_FLUX_HLLC) launch_faces_t<double, HYPE_FLUX_HLLC>(g, T, Fx, Fy, Fz, gamma, ds, slot, st);
+        else if (flux == HYPE_FLUX_ROTHLLC) launch_faces_t<double, HYPE_FLUX_ROTHLLC>(g, T, Fx, Fy, Fz, gamma, ds, slot, st);
+        else launch_faces_t<double, HYPE_FLUX_RUSANOV>(g, T, Fx, Fy, Fz, gamma, ds, slot, st);
+    }
+}
+
 static int launch_rhs(hype_euler* e, const double* Win, int slot) {
     const Geo& g = e->g;
     const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2);
@@ -308,18 +333,7 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
         k_recon<double><<<gr, br, 0, e->stream>>>(Win, (double*)e->T, g, lin);
     prof_mark(e, 0, false);
     prof_mark(e, 1, true);
-    const dim3 bf(32, 4);
-    const dim3 gx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4), g.nz), gy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4), g.nz),
-        gz(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz + 1);
-    if (f32) {
-        k_faces<float, 0><<<gx, bf, 0, e->stream>>>((const float*)e->T, e->Fx, g, e->p.gamma, e->ds, slot);
-        k_faces<float, 1><<<gy, bf, 0, e->stream>>>((const float*)e->T, e->Fy, g, e->p.gamma, e->ds, slot);
-        k_faces<float, 2><<<gz, bf, 0, e->stream>>>((const float*)e->T, e->Fz, g, e->p.gamma, e->ds, slot);
-    } else {
-        k_faces<double, 0><<<gx, bf, 0, e->stream>>>((const double*)e->T, e->Fx, g, e->p.gamma, e->ds, slot);
-        k_faces<double, 1><<<gy, bf, 0, e->stream>>>((const double*)e->T, e->Fy, g, e->p.gamma, e->ds, slot);
-        k_faces<double, 2><<<gz, bf, 0, e->stream>>>((const double*)e->T, e->Fz, g, e->p.gamma, e->ds, slot);
-    }
+    launch_faces(e->g, e->T, e->Fx, e->Fy, e->Fz, e->p.gamma, e->ds, slot, f32, e->p.flux, e->stream);
     prof_mark(e, 1, false);
     HYPE_LAUNCHED(4);
     return HYPE_OK;
@@ -346,6 +360,7 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
     if (p->recon != HYPE_RECON_CWENO4 && p->recon != HYPE_RECON_LINEAR4) return HYPE_ERR_ARG;
     if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32) return HYPE_ERR_ARG;
     if (p->dt_mode < HYPE_DT_MONITOR || p->dt_mode > HYPE_DT_FIXED) return HYPE_ERR_ARG;
+    if (p->flux < HYPE_FLUX_RUSANOV || p->flux > HYPE_FLUX_ROTHLLC) return HYPE_ERR_ARG;
     hype_euler* e = new hype_euler();
     e->p = *p;
     Geo& g = e->g;
@@ -616,6 +631,7 @@ extern "C" int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* 
         if ((p->bc[2 * d] == HYPE_BC_PERIODIC) != (p->bc[2 * d + 1] == HYPE_BC_PERIODIC)) return HYPE_ERR_ARG;
     if (p->recon != HYPE_RECON_CWENO4 && p->recon != HYPE_RECON_LINEAR4) return HYPE_ERR_ARG;
     if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32) return HYPE_ERR_ARG;
+    if (p->flux < HYPE_FLUX_RUSANOV || p->flux > HYPE_FLUX_ROTHLLC) return HYPE_ERR_ARG;
     const long long ne = (long long)(p->nx + 2) * (p->ny + 2) * (p->nz + 2);
     if (ne > kNoAllocMaxExt) {
         set_last_error("hype_euler_rhs_noalloc: grid exceeds the fixed scratch ((nx+2)(ny+2)(nz+2) > 5832)",
@@ -659,20 +675,11 @@ extern "C" int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* 
     k_reset_slot<<<1, 1, 0, s>>>(ds, 4);
     const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2);
     const int lin = p->recon == HYPE_RECON_LINEAR4;
-    const dim3 bf(32, 4);
-    const dim3 gx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4), g.nz), gy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4), g.nz),
-        gz(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz + 1);
-    if (p->precision == HYPE_PREC_FP32) {
+    if (p->precision == HYPE_PREC_FP32)
         k_recon<float><<<gr, br, 0, s>>>(dU, (float*)T, g, lin);
-        k_faces<float, 0><<<gx, bf, 0, s>>>((const float*)T, Fx, g, p->gamma, ds, 4);
-        k_faces<float, 1><<<gy, bf, 0, s>>>((const float*)T, Fy, g, p->gamma, ds, 4);
-        k_faces<float, 2><<<gz, bf, 0, s>>>((const float*)T, Fz, g, p->gamma, ds, 4);
-    } else {
+    else
         k_recon<double><<<gr, br, 0, s>>>(dU, (double*)T, g, lin);
-        k_faces<double, 0><<<gx, bf, 0, s>>>((const double*)T, Fx, g, p->gamma, ds, 4);
-        k_faces<double, 1><<<gy, bf, 0, s>>>((const double*)T, Fy, g, p->gamma, ds, 4);
-        k_faces<double, 2><<<gz, bf, 0, s>>>((const double*)T, Fz, g, p->gamma, ds, 4);
-    }
+    launch_faces(g, T, Fx, Fy, Fz, p->gamma, ds, 4, p->precision == HYPE_PREC_FP32, p->flux, s);
     const Stage st{0.0, 0.0, 0.0, 1};
     const dim3 bu(32, 8), gu(cdiv(g.nx, 32), cdiv(g.ny, 8), g.nz);
     k_update<<<gu, bu, 0, s>>>(Fx, Fy, Fz, nullptr, nullptr, dRHS, g, 1.0 / p->h, st, ds);

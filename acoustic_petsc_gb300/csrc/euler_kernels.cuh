@@ -308,5 +308,151 @@ __device__ __forceinline__ R rusanov(const R* QL, const R* QR, R gamma, R gm1, R
     return s;
 }
 
+// ---------------------------------------------------------------- HLLC family
+// PDEConsFlux with a general unit normal (Navier-Stokes-3D/pde.c:40-88)
+template <typename R>
+__device__ __forceinline__ R cons_flux_n(const R* Q, R nx, R ny, R nz, R gamma, R gm1, R* F, bool& bad) {
+    const R rho = Q[0];
+    const R ir = R(1) / rho;
+    const R u = ir * Q[1], v = ir * Q[2], w = ir * Q[3];
+    const R E = Q[4];
+    const R p = gm1 * (E - R(0.5) * rho * (u * u + v * v + w * w));
+    bad |= (rho < R(1.0e-14)) || (p < R(1.0e-12)) || !(rho == rho);
+    const R un = nx * u + ny * v + nz * w;
+    const R mun = rho * un;
+    F[0] = mun;
+    F[1] = mun * u + nx * p;
+    F[2] = mun * v + ny * p;
+    F[3] = mun * w + nz * p;
+    F[4] = (E + p) * un;
+    return fabs(un) + sqrt(ir * gamma * p);
+}
+
+// Miller-Colella tangents (pde.c:236-251; 'fixed' = the corrected t2z of pde.c:348)
+template <typename R>
+__device__ __forceinline__ void mc_tangents(R nx, R ny, R nz, bool fixed, R* t1, R* t2) {
+    if (fabs(ny + nz) > fabs(ny - nz)) {
+        const R iL = R(1) / sqrt(R(2) * (R(1) + nz * (ny - nx) + nx * ny));
+        t1[0] = (ny + nz) * iL; t1[1] = (nz - nx) * iL; t1[2] = -(nx + ny) * iL;
+        t2[0] = (nx * (nz - ny) - ny * ny - nz * nz) * iL;
+        t2[1] = (ny * (nx + nz) + nx * nx + nz * nz) * iL;
+        t2[2] = (fixed ? (nz * (nx - ny) - nx * nx - ny * ny) : (nz * (nx - nz) - nx * nx - ny * ny)) * iL;
+    } else {
+        const R iL = R(1) / sqrt(R(2) * (R(1) - nx * ny - nx * nz - ny * nz));
+        t1[0] = (ny - nz) * iL; t1[1] = (nz - nx) * iL; t1[2] = (nx - ny) * iL;
+        t2[0] = (nx * (ny + nz) - ny * ny - nz * nz) * iL;
+        t2[1] = (ny * (nx + nz) - nx * nx - nz * nz) * iL;
+        t2[2] = (nz * (nx + ny) - nx * nx - ny * ny) * iL;
+    }
+}
+
+// PDEHLLCRiemannSolver (pde.c:207-322): star states built in the (n, t1, t2)
+// frame and rotated back with the inverse frame matrix
+template <typename R>
+__device__ __forceinline__ R hllc(const R* QL, const R* QR, R nx, R ny, R nz, R gamma, R gm1, R* Flux, bool& bad) {
+    R FL[NV], FR[NV];
+    const R sl = cons_flux_n<R>(QL, nx, ny, nz, gamma, gm1, FL, bad);
+    const R sr = cons_flux_n<R>(QR, nx, ny, nz, gamma, gm1, FR, bad);
+    R t1[3], t2[3];
+    mc_tangents<R>(nx, ny, nz, false, t1, t2);
+    // inverse of the frame matrix [n; t1; t2] by cofactors (pde.c:189-205)
+    const R M00 = nx, M01 = ny, M02 = nz, M10 = t1[0], M11 = t1[1], M12 = t1[2], M20 = t2[0], M21 = t2[1], M22 = t2[2];
+    const R idet = R(1) / (M00 * (M11 * M22 - M12 * M21) - M01 * (M10 * M22 - M12 * M20) + M02 * (M10 * M21 - M11 * M20));
+    const R i00 = (M11 * M22 - M12 * M21) * idet, i01 = -(M01 * M22 - M02 * M21) * idet, i02 = (M01 * M12 - M02 * M11) * idet;
+    const R i10 = -(M10 * M22 - M12 * M20) * idet, i11 = (M00 * M22 - M02 * M20) * idet, i12 = -(M00 * M12 - M02 * M10) * idet;
+    const R i20 = (M10 * M21 - M11 * M20) * idet, i21 = -(M00 * M21 - M01 * M20) * idet, i22 = (M00 * M11 - M01 * M10) * idet;
+    R S[2], un[2], ut1[2], ut2[2], rho[2], P[2], E[2], c[2];
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+        const R* Q = side ? QR : QL;
+        const R ir = R(1) / Q[0];
+        const R u = ir * Q[1], v = ir * Q[2], w = ir * Q[3];
+        rho[side] = Q[0];
+        P[side] = gm1 * (Q[4] - R(0.5) * ir * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]));
+        E[side] = Q[4];
+        un[side] = u * nx + v * ny + w * nz;
+        ut1[side] = u * t1[0] + v * t1[1] + w * t1[2];
+        ut2[side] = u * t2[0] + v * t2[1] + w * t2[2];
+        c[side] = sqrt(gamma * P[side] / rho[side]);
+    }
+    const R SL = fmin(un[1] - c[1], un[0] - c[0]);
+    const R SR = fmax(un[0] + c[0], un[1] + c[1]);
+    S[0] = SL;
+    S[1] = SR;
+    const R Ss = (P[1] - P[0] + rho[0] * un[0] * (SL - un[0]) - rho[1] * un[1] * (SR - un[1])) /
+                 (rho[0] * (SL - un[0]) - rho[1] * (SR - un[1]));
+    R Fs[2][NV];
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+        const R* Q = side ? QR : QL;
+        const R* Fo = side ? FR : FL;
+        const R d = S[side] - un[side];
+        const R q0 = rho[side] * d / (S[side] - Ss);
+        R Qs[NV];
+        Qs[0] = q0;
+        Qs[1] = q0 * (Ss * i00 + ut1[side] * i01 + ut2[side] * i02);
+        Qs[2] = q0 * (Ss * i10 + ut1[side] * i11 + ut2[side] * i12);
+        Qs[3] = q0 * (Ss * i20 + ut1[side] * i21 + ut2[side] * i22);
+        Qs[4] = q0 * ((E[side] / rho[side]) + (Ss - un[side]) * (Ss + P[side] / (rho[side] * d)));
+#pragma unroll
+        for (int k = 0; k < NV; ++k) Fs[side][k] = Fo[k] + S[side] * (Qs[k] - Q[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+        Flux[k] = (SL > R(0)) ? FL[k] : (Ss >= R(0)) ? Fs[0][k] : (SR >= R(0)) ? Fs[1][k] : FR[k];
+    return sl < sr ? sr : sl;
+}
+
+// PDErotHLLCRiemannSolver (pde.c:324-384): HLLC along the velocity-jump
+// direction n1 and its two tangents, weighted by their projections on n
+template <typename R>
+__device__ __forceinline__ R rot_hllc(const R* QL, const R* QR, R nx, R ny, R nz, R gamma, R gm1, R* Flux, bool& bad) {
+    R irho = R(1) / QL[0];
+    const R uL = irho * QL[1], vL = irho * QL[2], wL = irho * QL[3];
+    irho = R(1) / QR[0];
+    const R du = irho * QR[1] - uL, dv = irho * QR[2] - vL, dw = irho * QR[3] - wL;
+    const R dq = sqrt(du * du + dv * dv + dw * dw);
+    R n1[3];
+    if (dq < R(1.0E-10)) {
+        n1[0] = nx; n1[1] = ny; n1[2] = nz;
+    } else {
+        const R idq = R(1) / dq;
+        n1[0] = du * idq; n1[1] = dv * idq; n1[2] = dw * idq;
+    }
+    R a1 = n1[0] * nx + n1[1] * ny + n1[2] * nz;
+    if (a1 < R(0)) {
+        n1[0] = -n1[0]; n1[1] = -n1[1]; n1[2] = -n1[2];
+        a1 = -a1;
+    }
+    R t1[3], t2[3];
+    mc_tangents<R>(n1[0], n1[1], n1[2], true, t1, t2);
+    R a2 = t1[0] * nx + t1[1] * ny + t1[2] * nz;
+    if (a2 < R(0)) {
+        t1[0] = -t1[0]; t1[1] = -t1[1]; t1[2] = -t1[2];
+        a2 = -a2;
+    }
+    R a3 = t2[0] * nx + t2[1] * ny + t2[2] * nz;
+    if (a3 < R(0)) {
+        t2[0] = -t2[0]; t2[1] = -t2[1]; t2[2] = -t2[2];
+        a3 = -a3;
+    }
+    R F1[NV], F2[NV], F3[NV];
+    const R s1 = hllc<R>(QL, QR, n1[0], n1[1], n1[2], gamma, gm1, F1, bad);
+    const R s2 = hllc<R>(QL, QR, t1[0], t1[1], t1[2], gamma, gm1, F2, bad);
+    const R s3 = hllc<R>(QL, QR, t2[0], t2[1], t2[2], gamma, gm1, F3, bad);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) Flux[k] = a1 * F1[k] + a2 * F2[k] + a3 * F3[k];
+    return fmax(s1, fmax(s2, s3));
+}
+
+// numerical flux selected by the context (HYPE_FLUX_*) across an axis face of normal D
+template <typename R, int D, int FLUX>
+__device__ __forceinline__ R face_solver(const R* QL, const R* QR, R gamma, R gm1, R* F, bool& bad) {
+    if (FLUX == HYPE_FLUX_RUSANOV) return rusanov<R, D>(QL, QR, gamma, gm1, F, bad);
+    const R nx = R(D == 0), ny = R(D == 1), nz = R(D == 2);
+    if (FLUX == HYPE_FLUX_HLLC) return hllc<R>(QL, QR, nx, ny, nz, gamma, gm1, F, bad);
+    return rot_hllc<R>(QL, QR, nx, ny, nz, gamma, gm1, F, bad);
+}
+
 }  // namespace euler
 }  // namespace hype

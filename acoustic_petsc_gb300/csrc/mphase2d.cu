@@ -1,0 +1,484 @@
+// mphase2d.cu -- 2D multiphase finite-volume RHS and SSP steppers on sm_103a.
+//
+// Per RHS evaluation (2d/weno4/bubble/rhs_function.c:12-390):
+//   k_mp_prim   conserved -> primitive (ComputePrimitiveVariables), FP64;
+//   k_mp_recon  one thread per cell of [-1,n]^2 that some owned face needs:
+//               boundary map of the 13-point primitive stencil (replaces
+//               DMGlobalToLocal + the BC sweeps :54-170), 2D CWENO4 per variable,
+//               the 8-node admissibility check and the minmod fallback (:220-250),
+//               the 4 faces x 2 Gauss-point traces (:252-273);
+//   k_mp_faces  rotated HLLC at the two Gauss points of each face with the
+//               interface-velocity component (:277-349), wave-speed max, flags;
+//   k_mp_update divergence with the non-conservative volume-fraction term
+//               (:351-380) fused with the stage combination.
+// dt = CFL h / (2 s_max) is formed on the device (:385).
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include "mphase2d_kernels.cuh"
+
+namespace hype {
+namespace mp2d {
+
+struct Geo {
+    int nx, ny, nv;
+    int bc[4];
+    long long N, NE;  // owned cells, extended cells (nx+2)(ny+2)
+};
+
+struct DevScalars {
+    unsigned long long smax_bits[12];  // per stage (10 max) + RHS-only slot 11
+    double dt, t;
+    unsigned long long bad;
+    unsigned long long fallback;  // owned cells reconstructed with the minmod fallback
+};
+
+__device__ __forceinline__ double node_x(int q) {
+    return q < 2 ? 0.5 : q < 4 ? -0.5 : (q == 4 || q == 6) ? -0.28867513459481287 : 0.28867513459481287;
+}
+__device__ __forceinline__ double node_y(int q) {
+    return q < 4 ? ((q & 1) ? 0.28867513459481287 : -0.28867513459481287) : (q < 6 ? -0.5 : 0.5);
+}
+// face f (0 -x, 1 +x, 2 -y, 3 +y), Gauss point q (0: -g, 1: +g)
+__device__ __forceinline__ double face_x(int f, int q) {
+    const double g = q ? 0.28867513459481287 : -0.28867513459481287;
+    return f == 0 ? -0.5 : f == 1 ? 0.5 : g;
+}
+__device__ __forceinline__ double face_y(int f, int q) {
+    const double g = q ? 0.28867513459481287 : -0.28867513459481287;
+    return f == 2 ? -0.5 : f == 3 ? 0.5 : g;
+}
+
+__global__ void k_mp_prim(const double* __restrict__ U, double* __restrict__ P, Eos e, long long N, int nv) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= N) return;
+    double Q[MAXV], V[MAXV];
+    for (int c = 0; c < nv; ++c) Q[c] = U[c * N + q];
+    cons2prim(e, Q, V);
+    for (int c = 0; c < nv; ++c) P[c * N + q] = V[c];
+}
+
+template <typename R, int MODEL>
+__global__ void __launch_bounds__(128) k_mp_recon(const double* __restrict__ P, R* __restrict__ T, Geo g, Eos e,
+                                                  DevScalars* __restrict__ ds) {
+    constexpr int NV = MODEL == HYPE_MP_DI4 ? 5 : 6;
+    constexpr int IU = MODEL == HYPE_MP_DI4 ? 1 : 2;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+    if (i > g.nx || j > g.ny) return;
+    const bool gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny);
+    if (gi && gj) return;
+    int mi[5], mj[5], fi = 0, fj = 0;
+#pragma unroll
+    for (int o = 0; o < 5; ++o) {
+        int f = 0;
+        mi[o] = bmap(i + o - 2, g.nx, g.bc[0], g.bc[1], &f);
+        fi |= f << o;
+        f = 0;
+        mj[o] = bmap(j + o - 2, g.ny, g.bc[2], g.bc[3], &f);
+        fj |= f << o;
+    }
+    const long long e_ = (long long)(j + 1) * (g.nx + 2) + (i + 1);
+    R VN[8][NV];
+#pragma unroll 1
+    for (int c = 0; c < NV; ++c) {
+        const double* Pc = P + (long long)c * g.N;
+        auto ld = [&](int oi, int oj) -> R {
+            double v = __ldg(Pc + (long long)mj[oj + 2] * g.nx + mi[oi + 2]);
+            // a reflective ghost negates the velocity normal to its wall (x: u, y: v)
+            if (c == IU && ((fi >> (oi + 2)) & 1)) v = -v;
+            if (c == IU + 1 && ((fj >> (oj + 2)) & 1)) v = -v;
+            return (R)v;
+        };
+        R ux[5], uy[5], cf[NDOF];
+#pragma unroll
+        for (int o = 0; o < 5; ++o) {
+            ux[o] = ld(o - 2, 0);
+            uy[o] = ld(0, o - 2);
+        }
+        cweno2d<R>(ux[2], ux, uy, ld(1, 1), ld(1, -1), ld(-1, 1), ld(-1, -1), cf);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            R v = R(0);
+#pragma unroll
+            for (int k = 0; k < NDOF; ++k) v += cf[k] * R(basis2(node_x(q), node_y(q), k));
+            VN[q][c] = v;
+        }
+        R* Tc = T + (long long)c * 8 * g.NE + e_;
+#pragma unroll
+        for (int f = 0; f < 4; ++f)
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                R v = R(0);
+#pragma unroll
+                for (int k = 0; k < NDOF; ++k) v += cf[k] * R(basis2(face_x(f, q), face_y(f, q), k));
+                Tc[(long long)(f * 2 + q) * g.NE] = v;
+            }
+    }
+    bool ok = true;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) ok = ok && pad_ok<R>(e, VN[q]);
+    if (ok) return;
+    // physically inadmissible somewhere in the cell: first order + minmod slopes (rhs_function.c:239-250)
+    if (!gi && !gj) atomicAdd(&ds->fallback, 1ull);
+#pragma unroll 1
+    for (int c = 0; c < NV; ++c) {
+        const double* Pc = P + (long long)c * g.N;
+        auto ld = [&](int oi, int oj) -> R {
+            double v = __ldg(Pc + (long long)mj[oj + 2] * g.nx + mi[oi + 2]);
+            if (c == IU && ((fi >> (oi + 2)) & 1)) v = -v;
+            if (c == IU + 1 && ((fj >> (oj + 2)) & 1)) v = -v;
+            return (R)v;
+        };
+        const R w0 = ld(0, 0);
+        const R sx = minmod<R>(ld(1, 0) - w0, w0 - ld(-1, 0));
+        const R sy = minmod<R>(ld(0, 1) - w0, w0 - ld(0, -1));
+        R* Tc = T + (long long)c * 8 * g.NE + e_;
+#pragma unroll
+        for (int f = 0; f < 4; ++f)
+#pragma unroll
+            for (int q = 0; q < 2; ++q) Tc[(long long)(f * 2 + q) * g.NE] = w0 + sx * R(face_x(f, q)) + sy * R(face_y(f, q));
+    }
+}
+
+template <typename R, int MODEL, int D>
+__global__ void __launch_bounds__(128) k_mp_faces(const R* __restrict__ T, double* __restrict__ F, Geo g, Eos e,
+                                                  DevScalars* __restrict__ ds, int slot) {
+    constexpr int NV = MODEL == HYPE_MP_DI4 ? 5 : 6;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int fx = g.nx + (D == 0), fy = g.ny + (D == 1);
+    double smax = 0.0;
+    bool bad = false;
+    if (i < fx && j < fy) {
+        const long long eR = (long long)(j + 1) * (g.nx + 2) + (i + 1);
+        const long long eL = eR - (D == 0 ? 1 : (g.nx + 2));
+        R acc[NV + 1];
+#pragma unroll
+        for (int c = 0; c <= NV; ++c) acc[c] = R(0);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            R VL[NV], VR[NV], fl[MAXV + 1];
+#pragma unroll
+            for (int c = 0; c < NV; ++c) {
+                VL[c] = T[((long long)c * 8 + (2 * D + 1) * 2 + q) * g.NE + eL];
+                VR[c] = T[((long long)c * 8 + (2 * D) * 2 + q) * g.NE + eR];
+            }
+            const R s = rot_hllc2<R, MODEL>(e, VL, VR, R(D == 0), R(D == 1), fl, bad);
+            smax = fmax(smax, (double)s);
+#pragma unroll
+            for (int c = 0; c <= NV; ++c) acc[c] += R(0.5) * fl[c];
+        }
+        const long long nf = (long long)fx * fy;
+        const long long f = (long long)j * fx + i;
+#pragma unroll
+        for (int c = 0; c <= NV; ++c) F[c * nf + f] = (double)acc[c];
+        if (bad) atomicMin(&ds->bad, (unsigned long long)((long long)(j < g.ny ? j : g.ny - 1) * g.nx + (i < g.nx ? i : g.nx - 1)));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, o));
+    if ((threadIdx.x & 31) == 0 && smax > 0.0) atomicMax(&ds->smax_bits[slot], (unsigned long long)__double_as_longlong(smax));
+}
+
+// out = a*X + b*Y + (c*dt)*L, L the divergence with the volume-fraction term
+struct Stage {
+    double a, b, c;
+    int rhs_only;
+};
+
+__global__ void __launch_bounds__(256) k_mp_update(const double* __restrict__ F, const double* __restrict__ G,
+                                                   const double* __restrict__ Win, const double* __restrict__ X,
+                                                   const double* __restrict__ Y, double* __restrict__ out, Geo g,
+                                                   double r1_h, Stage st, const DevScalars* __restrict__ ds) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.nx || j >= g.ny) return;
+    const int nv = g.nv, ia = nv - 1;
+    const long long nfx = (long long)(g.nx + 1) * g.ny, nfy = (long long)g.nx * (g.ny + 1);
+    const long long fxl = (long long)j * (g.nx + 1) + i, fyl = (long long)j * g.nx + i;
+    const long long cell = (long long)j * g.nx + i;
+    const double a = Win[ia * g.N + cell];
+    const double cdt = st.rhs_only ? 0.0 : st.c * ds->dt;
+    for (int c = 0; c < nv; ++c) {
+        double L;
+        if (c == ia)
+            L = -r1_h * ((F[c * nfx + fxl + 1] - a * F[(c + 1) * nfx + fxl + 1]) - (F[c * nfx + fxl] - a * F[(c + 1) * nfx + fxl])) -
+                r1_h * ((G[c * nfy + fyl + g.nx] - a * G[(c + 1) * nfy + fyl + g.nx]) - (G[c * nfy + fyl] - a * G[(c + 1) * nfy + fyl]));
+        else
+            L = -r1_h * (F[c * nfx + fxl + 1] - F[c * nfx + fxl]) - r1_h * (G[c * nfy + fyl + g.nx] - G[c * nfy + fyl]);
+        double v;
+        if (st.rhs_only) {
+            v = L;
+        } else {
+            v = st.a * X[c * g.N + cell] + cdt * L;
+            if (st.b != 0.0) v += st.b * Y[c * g.N + cell];
+        }
+        out[c * g.N + cell] = v;
+    }
+}
+
+__global__ void k_mp_axpby(const double* __restrict__ X, const double* __restrict__ Y, double* __restrict__ out, double a,
+                           double b, long long n) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q < n) out[q] = a * X[q] + b * Y[q];
+}
+
+__global__ void k_mp_begin(DevScalars* ds, int mode, int src, int use_src, int reset, double cfl_h) {
+    if (use_src && mode != HYPE_DT_FIXED) {
+        const double smax = __longlong_as_double((long long)ds->smax_bits[src]);
+        ds->dt = cfl_h / (2.0 * smax);
+    }
+    if (reset)
+        for (int s = 0; s < 10; ++s) ds->smax_bits[s] = 0ull;
+    ds->t += ds->dt;
+}
+
+__global__ void k_mp_reset(DevScalars* ds, int slot) {
+    ds->smax_bits[slot] = 0ull;
+    ds->bad = ~0ull;
+}
+
+__global__ void k_aos2soa(const double* __restrict__ a, double* __restrict__ s, long long N, int nv) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= N * nv) return;
+    const long long cell = q / nv;
+    s[(q - cell * nv) * N + cell] = a[q];
+}
+__global__ void k_soa2aos(const double* __restrict__ s, double* __restrict__ a, long long N, int nv) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= N * nv) return;
+    const long long cell = q / nv;
+    a[q] = s[(q - cell * nv) * N + cell];
+}
+
+}  // namespace mp2d
+}  // namespace hype
+
+using namespace hype;
+using namespace hype::mp2d;
+
+static inline double bits2d(unsigned long long b) {
+    double d;
+    memcpy(&d, &b, sizeof(d));
+    return d;
+}
+
+struct hype_mp2d {
+    hype_mp2d_params p;
+    Geo g;
+    Eos e;
+    cudaStream_t stream = nullptr;
+    double *U = nullptr, *W0 = nullptr, *W1 = nullptr, *L = nullptr, *S = nullptr, *P = nullptr;
+    void* T = nullptr;
+    double *F = nullptr, *G = nullptr, *stage_aos = nullptr;
+    DevScalars* ds = nullptr;
+    DevScalars* hs = nullptr;
+};
+
+static int mp_rhs(hype_mp2d* m, const double* Win, int slot) {
+    const Geo& g = m->g;
+    k_mp_prim<<<cdiv(g.N, 256), 256, 0, m->stream>>>(Win, m->P, m->e, g.N, g.nv);
+    const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4));
+    const dim3 gx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4)), gy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4));
+    const bool f32 = m->p.precision == HYPE_PREC_FP32;
+    double* Gf = m->G;
+#define MP_LAUNCH(R, M)                                                                                        \
+    do {                                                                                                       \
+        k_mp_recon<R, M><<<gr, br, 0, m->stream>>>(m->P, (R*)m->T, g, m->e, m->ds);                            \
+        k_mp_faces<R, M, 0><<<gx, br, 0, m->stream>>>((const R*)m->T, m->F, g, m->e, m->ds, slot);             \
+        k_mp_faces<R, M, 1><<<gy, br, 0, m->stream>>>((const R*)m->T, Gf, g, m->e, m->ds, slot);               \
+    } while (0)
+    if (m->e.model == HYPE_MP_DI4) {
+        if (f32) MP_LAUNCH(float, HYPE_MP_DI4);
+        else MP_LAUNCH(double, HYPE_MP_DI4);
+    } else {
+        if (f32) MP_LAUNCH(float, HYPE_MP_KAPILA5);
+        else MP_LAUNCH(double, HYPE_MP_KAPILA5);
+    }
+#undef MP_LAUNCH
+    HYPE_LAUNCHED(4);
+    return HYPE_OK;
+}
+
+static int mp_update(hype_mp2d* m, const double* Win, const double* X, const double* Y, double* out, Stage st) {
+    const Geo& g = m->g;
+    const dim3 b(32, 8), gr(cdiv(g.nx, 32), cdiv(g.ny, 8));
+    k_mp_update<<<gr, b, 0, m->stream>>>(m->F, m->G, Win, X, Y, out, g, 1.0 / m->p.h, st, m->ds);
+    HYPE_LAUNCHED(1);
+    return HYPE_OK;
+}
+
+extern "C" int hype_mp2d_create(const hype_mp2d_params* p, hype_mp2d** out) {
+    if (!p || !out) return HYPE_ERR_ARG;
+    *out = nullptr;
+    if (p->nx < 3 || p->ny < 3 || !(p->h > 0) || !(p->cfl > 0)) return HYPE_ERR_ARG;
+    if (p->model != HYPE_MP_DI4 && p->model != HYPE_MP_KAPILA5) return HYPE_ERR_ARG;
+    if (!(p->g1 > 1.0) || !(p->g2 > 1.0) || p->p1 < 0 || p->p2 < 0) return HYPE_ERR_ARG;
+    for (int f = 0; f < 4; ++f)
+        if (p->bc[f] < HYPE_BC_PERIODIC || p->bc[f] > HYPE_BC_TRANSMISSIVE) return HYPE_ERR_ARG;
+    for (int d = 0; d < 2; ++d)
+        if ((p->bc[2 * d] == HYPE_BC_PERIODIC) != (p->bc[2 * d + 1] == HYPE_BC_PERIODIC)) return HYPE_ERR_ARG;
+    if (p->stepper != HYPE_STEP_SSPRK43 && p->stepper != HYPE_STEP_SSPRK104) return HYPE_ERR_ARG;
+    if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32) return HYPE_ERR_ARG;
+    if (p->dt_mode < HYPE_DT_MONITOR || p->dt_mode > HYPE_DT_FIXED) return HYPE_ERR_ARG;
+    hype_mp2d* m = new hype_mp2d();
+    m->p = *p;
+    Geo& g = m->g;
+    g.nx = p->nx; g.ny = p->ny; g.nv = p->model == HYPE_MP_DI4 ? 5 : 6;
+    for (int f = 0; f < 4; ++f) g.bc[f] = p->bc[f];
+    g.N = (long long)p->nx * p->ny;
+    g.NE = (long long)(p->nx + 2) * (p->ny + 2);
+    m->e = Eos{p->model, p->g1, p->p1, p->g2, p->p2};
+    const size_t sN = sizeof(double) * g.nv * (size_t)g.N;
+    const size_t tsz = (p->precision == HYPE_PREC_FP32 ? 4 : 8) * (size_t)g.nv * 8 * g.NE;
+    cudaError_t ce = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+    double** bufs[] = {&m->U, &m->W0, &m->W1, &m->L, &m->S, &m->P, &m->stage_aos};
+    for (auto b : bufs)
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)b, sN);
+    if (ce == cudaSuccess) ce = cudaMalloc(&m->T, tsz);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&m->F, sizeof(double) * (g.nv + 1) * (size_t)(p->nx + 1) * p->ny);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&m->G, sizeof(double) * (g.nv + 1) * (size_t)p->nx * (p->ny + 1));
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&m->ds, sizeof(DevScalars));
+    if (ce == cudaSuccess) ce = cudaMallocHost((void**)&m->hs, sizeof(DevScalars));
+    if (ce == cudaSuccess) {
+        DevScalars z;
+        memset(&z, 0, sizeof(z));
+        z.bad = ~0ull;
+        ce = cudaMemcpy(m->ds, &z, sizeof(z), cudaMemcpyHostToDevice);
+    }
+    if (ce != cudaSuccess) {
+        set_last_error("hype_mp2d_create", ce);
+        hype_mp2d_destroy(m);
+        return ce == cudaErrorMemoryAllocation ? HYPE_ERR_NOMEM : HYPE_ERR_CUDA;
+    }
+    *out = m;
+    return HYPE_OK;
+}
+
+extern "C" void hype_mp2d_destroy(hype_mp2d* m) {
+    if (!m) return;
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    cudaFree(m->U); cudaFree(m->W0); cudaFree(m->W1); cudaFree(m->L); cudaFree(m->S); cudaFree(m->P);
+    cudaFree(m->stage_aos); cudaFree(m->T); cudaFree(m->F); cudaFree(m->G); cudaFree(m->ds);
+    if (m->hs) cudaFreeHost(m->hs);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+}
+
+static int mp_h2d(hype_mp2d* m, const double* aos, double* soa) {
+    const long long n = m->g.N * m->g.nv;
+    HYPE_CK(cudaMemcpyAsync(m->stage_aos, aos, sizeof(double) * n, cudaMemcpyHostToDevice, m->stream));
+    k_aos2soa<<<cdiv(n, 256), 256, 0, m->stream>>>(m->stage_aos, soa, m->g.N, m->g.nv);
+    HYPE_LAUNCHED(1);
+    return HYPE_OK;
+}
+
+static int mp_d2h(hype_mp2d* m, const double* soa, double* aos) {
+    const long long n = m->g.N * m->g.nv;
+    k_soa2aos<<<cdiv(n, 256), 256, 0, m->stream>>>(soa, m->stage_aos, m->g.N, m->g.nv);
+    HYPE_LAUNCHED(1);
+    HYPE_CK(cudaMemcpyAsync(aos, m->stage_aos, sizeof(double) * n, cudaMemcpyDeviceToHost, m->stream));
+    return HYPE_OK;
+}
+
+static int mp_scalars(hype_mp2d* m) {
+    HYPE_CK(cudaMemcpyAsync(m->hs, m->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, m->stream));
+    HYPE_CK(cudaStreamSynchronize(m->stream));
+    return HYPE_OK;
+}
+
+extern "C" int hype_mp2d_rhs(hype_mp2d* m, double t, const double* U_aos, double* RHS_aos, double* dt_out) {
+    (void)t;
+    if (!m || !U_aos || !RHS_aos) return HYPE_ERR_ARG;
+    int rc;
+    if ((rc = mp_h2d(m, U_aos, m->S))) return rc;
+    k_mp_reset<<<1, 1, 0, m->stream>>>(m->ds, 11);
+    HYPE_LAUNCHED(1);
+    if ((rc = mp_rhs(m, m->S, 11))) return rc;
+    if ((rc = mp_update(m, m->S, nullptr, nullptr, m->L, Stage{0, 0, 0, 1}))) return rc;
+    if ((rc = mp_d2h(m, m->L, RHS_aos))) return rc;
+    if ((rc = mp_scalars(m))) return rc;
+    if (dt_out) *dt_out = (m->p.cfl * m->p.h) / (2.0 * bits2d(m->hs->smax_bits[11]));
+    return m->hs->bad == ~0ull ? HYPE_OK : HYPE_ERR_STATE;
+}
+
+extern "C" int hype_mp2d_upload(hype_mp2d* m, const double* U_aos) {
+    if (!m || !U_aos) return HYPE_ERR_ARG;
+    int rc = mp_h2d(m, U_aos, m->U);
+    if (rc) return rc;
+    HYPE_CK(cudaStreamSynchronize(m->stream));
+    return HYPE_OK;
+}
+
+extern "C" int hype_mp2d_download(hype_mp2d* m, double* U_aos) {
+    if (!m || !U_aos) return HYPE_ERR_ARG;
+    int rc = mp_d2h(m, m->U, U_aos);
+    if (rc) return rc;
+    HYPE_CK(cudaStreamSynchronize(m->stream));
+    return HYPE_OK;
+}
+
+extern "C" void* hype_mp2d_stream(hype_mp2d* m) { return m ? (void*)m->stream : nullptr; }
+
+extern "C" int hype_mp2d_step(hype_mp2d* m, int nsteps, double* t_inout, double* dt_inout, long long* fallback_cells) {
+    if (!m || nsteps < 0 || !t_inout || !dt_inout) return HYPE_ERR_ARG;
+    const int mode = m->p.dt_mode;
+    if (mode == HYPE_DT_FIXED && !(*dt_inout > 0)) return HYPE_ERR_ARG;
+    const double cfl_h = m->p.cfl * m->p.h;
+    DevScalars init;
+    memset(&init, 0, sizeof(init));
+    init.t = *t_inout;
+    init.dt = *dt_inout;
+    init.bad = ~0ull;
+    HYPE_CK(cudaMemcpyAsync(m->ds, &init, sizeof(init), cudaMemcpyHostToDevice, m->stream));
+    const bool first_from_rhs = (mode != HYPE_DT_FIXED) && !(*dt_inout > 0);
+    const int last = m->p.stepper == HYPE_STEP_SSPRK43 ? 3 : 9;
+    int rc;
+    for (int s = 0; s < nsteps; ++s) {
+        if (s == 0 && first_from_rhs) {
+            if ((rc = mp_rhs(m, m->U, 0))) return rc;
+            k_mp_begin<<<1, 1, 0, m->stream>>>(m->ds, mode, 0, 1, 0, cfl_h);
+        } else {
+            k_mp_begin<<<1, 1, 0, m->stream>>>(m->ds, mode, last, mode == HYPE_DT_MONITOR && s > 0, 1, cfl_h);
+            HYPE_LAUNCHED(1);
+            if ((rc = mp_rhs(m, m->U, 0))) return rc;
+        }
+        HYPE_LAUNCHED(1);
+        if (m->p.stepper == HYPE_STEP_SSPRK43) {
+            // SSPRK(4,3): u1 = u + dt/2 L(u); u2 = u1 + dt/2 L(u1); u3 = 2/3 u + 1/3 u2 + dt/6 L(u2); u4 = u3 + dt/2 L(u3)
+            if ((rc = mp_update(m, m->U, m->U, nullptr, m->W0, Stage{1.0, 0.0, 0.5, 0}))) return rc;
+            if ((rc = mp_rhs(m, m->W0, 1)) || (rc = mp_update(m, m->W0, m->W0, nullptr, m->W0, Stage{1.0, 0.0, 0.5, 0}))) return rc;
+            if ((rc = mp_rhs(m, m->W0, 2)) || (rc = mp_update(m, m->W0, m->U, m->W0, m->W0, Stage{2.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 0})))
+                return rc;
+            if ((rc = mp_rhs(m, m->W0, 3)) || (rc = mp_update(m, m->W0, m->W0, nullptr, m->U, Stage{1.0, 0.0, 0.5, 0}))) return rc;
+        } else {
+            // SSPRK(10,4) low-storage (Ketcheson 2008): five dt/6 stages, q2 = 9/25 q1 + 1/25 u,
+            // q1 = 15 q2 - 5 q1, four dt/6 stages, u = 3/5 q1 + q2 + dt/10 L(q1)
+            const long long n = m->g.N * m->g.nv;
+            if ((rc = mp_update(m, m->U, m->U, nullptr, m->W0, Stage{1.0, 0.0, 1.0 / 6.0, 0}))) return rc;
+            for (int k = 1; k < 5; ++k)
+                if ((rc = mp_rhs(m, m->W0, k)) || (rc = mp_update(m, m->W0, m->W0, nullptr, m->W0, Stage{1.0, 0.0, 1.0 / 6.0, 0})))
+                    return rc;
+            k_mp_axpby<<<cdiv(n, 256), 256, 0, m->stream>>>(m->W0, m->U, m->W1, 9.0 / 25, 1.0 / 25, n);
+            k_mp_axpby<<<cdiv(n, 256), 256, 0, m->stream>>>(m->W1, m->W0, m->W0, 15.0, -5.0, n);
+            HYPE_LAUNCHED(2);
+            for (int k = 5; k < 9; ++k)
+                if ((rc = mp_rhs(m, m->W0, k)) || (rc = mp_update(m, m->W0, m->W0, nullptr, m->W0, Stage{1.0, 0.0, 1.0 / 6.0, 0})))
+                    return rc;
+            if ((rc = mp_rhs(m, m->W0, 9)) || (rc = mp_update(m, m->W0, m->W0, m->W1, m->U, Stage{3.0 / 5.0, 1.0, 1.0 / 10.0, 0})))
+                return rc;
+        }
+    }
+    if ((rc = mp_scalars(m))) return rc;
+    *t_inout = m->hs->t;
+    const double sl = bits2d(m->hs->smax_bits[last]);
+    *dt_inout = (nsteps > 0 && mode == HYPE_DT_MONITOR) ? cfl_h / (2.0 * sl) : m->hs->dt;
+    if (fallback_cells) *fallback_cells = (long long)m->hs->fallback;
+    return m->hs->bad == ~0ull ? HYPE_OK : HYPE_ERR_STATE;
+}
+
+extern "C" int hype_mp2d_sync(hype_mp2d* m) {
+    if (!m) return HYPE_ERR_ARG;
+    HYPE_CK(cudaStreamSynchronize(m->stream));
+    return HYPE_OK;
+}

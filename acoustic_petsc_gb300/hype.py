@@ -46,6 +46,7 @@ class AppCtx:
     recon: int = L.RECON_CWENO4
     precision: int = L.PREC_FP64
     dt_mode: int = L.DT_MONITOR
+    flux: int = L.FLUX_RUSANOV
     dt: float = 0.0  # the reference's Ctx->dt output of RHSFunction
 
     def params(self) -> L.EulerParams:
@@ -55,7 +56,7 @@ class AppCtx:
         p.cfl, p.gamma = self.CFL, self.gamma
         for q in range(6):
             p.bc[q] = int(self.boundaries[q])
-        p.recon, p.precision, p.dt_mode = self.recon, self.precision, self.dt_mode
+        p.recon, p.precision, p.dt_mode, p.flux = self.recon, self.precision, self.dt_mode, self.flux
         return p
 
 
@@ -251,3 +252,70 @@ class BatchLeapfrog:
 
     def sync(self):
         check(L.lib().hype_batch_sync(self._h), "hype_batch_sync")
+
+
+class Multiphase2D:
+    """2D multiphase RHS + SSP stepper: the 4-equation diffuse-interface model of
+    2d/weno4/bubble (model=MP_DI4) or the Kapila five-equation model (MP_KAPILA5)."""
+
+    def __init__(self, nx, ny, h, x_min=0.0, y_min=0.0, CFL=0.9, boundaries=(L.BC_TRANSMISSIVE,) * 4,
+                 model=L.MP_DI4, eos=(4.4, 6000.0, 1.4, 0.0), stepper=L.STEP_SSPRK43, precision=L.PREC_FP64,
+                 dt_mode=L.DT_MONITOR):
+        p = L.Mp2dParams()
+        p.nx, p.ny, p.x_min, p.y_min, p.h, p.cfl = nx, ny, x_min, y_min, h, CFL
+        for q in range(4):
+            p.bc[q] = int(boundaries[q])
+        p.model = model
+        p.g1, p.p1, p.g2, p.p2 = eos
+        p.stepper, p.precision, p.dt_mode = stepper, precision, dt_mode
+        self.nv = 5 if model == L.MP_DI4 else 6
+        self.shape = (ny, nx, self.nv)
+        self.dt = 0.0
+        self.t = 0.0
+        self.next_dt = 0.0
+        self.fallback_cells = 0
+        self._h = C.c_void_p()
+        check(L.lib().hype_mp2d_create(C.byref(p), C.byref(self._h)), "hype_mp2d_create")
+
+    def close(self):
+        if self._h:
+            L.lib().hype_mp2d_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def RHSFunction(self, t, U, RHS=None):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        if U.shape != self.shape:
+            raise ValueError(f"U must have shape {self.shape}")
+        if RHS is None:
+            RHS = np.empty_like(U)
+        dt = C.c_double()
+        rc = L.lib().hype_mp2d_rhs(self._h, t, _dp(U), _dp(RHS), C.byref(dt))
+        self.dt = dt.value
+        check(rc, "RHSFunction")
+        return RHS
+
+    def set_state(self, U):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        check(L.lib().hype_mp2d_upload(self._h, _dp(U)), "hype_mp2d_upload")
+
+    def get_state(self):
+        U = np.empty(self.shape)
+        check(L.lib().hype_mp2d_download(self._h, _dp(U)), "hype_mp2d_download")
+        return U
+
+    def step(self, nsteps, dt=None):
+        t = C.c_double(self.t)
+        d = C.c_double(self.next_dt if dt is None else dt)
+        fb = C.c_longlong(0)
+        rc = L.lib().hype_mp2d_step(self._h, int(nsteps), C.byref(t), C.byref(d), C.byref(fb))
+        self.t, self.next_dt, self.fallback_cells = t.value, d.value, fb.value
+        check(rc, "hype_mp2d_step")
+
+    def sync(self):
+        check(L.lib().hype_mp2d_sync(self._h), "hype_mp2d_sync")

@@ -85,3 +85,63 @@ def monopole_batch(ninst: int = 256, seed: int = 7, nmin: int = 64, nmax: int = 
         out.append(dict(nx=n, ny=n, xmin=-1.0, ymin=-1.0, h=h, c0=c, dt=cfl * h / c, xs=float(xs), ys=float(ys),
                         sigma=float(sigma), freq=c / (ppw * h)))
     return out
+
+
+def _prim2cons_mp(model: int, eos, V: np.ndarray) -> np.ndarray:
+    """vectorised conserved state of the 2D multiphase models (same formulas as the library)"""
+    g1, p1, g2, p2 = eos
+    Q = np.empty_like(V)
+    if model == 0:  # DI4: V = rho, u, v, p, phi
+        phi = V[..., 4]
+        g = 1.0 + (g1 - 1.0) * (g2 - 1.0) / ((1.0 - phi) * (g1 - 1.0) + phi * (g2 - 1.0))
+        pinf = ((g - 1.0) / g) * (g1 * p1 * phi / (g1 - 1.0) + g2 * p2 * (1.0 - phi) / (g2 - 1.0))
+        Q[..., 0] = V[..., 0]
+        Q[..., 1] = V[..., 0] * V[..., 1]
+        Q[..., 2] = V[..., 0] * V[..., 2]
+        Q[..., 3] = 0.5 * V[..., 0] * (V[..., 1] ** 2 + V[..., 2] ** 2) + (V[..., 3] + g * pinf) / (g - 1.0)
+        Q[..., 4] = phi
+        return Q
+    a1 = V[..., 5]
+    a2 = 1.0 - a1
+    g = 1.0 + ((g1 - 1.0) * (g2 - 1.0)) / ((g2 - 1.0) * a1 + (g1 - 1.0) * a2)
+    pi = ((g - 1.0) / g) * (g1 * p1 * a1 / (g1 - 1.0) + g2 * p2 * a2 / (g2 - 1.0))
+    rho = a1 * V[..., 0] + a2 * V[..., 1]
+    Q[..., 0] = a1 * V[..., 0]
+    Q[..., 1] = a2 * V[..., 1]
+    Q[..., 2] = rho * V[..., 2]
+    Q[..., 3] = rho * V[..., 3]
+    Q[..., 4] = (V[..., 4] + g * pi) / (g - 1.0) + 0.5 * rho * (V[..., 2] ** 2 + V[..., 3] ** 2)
+    Q[..., 5] = a1
+    return Q
+
+
+# water (phase 1) and air (phase 2) as stiffened gases, SI units
+KAPILA_EOS = (4.4, 6.0e8, 1.4, 0.0)
+
+
+def kapila_bubble(n: int = 1024, model: int = 1, smear: float = 2.0, eps: float = 1e-6):
+    """Shock-driven air-bubble collapse on [0,1]^2 m: air bubble r = 0.1 at the centre
+    (air fraction 1-eps inside, eps outside, tanh-smoothed over `smear` cells), water
+    1000 kg/m^3 at 1e5 Pa, air 1 kg/m^3, pressure 1e8 Pa for x < 0.2 (same smoothing).
+    Phase 1 = water (gamma 4.4, p_inf 6e8 Pa), phase 2 = air (1.4, 0).  Cell-centre
+    values; AoS [j][i][nv] (model 1: Kapila five-equation, model 0: diffuse interface)."""
+    h = 1.0 / n
+    x = (np.arange(n) + 0.5) * h
+    X, Y = np.meshgrid(x, x)
+    r = np.sqrt((X - 0.5) ** 2 + (Y - 0.5) ** 2)
+    t_b = 0.5 * (1.0 + np.tanh((r - 0.1) / (smear * h)))  # 0 inside the bubble, 1 outside
+    a_water = eps + (1.0 - 2.0 * eps) * t_b
+    t_p = 0.5 * (1.0 - np.tanh((X - 0.2) / (smear * h)))  # 1 for x < 0.2
+    p = 1.0e5 + (1.0e8 - 1.0e5) * t_p
+    if model == 1:
+        V = np.zeros((n, n, 6))
+        V[..., 0] = 1000.0
+        V[..., 1] = 1.0
+        V[..., 4] = p
+        V[..., 5] = a_water
+    else:
+        V = np.zeros((n, n, 5))
+        V[..., 0] = a_water * 1000.0 + (1.0 - a_water) * 1.0
+        V[..., 3] = p
+        V[..., 4] = a_water
+    return _prim2cons_mp(model, KAPILA_EOS, V), h

@@ -199,7 +199,7 @@ def cpu_ctcs_rate(n: int, steps: int):
 
 
 # ------------------------------------------------------------------ GPU workloads
-def run_euler(args, ws, rank, local, precision=0, recon=0, n=256):
+def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0):
     import torch
 
     import acoustic_petsc_gb300 as H
@@ -209,7 +209,7 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256):
     H._lib.check(L.hype_set_device(local), "hype_set_device")
     torch.cuda.set_device(local)
     U0 = workloads.euler_pulse(n)
-    ctx = H.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, precision=precision, recon=recon)
+    ctx = H.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, precision=precision, recon=recon, flux=flux)
     s = H.EulerSolver(ctx)
     s.set_state(U0)
     s.step(max(args.warmup, 3))
@@ -378,7 +378,56 @@ def run_batch(args, ws, rank, local, ninst=256):
             "gpu_launches": launches, "clocks": clk.summary()}
 
 
+def run_mp2d(args, ws, rank, local, n=1024, precision=0, model=1):
+    import torch
+
+    import acoustic_petsc_gb300 as H
+    from acoustic_petsc_gb300 import workloads
+
+    L = H.lib()
+    H._lib.check(L.hype_set_device(local), "hype_set_device")
+    torch.cuda.set_device(local)
+    U0, h = workloads.kapila_bubble(n, model=model)
+    m = H.Multiphase2D(n, n, h, CFL=0.4, boundaries=(2, 2, 2, 2), model=model, eos=workloads.KAPILA_EOS,
+                       stepper=H._lib.STEP_SSPRK43, precision=precision)
+    m.set_state(U0)
+    m.step(max(args.warmup, 3))
+    stream = torch.cuda.ExternalStream(L.hype_mp2d_stream(m._h))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = H.launches()
+    _barrier(ws)
+    torch.cuda.synchronize()
+    with Clocks(_gpu_index(local)) as clk:
+        e0.record(stream)
+        m.step(args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    launches = H.launches() - l0
+    ms = _max_over_ranks(ws, e0.elapsed_time(e1))
+    nv = 6 if model == 1 else 5
+    bytes_cu = 4 * (2 * 8 * nv) + 8 * nv  # SSPRK(4,3): 4 stages read+write the state, one extra read of u^n
+    cells = n * n
+    value = ws * cells * args.steps / (ms * 1e-3)
+    peak, kind = _peaks()
+    ach = bytes_cu * cells * args.steps / (ms * 1e-3) / 1e9
+    fb = m.fallback_cells
+    m.close()
+    return {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if precision == 0 else "f64 state / f32 recon+flux",
+            "data": "synthetic: shock-driven air bubble in water (1e8 Pa step at x<0.2)",
+            "config": {"workload": f"kapila5_2d_{n}" if model == 1 else f"diffuse_interface_2d_{n}", "grid": [n, n],
+                       "eos": "water gamma 4.4 p_inf 6e8 Pa / air gamma 1.4", "flux": "rotated HLLC",
+                       "time": "SSPRK(4,3)", "cfl": 0.4, "fallback_cells_in_run": fb},
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "traffic": None, "algorithmic_bytes_per_cell_update": bytes_cu},
+            "gpu_launches": launches, "clocks": clk.summary()}
+
+
 WORKLOADS = {
+    "kapila1024": lambda a, *r: run_mp2d(a, *r, precision=0),
+    "kapila1024_fp32": lambda a, *r: run_mp2d(a, *r, precision=1),
+    "euler256_hllc": lambda a, *r: run_euler(a, *r, precision=0, recon=0, flux=1),
     "euler256": lambda a, *r: run_euler(a, *r, precision=0, recon=0),
     "euler256_fp32": lambda a, *r: run_euler(a, *r, precision=1, recon=0),
     "euler256_linear": lambda a, *r: run_euler(a, *r, precision=0, recon=1),
@@ -435,7 +484,22 @@ def main():
         return
     out = WORKLOADS[args.workload](args, ws, rank, local)
     if rank == 0 and not args.no_cpu_baseline:
-        if args.workload.startswith("euler"):
+        if args.workload.startswith("kapila"):
+            from acoustic_petsc_gb300 import workloads
+            from oracle import pyoracle as O
+
+            O.build(None)
+            n = 256
+            U0, h = workloads.kapila_bubble(n)
+            cfg = O.mp2d_cfg(n, n, h, cfl=0.4, bc=(2, 2, 2, 2), model=1, eos=workloads.KAPILA_EOS,
+                             nthreads=os.cpu_count() or 1)
+            O.mp2d_run(cfg, U0, 1)
+            t0 = time.perf_counter()
+            O.mp2d_run(cfg, U0, 4)
+            d = time.perf_counter() - t0
+            out["cpu_baseline"] = {"value": n * n * 4 / d, "unit": "cell-updates/s", "cores": O.threads(),
+                                   "kind": "port", "sample": f"4 SSPRK(4,3) steps of the {n}^2 version ({d:.1f} s)"}
+        elif args.workload.startswith("euler"):
             n = 96 if args.workload != "euler64" else 48
             r, cores, kind, d = cpu_euler_rate(n, 2, use_ref=False)
             out["cpu_baseline"] = {"value": r, "unit": "cell-updates/s", "cores": cores, "kind": kind,

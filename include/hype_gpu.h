@@ -47,6 +47,11 @@ extern "C" {
                                 (3d/weno4/Viscous-Multiphase-Fourth-Order/reconstruction.c:38-259) */
 #define HYPE_RECON_LINEAR4 1 /* the optimal-weight limit: the 4th-order central polynomial R4 */
 
+/* numerical flux across each face Gauss point (3d/weno4/Navier-Stokes-3D/pde.c) */
+#define HYPE_FLUX_RUSANOV 0  /* PDELLFRiemannSolver, pde.c:164-187 */
+#define HYPE_FLUX_HLLC 1     /* PDEHLLCRiemannSolver, pde.c:207-322 */
+#define HYPE_FLUX_ROTHLLC 2  /* PDErotHLLCRiemannSolver, pde.c:324-384 */
+
 /* arithmetic of reconstruction + flux (the state and the RK accumulation are always FP64) */
 #define HYPE_PREC_FP64 0
 #define HYPE_PREC_FP32 1
@@ -69,6 +74,7 @@ typedef struct {
     int recon;                     /* HYPE_RECON_* */
     int precision;                 /* HYPE_PREC_* */
     int dt_mode;                   /* HYPE_DT_* */
+    int flux;                      /* HYPE_FLUX_* (0 = Rusanov) */
 } hype_euler_params;
 
 typedef struct {
@@ -143,6 +149,43 @@ int hype_euler_profile_read(hype_euler* e, double* ms, long long* count);
  *     returns without waiting. */
 int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* dU, double* dRHS, double* dt_out, void* stream);
 long long hype_euler_noalloc_max_ext(void);
+
+/* ============================================================ 2D multiphase */
+/* models */
+#define HYPE_MP_DI4 0     /* 4-equation diffuse interface, Q = (rho, rho u, rho v, E, phi)
+                             (2d/weno4/bubble: pde.c, rhs_function.c) */
+#define HYPE_MP_KAPILA5 1 /* Kapila five-equation, Q = (a1 rho1, a2 rho2, rho u, rho v, E, a1)
+                             (mixture EOS of 2d/HyPE-2D/kapila_5eqn.c:14-113) */
+/* steppers */
+#define HYPE_STEP_SSPRK43 0  /* TSSSP RKS3, 4 stages */
+#define HYPE_STEP_SSPRK104 1 /* TSSSP RK104 (2d/weno4/bubble/hype.c:209-210) */
+
+typedef struct hype_mp2d hype_mp2d;
+
+typedef struct {
+    int nx, ny;                 /* cells */
+    double x_min, y_min, h, cfl;
+    int bc[4];                  /* left, right, bottom, top: HYPE_BC_PERIODIC/REFLECTIVE/TRANSMISSIVE */
+    int model;                  /* HYPE_MP_* */
+    double g1, p1, g2, p2;      /* stiffened-gas phases: ratio of specific heats, stiffness */
+    int stepper;                /* HYPE_STEP_* */
+    int precision;              /* HYPE_PREC_*: FP32 = reconstruction + flux in FP32, EOS and state in FP64 */
+    int dt_mode;                /* HYPE_DT_* (dt = CFL h / (2 s_max), 2d/weno4/bubble/rhs_function.c:385) */
+} hype_mp2d_params;
+
+int hype_mp2d_create(const hype_mp2d_params* p, hype_mp2d** out);
+void hype_mp2d_destroy(hype_mp2d* m);
+/* Drop-in for the 2D RHSFunction (2d/weno4/bubble/rhs_function.c:12): primitive
+ * CWENO4 with the 8-node admissibility check and minmod fallback, rotated HLLC,
+ * divergence with the non-conservative volume-fraction term; host AoS [j][i][nv]. */
+int hype_mp2d_rhs(hype_mp2d* m, double t, const double* U_aos, double* RHS_aos, double* dt_out);
+int hype_mp2d_upload(hype_mp2d* m, const double* U_aos);
+int hype_mp2d_download(hype_mp2d* m, double* U_aos);
+/* nsteps of the chosen SSP stepper on the resident state; *fallback_cells gets the
+ * number of owned-cell reconstructions that fell back to minmod (PAD violations). */
+int hype_mp2d_step(hype_mp2d* m, int nsteps, double* t_inout, double* dt_inout, long long* fallback_cells);
+int hype_mp2d_sync(hype_mp2d* m);
+void* hype_mp2d_stream(hype_mp2d* m);
 
 /* ============================================================ CTCS acoustics */
 /* Drop-in for CTCS(DM, Vec Pold, Vec Pcurr, Vec Pnew, AppCtx*)

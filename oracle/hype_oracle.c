@@ -433,6 +433,158 @@ double orc_rusanov(const double* QL, const double* QR, int dir, double gamma, do
     return s;
 }
 
+/* ============================================================ HLLC (3D, general normal) */
+
+/* PDEConsFlux with a general unit normal (Navier-Stokes-3D/pde.c:40-88) */
+static double cons_flux_n(const double* Q, double nx, double ny, double nz, double gamma, double* F, int* bad) {
+    const double rho = Q[0];
+    const double r1_rho = 1.0 / rho;
+    const double u = r1_rho * Q[1], v = r1_rho * Q[2], w = r1_rho * Q[3];
+    const double E = Q[4];
+    const double p = (gamma - 1.0) * (E - 0.5 * rho * (u * u + v * v + w * w));
+    if (rho < 1.0e-14 || p < 1.0e-12) *bad = 1;
+    F[0] = nx * rho * u + ny * rho * v + nz * rho * w;
+    F[1] = nx * (rho * u * u + p) + ny * rho * u * v + nz * rho * u * w;
+    F[2] = nx * rho * u * v + ny * (rho * v * v + p) + nz * rho * v * w;
+    F[3] = nx * rho * u * w + ny * rho * v * w + nz * (rho * w * w + p);
+    F[4] = (E + p) * (nx * u + ny * v + nz * w);
+    const double a = sqrt(r1_rho * gamma * p);
+    return fabs(u * nx + v * ny + w * nz) + a;
+}
+
+/* PDECons2Prim (pde.c:9-18) */
+static void cons2prim(const double* Q, double gamma, double* V) {
+    const double r1_rho = 1.0 / Q[0];
+    V[0] = Q[0];
+    V[1] = r1_rho * Q[1];
+    V[2] = r1_rho * Q[2];
+    V[3] = r1_rho * Q[3];
+    V[4] = (gamma - 1.0) * (Q[4] - 0.5 * r1_rho * ((Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3])));
+}
+
+/* 3x3 inverse by cofactors (pde.c:189-205) */
+static void inv3(const double M[3][3], double iM[3][3]) {
+    const double t4 = M[0][0] * M[1][1], t6 = M[0][0] * M[1][2], t8 = M[0][1] * M[1][0], t00 = M[0][2] * M[1][0],
+                 t01 = M[0][1] * M[2][0], t04 = M[0][2] * M[2][0],
+                 t07 = 1.0 / (t4 * M[2][2] - t6 * M[2][1] - t8 * M[2][2] + t00 * M[2][1] + t01 * M[1][2] - t04 * M[1][1]);
+    iM[0][0] = (M[1][1] * M[2][2] - M[1][2] * M[2][1]) * t07;
+    iM[0][1] = -(M[0][1] * M[2][2] - M[0][2] * M[2][1]) * t07;
+    iM[0][2] = -(-M[0][1] * M[1][2] + M[0][2] * M[1][1]) * t07;
+    iM[1][0] = -(M[1][0] * M[2][2] - M[1][2] * M[2][0]) * t07;
+    iM[1][1] = (M[0][0] * M[2][2] - t04) * t07;
+    iM[1][2] = -(t6 - t00) * t07;
+    iM[2][0] = -(-M[1][0] * M[2][1] + M[1][1] * M[2][0]) * t07;
+    iM[2][1] = -(M[0][0] * M[2][1] - t01) * t07;
+    iM[2][2] = (t4 - t8) * t07;
+}
+
+/* Miller-Colella tangents of a unit normal; 'fixed' selects the corrected t2z
+ * of the rotated solver (pde.c:348) instead of the HLLC one (pde.c:238) */
+static void tangents(double nx, double ny, double nz, int fixed, double* t1, double* t2) {
+    double L;
+    if (fabs(ny + nz) > fabs(ny - nz)) {
+        L = sqrt(2.0 * (1.0 + nz * (ny - nx) + nx * ny));
+        t1[0] = (ny + nz) / L; t1[1] = (nz - nx) / L; t1[2] = -(nx + ny) / L;
+        t2[0] = (nx * (nz - ny) - ny * ny - nz * nz) / L;
+        t2[1] = (ny * (nx + nz) + nx * nx + nz * nz) / L;
+        t2[2] = fixed ? (nz * (nx - ny) - nx * nx - ny * ny) / L : (nz * (nx - nz) - nx * nx - ny * ny) / L;
+    } else {
+        L = sqrt(2.0 * (1.0 - nx * ny - nx * nz - ny * nz));
+        t1[0] = (ny - nz) / L; t1[1] = (nz - nx) / L; t1[2] = (nx - ny) / L;
+        t2[0] = (nx * (ny + nz) - ny * ny - nz * nz) / L;
+        t2[1] = (ny * (nx + nz) - nx * nx - nz * nz) / L;
+        t2[2] = (nz * (nx + ny) - nx * nx - ny * ny) / L;
+    }
+}
+
+/* PDEHLLCRiemannSolver (pde.c:207-322) */
+double orc_hllc(const double* QL, const double* QR, double nx, double ny, double nz, double gamma, double* Flux, int* bad) {
+    double FL[5], FR[5], VL[5], VR[5], t1[3], t2[3], M[3][3], iM[3][3];
+    double sl = cons_flux_n(QL, nx, ny, nz, gamma, FL, bad);
+    double sr = cons_flux_n(QR, nx, ny, nz, gamma, FR, bad);
+    double smax = (sl < sr) ? sr : sl;
+    cons2prim(QL, gamma, VL);
+    cons2prim(QR, gamma, VR);
+    const double rL = VL[0], uL = VL[1], vL = VL[2], wL = VL[3], PL = VL[4];
+    const double rR = VR[0], uR = VR[1], vR = VR[2], wR = VR[3], PR = VR[4];
+    tangents(nx, ny, nz, 0, t1, t2);
+    M[0][0] = nx; M[0][1] = ny; M[0][2] = nz;
+    M[1][0] = t1[0]; M[1][1] = t1[1]; M[1][2] = t1[2];
+    M[2][0] = t2[0]; M[2][1] = t2[1]; M[2][2] = t2[2];
+    inv3(M, iM);
+    const double unL = uL * nx + vL * ny + wL * nz, ut1L = uL * t1[0] + vL * t1[1] + wL * t1[2], ut2L = uL * t2[0] + vL * t2[1] + wL * t2[2];
+    const double unR = uR * nx + vR * ny + wR * nz, ut1R = uR * t1[0] + vR * t1[1] + wR * t1[2], ut2R = uR * t2[0] + vR * t2[1] + wR * t2[2];
+    const double cL = sqrt(gamma * PL / rL), cR = sqrt(gamma * PR / rR);
+    const double EL = QL[4], ER = QR[4];
+    const double a1 = unR - cR, b1 = unL - cL;
+    const double SL = (a1 < b1) ? a1 : b1;
+    const double a2 = unL + cL, b2 = unR + cR;
+    const double SR = (a2 < b2) ? b2 : a2;
+    const double Ss = (PR - PL + rL * unL * (SL - unL) - rR * unR * (SR - unR)) / (rL * (SL - unL) - rR * (SR - unR));
+    double QLs[5], QRs[5];
+    QLs[0] = rL * (SL - unL) / (SL - Ss);
+    QLs[1] = QLs[0] * (Ss * iM[0][0] + ut1L * iM[0][1] + ut2L * iM[0][2]);
+    QLs[2] = QLs[0] * (Ss * iM[1][0] + ut1L * iM[1][1] + ut2L * iM[1][2]);
+    QLs[3] = QLs[0] * (Ss * iM[2][0] + ut1L * iM[2][1] + ut2L * iM[2][2]);
+    QLs[4] = QLs[0] * ((EL / rL) + (Ss - unL) * (Ss + PL / (rL * (SL - unL))));
+    QRs[0] = rR * (SR - unR) / (SR - Ss);
+    QRs[1] = QRs[0] * (Ss * iM[0][0] + ut1R * iM[0][1] + ut2R * iM[0][2]);
+    QRs[2] = QRs[0] * (Ss * iM[1][0] + ut1R * iM[1][1] + ut2R * iM[1][2]);
+    QRs[3] = QRs[0] * (Ss * iM[2][0] + ut1R * iM[2][1] + ut2R * iM[2][2]);
+    QRs[4] = QRs[0] * ((ER / rR) + (Ss - unR) * (Ss + PR / (rR * (SR - unR))));
+    for (int c = 0; c < 5; ++c) {
+        const double FLs = FL[c] + SL * (QLs[c] - QL[c]);
+        const double FRs = FR[c] + SR * (QRs[c] - QR[c]);
+        /* the reference leaves the flux unset when S_L == 0 and S* >= 0; the
+         * (continuous) star state is taken there */
+        if (SL > 0.0) Flux[c] = FL[c];
+        else if (Ss >= 0.0) Flux[c] = FLs;
+        else if (SR >= 0.0) Flux[c] = FRs;
+        else Flux[c] = FR[c];
+    }
+    return smax;
+}
+
+/* PDErotHLLCRiemannSolver (pde.c:324-384) */
+double orc_rothllc(const double* QL, const double* QR, double nx, double ny, double nz, double gamma, double* Flux, int* bad) {
+    double irho = 1.0 / QL[0];
+    const double uL = irho * QL[1], vL = irho * QL[2], wL = irho * QL[3];
+    irho = 1.0 / QR[0];
+    const double uR = irho * QR[1], vR = irho * QR[2], wR = irho * QR[3];
+    const double du = uR - uL, dv = vR - vL, dw = wR - wL;
+    const double dq = sqrt(du * du + dv * dv + dw * dw);
+    double n1[3];
+    if (dq < 1.0E-10) {
+        n1[0] = nx; n1[1] = ny; n1[2] = nz;
+    } else {
+        n1[0] = du / dq; n1[1] = dv / dq; n1[2] = dw / dq;
+    }
+    double a1 = (n1[0] * nx + n1[1] * ny + n1[2] * nz);
+    if (a1 < 0.0) {
+        n1[0] = -n1[0]; n1[1] = -n1[1]; n1[2] = -n1[2];
+        a1 = -a1;
+    }
+    double t1[3], t2[3];
+    tangents(n1[0], n1[1], n1[2], 1, t1, t2);
+    double a2 = (t1[0] * nx + t1[1] * ny + t1[2] * nz);
+    if (a2 < 0) {
+        t1[0] = -t1[0]; t1[1] = -t1[1]; t1[2] = -t1[2];
+        a2 = -a2;
+    }
+    double a3 = (t2[0] * nx + t2[1] * ny + t2[2] * nz);
+    if (a3 < 0) {
+        t2[0] = -t2[0]; t2[1] = -t2[1]; t2[2] = -t2[2];
+        a3 = -a3;
+    }
+    double F1[5], F2[5], F3[5];
+    double s1 = orc_hllc(QL, QR, n1[0], n1[1], n1[2], gamma, F1, bad);
+    double s2 = orc_hllc(QL, QR, t1[0], t1[1], t1[2], gamma, F2, bad);
+    double s3 = orc_hllc(QL, QR, t2[0], t2[1], t2[2], gamma, F3, bad);
+    for (int c = 0; c < 5; ++c) Flux[c] = a1 * F1[c] + a2 * F2[c] + a3 * F3[c];
+    double m23 = (s2 < s3) ? s3 : s2;
+    return (s1 < m23) ? m23 : s1;
+}
+
 /* ============================================================ Euler RHS */
 
 #define NV 5
@@ -536,6 +688,8 @@ static void cell_traces(const Padded* P, int i, int j, int k, double gam, int li
 }
 
 /* face flux from the left cell's trace set (face fl) and the right cell's (face fr) */
+static int g_flux_kind = 0; /* set per RHS call: 0 Rusanov, 1 HLLC, 2 rotated HLLC */
+
 static inline double face_flux(const double* trL, int fl, const double* trR, int fr, int dir, double gamma, double* F, int* bad) {
     double smax = 0.0;
     for (int c = 0; c < NV; ++c) F[c] = 0.0;
@@ -545,7 +699,14 @@ static inline double face_flux(const double* trL, int fl, const double* trR, int
             QL[c] = trL[c * NTR + fl * 4 + g];
             QR[c] = trR[c * NTR + fr * 4 + g];
         }
-        double s = orc_rusanov(QL, QR, dir, gamma, fl5, bad);
+        double s;
+        if (g_flux_kind == 0) {
+            s = orc_rusanov(QL, QR, dir, gamma, fl5, bad);
+        } else {
+            const double nx = dir == 0 ? 1.0 : 0.0, ny = dir == 1 ? 1.0 : 0.0, nz = dir == 2 ? 1.0 : 0.0;
+            s = (g_flux_kind == 1) ? orc_hllc(QL, QR, nx, ny, nz, gamma, fl5, bad)
+                                   : orc_rothllc(QL, QR, nx, ny, nz, gamma, fl5, bad);
+        }
         if (s > smax) smax = s;
         for (int c = 0; c < NV; ++c) F[c] += 0.25 * fl5[c];
     }
@@ -557,6 +718,7 @@ int orc_euler_rhs(const orc_euler_cfg* g, const double* U, double* RHS, double* 
     const double gam = 0.85;
     const int linear = g->recon == 1;
     const double r1_h = 1. / (g->h);
+    g_flux_kind = g->flux;
 #ifdef _OPENMP
     if (g->nthreads > 0) omp_set_num_threads(g->nthreads);
 #endif

@@ -56,6 +56,7 @@ typedef struct {
     int bc[6];
     int recon; /* 0 = CWENO4 (gamma 0.85), 1 = linear R4 (the optimal-weight polynomial) */
     int nthreads;
+    int flux;  /* 0 = Rusanov (LLF), 1 = HLLC, 2 = rotated HLLC (Navier-Stokes-3D/pde.c:164-384) */
 } orc_euler_cfg;
 int orc_euler_rhs(const orc_euler_cfg* cfg, const double* U, double* RHS, double* smax_out, long* bad);
 /* SSPRK(4,3) steps with dt semantics: dt_mode 0 -> dt refreshed each step from
@@ -69,9 +70,30 @@ void orc_cweno4_ref_args(const double* Ux, const double* Uy, const double* Uz, c
                          const double* Uzx, const double* Uxyz, double* coeffs);
 double orc_eval_poly3(double x, double y, double z, const double* coeffs);
 double orc_rusanov(const double* QL, const double* QR, int dir, double gamma, double* flux, int* bad);
+double orc_hllc(const double* QL, const double* QR, double nx, double ny, double nz, double gamma, double* flux, int* bad);
+double orc_rothllc(const double* QL, const double* QR, double nx, double ny, double nz, double gamma, double* flux, int* bad);
 
-/* flop tally of one Euler RHS evaluation per interior cell (counted by the
- * instrumented build of the same arithmetic); -1 when not available */
+/* 2D multiphase RHS: model 0 = 4-equation diffuse interface (2d/weno4/bubble),
+ * model 1 = Kapila five-equation (2d/HyPE-2D/kapila_5eqn.c) with the same
+ * machinery.  AoS [j][i][nv], nv = 5 or 6; bc[4] = left,right,bottom,top;
+ * EOS: phase 1 (g1, p1), phase 2 (g2, p2). */
+typedef struct {
+    int nx, ny;
+    double xmin, ymin, h, cfl;
+    int bc[4];
+    int model;
+    double g1, p1, g2, p2;
+    int nthreads;
+} orc_mp2d_cfg;
+int orc_mp2d_rhs(const orc_mp2d_cfg* g, const double* U, double* RHS, double* smax_out, long* bad_out, long* fallback_out);
+int orc_mp2d_run(const orc_mp2d_cfg* g, int nsteps, int stepper, int dt_mode, double* U, double* t_inout, double* dt_inout,
+                 long* bad);
+void orc_mp_cons2prim(int model, const double* eos4, const double* Q, double* V);
+void orc_mp_prim2cons(int model, const double* eos4, const double* V, double* Q);
+void orc_cweno4_2d(double u0, const double* ux, const double* uy, double upp, double upm, double ump, double umm,
+                   double* coeffs);
+
+/* OpenMP threads the restatement runs with */
 int orc_threads(void);
 
 #ifdef __cplusplus

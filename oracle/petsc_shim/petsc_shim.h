@@ -97,6 +97,8 @@ typedef enum { TS_LINEAR = 0, TS_NONLINEAR = 1 } TSProblemType;
 typedef enum { TS_EXACTFINALTIME_UNSPECIFIED = 0, TS_EXACTFINALTIME_STEPOVER = 1, TS_EXACTFINALTIME_INTERPOLATE = 2,
                TS_EXACTFINALTIME_MATCHSTEP = 3 } TSExactFinalTimeOption;
 
+typedef struct { PetscScalar x, y; } DMDACoor2d;
+typedef struct { PetscScalar x, y, z; } DMDACoor3d;
 typedef struct _p_DM* DM;
 typedef struct _p_Vec* Vec;
 typedef struct _p_TS* TS;

@@ -43,7 +43,7 @@ class EulerCfg(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
                 ("xmin", C.c_double), ("ymin", C.c_double), ("zmin", C.c_double),
                 ("h", C.c_double), ("cfl", C.c_double), ("gamma", C.c_double),
-                ("bc", C.c_int * 6), ("recon", C.c_int), ("nthreads", C.c_int)]
+                ("bc", C.c_int * 6), ("recon", C.c_int), ("nthreads", C.c_int), ("flux", C.c_int)]
 
 
 class CtcsCfg(C.Structure):
@@ -89,7 +89,7 @@ def threads() -> int:
     return lib().orc_threads()
 
 
-def euler_cfg(n, h, cfl=0.4, gamma=1.4, bc=(0,) * 6, origin=(0.0, 0.0, 0.0), recon=0, nthreads=0):
+def euler_cfg(n, h, cfl=0.4, gamma=1.4, bc=(0,) * 6, origin=(0.0, 0.0, 0.0), recon=0, nthreads=0, flux=0):
     nx, ny, nz = (n, n, n) if isinstance(n, int) else n
     c = EulerCfg()
     c.nx, c.ny, c.nz = nx, ny, nz
@@ -97,7 +97,7 @@ def euler_cfg(n, h, cfl=0.4, gamma=1.4, bc=(0,) * 6, origin=(0.0, 0.0, 0.0), rec
     c.h, c.cfl, c.gamma = h, cfl, gamma
     for q in range(6):
         c.bc[q] = bc[q]
-    c.recon, c.nthreads = recon, nthreads
+    c.recon, c.nthreads, c.flux = recon, nthreads, flux
     return c
 
 
@@ -153,21 +153,25 @@ def ref_available() -> bool:
     return os.path.exists(os.path.join(HERE, "_ref", "libref_euler.so"))
 
 
-def _ref_euler_lib():
+_REF_FLUX_LIB = {0: "libref_euler.so", 1: "libref_euler_hllc.so", 2: "libref_euler_rothllc.so"}
+_ref_euler_libs = {}
+
+
+def _ref_euler_lib(flux: int = 0):
     global _ref_euler
-    if _ref_euler is None:
-        L = C.CDLL(os.path.join(HERE, "_ref", "libref_euler.so"))
+    if flux not in _ref_euler_libs:
+        L = C.CDLL(os.path.join(HERE, "_ref", _REF_FLUX_LIB[flux]))
         IP = C.POINTER(C.c_int)
         L.ref_euler_rhs.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                     C.c_double, IP, D, D, D]
         L.ref_euler_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                     C.c_double, IP, C.c_int, C.c_int, D, D, D]
-        _ref_euler = L
-    return _ref_euler
+        _ref_euler_libs[flux] = L
+    return _ref_euler_libs[flux]
 
 
 def ref_euler_rhs(cfg: EulerCfg, U):
-    L = _ref_euler_lib()
+    L = _ref_euler_lib(cfg.flux)
     U = np.ascontiguousarray(U, dtype=np.float64)
     R = np.zeros_like(U)
     dt = C.c_double(0.0)
@@ -178,7 +182,7 @@ def ref_euler_rhs(cfg: EulerCfg, U):
 
 
 def ref_euler_run(cfg: EulerCfg, U, nsteps, dt_mode=0, dt=0.0):
-    L = _ref_euler_lib()
+    L = _ref_euler_lib(cfg.flux)
     U = np.array(U, dtype=np.float64, order="C", copy=True)
     t = C.c_double(0.0)
     d = C.c_double(dt)
@@ -210,3 +214,102 @@ def ref_point_source_trace() -> np.ndarray:
         subprocess.run([exe], cwd=d, check=True, stdout=subprocess.DEVNULL)
         with open(os.path.join(d, "results", "p.dat")) as f:
             return f.read()
+
+
+# ---------------------------------------------------------------- 2D multiphase
+class Mp2dCfg(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("xmin", C.c_double), ("ymin", C.c_double), ("h", C.c_double),
+                ("cfl", C.c_double), ("bc", C.c_int * 4), ("model", C.c_int), ("g1", C.c_double), ("p1", C.c_double),
+                ("g2", C.c_double), ("p2", C.c_double), ("nthreads", C.c_int)]
+
+
+# the reference bubble code's compiled-in EOS (2d/weno4/bubble/hype.h: g1, p1, g2, p2)
+BUBBLE_EOS = (4.4, 6000.0, 1.4, 0.0)
+
+
+def mp2d_cfg(nx, ny, h, xmin=0.0, ymin=0.0, cfl=0.9, bc=(2, 2, 2, 2), model=0, eos=BUBBLE_EOS, nthreads=0):
+    c = Mp2dCfg()
+    c.nx, c.ny, c.xmin, c.ymin, c.h, c.cfl = nx, ny, xmin, ymin, h, cfl
+    for q in range(4):
+        c.bc[q] = bc[q]
+    c.model = model
+    c.g1, c.p1, c.g2, c.p2 = eos
+    c.nthreads = nthreads
+    return c
+
+
+def _mp_lib():
+    L = lib()
+    if not getattr(L, "_mp_bound", False):
+        L.orc_mp2d_rhs.argtypes = [C.POINTER(Mp2dCfg), D, D, D, C.POINTER(C.c_long), C.POINTER(C.c_long)]
+        L.orc_mp2d_run.argtypes = [C.POINTER(Mp2dCfg), C.c_int, C.c_int, C.c_int, D, D, D, C.POINTER(C.c_long)]
+        L.orc_mp_prim2cons.argtypes = [C.c_int, D, D, D]
+        L.orc_mp_cons2prim.argtypes = [C.c_int, D, D, D]
+        L._mp_bound = True
+    return L
+
+
+def mp2d_rhs(cfg, U):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    smax = C.c_double()
+    bad = C.c_long(-1)
+    fb = C.c_long(0)
+    rc = _mp_lib().orc_mp2d_rhs(C.byref(cfg), _dp(U), _dp(R), C.byref(smax), C.byref(bad), C.byref(fb))
+    return R, smax.value, rc, fb.value
+
+
+def mp2d_run(cfg, U, nsteps, stepper=0, dt_mode=0, dt=0.0):
+    U = np.array(U, dtype=np.float64, order="C", copy=True)
+    t = C.c_double(0.0)
+    d = C.c_double(dt)
+    bad = C.c_long(-1)
+    rc = _mp_lib().orc_mp2d_run(C.byref(cfg), nsteps, stepper, dt_mode, _dp(U), C.byref(t), C.byref(d), C.byref(bad))
+    return U, t.value, d.value, rc
+
+
+def mp_prim2cons(model, eos, V):
+    """vectorised over the leading axes"""
+    V = np.ascontiguousarray(V, dtype=np.float64)
+    nv = V.shape[-1]
+    Q = np.empty_like(V)
+    e = np.array(eos, dtype=np.float64)
+    L = _mp_lib()
+    Vf, Qf = V.reshape(-1, nv), Q.reshape(-1, nv)
+    for q in range(Vf.shape[0]):
+        L.orc_mp_prim2cons(model, _dp(e), Vf[q].ctypes.data_as(D), Qf[q].ctypes.data_as(D))
+    return Q
+
+
+_ref_bub = None
+
+
+def _ref_bubble_lib():
+    global _ref_bub
+    if _ref_bub is None:
+        L = C.CDLL(os.path.join(HERE, "_ref", "libref_bubble.so"))
+        IP = C.POINTER(C.c_int)
+        L.ref_bubble_rhs.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, IP, D, D, D]
+        L.ref_bubble_run.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, IP, C.c_int, D, D,
+                                     D]
+        _ref_bub = L
+    return _ref_bub
+
+
+def ref_bubble_rhs(cfg, U):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    dt = C.c_double()
+    bc = (C.c_int * 4)(*cfg.bc)
+    rc = _ref_bubble_lib().ref_bubble_rhs(cfg.nx, cfg.ny, cfg.xmin, cfg.ymin, cfg.h, cfg.cfl, bc, _dp(U), _dp(R),
+                                          C.byref(dt))
+    return R, dt.value, rc
+
+
+def ref_bubble_run(cfg, U, nsteps):
+    U = np.array(U, dtype=np.float64, order="C", copy=True)
+    t, d = C.c_double(), C.c_double()
+    bc = (C.c_int * 4)(*cfg.bc)
+    rc = _ref_bubble_lib().ref_bubble_run(cfg.nx, cfg.ny, cfg.xmin, cfg.ymin, cfg.h, cfg.cfl, bc, nsteps, _dp(U),
+                                          C.byref(t), C.byref(d))
+    return U, t.value, d.value, rc

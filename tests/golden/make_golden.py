@@ -10,9 +10,14 @@ tree is available; the GPU machine has none, so the fixtures are committed).
                            (3d/weno4/Navier-Stokes-3D/rhs_function.c with the
                            CWENO4 weno() of Viscous-Multiphase-Fourth-Order,
                            viscous flux zero) compiled through oracle/petsc_shim,
-                           and of 3 SSP RKS3/4-stage steps of the same
+                           and of 3 SSP RKS3/4-stage steps of the same; the
+                           *_hllc / *_rothllc cases switch its Riemann solver to
+                           the reference's PDEHLLCRiemannSolver / PDErotHLLCRiemannSolver
 * ref_ctcs2d.npz        -- the reference's CTCS() (2d/ctcs/plane_wave/wave.c)
                            on a zero-exterior grid
+* ref_bubble_*.npz      -- the reference's 2D diffuse-interface RHSFunction
+                           (2d/weno4/bubble) and RK104 steps of it; "sharp" trips the
+                           admissibility fallback
 """
 import json
 import os
@@ -63,15 +68,18 @@ def main():
                                         [128, 1.94e-06, 1.74e-07]]
     with open(os.path.join(HERE, "accuracy_tables.json"), "w") as f:
         json.dump(tables, f, indent=1)
-    for name, n, seed, bc in CASES:
-        cfg = O.euler_cfg(n, 1.0 / n, cfl=0.4, bc=bc)
-        U = euler_case(n, seed, bc)
-        R, dt, rc = O.ref_euler_rhs(cfg, U)
-        assert rc == 0
-        U3, t3, dt3, rc3 = O.ref_euler_run(cfg, U, 3)
-        assert rc3 == 0
-        np.savez_compressed(os.path.join(HERE, f"ref_euler_{name}.npz"), U=U, RHS=R, dt=dt, U3=U3, t3=t3, dt3=dt3,
-                            bc=np.array(bc), n=n, cfl=0.4)
+    for flux, tag in ((0, ""), (1, "_hllc"), (2, "_rothllc")):
+        for name, n, seed, bc in CASES:
+            if flux and name == "mixed":
+                continue
+            cfg = O.euler_cfg(n, 1.0 / n, cfl=0.4, bc=bc, flux=flux)
+            U = euler_case(n, seed, bc, vel=0.05 if flux == 0 else 0.2)
+            R, dt, rc = O.ref_euler_rhs(cfg, U)
+            assert rc == 0
+            U3, t3, dt3, rc3 = O.ref_euler_run(cfg, U, 3)
+            assert rc3 == 0
+            np.savez_compressed(os.path.join(HERE, f"ref_euler_{name}{tag}.npz"), U=U, RHS=R, dt=dt, U3=U3, t3=t3,
+                                dt3=dt3, bc=np.array(bc), n=n, cfl=0.4, flux=flux)
     n = 32
     x = -1 + np.arange(n) * (2.0 / n)
     Xg, Yg = np.meshgrid(x, x)
@@ -80,7 +88,35 @@ def main():
     assert rc == 0
     np.savez_compressed(os.path.join(HERE, "ref_ctcs2d.npz"), p0=p0, p1=0.999 * p0, h=2.0 / n, dt=0.5 * 2.0 / n,
                         steps=25, p_old=a, p=b)
+    # 2D diffuse-interface RHS of 2d/weno4/bubble (its compiled-in EOS), smooth and sharp interfaces
+    for name, smear, nst in (("smooth", 2.0, 3), ("sharp", 0.05, 2)):
+        nx, ny, h = 22, 18, 1.0 / 22
+        cfg = O.mp2d_cfg(nx, ny, h, -0.5, -0.45, cfl=0.9, bc=(1, 2, 0, 0) if name == "sharp" else (1, 2, 2, 2))
+        U = bubble_state(nx, ny, h, -0.5, -0.45, smear=smear, seed=7)
+        R, dt, rc = O.ref_bubble_rhs(cfg, U)
+        assert rc == 0
+        U3, t3, dt3, rc3 = O.ref_bubble_run(cfg, U, nst)
+        assert rc3 == 0
+        np.savez_compressed(os.path.join(HERE, f"ref_bubble_{name}.npz"), U=U, RHS=R, dt=dt, U3=U3, t3=t3, dt3=dt3,
+                            bc=np.array(list(cfg.bc)), nx=nx, ny=ny, h=h, xmin=-0.5, ymin=-0.45, cfl=0.9, steps=nst)
     print("golden fixtures written to", HERE)
+
+
+def bubble_state(nx, ny, h, xmin, ymin, R0=0.3, smear=2.0, seed=None):
+    """bubble_collapse-like primitive field (2d/weno4/bubble/initial_condition.c:173-202
+    shape, smaller radius), with seeded velocities, as conserved variables"""
+    x = xmin + (np.arange(nx) + 0.5) * h
+    y = ymin + (np.arange(ny) + 0.5) * h
+    X, Y = np.meshgrid(x, y)
+    th = np.tanh((np.sqrt(X**2 + Y**2) - R0) / (smear * h))
+    V = np.zeros((ny, nx, 5))
+    V[..., 0] = 0.5 * ((1e-2 + 1.0) + (1.0 - 1e-2) * th)
+    V[..., 3] = 0.5 * ((1.0 + 100.0) + (100.0 - 1.0) * th)
+    V[..., 4] = 0.5 * ((0.0 + 1.0) + (1.0 - 0.0) * th)
+    if seed is not None:
+        rng = np.random.default_rng(seed)
+        V[..., 1:3] = 0.1 * rng.standard_normal((ny, nx, 2))
+    return O.mp_prim2cons(0, O.BUBBLE_EOS, V)
 
 
 if __name__ == "__main__":

@@ -24,21 +24,28 @@ def solver(hype, n, bc=(0,) * 6, **kw):
     return hype.EulerSolver(ctx)
 
 
-@pytest.mark.parametrize("name", ["periodic", "walls", "mixed"])
+NAMES = ["periodic", "walls", "mixed", "periodic_hllc", "walls_hllc", "periodic_rothllc", "walls_rothllc"]
+
+
+def _golden_solver(hype, z):
+    n = int(z["n"])
+    flux = int(z["flux"]) if "flux" in z else 0
+    return solver(hype, n, tuple(int(b) for b in z["bc"]), cfl=float(z["cfl"]), flux=flux)
+
+
+@pytest.mark.parametrize("name", NAMES)
 def test_rhs_vs_reference(hype, name):
     z = np.load(os.path.join(GOLDEN, f"ref_euler_{name}.npz"))
-    n = int(z["n"])
-    s = solver(hype, n, tuple(int(b) for b in z["bc"]), cfl=float(z["cfl"]))
+    s = _golden_solver(hype, z)
     R = s.RHSFunction(0.0, z["U"])
     assert rel(R, z["RHS"]) <= TOL_STEP
     assert abs(s.ctx.dt - float(z["dt"])) <= 1e-14 * float(z["dt"])
 
 
-@pytest.mark.parametrize("name", ["periodic", "walls", "mixed"])
+@pytest.mark.parametrize("name", NAMES)
 def test_three_steps_vs_reference(hype, name):
     z = np.load(os.path.join(GOLDEN, f"ref_euler_{name}.npz"))
-    n = int(z["n"])
-    s = solver(hype, n, tuple(int(b) for b in z["bc"]), cfl=float(z["cfl"]))
+    s = _golden_solver(hype, z)
     s.set_state(z["U"])
     s.step(1)
     s.step(2)
@@ -170,3 +177,21 @@ def test_inadmissible_state_returns_error(hype):
     # the context stays usable
     R = s.RHSFunction(0.0, _pulse(n))
     assert np.isfinite(R).all()
+
+
+@pytest.mark.parametrize("flux", [1, 2])
+def test_hllc_family_run_vs_oracle(hype, oracle, flux):
+    n = 14
+    U0 = _pulse(n, amp=0.3)
+    rng = np.random.default_rng(5)
+    U0[..., 1:4] += 0.05 * rng.standard_normal(U0[..., 1:4].shape)
+    U0[..., 4] += 0.5 * (U0[..., 1:4] ** 2).sum(-1) / U0[..., 0]
+    bc = (1, 1, 2, 2, 0, 0)
+    ctx = hype.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, boundaries=bc, flux=flux)
+    s = hype.EulerSolver(ctx)
+    s.set_state(U0)
+    s.step(8)
+    Uo, t, dt, rc = oracle.euler_run(oracle.euler_cfg(n, 1.0 / n, cfl=0.4, bc=bc, flux=flux), U0, 8)
+    assert rc == 0
+    assert rel(s.get_state(), Uo) <= TOL_RUN
+    assert abs(s.t - t) <= 1e-12 * t

@@ -9,11 +9,19 @@ import pytest
 from conftest import GOLDEN
 
 
-@pytest.mark.parametrize("name", ["periodic", "walls", "mixed"])
+NAMES = ["periodic", "walls", "mixed", "periodic_hllc", "walls_hllc", "periodic_rothllc", "walls_rothllc"]
+
+
+def _cfg(oracle, z):
+    n = int(z["n"])
+    flux = int(z["flux"]) if "flux" in z else 0
+    return oracle.euler_cfg(n, 1.0 / n, cfl=float(z["cfl"]), bc=tuple(int(b) for b in z["bc"]), flux=flux)
+
+
+@pytest.mark.parametrize("name", NAMES)
 def test_euler_rhs_matches_reference_bitwise(oracle, name):
     z = np.load(os.path.join(GOLDEN, f"ref_euler_{name}.npz"))
-    n = int(z["n"])
-    cfg = oracle.euler_cfg(n, 1.0 / n, cfl=float(z["cfl"]), bc=tuple(int(b) for b in z["bc"]))
+    cfg = _cfg(oracle, z)
     R, smax, rc, bad = oracle.euler_rhs(cfg, z["U"])
     assert rc == 0 and bad == -1
     assert np.array_equal(R, z["RHS"])
@@ -21,11 +29,10 @@ def test_euler_rhs_matches_reference_bitwise(oracle, name):
     assert dt == float(z["dt"])
 
 
-@pytest.mark.parametrize("name", ["periodic", "walls", "mixed"])
+@pytest.mark.parametrize("name", NAMES)
 def test_euler_ssprk43_matches_reference_bitwise(oracle, name):
     z = np.load(os.path.join(GOLDEN, f"ref_euler_{name}.npz"))
-    n = int(z["n"])
-    cfg = oracle.euler_cfg(n, 1.0 / n, cfl=float(z["cfl"]), bc=tuple(int(b) for b in z["bc"]))
+    cfg = _cfg(oracle, z)
     U3, t3, dt3, rc = oracle.euler_run(cfg, z["U"], 3)
     assert rc == 0
     assert np.array_equal(U3, z["U3"])
@@ -61,3 +68,19 @@ def test_accuracy_tables_present():
         t = json.load(f)
     assert len(t["standing_wave_2d_Error_dat"]) == 4
     assert t["plane_wave_3d_main_tex"][0][0] == 16
+
+
+@pytest.mark.parametrize("name", ["smooth", "sharp"])
+def test_bubble_rhs_and_rk104_match_reference_bitwise(oracle, name):
+    """2D diffuse-interface RHS (primitive CWENO4, PAD fallback, rotated HLLC, phi term)
+    and RK104 steps against 2d/weno4/bubble compiled in place."""
+    z = np.load(os.path.join(GOLDEN, f"ref_bubble_{name}.npz"))
+    cfg = oracle.mp2d_cfg(int(z["nx"]), int(z["ny"]), float(z["h"]), float(z["xmin"]), float(z["ymin"]),
+                          cfl=float(z["cfl"]), bc=tuple(int(b) for b in z["bc"]))
+    R, smax, rc, fb = oracle.mp2d_rhs(cfg, z["U"])
+    assert rc == 0 and np.array_equal(R, z["RHS"])
+    assert (cfg.cfl * cfg.h) / (2.0 * smax) == float(z["dt"])
+    if name == "sharp":
+        assert fb > 0  # the admissibility fallback is exercised
+    U3, t3, dt3, rc = oracle.mp2d_run(cfg, z["U"], int(z["steps"]), stepper=1)
+    assert rc == 0 and np.array_equal(U3, z["U3"]) and t3 == float(z["t3"]) and dt3 == float(z["dt3"])

@@ -36,6 +36,22 @@ def test_rhs_bitwise(oracle, bc):
     assert (1.0 / 3.0) * (cfg.cfl * cfg.h) / (smax + 0.0) == dt2
 
 
+@pytest.mark.parametrize("flux", [1, 2])
+@pytest.mark.parametrize("bc", [(0,) * 6, (1, 2, 2, 1, 0, 0)])
+def test_hllc_family_bitwise(oracle, flux, bc):
+    _need_ref(oracle)
+    n = 7
+    cfg = oracle.euler_cfg(n, 1.0 / n, cfl=0.4, bc=bc, flux=flux)
+    U = _state(n, 17)
+    R1, smax, rc, _ = oracle.euler_rhs(cfg, U)
+    R2, dt2, rc2 = oracle.ref_euler_rhs(cfg, U)
+    assert rc == rc2 == 0 and np.array_equal(R1, R2)
+    assert (1.0 / 3.0) * (cfg.cfl * cfg.h) / (smax + 0.0) == dt2
+    a = oracle.euler_run(cfg, U, 2)
+    b = oracle.ref_euler_run(cfg, U, 2)
+    assert np.array_equal(a[0], b[0]) and a[1] == b[1] and a[2] == b[2]
+
+
 @pytest.mark.parametrize("dt_mode", [0, 1, 2])
 def test_run_bitwise_dt_modes(oracle, dt_mode):
     _need_ref(oracle)
