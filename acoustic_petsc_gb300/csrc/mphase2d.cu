@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(128) k_mp_faces(const R* __restrict__ T, doubl
 
 // out = a*X + b*Y + (c*dt)*L, L the divergence with the volume-fraction term
 struct Stage {
-    double a, b, c;
+    double a, b, c, d;  // c*dt/d: the stage's dt fraction formed as the reference forms dt/r
     int rhs_only;
 };
 
@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(256) k_mp_update(const double* __restrict__ F,
     const long long fxl = (long long)j * (g.nx + 1) + i, fyl = (long long)j * g.nx + i;
     const long long cell = (long long)j * g.nx + i;
     const double a = Win[ia * g.N + cell];
-    const double cdt = st.rhs_only ? 0.0 : st.c * ds->dt;
+    const double cdt = st.rhs_only ? 0.0 : st.c * ds->dt / st.d;
     for (int c = 0; c < nv; ++c) {
         double L;
         if (c == ia)
@@ -395,7 +395,7 @@ extern "C" int hype_mp2d_rhs(hype_mp2d* m, double t, const double* U_aos, double
     k_mp_reset<<<1, 1, 0, m->stream>>>(m->ds, 11);
     HYPE_LAUNCHED(1);
     if ((rc = mp_rhs(m, m->S, 11))) return rc;
-    if ((rc = mp_update(m, m->S, nullptr, nullptr, m->L, Stage{0, 0, 0, 1}))) return rc;
+    if ((rc = mp_update(m, m->S, nullptr, nullptr, m->L, Stage{0, 0, 0, 1, 1}))) return rc;
     if ((rc = mp_d2h(m, m->L, RHS_aos))) return rc;
     if ((rc = mp_scalars(m))) return rc;
     if (dt_out) *dt_out = (m->p.cfl * m->p.h) / (2.0 * bits2d(m->hs->smax_bits[11]));
@@ -446,26 +446,26 @@ extern "C" int hype_mp2d_step(hype_mp2d* m, int nsteps, double* t_inout, double*
         HYPE_LAUNCHED(1);
         if (m->p.stepper == HYPE_STEP_SSPRK43) {
             // SSPRK(4,3): u1 = u + dt/2 L(u); u2 = u1 + dt/2 L(u1); u3 = 2/3 u + 1/3 u2 + dt/6 L(u2); u4 = u3 + dt/2 L(u3)
-            if ((rc = mp_update(m, m->U, m->U, nullptr, m->W0, Stage{1.0, 0.0, 0.5, 0}))) return rc;
-            if ((rc = mp_rhs(m, m->W0, 1)) || (rc = mp_update(m, m->W0, m->W0, nullptr, m->W0, Stage{1.0, 0.0, 0.5, 0}))) return rc;
-            if ((rc = mp_rhs(m, m->W0, 2)) || (rc = mp_update(m, m->W0, m->U, m->W0, m->W0, Stage{2.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 0})))
+            if ((rc = mp_update(m, m->U, m->U, nullptr, m->W0, Stage{1.0, 0.0, 1.0, 2.0, 0}))) return rc;
+            if ((rc = mp_rhs(m, m->W0, 1)) || (rc = mp_update(m, m->W0, m->W0, nullptr, m->W0, Stage{1.0, 0.0, 1.0, 2.0, 0}))) return rc;
+            if ((rc = mp_rhs(m, m->W0, 2)) || (rc = mp_update(m, m->W0, m->U, m->W0, m->W0, Stage{1.0 * 2 / (2 * 2 - 1.0), (2 - 1.0) / (2 * 2 - 1), 2 - 1.0, 2.0 * (2 * 2 - 1), 0})))
                 return rc;
-            if ((rc = mp_rhs(m, m->W0, 3)) || (rc = mp_update(m, m->W0, m->W0, nullptr, m->U, Stage{1.0, 0.0, 0.5, 0}))) return rc;
+            if ((rc = mp_rhs(m, m->W0, 3)) || (rc = mp_update(m, m->W0, m->W0, nullptr, m->U, Stage{1.0, 0.0, 1.0, 2.0, 0}))) return rc;
         } else {
             // SSPRK(10,4) low-storage (Ketcheson 2008): five dt/6 stages, q2 = 9/25 q1 + 1/25 u,
             // q1 = 15 q2 - 5 q1, four dt/6 stages, u = 3/5 q1 + q2 + dt/10 L(q1)
             const long long n = m->g.N * m->g.nv;
-            if ((rc = mp_update(m, m->U, m->U, nullptr, m->W0, Stage{1.0, 0.0, 1.0 / 6.0, 0}))) return rc;
+            if ((rc = mp_update(m, m->U, m->U, nullptr, m->W0, Stage{1.0, 0.0, 1.0, 6.0, 0}))) return rc;
             for (int k = 1; k < 5; ++k)
-                if ((rc = mp_rhs(m, m->W0, k)) || (rc = mp_update(m, m->W0, m->W0, nullptr, m->W0, Stage{1.0, 0.0, 1.0 / 6.0, 0})))
+                if ((rc = mp_rhs(m, m->W0, k)) || (rc = mp_update(m, m->W0, m->W0, nullptr, m->W0, Stage{1.0, 0.0, 1.0, 6.0, 0})))
                     return rc;
             k_mp_axpby<<<cdiv(n, 256), 256, 0, m->stream>>>(m->W0, m->U, m->W1, 9.0 / 25, 1.0 / 25, n);
             k_mp_axpby<<<cdiv(n, 256), 256, 0, m->stream>>>(m->W1, m->W0, m->W0, 15.0, -5.0, n);
             HYPE_LAUNCHED(2);
             for (int k = 5; k < 9; ++k)
-                if ((rc = mp_rhs(m, m->W0, k)) || (rc = mp_update(m, m->W0, m->W0, nullptr, m->W0, Stage{1.0, 0.0, 1.0 / 6.0, 0})))
+                if ((rc = mp_rhs(m, m->W0, k)) || (rc = mp_update(m, m->W0, m->W0, nullptr, m->W0, Stage{1.0, 0.0, 1.0, 6.0, 0})))
                     return rc;
-            if ((rc = mp_rhs(m, m->W0, 9)) || (rc = mp_update(m, m->W0, m->W0, m->W1, m->U, Stage{3.0 / 5.0, 1.0, 1.0 / 10.0, 0})))
+            if ((rc = mp_rhs(m, m->W0, 9)) || (rc = mp_update(m, m->W0, m->W0, m->W1, m->U, Stage{3.0 / 5, 1.0, 1.0, 10.0, 0})))
                 return rc;
         }
     }

@@ -54,68 +54,127 @@ __device__ __forceinline__ R minmod(R a, R b) {
     return (fabs(a) < fabs(b)) ? a : b;
 }
 
-// 2D CWENO4: 13-point stencil (centre, x-2..x+2, y-2..y+2, diagonals) -> 10 coefficients
+// 2D CWENO4: 13-point stencil (centre, x-2..x+2, y-2..y+2, diagonals) -> 10 coefficients.
+// Written operation by operation in the reference's order; the file is compiled
+// without FMA contraction, so the FP64 instance rounds exactly like the CPU code
+// (the admissibility test downstream is a hard threshold on these values).
+template <typename R>
+struct Cw2Weights;
+
 template <typename R>
 __device__ __forceinline__ void cweno2d(R u0, const R* ux, const R* uy, R upp, R upm, R ump, R umm, R* cf) {
     const R u_im2 = ux[0], u_im1 = ux[1], u_ip1 = ux[3], u_ip2 = ux[4];
     const R u_jm2 = uy[0], u_jm1 = uy[1], u_jp1 = uy[3], u_jp2 = uy[4];
-    const R h = R(0.5), q = R(0.25);
-    const R xR4 = R(41. / 60.) * (-u_im1 + u_ip1) + R(11. / 120.) * (u_im2 - u_ip2);
-    const R yR4 = R(41. / 60.) * (-u_jm1 + u_jp1) + R(11. / 120.) * (u_jm2 - u_jp2);
-    const R xxR4 = -u0 + h * (u_im1 + u_ip1);
-    const R yyR4 = -u0 + h * (u_jm1 + u_jp1);
-    const R xyR4 = q * (umm - ump - upm + upp);
-    const R xxxR4 = R(1. / 6.) * (u_im1 - u_ip1) + R(1. / 12.) * (u_ip2 - u_im2);
-    const R yyyR4 = R(1. / 6.) * (u_jm1 - u_jp1) + R(1. / 12.) * (u_jp2 - u_jm2);
-    const R xxyR4 = q * (-umm + ump - upm + upp) + h * (u_jm1 - u_jp1);
-    const R xyyR4 = h * (u_im1 - u_ip1) + q * (upp - umm - ump + upm);
+    const R u_ip1jp1 = upp, u_ip1jm1 = upm, u_im1jp1 = ump, u_im1jm1 = umm;
+    const R r41_60 = R(41. / 60.), r11_120 = R(11. / 120.), r1_6 = R(1. / 6.), r1_12 = R(1. / 12.);
     const R r13_3 = R(13. / 3.), r7_6 = R(7. / 6.);
-    const R a = xR4 + R(0.1) * xxxR4, b = yR4 + R(0.1) * yyyR4;
-    const R IS4 = a * a + r13_3 * (xxR4 * xxR4 + yyR4 * yyR4) + b * b + R(39.05) * (xxxR4 * xxxR4 + yyyR4 * yyyR4) +
+    const R gH = R(0.85), gL = R(0.85);
+    R g3[5];
+    g3[0] = (R(1.0) - gH) * gL;
+#pragma unroll
+    for (int i = 1; i < 5; ++i) g3[i] = R(0.25) * (R(1) - gH) * (R(1) - gL);
+    const R xR4 = r41_60 * (-u_im1 + u_ip1) + r11_120 * (u_im2 - u_ip2);
+    const R yR4 = r41_60 * (-u_jm1 + u_jp1) + r11_120 * (u_jm2 - u_jp2);
+    const R xxR4 = -u0 + R(0.5) * (u_im1 + u_ip1);
+    const R yyR4 = -u0 + R(0.5) * (u_jm1 + u_jp1);
+    const R xyR4 = R(0.25) * (u_im1jm1 - u_im1jp1 - u_ip1jm1 + u_ip1jp1);
+    const R xxxR4 = r1_6 * (u_im1 - u_ip1) + r1_12 * (u_ip2 - u_im2);
+    const R yyyR4 = r1_6 * (u_jm1 - u_jp1) + r1_12 * (u_jp2 - u_jm2);
+    const R xxyR4 = R(0.25) * (-u_im1jm1 + u_im1jp1 - u_ip1jm1 + u_ip1jp1) + R(0.5) * (u_jm1 - u_jp1);
+    const R xyyR4 = R(0.5) * (u_im1 - u_ip1) + R(0.25) * (u_ip1jp1 - u_im1jm1 - u_im1jp1 + u_ip1jm1);
+    const R IS4 = (xR4 + R(0.1) * xxxR4) * (xR4 + R(0.1) * xxxR4) + r13_3 * (xxR4 * xxR4 + yyR4 * yyR4) +
+                  (yR4 + R(0.1) * yyyR4) * (yR4 + R(0.1) * yyyR4) + R(39.05) * (xxxR4 * xxxR4 + yyyR4 * yyyR4) +
                   r7_6 * xyR4 * xyR4 + R(4.7) * (xxyR4 * xxyR4 + xyyR4 * xyyR4);
-    // R3 stencils: 0 centred, 1 towards -x, 2 towards +x, 3 towards -y, 4 towards +y
-    const R cx = h * (-u_im1 + u_ip1), cy = h * (-u_jm1 + u_jp1);
-    const R X1 = R(1.5) * u0 - R(2.0) * u_im1 + h * u_im2, XX1 = h * u0 - u_im1 + h * u_im2, XY1 = h * (umm - ump - u_jm1 + u_jp1);
-    const R X2 = R(-1.5) * u0 + R(2.0) * u_ip1 - h * u_ip2, XX2 = h * u0 - u_ip1 + h * u_ip2, XY2 = h * (-upm + upp + u_jm1 - u_jp1);
-    const R Y3 = R(1.5) * u0 - R(2.0) * u_jm1 + h * u_jm2, YY3 = h * u0 - u_jm1 + h * u_jm2, XY3 = h * (-u_im1 + umm + u_ip1 - upm);
-    const R Y4 = R(-1.5) * u0 + R(2.0) * u_jp1 - h * u_jp2, YY4 = h * u0 - u_jp1 + h * u_jp2, XY4 = h * (u_im1 - ump - u_ip1 + upp);
-    const R IS0 = cx * cx + cy * cy + r13_3 * (xxR4 * xxR4 + yyR4 * yyR4) + r7_6 * xyR4 * xyR4;
-    const R IS1 = X1 * X1 + cy * cy + r13_3 * (XX1 * XX1 + yyR4 * yyR4) + r7_6 * XY1 * XY1;
-    const R IS2 = X2 * X2 + cy * cy + r13_3 * (XX2 * XX2 + yyR4 * yyR4) + r7_6 * XY2 * XY2;
-    const R IS3 = cx * cx + Y3 * Y3 + r13_3 * (xxR4 * xxR4 + YY3 * YY3) + r7_6 * XY3 * XY3;
-    const R IS4b = cx * cx + Y4 * Y4 + r13_3 * (xxR4 * xxR4 + YY4 * YY4) + r7_6 * XY4 * XY4;
-    const R gH = R(0.85), g0 = R((1.0 - 0.85) * 0.85), gs = R(0.25 * (1 - 0.85) * (1 - 0.85));
-    // w = gamma / (IS + eps)^4, normalised; formed from ratios to the smallest (IS + eps)
-    // so that FP32 does not underflow (the same normalised weights)
-    R s[6] = {IS4 + R(1e-12), IS0 + R(1e-12), IS1 + R(1e-12), IS2 + R(1e-12), IS3 + R(1e-12), IS4b + R(1e-12)};
-    R mn = s[0];
+    R X[5], Y[5], XX[5], YY[5], XY[5];
+    X[0] = R(0.5) * (-u_im1 + u_ip1);
+    Y[0] = R(0.5) * (-u_jm1 + u_jp1);
+    XX[0] = -u0 + R(0.5) * (u_im1 + u_ip1);
+    YY[0] = -u0 + R(0.5) * (u_jm1 + u_jp1);
+    XY[0] = R(0.25) * (u_im1jm1 - u_im1jp1 - u_ip1jm1 + u_ip1jp1);
+    X[1] = R(1.5) * u0 - R(2.0) * u_im1 + R(0.5) * u_im2;
+    Y[1] = R(0.5) * (-u_jm1 + u_jp1);
+    XX[1] = R(0.5) * u0 - u_im1 + R(0.5) * u_im2;
+    YY[1] = -u0 + R(0.5) * u_jm1 + R(0.5) * u_jp1;
+    XY[1] = R(0.5) * (u_im1jm1 - u_im1jp1 - u_jm1 + u_jp1);
+    X[2] = R(-1.5) * u0 + R(2.0) * u_ip1 - R(0.5) * u_ip2;
+    Y[2] = R(0.5) * (-u_jm1 + u_jp1);
+    XX[2] = R(0.5) * u0 - u_ip1 + R(0.5) * u_ip2;
+    YY[2] = -u0 + R(0.5) * u_jm1 + R(0.5) * u_jp1;
+    XY[2] = R(0.5) * (-u_ip1jm1 + u_ip1jp1 + u_jm1 - u_jp1);
+    X[3] = R(0.5) * (-u_im1 + u_ip1);
+    Y[3] = R(1.5) * u0 - R(2.0) * u_jm1 + R(0.5) * u_jm2;
+    XX[3] = -u0 + R(0.5) * u_im1 + R(0.5) * u_ip1;
+    YY[3] = R(0.5) * u0 - u_jm1 + R(0.5) * u_jm2;
+    XY[3] = R(0.5) * (-u_im1 + u_im1jm1 + u_ip1 - u_ip1jm1);
+    X[4] = R(0.5) * (-u_im1 + u_ip1);
+    Y[4] = R(-1.5) * u0 + R(2.0) * u_jp1 - R(0.5) * u_jp2;
+    XX[4] = -u0 + R(0.5) * u_im1 + R(0.5) * u_ip1;
+    YY[4] = R(0.5) * u0 - u_jp1 + R(0.5) * u_jp2;
+    XY[4] = R(0.5) * (u_im1 - u_im1jp1 - u_ip1 + u_ip1jp1);
+    R IS3[5];
 #pragma unroll
-    for (int k = 1; k < 6; ++k) mn = fmin(mn, s[k]);
-    R w[6];
-    const R gam[6] = {gH, g0, gs, gs, gs, gs};
-    R tot = R(0);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        w[k] = gam[k] * pow4(mn / s[k]);
-        tot += w[k];
-    }
-    const R it = R(1) / tot;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) w[k] *= it;
-    const R wr = w[0] / gH;
-    const R w0 = w[1], w1 = w[2], w2 = w[3], w3 = w[4], w4 = w[5];
+    for (int i = 0; i < 5; ++i)
+        IS3[i] = X[i] * X[i] + Y[i] * Y[i] + r13_3 * (XX[i] * XX[i] + YY[i] * YY[i]) + r7_6 * XY[i] * XY[i];
+    R w4, w3[5];
+    Cw2Weights<R>::compute(IS4, IS3, gH, g3, w4, w3);
+    const R wr = w4 / gH;
+    const R* Q[5] = {X, Y, XX, YY, XY};
+    const R R4[5] = {xR4, yR4, xxR4, yyR4, xyR4};
     cf[0] = u0;
-    // x derivative: modified by stencils 1, 2
-    cf[1] = wr * (xR4 - (g0 + R(2) * gs) * cx - gs * (X1 + X2)) + (w0 + w3 + w4) * cx + w1 * X1 + w2 * X2;
-    cf[2] = wr * (yR4 - (g0 + R(2) * gs) * cy - gs * (Y3 + Y4)) + (w0 + w1 + w2) * cy + w3 * Y3 + w4 * Y4;
-    cf[3] = wr * (xxR4 - (g0 + R(2) * gs) * xxR4 - gs * (XX1 + XX2)) + (w0 + w3 + w4) * xxR4 + w1 * XX1 + w2 * XX2;
-    cf[4] = wr * (yyR4 - (g0 + R(2) * gs) * yyR4 - gs * (YY3 + YY4)) + (w0 + w1 + w2) * yyR4 + w3 * YY3 + w4 * YY4;
-    cf[5] = wr * (xyR4 - g0 * xyR4 - gs * (XY1 + XY2 + XY3 + XY4)) + w0 * xyR4 + w1 * XY1 + w2 * XY2 + w3 * XY3 + w4 * XY4;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        const R* v = Q[q];
+        cf[1 + q] = wr * (R4[q] - g3[0] * v[0] - g3[1] * v[1] - g3[2] * v[2] - g3[3] * v[3] - g3[4] * v[4]) + w3[0] * v[0] +
+                    w3[1] * v[1] + w3[2] * v[2] + w3[3] * v[3] + w3[4] * v[4];
+    }
     cf[6] = wr * xxxR4;
     cf[7] = wr * yyyR4;
     cf[8] = wr * xxyR4;
     cf[9] = wr * xyyR4;
 }
+
+// FP64: w = gamma / pow4(IS + eps), normalised by division, as the reference does
+template <>
+struct Cw2Weights<double> {
+    __device__ __forceinline__ static void compute(double IS4, const double* IS3, double gH, const double* g3, double& w4,
+                                                   double* w3) {
+        w4 = gH / (pow4(IS4 + 1.0e-12));
+        double sum = w4;
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            w3[i] = g3[i] / (pow4(IS3[i] + 1.0e-12));
+            sum += w3[i];
+        }
+        w4 = w4 / sum;
+#pragma unroll
+        for (int i = 0; i < 5; ++i) w3[i] = w3[i] / sum;
+    }
+};
+
+// FP32: (1e-12)^4 underflows; the same normalised weights from ratios to the smallest (IS + eps)
+template <>
+struct Cw2Weights<float> {
+    __device__ __forceinline__ static void compute(float IS4, const float* IS3, float gH, const float* g3, float& w4,
+                                                   float* w3) {
+        float s4 = IS4 + 1.0e-12f, ss[5];
+        float mn = s4;
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            ss[i] = IS3[i] + 1.0e-12f;
+            mn = fminf(mn, ss[i]);
+        }
+        w4 = gH * pow4(mn / s4);
+        float sum = w4;
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            w3[i] = g3[i] * pow4(mn / ss[i]);
+            sum += w3[i];
+        }
+        w4 = w4 / sum;
+#pragma unroll
+        for (int i = 0; i < 5; ++i) w3[i] = w3[i] / sum;
+    }
+};
 
 // mixture ratio of specific heats and stiffness (FP64)
 __device__ __forceinline__ void mix(const Eos& e, double a, double& g, double& pi) {
@@ -169,86 +228,127 @@ __device__ __forceinline__ bool pad_ok(const Eos& e, const R* V) {
     return !((double)V[0] < 1.0e-14 || (double)V[1] < 1.0e-14 || ((double)V[4] + pi) < 1.0e-12 || a1 < 0.0 || a1 > 1.0);
 }
 
-// one side of an HLLC solve: primitive state in the rotated frame
-template <typename R>
-struct Side {
-    R rho, un, ut, p, E, c, a;  // mixture density, normal/tangential velocity, pressure, energy, sound speed, fraction
-    R q[MAXV];                  // conserved state
-    R f[MAXV + 1];              // physical flux (+ u_n)
-};
-
+// conserved state of a primitive state (PDEPrim2Cons, pde.c:24-36; kapila_5eqn.c:44-60)
 template <typename R, int MODEL>
-__device__ __forceinline__ void make_side(const Eos& e, const R* V, R nx, R ny, Side<R>& s, bool& bad) {
-    constexpr int NV = MODEL == HYPE_MP_DI4 ? 5 : 6;
+__device__ __forceinline__ void prim2cons(const Eos& e, const R* V, R* Q) {
     double gd, pid;
-    mix(e, (double)V[NV - 1], gd, pid);
-    const R g = (R)gd, pi = (R)pid;
-    R u, v, p;
     if (MODEL == HYPE_MP_DI4) {
-        s.rho = V[0]; u = V[1]; v = V[2]; p = V[3];
+        mix(e, (double)V[4], gd, pid);
+        const R g = (R)gd, pi = (R)pid;
+        const R en = (V[3] + g * pi) / (g - R(1.0));
+        const R k = R(0.5) * V[0] * (V[1] * V[1] + V[2] * V[2]);
+        Q[0] = V[0]; Q[1] = V[0] * V[1]; Q[2] = V[0] * V[2]; Q[3] = k + en; Q[4] = V[4];
     } else {
-        s.rho = V[5] * V[0] + (R(1) - V[5]) * V[1]; u = V[2]; v = V[3]; p = V[4];
+        const R a1 = V[5], a2 = R(1.0) - a1;
+        mix(e, (double)a1, gd, pid);
+        const R g = (R)gd, pi = (R)pid;
+        const R rho = a1 * V[0] + a2 * V[1];
+        Q[0] = a1 * V[0]; Q[1] = a2 * V[1]; Q[2] = rho * V[2]; Q[3] = rho * V[3];
+        Q[4] = (V[4] + g * pi) / (g - R(1.0)) + R(0.5) * rho * (V[2] * V[2] + V[3] * V[3]);
+        Q[5] = a1;
     }
-    s.a = V[NV - 1];
-    s.p = p;
-    s.un = u * nx + v * ny;
-    s.ut = -u * ny + v * nx;
-    s.E = (p + g * pi) / (g - R(1)) + R(0.5) * s.rho * (u * u + v * v);
-    s.c = sqrt(g * (p + pi) / s.rho);
-    bad |= (s.rho < R(1.0e-14)) || ((p + pi) < R(1.0e-12)) || !(s.rho == s.rho);
-    if (MODEL == HYPE_MP_DI4) {
-        s.q[0] = s.rho; s.q[1] = s.rho * u; s.q[2] = s.rho * v; s.q[3] = s.E; s.q[4] = s.a;
-        const R m = s.rho * s.un;
-        s.f[0] = m; s.f[1] = m * u + p * nx; s.f[2] = m * v + p * ny; s.f[3] = s.un * (s.E + p); s.f[4] = s.a * s.un;
-    } else {
-        s.q[0] = V[5] * V[0]; s.q[1] = (R(1) - V[5]) * V[1]; s.q[2] = s.rho * u; s.q[3] = s.rho * v; s.q[4] = s.E; s.q[5] = s.a;
-        s.f[0] = s.q[0] * s.un; s.f[1] = s.q[1] * s.un; s.f[2] = s.rho * u * s.un + p * nx; s.f[3] = s.rho * v * s.un + p * ny;
-        s.f[4] = (s.E + p) * s.un; s.f[5] = s.a * s.un;
-    }
-    s.f[NV] = s.un;
 }
 
-// HLLC with the interface velocity as the last component (pde.c:131-232)
+// physical flux of a primitive state and its wave speed (PDEFluxPrim, pde.c:62-97)
+template <typename R, int MODEL>
+__device__ __forceinline__ R flux_prim(const Eos& e, const R* V, R nx, R ny, R* F, bool& bad) {
+    double gd, pid;
+    if (MODEL == HYPE_MP_DI4) {
+        const R phi = V[4];
+        mix(e, (double)phi, gd, pid);
+        const R g = (R)gd, pi = (R)pid;
+        const R rho = V[0], u = V[1], v = V[2], p = V[3];
+        const R E = (p + g * pi) / (g - R(1.0)) + R(0.5) * rho * (u * u + v * v);
+        const R un = u * nx + v * ny;
+        const R rhoun = rho * un;
+        bad |= (rho < R(1.0e-14)) || ((p + pi) < R(1.0e-12)) || !(rho == rho);
+        F[0] = rhoun; F[1] = rhoun * u + p * nx; F[2] = rhoun * v + p * ny; F[3] = un * (E + p); F[4] = phi * un;
+        return fabs(un) + sqrt(g * (p + pi) / rho);
+    }
+    const R a1 = V[5], a2 = R(1.0) - a1;
+    mix(e, (double)a1, gd, pid);
+    const R g = (R)gd, pi = (R)pid;
+    const R r1 = V[0], r2 = V[1], u = V[2], v = V[3], p = V[4];
+    const R rho = a1 * r1 + a2 * r2;
+    const R E = (p + g * pi) / (g - R(1.0)) + R(0.5) * rho * (u * u + v * v);
+    const R un = u * nx + v * ny;
+    bad |= (rho < R(1.0e-14)) || ((p + pi) < R(1.0e-12)) || !(rho == rho);
+    F[0] = a1 * r1 * un; F[1] = a2 * r2 * un; F[2] = rho * u * un + p * nx; F[3] = rho * v * un + p * ny;
+    F[4] = (E + p) * un; F[5] = a1 * un;
+    return fabs(un) + sqrt(g * (p + pi) / rho);
+}
+
+// HLLC with the interface velocity as the last component (HLLCRiemannSolver, pde.c:131-232);
+// star partial densities of the five-equation model a_k r_k (S - u_n)/(S - S*)
 template <typename R, int MODEL>
 __device__ __forceinline__ R hllc2(const Eos& e, const R* VL, const R* VR, R nx, R ny, R* Flux, bool& bad) {
     constexpr int NV = MODEL == HYPE_MP_DI4 ? 5 : 6;
-    Side<R> L, Rr;
-    make_side<R, MODEL>(e, VL, nx, ny, L, bad);
-    make_side<R, MODEL>(e, VR, nx, ny, Rr, bad);
-    const R SL = fmin(Rr.un - Rr.c, L.un - L.c);
-    const R SR = fmax(L.un + L.c, Rr.un + Rr.c);
-    const R Ss = (Rr.p - L.p + L.rho * L.un * (SL - L.un) - Rr.rho * Rr.un * (SR - Rr.un)) /
-                 (L.rho * (SL - L.un) - Rr.rho * (SR - Rr.un));
-    const R sel = SL > R(0) ? R(0) : (Ss >= R(0) ? R(1) : (SR >= R(0) ? R(2) : R(3)));
-    const Side<R>& S = (sel < R(1.5)) ? L : Rr;
-    const R Sk = (sel < R(1.5)) ? SL : SR;
-    if (sel == R(0) || sel == R(3)) {
-#pragma unroll
-        for (int k = 0; k <= NV; ++k) Flux[k] = S.f[k];
+    R QL[MAXV], QR[MAXV], FL[MAXV + 1], FR[MAXV + 1];
+    prim2cons<R, MODEL>(e, VL, QL);
+    prim2cons<R, MODEL>(e, VR, QR);
+    const R sl = flux_prim<R, MODEL>(e, VL, nx, ny, FL, bad);
+    const R sr = flux_prim<R, MODEL>(e, VR, nx, ny, FR, bad);
+    double gLd, piLd, gRd, piRd;
+    mix(e, (double)VL[NV - 1], gLd, piLd);
+    mix(e, (double)VR[NV - 1], gRd, piRd);
+    const R gL = (R)gLd, piL = (R)piLd, gR = (R)gRd, piR = (R)piRd;
+    R rL, rR, uL, uR, vL, vR, PL, PR;
+    if (MODEL == HYPE_MP_DI4) {
+        rL = VL[0]; uL = VL[1]; vL = VL[2]; PL = VL[3];
+        rR = VR[0]; uR = VR[1]; vR = VR[2]; PR = VR[3];
     } else {
-        const R fr = (Sk - S.un) / (Sk - Ss);
-        const R rs = S.rho * fr;
+        rL = VL[5] * VL[0] + (R(1.0) - VL[5]) * VL[1];
+        rR = VR[5] * VR[0] + (R(1.0) - VR[5]) * VR[1];
+        uL = VL[2]; vL = VL[3]; PL = VL[4];
+        uR = VR[2]; vR = VR[3]; PR = VR[4];
+    }
+    const R unL = uL * nx + vL * ny, utL = -uL * ny + vL * nx;
+    const R unR = uR * nx + vR * ny, utR = -uR * ny + vR * nx;
+    const R cL = sqrt(gL * (PL + piL) / rL), cR = sqrt(gR * (PR + piR) / rR);
+    const R EL = (PL + gL * piL) / (gL - R(1.0)) + R(0.5) * rL * uL * uL + R(0.5) * rL * vL * vL;
+    const R ER = (PR + gR * piR) / (gR - R(1.0)) + R(0.5) * rR * uR * uR + R(0.5) * rR * vR * vR;
+    const R a1 = unR - cR, b1 = unL - cL;
+    const R SL = (a1 < b1) ? a1 : b1;
+    const R a2 = unL + cL, b2 = unR + cR;
+    const R SR = (a2 < b2) ? b2 : a2;
+    const R Ss = (PR - PL + rL * unL * (SL - unL) - rR * unR * (SR - unR)) / (rL * (SL - unL) - rR * (SR - unR));
+    FL[NV] = unL;
+    FR[NV] = unR;
+    // only the star state of the selected side is needed
+    const int sel = (SL > R(0)) ? 0 : (Ss >= R(0)) ? 1 : (SR >= R(0)) ? 2 : 3;
+    if (sel == 0 || sel == 3) {
+        const R* Fo = sel == 0 ? FL : FR;
+#pragma unroll
+        for (int i = 0; i <= NV; ++i) Flux[i] = Fo[i];
+    } else {
+        const bool left = sel == 1;
+        const R Sk = left ? SL : SR, rk = left ? rL : rR, unk = left ? unL : unR, utk = left ? utL : utR;
+        const R Pk = left ? PL : PR, Ek = left ? EL : ER;
+        const R* Vk = left ? VL : VR;
+        const R* Qk = left ? QL : QR;
+        const R* Fk = left ? FL : FR;
         R Us[MAXV];
         if (MODEL == HYPE_MP_DI4) {
-            Us[0] = rs;
-            Us[1] = rs * (Ss * nx - S.ut * ny);
-            Us[2] = rs * (Ss * ny + S.ut * nx);
-            Us[3] = rs * ((S.E / S.rho) + (Ss - S.un) * (Ss + S.p / (S.rho * (Sk - S.un))));
-            Us[4] = S.a * fr;
+            Us[0] = rk * (Sk - unk) / (Sk - Ss);
+            Us[1] = Us[0] * (Ss * nx - utk * ny);
+            Us[2] = Us[0] * (Ss * ny + utk * nx);
+            Us[3] = Us[0] * ((Ek / rk) + (Ss - unk) * (Ss + Pk / (rk * (Sk - unk))));
+            Us[4] = Vk[4] * (Sk - unk) / (Sk - Ss);
         } else {
-            Us[0] = S.q[0] * fr;
-            Us[1] = S.q[1] * fr;
-            Us[2] = rs * (Ss * nx - S.ut * ny);
-            Us[3] = rs * (Ss * ny + S.ut * nx);
-            Us[4] = rs * ((S.E / S.rho) + (Ss - S.un) * (Ss + S.p / (S.rho * (Sk - S.un))));
-            Us[5] = S.a * fr;
+            const R f = (Sk - unk) / (Sk - Ss);
+            const R rs = rk * f;
+            Us[0] = Qk[0] * f;
+            Us[1] = Qk[1] * f;
+            Us[2] = rs * (Ss * nx - utk * ny);
+            Us[3] = rs * (Ss * ny + utk * nx);
+            Us[4] = rs * ((Ek / rk) + (Ss - unk) * (Ss + Pk / (rk * (Sk - unk))));
+            Us[5] = Vk[5] * f;
         }
 #pragma unroll
-        for (int k = 0; k < NV; ++k) Flux[k] = S.f[k] + Sk * (Us[k] - S.q[k]);
-        Flux[NV] = S.un + Sk * (fr - R(1));
+        for (int i = 0; i < NV; ++i) Flux[i] = Fk[i] + Sk * (Us[i] - Qk[i]);
+        Flux[NV] = unk + Sk * (((Sk - unk) / (Sk - Ss)) - R(1.0));
     }
-    const R sl = fabs(L.un) + L.c, sr = fabs(Rr.un) + Rr.c;
-    return sl < sr ? sr : sl;
+    return (sl < sr) ? sr : sl;
 }
 
 // rotated HLLC (pde.c:234-274): HLLC along the velocity-jump direction and its normal
@@ -260,9 +360,11 @@ __device__ __forceinline__ R rot_hllc2(const Eos& e, const R* VL, const R* VR, R
     const R dq = sqrt(du * du + dv * dv);
     R n1x, n1y;
     if (dq < R(1.0E-10)) {
-        n1x = nx; n1y = ny;
+        n1x = nx;
+        n1y = ny;
     } else {
-        n1x = du / dq; n1y = dv / dq;
+        n1x = du / dq;
+        n1y = dv / dq;
     }
     R a1 = n1x * nx + n1y * ny;
     if (a1 < R(0)) {
@@ -278,7 +380,7 @@ __device__ __forceinline__ R rot_hllc2(const Eos& e, const R* VL, const R* VR, R
     const R s2 = hllc2<R, MODEL>(e, VL, VR, n2x, n2y, f2, bad);
 #pragma unroll
     for (int k = 0; k <= NV; ++k) Flux[k] = a1 * f1[k] + a2 * f2[k];
-    return s1 < s2 ? s2 : s1;
+    return (s1 < s2) ? s2 : s1;
 }
 
 }  // namespace mp2d
