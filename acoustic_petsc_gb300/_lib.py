@@ -14,10 +14,11 @@ _L = None
 
 D = C.POINTER(C.c_double)
 I = C.POINTER(C.c_int)
+F = C.POINTER(C.c_float)
 
 HYPE_OK, HYPE_ERR_ARG, HYPE_ERR_STATE, HYPE_ERR_CUDA, HYPE_ERR_NOMEM, HYPE_ERR_UNSUPPORTED = range(6)
 BC_PERIODIC, BC_REFLECTIVE, BC_TRANSMISSIVE, BC_ZERO = range(4)
-RECON_CWENO4, RECON_LINEAR4 = 0, 1
+RECON_CWENO4, RECON_LINEAR4, RECON_LEARNED = 0, 1, 2
 PREC_FP64, PREC_FP32 = 0, 1
 DT_MONITOR, DT_FROZEN, DT_FIXED = 0, 1, 2
 FLUX_RUSANOV, FLUX_HLLC, FLUX_ROTHLLC = 0, 1, 2
@@ -37,6 +38,8 @@ SYMBOLS = [
     "hype_probe_fma_peak", "hype_euler_rhs_noalloc", "hype_euler_noalloc_max_ext",
     "hype_mp2d_create", "hype_mp2d_destroy", "hype_mp2d_rhs", "hype_mp2d_upload", "hype_mp2d_download",
     "hype_mp2d_step", "hype_mp2d_sync", "hype_mp2d_stream",
+    "hype_euler_set_mlp", "hype_euler_set_recon", "hype_euler_indicator_stats", "hype_euler_sample_features",
+    "hype_mlp_nparam", "hype_mlp_score", "hype_mlp_grad", "hype_mlp_train", "hype_euler_shadow_step",
 ]
 
 
@@ -140,6 +143,15 @@ def lib():
         "hype_mp2d_step": ([V, C.c_int, D, D, P(C.c_longlong)], C.c_int),
         "hype_mp2d_sync": ([V], C.c_int),
         "hype_mp2d_stream": ([V], C.c_void_p),
+        "hype_euler_set_mlp": ([V, F, C.c_float], C.c_int),
+        "hype_euler_set_recon": ([V, C.c_int], C.c_int),
+        "hype_euler_indicator_stats": ([V, P(C.c_longlong), P(C.c_longlong), C.c_int], C.c_int),
+        "hype_euler_sample_features": ([V, C.c_longlong, F, F, P(C.c_longlong)], C.c_int),
+        "hype_euler_shadow_step": ([V, D, D, D], C.c_int),
+        "hype_mlp_nparam": ([], C.c_int),
+        "hype_mlp_score": ([F, C.c_int, F, F], C.c_int),
+        "hype_mlp_grad": ([F, F, C.c_int, F, C.c_float, F, D], C.c_int),
+        "hype_mlp_train": ([F, F, C.c_int, F, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint, D], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "euler_kernels.cuh"
+#include "mlp_kernels.cuh"
 
 namespace hype {
 namespace euler {
@@ -47,6 +48,83 @@ __device__ __forceinline__ long long ext_index(const Geo& g, int i, int j, int k
     return ((long long)(k + 1) * (g.ny + 2) + (j + 1)) * (long long)g.ex + (i + 1);
 }
 
+// boundary maps of the offsets -2..2 of one cell along each direction
+struct StencilMap {
+    int mi[5], mj[5], mk[5];
+    int fi, fj, fk;  // bit o set: offset o-2 is a reflective ghost
+};
+
+__device__ __forceinline__ void make_map(const Geo& g, int i, int j, int k, StencilMap& m) {
+    m.fi = m.fj = m.fk = 0;
+#pragma unroll
+    for (int o = 0; o < 5; ++o) {
+        int f = 0;
+        m.mi[o] = bmap(i + o - 2, g.nx, g.bc[0], g.bc[1], &f);
+        m.fi |= f << o;
+        f = 0;
+        m.mj[o] = bmap(j + o - 2, g.ny, g.bc[2], g.bc[3], &f);
+        m.fj |= f << o;
+        f = 0;
+        m.mk[o] = bmap(k + o - 2, g.nz, g.bc[4], g.bc[5], &f);
+        m.fk |= f << o;
+    }
+}
+
+// one value of variable c at offset (oi, oj, ok); a reflective ghost negates the
+// momentum component normal to its wall
+template <typename R>
+__device__ __forceinline__ R ldw(const double* __restrict__ Wc, int c, const Geo& g, const StencilMap& m, int oi, int oj,
+                                 int ok) {
+    double v = __ldg(Wc + ((long long)m.mk[ok + 2] * g.ny + m.mj[oj + 2]) * g.nx + m.mi[oi + 2]);
+    const int fm = (c == 1) ? m.fi : (c == 2) ? m.fj : (c == 3) ? m.fk : 0;
+    const int o = (c == 1) ? oi : (c == 2) ? oj : ok;
+    if (fm && ((fm >> (o + 2)) & 1)) v = -v;
+    return (R)v;
+}
+
+// the 33-point stencil of variable c (index map of euler_kernels.cuh)
+template <typename R>
+__device__ __forceinline__ void gather33(const double* __restrict__ Wc, int c, const Geo& g, const StencilMap& m, R* s) {
+    s[0] = ldw<R>(Wc, c, g, m, 0, 0, 0);
+#pragma unroll
+    for (int o = 0; o < 4; ++o) {
+        const int off = (o == 0) ? -2 : (o == 1) ? -1 : (o == 2) ? 1 : 2;
+        s[S1(0, off)] = ldw<R>(Wc, c, g, m, off, 0, 0);
+        s[S1(1, off)] = ldw<R>(Wc, c, g, m, 0, off, 0);
+        s[S1(2, off)] = ldw<R>(Wc, c, g, m, 0, 0, off);
+    }
+#pragma unroll
+    for (int sa = 0; sa < 2; ++sa)
+#pragma unroll
+        for (int sb = 0; sb < 2; ++sb) {
+            s[SQ(0, sa, 1, sb)] = ldw<R>(Wc, c, g, m, 2 * sa - 1, 2 * sb - 1, 0);
+            s[SQ(1, sa, 2, sb)] = ldw<R>(Wc, c, g, m, 0, 2 * sa - 1, 2 * sb - 1);
+            s[SQ(0, sa, 2, sb)] = ldw<R>(Wc, c, g, m, 2 * sa - 1, 0, 2 * sb - 1);
+        }
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int d = 0; d < 2; ++d) s[SO(a, b, d)] = ldw<R>(Wc, c, g, m, 2 * a - 1, 2 * b - 1, 2 * d - 1);
+}
+
+// the 24 face traces of one variable into the trace array
+template <typename R>
+__device__ __forceinline__ void store_traces(R* __restrict__ T, const Geo& g, long long e, int c, const R* cf) {
+    R tr[8];
+    R* Tc = T + (long long)c * NTR * g.NE + e;
+    face_traces<R, 0>(cf, tr);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) Tc[(long long)q * g.NE] = tr[q];
+    face_traces<R, 1>(cf, tr);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) Tc[(long long)(8 + q) * g.NE] = tr[q];
+    face_traces<R, 2>(cf, tr);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) Tc[(long long)(16 + q) * g.NE] = tr[q];
+}
+
 template <typename R>
 __global__ void __launch_bounds__(128) k_recon(const double* __restrict__ W, R* __restrict__ T, Geo g, int linear) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
@@ -55,72 +133,117 @@ __global__ void __launch_bounds__(128) k_recon(const double* __restrict__ W, R* 
     if (i > g.nx || j > g.ny) return;
     const int gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny), gk = (k < 0 || k >= g.nz);
     if (gi + gj + gk > 1) return;  // edge/corner ghosts feed no face of an owned cell
-    // boundary maps of the offsets -2..2 along each direction
-    int mi[5], mj[5], mk[5], fi = 0, fj = 0, fk = 0;
-#pragma unroll
-    for (int o = 0; o < 5; ++o) {
-        int f = 0;
-        mi[o] = bmap(i + o - 2, g.nx, g.bc[0], g.bc[1], &f);
-        fi |= f << o;
-        f = 0;
-        mj[o] = bmap(j + o - 2, g.ny, g.bc[2], g.bc[3], &f);
-        fj |= f << o;
-        f = 0;
-        mk[o] = bmap(k + o - 2, g.nz, g.bc[4], g.bc[5], &f);
-        fk |= f << o;
-    }
+    StencilMap m;
+    make_map(g, i, j, k, m);
     const long long e = ext_index(g, i, j, k);
-    const long long sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
-    (void)sx;
 #pragma unroll 1
     for (int c = 0; c < NV; ++c) {
-        const double* Wc = W + (long long)c * g.N;
-        // sign flip of the momentum normal to a reflective boundary
-        const int fm = (c == 1) ? fi : (c == 2) ? fj : (c == 3) ? fk : 0;
-        const int ax = (c == 1) ? 0 : (c == 2) ? 1 : (c == 3) ? 2 : -1;
-        auto ld = [&](int oi, int oj, int ok) -> R {
-            double v = __ldg(Wc + mk[ok + 2] * sz + mj[oj + 2] * sy + mi[oi + 2]);
-            const int o = (ax == 0) ? oi : (ax == 1) ? oj : ok;
-            if (fm && ((fm >> (o + 2)) & 1)) v = -v;
-            return (R)v;
-        };
-        R s[33];
-        s[0] = ld(0, 0, 0);
-#pragma unroll
-        for (int o = 0; o < 4; ++o) {
-            const int off = (o == 0) ? -2 : (o == 1) ? -1 : (o == 2) ? 1 : 2;
-            s[S1(0, off)] = ld(off, 0, 0);
-            s[S1(1, off)] = ld(0, off, 0);
-            s[S1(2, off)] = ld(0, 0, off);
-        }
-#pragma unroll
-        for (int sa = 0; sa < 2; ++sa)
-#pragma unroll
-            for (int sb = 0; sb < 2; ++sb) {
-                s[SQ(0, sa, 1, sb)] = ld(2 * sa - 1, 2 * sb - 1, 0);
-                s[SQ(1, sa, 2, sb)] = ld(0, 2 * sa - 1, 2 * sb - 1);
-                s[SQ(0, sa, 2, sb)] = ld(2 * sa - 1, 0, 2 * sb - 1);
-            }
-#pragma unroll
-        for (int a = 0; a < 2; ++a)
-#pragma unroll
-            for (int b = 0; b < 2; ++b)
-#pragma unroll
-                for (int d = 0; d < 2; ++d) s[SO(a, b, d)] = ld(2 * a - 1, 2 * b - 1, 2 * d - 1);
-        R cf[20];
+        R s[33], cf[20];
+        gather33<R>(W + (long long)c * g.N, c, g, m, s);
         cweno4<R>(s, linear != 0, cf);
-        R tr[8];
-        R* Tc = T + (long long)c * NTR * g.NE + e;
-        face_traces<R, 0>(cf, tr);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) Tc[(long long)q * g.NE] = tr[q];
-        face_traces<R, 1>(cf, tr);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) Tc[(long long)(8 + q) * g.NE] = tr[q];
-        face_traces<R, 2>(cf, tr);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) Tc[(long long)(16 + q) * g.NE] = tr[q];
+        store_traces<R>(T, g, e, c, cf);
     }
+}
+
+// Indicator-gated reconstruction: the network scores the cell from its three
+// directional 5-point stencils; flagged or low-confidence cells take the full
+// CWENO4, the others the linear R4 -- unless the linear traces give a density
+// or pressure below the floors at any face Gauss point, in which case the cell
+// is redone with CWENO4 (positivity fallback).
+template <typename R>
+__global__ void __launch_bounds__(128) k_recon_learned(const double* __restrict__ W, R* __restrict__ T, Geo g,
+                                                       const __nv_bfloat16* __restrict__ pg, float logit_thr, double gm1,
+                                                       unsigned long long* __restrict__ counters) {
+    __shared__ __nv_bfloat16 prm[mlp::NPARAM];
+    __shared__ unsigned cnt[2];
+    for (int q = threadIdx.y * blockDim.x + threadIdx.x; q < mlp::NPARAM; q += blockDim.x * blockDim.y) prm[q] = pg[q];
+    if (threadIdx.x == 0 && threadIdx.y == 0) cnt[0] = cnt[1] = 0;
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+    const int k = blockIdx.z - 1;
+    bool active = !(i > g.nx || j > g.ny);
+    const int gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny), gk = (k < 0 || k >= g.nz);
+    active = active && (gi + gj + gk <= 1);
+    if (active) {
+        StencilMap m;
+        make_map(g, i, j, k, m);
+        const long long e = ext_index(g, i, j, k);
+        float best = -INFINITY;
+#pragma unroll 1
+        for (int d = 0; d < 3; ++d) {
+            float x[mlp::NIN];
+#pragma unroll
+            for (int c = 0; c < NV; ++c) {
+                double s5[5];
+#pragma unroll
+                for (int o = 0; o < 5; ++o)
+                    s5[o] = (double)ldw<double>(W + (long long)c * g.N, c, g, m, d == 0 ? o - 2 : 0, d == 1 ? o - 2 : 0,
+                                                d == 2 ? o - 2 : 0);
+                mlp::normalise5(s5, x + c * 5);
+            }
+            best = fmaxf(best, mlp::forward(prm, x));
+        }
+        bool full = best > logit_thr;
+#pragma unroll 1
+        for (int pass = 0; pass < 2; ++pass) {
+#pragma unroll 1
+            for (int c = 0; c < NV; ++c) {
+                R s[33], cf[20];
+                gather33<R>(W + (long long)c * g.N, c, g, m, s);
+                cweno4<R>(s, !full, cf);
+                store_traces<R>(T, g, e, c, cf);
+            }
+            if (full) break;
+            // admissibility of the linear traces at the 24 face Gauss points
+            bool ok = true;
+            for (int q = 0; q < NTR && ok; ++q) {
+                const double rho = (double)T[((long long)0 * NTR + q) * g.NE + e];
+                const double mx = (double)T[((long long)1 * NTR + q) * g.NE + e];
+                const double my = (double)T[((long long)2 * NTR + q) * g.NE + e];
+                const double mz = (double)T[((long long)3 * NTR + q) * g.NE + e];
+                const double E = (double)T[((long long)4 * NTR + q) * g.NE + e];
+                const double p = gm1 * (E - 0.5 * (mx * mx + my * my + mz * mz) / rho);
+                ok = (rho >= 1.0e-14) && (p >= 1.0e-12);
+            }
+            if (ok) break;
+            full = true;
+            if (!gi && !gj && !gk) atomicAdd(&cnt[1], 1u);
+        }
+        if (full && !gi && !gj && !gk && best > logit_thr) atomicAdd(&cnt[0], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        if (cnt[0]) atomicAdd(&counters[0], (unsigned long long)cnt[0]);
+        if (cnt[1]) atomicAdd(&counters[1], (unsigned long long)cnt[1]);
+    }
+}
+
+// Indicator training data: for every stride-th owned cell, the three directional
+// normalised stencils (X[s][3][25]) and the largest departure of its CWENO4
+// weights from the linear ones over the 5 variables (D[s]).
+__global__ void __launch_bounds__(128) k_features(const double* __restrict__ W, Geo g, long long stride, long long ns,
+                                                  float* __restrict__ X, float* __restrict__ D) {
+    const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (s >= ns) return;
+    const long long cell = s * stride;
+    const int i = (int)(cell % g.nx), j = (int)((cell / g.nx) % g.ny), k = (int)(cell / ((long long)g.nx * g.ny));
+    StencilMap m;
+    make_map(g, i, j, k, m);
+    double dmax = 0.0;
+#pragma unroll 1
+    for (int c = 0; c < NV; ++c) {
+        double st[33], cf[20], dev;
+        gather33<double>(W + (long long)c * g.N, c, g, m, st);
+        cweno4<double>(st, false, cf, &dev);
+        dmax = fmax(dmax, dev);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double s5[5] = {st[S1(d, -2)], st[S1(d, -1)], st[0], st[S1(d, 1)], st[S1(d, 2)]};
+            mlp::normalise5(s5, X + (s * 3 + d) * mlp::NIN + c * 5);
+        }
+    }
+    D[s] = (float)dmax;
 }
 
 __device__ __forceinline__ void atomic_max_pos(unsigned long long* a, double v) {
@@ -221,6 +344,24 @@ __global__ void k_begin_step(DevScalars* ds, int dt_mode, int src_slot, int use_
     ds->t += ds->dt;
 }
 
+// sum |a - b| and sum |b| over n values (two doubles accumulated with atomics)
+__global__ void k_l1(const double* __restrict__ a, const double* __restrict__ b, long long n, double* __restrict__ acc) {
+    double d = 0.0, r = 0.0;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        d += fabs(a[q] - b[q]);
+        r += fabs(b[q]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        d += __shfl_xor_sync(0xffffffffu, d, o);
+        r += __shfl_xor_sync(0xffffffffu, r, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&acc[0], d);
+        atomicAdd(&acc[1], r);
+    }
+}
+
 __global__ void k_reset_slot(DevScalars* ds, int slot) {
     ds->smax_bits[slot] = 0ull;
     ds->bad = ~0ull;
@@ -270,6 +411,10 @@ struct hype_euler {
     DevScalars* ds = nullptr;
     DevScalars* hs = nullptr;  // pinned host copy
     double* pin = nullptr;     // pinned host staging for AoS transfers
+    // learned indicator: BF16 parameters, logit threshold, counters (flagged, positivity fallbacks)
+    __nv_bfloat16* mlp = nullptr;
+    float logit_thr = 0.0f;
+    unsigned long long* mlp_cnt = nullptr;
     // per-kernel event timing inside a timed region (hype_euler_profile)
     bool prof = false;
     std::vector<cudaEvent_t> ev;  // pairs (start, end)
@@ -327,10 +472,18 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
     const bool f32 = e->p.precision == HYPE_PREC_FP32;
     const int lin = e->p.recon == HYPE_RECON_LINEAR4;
     prof_mark(e, 0, true);
-    if (f32)
+    if (e->p.recon == HYPE_RECON_LEARNED) {
+        if (!e->mlp) return HYPE_ERR_ARG;  // hype_euler_set_mlp first
+        const double gm1 = e->p.gamma - 1.0;
+        if (f32)
+            k_recon_learned<float><<<gr, br, 0, e->stream>>>(Win, (float*)e->T, g, e->mlp, e->logit_thr, gm1, e->mlp_cnt);
+        else
+            k_recon_learned<double><<<gr, br, 0, e->stream>>>(Win, (double*)e->T, g, e->mlp, e->logit_thr, gm1, e->mlp_cnt);
+    } else if (f32) {
         k_recon<float><<<gr, br, 0, e->stream>>>(Win, (float*)e->T, g, lin);
-    else
+    } else {
         k_recon<double><<<gr, br, 0, e->stream>>>(Win, (double*)e->T, g, lin);
+    }
     prof_mark(e, 0, false);
     prof_mark(e, 1, true);
     launch_faces(e->g, e->T, e->Fx, e->Fy, e->Fz, e->p.gamma, e->ds, slot, f32, e->p.flux, e->stream);
@@ -357,7 +510,7 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
         if (p->bc[f] < HYPE_BC_PERIODIC || p->bc[f] > HYPE_BC_TRANSMISSIVE) return HYPE_ERR_ARG;
     for (int d = 0; d < 3; ++d)
         if ((p->bc[2 * d] == HYPE_BC_PERIODIC) != (p->bc[2 * d + 1] == HYPE_BC_PERIODIC)) return HYPE_ERR_ARG;
-    if (p->recon != HYPE_RECON_CWENO4 && p->recon != HYPE_RECON_LINEAR4) return HYPE_ERR_ARG;
+    if (p->recon != HYPE_RECON_CWENO4 && p->recon != HYPE_RECON_LINEAR4 && p->recon != HYPE_RECON_LEARNED) return HYPE_ERR_ARG;
     if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32) return HYPE_ERR_ARG;
     if (p->dt_mode < HYPE_DT_MONITOR || p->dt_mode > HYPE_DT_FIXED) return HYPE_ERR_ARG;
     if (p->flux < HYPE_FLUX_RUSANOV || p->flux > HYPE_FLUX_ROTHLLC) return HYPE_ERR_ARG;
@@ -399,7 +552,13 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
     ALLOC(e->Fz, sizeof(double) * NV * (size_t)p->nx * p->ny * (p->nz + 1));
     ALLOC(e->stage_aos, sN);
     ALLOC(e->ds, sizeof(DevScalars));
+    ALLOC(e->mlp_cnt, 2 * sizeof(unsigned long long));
 #undef ALLOC
+    ce = cudaMemset(e->mlp_cnt, 0, 2 * sizeof(unsigned long long));
+    if (ce != cudaSuccess) {
+        set_last_error("cudaMemset", ce);
+        return fail(HYPE_ERR_CUDA);
+    }
     ce = cudaMallocHost((void**)&e->hs, sizeof(DevScalars));
     if (ce != cudaSuccess) {
         set_last_error("cudaMallocHost", ce);
@@ -422,6 +581,7 @@ extern "C" void hype_euler_destroy(hype_euler* e) {
     if (e->stream) cudaStreamSynchronize(e->stream);
     cudaFree(e->U); cudaFree(e->W); cudaFree(e->L); cudaFree(e->S); cudaFree(e->T);
     cudaFree(e->Fx); cudaFree(e->Fy); cudaFree(e->Fz); cudaFree(e->stage_aos); cudaFree(e->ds);
+    cudaFree(e->mlp); cudaFree(e->mlp_cnt);
     if (e->hs) cudaFreeHost(e->hs);
     for (auto x : e->ev) cudaEventDestroy(x);
     if (e->stream) cudaStreamDestroy(e->stream);
@@ -563,6 +723,59 @@ extern "C" int hype_euler_step(hype_euler* e, int nsteps, double* t_inout, doubl
 
 extern "C" void* hype_euler_stream(hype_euler* e) { return e ? (void*)e->stream : nullptr; }
 
+extern "C" int hype_euler_set_mlp(hype_euler* e, const float* params, float prob_threshold) {
+    if (!e || !params || !(prob_threshold > 0.0f) || !(prob_threshold < 1.0f)) return HYPE_ERR_ARG;
+    std::vector<__nv_bfloat16> h(mlp::NPARAM);
+    for (int q = 0; q < mlp::NPARAM; ++q) h[q] = __float2bfloat16_rn(params[q]);
+    if (!e->mlp) HYPE_CK(cudaMalloc((void**)&e->mlp, sizeof(__nv_bfloat16) * mlp::NPARAM));
+    HYPE_CK(cudaMemcpyAsync(e->mlp, h.data(), sizeof(__nv_bfloat16) * mlp::NPARAM, cudaMemcpyHostToDevice, e->stream));
+    HYPE_CK(cudaStreamSynchronize(e->stream));
+    e->logit_thr = logf(prob_threshold / (1.0f - prob_threshold));
+    return HYPE_OK;
+}
+
+extern "C" int hype_euler_indicator_stats(hype_euler* e, long long* flagged, long long* positivity_fallbacks, int reset) {
+    if (!e) return HYPE_ERR_ARG;
+    unsigned long long c[2];
+    HYPE_CK(cudaMemcpyAsync(c, e->mlp_cnt, sizeof(c), cudaMemcpyDeviceToHost, e->stream));
+    HYPE_CK(cudaStreamSynchronize(e->stream));
+    if (flagged) *flagged = (long long)c[0];
+    if (positivity_fallbacks) *positivity_fallbacks = (long long)c[1];
+    if (reset) HYPE_CK(cudaMemsetAsync(e->mlp_cnt, 0, sizeof(c), e->stream));
+    return HYPE_OK;
+}
+
+extern "C" int hype_euler_set_recon(hype_euler* e, int recon) {
+    if (!e || recon < HYPE_RECON_CWENO4 || recon > HYPE_RECON_LEARNED) return HYPE_ERR_ARG;
+    HYPE_CK(cudaStreamSynchronize(e->stream));
+    e->p.recon = recon;
+    return HYPE_OK;
+}
+
+extern "C" int hype_euler_sample_features(hype_euler* e, long long stride, float* X, float* D, long long* ns_out) {
+    if (!e || stride < 1 || !X || !D) return HYPE_ERR_ARG;
+    const long long ns = (e->g.N + stride - 1) / stride;
+    float *dX = nullptr, *dD = nullptr;
+    cudaError_t ce = cudaMalloc((void**)&dX, sizeof(float) * ns * 3 * mlp::NIN);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&dD, sizeof(float) * ns);
+    if (ce == cudaSuccess) {
+        k_features<<<cdiv(ns, 128), 128, 0, e->stream>>>(e->U, e->g, stride, ns, dX, dD);
+        count_launch(1);
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(X, dX, sizeof(float) * ns * 3 * mlp::NIN, cudaMemcpyDeviceToHost, e->stream);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(D, dD, sizeof(float) * ns, cudaMemcpyDeviceToHost, e->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+    cudaFree(dX);
+    cudaFree(dD);
+    if (ce != cudaSuccess) {
+        set_last_error("hype_euler_sample_features", ce);
+        return HYPE_ERR_CUDA;
+    }
+    if (ns_out) *ns_out = ns;
+    return HYPE_OK;
+}
+
 extern "C" int hype_euler_profile(hype_euler* e, int enable) {
     if (!e) return HYPE_ERR_ARG;
     HYPE_CK(cudaStreamSynchronize(e->stream));
@@ -692,5 +905,34 @@ extern "C" int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* 
         *dt_out = (1.0 / 3.0) * (p->cfl * p->h) / (bits_to_double(w[0]) + 0.0);
         if (w[1] != ~0ull) return HYPE_ERR_STATE;
     }
+    return HYPE_OK;
+}
+
+// One step of the current reconstruction and, from the same state, one full-CWENO4
+// step; keeps the first, returns the relative L1 difference of the densities.
+extern "C" int hype_euler_shadow_step(hype_euler* e, double* t_inout, double* dt_inout, double* l1_rel) {
+    if (!e || !t_inout || !dt_inout || !l1_rel) return HYPE_ERR_ARG;
+    const size_t bytes = sizeof(double) * NV * (size_t)e->g.N;
+    const int recon = e->p.recon;
+    const double t0 = *t_inout, dt0 = *dt_inout;
+    HYPE_CK(cudaMemcpyAsync(e->S, e->U, bytes, cudaMemcpyDeviceToDevice, e->stream));
+    e->p.recon = HYPE_RECON_CWENO4;
+    double t = t0, dt = dt0;
+    int rc = hype_euler_step(e, 1, &t, &dt, nullptr);
+    e->p.recon = recon;
+    if (rc) return rc;
+    HYPE_CK(cudaMemcpyAsync(e->L, e->U, sizeof(double) * (size_t)e->g.N, cudaMemcpyDeviceToDevice, e->stream));
+    HYPE_CK(cudaMemcpyAsync(e->U, e->S, bytes, cudaMemcpyDeviceToDevice, e->stream));
+    *t_inout = t0;
+    *dt_inout = dt0;
+    if ((rc = hype_euler_step(e, 1, t_inout, dt_inout, nullptr))) return rc;
+    double* acc = (double*)e->Fx;  // scratch: the face fluxes are rebuilt by the next RHS
+    HYPE_CK(cudaMemsetAsync(acc, 0, 2 * sizeof(double), e->stream));
+    k_l1<<<608, 256, 0, e->stream>>>(e->U, e->L, e->g.N, acc);
+    HYPE_LAUNCHED(1);
+    double h[2];
+    HYPE_CK(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, e->stream));
+    HYPE_CK(cudaStreamSynchronize(e->stream));
+    *l1_rel = h[0] / h[1];
     return HYPE_OK;
 }

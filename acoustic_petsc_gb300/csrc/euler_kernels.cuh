@@ -57,7 +57,7 @@ struct Weights;
 // CWENO4 coefficients (20) of one variable from its 33-point stencil.
 // linear: the R4 polynomial (the limit in which all nonlinear weights equal the linear ones).
 template <typename R>
-__device__ __forceinline__ void cweno4(const R* __restrict__ s, bool linear, R* __restrict__ cf) {
+__device__ __forceinline__ void cweno4(const R* __restrict__ s, bool linear, R* __restrict__ cf, R* wdev = nullptr) {
     const R u0 = s[0];
     const R h = R(0.5), q = R(0.25);
     R d4[3], dd4[3], ddd4[3];
@@ -93,6 +93,7 @@ __device__ __forceinline__ void cweno4(const R* __restrict__ s, bool linear, R* 
         }
         cf[7] = xy4; cf[8] = yz4; cf[9] = xz4;
         cf[13] = xxy; cf[14] = xyy; cf[15] = yyz; cf[16] = yzz; cf[17] = xxz; cf[18] = xzz; cf[19] = xyz;
+        if (wdev) *wdev = R(0);
         return;
     }
     const R r13_3 = R(13. / 3.), r7_6 = R(7. / 6.);
@@ -149,6 +150,12 @@ __device__ __forceinline__ void cweno4(const R* __restrict__ s, bool linear, R* 
     R w4, w0, ws[6];
     Weights<R>::compute(IS4, IS0, IS3, gH, g0, gs, w4, w0, ws);
     const R wr = w4 / gH;
+    if (wdev) {  // largest departure of a nonlinear weight from its linear value (indicator labels)
+        R d = fmax(fabs(w4 - gH), fabs(w0 - g0));
+#pragma unroll
+        for (int m = 0; m < 6; ++m) d = fmax(d, fabs(ws[m] - gs));
+        *wdev = d;
+    }
     // linear and nonlinear R3 combinations of every quantity; the weight of the
     // centred value is summed from the stencils that keep it (all weights are positive)
     const R wx = ws[0] + ws[1], wy = ws[2] + ws[3], wz = ws[4] + ws[5];

@@ -119,6 +119,31 @@ class EulerSolver:
     def device_state_ptr(self) -> int:
         return int(L.lib().hype_euler_state_device(self._h))
 
+    # ---- learned troubled-cell indicator (no counterpart in the reference) ----
+    def set_mlp(self, params: np.ndarray, prob_threshold: float = 0.2) -> None:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        check(L.lib().hype_euler_set_mlp(self._h, p.ctypes.data_as(L.F), float(prob_threshold)), "hype_euler_set_mlp")
+
+    def set_recon(self, recon: int) -> None:
+        check(L.lib().hype_euler_set_recon(self._h, int(recon)), "hype_euler_set_recon")
+        self.ctx.recon = recon
+
+    def indicator_stats(self, reset: bool = True):
+        f, b = C.c_longlong(), C.c_longlong()
+        check(L.lib().hype_euler_indicator_stats(self._h, C.byref(f), C.byref(b), int(reset)), "indicator_stats")
+        return f.value, b.value
+
+    def shadow_step(self) -> float:
+        """One step with the current reconstruction (the learned indicator) and, from the
+        same state, one full-CWENO4 step (the shadow); the learned result is kept.
+        Returns the relative L1 difference of the densities of the two."""
+        t = C.c_double(self.t)
+        d = C.c_double(self.next_dt)
+        l1 = C.c_double()
+        check(L.lib().hype_euler_shadow_step(self._h, C.byref(t), C.byref(d), C.byref(l1)), "hype_euler_shadow_step")
+        self.t, self.next_dt = t.value, d.value
+        return l1.value
+
     def sync(self):
         check(L.lib().hype_euler_sync(self._h), "hype_euler_sync")
 

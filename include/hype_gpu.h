@@ -46,6 +46,10 @@ extern "C" {
 #define HYPE_RECON_CWENO4 0  /* nonlinear CWENO4, gammaHi=gammaLo=0.85
                                 (3d/weno4/Viscous-Multiphase-Fourth-Order/reconstruction.c:38-259) */
 #define HYPE_RECON_LINEAR4 1 /* the optimal-weight limit: the 4th-order central polynomial R4 */
+#define HYPE_RECON_LEARNED 2 /* no counterpart in the reference: a small network (hype_euler_set_mlp) scores
+                                each cell from its normalised 5-point stencils; flagged or low-confidence
+                                cells take CWENO4, the others R4, and any cell whose R4 face traces break
+                                density/pressure positivity is redone with CWENO4 */
 
 /* numerical flux across each face Gauss point (3d/weno4/Navier-Stokes-3D/pde.c) */
 #define HYPE_FLUX_RUSANOV 0  /* PDELLFRiemannSolver, pde.c:164-187 */
@@ -123,6 +127,24 @@ void* hype_euler_stream(hype_euler* e);
  * [2] divergence + stage update since the last enable. */
 int hype_euler_profile(hype_euler* e, int enable);
 int hype_euler_profile_read(hype_euler* e, double* ms, long long* count);
+
+/* ---- learned troubled-cell indicator (no counterpart in the reference) ----
+ * Network 25 -> 32 -> 32 -> 1 (ReLU), BF16 weights, FP32 accumulation; params are
+ * hype_mlp_nparam() FP32 values W1[32][25] b1[32] W2[32][32] b2[32] W3[32] b3. A cell
+ * is flagged when the sigmoid of the max of its three directional logits exceeds
+ * prob_threshold (a low threshold sends low-confidence cells to CWENO4). */
+int hype_euler_set_mlp(hype_euler* e, const float* params, float prob_threshold);
+/* switch the reconstruction (HYPE_RECON_*) of an existing context, e.g. for a full-WENO shadow step */
+int hype_euler_set_recon(hype_euler* e, int recon);
+/* counts of owned cells sent to CWENO4 by the network / by the positivity fallback since the last reset */
+int hype_euler_indicator_stats(hype_euler* e, long long* flagged, long long* positivity_fallbacks, int reset);
+/* training samples from the resident state: every stride-th owned cell, its three
+ * directional normalised stencils X[s][3][25] and the largest departure D[s] of its
+ * CWENO4 nonlinear weights from the linear ones (labels: D > threshold). */
+int hype_euler_sample_features(hype_euler* e, long long stride, float* X, float* D, long long* ns_out);
+/* Shadow step: one step with the context's reconstruction and, from the same state,
+ * one full-CWENO4 step; the first result is kept, *l1_rel = sum|rho - rho_full| / sum|rho_full|. */
+int hype_euler_shadow_step(hype_euler* e, double* t_inout, double* dt_inout, double* l1_rel);
 
 /* Allocation-free RHS evaluation.  This entry point has no counterpart in the
  * reference.  It serves callers that cannot let the library allocate device
@@ -247,6 +269,16 @@ int hype_batch_get(hype_batch* b, int q, double* p_old, double* p);
 /* nsteps of every instance; graph=1 replays a captured CUDA graph of the step */
 int hype_batch_step(hype_batch* b, int nsteps, int graph);
 int hype_batch_sync(hype_batch* b);
+
+/* ============================================================ indicator training */
+int hype_mlp_nparam(void);
+/* max-pooled logits of n cells (X[n][3][25]) */
+int hype_mlp_score(const float* X, int n, const float* params, float* score);
+/* summed BCE loss (positive-class weight) and its gradient over n cells, BF16 forward, FP32 accumulation */
+int hype_mlp_grad(const float* X, const float* y, int n, const float* params, float pos_weight, float* grad, double* loss);
+/* Adam on seeded shuffled minibatches; params updated in place; mean loss of the last epoch */
+int hype_mlp_train(const float* X, const float* y, int n, float* params, int epochs, int batch, float lr, float pos_weight,
+                   unsigned seed, double* final_loss);
 
 /* ============================================================ misc */
 /* Select the CUDA device that later hype_*_create calls of this thread use. */
