@@ -56,7 +56,8 @@ class EulerParams(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
                 ("x_min", C.c_double), ("y_min", C.c_double), ("z_min", C.c_double), ("h", C.c_double),
                 ("cfl", C.c_double), ("gamma", C.c_double), ("bc", C.c_int * 6),
-                ("recon", C.c_int), ("precision", C.c_int), ("dt_mode", C.c_int), ("flux", C.c_int)]
+                ("recon", C.c_int), ("precision", C.c_int), ("dt_mode", C.c_int), ("flux", C.c_int),
+                ("positivity", C.c_int)]
 
 
 class Mp2dParams(C.Structure):

@@ -125,8 +125,38 @@ __device__ __forceinline__ void store_traces(R* __restrict__ T, const Geo& g, lo
     for (int q = 0; q < 8; ++q) Tc[(long long)(16 + q) * g.NE] = tr[q];
 }
 
+// density and pressure at the 24 face Gauss-point traces of one cell (what the
+// Riemann solver consumes) against the floors of pde.c:56-66
 template <typename R>
-__global__ void __launch_bounds__(128) k_recon(const double* __restrict__ W, R* __restrict__ T, Geo g, int linear) {
+__device__ __forceinline__ bool traces_admissible(const R* __restrict__ T, const Geo& g, long long e, double gm1) {
+    for (int q = 0; q < NTR; ++q) {
+        const double rho = (double)T[((long long)0 * NTR + q) * g.NE + e];
+        const double mx = (double)T[((long long)1 * NTR + q) * g.NE + e];
+        const double my = (double)T[((long long)2 * NTR + q) * g.NE + e];
+        const double mz = (double)T[((long long)3 * NTR + q) * g.NE + e];
+        const double E = (double)T[((long long)4 * NTR + q) * g.NE + e];
+        const double p = gm1 * (E - 0.5 * (mx * mx + my * my + mz * mz) / rho);
+        if (!(rho >= 1.0e-14) || !(p >= 1.0e-12)) return false;
+    }
+    return true;
+}
+
+// first-order traces (all higher coefficients zero): the fallback of
+// 3d/weno4/Viscous-Multiphase-Fourth-Order/rhs_function.c:297-305
+template <typename R>
+__device__ __forceinline__ void store_first_order(const double* __restrict__ W, R* __restrict__ T, const Geo& g,
+                                                  const StencilMap& m, long long e) {
+#pragma unroll 1
+    for (int c = 0; c < NV; ++c) {
+        const R v = ldw<R>(W + (long long)c * g.N, c, g, m, 0, 0, 0);
+        R* Tc = T + (long long)c * NTR * g.NE + e;
+        for (int q = 0; q < NTR; ++q) Tc[(long long)q * g.NE] = v;
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_recon(const double* __restrict__ W, R* __restrict__ T, Geo g, int linear,
+                                               int pad, double gm1, unsigned long long* __restrict__ counters) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
     const int k = blockIdx.z - 1;
@@ -143,6 +173,10 @@ __global__ void __launch_bounds__(128) k_recon(const double* __restrict__ W, R* 
         cweno4<R>(s, linear != 0, cf);
         store_traces<R>(T, g, e, c, cf);
     }
+    if (pad && !traces_admissible<R>(T, g, e, gm1)) {
+        store_first_order<R>(W, T, g, m, e);
+        if (!gi && !gj && !gk) atomicAdd(&counters[1], 1ull);
+    }
 }
 
 // Indicator-gated reconstruction: the network scores the cell from its three
@@ -153,7 +187,7 @@ __global__ void __launch_bounds__(128) k_recon(const double* __restrict__ W, R* 
 template <typename R>
 __global__ void __launch_bounds__(128) k_recon_learned(const double* __restrict__ W, R* __restrict__ T, Geo g,
                                                        const __nv_bfloat16* __restrict__ pg, float logit_thr, double gm1,
-                                                       unsigned long long* __restrict__ counters) {
+                                                       int pad, unsigned long long* __restrict__ counters) {
     __shared__ __nv_bfloat16 prm[mlp::NPARAM];
     __shared__ unsigned cnt[2];
     for (int q = threadIdx.y * blockDim.x + threadIdx.x; q < mlp::NPARAM; q += blockDim.x * blockDim.y) prm[q] = pg[q];
@@ -194,21 +228,15 @@ __global__ void __launch_bounds__(128) k_recon_learned(const double* __restrict_
                 cweno4<R>(s, !full, cf);
                 store_traces<R>(T, g, e, c, cf);
             }
-            if (full) break;
-            // admissibility of the linear traces at the 24 face Gauss points
-            bool ok = true;
-            for (int q = 0; q < NTR && ok; ++q) {
-                const double rho = (double)T[((long long)0 * NTR + q) * g.NE + e];
-                const double mx = (double)T[((long long)1 * NTR + q) * g.NE + e];
-                const double my = (double)T[((long long)2 * NTR + q) * g.NE + e];
-                const double mz = (double)T[((long long)3 * NTR + q) * g.NE + e];
-                const double E = (double)T[((long long)4 * NTR + q) * g.NE + e];
-                const double p = gm1 * (E - 0.5 * (mx * mx + my * my + mz * mz) / rho);
-                ok = (rho >= 1.0e-14) && (p >= 1.0e-12);
+            if (traces_admissible<R>(T, g, e, gm1)) break;
+            if (full) {  // CWENO4 itself inadmissible: first order (when enabled)
+                if (pad) {
+                    store_first_order<R>(W, T, g, m, e);
+                    if (!gi && !gj && !gk) atomicAdd(&cnt[1], 1u);
+                }
+                break;
             }
-            if (ok) break;
-            full = true;
-            if (!gi && !gj && !gk) atomicAdd(&cnt[1], 1u);
+            full = true;  // the R4 traces broke positivity: redo the cell with CWENO4
         }
         if (full && !gi && !gj && !gk && best > logit_thr) atomicAdd(&cnt[0], 1u);
     }
@@ -476,13 +504,15 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
         if (!e->mlp) return HYPE_ERR_ARG;  // hype_euler_set_mlp first
         const double gm1 = e->p.gamma - 1.0;
         if (f32)
-            k_recon_learned<float><<<gr, br, 0, e->stream>>>(Win, (float*)e->T, g, e->mlp, e->logit_thr, gm1, e->mlp_cnt);
+            k_recon_learned<float><<<gr, br, 0, e->stream>>>(Win, (float*)e->T, g, e->mlp, e->logit_thr, gm1, e->p.positivity,
+                                                             e->mlp_cnt);
         else
-            k_recon_learned<double><<<gr, br, 0, e->stream>>>(Win, (double*)e->T, g, e->mlp, e->logit_thr, gm1, e->mlp_cnt);
+            k_recon_learned<double><<<gr, br, 0, e->stream>>>(Win, (double*)e->T, g, e->mlp, e->logit_thr, gm1,
+                                                              e->p.positivity, e->mlp_cnt);
     } else if (f32) {
-        k_recon<float><<<gr, br, 0, e->stream>>>(Win, (float*)e->T, g, lin);
+        k_recon<float><<<gr, br, 0, e->stream>>>(Win, (float*)e->T, g, lin, e->p.positivity, e->p.gamma - 1.0, e->mlp_cnt);
     } else {
-        k_recon<double><<<gr, br, 0, e->stream>>>(Win, (double*)e->T, g, lin);
+        k_recon<double><<<gr, br, 0, e->stream>>>(Win, (double*)e->T, g, lin, e->p.positivity, e->p.gamma - 1.0, e->mlp_cnt);
     }
     prof_mark(e, 0, false);
     prof_mark(e, 1, true);
@@ -514,6 +544,7 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
     if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32) return HYPE_ERR_ARG;
     if (p->dt_mode < HYPE_DT_MONITOR || p->dt_mode > HYPE_DT_FIXED) return HYPE_ERR_ARG;
     if (p->flux < HYPE_FLUX_RUSANOV || p->flux > HYPE_FLUX_ROTHLLC) return HYPE_ERR_ARG;
+    if (p->positivity != 0 && p->positivity != 1) return HYPE_ERR_ARG;
     hype_euler* e = new hype_euler();
     e->p = *p;
     Geo& g = e->g;
@@ -889,9 +920,9 @@ extern "C" int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* 
     const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2);
     const int lin = p->recon == HYPE_RECON_LINEAR4;
     if (p->precision == HYPE_PREC_FP32)
-        k_recon<float><<<gr, br, 0, s>>>(dU, (float*)T, g, lin);
+        k_recon<float><<<gr, br, 0, s>>>(dU, (float*)T, g, lin, 0, p->gamma - 1.0, nullptr);
     else
-        k_recon<double><<<gr, br, 0, s>>>(dU, (double*)T, g, lin);
+        k_recon<double><<<gr, br, 0, s>>>(dU, (double*)T, g, lin, 0, p->gamma - 1.0, nullptr);
     launch_faces(g, T, Fx, Fy, Fz, p->gamma, ds, 4, p->precision == HYPE_PREC_FP32, p->flux, s);
     const Stage st{0.0, 0.0, 0.0, 1};
     const dim3 bu(32, 8), gu(cdiv(g.nx, 32), cdiv(g.ny, 8), g.nz);

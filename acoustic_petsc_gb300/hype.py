@@ -47,6 +47,7 @@ class AppCtx:
     precision: int = L.PREC_FP64
     dt_mode: int = L.DT_MONITOR
     flux: int = L.FLUX_RUSANOV
+    positivity: int = 0  # 1: first-order fallback on inadmissible face traces
     dt: float = 0.0  # the reference's Ctx->dt output of RHSFunction
 
     def params(self) -> L.EulerParams:
@@ -57,6 +58,7 @@ class AppCtx:
         for q in range(6):
             p.bc[q] = int(self.boundaries[q])
         p.recon, p.precision, p.dt_mode, p.flux = self.recon, self.precision, self.dt_mode, self.flux
+        p.positivity = self.positivity
         return p
 
 

@@ -424,7 +424,108 @@ def run_mp2d(args, ws, rank, local, n=1024, precision=0, model=1):
             "gpu_launches": launches, "clocks": clk.summary()}
 
 
+def run_blast(args, ws, rank, local, n=512, ntrain=64, tau=0.05, prob=0.2):
+    """3D Euler blast at scale: learned troubled-cell indicator + FP32 reconstruction/flux
+    vs the plain full-CWENO4 forms (FP32 and FP64) on the same GPU."""
+    import torch
+
+    import acoustic_petsc_gb300 as H
+    from acoustic_petsc_gb300 import indicator, workloads
+
+    L = H.lib()
+    H._lib.check(L.hype_set_device(local), "hype_set_device")
+    torch.cuda.set_device(local)
+    # 1. labels from the solver itself on a small run of the same problem, trained on the GPU
+    tr = H.EulerSolver(H.AppCtx(N_x=ntrain, N_y=ntrain, N_z=ntrain, h=1.0 / ntrain, CFL=0.4, positivity=1,
+                                precision=H._lib.PREC_FP32))
+    tr.set_state(workloads.euler_blast(ntrain))
+    Xs, Ds = [], []
+    for _ in range(6):
+        tr.step(4)
+        X, D = indicator.sample(tr)
+        Xs.append(X)
+        Ds.append(D)
+    tr.close()
+    X, D = np.concatenate(Xs), np.concatenate(Ds)
+    y = indicator.labels(D, tau)
+    t0 = time.perf_counter()
+    params, loss = indicator.train(X, y, epochs=10, batch=4096, lr=3e-3, seed=0)
+    t_train = time.perf_counter() - t0
+    recall, precision, flagged_train = indicator.recall_precision(indicator.score(X, params), y, prob)
+    # 2. the 512^3 runs (one context, reconstruction switched between the forms)
+    U0 = workloads.euler_blast(n)
+    cells = n**3
+    res = {}
+    ctx = H.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, positivity=1, precision=H._lib.PREC_FP32,
+                   recon=H._lib.RECON_CWENO4)
+    s = H.EulerSolver(ctx)
+    s.set_mlp(params, prob)
+    stream = torch.cuda.ExternalStream(L.hype_euler_stream(s._h))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    rho = {}
+    clocks = None
+    launches = 0
+    for form, recon in (("plain_fp32", H._lib.RECON_CWENO4), ("learned_fp32", H._lib.RECON_LEARNED)):
+        s.set_recon(recon)
+        s.set_state(U0)
+        s.t, s.next_dt = 0.0, 0.0
+        s.step(max(args.warmup, 3))
+        s.indicator_stats(reset=True)
+        l0 = H.launches()
+        torch.cuda.synchronize()
+        with Clocks(_gpu_index(local)) as clk:
+            e0.record(stream)
+            s.step(args.steps)
+            e1.record(stream)
+            e1.synchronize()
+        ms = _max_over_ranks(ws, e0.elapsed_time(e1))
+        flagged, fb = s.indicator_stats(reset=True)
+        res[form] = {"value": ws * cells * args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
+                     "flagged_per_cell_stage": flagged / (4.0 * cells * args.steps),
+                     "positivity_fallback_rate": fb / (4.0 * cells * args.steps)}
+        rho[form] = s.get_state()[..., 0]
+        if form == "learned_fp32":
+            clocks = clk.summary()
+            launches = H.launches() - l0
+    l1 = float(np.abs(rho["learned_fp32"] - rho["plain_fp32"]).mean() / np.abs(rho["plain_fp32"]).mean())
+    s.close()
+    del rho
+    # 3. the plain FP64 form, one timed step (FP64 traces: 130 GB of scratch)
+    s64 = H.EulerSolver(H.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, positivity=1))
+    s64.set_state(U0)
+    s64.step(1)
+    stream = torch.cuda.ExternalStream(L.hype_euler_stream(s64._h))
+    e0.record(stream)
+    s64.step(1)
+    e1.record(stream)
+    e1.synchronize()
+    ms64 = e0.elapsed_time(e1)
+    s64.close()
+    res["plain_fp64"] = {"value": ws * cells / (ms64 * 1e-3), "ms_per_step": ms64}
+    v = res["learned_fp32"]["value"]
+    peak, kind = _peaks()
+    ach = EULER_BYTES_PER_CELL_UPDATE * v / ws / 1e9
+    return {"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": res["learned_fp32"]["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 state / f32 recon+flux, bf16 indicator",
+            "data": "synthetic: spherical blast p ratio 10, rho ratio 8, r0 0.1, seeded 1e-3 pressure noise",
+            "config": {"workload": f"euler3d_blast_{n}_learned_indicator", "grid": [n, n, n], "cfl": 0.4,
+                       "positivity_fallback": "first order at inadmissible face traces",
+                       "indicator": {"train_grid": ntrain, "samples": int(X.shape[0]), "tau": tau,
+                                     "prob_threshold": prob, "train_s": t_train, "final_loss": loss,
+                                     "recall": recall, "precision": precision, "flagged_train": flagged_train}},
+            "forms": res,
+            "speedup_vs_plain_fp32": v / res["plain_fp32"]["value"],
+            "speedup_vs_plain_fp64": v / res["plain_fp64"]["value"],
+            "l1_rho_learned_vs_plain_fp32": l1,
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "traffic": None},
+            "gpu_launches": launches, "clocks": clocks}
+
+
 WORKLOADS = {
+    "blast512": run_blast,
+    "blast256": lambda a, *r: run_blast(a, *r, n=256),
     "kapila1024": lambda a, *r: run_mp2d(a, *r, precision=0),
     "kapila1024_fp32": lambda a, *r: run_mp2d(a, *r, precision=1),
     "euler256_hllc": lambda a, *r: run_euler(a, *r, precision=0, recon=0, flux=1),

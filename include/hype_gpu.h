@@ -79,6 +79,11 @@ typedef struct {
     int precision;                 /* HYPE_PREC_* */
     int dt_mode;                   /* HYPE_DT_* */
     int flux;                      /* HYPE_FLUX_* (0 = Rusanov) */
+    int positivity;                /* 0: an inadmissible face trace is an error (the reference aborts,
+                                      pde.c:56-66); 1: the cell drops to first order, the fallback of
+                                      3d/weno4/Viscous-Multiphase-Fourth-Order/rhs_function.c:297-305, checked
+                                      at the 24 face Gauss-point traces the flux uses; counted in
+                                      hype_euler_indicator_stats */
 } hype_euler_params;
 
 typedef struct {

@@ -668,7 +668,35 @@ static void gather(const Padded* P, int i, int j, int k, int c, Stencil* s) {
 }
 
 /* traces of one cell: tr[c*NTR + f*4 + g], faces 0..5 = -x,+x,-y,+y,-z,+z */
+static void cell_traces_raw(const Padded* P, int i, int j, int k, double gam, int linear, double* tr);
+
+/* optional first-order fallback (positivity = 1): when a face trace has rho < 1e-14
+ * or p < 1e-12 the cell is reconstructed at first order, the rule of
+ * 3d/weno4/Viscous-Multiphase-Fourth-Order/rhs_function.c:297-305 applied at the traces */
+static int g_positivity = 0;
+static long g_fallbacks = 0;
+
 static void cell_traces(const Padded* P, int i, int j, int k, double gam, int linear, double* tr) {
+    cell_traces_raw(P, i, j, k, gam, linear, tr);
+    if (!g_positivity) return;
+    const double gm1 = P->g->gamma - 1.0;
+    for (int q = 0; q < NTR; ++q) {
+        const double rho = tr[0 * NTR + q], mx = tr[1 * NTR + q], my = tr[2 * NTR + q], mz = tr[3 * NTR + q],
+                     E = tr[4 * NTR + q];
+        const double p = gm1 * (E - 0.5 * (mx * mx + my * my + mz * mz) / rho);
+        if (!(rho >= 1.0e-14) || !(p >= 1.0e-12)) {
+            for (int c = 0; c < NV; ++c)
+                for (int qq = 0; qq < NTR; ++qq) tr[c * NTR + qq] = padp(P, i, j, k)[c];
+            if (i >= 0 && i < P->g->nx && j >= 0 && j < P->g->ny && k >= 0 && k < P->g->nz) {
+#pragma omp atomic
+                ++g_fallbacks;
+            }
+            return;
+        }
+    }
+}
+
+static void cell_traces_raw(const Padded* P, int i, int j, int k, double gam, int linear, double* tr) {
     Stencil s;
     double coef[20];
     for (int c = 0; c < NV; ++c) {
@@ -719,6 +747,7 @@ int orc_euler_rhs(const orc_euler_cfg* g, const double* U, double* RHS, double* 
     const int linear = g->recon == 1;
     const double r1_h = 1. / (g->h);
     g_flux_kind = g->flux;
+    g_positivity = g->positivity;
 #ifdef _OPENMP
     if (g->nthreads > 0) omp_set_num_threads(g->nthreads);
 #endif
@@ -871,4 +900,10 @@ out:
     if (t_inout) *t_inout = t;
     if (dt_inout) *dt_inout = dt;
     return rc;
+}
+
+long orc_positivity_fallbacks(int reset) {
+    long v = g_fallbacks;
+    if (reset) g_fallbacks = 0;
+    return v;
 }

@@ -57,7 +57,9 @@ typedef struct {
     int recon; /* 0 = CWENO4 (gamma 0.85), 1 = linear R4 (the optimal-weight polynomial) */
     int nthreads;
     int flux;  /* 0 = Rusanov (LLF), 1 = HLLC, 2 = rotated HLLC (Navier-Stokes-3D/pde.c:164-384) */
+    int positivity; /* 1: first-order fallback of cells with an inadmissible face trace */
 } orc_euler_cfg;
+long orc_positivity_fallbacks(int reset);
 int orc_euler_rhs(const orc_euler_cfg* cfg, const double* U, double* RHS, double* smax_out, long* bad);
 /* SSPRK(4,3) steps with dt semantics: dt_mode 0 -> dt refreshed each step from
  * the last stage RHS (Navier-Stokes-3D monitor), 1 -> frozen at the initial RHS

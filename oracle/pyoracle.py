@@ -43,7 +43,8 @@ class EulerCfg(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
                 ("xmin", C.c_double), ("ymin", C.c_double), ("zmin", C.c_double),
                 ("h", C.c_double), ("cfl", C.c_double), ("gamma", C.c_double),
-                ("bc", C.c_int * 6), ("recon", C.c_int), ("nthreads", C.c_int), ("flux", C.c_int)]
+                ("bc", C.c_int * 6), ("recon", C.c_int), ("nthreads", C.c_int), ("flux", C.c_int),
+                ("positivity", C.c_int)]
 
 
 class CtcsCfg(C.Structure):
@@ -81,6 +82,8 @@ def lib():
         L.orc_rusanov.argtypes = [D, D, C.c_int, C.c_double, D, C.POINTER(C.c_int)]
         L.orc_rusanov.restype = C.c_double
         L.orc_threads.restype = C.c_int
+        L.orc_positivity_fallbacks.argtypes = [C.c_int]
+        L.orc_positivity_fallbacks.restype = C.c_long
         _lib = L
     return _lib
 
@@ -89,7 +92,8 @@ def threads() -> int:
     return lib().orc_threads()
 
 
-def euler_cfg(n, h, cfl=0.4, gamma=1.4, bc=(0,) * 6, origin=(0.0, 0.0, 0.0), recon=0, nthreads=0, flux=0):
+def euler_cfg(n, h, cfl=0.4, gamma=1.4, bc=(0,) * 6, origin=(0.0, 0.0, 0.0), recon=0, nthreads=0, flux=0,
+              positivity=0):
     nx, ny, nz = (n, n, n) if isinstance(n, int) else n
     c = EulerCfg()
     c.nx, c.ny, c.nz = nx, ny, nz
@@ -97,7 +101,7 @@ def euler_cfg(n, h, cfl=0.4, gamma=1.4, bc=(0,) * 6, origin=(0.0, 0.0, 0.0), rec
     c.h, c.cfl, c.gamma = h, cfl, gamma
     for q in range(6):
         c.bc[q] = bc[q]
-    c.recon, c.nthreads, c.flux = recon, nthreads, flux
+    c.recon, c.nthreads, c.flux, c.positivity = recon, nthreads, flux, positivity
     return c
 
 

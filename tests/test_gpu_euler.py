@@ -228,3 +228,23 @@ def test_rothllc_at_reflective_walls(hype):
     err = np.abs(R - z["RHS"]).max(axis=-1)
     scale = np.abs(z["RHS"]).max()
     assert err[interior].max() <= TOL_STEP * scale
+
+
+def test_blast_positivity_fallback_vs_oracle(hype, oracle):
+    """Pressure-ratio-10 blast: the CWENO4 traces break positivity next to the shock;
+    with the first-order fallback the run proceeds and matches the CPU checker."""
+    from acoustic_petsc_gb300 import workloads
+
+    n = 20
+    U0 = workloads.euler_blast(n)
+    ctx = hype.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, positivity=1)
+    s = hype.EulerSolver(ctx)
+    s.set_state(U0)
+    s.step(6)
+    flagged, fallbacks = s.indicator_stats()
+    cfg = oracle.euler_cfg(n, 1.0 / n, cfl=0.4, positivity=1)
+    oracle.lib().orc_positivity_fallbacks(1)
+    Uo, t, dt, rc = oracle.euler_run(cfg, U0, 6)
+    assert rc == 0
+    assert rel(s.get_state(), Uo) <= TOL_RUN
+    print(f"blast {n}^3: {fallbacks} GPU cell-stage fallbacks, oracle {oracle.lib().orc_positivity_fallbacks(1)}")

@@ -42,7 +42,7 @@ def _blast_solver(hype, n, precision=0, recon=0):
     from acoustic_petsc_gb300 import workloads
 
     U0 = workloads.euler_blast(n)
-    ctx = hype.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, precision=precision, recon=recon)
+    ctx = hype.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, precision=precision, recon=recon, positivity=1)
     s = hype.EulerSolver(ctx)
     s.set_state(U0)
     return s, U0
