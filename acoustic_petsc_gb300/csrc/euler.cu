@@ -129,6 +129,18 @@ __device__ __forceinline__ void store_traces(R* __restrict__ T, const Geo& g, lo
 // Riemann solver consumes) against the floors of pde.c:56-66
 template <typename R>
 __device__ __forceinline__ bool traces_admissible(const R* __restrict__ T, const Geo& g, long long e, double gm1) {
+    if (sizeof(R) == sizeof(float)) {  // FP32 traces: p >= floor as (E rho - |m|^2/2)(gamma-1) >= floor rho
+        const float g1 = (float)gm1;
+        for (int q = 0; q < NTR; ++q) {
+            const float rho = (float)T[((long long)0 * NTR + q) * g.NE + e];
+            const float mx = (float)T[((long long)1 * NTR + q) * g.NE + e];
+            const float my = (float)T[((long long)2 * NTR + q) * g.NE + e];
+            const float mz = (float)T[((long long)3 * NTR + q) * g.NE + e];
+            const float E = (float)T[((long long)4 * NTR + q) * g.NE + e];
+            if (!(rho >= 1.0e-14f) || !(g1 * (E * rho - 0.5f * (mx * mx + my * my + mz * mz)) >= 1.0e-12f * rho)) return false;
+        }
+        return true;
+    }
     for (int q = 0; q < NTR; ++q) {
         const double rho = (double)T[((long long)0 * NTR + q) * g.NE + e];
         const double mx = (double)T[((long long)1 * NTR + q) * g.NE + e];
@@ -209,11 +221,11 @@ __global__ void __launch_bounds__(128) k_recon_learned(const double* __restrict_
             float x[mlp::NIN];
 #pragma unroll
             for (int c = 0; c < NV; ++c) {
-                double s5[5];
+                float s5[5];
 #pragma unroll
                 for (int o = 0; o < 5; ++o)
-                    s5[o] = (double)ldw<double>(W + (long long)c * g.N, c, g, m, d == 0 ? o - 2 : 0, d == 1 ? o - 2 : 0,
-                                                d == 2 ? o - 2 : 0);
+                    s5[o] = ldw<float>(W + (long long)c * g.N, c, g, m, d == 0 ? o - 2 : 0, d == 1 ? o - 2 : 0,
+                                       d == 2 ? o - 2 : 0);
                 mlp::normalise5(s5, x + c * 5);
             }
             best = fmaxf(best, mlp::forward(prm, x));
@@ -248,8 +260,9 @@ __global__ void __launch_bounds__(128) k_recon_learned(const double* __restrict_
 }
 
 // Indicator training data: for every stride-th owned cell, the three directional
-// normalised stencils (X[s][3][25]) and the largest departure of its CWENO4
-// weights from the linear ones over the 5 variables (D[s]).
+// normalised stencils (X[s][3][25]) and D[s], the largest change that the nonlinear
+// CWENO4 weights make to a face trace relative to the linear R4 polynomial, over the
+// 5 variables and 24 traces, in units of |cell value| + 1e-3 (labels: D > tau).
 __global__ void __launch_bounds__(128) k_features(const double* __restrict__ W, Geo g, long long stride, long long ns,
                                                   float* __restrict__ X, float* __restrict__ D) {
     const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -261,13 +274,26 @@ __global__ void __launch_bounds__(128) k_features(const double* __restrict__ W, 
     double dmax = 0.0;
 #pragma unroll 1
     for (int c = 0; c < NV; ++c) {
-        double st[33], cf[20], dev;
+        double st[33], cf[20], cl[20], ta[8], tb[8];
         gather33<double>(W + (long long)c * g.N, c, g, m, st);
-        cweno4<double>(st, false, cf, &dev);
-        dmax = fmax(dmax, dev);
+        cweno4<double>(st, false, cf);
+        cweno4<double>(st, true, cl);
+        const double scale = fabs(st[0]) + 1e-3;
+        double dd = 0.0;
+        face_traces<double, 0>(cf, ta);
+        face_traces<double, 0>(cl, tb);
+        for (int q = 0; q < 8; ++q) dd = fmax(dd, fabs(ta[q] - tb[q]));
+        face_traces<double, 1>(cf, ta);
+        face_traces<double, 1>(cl, tb);
+        for (int q = 0; q < 8; ++q) dd = fmax(dd, fabs(ta[q] - tb[q]));
+        face_traces<double, 2>(cf, ta);
+        face_traces<double, 2>(cl, tb);
+        for (int q = 0; q < 8; ++q) dd = fmax(dd, fabs(ta[q] - tb[q]));
+        dmax = fmax(dmax, dd / scale);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            const double s5[5] = {st[S1(d, -2)], st[S1(d, -1)], st[0], st[S1(d, 1)], st[S1(d, 2)]};
+            const float s5[5] = {(float)st[S1(d, -2)], (float)st[S1(d, -1)], (float)st[0], (float)st[S1(d, 1)],
+                                 (float)st[S1(d, 2)]};
             mlp::normalise5(s5, X + (s * 3 + d) * mlp::NIN + c * 5);
         }
     }

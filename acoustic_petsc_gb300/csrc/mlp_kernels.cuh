@@ -16,17 +16,18 @@ constexpr int NIN = 25, NH = 32;
 constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NH * NIN, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NH * NH, OFF_W3 = OFF_B2 + NH,
               OFF_B3 = OFF_W3 + NH, NPARAM = OFF_B3 + 1;
 
-// normalised 5-point stencil: (s_k - mean) / (range + delta), delta = 1e-6 (|mean| + 1e-3):
-// variations far below the CWENO epsilon scale read as flat
-__host__ __device__ __forceinline__ void normalise5(const double* s, float* out) {
-    const double mu = 0.2 * (s[0] + s[1] + s[2] + s[3] + s[4]);
-    double lo = s[0], hi = s[0];
+// normalised 5-point stencil: (s_k - mean) / (range + delta), delta = 1e-2 (|mean| + 1e-3):
+// variations of less than about a percent of the local magnitude (grid noise, small
+// acoustic perturbations) read as flat, a jump of the order of the state as O(1)
+__host__ __device__ __forceinline__ void normalise5(const float* s, float* out) {
+    const float mu = 0.2f * (s[0] + s[1] + s[2] + s[3] + s[4]);
+    float lo = s[0], hi = s[0];
     for (int k = 1; k < 5; ++k) {
         lo = s[k] < lo ? s[k] : lo;
         hi = s[k] > hi ? s[k] : hi;
     }
-    const double r = (hi - lo) + 1e-6 * ((mu < 0 ? -mu : mu) + 1e-3);
-    for (int k = 0; k < 5; ++k) out[k] = (float)((s[k] - mu) / r);
+    const float inv = 1.0f / ((hi - lo) + 1e-2f * ((mu < 0 ? -mu : mu) + 1e-3f));
+    for (int k = 0; k < 5; ++k) out[k] = (s[k] - mu) * inv;
 }
 
 // forward pass of one input with weights p (bf16 in shared or global memory)

@@ -3,8 +3,9 @@
 A 25 -> 32 -> 32 -> 1 network (BF16 weights, FP32 accumulation) scores each
 cell from the normalised 5-point stencils of its 5 conserved variables along x,
 y and z (max of the three logits).  Labels come from the solver itself: a cell
-is troubled when its CWENO4 nonlinear weights depart from the linear ones by
-more than ``tau``.  Training, scoring and inference run in the library's own
+is troubled when its CWENO4 nonlinear weights depart from the linear ones enough
+to move one of its face traces by more than ``tau`` of the cell's magnitude
+(``hype_euler_sample_features``).  Training, scoring and inference run in the library's own
 CUDA kernels (``hype_mlp_*``, ``HYPE_RECON_LEARNED``).
 """
 from __future__ import annotations
@@ -76,7 +77,7 @@ def train(X: np.ndarray, y: np.ndarray, params: np.ndarray | None = None, epochs
     p = init_params(seed) if params is None else np.array(params, dtype=np.float32, copy=True)
     if pos_weight is None:
         pos = float(y.mean())
-        pos_weight = min(50.0, (1.0 - pos) / max(pos, 1e-4))
+        pos_weight = 1.0 if pos <= 0.0 or pos >= 1.0 else min(50.0, (1.0 - pos) / pos)
     loss = C.c_double()
     check(L.lib().hype_mlp_train(_fp(X), _fp(y), X.shape[0], _fp(p), epochs, batch, float(lr), float(pos_weight),
                                  int(seed) & 0xFFFFFFFF, C.byref(loss)), "mlp_train")

@@ -424,7 +424,7 @@ def run_mp2d(args, ws, rank, local, n=1024, precision=0, model=1):
             "gpu_launches": launches, "clocks": clk.summary()}
 
 
-def run_blast(args, ws, rank, local, n=512, ntrain=64, tau=0.05, prob=0.2):
+def run_blast(args, ws, rank, local, n=512, ntrain=64, tau=0.01, prob=0.2):
     """3D Euler blast at scale: learned troubled-cell indicator + FP32 reconstruction/flux
     vs the plain full-CWENO4 forms (FP32 and FP64) on the same GPU."""
     import torch

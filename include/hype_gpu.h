@@ -144,8 +144,9 @@ int hype_euler_set_recon(hype_euler* e, int recon);
 /* counts of owned cells sent to CWENO4 by the network / by the positivity fallback since the last reset */
 int hype_euler_indicator_stats(hype_euler* e, long long* flagged, long long* positivity_fallbacks, int reset);
 /* training samples from the resident state: every stride-th owned cell, its three
- * directional normalised stencils X[s][3][25] and the largest departure D[s] of its
- * CWENO4 nonlinear weights from the linear ones (labels: D > threshold). */
+ * directional normalised stencils X[s][3][25] and D[s], the largest change the CWENO4
+ * nonlinear weights make to one of its 24 face traces relative to the linear R4
+ * polynomial, in units of |cell value| + 1e-3 (labels: D > threshold). */
 int hype_euler_sample_features(hype_euler* e, long long stride, float* X, float* D, long long* ns_out);
 /* Shadow step: one step with the context's reconstruction and, from the same state,
  * one full-CWENO4 step; the first result is kept, *l1_rel = sum|rho - rho_full| / sum|rho_full|. */

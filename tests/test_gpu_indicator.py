@@ -48,7 +48,7 @@ def _blast_solver(hype, n, precision=0, recon=0):
     return s, U0
 
 
-def _train_on_blast(hype, n=32, tau=0.05):
+def _train_on_blast(hype, n=32, tau=0.01):
     from acoustic_petsc_gb300 import indicator
 
     s, _ = _blast_solver(hype, n)
