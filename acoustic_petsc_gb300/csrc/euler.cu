@@ -33,7 +33,23 @@ struct Geo {
     long long N;   // owned cells
     long long NE;  // extended cells (n+2)^3
     int ex, ey;    // extended x, y extents
+    int gx, gy;    // ghosted x, y extents (n + 2 GW): the stage input with its ghost layers
+    long long GN;  // ghosted cells per variable
 };
+
+// ghost width of the stage-input copy: the reconstruction of the first ghost layer
+// (i = -1) reads offsets down to -3
+constexpr int GW = 3;
+
+__host__ __device__ __forceinline__ void set_ghost_extents(Geo& g) {
+    g.gx = g.nx + 2 * GW;
+    g.gy = g.ny + 2 * GW;
+    g.GN = (long long)g.gx * g.gy * (g.nz + 2 * GW);
+}
+
+__device__ __forceinline__ long long ghost_index(const Geo& g, int i, int j, int k) {
+    return ((long long)(k + GW) * g.gy + (j + GW)) * g.gx + (i + GW);
+}
 
 // device scalars of one context
 struct DevScalars {
@@ -70,12 +86,13 @@ __device__ __forceinline__ void make_map(const Geo& g, int i, int j, int k, Sten
     }
 }
 
-// one value of variable c at offset (oi, oj, ok); a reflective ghost negates the
-// momentum component normal to its wall
-template <typename R>
-__device__ __forceinline__ R ldw(const double* __restrict__ Wc, int c, const Geo& g, const StencilMap& m, int oi, int oj,
+// one value of variable c at offset (oi, oj, ok) from the state (S = double) or its
+// FP32 mirror (S = float); a reflective ghost negates the momentum component normal
+// to its wall
+template <typename R, typename S>
+__device__ __forceinline__ R ldw(const S* __restrict__ Wc, int c, const Geo& g, const StencilMap& m, int oi, int oj,
                                  int ok) {
-    double v = __ldg(Wc + ((long long)m.mk[ok + 2] * g.ny + m.mj[oj + 2]) * g.nx + m.mi[oi + 2]);
+    S v = __ldg(Wc + ((long long)m.mk[ok + 2] * g.ny + m.mj[oj + 2]) * g.nx + m.mi[oi + 2]);
     const int fm = (c == 1) ? m.fi : (c == 2) ? m.fj : (c == 3) ? m.fk : 0;
     const int o = (c == 1) ? oi : (c == 2) ? oj : ok;
     if (fm && ((fm >> (o + 2)) & 1)) v = -v;
@@ -83,8 +100,8 @@ __device__ __forceinline__ R ldw(const double* __restrict__ Wc, int c, const Geo
 }
 
 // the 33-point stencil of variable c (index map of euler_kernels.cuh)
-template <typename R>
-__device__ __forceinline__ void gather33(const double* __restrict__ Wc, int c, const Geo& g, const StencilMap& m, R* s) {
+template <typename R, typename S>
+__device__ __forceinline__ void gather33(const S* __restrict__ Wc, int c, const Geo& g, const StencilMap& m, R* s) {
     s[0] = ldw<R>(Wc, c, g, m, 0, 0, 0);
 #pragma unroll
     for (int o = 0; o < 4; ++o) {
@@ -109,20 +126,50 @@ __device__ __forceinline__ void gather33(const double* __restrict__ Wc, int c, c
             for (int d = 0; d < 2; ++d) s[SO(a, b, d)] = ldw<R>(Wc, c, g, m, 2 * a - 1, 2 * b - 1, 2 * d - 1);
 }
 
-// the 24 face traces of one variable into the trace array
+// Admissibility of a cell's FP32 traces, decided while they are stored: the density
+// (c = 0) and the squared momentum (c = 1..3) of each trace point wait in the thread's
+// column of a per-warp shared-memory scratch [2][NTR][32] until the energy (c = 4)
+// arrives; the test is pde.c:56-66's floors, p >= 1e-12 as
+// (gamma-1)(E rho - |m|^2/2) >= 1e-12 rho.
+struct TraceCheck {
+    float* col;  // the lane's column: [q * 32] density, [(NTR + q) * 32] |m|^2
+    float g1;
+    bool ok;
+};
+
+__device__ __forceinline__ void trace_check(TraceCheck* ck, int c, int q, float v) {
+    float* r = ck->col + q * 32;
+    float* m = ck->col + (NTR + q) * 32;
+    if (c == 0) {
+        *r = v;
+    } else if (c == 1) {
+        *m = v * v;
+    } else if (c < 4) {
+        *m += v * v;
+    } else {
+        const float rho = *r;
+        ck->ok = ck->ok && (rho >= 1.0e-14f) && (ck->g1 * (v * rho - 0.5f * *m) >= 1.0e-12f * rho);
+    }
+}
+
+// the 24 face traces of one variable into the trace array (FP32 traces: and into the
+// admissibility check ck when one is given)
 template <typename R>
-__device__ __forceinline__ void store_traces(R* __restrict__ T, const Geo& g, long long e, int c, const R* cf) {
+__device__ __forceinline__ void store_traces(R* __restrict__ T, const Geo& g, long long e, int c, const R* cf,
+                                             TraceCheck* ck = nullptr) {
     R tr[8];
     R* Tc = T + (long long)c * NTR * g.NE + e;
-    face_traces<R, 0>(cf, tr);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) Tc[(long long)q * g.NE] = tr[q];
-    face_traces<R, 1>(cf, tr);
+    for (int d = 0; d < 3; ++d) {
+        if (d == 0) face_traces<R, 0>(cf, tr);
+        else if (d == 1) face_traces<R, 1>(cf, tr);
+        else face_traces<R, 2>(cf, tr);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) Tc[(long long)(8 + q) * g.NE] = tr[q];
-    face_traces<R, 2>(cf, tr);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) Tc[(long long)(16 + q) * g.NE] = tr[q];
+        for (int q = 0; q < 8; ++q) {
+            Tc[(long long)(8 * d + q) * g.NE] = tr[q];
+            if (sizeof(R) == sizeof(float) && ck) trace_check(ck, c, 8 * d + q, (float)tr[q]);
+        }
+    }
 }
 
 // density and pressure at the 24 face Gauss-point traces of one cell (what the
@@ -153,40 +200,100 @@ __device__ __forceinline__ bool traces_admissible(const R* __restrict__ T, const
     return true;
 }
 
+
+// Device-side ghost fill (what DMGlobalToLocal does for the reference's DMDA, with
+// the boundary treatment of rhs_function.c's ghost loops): the stage input W (owned
+// cells, SoA) copied into G with GW ghost layers on every side, each ghost the value
+// its per-axis boundary map picks (periodic wrap, reflective mirror, transmissive
+// copy) and a reflective ghost's wall-normal momentum negated; G is in the
+// reconstruction's precision, so the FP32 form converts each value once per stage.
+template <typename R>
+__global__ void __launch_bounds__(128) k_ghost(const double* __restrict__ W, R* __restrict__ G, Geo g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - GW;
+    const int j = blockIdx.y - GW, k = blockIdx.z - GW;
+    if (i >= g.nx + GW) return;
+    int fi = 0, fj = 0, fk = 0;
+    const int mi = bmap(i, g.nx, g.bc[0], g.bc[1], &fi);
+    const int mj = bmap(j, g.ny, g.bc[2], g.bc[3], &fj);
+    const int mk = bmap(k, g.nz, g.bc[4], g.bc[5], &fk);
+    const long long src = ((long long)mk * g.ny + mj) * g.nx + mi;
+    const long long dst = ghost_index(g, i, j, k);
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        double v = __ldg(W + (long long)c * g.N + src);
+        if ((c == 1 && fi) || (c == 2 && fj) || (c == 3 && fk)) v = -v;
+        G[(long long)c * g.GN + dst] = (R)v;
+    }
+}
+
+// the 33-point stencil (index map of euler_kernels.cuh) of one variable about p = &G[cell]
+template <typename R>
+__device__ __forceinline__ void gather33g(const R* __restrict__ p, int sy, int sz, R* s) {
+    s[0] = __ldg(p);
+#pragma unroll
+    for (int o = 0; o < 4; ++o) {
+        const int off = (o == 0) ? -2 : (o == 1) ? -1 : (o == 2) ? 1 : 2;
+        s[S1(0, off)] = __ldg(p + off);
+        s[S1(1, off)] = __ldg(p + off * sy);
+        s[S1(2, off)] = __ldg(p + off * sz);
+    }
+#pragma unroll
+    for (int sa = 0; sa < 2; ++sa)
+#pragma unroll
+        for (int sb = 0; sb < 2; ++sb) {
+            s[SQ(0, sa, 1, sb)] = __ldg(p + (2 * sa - 1) + (2 * sb - 1) * sy);
+            s[SQ(1, sa, 2, sb)] = __ldg(p + (2 * sa - 1) * sy + (2 * sb - 1) * sz);
+            s[SQ(0, sa, 2, sb)] = __ldg(p + (2 * sa - 1) + (2 * sb - 1) * sz);
+        }
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int d = 0; d < 2; ++d) s[SO(a, b, d)] = __ldg(p + (2 * a - 1) + (2 * b - 1) * sy + (2 * d - 1) * sz);
+}
+
 // first-order traces (all higher coefficients zero): the fallback of
 // 3d/weno4/Viscous-Multiphase-Fourth-Order/rhs_function.c:297-305
 template <typename R>
-__device__ __forceinline__ void store_first_order(const double* __restrict__ W, R* __restrict__ T, const Geo& g,
-                                                  const StencilMap& m, long long e) {
+__device__ __forceinline__ void store_first_order_g(const R* __restrict__ G, R* __restrict__ T, const Geo& g,
+                                                    long long ge, long long e) {
 #pragma unroll 1
     for (int c = 0; c < NV; ++c) {
-        const R v = ldw<R>(W + (long long)c * g.N, c, g, m, 0, 0, 0);
+        const R v = __ldg(G + (long long)c * g.GN + ge);
         R* Tc = T + (long long)c * NTR * g.NE + e;
         for (int q = 0; q < NTR; ++q) Tc[(long long)q * g.NE] = v;
     }
 }
 
+// Reconstruction of every owned cell and of the first ghost layer (faces of the
+// domain boundary); the FP32 form checks admissibility in dynamic shared memory
+// (4 warps x 2 x NTR x 32 floats, launched only with the positivity fallback on).
 template <typename R>
-__global__ void __launch_bounds__(128) k_recon(const double* __restrict__ W, R* __restrict__ T, Geo g, int linear,
-                                               int pad, double gm1, unsigned long long* __restrict__ counters) {
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1)
+    k_recon(const R* __restrict__ G, R* __restrict__ T, Geo g, int linear, int pad, double gm1,
+            unsigned long long* __restrict__ counters) {
+    extern __shared__ float ck_dyn[];
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
     const int k = blockIdx.z - 1;
     if (i > g.nx || j > g.ny) return;
     const int gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny), gk = (k < 0 || k >= g.nz);
     if (gi + gj + gk > 1) return;  // edge/corner ghosts feed no face of an owned cell
-    StencilMap m;
-    make_map(g, i, j, k, m);
-    const long long e = ext_index(g, i, j, k);
+    const long long e = ext_index(g, i, j, k), ge = ghost_index(g, i, j, k);
+    const int sy = g.gx, sz = g.gx * g.gy;
+    constexpr bool f32 = sizeof(R) == sizeof(float);
+    TraceCheck ck{ck_dyn + threadIdx.y * (2 * NTR * 32) + threadIdx.x, (float)gm1, true};
+    TraceCheck* ckp = (f32 && pad) ? &ck : nullptr;
 #pragma unroll 1
     for (int c = 0; c < NV; ++c) {
         R s[33], cf[20];
-        gather33<R>(W + (long long)c * g.N, c, g, m, s);
+        gather33g<R>(G + (long long)c * g.GN + ge, sy, sz, s);
         cweno4<R>(s, linear != 0, cf);
-        store_traces<R>(T, g, e, c, cf);
+        store_traces<R>(T, g, e, c, cf, ckp);
     }
-    if (pad && !traces_admissible<R>(T, g, e, gm1)) {
-        store_first_order<R>(W, T, g, m, e);
+    if (pad && !(f32 ? ck.ok : traces_admissible<R>(T, g, e, gm1))) {
+        store_first_order_g<R>(G, T, g, ge, e);
         if (!gi && !gj && !gk) atomicAdd(&counters[1], 1ull);
     }
 }
@@ -197,53 +304,71 @@ __global__ void __launch_bounds__(128) k_recon(const double* __restrict__ W, R* 
 // or pressure below the floors at any face Gauss point, in which case the cell
 // is redone with CWENO4 (positivity fallback).
 template <typename R>
-__global__ void __launch_bounds__(128) k_recon_learned(const double* __restrict__ W, R* __restrict__ T, Geo g,
-                                                       const __nv_bfloat16* __restrict__ pg, float logit_thr, double gm1,
-                                                       int pad, unsigned long long* __restrict__ counters) {
-    __shared__ __nv_bfloat16 prm[mlp::NPARAM];
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1)
+    k_recon_learned(const R* __restrict__ G, R* __restrict__ T, Geo g, const mlp::MmaWeights* __restrict__ wts,
+                    float logit_thr, double gm1, int pad, unsigned long long* __restrict__ counters) {
+    // per warp: the staged network inputs, later the FP32 admissibility scratch
+    static_assert(mlp::ROWS * mlp::RSTRIDE * sizeof(__nv_bfloat16) >= 2 * NTR * 32 * sizeof(float), "scratch");
+    __shared__ __align__(16) __nv_bfloat16 rows[4][mlp::ROWS * mlp::RSTRIDE];
+    __shared__ float lg[4][mlp::ROWS];
     __shared__ unsigned cnt[2];
-    for (int q = threadIdx.y * blockDim.x + threadIdx.x; q < mlp::NPARAM; q += blockDim.x * blockDim.y) prm[q] = pg[q];
     if (threadIdx.x == 0 && threadIdx.y == 0) cnt[0] = cnt[1] = 0;
-    __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
     const int k = blockIdx.z - 1;
     bool active = !(i > g.nx || j > g.ny);
     const int gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny), gk = (k < 0 || k >= g.nz);
     active = active && (gi + gj + gk <= 1);
+    const long long ge = active ? ghost_index(g, i, j, k) : 0;
+    const int sy = g.gx, sz = g.gx * g.gy;
+    // features of the warp's 32 cells (3 rows each) staged as BF16, scored on the tensor cores
+    __nv_bfloat16* my_rows = rows[threadIdx.y] + threadIdx.x * 3 * mlp::RSTRIDE;
+    float sc[NV];
     if (active) {
-        StencilMap m;
-        make_map(g, i, j, k, m);
-        const long long e = ext_index(g, i, j, k);
-        float best = -INFINITY;
+        const float rho = (float)__ldg(G + ge), E = (float)__ldg(G + 4 * g.GN + ge);
+#pragma unroll
+        for (int c = 0; c < NV; ++c) sc[c] = mlp::var_scale<float>(c, rho, E);
+    }
 #pragma unroll 1
-        for (int d = 0; d < 3; ++d) {
-            float x[mlp::NIN];
+    for (int d = 0; d < 3; ++d) {
+        float x[mlp::NIN];
+        const int st = d == 0 ? 1 : d == 1 ? sy : sz;
+        if (active) {
 #pragma unroll
             for (int c = 0; c < NV; ++c) {
+                const R* p = G + (long long)c * g.GN + ge;
                 float s5[5];
 #pragma unroll
-                for (int o = 0; o < 5; ++o)
-                    s5[o] = ldw<float>(W + (long long)c * g.N, c, g, m, d == 0 ? o - 2 : 0, d == 1 ? o - 2 : 0,
-                                       d == 2 ? o - 2 : 0);
-                mlp::normalise5(s5, x + c * 5);
+                for (int o = 0; o < 5; ++o) s5[o] = (float)__ldg(p + (o - 2) * st);
+                mlp::normalise5(s5, sc[c], x + c * 5);
             }
-            best = fmaxf(best, mlp::forward(prm, x));
         }
+        mlp::stage_row(my_rows + d * mlp::RSTRIDE, x, active);
+    }
+    __syncthreads();  // counters cleared, rows staged
+    mlp::warp_logits(wts, rows[threadIdx.y], lg[threadIdx.y]);
+    __syncwarp();
+    const float best = fmaxf(lg[threadIdx.y][threadIdx.x * 3], fmaxf(lg[threadIdx.y][threadIdx.x * 3 + 1],
+                                                                       lg[threadIdx.y][threadIdx.x * 3 + 2]));
+    if (active) {
+        const long long e = ext_index(g, i, j, k);
+        constexpr bool f32 = sizeof(R) == sizeof(float);
+        TraceCheck ck{reinterpret_cast<float*>(rows[threadIdx.y]) + threadIdx.x, (float)gm1, true};
         bool full = best > logit_thr;
 #pragma unroll 1
         for (int pass = 0; pass < 2; ++pass) {
+            ck.ok = true;
 #pragma unroll 1
             for (int c = 0; c < NV; ++c) {
                 R s[33], cf[20];
-                gather33<R>(W + (long long)c * g.N, c, g, m, s);
+                gather33g<R>(G + (long long)c * g.GN + ge, sy, sz, s);
                 cweno4<R>(s, !full, cf);
-                store_traces<R>(T, g, e, c, cf);
+                store_traces<R>(T, g, e, c, cf, f32 ? &ck : nullptr);
             }
-            if (traces_admissible<R>(T, g, e, gm1)) break;
+            if (f32 ? ck.ok : traces_admissible<R>(T, g, e, gm1)) break;
             if (full) {  // CWENO4 itself inadmissible: first order (when enabled)
                 if (pad) {
-                    store_first_order<R>(W, T, g, m, e);
+                    store_first_order_g<R>(G, T, g, ge, e);
                     if (!gi && !gj && !gk) atomicAdd(&cnt[1], 1u);
                 }
                 break;
@@ -262,7 +387,8 @@ __global__ void __launch_bounds__(128) k_recon_learned(const double* __restrict_
 // Indicator training data: for every stride-th owned cell, the three directional
 // normalised stencils (X[s][3][25]) and D[s], the largest change that the nonlinear
 // CWENO4 weights make to a face trace relative to the linear R4 polynomial, over the
-// 5 variables and 24 traces, in units of |cell value| + 1e-3 (labels: D > tau).
+// 5 variables and 24 traces, in units of the variable's magnitude in the cell (labels:
+// D > tau).
 __global__ void __launch_bounds__(128) k_features(const double* __restrict__ W, Geo g, long long stride, long long ns,
                                                   float* __restrict__ X, float* __restrict__ D) {
     const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -271,14 +397,15 @@ __global__ void __launch_bounds__(128) k_features(const double* __restrict__ W, 
     const int i = (int)(cell % g.nx), j = (int)((cell / g.nx) % g.ny), k = (int)(cell / ((long long)g.nx * g.ny));
     StencilMap m;
     make_map(g, i, j, k, m);
+    const double rho = ldw<double, double>(W, 0, g, m, 0, 0, 0), E = ldw<double, double>(W + 4 * g.N, 4, g, m, 0, 0, 0);
     double dmax = 0.0;
 #pragma unroll 1
     for (int c = 0; c < NV; ++c) {
         double st[33], cf[20], cl[20], ta[8], tb[8];
-        gather33<double>(W + (long long)c * g.N, c, g, m, st);
+        gather33<double, double>(W + (long long)c * g.N, c, g, m, st);
         cweno4<double>(st, false, cf);
         cweno4<double>(st, true, cl);
-        const double scale = fabs(st[0]) + 1e-3;
+        const double scale = mlp::var_scale<double>(c, rho, E) + 1e-30;
         double dd = 0.0;
         face_traces<double, 0>(cf, ta);
         face_traces<double, 0>(cl, tb);
@@ -294,7 +421,7 @@ __global__ void __launch_bounds__(128) k_features(const double* __restrict__ W, 
         for (int d = 0; d < 3; ++d) {
             const float s5[5] = {(float)st[S1(d, -2)], (float)st[S1(d, -1)], (float)st[0], (float)st[S1(d, 1)],
                                  (float)st[S1(d, 2)]};
-            mlp::normalise5(s5, X + (s * 3 + d) * mlp::NIN + c * 5);
+            mlp::normalise5(s5, (float)mlp::var_scale<double>(c, rho, E), X + (s * 3 + d) * mlp::NIN + c * 5);
         }
     }
     D[s] = (float)dmax;
@@ -462,11 +589,12 @@ struct hype_euler {
     double* Fy = nullptr;
     double* Fz = nullptr;
     double* stage_aos = nullptr;  // device AoS staging
+    void* G = nullptr;            // ghosted stage input in the reconstruction's precision
     DevScalars* ds = nullptr;
     DevScalars* hs = nullptr;  // pinned host copy
     double* pin = nullptr;     // pinned host staging for AoS transfers
     // learned indicator: BF16 parameters, logit threshold, counters (flagged, positivity fallbacks)
-    __nv_bfloat16* mlp = nullptr;
+    mlp::MmaWeights* mlp = nullptr;  // packed for the tensor-core inference
     float logit_thr = 0.0f;
     unsigned long long* mlp_cnt = nullptr;
     // per-kernel event timing inside a timed region (hype_euler_profile)
@@ -526,19 +654,26 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
     const bool f32 = e->p.precision == HYPE_PREC_FP32;
     const int lin = e->p.recon == HYPE_RECON_LINEAR4;
     prof_mark(e, 0, true);
+    const dim3 bgh(128), ggh(cdiv(g.gx, 128), g.gy, g.nz + 2 * GW);
+    if (f32) k_ghost<float><<<ggh, bgh, 0, e->stream>>>(Win, (float*)e->G, g);
+    else k_ghost<double><<<ggh, bgh, 0, e->stream>>>(Win, (double*)e->G, g);
+    HYPE_LAUNCHED(1);
+    const double gm1 = e->p.gamma - 1.0;
+    const size_t ck_bytes = (f32 && e->p.positivity) ? sizeof(float) * 4 * 2 * NTR * 32 : 0;
     if (e->p.recon == HYPE_RECON_LEARNED) {
         if (!e->mlp) return HYPE_ERR_ARG;  // hype_euler_set_mlp first
-        const double gm1 = e->p.gamma - 1.0;
         if (f32)
-            k_recon_learned<float><<<gr, br, 0, e->stream>>>(Win, (float*)e->T, g, e->mlp, e->logit_thr, gm1, e->p.positivity,
-                                                             e->mlp_cnt);
+            k_recon_learned<float><<<gr, br, 0, e->stream>>>((const float*)e->G, (float*)e->T, g, e->mlp, e->logit_thr, gm1,
+                                                             e->p.positivity, e->mlp_cnt);
         else
-            k_recon_learned<double><<<gr, br, 0, e->stream>>>(Win, (double*)e->T, g, e->mlp, e->logit_thr, gm1,
-                                                              e->p.positivity, e->mlp_cnt);
+            k_recon_learned<double><<<gr, br, 0, e->stream>>>((const double*)e->G, (double*)e->T, g, e->mlp, e->logit_thr,
+                                                              gm1, e->p.positivity, e->mlp_cnt);
     } else if (f32) {
-        k_recon<float><<<gr, br, 0, e->stream>>>(Win, (float*)e->T, g, lin, e->p.positivity, e->p.gamma - 1.0, e->mlp_cnt);
+        k_recon<float><<<gr, br, ck_bytes, e->stream>>>((const float*)e->G, (float*)e->T, g, lin, e->p.positivity, gm1,
+                                                        e->mlp_cnt);
     } else {
-        k_recon<double><<<gr, br, 0, e->stream>>>(Win, (double*)e->T, g, lin, e->p.positivity, e->p.gamma - 1.0, e->mlp_cnt);
+        k_recon<double><<<gr, br, 0, e->stream>>>((const double*)e->G, (double*)e->T, g, lin, e->p.positivity, gm1,
+                                                  e->mlp_cnt);
     }
     prof_mark(e, 0, false);
     prof_mark(e, 1, true);
@@ -580,6 +715,7 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
     g.NE = (long long)(p->nx + 2) * (p->ny + 2) * (p->nz + 2);
     g.ex = p->nx + 2;
     g.ey = p->ny + 2;
+    set_ghost_extents(g);
     const size_t sN = sizeof(double) * NV * (size_t)g.N;
     const size_t tsz = (p->precision == HYPE_PREC_FP32 ? sizeof(float) : sizeof(double)) * NV * NTR * (size_t)g.NE;
     int rc = HYPE_OK;
@@ -610,6 +746,7 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
     ALLOC(e->stage_aos, sN);
     ALLOC(e->ds, sizeof(DevScalars));
     ALLOC(e->mlp_cnt, 2 * sizeof(unsigned long long));
+    ALLOC(e->G, (p->precision == HYPE_PREC_FP32 ? sizeof(float) : sizeof(double)) * NV * (size_t)g.GN);
 #undef ALLOC
     ce = cudaMemset(e->mlp_cnt, 0, 2 * sizeof(unsigned long long));
     if (ce != cudaSuccess) {
@@ -637,7 +774,7 @@ extern "C" void hype_euler_destroy(hype_euler* e) {
     if (!e) return;
     if (e->stream) cudaStreamSynchronize(e->stream);
     cudaFree(e->U); cudaFree(e->W); cudaFree(e->L); cudaFree(e->S); cudaFree(e->T);
-    cudaFree(e->Fx); cudaFree(e->Fy); cudaFree(e->Fz); cudaFree(e->stage_aos); cudaFree(e->ds);
+    cudaFree(e->Fx); cudaFree(e->Fy); cudaFree(e->Fz); cudaFree(e->stage_aos); cudaFree(e->ds); cudaFree(e->G);
     cudaFree(e->mlp); cudaFree(e->mlp_cnt);
     if (e->hs) cudaFreeHost(e->hs);
     for (auto x : e->ev) cudaEventDestroy(x);
@@ -784,8 +921,10 @@ extern "C" int hype_euler_set_mlp(hype_euler* e, const float* params, float prob
     if (!e || !params || !(prob_threshold > 0.0f) || !(prob_threshold < 1.0f)) return HYPE_ERR_ARG;
     std::vector<__nv_bfloat16> h(mlp::NPARAM);
     for (int q = 0; q < mlp::NPARAM; ++q) h[q] = __float2bfloat16_rn(params[q]);
-    if (!e->mlp) HYPE_CK(cudaMalloc((void**)&e->mlp, sizeof(__nv_bfloat16) * mlp::NPARAM));
-    HYPE_CK(cudaMemcpyAsync(e->mlp, h.data(), sizeof(__nv_bfloat16) * mlp::NPARAM, cudaMemcpyHostToDevice, e->stream));
+    mlp::MmaWeights hw;  // host staging, copied before the stream synchronisation below
+    mlp::pack_weights(h.data(), hw);
+    if (!e->mlp) HYPE_CK(cudaMalloc((void**)&e->mlp, sizeof(mlp::MmaWeights)));
+    HYPE_CK(cudaMemcpyAsync(e->mlp, &hw, sizeof(mlp::MmaWeights), cudaMemcpyHostToDevice, e->stream));
     HYPE_CK(cudaStreamSynchronize(e->stream));
     e->logit_thr = logf(prob_threshold / (1.0f - prob_threshold));
     return HYPE_OK;
@@ -877,7 +1016,11 @@ constexpr size_t align_up(size_t b) { return (b + kAlign - 1) / kAlign * kAlign;
 constexpr size_t kNoAllocTraceBytes = align_up(sizeof(double) * NV * NTR * kNoAllocMaxExt);
 constexpr size_t kNoAllocFluxBytes = align_up(sizeof(double) * NV * kNoAllocMaxExt);  // one direction
 constexpr size_t kNoAllocScalarBytes = align_up(sizeof(DevScalars));
-constexpr size_t kNoAllocBytes = kNoAllocTraceBytes + 3 * kNoAllocFluxBytes + kNoAllocScalarBytes;  // ~6.3 MB
+// ghosted stage input: (nx+6)(ny+6)(nz+6) <= (9/5)^3 (nx+2)(ny+2)(nz+2) for n >= 3
+constexpr long long kNoAllocMaxGhost = kNoAllocMaxExt * 729 / 125 + 1;
+constexpr size_t kNoAllocGhostBytes = align_up(sizeof(double) * NV * kNoAllocMaxGhost);
+constexpr size_t kNoAllocBytes =
+    kNoAllocTraceBytes + 3 * kNoAllocFluxBytes + kNoAllocScalarBytes + kNoAllocGhostBytes;  // ~7.7 MB
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -934,26 +1077,32 @@ extern "C" int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* 
     g.NE = ne;
     g.ex = p->nx + 2;
     g.ey = p->ny + 2;
+    set_ghost_extents(g);
     void* T = base;
     double* Fx = (double*)(base + kNoAllocTraceBytes);
     double* Fy = (double*)(base + kNoAllocTraceBytes + kNoAllocFluxBytes);
     double* Fz = (double*)(base + kNoAllocTraceBytes + 2 * kNoAllocFluxBytes);
     DevScalars* ds = (DevScalars*)(base + kNoAllocTraceBytes + 3 * kNoAllocFluxBytes);
+    void* G = base + kNoAllocTraceBytes + 3 * kNoAllocFluxBytes + kNoAllocScalarBytes;
     cudaStream_t s = (cudaStream_t)stream;
     // the scratch keeps the previous call's contents: the wave-speed maximum and the
     // admissibility word must start cleared; traces and fluxes are fully rewritten
     k_reset_slot<<<1, 1, 0, s>>>(ds, 4);
     const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2);
     const int lin = p->recon == HYPE_RECON_LINEAR4;
-    if (p->precision == HYPE_PREC_FP32)
-        k_recon<float><<<gr, br, 0, s>>>(dU, (float*)T, g, lin, 0, p->gamma - 1.0, nullptr);
-    else
-        k_recon<double><<<gr, br, 0, s>>>(dU, (double*)T, g, lin, 0, p->gamma - 1.0, nullptr);
+    const dim3 bgh(128), ggh(cdiv(g.gx, 128), g.gy, g.nz + 2 * GW);
+    if (p->precision == HYPE_PREC_FP32) {
+        k_ghost<float><<<ggh, bgh, 0, s>>>(dU, (float*)G, g);
+        k_recon<float><<<gr, br, 0, s>>>((const float*)G, (float*)T, g, lin, 0, p->gamma - 1.0, nullptr);
+    } else {
+        k_ghost<double><<<ggh, bgh, 0, s>>>(dU, (double*)G, g);
+        k_recon<double><<<gr, br, 0, s>>>((const double*)G, (double*)T, g, lin, 0, p->gamma - 1.0, nullptr);
+    }
     launch_faces(g, T, Fx, Fy, Fz, p->gamma, ds, 4, p->precision == HYPE_PREC_FP32, p->flux, s);
     const Stage st{0.0, 0.0, 0.0, 1};
     const dim3 bu(32, 8), gu(cdiv(g.nx, 32), cdiv(g.ny, 8), g.nz);
     k_update<<<gu, bu, 0, s>>>(Fx, Fy, Fz, nullptr, nullptr, dRHS, g, 1.0 / p->h, st, ds);
-    HYPE_LAUNCHED(6);
+    HYPE_LAUNCHED(7);
     if (dt_out) {
         unsigned long long w[2];
         HYPE_CK(cudaMemcpyAsync(&w[0], &ds->smax_bits[4], sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));

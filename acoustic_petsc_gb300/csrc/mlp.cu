@@ -3,9 +3,10 @@
 // Hand-written forward / backward / Adam kernels (no framework).  A sample is a
 // cell: X[s][3][25] (normalised stencils along x, y, z), label y[s] in {0,1}.
 // The cell's logit is the max over its three directional logits; the loss is
-// binary cross-entropy with a positive-class weight.  Forward and backward use
-// the BF16-rounded weights (what inference uses), with FP32 accumulation and an
-// FP32 master copy updated by Adam.
+// binary cross-entropy with a positive-class weight.  Training uses the
+// BF16-rounded weights with FP32 activations and accumulation and an FP32 master
+// copy updated by Adam; inference (k_score and the gated reconstruction) runs the
+// same network on the tensor cores with BF16 inputs and first-layer activations.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
@@ -23,20 +24,23 @@ __global__ void k_to_bf16(const float* __restrict__ p, __nv_bfloat16* __restrict
     if (i < n) q[i] = __float2bfloat16_rn(p[i]);
 }
 
-__global__ void k_score(const float* __restrict__ X, int n, const __nv_bfloat16* __restrict__ pg, float* __restrict__ score) {
-    __shared__ __nv_bfloat16 p[NPARAM];
-    for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) p[i] = pg[i];
-    __syncthreads();
+// cell scores on the tensor cores, the same code path as the gated reconstruction
+__global__ void __launch_bounds__(128) k_score(const float* __restrict__ X, int n, const MmaWeights* __restrict__ w,
+                                               float* __restrict__ score) {
+    __shared__ __align__(16) __nv_bfloat16 rows[4][ROWS * RSTRIDE];
+    __shared__ float lg[4][ROWS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    float best = -INFINITY;
     for (int d = 0; d < 3; ++d) {
         float x[NIN];
 #pragma unroll
-        for (int k = 0; k < NIN; ++k) x[k] = X[((long long)s * 3 + d) * NIN + k];
-        best = fmaxf(best, forward(p, x));
+        for (int k = 0; k < NIN; ++k) x[k] = s < n ? X[((long long)s * 3 + d) * NIN + k] : 0.0f;
+        stage_row(rows[warp] + (lane * 3 + d) * RSTRIDE, x, s < n);
     }
-    score[s] = best;
+    __syncwarp();
+    warp_logits(w, rows[warp], lg[warp]);
+    __syncwarp();
+    if (s < n) score[s] = fmaxf(lg[warp][lane * 3], fmaxf(lg[warp][lane * 3 + 1], lg[warp][lane * 3 + 2]));
 }
 
 __device__ __forceinline__ float softplus(float z) { return z > 20.f ? z : log1pf(expf(z)); }
@@ -157,16 +161,18 @@ struct DevBuf {
 extern "C" int hype_mlp_score(const float* X, int n, const float* params, float* score) {
     if (!X || !params || !score || n < 0) return HYPE_ERR_ARG;
     if (n == 0) return HYPE_OK;
-    DevBuf dX, dp, dq, ds;
+    DevBuf dX, dw, ds;
     MLP_ALLOC(dX, sizeof(float) * (size_t)n * 3 * NIN);
-    MLP_ALLOC(dp, sizeof(float) * NPARAM);
-    MLP_ALLOC(dq, sizeof(__nv_bfloat16) * NPARAM);
+    MLP_ALLOC(dw, sizeof(MmaWeights));
     MLP_ALLOC(ds, sizeof(float) * (size_t)n);
+    std::vector<__nv_bfloat16> q(NPARAM);
+    for (int i = 0; i < NPARAM; ++i) q[i] = __float2bfloat16_rn(params[i]);
+    MmaWeights hw;
+    pack_weights(q.data(), hw);
     HYPE_CK(cudaMemcpy(dX.p, X, sizeof(float) * (size_t)n * 3 * NIN, cudaMemcpyHostToDevice));
-    HYPE_CK(cudaMemcpy(dp.p, params, sizeof(float) * NPARAM, cudaMemcpyHostToDevice));
-    k_to_bf16<<<cdiv(NPARAM, 256), 256>>>((const float*)dp.p, (__nv_bfloat16*)dq.p, NPARAM);
-    k_score<<<cdiv(n, 128), 128>>>((const float*)dX.p, n, (const __nv_bfloat16*)dq.p, (float*)ds.p);
-    HYPE_LAUNCHED(2);
+    HYPE_CK(cudaMemcpy(dw.p, &hw, sizeof(MmaWeights), cudaMemcpyHostToDevice));
+    k_score<<<cdiv(n, 128), 128>>>((const float*)dX.p, n, (const MmaWeights*)dw.p, (float*)ds.p);
+    HYPE_LAUNCHED(1);
     HYPE_CK(cudaMemcpy(score, ds.p, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost));
     return HYPE_OK;
 }

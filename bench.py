@@ -532,6 +532,7 @@ WORKLOADS = {
     "euler256": lambda a, *r: run_euler(a, *r, precision=0, recon=0),
     "euler256_fp32": lambda a, *r: run_euler(a, *r, precision=1, recon=0),
     "euler256_linear": lambda a, *r: run_euler(a, *r, precision=0, recon=1),
+    "euler256_fp32_linear": lambda a, *r: run_euler(a, *r, precision=1, recon=1),
     "euler64": lambda a, *r: run_euler(a, *r, precision=0, recon=0, n=64),
     "euler128": lambda a, *r: run_euler(a, *r, precision=0, recon=0, n=128),
     "euler128_fp32": lambda a, *r: run_euler(a, *r, precision=1, recon=0, n=128),

@@ -161,7 +161,7 @@ int hype_euler_shadow_step(hype_euler* e, double* t_inout, double* dt_inout, dou
  * device buffers dU -> dRHS (SoA [5][nz][ny][nx]) for the grid and options in
  * *p, without creating a context and without any cudaMalloc / cudaFree: all
  * scratch (face traces, face fluxes, the wave-speed and admissibility words)
- * lives in one fixed device array of this library, about 6.3 MB, that every GPU
+ * lives in one fixed device array of this library, about 7.7 MB, that every GPU
  * which loads the library holds until the process exits.
  *   - Limit: (nx+2)(ny+2)(nz+2) <= 5832 (e.g. 16^3 cells; hype_euler_noalloc_max_ext
  *     returns the bound); larger grids return HYPE_ERR_ARG.

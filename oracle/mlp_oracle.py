@@ -1,6 +1,7 @@
 """CPU FP64 restatement of the indicator network (TEST INFRASTRUCTURE ONLY):
 forward, max-pooled BCE loss and its gradient, with the BF16-rounded weights
-the GPU kernels use.  Used to check the GPU backward kernel."""
+the GPU kernels use.  Used to check the GPU inference (tensor-core) and backward
+kernels."""
 from __future__ import annotations
 
 import numpy as np
@@ -27,11 +28,15 @@ def unpack(p):
     return W1, b1, W2, b2, W3, b3
 
 
-def logits(X, params):
-    """[n][3] logits of every direction"""
+def logits(X, params, act_bf16=False):
+    """[n][3] logits of every direction; act_bf16 rounds the inputs and the first
+    hidden layer to BF16 as the tensor-core inference path does (its operand type)"""
     W1, b1, W2, b2, W3, b3 = unpack(bf16_round(params))
-    a1 = X.astype(np.float64) @ W1.T + b1
+    X = bf16_round(X).reshape(X.shape) if act_bf16 else X.astype(np.float64)
+    a1 = X @ W1.T + b1
     h1 = np.maximum(a1, 0.0)
+    if act_bf16:
+        h1 = bf16_round(h1).reshape(h1.shape)
     a2 = h1 @ W2.T + b2
     return np.maximum(a2, 0.0) @ W3 + b3
 

@@ -21,8 +21,13 @@ def test_forward_matches_cpu_restatement(hype):
     X, _ = _rand(2000, 1)
     p = indicator.init_params(3)
     s_gpu = indicator.score(X, p)
-    s_cpu = mlp_oracle.logits(X, p).max(axis=1)
-    assert np.abs(s_gpu - s_cpu).max() <= 1e-4 * max(1.0, np.abs(s_cpu).max())
+    # tensor-core inference: BF16 inputs and first hidden layer, FP32 accumulation; the
+    # FP32 sums can round a hidden value to the neighbouring BF16 number (2^-8 relative)
+    s_cpu = mlp_oracle.logits(X, p, act_bf16=True).max(axis=1)
+    err = np.abs(s_gpu - s_cpu)
+    scale = max(1.0, np.abs(s_cpu).max())
+    assert err.max() <= 2e-3 * scale
+    assert np.median(err) <= 1e-5 * scale
 
 
 def test_backward_matches_cpu_restatement(hype):
