@@ -18,7 +18,7 @@ F = C.POINTER(C.c_float)
 
 HYPE_OK, HYPE_ERR_ARG, HYPE_ERR_STATE, HYPE_ERR_CUDA, HYPE_ERR_NOMEM, HYPE_ERR_UNSUPPORTED = range(6)
 BC_PERIODIC, BC_REFLECTIVE, BC_TRANSMISSIVE, BC_ZERO = range(4)
-RECON_CWENO4, RECON_LINEAR4, RECON_LEARNED = 0, 1, 2
+RECON_CWENO4, RECON_LINEAR4, RECON_LEARNED, RECON_WENO3 = 0, 1, 2, 3
 PREC_FP64, PREC_FP32 = 0, 1
 DT_MONITOR, DT_FROZEN, DT_FIXED = 0, 1, 2
 FLUX_RUSANOV, FLUX_HLLC, FLUX_ROTHLLC = 0, 1, 2

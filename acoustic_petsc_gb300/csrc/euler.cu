@@ -271,7 +271,7 @@ __device__ __forceinline__ void store_first_order_g(const R* __restrict__ G, R* 
 // (4 warps x 2 x NTR x 32 floats, launched only with the positivity fallback on).
 template <typename R>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1)
-    k_recon(const R* __restrict__ G, R* __restrict__ T, Geo g, int linear, int pad, double gm1,
+    k_recon(const R* __restrict__ G, R* __restrict__ T, Geo g, int recon, int pad, double gm1,
             unsigned long long* __restrict__ counters) {
     extern __shared__ float ck_dyn[];
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
@@ -289,7 +289,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1)
     for (int c = 0; c < NV; ++c) {
         R s[33], cf[20];
         gather33g<R>(G + (long long)c * g.GN + ge, sy, sz, s);
-        cweno4<R>(s, linear != 0, cf);
+        if (recon == HYPE_RECON_WENO3) weno3<R>(s, cf);
+        else cweno4<R>(s, recon == HYPE_RECON_LINEAR4, cf);
         store_traces<R>(T, g, e, c, cf, ckp);
     }
     if (pad && !(f32 ? ck.ok : traces_admissible<R>(T, g, e, gm1))) {
@@ -514,11 +515,19 @@ __global__ void __launch_bounds__(256) k_update(const double* __restrict__ Fx, c
     }
 }
 
+// dt from the largest wave speed, rounded as each reference program does:
+// (1/3) (CFL h) / s_max (3d/weno4/Navier-Stokes-3D/rhs_function.c:438-440) or
+// (CFL h) / (3 s_max) (3d/weno3/Euler/rhs_function.c:383)
+__host__ __device__ inline double cfl_dt(double cfl_h, double smax, int recon) {
+    return recon == HYPE_RECON_WENO3 ? cfl_h / (3.0 * smax) : (1.0 / 3.0) * cfl_h / (smax + 0.0);
+}
+
 // dt of the coming step and the time update (one thread)
-__global__ void k_begin_step(DevScalars* ds, int dt_mode, int src_slot, int use_src, int reset_stages, double cfl_h) {
+__global__ void k_begin_step(DevScalars* ds, int dt_mode, int src_slot, int use_src, int reset_stages, double cfl_h,
+                             int recon) {
     if (use_src && dt_mode != HYPE_DT_FIXED) {
         const double smax = __longlong_as_double((long long)ds->smax_bits[src_slot]);
-        ds->dt = (1.0 / 3.0) * cfl_h / (smax + 0.0);
+        ds->dt = cfl_dt(cfl_h, smax, recon);
     }
     if (reset_stages)
         for (int s = 0; s < 4; ++s) ds->smax_bits[s] = 0ull;
@@ -652,7 +661,7 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
     const Geo& g = e->g;
     const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2);
     const bool f32 = e->p.precision == HYPE_PREC_FP32;
-    const int lin = e->p.recon == HYPE_RECON_LINEAR4;
+    const int rec = e->p.recon;
     prof_mark(e, 0, true);
     const dim3 bgh(128), ggh(cdiv(g.gx, 128), g.gy, g.nz + 2 * GW);
     if (f32) k_ghost<float><<<ggh, bgh, 0, e->stream>>>(Win, (float*)e->G, g);
@@ -669,10 +678,10 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
             k_recon_learned<double><<<gr, br, 0, e->stream>>>((const double*)e->G, (double*)e->T, g, e->mlp, e->logit_thr,
                                                               gm1, e->p.positivity, e->mlp_cnt);
     } else if (f32) {
-        k_recon<float><<<gr, br, ck_bytes, e->stream>>>((const float*)e->G, (float*)e->T, g, lin, e->p.positivity, gm1,
+        k_recon<float><<<gr, br, ck_bytes, e->stream>>>((const float*)e->G, (float*)e->T, g, rec, e->p.positivity, gm1,
                                                         e->mlp_cnt);
     } else {
-        k_recon<double><<<gr, br, 0, e->stream>>>((const double*)e->G, (double*)e->T, g, lin, e->p.positivity, gm1,
+        k_recon<double><<<gr, br, 0, e->stream>>>((const double*)e->G, (double*)e->T, g, rec, e->p.positivity, gm1,
                                                   e->mlp_cnt);
     }
     prof_mark(e, 0, false);
@@ -701,7 +710,7 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
         if (p->bc[f] < HYPE_BC_PERIODIC || p->bc[f] > HYPE_BC_TRANSMISSIVE) return HYPE_ERR_ARG;
     for (int d = 0; d < 3; ++d)
         if ((p->bc[2 * d] == HYPE_BC_PERIODIC) != (p->bc[2 * d + 1] == HYPE_BC_PERIODIC)) return HYPE_ERR_ARG;
-    if (p->recon != HYPE_RECON_CWENO4 && p->recon != HYPE_RECON_LINEAR4 && p->recon != HYPE_RECON_LEARNED) return HYPE_ERR_ARG;
+    if (p->recon < HYPE_RECON_CWENO4 || p->recon > HYPE_RECON_WENO3) return HYPE_ERR_ARG;
     if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32) return HYPE_ERR_ARG;
     if (p->dt_mode < HYPE_DT_MONITOR || p->dt_mode > HYPE_DT_FIXED) return HYPE_ERR_ARG;
     if (p->flux < HYPE_FLUX_RUSANOV || p->flux > HYPE_FLUX_ROTHLLC) return HYPE_ERR_ARG;
@@ -813,7 +822,7 @@ static int rhs_core(hype_euler* e, const double* dU, double* dRHS, double* dt_ou
     if ((rc = launch_update(e, nullptr, nullptr, dRHS, st))) return rc;
     if ((rc = read_scalars(e))) return rc;
     const double smax = bits_to_double(e->hs->smax_bits[4]);
-    if (dt_out) *dt_out = (1.0 / 3.0) * (e->p.cfl * e->p.h) / (smax + 0.0);
+    if (dt_out) *dt_out = cfl_dt(e->p.cfl * e->p.h, smax, e->p.recon);
     if (e->hs->bad != ~0ull) return HYPE_ERR_STATE;
     return HYPE_OK;
 }
@@ -883,12 +892,12 @@ extern "C" int hype_euler_step(hype_euler* e, int nsteps, double* t_inout, doubl
         if (s == 0 && first_from_rhs) {
             // the initial RHS call of hype.c:175 is this step's first stage RHS
             if ((rc = launch_rhs(e, e->U, 0))) return rc;
-            k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 0, 1, 0, cfl_h);
+            k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 0, 1, 0, cfl_h, e->p.recon);
             HYPE_LAUNCHED(1);
         } else {
             // dt: MONITOR refreshes it from the last stage of the previous step
             const int use_src = (mode == HYPE_DT_MONITOR) && s > 0;
-            k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 3, use_src, 1, cfl_h);
+            k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 3, use_src, 1, cfl_h, e->p.recon);
             HYPE_LAUNCHED(1);
             if ((rc = launch_rhs(e, e->U, 0))) return rc;
         }
@@ -904,7 +913,7 @@ extern "C" int hype_euler_step(hype_euler* e, int nsteps, double* t_inout, doubl
     *t_inout = e->hs->t;
     const double smax3 = bits_to_double(e->hs->smax_bits[3]);
     if (nsteps > 0 && mode == HYPE_DT_MONITOR)
-        *dt_inout = (1.0 / 3.0) * cfl_h / (smax3 + 0.0);
+        *dt_inout = cfl_dt(cfl_h, smax3, e->p.recon);
     else
         *dt_inout = e->hs->dt;
     if (st) {
@@ -942,7 +951,7 @@ extern "C" int hype_euler_indicator_stats(hype_euler* e, long long* flagged, lon
 }
 
 extern "C" int hype_euler_set_recon(hype_euler* e, int recon) {
-    if (!e || recon < HYPE_RECON_CWENO4 || recon > HYPE_RECON_LEARNED) return HYPE_ERR_ARG;
+    if (!e || recon < HYPE_RECON_CWENO4 || recon > HYPE_RECON_WENO3) return HYPE_ERR_ARG;
     HYPE_CK(cudaStreamSynchronize(e->stream));
     e->p.recon = recon;
     return HYPE_OK;
@@ -1042,7 +1051,7 @@ extern "C" int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* 
         if (p->bc[f] < HYPE_BC_PERIODIC || p->bc[f] > HYPE_BC_TRANSMISSIVE) return HYPE_ERR_ARG;
     for (int d = 0; d < 3; ++d)
         if ((p->bc[2 * d] == HYPE_BC_PERIODIC) != (p->bc[2 * d + 1] == HYPE_BC_PERIODIC)) return HYPE_ERR_ARG;
-    if (p->recon != HYPE_RECON_CWENO4 && p->recon != HYPE_RECON_LINEAR4) return HYPE_ERR_ARG;
+    if (p->recon != HYPE_RECON_CWENO4 && p->recon != HYPE_RECON_LINEAR4 && p->recon != HYPE_RECON_WENO3) return HYPE_ERR_ARG;
     if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32) return HYPE_ERR_ARG;
     if (p->flux < HYPE_FLUX_RUSANOV || p->flux > HYPE_FLUX_ROTHLLC) return HYPE_ERR_ARG;
     const long long ne = (long long)(p->nx + 2) * (p->ny + 2) * (p->nz + 2);
@@ -1089,14 +1098,14 @@ extern "C" int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* 
     // admissibility word must start cleared; traces and fluxes are fully rewritten
     k_reset_slot<<<1, 1, 0, s>>>(ds, 4);
     const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2);
-    const int lin = p->recon == HYPE_RECON_LINEAR4;
+    const int rec = p->recon;
     const dim3 bgh(128), ggh(cdiv(g.gx, 128), g.gy, g.nz + 2 * GW);
     if (p->precision == HYPE_PREC_FP32) {
         k_ghost<float><<<ggh, bgh, 0, s>>>(dU, (float*)G, g);
-        k_recon<float><<<gr, br, 0, s>>>((const float*)G, (float*)T, g, lin, 0, p->gamma - 1.0, nullptr);
+        k_recon<float><<<gr, br, 0, s>>>((const float*)G, (float*)T, g, rec, 0, p->gamma - 1.0, nullptr);
     } else {
         k_ghost<double><<<ggh, bgh, 0, s>>>(dU, (double*)G, g);
-        k_recon<double><<<gr, br, 0, s>>>((const double*)G, (double*)T, g, lin, 0, p->gamma - 1.0, nullptr);
+        k_recon<double><<<gr, br, 0, s>>>((const double*)G, (double*)T, g, rec, 0, p->gamma - 1.0, nullptr);
     }
     launch_faces(g, T, Fx, Fy, Fz, p->gamma, ds, 4, p->precision == HYPE_PREC_FP32, p->flux, s);
     const Stage st{0.0, 0.0, 0.0, 1};
@@ -1108,7 +1117,7 @@ extern "C" int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* 
         HYPE_CK(cudaMemcpyAsync(&w[0], &ds->smax_bits[4], sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
         HYPE_CK(cudaMemcpyAsync(&w[1], &ds->bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
         HYPE_CK(cudaStreamSynchronize(s));
-        *dt_out = (1.0 / 3.0) * (p->cfl * p->h) / (bits_to_double(w[0]) + 0.0);
+        *dt_out = cfl_dt(p->cfl * p->h, bits_to_double(w[0]), p->recon);
         if (w[1] != ~0ull) return HYPE_ERR_STATE;
     }
     return HYPE_OK;

@@ -56,34 +56,53 @@ struct Weights;
 
 // CWENO4 coefficients (20) of one variable from its 33-point stencil.
 // linear: the R4 polynomial (the limit in which all nonlinear weights equal the linear ones).
+//
+// The mathematics is the reference's weno() (3d/weno4/Viscous-Multiphase-Fourth-Order/
+// reconstruction.c:38-259); the operation count is cut for the FP64 pipe, which bounds
+// this kernel on GB300, with every value still formed in the working precision:
+//  * per axis the differences a = u(+1) - u(-1), b = u(+2) - u(-2) and the sum
+//    u(-1) + u(+1) serve the R4 first/second/third derivatives (:90-108) and the
+//    centred R3 derivatives (:123-140);
+//  * per axis pair the corner sums P = pp - mm, Q = mp - pm give the R4 cross term,
+//    both mixed third derivatives and the centred R3 cross term (the same value as
+//    the R4 one, :94-96 and :133-135);
+//  * the squared sums shared by IS_R4 (:110-116) and IS_R3 of the centred stencil
+//    (:205-213) are formed once;
+//  * CWENO combination (:215-257): P = (w4/g4)(P4 - sum_k g_k P_k) + sum_k w_k P_k is
+//    evaluated per coefficient as (w4/g4) c4 + sum_k (w_k - (w4/g4) g_k) c_k, one
+//    weighted sum instead of a linear and a nonlinear one.
 template <typename R>
-__device__ __forceinline__ void cweno4(const R* __restrict__ s, bool linear, R* __restrict__ cf, R* wdev = nullptr) {
+__host__ __device__ __forceinline__ void cweno4(const R* __restrict__ s, bool linear, R* __restrict__ cf,
+                                                R* wdev = nullptr) {
     const R u0 = s[0];
     const R h = R(0.5), q = R(0.25);
-    R d4[3], dd4[3], ddd4[3];
+    R d4[3], dd4[3], ddd4[3], c1[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const R m2 = s[S1(d, -2)], m1 = s[S1(d, -1)], p1 = s[S1(d, 1)], p2 = s[S1(d, 2)];
-        d4[d] = R(1. / 120.) * (R(11.0) * m2 - R(82.0) * m1 + R(82.0) * p1 - R(11.0) * p2);
-        dd4[d] = h * (m1 - R(2.0) * u0 + p1);
-        ddd4[d] = R(1. / 12.) * (-m2 + R(2.0) * (m1 - p1) + p2);
+        const R a = p1 - m1, b = p2 - m2;
+        d4[d] = R(82. / 120.) * a - R(11. / 120.) * b;  // (11 m2 - 82 m1 + 82 p1 - 11 p2) / 120
+        dd4[d] = h * (m1 + p1) - u0;                    // (m1 - 2 u0 + p1) / 2
+        ddd4[d] = R(1. / 12.) * b - R(1. / 6.) * a;      // (-m2 + 2 (m1 - p1) + p2) / 12
+        c1[d] = h * a;                                  // centred R3 first derivative
     }
 #define QV(a, sa, b, sb) s[SQ(a, sa, b, sb)]
-    // mixed second derivatives (pairs xy, yz, zx as in the reference)
-    const R xy4 = q * (QV(0, 0, 1, 0) - QV(0, 0, 1, 1) - QV(0, 1, 1, 0) + QV(0, 1, 1, 1));
-    const R yz4 = q * (QV(1, 0, 2, 0) - QV(1, 0, 2, 1) - QV(1, 1, 2, 0) + QV(1, 1, 2, 1));
-    const R xz4 = q * (QV(2, 0, 0, 0) - QV(2, 0, 0, 1) - QV(2, 1, 0, 0) + QV(2, 1, 0, 1));
-    // third derivatives u_aab = 0.25(-mm+mp-pm+pp) + 0.5(u_b- - u_b+), u_abb = 0.5(u_a- - u_a+) + 0.25(pp-mm-mp+pm)
-#define AAB(a, b) (q * (-QV(a, 0, b, 0) + QV(a, 0, b, 1) - QV(a, 1, b, 0) + QV(a, 1, b, 1)) + h * (s[S1(b, -1)] - s[S1(b, 1)]))
-#define ABB(a, b) (h * (s[S1(a, -1)] - s[S1(a, 1)]) + q * (QV(a, 1, b, 1) - QV(a, 0, b, 0) - QV(a, 0, b, 1) + QV(a, 1, b, 0)))
-    const R xxy = AAB(0, 1), xyy = ABB(0, 1);
-    const R yyz = AAB(1, 2), yzz = ABB(1, 2);
-    const R xxz = AAB(0, 2), xzz = ABB(0, 2);
-#undef AAB
-#undef ABB
-    const R xyz = R(0.125) * (s[SO(1, 1, 1)] - s[SO(0, 1, 1)] - s[SO(1, 0, 1)] - s[SO(1, 1, 0)] + s[SO(0, 0, 1)] +
-                              s[SO(0, 1, 0)] + s[SO(1, 0, 0)] - s[SO(0, 0, 0)]);
+    // pairs 0: (x,y), 1: (y,z), 2: (x,z); corners mm, mp, pm, pp (first index: sign along a)
+    R cx[3], aab[3], abb[3];
+#pragma unroll
+    for (int P = 0; P < 3; ++P) {
+        const int a = P == 1 ? 1 : 0, b = P == 0 ? 1 : 2;
+        const R mm = QV(a, 0, b, 0), mp = QV(a, 0, b, 1), pm = QV(a, 1, b, 0), pp = QV(a, 1, b, 1);
+        const R Pd = pp - mm, Qd = mp - pm;
+        cx[P] = q * ((mm + pp) - (mp + pm));  // u_ab
+        aab[P] = q * (Pd + Qd) - c1[b];       // u_aab = 0.25 (-mm + mp - pm + pp) + 0.5 (u_b- - u_b+)
+        abb[P] = q * (Pd - Qd) - c1[a];       // u_abb = 0.5 (u_a- - u_a+) + 0.25 (pp - mm - mp + pm)
+    }
+#undef QV
+    const R xyz = R(0.125) * ((s[SO(1, 1, 1)] - s[SO(0, 0, 0)]) + ((s[SO(0, 0, 1)] + s[SO(0, 1, 0)] + s[SO(1, 0, 0)]) -
+                                                                 (s[SO(0, 1, 1)] + s[SO(1, 0, 1)] + s[SO(1, 1, 0)])));
     cf[0] = u0;
+    // the cubic part is the R4 one scaled by w4/g4 (1 in the linear limit)
     if (linear) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
@@ -91,25 +110,24 @@ __device__ __forceinline__ void cweno4(const R* __restrict__ s, bool linear, R* 
             cf[CSQ(d)] = dd4[d];
             cf[CCUBE(d)] = ddd4[d];
         }
-        cf[7] = xy4; cf[8] = yz4; cf[9] = xz4;
-        cf[13] = xxy; cf[14] = xyy; cf[15] = yyz; cf[16] = yzz; cf[17] = xxz; cf[18] = xzz; cf[19] = xyz;
+        cf[7] = cx[0]; cf[8] = cx[1]; cf[9] = cx[2];
+        cf[13] = aab[0]; cf[14] = abb[0]; cf[15] = aab[1]; cf[16] = abb[1]; cf[17] = aab[2]; cf[18] = abb[2]; cf[19] = xyz;
         if (wdev) *wdev = R(0);
         return;
     }
     const R r13_3 = R(13. / 3.), r7_6 = R(7. / 6.);
-    const R IS4 = d4[0] * d4[0] + d4[1] * d4[1] + d4[2] * d4[2] + r13_3 * (dd4[0] * dd4[0] + dd4[1] * dd4[1] + dd4[2] * dd4[2]) +
-                  r7_6 * (xy4 * xy4 + yz4 * yz4 + xz4 * xz4) + R(0.2) * (d4[0] * ddd4[0] + d4[1] * ddd4[1] + d4[2] * ddd4[2]) +
-                  R(4.7) * (xxy * xxy + xxz * xxz + xyy * xyy + xzz * xzz + yyz * yyz + yzz * yzz) +
-                  R(39.06) * (ddd4[0] * ddd4[0] + ddd4[1] * ddd4[1] + ddd4[2] * ddd4[2]) + R(61. / 48.) * xyz * xyz;
-    // centred R3 stencil: first derivatives c1[d], second = dd4[d], cross terms (xy, yz, xz)
-    R c1[3];
+    R c1sq[3], ddsq[3], cxsq[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) c1[d] = h * (s[S1(d, 1)] - s[S1(d, -1)]);
-    const R cx[3] = {q * (QV(0, 1, 1, 1) - QV(0, 1, 1, 0) - QV(0, 0, 1, 1) + QV(0, 0, 1, 0)),
-                     q * (QV(1, 1, 2, 1) - QV(1, 1, 2, 0) - QV(1, 0, 2, 1) + QV(1, 0, 2, 0)),
-                     q * (QV(2, 1, 0, 1) - QV(2, 1, 0, 0) - QV(2, 0, 0, 1) + QV(2, 0, 0, 0))};
-    const R IS0 = (c1[0] * c1[0] + c1[1] * c1[1] + c1[2] * c1[2]) + r13_3 * (dd4[0] * dd4[0] + dd4[1] * dd4[1] + dd4[2] * dd4[2]) +
-                  r7_6 * (cx[0] * cx[0] + cx[1] * cx[1] + cx[2] * cx[2]);
+    for (int d = 0; d < 3; ++d) {
+        c1sq[d] = c1[d] * c1[d];
+        ddsq[d] = dd4[d] * dd4[d];
+        cxsq[d] = cx[d] * cx[d];
+    }
+    const R common = r13_3 * (ddsq[0] + ddsq[1] + ddsq[2]) + r7_6 * (cxsq[0] + cxsq[1] + cxsq[2]);
+    const R IS4 = d4[0] * (d4[0] + R(0.2) * ddd4[0]) + d4[1] * (d4[1] + R(0.2) * ddd4[1]) + d4[2] * (d4[2] + R(0.2) * ddd4[2]) +
+                  common + R(4.7) * (aab[0] * aab[0] + abb[0] * abb[0] + aab[1] * aab[1] + abb[1] * abb[1] + aab[2] * aab[2] + abb[2] * abb[2]) +
+                  R(39.06) * (ddd4[0] * ddd4[0] + ddd4[1] * ddd4[1] + ddd4[2] * ddd4[2]) + R(61. / 48.) * xyz * xyz;
+    const R IS0 = (c1sq[0] + c1sq[1] + c1sq[2]) + common;
     // one-sided stencils: index 2d (towards +d) and 2d+1 (towards -d): first and second
     // derivative along d and the two cross terms that involve d
     R sd1[6], sd2[6], sx1[6], sx2[6], IS3[6];
@@ -119,22 +137,22 @@ __device__ __forceinline__ void cweno4(const R* __restrict__ s, bool linear, R* 
         const int k1 = (d + e1 == 1) ? 0 : (d + e1 == 3) ? 1 : 2;  // cross slot of (d,e1)
         const int k2 = (d + e2 == 1) ? 0 : (d + e2 == 3) ? 1 : 2;  // cross slot of (d,e2)
         const R p1 = s[S1(d, 1)], p2 = s[S1(d, 2)], m1 = s[S1(d, -1)], m2 = s[S1(d, -2)];
-        // towards +d
-        sd1[2 * d] = R(-1.5) * u0 + R(2.0) * p1 - h * p2;
-        sd2[2 * d] = h * (u0 - R(2.0) * p1 + p2);
-        sx1[2 * d] = h * (QV(d, 1, e1, 1) - QV(d, 1, e1, 0)) - c1[e1];
-        sx2[2 * d] = h * (QV(d, 1, e2, 1) - QV(d, 1, e2, 0)) - c1[e2];
-        // towards -d
-        sd1[2 * d + 1] = R(-2.0) * m1 + h * m2 + R(1.5) * u0;
-        sd2[2 * d + 1] = h * (m2 - R(2.0) * m1 + u0);
-        sx1[2 * d + 1] = h * (QV(d, 0, e1, 0) - QV(d, 0, e1, 1)) + c1[e1];
-        sx2[2 * d + 1] = h * (QV(d, 0, e2, 0) - QV(d, 0, e2, 1)) + c1[e2];
+        // towards +d: u_d = -1.5 u0 + 2 p1 - 0.5 p2, u_dd = 0.5 (u0 - 2 p1 + p2)
+        sd2[2 * d] = h * (u0 + p2) - p1;
+        sd1[2 * d] = (p1 - u0) - sd2[2 * d];
+        sx1[2 * d] = h * (s[SQ(d, 1, e1, 1)] - s[SQ(d, 1, e1, 0)]) - c1[e1];
+        sx2[2 * d] = h * (s[SQ(d, 1, e2, 1)] - s[SQ(d, 1, e2, 0)]) - c1[e2];
+        // towards -d: u_d = -2 m1 + 0.5 m2 + 1.5 u0, u_dd = 0.5 (m2 - 2 m1 + u0)
+        sd2[2 * d + 1] = h * (m2 + u0) - m1;
+        sd1[2 * d + 1] = (u0 - m1) + sd2[2 * d + 1];
+        sx1[2 * d + 1] = h * (s[SQ(d, 0, e1, 0)] - s[SQ(d, 0, e1, 1)]) + c1[e1];
+        sx2[2 * d + 1] = h * (s[SQ(d, 0, e2, 0)] - s[SQ(d, 0, e2, 1)]) + c1[e2];
         // the unchanged terms are summed directly (no subtraction from the centred sums:
         // IS values near zero must keep their relative accuracy)
         const int k3 = 3 - k1 - k2;
-        const R rest1 = c1[e1] * c1[e1] + c1[e2] * c1[e2];
-        const R rest2 = dd4[e1] * dd4[e1] + dd4[e2] * dd4[e2];
-        const R restx = cx[k3] * cx[k3];
+        const R rest1 = c1sq[e1] + c1sq[e2];
+        const R rest2 = ddsq[e1] + ddsq[e2];
+        const R restx = cxsq[k3];
 #pragma unroll
         for (int sg = 0; sg < 2; ++sg) {
             const int m = 2 * d + sg;
@@ -144,7 +162,6 @@ __device__ __forceinline__ void cweno4(const R* __restrict__ s, bool linear, R* 
             IS3[m] = a1 + r13_3 * a2 + r7_6 * a3;
         }
     }
-#undef QV
     // nonlinear weights: gammaHi = gammaLo = 0.85, p = 4, eps = 1e-12
     const R gH = R(0.85), g0 = R((1.0 - 0.85) * 0.85), gs = R((1. / 6.) * (1 - 0.85) * (1 - 0.85));
     R w4, w0, ws[6];
@@ -156,64 +173,74 @@ __device__ __forceinline__ void cweno4(const R* __restrict__ s, bool linear, R* 
         for (int m = 0; m < 6; ++m) d = fmax(d, fabs(ws[m] - gs));
         *wdev = d;
     }
-    // linear and nonlinear R3 combinations of every quantity; the weight of the
-    // centred value is summed from the stencils that keep it (all weights are positive)
-    const R wx = ws[0] + ws[1], wy = ws[2] + ws[3], wz = ws[4] + ws[5];
-    const R lin_c = g0 + R(4) * gs;  // gamma weight of the centred value for a quantity two sided stencils modify
+    // weights of the lower-order stencils' values in the combination: w_k - wr g_k
+    const R o0 = w0 - wr * g0;
+    R os[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) os[m] = ws[m] - wr * gs;
+    const R ox = os[0] + os[1], oy = os[2] + os[3], oz = os[4] + os[5];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const R wkeep = w0 + ((d == 0) ? wy + wz : (d == 1) ? wx + wz : wx + wy);
-        const R nl1 = wkeep * c1[d] + ws[2 * d] * sd1[2 * d] + ws[2 * d + 1] * sd1[2 * d + 1];
-        const R l1 = lin_c * c1[d] + gs * (sd1[2 * d] + sd1[2 * d + 1]);
-        cf[CLIN(d)] = wr * (d4[d] - l1) + nl1;
-        const R nl2 = wkeep * dd4[d] + ws[2 * d] * sd2[2 * d] + ws[2 * d + 1] * sd2[2 * d + 1];
-        const R l2 = lin_c * dd4[d] + gs * (sd2[2 * d] + sd2[2 * d + 1]);
-        cf[CSQ(d)] = wr * (dd4[d] - l2) + nl2;
+        // the centred values of direction d are kept by the centred stencil and by the
+        // one-sided stencils of the two other directions
+        const R okeep = o0 + ((d == 0) ? oy + oz : (d == 1) ? ox + oz : ox + oy);
+        cf[CLIN(d)] = wr * d4[d] + okeep * c1[d] + os[2 * d] * sd1[2 * d] + os[2 * d + 1] * sd1[2 * d + 1];
+        cf[CSQ(d)] = (wr + okeep) * dd4[d] + os[2 * d] * sd2[2 * d] + os[2 * d + 1] * sd2[2 * d + 1];
     }
     // cross terms: slot 0 (xy) is modified by the x-sided (via sx1 of d=0) and y-sided (sx1 of d=1) stencils,
     // slot 1 (yz) by y-sided (sx2 of d=1) and z-sided (sx2 of d=2), slot 2 (xz) by x-sided (sx2 of d=0) and z-sided (sx1 of d=2)
-    {
-        const R lin_x = g0 + R(2) * gs;
-        const R nlxy = (w0 + wz) * cx[0] + ws[0] * sx1[0] + ws[1] * sx1[1] + ws[2] * sx1[2] + ws[3] * sx1[3];
-        const R lxy = lin_x * cx[0] + gs * (sx1[0] + sx1[1] + sx1[2] + sx1[3]);
-        const R nlyz = (w0 + wx) * cx[1] + ws[2] * sx2[2] + ws[3] * sx2[3] + ws[4] * sx2[4] + ws[5] * sx2[5];
-        const R lyz = lin_x * cx[1] + gs * (sx2[2] + sx2[3] + sx2[4] + sx2[5]);
-        const R nlxz = (w0 + wy) * cx[2] + ws[0] * sx2[0] + ws[1] * sx2[1] + ws[4] * sx1[4] + ws[5] * sx1[5];
-        const R lxz = lin_x * cx[2] + gs * (sx2[0] + sx2[1] + sx1[4] + sx1[5]);
-        cf[7] = wr * (xy4 - lxy) + nlxy;
-        cf[8] = wr * (yz4 - lyz) + nlyz;
-        cf[9] = wr * (xz4 - lxz) + nlxz;
-    }
+    cf[7] = (wr + o0 + oz) * cx[0] + os[0] * sx1[0] + os[1] * sx1[1] + os[2] * sx1[2] + os[3] * sx1[3];
+    cf[8] = (wr + o0 + ox) * cx[1] + os[2] * sx2[2] + os[3] * sx2[3] + os[4] * sx2[4] + os[5] * sx2[5];
+    cf[9] = (wr + o0 + oy) * cx[2] + os[0] * sx2[0] + os[1] * sx2[1] + os[4] * sx1[4] + os[5] * sx1[5];
 #pragma unroll
     for (int d = 0; d < 3; ++d) cf[CCUBE(d)] = wr * ddd4[d];
-    cf[13] = wr * xxy; cf[14] = wr * xyy; cf[15] = wr * yyz; cf[16] = wr * yzz;
-    cf[17] = wr * xxz; cf[18] = wr * xzz; cf[19] = wr * xyz;
+    cf[13] = wr * aab[0]; cf[14] = wr * abb[0]; cf[15] = wr * aab[1]; cf[16] = wr * abb[1];
+    cf[17] = wr * aab[2]; cf[18] = wr * abb[2]; cf[19] = wr * xyz;
 }
 
-// w = gamma / (IS + eps)^4, normalised.  FP64: directly, as the reference does.
+// w = gamma / (IS + eps)^4, normalised.  FP64: the eight reciprocals 1/(IS + eps)^2
+// come from one division by their product (prefix products, then back-substitution:
+// 21 multiplications instead of 7 more reciprocals); a product outside the normal
+// range (IS beyond ~1e36) takes the plain reciprocals instead.
 template <>
 struct Weights<double> {
-    __device__ __forceinline__ static void compute(double IS4, double IS0, const double* IS3, double gH, double g0, double gs,
+    __host__ __device__ __forceinline__ static void compute(double IS4, double IS0, const double* IS3, double gH, double g0, double gs,
                                                    double& w4, double& w0, double* ws) {
-        double t = IS4 + 1.0e-12;
-        t *= t;
-        w4 = gH / (t * t);
-        t = IS0 + 1.0e-12;
-        t *= t;
-        w0 = g0 / (t * t);
+        double q[8], P[8], r[8];
+        q[0] = IS4 + 1.0e-12;
+        q[1] = IS0 + 1.0e-12;
+#pragma unroll
+        for (int m = 0; m < 6; ++m) q[2 + m] = IS3[m] + 1.0e-12;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) q[k] *= q[k];
+        P[0] = q[0];
+#pragma unroll
+        for (int k = 1; k < 8; ++k) P[k] = P[k - 1] * q[k];
+        if (P[7] > 1.0e-290 && P[7] < 1.0e290) {
+            double inv = 1.0 / P[7];
+#pragma unroll
+            for (int k = 7; k > 0; --k) {
+                r[k] = inv * P[k - 1];
+                inv *= q[k];
+            }
+            r[0] = inv;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) r[k] = 1.0 / q[k];
+        }
+        w4 = gH * (r[0] * r[0]);
+        w0 = g0 * (r[1] * r[1]);
         double total = w4 + w0;
 #pragma unroll
         for (int m = 0; m < 6; ++m) {
-            t = IS3[m] + 1.0e-12;
-            t *= t;
-            ws[m] = gs / (t * t);
+            ws[m] = gs * (r[2 + m] * r[2 + m]);
             total += ws[m];
         }
-        const double r = 1.0 / total;
-        w4 *= r;
-        w0 *= r;
+        const double rt = 1.0 / total;
+        w4 *= rt;
+        w0 *= rt;
 #pragma unroll
-        for (int m = 0; m < 6; ++m) ws[m] *= r;
+        for (int m = 0; m < 6; ++m) ws[m] *= rt;
     }
 };
 
@@ -221,7 +248,7 @@ struct Weights<double> {
 // smallest (IS + eps), which is the same normalised quantity.
 template <>
 struct Weights<float> {
-    __device__ __forceinline__ static void compute(float IS4, float IS0, const float* IS3, float gH, float g0, float gs,
+    __host__ __device__ __forceinline__ static void compute(float IS4, float IS0, const float* IS3, float gH, float g0, float gs,
                                                    float& w4, float& w0, float* ws) {
         float s4 = IS4 + 1.0e-12f, s0 = IS0 + 1.0e-12f, ss[6];
         float mn = fminf(s4, s0);
@@ -251,6 +278,90 @@ struct Weights<float> {
         for (int m = 0; m < 6; ++m) ws[m] *= inv;
     }
 };
+
+// Normalised WENO weights w_m = gam_m / (IS_m + eps)^4 / sum, eps = 1e-12.  FP64:
+// directly, as 3d/weno3/Euler/reconstruction.c:60-67 does; FP32: from ratios to the
+// smallest IS + eps, because (1e-12)^4 underflows.
+template <typename R, int M>
+__device__ __forceinline__ void weno_weights(const R* IS, const R* gam, R* w) {
+    if (sizeof(R) == sizeof(double)) {
+        R total = R(0);
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            R t = IS[m] + R(1.0e-12);
+            t *= t;
+            w[m] = gam[m] / (t * t);
+            total += w[m];
+        }
+        const R r = R(1) / total;
+#pragma unroll
+        for (int m = 0; m < M; ++m) w[m] *= r;
+    } else {
+        R mn = IS[0] + R(1.0e-12);
+#pragma unroll
+        for (int m = 1; m < M; ++m) mn = fmin(mn, IS[m] + R(1.0e-12));
+        R total = R(0);
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            R r = mn / (IS[m] + R(1.0e-12));
+            r *= r;
+            w[m] = gam[m] * r * r;
+            total += w[m];
+        }
+        const R inv = R(1) / total;
+#pragma unroll
+        for (int m = 0; m < M; ++m) w[m] *= inv;
+    }
+}
+
+// Third-order WENO coefficients (the first 10 of the 20-term basis; the cubic ones
+// are zero) of one variable from the 25 axis and face-diagonal points of its
+// 33-point stencil, following 3d/weno3/Euler/reconstruction.c:29-177: per axis the
+// three one-sided/central quadratics with linear weights 1 : 100 : 1 (:54-106),
+// then per axis pair the four corner-based cross terms with equal weights (:108-163).
+template <typename R>
+__device__ __forceinline__ void weno3(const R* __restrict__ s, R* __restrict__ cf) {
+    const R u0 = s[0];
+    cf[0] = u0;
+    const R h = R(0.5), r13_3 = R(13. / 3.);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const R m2 = s[S1(d, -2)], m1 = s[S1(d, -1)], p1 = s[S1(d, 1)], p2 = s[S1(d, 2)];
+        R ux[3], uxx[3], IS[3], w[3];
+        ux[0] = R(-2.0) * m1 + h * m2 + R(1.5) * u0;
+        uxx[0] = h * (m2 - R(2.0) * m1 + u0);
+        ux[1] = h * (p1 - m1);
+        uxx[1] = h * (m1 - R(2.0) * u0 + p1);
+        ux[2] = R(-1.5) * u0 + R(2.0) * p1 - h * p2;
+        uxx[2] = h * (u0 - R(2.0) * p1 + p2);
+#pragma unroll
+        for (int m = 0; m < 3; ++m) IS[m] = ux[m] * ux[m] + r13_3 * uxx[m] * uxx[m];
+        const R gam[3] = {R(1), R(100), R(1)};
+        weno_weights<R, 3>(IS, gam, w);
+        cf[CLIN(d)] = w[0] * ux[0] + w[1] * ux[1] + w[2] * ux[2];
+        cf[CSQ(d)] = w[0] * uxx[0] + w[1] * uxx[1] + w[2] * uxx[2];
+    }
+    // cross terms of the pairs (x,y) -> 7, (y,z) -> 8, (z,x) -> 9
+#pragma unroll
+    for (int P = 0; P < 3; ++P) {
+        const int a = P == 0 ? 0 : P == 1 ? 1 : 2, b = P == 0 ? 1 : P == 1 ? 2 : 0;
+        const R pp = s[SQ(a, 1, b, 1)], pm = s[SQ(a, 1, b, 0)], mp = s[SQ(a, 0, b, 1)], mm = s[SQ(a, 0, b, 0)];
+        const R ca = cf[CLIN(a)], cb = cf[CLIN(b)], caa = cf[CSQ(a)], cbb = cf[CSQ(b)];
+        R u[4], IS[4], w[4];
+        u[0] = pp - u0 - ca - cb - caa - cbb;
+        u[1] = -pm + u0 + ca - cb + caa + cbb;
+        u[2] = -mp + u0 - ca + cb + caa + cbb;
+        u[3] = mm - u0 + ca + cb - caa - cbb;
+        const R temp = R(4.0) * (caa * caa + cbb * cbb);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) IS[m] = temp + u[m] * u[m];
+        const R gam[4] = {R(1), R(1), R(1), R(1)};
+        weno_weights<R, 4>(IS, gam, w);
+        cf[7 + P] = w[0] * u[0] + w[1] * u[1] + w[2] * u[2] + w[3] * u[3];
+    }
+#pragma unroll
+    for (int q = 10; q < 20; ++q) cf[q] = R(0);
+}
 
 // The 8 traces of the two faces normal to d (4 Gauss points each) from the
 // coefficients: even/odd split of the polynomial in the normal coordinate.
@@ -297,16 +408,20 @@ __device__ __forceinline__ R rusanov(const R* QL, const R* QR, R gamma, R gm1, R
         const R ir = R(1) / rho;
         const R u = ir * Q[1], v = ir * Q[2], w = ir * Q[3];
         const R E = Q[4];
-        const R p = gm1 * (E - R(0.5) * rho * (u * u + v * v + w * w));
-        bad |= (rho < R(1.0e-14)) || (p < R(1.0e-12)) || !(rho == rho);
+        // 0.5 rho |u|^2 as 0.5 (m . u); the floors rho >= 1e-14, p >= 1e-12 (a NaN fails both)
+        const R p = gm1 * (E - R(0.5) * (Q[1] * u + Q[2] * v + Q[3] * w));
+        bad |= !(rho >= R(1.0e-14) && p >= R(1.0e-12));
         const R un = (D == 0) ? u : (D == 1) ? v : w;
-        const R mun = rho * un;
+        const R mun = Q[1 + D];
         Fo[0] = mun;
         Fo[1] = mun * u + ((D == 0) ? p : R(0));
         Fo[2] = mun * v + ((D == 1) ? p : R(0));
         Fo[3] = mun * w + ((D == 2) ? p : R(0));
         Fo[4] = (E + p) * un;
-        const R a = sqrt(ir * gamma * p);
+        // sound speed sqrt(gamma p / rho) as x rsqrt(x): it only scales the dissipation
+        // s (QR - QL) and sets dt, where a last-bit difference is immaterial
+        const R x = ir * gamma * p;
+        const R a = x * rsqrt(x);
         (side ? sR : sL) = fabs(un) + a;
     }
     const R s = sL < sR ? sR : sL;

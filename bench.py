@@ -199,6 +199,12 @@ def cpu_ctcs_rate(n: int, steps: int):
 
 
 # ------------------------------------------------------------------ GPU workloads
+RECON_TAG = {0: "cweno4", 1: "cweno4_linear", 3: "weno3"}
+RECON_NAME = {0: "CWENO4 (gamma 0.85)", 1: "linear R4", 3: "WENO3 (3d/weno3/Euler, central weight 100)"}
+FLUX_TAG = {0: "rusanov", 1: "hllc", 2: "rothllc"}
+FLUX_NAME = {0: "Rusanov", 1: "HLLC", 2: "rotated HLLC"}
+
+
 def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0):
     import torch
 
@@ -288,9 +294,9 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0):
         "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == 0 else "f64 state / f32 recon+flux",
         "data": "synthetic: Gaussian acoustic pulse dp = 1e-3 exp(-r^2/(2*0.04^2)), 5^3-Gauss cell averages",
-        "config": {"workload": f"euler3d_cweno4{'_linear' if recon else ''}_rusanov_ssprk43_{n}",
+        "config": {"workload": f"euler3d_{RECON_TAG[recon]}_{FLUX_TAG[flux]}_ssprk43_{n}",
                    "cells": cells, "grid": [n, n, n], "domain": "[0,1]^3 periodic", "cfl": 0.4, "gamma": 1.4,
-                   "reconstruction": "linear R4" if recon else "CWENO4 (gamma 0.85)", "flux": "Rusanov",
+                   "reconstruction": RECON_NAME[recon], "flux": FLUX_NAME[flux],
                    "time": "SSPRK(4,3) (PETSc TSSSP RKS3, 4 stages), dt from the last stage (monitor semantics)",
                    "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "inputs larger than L2 (state 5*8*256^3 B = 671 MB > 129 MB); no flush"},
@@ -533,6 +539,7 @@ WORKLOADS = {
     "euler256_fp32": lambda a, *r: run_euler(a, *r, precision=1, recon=0),
     "euler256_linear": lambda a, *r: run_euler(a, *r, precision=0, recon=1),
     "euler256_fp32_linear": lambda a, *r: run_euler(a, *r, precision=1, recon=1),
+    "euler256_weno3": lambda a, *r: run_euler(a, *r, precision=0, recon=3),
     "euler64": lambda a, *r: run_euler(a, *r, precision=0, recon=0, n=64),
     "euler128": lambda a, *r: run_euler(a, *r, precision=0, recon=0, n=128),
     "euler128_fp32": lambda a, *r: run_euler(a, *r, precision=1, recon=0, n=128),

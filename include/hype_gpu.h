@@ -50,6 +50,9 @@ extern "C" {
                                 each cell from its normalised 5-point stencils; flagged or low-confidence
                                 cells take CWENO4, the others R4, and any cell whose R4 face traces break
                                 density/pressure positivity is redone with CWENO4 */
+#define HYPE_RECON_WENO3 3   /* third-order WENO: per-direction 3-stencil WENO with central weight 100 and
+                                4-stencil WENO cross terms, 10 coefficients
+                                (3d/weno3/Euler/reconstruction.c:29-177) */
 
 /* numerical flux across each face Gauss point (3d/weno4/Navier-Stokes-3D/pde.c) */
 #define HYPE_FLUX_RUSANOV 0  /* PDELLFRiemannSolver, pde.c:164-187 */

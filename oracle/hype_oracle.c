@@ -365,6 +365,64 @@ double orc_eval_poly3(double x, double y, double z, const double* c) {
            c[18] * x * (z * z - R1_12) + c[19] * x * y * z;
 }
 
+/* Third-order WENO (3d/weno3/Euler/reconstruction.c:29-177), operation for
+ * operation: per axis the quadratics of the left, centred and right stencils with
+ * weights 1 : 100 : 1 (:54-106), then per axis pair (xy, yz, zx) four corner-based
+ * cross terms with equal weights (:108-163); weights 1/pow(IS + 1e-12, 4). */
+static void weno3_axis(double u0, double m2, double m1, double p1, double p2, double* c1, double* c2) {
+    double u_x[3], u_xx[3], IS[3], wt[3], total;
+    u_x[0] = -2.0 * m1 + 0.5 * m2 + 1.5 * u0; u_xx[0] = 0.5 * (m2 - 2.0 * m1 + u0);
+    u_x[1] = 0.5 * (p1 - m1);                 u_xx[1] = 0.5 * (m1 - 2.0 * u0 + p1);
+    u_x[2] = -1.5 * u0 + 2.0 * p1 - 0.5 * p2; u_xx[2] = 0.5 * (u0 - 2.0 * p1 + p2);
+    for (int i = 0; i < 3; ++i) {
+        IS[i] = u_x[i] * u_x[i] + R13_3 * u_xx[i] * u_xx[i];
+        wt[i] = 1.0 / pow(IS[i] + 1.0e-12, 4.0);
+    }
+    wt[1] = 100.0 * wt[1];
+    total = wt[0] + wt[1] + wt[2];
+    wt[0] = wt[0] / total; wt[1] = wt[1] / total; wt[2] = wt[2] / total;
+    *c1 = wt[0] * u_x[0] + wt[1] * u_x[1] + wt[2] * u_x[2];
+    *c2 = wt[0] * u_xx[0] + wt[1] * u_xx[1] + wt[2] * u_xx[2];
+}
+
+/* pair (a, b) with a's and b's first/second coefficients; pp = u(a+1, b+1) etc. */
+static double weno3_cross(double u0, double pp, double pm, double mp, double mm, double ca, double cb, double caa, double cbb) {
+    double u_xy[4], IS[4], wt[4], total;
+    u_xy[0] = pp - u0 - ca - cb - caa - cbb;
+    u_xy[1] = -pm + u0 + ca - cb + caa + cbb;
+    u_xy[2] = -mp + u0 - ca + cb + caa + cbb;
+    u_xy[3] = mm - u0 + ca + cb - caa - cbb;
+    const double temp = 4.0 * (caa * caa + cbb * cbb);
+    for (int i = 0; i < 4; ++i) {
+        IS[i] = temp + u_xy[i] * u_xy[i];
+        wt[i] = 1.0 / pow(IS[i] + 1.0e-12, 4.0);
+    }
+    total = wt[0] + wt[1] + wt[2] + wt[3];
+    wt[0] = wt[0] / total; wt[1] = wt[1] / total; wt[2] = wt[2] / total; wt[3] = wt[3] / total;
+    return wt[0] * u_xy[0] + wt[1] * u_xy[1] + wt[2] * u_xy[2] + wt[3] * u_xy[3];
+}
+
+/* coef[0..9] in the basis of 3d/weno3/Euler/reconstruction.c:12-16; coef[10..19] = 0 */
+static void weno3(const Stencil* s, double* coef) {
+    const double u0 = s->c;
+    coef[0] = u0;
+    for (int d = 0; d < 3; ++d) weno3_axis(u0, s->m2[d], s->m1[d], s->p1[d], s->p2[d], &coef[1 + d], &coef[4 + d]);
+    /* q[a][b][sa][sb]: the point at (a: 2sa-1, b: 2sb-1) */
+    coef[7] = weno3_cross(u0, s->q[0][1][1][1], s->q[0][1][1][0], s->q[0][1][0][1], s->q[0][1][0][0], coef[1], coef[2],
+                          coef[4], coef[5]);
+    coef[8] = weno3_cross(u0, s->q[1][2][1][1], s->q[1][2][1][0], s->q[1][2][0][1], s->q[1][2][0][0], coef[2], coef[3],
+                          coef[5], coef[6]);
+    coef[9] = weno3_cross(u0, s->q[2][0][1][1], s->q[2][0][1][0], s->q[2][0][0][1], s->q[2][0][0][0], coef[3], coef[1],
+                          coef[6], coef[4]);
+    for (int q = 10; q < 20; ++q) coef[q] = 0.0;
+}
+
+/* evaluate_polynomial of 3d/weno3/Euler/reconstruction.c:12-16 (10 terms, same order) */
+static double eval_poly_w3(double x, double y, double z, const double* c) {
+    return c[0] + c[1] * x + c[2] * y + c[3] * z + c[4] * (x * x - R1_12) + c[5] * (y * y - R1_12) + c[6] * (z * z - R1_12) +
+           c[7] * x * y + c[8] * y * z + c[9] * z * x;
+}
+
 void orc_cweno4_ref_args(const double* Ux, const double* Uy, const double* Uz, const double* Uxy, const double* Uyz,
                          const double* Uzx, const double* Uxyz, double* coeffs) {
     Stencil s;
@@ -668,7 +726,7 @@ static void gather(const Padded* P, int i, int j, int k, int c, Stencil* s) {
 }
 
 /* traces of one cell: tr[c*NTR + f*4 + g], faces 0..5 = -x,+x,-y,+y,-z,+z */
-static void cell_traces_raw(const Padded* P, int i, int j, int k, double gam, int linear, double* tr);
+static void cell_traces_raw(const Padded* P, int i, int j, int k, double gam, int recon, double* tr);
 
 /* optional first-order fallback (positivity = 1): when a face trace has rho < 1e-14
  * or p < 1e-12 the cell is reconstructed at first order, the rule of
@@ -676,8 +734,8 @@ static void cell_traces_raw(const Padded* P, int i, int j, int k, double gam, in
 static int g_positivity = 0;
 static long g_fallbacks = 0;
 
-static void cell_traces(const Padded* P, int i, int j, int k, double gam, int linear, double* tr) {
-    cell_traces_raw(P, i, j, k, gam, linear, tr);
+static void cell_traces(const Padded* P, int i, int j, int k, double gam, int recon, double* tr) {
+    cell_traces_raw(P, i, j, k, gam, recon, tr);
     if (!g_positivity) return;
     const double gm1 = P->g->gamma - 1.0;
     for (int q = 0; q < NTR; ++q) {
@@ -696,13 +754,25 @@ static void cell_traces(const Padded* P, int i, int j, int k, double gam, int li
     }
 }
 
-static void cell_traces_raw(const Padded* P, int i, int j, int k, double gam, int linear, double* tr) {
+static void cell_traces_raw(const Padded* P, int i, int j, int k, double gam, int recon, double* tr) {
     Stencil s;
     double coef[20];
     for (int c = 0; c < NV; ++c) {
         gather(P, i, j, k, c, &s);
-        cweno4(&s, gam, linear, coef);
         double* t = tr + c * NTR;
+        if (recon == 3) {
+            weno3(&s, coef);
+            for (int g = 0; g < 4; ++g) {
+                t[0 * 4 + g] = eval_poly_w3(-0.5, GPX[g], GPY[g], coef);
+                t[1 * 4 + g] = eval_poly_w3(0.5, GPX[g], GPY[g], coef);
+                t[2 * 4 + g] = eval_poly_w3(GPX[g], -0.5, GPY[g], coef);
+                t[3 * 4 + g] = eval_poly_w3(GPX[g], 0.5, GPY[g], coef);
+                t[4 * 4 + g] = eval_poly_w3(GPX[g], GPY[g], -0.5, coef);
+                t[5 * 4 + g] = eval_poly_w3(GPX[g], GPY[g], 0.5, coef);
+            }
+            continue;
+        }
+        cweno4(&s, gam, recon == 1, coef);
         for (int g = 0; g < 4; ++g) {
             t[0 * 4 + g] = orc_eval_poly3(-0.5, GPX[g], GPY[g], coef);
             t[1 * 4 + g] = orc_eval_poly3(0.5, GPX[g], GPY[g], coef);
@@ -744,7 +814,7 @@ static inline double face_flux(const double* trL, int fl, const double* trR, int
 int orc_euler_rhs(const orc_euler_cfg* g, const double* U, double* RHS, double* smax_out, long* bad_out) {
     const int nx = g->nx, ny = g->ny, nz = g->nz;
     const double gam = 0.85;
-    const int linear = g->recon == 1;
+    const int recon = g->recon;
     const double r1_h = 1. / (g->h);
     g_flux_kind = g->flux;
     g_positivity = g->positivity;
@@ -783,7 +853,7 @@ int orc_euler_rhs(const orc_euler_cfg* g, const double* U, double* RHS, double* 
             for (int i = -1; i <= nx; ++i) {
                 const int ghosti = (i < 0 || i >= nx);
                 if (ghosti + ghostj + ghostk > 1) continue;
-                cell_traces(&P, i, j, k, gam, linear, TR(Tk, i, j));
+                cell_traces(&P, i, j, k, gam, recon, TR(Tk, i, j));
             }
         }
         if (k < 0) continue;
@@ -851,7 +921,11 @@ int orc_euler_rhs(const orc_euler_cfg* g, const double* U, double* RHS, double* 
 }
 
 /* dt = CFL*h/(3*s_max), rhs_function.c:438 with the viscous speed zero */
-static inline double euler_dt(const orc_euler_cfg* g, double smax) { return (1.0 / 3.0) * (g->cfl * g->h) / (smax + 0.0); }
+/* (1/3)(CFL h)/s_max: 3d/weno4/Navier-Stokes-3D/rhs_function.c:438-440;
+ * (CFL h)/(3 s_max): 3d/weno3/Euler/rhs_function.c:383 (the WENO3 program) */
+static inline double euler_dt(const orc_euler_cfg* g, double smax) {
+    return g->recon == 3 ? (g->cfl * g->h) / (3.0 * smax) : (1.0 / 3.0) * (g->cfl * g->h) / (smax + 0.0);
+}
 
 int orc_euler_run(const orc_euler_cfg* g, int nsteps, int dt_mode, double* U, double* t_inout, double* dt_inout, long* bad) {
     const size_t n = (size_t)g->nx * g->ny * g->nz * NV;

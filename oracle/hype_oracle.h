@@ -54,7 +54,8 @@ typedef struct {
     int nx, ny, nz;
     double xmin, ymin, zmin, h, cfl, gamma;
     int bc[6];
-    int recon; /* 0 = CWENO4 (gamma 0.85), 1 = linear R4 (the optimal-weight polynomial) */
+    int recon; /* 0 = CWENO4 (gamma 0.85), 1 = linear R4 (the optimal-weight polynomial),
+                  3 = WENO3 (3d/weno3/Euler/reconstruction.c:29-177) */
     int nthreads;
     int flux;  /* 0 = Rusanov (LLF), 1 = HLLC, 2 = rotated HLLC (Navier-Stokes-3D/pde.c:164-384) */
     int positivity; /* 1: first-order fallback of cells with an inadmissible face trace */

@@ -161,38 +161,44 @@ _REF_FLUX_LIB = {0: "libref_euler.so", 1: "libref_euler_hllc.so", 2: "libref_eul
 _ref_euler_libs = {}
 
 
-def _ref_euler_lib(flux: int = 0):
-    global _ref_euler
-    if flux not in _ref_euler_libs:
-        L = C.CDLL(os.path.join(HERE, "_ref", _REF_FLUX_LIB[flux]))
+def _ref_euler_fns(cfg):
+    """(rhs, run) entry points of the reference program for cfg: the CWENO4 Euler RHS
+    with its Riemann solver (cfg.flux), or the WENO3 Euler program (cfg.recon == 3)."""
+    if cfg.recon == 3:
+        if cfg.flux != 0:
+            raise ValueError("the WENO3 reference program has the Rusanov flux only")
+        key, name, pre = "w3", "libref_euler_w3.so", "ref_euler_w3_"
+    else:
+        key, name, pre = cfg.flux, _REF_FLUX_LIB[cfg.flux], "ref_euler_"
+    if key not in _ref_euler_libs:
+        L = C.CDLL(os.path.join(HERE, "_ref", name))
         IP = C.POINTER(C.c_int)
-        L.ref_euler_rhs.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
-                                    C.c_double, IP, D, D, D]
-        L.ref_euler_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
-                                    C.c_double, IP, C.c_int, C.c_int, D, D, D]
-        _ref_euler_libs[flux] = L
-    return _ref_euler_libs[flux]
+        rhs, run = getattr(L, pre + "rhs"), getattr(L, pre + "run")
+        rhs.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, IP, D, D, D]
+        run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, IP,
+                        C.c_int, C.c_int, D, D, D]
+        _ref_euler_libs[key] = (rhs, run)
+    return _ref_euler_libs[key]
 
 
 def ref_euler_rhs(cfg: EulerCfg, U):
-    L = _ref_euler_lib(cfg.flux)
+    rhs, _ = _ref_euler_fns(cfg)
     U = np.ascontiguousarray(U, dtype=np.float64)
     R = np.zeros_like(U)
     dt = C.c_double(0.0)
     bc = (C.c_int * 6)(*cfg.bc)
-    rc = L.ref_euler_rhs(cfg.nx, cfg.ny, cfg.nz, cfg.xmin, cfg.ymin, cfg.zmin, cfg.h, cfg.cfl, bc, _dp(U), _dp(R),
-                         C.byref(dt))
+    rc = rhs(cfg.nx, cfg.ny, cfg.nz, cfg.xmin, cfg.ymin, cfg.zmin, cfg.h, cfg.cfl, bc, _dp(U), _dp(R), C.byref(dt))
     return R, dt.value, rc
 
 
 def ref_euler_run(cfg: EulerCfg, U, nsteps, dt_mode=0, dt=0.0):
-    L = _ref_euler_lib(cfg.flux)
+    _, run = _ref_euler_fns(cfg)
     U = np.array(U, dtype=np.float64, order="C", copy=True)
     t = C.c_double(0.0)
     d = C.c_double(dt)
     bc = (C.c_int * 6)(*cfg.bc)
-    rc = L.ref_euler_run(cfg.nx, cfg.ny, cfg.nz, cfg.xmin, cfg.ymin, cfg.zmin, cfg.h, cfg.cfl, bc, nsteps, dt_mode,
-                         _dp(U), C.byref(t), C.byref(d))
+    rc = run(cfg.nx, cfg.ny, cfg.nz, cfg.xmin, cfg.ymin, cfg.zmin, cfg.h, cfg.cfl, bc, nsteps, dt_mode, _dp(U),
+             C.byref(t), C.byref(d))
     return U, t.value, d.value, rc
 
 

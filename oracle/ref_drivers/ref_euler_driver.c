@@ -16,10 +16,16 @@
  * The driver mirrors 3d/weno4/Navier-Stokes-3D/hype.c:96-188 (DMDA with box
  * stencil width 3, scratch allocation, the initial RHS call that sets dt, the
  * SSP RKS3 4-stage TS) and the dt update of monitor_function.c:31.
+ *
+ * Built with -DREF_WENO3 against 3d/weno3/Euler (rhs_function.c:12-387,
+ * reconstruction.c:12-177, pde.c:40-106, array.c; set-up of hype.c:96-196) it
+ * drives the third-order WENO Euler program instead, which has no viscous terms
+ * and no gradient traces; its entry points are then renamed by the Makefile.
  */
 #include "hype.h"
 #include <setjmp.h>
 
+#ifndef REF_WENO3
 /* Zero viscous flux: replaces PDEViscRiemannSolver (pde.c:386-404). */
 PetscReal PDEViscRiemannSolver(const Field* QL, PetscReal grad_QL[nVar][DIM], const Field* QR, PetscReal grad_QR[nVar][DIM],
                                const PetscReal nx, const PetscReal ny, const PetscReal nz, Field* Flux) {
@@ -27,6 +33,7 @@ PetscReal PDEViscRiemannSolver(const Field* QL, PetscReal grad_QL[nVar][DIM], co
     for (int c = 0; c < nVar; ++c) Flux->comp[c] = 0.0;
     return 0.0;
 }
+#endif
 
 /* bc codes shared with the GPU library: 0 periodic, 1 reflective, 2 transmissive */
 static enum bndry_type map_bc(int b) {
@@ -65,7 +72,9 @@ static void setup(RefEuler* R, int nx, int ny, int nz, double xmin, double ymin,
     PetscInt xs, ys, zs, xm, ym, zm;
     DMDAGetCorners(R->da, &xs, &ys, &zs, &xm, &ym, &zm);
     C->u_bnd = allocate6d(zm + 2, ym + 2, xm + 2, nVar, 6, N_gp2d);
+#ifndef REF_WENO3
     C->u_bnd_grad = allocate7d(zm + 2, ym + 2, xm + 2, nVar, 6, N_gp2d, DIM);
+#endif
     C->F = allocate4d(zm, ym, xm + 1, nVar);
     C->G = allocate4d(zm, ym + 1, xm, nVar);
     C->H = allocate4d(zm + 1, ym, xm, nVar);
@@ -76,7 +85,9 @@ static void setup(RefEuler* R, int nx, int ny, int nz, double xmin, double ymin,
 
 static void teardown(RefEuler* R) {
     free6d(R->ctx.u_bnd);
+#ifndef REF_WENO3
     free7d(R->ctx.u_bnd_grad);
+#endif
     free4d(R->ctx.F); free4d(R->ctx.G); free4d(R->ctx.H);
     VecDestroy(&R->ctx.localU);
     VecDestroy(&R->U); VecDestroy(&R->RHS);

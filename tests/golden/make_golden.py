@@ -13,6 +13,9 @@ tree is available; the GPU machine has none, so the fixtures are committed).
                            and of 3 SSP RKS3/4-stage steps of the same; the
                            *_hllc / *_rothllc cases switch its Riemann solver to
                            the reference's PDEHLLCRiemannSolver / PDErotHLLCRiemannSolver
+* ref_euler_*_weno3.npz -- the same for the third-order WENO Euler program
+                           3d/weno3/Euler (its rhs_function.c, reconstruction.c,
+                           pde.c), stepped with its monitor disabled (fixed dt)
 * ref_ctcs2d.npz        -- the reference's CTCS() (2d/ctcs/plane_wave/wave.c)
                            on a zero-exterior grid
 * ref_bubble_*.npz      -- the reference's 2D diffuse-interface RHSFunction
@@ -80,6 +83,15 @@ def main():
             assert rc3 == 0
             np.savez_compressed(os.path.join(HERE, f"ref_euler_{name}{tag}.npz"), U=U, RHS=R, dt=dt, U3=U3, t3=t3,
                                 dt3=dt3, bc=np.array(bc), n=n, cfl=0.4, flux=flux)
+    for name, n, seed, bc in CASES:  # 3d/weno3/Euler: WENO3, Rusanov, dt fixed by the first RHS call
+        cfg = O.euler_cfg(n, 1.0 / n, cfl=0.4, bc=bc, recon=3)
+        U = euler_case(n, seed + 100, bc, vel=0.1)
+        R, dt, rc = O.ref_euler_rhs(cfg, U)
+        assert rc == 0
+        U3, t3, dt3, rc3 = O.ref_euler_run(cfg, U, 3, dt_mode=1)
+        assert rc3 == 0
+        np.savez_compressed(os.path.join(HERE, f"ref_euler_{name}_weno3.npz"), U=U, RHS=R, dt=dt, U3=U3, t3=t3,
+                            dt3=dt3, bc=np.array(bc), n=n, cfl=0.4, flux=0, recon=3, dt_mode=1)
     n = 32
     x = -1 + np.arange(n) * (2.0 / n)
     Xg, Yg = np.meshgrid(x, x)

@@ -25,13 +25,17 @@ def solver(hype, n, bc=(0,) * 6, **kw):
 
 
 # walls_rothllc is checked separately below: the reference's rotated HLLC is discontinuous at reflective walls
-NAMES = ["periodic", "walls", "mixed", "periodic_hllc", "walls_hllc", "periodic_rothllc"]
+NAMES = ["periodic", "walls", "mixed", "periodic_hllc", "walls_hllc", "periodic_rothllc", "periodic_weno3", "walls_weno3",
+         "mixed_weno3"]
 
 
 def _golden_solver(hype, z):
     n = int(z["n"])
     flux = int(z["flux"]) if "flux" in z else 0
-    return solver(hype, n, tuple(int(b) for b in z["bc"]), cfl=float(z["cfl"]), flux=flux)
+    recon = int(z["recon"]) if "recon" in z else 0
+    dt_mode = int(z["dt_mode"]) if "dt_mode" in z else 0
+    return solver(hype, n, tuple(int(b) for b in z["bc"]), cfl=float(z["cfl"]), flux=flux, recon=recon,
+                  dt_mode=dt_mode)
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -120,6 +124,31 @@ def test_dt_semantics(hype, oracle, mode):
     Uo, t, dt, rc = oracle.euler_run(oracle.euler_cfg(n, 1.0 / n, cfl=0.4), U0, 6, dt_mode=mode, dt=0.003)
     assert rel(s.get_state(), Uo) <= TOL_STEP * 10
     assert abs(s.t - t) <= 1e-13 * t and abs(s.next_dt - dt) <= 1e-13 * dt
+
+
+def test_weno3_run_vs_oracle(hype, oracle):
+    """the WENO3 program (3d/weno3/Euler: fixed dt from the first RHS) over 20 steps, walls and periodic"""
+    n = 14
+    U0 = _pulse(n, amp=0.2)
+    for bc in ((0,) * 6, (1, 1, 2, 2, 1, 2)):
+        s = solver(hype, n, bc, recon=hype._lib.RECON_WENO3, dt_mode=hype._lib.DT_FROZEN)
+        s.set_state(U0)
+        s.step(20)
+        cfg = oracle.euler_cfg(n, 1.0 / n, cfl=0.4, bc=bc, recon=3)
+        U, t, dt, rc = oracle.euler_run(cfg, U0, 20, dt_mode=1)
+        assert rc == 0
+        assert rel(s.get_state(), U) <= TOL_RUN
+        assert abs(s.t - t) <= 1e-12 * t
+
+
+def test_weno3_fp32_error_is_bounded(hype, oracle):
+    n = 16
+    U0 = _pulse(n, amp=0.2)
+    s = solver(hype, n, recon=hype._lib.RECON_WENO3, precision=hype._lib.PREC_FP32)
+    s.set_state(U0)
+    s.step(5)
+    U, t, dt, rc = oracle.euler_run(oracle.euler_cfg(n, 1.0 / n, cfl=0.4, recon=3), U0, 5)
+    assert rel(s.get_state(), U) <= 1e-5
 
 
 def test_linear_reconstruction(hype, oracle):

@@ -9,13 +9,16 @@ import pytest
 from conftest import GOLDEN
 
 
-NAMES = ["periodic", "walls", "mixed", "periodic_hllc", "walls_hllc", "periodic_rothllc", "walls_rothllc"]
+NAMES = ["periodic", "walls", "mixed", "periodic_hllc", "walls_hllc", "periodic_rothllc", "walls_rothllc",
+         "periodic_weno3", "walls_weno3", "mixed_weno3"]
 
 
 def _cfg(oracle, z):
     n = int(z["n"])
     flux = int(z["flux"]) if "flux" in z else 0
-    return oracle.euler_cfg(n, 1.0 / n, cfl=float(z["cfl"]), bc=tuple(int(b) for b in z["bc"]), flux=flux)
+    recon = int(z["recon"]) if "recon" in z else 0
+    return oracle.euler_cfg(n, 1.0 / n, cfl=float(z["cfl"]), bc=tuple(int(b) for b in z["bc"]), flux=flux,
+                            recon=recon)
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -25,7 +28,10 @@ def test_euler_rhs_matches_reference_bitwise(oracle, name):
     R, smax, rc, bad = oracle.euler_rhs(cfg, z["U"])
     assert rc == 0 and bad == -1
     assert np.array_equal(R, z["RHS"])
-    dt = (1.0 / 3.0) * (cfg.cfl * cfg.h) / (smax + 0.0)
+    if cfg.recon == 3:  # 3d/weno3/Euler/rhs_function.c:383
+        dt = (cfg.cfl * cfg.h) / (3.0 * smax)
+    else:
+        dt = (1.0 / 3.0) * (cfg.cfl * cfg.h) / (smax + 0.0)
     assert dt == float(z["dt"])
 
 
@@ -33,7 +39,7 @@ def test_euler_rhs_matches_reference_bitwise(oracle, name):
 def test_euler_ssprk43_matches_reference_bitwise(oracle, name):
     z = np.load(os.path.join(GOLDEN, f"ref_euler_{name}.npz"))
     cfg = _cfg(oracle, z)
-    U3, t3, dt3, rc = oracle.euler_run(cfg, z["U"], 3)
+    U3, t3, dt3, rc = oracle.euler_run(cfg, z["U"], 3, dt_mode=int(z["dt_mode"]) if "dt_mode" in z else 0)
     assert rc == 0
     assert np.array_equal(U3, z["U3"])
     assert t3 == float(z["t3"]) and dt3 == float(z["dt3"])

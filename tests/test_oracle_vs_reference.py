@@ -52,6 +52,23 @@ def test_hllc_family_bitwise(oracle, flux, bc):
     assert np.array_equal(a[0], b[0]) and a[1] == b[1] and a[2] == b[2]
 
 
+@pytest.mark.parametrize("bc", [(0,) * 6, (1, 1, 1, 1, 1, 1), (2, 2, 2, 2, 2, 2), (1, 2, 0, 0, 2, 1)])
+def test_weno3_program_bitwise(oracle, bc):
+    """3d/weno3/Euler (WENO3 + Rusanov, monitor disabled: fixed dt) against the restatement"""
+    _need_ref(oracle)
+    n = 7
+    cfg = oracle.euler_cfg(n, 1.0 / n, cfl=0.4, bc=bc, recon=3)
+    U = _state(n, 23)
+    R1, smax, rc, _ = oracle.euler_rhs(cfg, U)
+    R2, dt2, rc2 = oracle.ref_euler_rhs(cfg, U)
+    assert rc == rc2 == 0 and np.array_equal(R1, R2)
+    assert (cfg.cfl * cfg.h) / (3.0 * smax) == dt2  # this program's rounding of dt (rhs_function.c:383)
+    a = oracle.euler_run(cfg, U, 3, dt_mode=1)
+    b = oracle.ref_euler_run(cfg, U, 3, dt_mode=1)
+    assert a[3] == b[3] == 0
+    assert np.array_equal(a[0], b[0]) and a[1] == b[1] and a[2] == b[2]
+
+
 @pytest.mark.parametrize("dt_mode", [0, 1, 2])
 def test_run_bitwise_dt_modes(oracle, dt_mode):
     _need_ref(oracle)
