@@ -91,14 +91,17 @@ def test_learned_indicator_gain(hype):
     learned.set_mlp(p, 0.2)
     learned.indicator_stats(reset=True)
     T = 0.02
-    for s in (ref, full, learned):
+    nsteps = {}
+    for name, s in (("ref", ref), ("full", full), ("learned", learned)):
+        nsteps[name] = 0
         while s.t < T:
             s.step(1)
+            nsteps[name] += 1
     rho_ref = ref.get_state()[..., 0].reshape(n, 2, n, 2, n, 2).mean(axis=(1, 3, 5))
     e_full = np.abs(full.get_state()[..., 0] - rho_ref).mean()
     e_learn = np.abs(learned.get_state()[..., 0] - rho_ref).mean()
     flagged, fallbacks = learned.indicator_stats()
-    frac = flagged / (n**3 * 4.0 * 1)
+    frac = flagged / (n**3 * 4.0 * nsteps["learned"])
     shadow = learned.shadow_step()
     print(f"L1 vs 2x reference: full {e_full:.3e} learned {e_learn:.3e}; flagged/cell-stage {frac:.3f} "
           f"positivity fallbacks {fallbacks}; shadow L1 {shadow:.2e}")
