@@ -31,7 +31,8 @@ SYMBOLS = [
     "hype_euler_download", "hype_euler_state_device", "hype_euler_step", "hype_euler_sync",
     "hype_ctcs2d_update", "hype_ctcs_create", "hype_ctcs_destroy", "hype_ctcs_set", "hype_ctcs_get",
     "hype_ctcs_step", "hype_ctcs_level_device", "hype_ctcs_sync",
-    "hype_batch_create", "hype_batch_destroy", "hype_batch_set_tile", "hype_batch_set", "hype_batch_get",
+    "hype_batch_create", "hype_batch_destroy", "hype_batch_set_tile", "hype_batch_get_tile", "hype_batch_set",
+    "hype_batch_get",
     "hype_batch_step", "hype_batch_sync",
     "hype_strerror", "hype_last_error", "hype_launch_count", "hype_version",
     "hype_euler_stream", "hype_euler_profile", "hype_euler_profile_read", "hype_set_device", "hype_device_count",
@@ -120,6 +121,7 @@ def lib():
         "hype_batch_create": ([C.c_int, P(MonoInstance), P(V)], C.c_int),
         "hype_batch_destroy": ([V], None),
         "hype_batch_set_tile": ([V, C.c_int, C.c_int], C.c_int),
+        "hype_batch_get_tile": ([V, I, I], C.c_int),
         "hype_batch_set": ([V, C.c_int, D, D], C.c_int),
         "hype_batch_get": ([V, C.c_int, D, D], C.c_int),
         "hype_batch_step": ([V, C.c_int, C.c_int], C.c_int),

@@ -31,7 +31,8 @@ struct Inst {
     int nx, ny;
     long long off;   // offset of the instance in a level pool
     long long goff;  // offset of its Gaussian factors (gx: nx, then gy: ny)
-    double inv_h2;   // 1/(h*h)
+    double a;        // (c0 dt / h)^2: weight of the neighbours
+    double b;        // 2 - 4a: weight of the centre
     double k2;       // c0*c0*dt*dt
 };
 
@@ -39,7 +40,16 @@ struct Work {
     int q, i0, j0, pad;
 };
 
-template <int TX, int TY>
+// One work item is a tile of TX x (TY R) nodes of one instance; thread (x, y) marches
+// the R consecutive rows j0 + y R ... of column i0 + x, carrying the centre and
+// north values from row to row (4 loads per node: north, west, east, p^{n-1}).  The
+// item's instance record, its x source factor and the step's sin(2 pi f t) are read
+// once per item.  On GB300 this update is bound by the FP64 pipe (1/64 of the FP32
+// rate), not by HBM, so it is written with 6 FP64 operations per node:
+//   p^{n+1} = (2 - 4a) p - p^{n-1} + a ((e + w) + (n + s)) + (k2 sin gx) gy,
+// a = (c0 dt/h)^2, the same update as 2p - p^{n-1} + c0^2 dt^2 (lap_h p + s) up to
+// rounding.
+template <int TX, int TY, int R>
 __global__ void __launch_bounds__(TX* TY) k_batch(const Inst* __restrict__ inst, const Work* __restrict__ work, int nwork,
                                                   const double* __restrict__ pold, const double* __restrict__ p,
                                                   double* __restrict__ pnew, const double* __restrict__ gauss,
@@ -48,19 +58,30 @@ __global__ void __launch_bounds__(TX* TY) k_batch(const Inst* __restrict__ inst,
     for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
         const Work wk = work[w];
         const Inst I = inst[wk.q];
-        const int i = wk.i0 + (int)threadIdx.x, j = wk.j0 + (int)threadIdx.y;
-        if (i >= I.nx || j >= I.ny) continue;
+        const int i = wk.i0 + (int)threadIdx.x, jb = wk.j0 + (int)threadIdx.y * R;
+        if (i >= I.nx || jb >= I.ny) continue;
         const double* P = p + I.off;
-        const long long o = (long long)j * I.nx + i;
-        const double c = P[o];
-        const double w_ = i > 0 ? P[o - 1] : 0.0;
-        const double e_ = i < I.nx - 1 ? P[o + 1] : 0.0;
-        const double s_ = j > 0 ? P[o - I.nx] : 0.0;
-        const double n_ = j < I.ny - 1 ? P[o + I.nx] : 0.0;
-        const double pxx = (e_ - 2.0 * c + w_) * I.inv_h2;
-        const double pyy = (n_ - 2.0 * c + s_) * I.inv_h2;
-        const double src = (gauss[I.goff + i] * gauss[I.goff + I.nx + j]) * sinv[(long long)s * ninst + wk.q];
-        pnew[I.off + o] = 2.0 * c - pold[I.off + o] + I.k2 * (pxx + pyy) + I.k2 * src;
+        const double* PO = pold + I.off;
+        double* PN = pnew + I.off;
+        const double gxa = (I.k2 * sinv[(long long)s * ninst + wk.q]) * gauss[I.goff + i];
+        const double* gy = gauss + I.goff + I.nx;
+        long long o = (long long)jb * I.nx + i;
+        double sv = jb > 0 ? P[o - I.nx] : 0.0;
+        double c = P[o];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int j = jb + r;
+            if (j < I.ny) {
+                const double nv = j < I.ny - 1 ? P[o + I.nx] : 0.0;
+                const double w_ = i > 0 ? P[o - 1] : 0.0;
+                const double e_ = i < I.nx - 1 ? P[o + 1] : 0.0;
+                const double nb = (e_ + w_) + (nv + sv);
+                PN[o] = fma(gxa, gy[j], fma(I.a, nb, fma(I.b, c, -PO[o])));
+                sv = c;
+                c = nv;
+                o += I.nx;
+            }
+        }
     }
 }
 
@@ -97,18 +118,24 @@ static const int kBatchChunk = 30;
 typedef void (*BatchKernel)(const Inst*, const Work*, int, const double*, const double*, double*, const double*,
                             const double*, int, const int*);
 
-static BatchKernel pick_kernel(int tx, int ty) {
-    if (tx == 32 && ty == 4) return k_batch<32, 4>;
-    if (tx == 32 && ty == 8) return k_batch<32, 8>;
-    if (tx == 32 && ty == 16) return k_batch<32, 16>;
-    if (tx == 64 && ty == 4) return k_batch<64, 4>;
-    if (tx == 64 && ty == 8) return k_batch<64, 8>;
-    if (tx == 128 && ty == 2) return k_batch<128, 2>;
-    if (tx == 128 && ty == 4) return k_batch<128, 4>;
-    if (tx == 256 && ty == 1) return k_batch<256, 1>;
+// tile shapes (width x height in nodes) and their thread blocks: TX x TY threads,
+// R rows per thread
+struct TileCfg {
+    int tx, ty;  // tile in nodes
+    BatchKernel k;
+    int threads_y;
+};
+static const TileCfg kTiles[] = {
+    {32, 16, k_batch<32, 8, 2>, 8},    {32, 32, k_batch<32, 8, 4>, 8},     {32, 64, k_batch<32, 8, 8>, 8},
+    {64, 16, k_batch<64, 4, 4>, 4},    {64, 32, k_batch<64, 4, 8>, 4},     {64, 64, k_batch<64, 4, 16>, 4},
+    {128, 16, k_batch<128, 2, 8>, 2},  {128, 32, k_batch<128, 2, 16>, 2}, {256, 16, k_batch<256, 1, 16>, 1},
+};
+
+static const TileCfg* pick_tile(int tx, int ty) {
+    for (const TileCfg& t : kTiles)
+        if (t.tx == tx && t.ty == ty) return &t;
     return nullptr;
 }
-static const int kTiles[][2] = {{32, 4}, {32, 8}, {32, 16}, {64, 4}, {64, 8}, {128, 2}, {128, 4}, {256, 1}};
 
 static void drop_graphs(hype_batch* b) {
     for (int q = 0; q < 3; ++q)
@@ -119,8 +146,8 @@ static void drop_graphs(hype_batch* b) {
 }
 
 static int build_worklist(hype_batch* b, int tx, int ty) {
-    BatchKernel k = pick_kernel(tx, ty);
-    if (!k) return HYPE_ERR_ARG;
+    const TileCfg* tc = pick_tile(tx, ty);
+    if (!tc) return HYPE_ERR_ARG;
     std::vector<Work> w;
     for (size_t q = 0; q < b->inst.size(); ++q)
         for (int j0 = 0; j0 < b->inst[q].ny; j0 += ty)
@@ -133,7 +160,7 @@ static int build_worklist(hype_batch* b, int tx, int ty) {
     int dev = 0, sms = 0, per_sm = 0;
     HYPE_CK(cudaGetDevice(&dev));
     HYPE_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    HYPE_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, tx * ty, 0));
+    HYPE_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc->k, tx * tc->threads_y, 0));
     if (per_sm < 1) per_sm = 1;
     b->grid = std::min<long long>((long long)sms * per_sm, (long long)b->nwork);
     b->tx = tx;
@@ -143,12 +170,12 @@ static int build_worklist(hype_batch* b, int tx, int ty) {
 }
 
 static int batch_launch(hype_batch* b, int phase) {
-    BatchKernel k = pick_kernel(b->tx, b->ty);
+    const TileCfg* tc = pick_tile(b->tx, b->ty);
     double* po = b->lv[(phase + 2) % 3];
     double* pc = b->lv[phase];
     double* pn = b->lv[(phase + 1) % 3];
-    k<<<b->grid, dim3(b->tx, b->ty), 0, b->stream>>>(b->d_inst, b->d_work, b->nwork, po, pc, pn, b->gauss, b->sinv,
-                                                     (int)b->inst.size(), b->d_step);
+    tc->k<<<b->grid, dim3(b->tx, tc->threads_y), 0, b->stream>>>(b->d_inst, b->d_work, b->nwork, po, pc, pn, b->gauss,
+                                                                 b->sinv, (int)b->inst.size(), b->d_step);
     k_tick<<<1, 1, 0, b->stream>>>(b->d_step);
     HYPE_LAUNCHED(2);
     return HYPE_OK;
@@ -231,7 +258,7 @@ static std::string shape_key(const hype_batch* b) {
         h = (h ^ (unsigned)x.second) * 1099511628211ull;
     }
     char buf[64];
-    snprintf(buf, sizeof(buf), "%zu-%016llx", s.size(), h);
+    snprintf(buf, sizeof(buf), "v2-%zu-%016llx", s.size(), h);
     return buf;
 }
 
@@ -245,11 +272,11 @@ static std::string cache_path() {
 static bool cache_lookup(const std::string& key, int* tx, int* ty) {
     FILE* f = fopen(cache_path().c_str(), "r");
     if (!f) return false;
-    char k[128];
+    char line[256], k[128];
     int a, c;
     bool found = false;
-    while (fscanf(f, "%127s %d %d", k, &a, &c) == 3)
-        if (key == k && pick_kernel(a, c)) {
+    while (fgets(line, sizeof(line), f))
+        if (sscanf(line, "%127s %d %d", k, &a, &c) == 3 && key == k && pick_tile(a, c)) {
             *tx = a;
             *ty = c;
             found = true;
@@ -285,10 +312,10 @@ static int autotune(hype_batch* b) {
     HYPE_CK(cudaEventCreate(&e0));
     HYPE_CK(cudaEventCreate(&e1));
     float best = 1e30f;
-    int bx = 32, by = 8;
+    int bx = 32, by = 32;
     int rc = HYPE_OK;
-    for (auto& t : kTiles) {
-        if ((rc = build_worklist(b, t[0], t[1]))) break;
+    for (const TileCfg& t : kTiles) {
+        if ((rc = build_worklist(b, t.tx, t.ty))) break;
         if ((rc = run_steps(b, 3, 0))) break;  // warm-up
         HYPE_CK(cudaEventRecord(e0, b->stream));
         if ((rc = run_steps(b, 12, 0))) break;
@@ -298,8 +325,8 @@ static int autotune(hype_batch* b) {
         HYPE_CK(cudaEventElapsedTime(&ms, e0, e1));
         if (ms < best) {
             best = ms;
-            bx = t[0];
-            by = t[1];
+            bx = t.tx;
+            by = t.ty;
         }
     }
     cudaEventDestroy(e0);
@@ -333,8 +360,9 @@ extern "C" int hype_batch_create(int ninst, const hype_mono_instance* in, hype_b
         I.ny = m.ny;
         I.off = off;
         I.goff = goff;
-        I.inv_h2 = 1.0 / (m.h * m.h);
         I.k2 = m.c0 * m.c0 * m.dt * m.dt;
+        I.a = I.k2 / (m.h * m.h);
+        I.b = 2.0 - 4.0 * I.a;
         b->inst.push_back(I);
         off += ((long long)m.nx * m.ny + 31) / 32 * 32;  // 256-byte aligned instance starts
         goff += m.nx + m.ny;
@@ -369,7 +397,7 @@ extern "C" int hype_batch_create(int ninst, const hype_mono_instance* in, hype_b
         hype_batch_destroy(b);
         return e == cudaErrorMemoryAllocation ? HYPE_ERR_NOMEM : HYPE_ERR_CUDA;
     }
-    int rc = build_worklist(b, 32, 8);
+    int rc = build_worklist(b, 32, 32);
     if (rc) {
         hype_batch_destroy(b);
         return rc;
@@ -396,6 +424,13 @@ extern "C" int hype_batch_set_tile(hype_batch* b, int tx, int ty) {
     if (!b) return HYPE_ERR_ARG;
     if (tx == 0 && ty == 0) return autotune(b);
     return build_worklist(b, tx, ty);
+}
+
+extern "C" int hype_batch_get_tile(const hype_batch* b, int* tx, int* ty) {
+    if (!b || !tx || !ty) return HYPE_ERR_ARG;
+    *tx = b->tx;
+    *ty = b->ty;
+    return HYPE_OK;
 }
 
 extern "C" int hype_batch_set(hype_batch* b, int q, const double* p_old, const double* p) {

@@ -251,6 +251,12 @@ class BatchLeapfrog:
     def set_tile(self, tx=0, ty=0):
         check(L.lib().hype_batch_set_tile(self._h, int(tx), int(ty)), "hype_batch_set_tile")
 
+    def tile(self):
+        """the tile shape in use (width, height in nodes)"""
+        tx, ty = C.c_int(), C.c_int()
+        check(L.lib().hype_batch_get_tile(self._h, C.byref(tx), C.byref(ty)), "hype_batch_get_tile")
+        return tx.value, ty.value
+
     def close(self):
         if self._h:
             L.lib().hype_batch_destroy(self._h)

@@ -270,8 +270,12 @@ typedef struct hype_batch hype_batch;
 
 int hype_batch_create(int ninst, const hype_mono_instance* inst, hype_batch** out);
 void hype_batch_destroy(hype_batch* b);
-/* tile shape (0 = autotuned and cached per grid shape) */
+/* tile shape in nodes, width x height: 32x16, 32x32, 32x64, 64x16, 64x32, 64x64,
+ * 128x16, 128x32 or 256x16 (each thread marches the rows of its column);
+ * 0 x 0 = autotuned by timing every shape and cached per grid-shape signature */
 int hype_batch_set_tile(hype_batch* b, int tile_x, int tile_y);
+/* the tile shape in use (after autotuning: the chosen one) */
+int hype_batch_get_tile(const hype_batch* b, int* tile_x, int* tile_y);
 /* initial levels of instance q (host arrays ny*nx) */
 int hype_batch_set(hype_batch* b, int q, const double* p_old, const double* p);
 int hype_batch_get(hype_batch* b, int q, double* p_old, double* p);

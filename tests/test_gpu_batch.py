@@ -26,7 +26,7 @@ def _oracle_run(oracle, m, nsteps):
 
 def test_batch_vs_oracle(hype, oracle):
     inst = _instances(7)
-    b = hype.BatchLeapfrog([hype.Monopole(**m) for m in inst], tile=(32, 8))
+    b = hype.BatchLeapfrog([hype.Monopole(**m) for m in inst], tile=(32, 32))
     b.step(65)
     for q, m in enumerate(inst):
         a, p = b.get(q)
@@ -38,7 +38,7 @@ def test_batch_vs_oracle(hype, oracle):
 def test_graph_and_tiles_do_not_change_results(hype):
     inst = _instances(5, seed=11)
     res = []
-    for tile, graph in [((32, 8), True), ((32, 8), False), ((128, 2), True), ((0, 0), True)]:
+    for tile, graph in [((32, 32), True), ((32, 32), False), ((128, 16), True), ((64, 64), False), ((0, 0), True)]:
         b = hype.BatchLeapfrog([hype.Monopole(**m) for m in inst], tile=tile)
         b.step(40, graph=graph)
         b.step(23, graph=graph)
