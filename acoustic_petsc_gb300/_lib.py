@@ -38,7 +38,8 @@ SYMBOLS = [
     "hype_euler_stream", "hype_euler_profile", "hype_euler_profile_read", "hype_set_device", "hype_device_count",
     "hype_probe_fma_peak", "hype_euler_rhs_noalloc", "hype_euler_noalloc_max_ext",
     "hype_mp2d_create", "hype_mp2d_destroy", "hype_mp2d_rhs", "hype_mp2d_upload", "hype_mp2d_download",
-    "hype_mp2d_step", "hype_mp2d_sync", "hype_mp2d_stream",
+    "hype_mp2d_step", "hype_mp2d_sync", "hype_mp2d_stream", "hype_mp2d_set_mlp", "hype_mp2d_set_recon",
+    "hype_mp2d_indicator_stats", "hype_mp2d_sample_features",
     "hype_euler_set_mlp", "hype_euler_set_recon", "hype_euler_indicator_stats", "hype_euler_sample_features",
     "hype_mlp_nparam", "hype_mlp_score", "hype_mlp_grad", "hype_mlp_train", "hype_euler_shadow_step",
 ]
@@ -65,7 +66,7 @@ class Mp2dParams(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("x_min", C.c_double), ("y_min", C.c_double), ("h", C.c_double),
                 ("cfl", C.c_double), ("bc", C.c_int * 4), ("model", C.c_int), ("g1", C.c_double), ("p1", C.c_double),
                 ("g2", C.c_double), ("p2", C.c_double), ("stepper", C.c_int), ("precision", C.c_int),
-                ("dt_mode", C.c_int)]
+                ("dt_mode", C.c_int), ("recon", C.c_int)]
 
 
 class Status(C.Structure):
@@ -146,6 +147,10 @@ def lib():
         "hype_mp2d_step": ([V, C.c_int, D, D, P(C.c_longlong)], C.c_int),
         "hype_mp2d_sync": ([V], C.c_int),
         "hype_mp2d_stream": ([V], C.c_void_p),
+        "hype_mp2d_set_mlp": ([V, F, C.c_float], C.c_int),
+        "hype_mp2d_set_recon": ([V, C.c_int], C.c_int),
+        "hype_mp2d_indicator_stats": ([V, P(C.c_longlong), C.c_int], C.c_int),
+        "hype_mp2d_sample_features": ([V, C.c_longlong, F, F, P(C.c_longlong)], C.c_int),
         "hype_euler_set_mlp": ([V, F, C.c_float], C.c_int),
         "hype_euler_set_recon": ([V, C.c_int], C.c_int),
         "hype_euler_indicator_stats": ([V, P(C.c_longlong), P(C.c_longlong), C.c_int], C.c_int),

@@ -61,7 +61,7 @@ __device__ __forceinline__ float forward(const __nv_bfloat16* __restrict__ p, co
 }
 
 // ---- tensor-core inference (mma.sync m16n8k16, BF16 operands, FP32 accumulation) ----
-// A warp scores 32 cells x 3 directions = 96 rows.  Inputs and the first hidden layer
+// A warp scores 32 cells x 3 directions = 96 rows (3D), or x 2 directions = 64 rows (2D).  Inputs and the first hidden layer
 // are rounded to BF16 (the operand type); b1 rides in W1's padding column 25 against a
 // constant-1 input, b2 initialises the second accumulator.
 constexpr int KP = 32;       // padded input width (25 features, the bias input, zeros)
@@ -112,10 +112,12 @@ __device__ __forceinline__ unsigned pack_relu(float lo, float hi) {
     return *reinterpret_cast<unsigned*>(&v);
 }
 
-// logits of the warp's 96 staged rows (shared memory) into lg[96] (shared memory);
+// logits of the warp's NROWS staged rows (shared memory) into lg[NROWS] (shared memory);
 // w is the packed network in global memory (L1-resident after the first warp);
 // every lane of the warp must call it
+template <int NROWS = ROWS>
 __device__ __forceinline__ void warp_logits(const MmaWeights* __restrict__ w, const __nv_bfloat16* rows, float* lg) {
+    static_assert(NROWS % 16 == 0, "rows come in m16 tiles");
     const int lane = threadIdx.x & 31, g = lane >> 2, tg = lane & 3;
     unsigned bw1[4][2][2], bw2[4][2][2];
 #pragma unroll
@@ -131,7 +133,7 @@ __device__ __forceinline__ void warp_logits(const MmaWeights* __restrict__ w, co
     const float b3 = __ldg(&w->b3);
     const unsigned* r32 = reinterpret_cast<const unsigned*>(rows);
 #pragma unroll 1
-    for (int mt = 0; mt < ROWS / 16; ++mt) {
+    for (int mt = 0; mt < NROWS / 16; ++mt) {
         unsigned a[2][4];
 #pragma unroll
         for (int kt = 0; kt < 2; ++kt) {

@@ -13,8 +13,12 @@
 //               (:351-380) fused with the stage combination.
 // dt = CFL h / (2 s_max) is formed on the device (:385).
 #include <cuda_runtime.h>
+#include <math.h>
 #include <string.h>
 
+#include <vector>
+
+#include "mlp_kernels.cuh"
 #include "mphase2d_kernels.cuh"
 
 namespace hype {
@@ -58,45 +62,55 @@ __global__ void k_mp_prim(const double* __restrict__ U, double* __restrict__ P, 
     for (int c = 0; c < nv; ++c) P[c * N + q] = V[c];
 }
 
-template <typename R, int MODEL>
-__global__ void __launch_bounds__(128) k_mp_recon(const double* __restrict__ P, R* __restrict__ T, Geo g, Eos e,
-                                                  DevScalars* __restrict__ ds) {
-    constexpr int NV = MODEL == HYPE_MP_DI4 ? 5 : 6;
-    constexpr int IU = MODEL == HYPE_MP_DI4 ? 1 : 2;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
-    if (i > g.nx || j > g.ny) return;
-    const bool gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny);
-    if (gi && gj) return;
-    int mi[5], mj[5], fi = 0, fj = 0;
+// boundary maps of the offsets -2..2 of one cell (replaces DMGlobalToLocal + the
+// BC sweeps of rhs_function.c:54-170)
+struct CellMap {
+    int mi[5], mj[5], fi, fj;  // fi/fj bit o: offset o-2 is a reflective ghost
+    long long e;               // extended-cell index of the traces
+};
+
+__device__ __forceinline__ void cell_map(const Geo& g, int i, int j, CellMap& cm) {
+    cm.fi = cm.fj = 0;
 #pragma unroll
     for (int o = 0; o < 5; ++o) {
         int f = 0;
-        mi[o] = bmap(i + o - 2, g.nx, g.bc[0], g.bc[1], &f);
-        fi |= f << o;
+        cm.mi[o] = bmap(i + o - 2, g.nx, g.bc[0], g.bc[1], &f);
+        cm.fi |= f << o;
         f = 0;
-        mj[o] = bmap(j + o - 2, g.ny, g.bc[2], g.bc[3], &f);
-        fj |= f << o;
+        cm.mj[o] = bmap(j + o - 2, g.ny, g.bc[2], g.bc[3], &f);
+        cm.fj |= f << o;
     }
-    const long long e_ = (long long)(j + 1) * (g.nx + 2) + (i + 1);
+    cm.e = (long long)(j + 1) * (g.nx + 2) + (i + 1);
+}
+
+// primitive variable c at offset (oi, oj); a reflective ghost negates the velocity
+// normal to its wall (x: u, y: v)
+template <int MODEL>
+__device__ __forceinline__ double ldp(const double* __restrict__ P, const Geo& g, const CellMap& cm, int c, int oi, int oj) {
+    constexpr int IU = MODEL == HYPE_MP_DI4 ? 1 : 2;
+    double v = __ldg(P + (long long)c * g.N + (long long)cm.mj[oj + 2] * g.nx + cm.mi[oi + 2]);
+    if (c == IU && ((cm.fi >> (oi + 2)) & 1)) v = -v;
+    if (c == IU + 1 && ((cm.fj >> (oj + 2)) & 1)) v = -v;
+    return v;
+}
+
+// one cell: 2D CWENO4 (or its optimal-weight R4 limit) of every primitive variable,
+// its 8 face traces; returns whether the 8 admissibility nodes pass (rhs_function.c:173-250)
+template <typename R, int MODEL>
+__device__ __forceinline__ bool mp_cell_recon(const double* __restrict__ P, R* __restrict__ T, const Geo& g, const Eos& e,
+                                              const CellMap& cm, bool linear) {
+    constexpr int NV = MODEL == HYPE_MP_DI4 ? 5 : 6;
     R VN[8][NV];
 #pragma unroll 1
     for (int c = 0; c < NV; ++c) {
-        const double* Pc = P + (long long)c * g.N;
-        auto ld = [&](int oi, int oj) -> R {
-            double v = __ldg(Pc + (long long)mj[oj + 2] * g.nx + mi[oi + 2]);
-            // a reflective ghost negates the velocity normal to its wall (x: u, y: v)
-            if (c == IU && ((fi >> (oi + 2)) & 1)) v = -v;
-            if (c == IU + 1 && ((fj >> (oj + 2)) & 1)) v = -v;
-            return (R)v;
-        };
+        auto ld = [&](int oi, int oj) -> R { return (R)ldp<MODEL>(P, g, cm, c, oi, oj); };
         R ux[5], uy[5], cf[NDOF];
 #pragma unroll
         for (int o = 0; o < 5; ++o) {
             ux[o] = ld(o - 2, 0);
             uy[o] = ld(0, o - 2);
         }
-        cweno2d<R>(ux[2], ux, uy, ld(1, 1), ld(1, -1), ld(-1, 1), ld(-1, -1), cf);
+        cweno2d<R>(ux[2], ux, uy, ld(1, 1), ld(1, -1), ld(-1, 1), ld(-1, -1), cf, linear);
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             R v = R(0);
@@ -104,7 +118,7 @@ __global__ void __launch_bounds__(128) k_mp_recon(const double* __restrict__ P, 
             for (int k = 0; k < NDOF; ++k) v += cf[k] * R(basis2(node_x(q), node_y(q), k));
             VN[q][c] = v;
         }
-        R* Tc = T + (long long)c * 8 * g.NE + e_;
+        R* Tc = T + (long long)c * 8 * g.NE + cm.e;
 #pragma unroll
         for (int f = 0; f < 4; ++f)
 #pragma unroll
@@ -118,27 +132,173 @@ __global__ void __launch_bounds__(128) k_mp_recon(const double* __restrict__ P, 
     bool ok = true;
 #pragma unroll
     for (int q = 0; q < 8; ++q) ok = ok && pad_ok<R>(e, VN[q]);
-    if (ok) return;
-    // physically inadmissible somewhere in the cell: first order + minmod slopes (rhs_function.c:239-250)
-    if (!gi && !gj) atomicAdd(&ds->fallback, 1ull);
+    return ok;
+}
+
+// physically inadmissible somewhere in the cell: first order + minmod slopes (rhs_function.c:239-250)
+template <typename R, int MODEL>
+__device__ __forceinline__ void mp_cell_fallback(const double* __restrict__ P, R* __restrict__ T, const Geo& g,
+                                                 const CellMap& cm) {
+    constexpr int NV = MODEL == HYPE_MP_DI4 ? 5 : 6;
 #pragma unroll 1
     for (int c = 0; c < NV; ++c) {
-        const double* Pc = P + (long long)c * g.N;
-        auto ld = [&](int oi, int oj) -> R {
-            double v = __ldg(Pc + (long long)mj[oj + 2] * g.nx + mi[oi + 2]);
-            if (c == IU && ((fi >> (oi + 2)) & 1)) v = -v;
-            if (c == IU + 1 && ((fj >> (oj + 2)) & 1)) v = -v;
-            return (R)v;
-        };
+        auto ld = [&](int oi, int oj) -> R { return (R)ldp<MODEL>(P, g, cm, c, oi, oj); };
         const R w0 = ld(0, 0);
         const R sx = minmod<R>(ld(1, 0) - w0, w0 - ld(-1, 0));
         const R sy = minmod<R>(ld(0, 1) - w0, w0 - ld(0, -1));
-        R* Tc = T + (long long)c * 8 * g.NE + e_;
+        R* Tc = T + (long long)c * 8 * g.NE + cm.e;
 #pragma unroll
         for (int f = 0; f < 4; ++f)
 #pragma unroll
             for (int q = 0; q < 2; ++q) Tc[(long long)(f * 2 + q) * g.NE] = w0 + sx * R(face_x(f, q)) + sy * R(face_y(f, q));
     }
+}
+
+template <typename R, int MODEL>
+__global__ void __launch_bounds__(128) k_mp_recon(const double* __restrict__ P, R* __restrict__ T, Geo g, Eos e,
+                                                  DevScalars* __restrict__ ds) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+    if (i > g.nx || j > g.ny) return;
+    const bool gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny);
+    if (gi && gj) return;
+    CellMap cm;
+    cell_map(g, i, j, cm);
+    if (mp_cell_recon<R, MODEL>(P, T, g, e, cm, false)) return;
+    if (!gi && !gj) atomicAdd(&ds->fallback, 1ull);
+    mp_cell_fallback<R, MODEL>(P, T, g, cm);
+}
+
+// Network inputs of one cell along direction d (0: x, 1: y): the normalised 5-point
+// stencils of the mixture density, the normal and tangential velocity, the pressure
+// and the volume fraction, each against a floor of 1 % of its magnitude in the cell
+// (density |rho|, velocities sqrt((|p| + pi)/rho), pressure |p| + pi, volume fraction 1).
+template <int MODEL>
+__device__ __forceinline__ void mp_features(const double* __restrict__ P, const Geo& g, const Eos& e, const CellMap& cm,
+                                            int d, float* x) {
+    constexpr int IU = MODEL == HYPE_MP_DI4 ? 1 : 2;
+    constexpr int IP = MODEL == HYPE_MP_DI4 ? 3 : 4;
+    constexpr int IA = MODEL == HYPE_MP_DI4 ? 4 : 5;
+    float q[5][5];
+#pragma unroll
+    for (int o = 0; o < 5; ++o) {
+        const int oi = d == 0 ? o - 2 : 0, oj = d == 1 ? o - 2 : 0;
+        const double a = ldp<MODEL>(P, g, cm, IA, oi, oj);
+        const double rho = MODEL == HYPE_MP_DI4
+                               ? ldp<MODEL>(P, g, cm, 0, oi, oj)
+                               : a * ldp<MODEL>(P, g, cm, 0, oi, oj) + (1.0 - a) * ldp<MODEL>(P, g, cm, 1, oi, oj);
+        const double u = ldp<MODEL>(P, g, cm, IU, oi, oj), v = ldp<MODEL>(P, g, cm, IU + 1, oi, oj);
+        q[0][o] = (float)rho;
+        q[1][o] = (float)(d == 0 ? u : v);
+        q[2][o] = (float)(d == 0 ? v : u);
+        q[3][o] = (float)ldp<MODEL>(P, g, cm, IP, oi, oj);
+        q[4][o] = (float)a;
+    }
+    double gm, pi;
+    mix(e, (double)q[4][2], gm, pi);
+    const float srho = fabsf(q[0][2]) + 1e-30f;
+    const float sp = fabsf(q[3][2]) + (float)pi;
+    const float svel = sqrtf(sp / srho);
+    const float sc[5] = {srho, svel, svel, sp, 1.0f};
+#pragma unroll
+    for (int k = 0; k < 5; ++k) mlp::normalise5(q[k], sc[k], x + 5 * k);
+}
+
+// Indicator-gated reconstruction (no counterpart in the reference): the network scores
+// each cell from its two directional stencils on the tensor cores; flagged cells take
+// the full CWENO4, the others its R4 limit; R4 traces that fail the admissibility
+// nodes are redone with CWENO4, and the minmod fallback stays the last resort.
+template <typename R, int MODEL>
+__global__ void __launch_bounds__(128) k_mp_recon_learned(const double* __restrict__ P, R* __restrict__ T, Geo g, Eos e,
+                                                          DevScalars* __restrict__ ds,
+                                                          const mlp::MmaWeights* __restrict__ wts, float logit_thr,
+                                                          unsigned long long* __restrict__ flagged) {
+    constexpr int NR = 64;  // 32 cells x 2 directions per warp
+    __shared__ __align__(16) __nv_bfloat16 rows[4][NR * mlp::RSTRIDE];
+    __shared__ float lg[4][NR];
+    __shared__ unsigned cnt;
+    if (threadIdx.x == 0 && threadIdx.y == 0) cnt = 0;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+    const bool gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny);
+    const bool active = !(i > g.nx || j > g.ny) && !(gi && gj);
+    CellMap cm;
+    if (active) cell_map(g, i, j, cm);
+#pragma unroll 1
+    for (int d = 0; d < 2; ++d) {
+        float x[mlp::NIN];
+        if (active) mp_features<MODEL>(P, g, e, cm, d, x);
+        mlp::stage_row(rows[threadIdx.y] + (threadIdx.x * 2 + d) * mlp::RSTRIDE, x, active);
+    }
+    __syncthreads();  // counter cleared, rows staged
+    mlp::warp_logits<NR>(wts, rows[threadIdx.y], lg[threadIdx.y]);
+    __syncwarp();
+    const float best = fmaxf(lg[threadIdx.y][threadIdx.x * 2], lg[threadIdx.y][threadIdx.x * 2 + 1]);
+    if (active) {
+        bool full = best > logit_thr;
+        bool ok = mp_cell_recon<R, MODEL>(P, T, g, e, cm, !full);
+        if (!ok && !full) {
+            full = true;
+            ok = mp_cell_recon<R, MODEL>(P, T, g, e, cm, false);
+        }
+        if (!ok) {
+            if (!gi && !gj) atomicAdd(&ds->fallback, 1ull);
+            mp_cell_fallback<R, MODEL>(P, T, g, cm);
+        }
+        if (full && best > logit_thr && !gi && !gj) atomicAdd(&cnt, 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0 && cnt) atomicAdd(flagged, (unsigned long long)cnt);
+}
+
+// Training data: for every stride-th owned cell its features X[s][3][25] (x, y, and y
+// again: the training kernels take three directions and the max over a repeated row
+// is the max over the two) and D[s], the largest change that the nonlinear CWENO4
+// weights make to one of its 8 face traces relative to the R4 polynomial, over the
+// primitive variables, in units of the variable's magnitude in the cell.
+template <int MODEL>
+__global__ void __launch_bounds__(128) k_mp_features(const double* __restrict__ P, Geo g, Eos e, long long stride,
+                                                     long long ns, float* __restrict__ X, float* __restrict__ D) {
+    constexpr int NV = MODEL == HYPE_MP_DI4 ? 5 : 6;
+    constexpr int IU = MODEL == HYPE_MP_DI4 ? 1 : 2;
+    constexpr int IP = MODEL == HYPE_MP_DI4 ? 3 : 4;
+    const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (s >= ns) return;
+    const long long cell = s * stride;
+    const int i = (int)(cell % g.nx), j = (int)(cell / g.nx);
+    CellMap cm;
+    cell_map(g, i, j, cm);
+    float* xs = X + s * 3 * mlp::NIN;
+    mp_features<MODEL>(P, g, e, cm, 0, xs);
+    mp_features<MODEL>(P, g, e, cm, 1, xs + mlp::NIN);
+    for (int k = 0; k < mlp::NIN; ++k) xs[2 * mlp::NIN + k] = xs[mlp::NIN + k];
+    const double a = ldp<MODEL>(P, g, cm, MODEL == HYPE_MP_DI4 ? 4 : 5, 0, 0);
+    const double rho = MODEL == HYPE_MP_DI4 ? ldp<MODEL>(P, g, cm, 0, 0, 0)
+                                            : a * ldp<MODEL>(P, g, cm, 0, 0, 0) + (1.0 - a) * ldp<MODEL>(P, g, cm, 1, 0, 0);
+    double gm, pi;
+    mix(e, a, gm, pi);
+    const double sp = fabs(ldp<MODEL>(P, g, cm, IP, 0, 0)) + pi;
+    const double svel = sqrt(sp / (fabs(rho) + 1e-300));
+    double dmax = 0.0;
+#pragma unroll 1
+    for (int c = 0; c < NV; ++c) {
+        auto ld = [&](int oi, int oj) { return ldp<MODEL>(P, g, cm, c, oi, oj); };
+        double ux[5], uy[5], cf[NDOF], cl[NDOF];
+        for (int o = 0; o < 5; ++o) {
+            ux[o] = ld(o - 2, 0);
+            uy[o] = ld(0, o - 2);
+        }
+        cweno2d<double>(ux[2], ux, uy, ld(1, 1), ld(1, -1), ld(-1, 1), ld(-1, -1), cf, false);
+        cweno2d<double>(ux[2], ux, uy, ld(1, 1), ld(1, -1), ld(-1, 1), ld(-1, -1), cl, true);
+        const double scale = (c == IU || c == IU + 1) ? svel : c == IP ? sp : c == NV - 1 ? 1.0 : fabs(ux[2]) + 1e-300;
+        for (int f = 0; f < 4; ++f)
+            for (int q = 0; q < 2; ++q) {
+                double dv = 0.0;
+                for (int k = 0; k < NDOF; ++k) dv += (cf[k] - cl[k]) * basis2(face_x(f, q), face_y(f, q), k);
+                dmax = fmax(dmax, fabs(dv) / scale);
+            }
+    }
+    D[s] = (float)dmax;
 }
 
 template <typename R, int MODEL, int D>
@@ -273,6 +433,10 @@ struct hype_mp2d {
     double *F = nullptr, *G = nullptr, *stage_aos = nullptr;
     DevScalars* ds = nullptr;
     DevScalars* hs = nullptr;
+    // learned indicator: packed network, logit threshold, flagged-cell counter
+    mlp::MmaWeights* mlp = nullptr;
+    float logit_thr = 0.0f;
+    unsigned long long* flagged = nullptr;
 };
 
 static int mp_rhs(hype_mp2d* m, const double* Win, int slot) {
@@ -281,10 +445,16 @@ static int mp_rhs(hype_mp2d* m, const double* Win, int slot) {
     const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4));
     const dim3 gx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4)), gy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4));
     const bool f32 = m->p.precision == HYPE_PREC_FP32;
+    const bool learned = m->p.recon == HYPE_RECON_LEARNED;
+    if (learned && !m->mlp) return HYPE_ERR_ARG;  // hype_mp2d_set_mlp first
     double* Gf = m->G;
 #define MP_LAUNCH(R, M)                                                                                        \
     do {                                                                                                       \
-        k_mp_recon<R, M><<<gr, br, 0, m->stream>>>(m->P, (R*)m->T, g, m->e, m->ds);                            \
+        if (learned)                                                                                           \
+            k_mp_recon_learned<R, M><<<gr, br, 0, m->stream>>>(m->P, (R*)m->T, g, m->e, m->ds, m->mlp,         \
+                                                               m->logit_thr, m->flagged);                      \
+        else                                                                                                   \
+            k_mp_recon<R, M><<<gr, br, 0, m->stream>>>(m->P, (R*)m->T, g, m->e, m->ds);                        \
         k_mp_faces<R, M, 0><<<gx, br, 0, m->stream>>>((const R*)m->T, m->F, g, m->e, m->ds, slot);             \
         k_mp_faces<R, M, 1><<<gy, br, 0, m->stream>>>((const R*)m->T, Gf, g, m->e, m->ds, slot);               \
     } while (0)
@@ -321,6 +491,7 @@ extern "C" int hype_mp2d_create(const hype_mp2d_params* p, hype_mp2d** out) {
     if (p->stepper != HYPE_STEP_SSPRK43 && p->stepper != HYPE_STEP_SSPRK104) return HYPE_ERR_ARG;
     if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32) return HYPE_ERR_ARG;
     if (p->dt_mode < HYPE_DT_MONITOR || p->dt_mode > HYPE_DT_FIXED) return HYPE_ERR_ARG;
+    if (p->recon != HYPE_RECON_CWENO4 && p->recon != HYPE_RECON_LEARNED) return HYPE_ERR_ARG;
     hype_mp2d* m = new hype_mp2d();
     m->p = *p;
     Geo& g = m->g;
@@ -340,6 +511,8 @@ extern "C" int hype_mp2d_create(const hype_mp2d_params* p, hype_mp2d** out) {
     if (ce == cudaSuccess) ce = cudaMalloc((void**)&m->G, sizeof(double) * (g.nv + 1) * (size_t)p->nx * (p->ny + 1));
     if (ce == cudaSuccess) ce = cudaMalloc((void**)&m->ds, sizeof(DevScalars));
     if (ce == cudaSuccess) ce = cudaMallocHost((void**)&m->hs, sizeof(DevScalars));
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&m->flagged, sizeof(unsigned long long));
+    if (ce == cudaSuccess) ce = cudaMemset(m->flagged, 0, sizeof(unsigned long long));
     if (ce == cudaSuccess) {
         DevScalars z;
         memset(&z, 0, sizeof(z));
@@ -360,6 +533,7 @@ extern "C" void hype_mp2d_destroy(hype_mp2d* m) {
     if (m->stream) cudaStreamSynchronize(m->stream);
     cudaFree(m->U); cudaFree(m->W0); cudaFree(m->W1); cudaFree(m->L); cudaFree(m->S); cudaFree(m->P);
     cudaFree(m->stage_aos); cudaFree(m->T); cudaFree(m->F); cudaFree(m->G); cudaFree(m->ds);
+    cudaFree(m->mlp); cudaFree(m->flagged);
     if (m->hs) cudaFreeHost(m->hs);
     if (m->stream) cudaStreamDestroy(m->stream);
     delete m;
@@ -480,5 +654,64 @@ extern "C" int hype_mp2d_step(hype_mp2d* m, int nsteps, double* t_inout, double*
 extern "C" int hype_mp2d_sync(hype_mp2d* m) {
     if (!m) return HYPE_ERR_ARG;
     HYPE_CK(cudaStreamSynchronize(m->stream));
+    return HYPE_OK;
+}
+
+// ------------------------------------------------------------------ learned indicator
+extern "C" int hype_mp2d_set_mlp(hype_mp2d* m, const float* params, float prob_threshold) {
+    if (!m || !params || !(prob_threshold > 0.0f) || !(prob_threshold < 1.0f)) return HYPE_ERR_ARG;
+    std::vector<__nv_bfloat16> h(mlp::NPARAM);
+    for (int q = 0; q < mlp::NPARAM; ++q) h[q] = __float2bfloat16_rn(params[q]);
+    mlp::MmaWeights hw;  // host staging, copied before the stream synchronisation below
+    mlp::pack_weights(h.data(), hw);
+    if (!m->mlp) HYPE_CK(cudaMalloc((void**)&m->mlp, sizeof(mlp::MmaWeights)));
+    HYPE_CK(cudaMemcpyAsync(m->mlp, &hw, sizeof(mlp::MmaWeights), cudaMemcpyHostToDevice, m->stream));
+    HYPE_CK(cudaStreamSynchronize(m->stream));
+    m->logit_thr = logf(prob_threshold / (1.0f - prob_threshold));
+    return HYPE_OK;
+}
+
+extern "C" int hype_mp2d_set_recon(hype_mp2d* m, int recon) {
+    if (!m || (recon != HYPE_RECON_CWENO4 && recon != HYPE_RECON_LEARNED)) return HYPE_ERR_ARG;
+    HYPE_CK(cudaStreamSynchronize(m->stream));
+    m->p.recon = recon;
+    return HYPE_OK;
+}
+
+extern "C" int hype_mp2d_indicator_stats(hype_mp2d* m, long long* flagged, int reset) {
+    if (!m) return HYPE_ERR_ARG;
+    unsigned long long c = 0;
+    HYPE_CK(cudaMemcpyAsync(&c, m->flagged, sizeof(c), cudaMemcpyDeviceToHost, m->stream));
+    HYPE_CK(cudaStreamSynchronize(m->stream));
+    if (flagged) *flagged = (long long)c;
+    if (reset) HYPE_CK(cudaMemsetAsync(m->flagged, 0, sizeof(c), m->stream));
+    return HYPE_OK;
+}
+
+extern "C" int hype_mp2d_sample_features(hype_mp2d* m, long long stride, float* X, float* D, long long* ns_out) {
+    if (!m || stride < 1 || !X || !D) return HYPE_ERR_ARG;
+    const Geo& g = m->g;
+    const long long ns = (g.N + stride - 1) / stride;
+    float *dX = nullptr, *dD = nullptr;
+    cudaError_t ce = cudaMalloc((void**)&dX, sizeof(float) * ns * 3 * mlp::NIN);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&dD, sizeof(float) * ns);
+    if (ce == cudaSuccess) {
+        k_mp_prim<<<cdiv(g.N, 256), 256, 0, m->stream>>>(m->U, m->P, m->e, g.N, g.nv);
+        if (m->e.model == HYPE_MP_DI4)
+            k_mp_features<HYPE_MP_DI4><<<cdiv(ns, 128), 128, 0, m->stream>>>(m->P, g, m->e, stride, ns, dX, dD);
+        else
+            k_mp_features<HYPE_MP_KAPILA5><<<cdiv(ns, 128), 128, 0, m->stream>>>(m->P, g, m->e, stride, ns, dX, dD);
+        HYPE_LAUNCHED(2);
+        ce = cudaMemcpyAsync(X, dX, sizeof(float) * ns * 3 * mlp::NIN, cudaMemcpyDeviceToHost, m->stream);
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(D, dD, sizeof(float) * ns, cudaMemcpyDeviceToHost, m->stream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(m->stream);
+    }
+    cudaFree(dX);
+    cudaFree(dD);
+    if (ce != cudaSuccess) {
+        set_last_error("hype_mp2d_sample_features", ce);
+        return ce == cudaErrorMemoryAllocation ? HYPE_ERR_NOMEM : HYPE_ERR_CUDA;
+    }
+    if (ns_out) *ns_out = ns;
     return HYPE_OK;
 }

@@ -62,7 +62,8 @@ template <typename R>
 struct Cw2Weights;
 
 template <typename R>
-__device__ __forceinline__ void cweno2d(R u0, const R* ux, const R* uy, R upp, R upm, R ump, R umm, R* cf) {
+__device__ __forceinline__ void cweno2d(R u0, const R* ux, const R* uy, R upp, R upm, R ump, R umm, R* cf,
+                                        bool linear = false) {
     const R u_im2 = ux[0], u_im1 = ux[1], u_ip1 = ux[3], u_ip2 = ux[4];
     const R u_jm2 = uy[0], u_jm1 = uy[1], u_jp1 = uy[3], u_jp2 = uy[4];
     const R u_ip1jp1 = upp, u_ip1jm1 = upm, u_im1jp1 = ump, u_im1jm1 = umm;
@@ -82,6 +83,12 @@ __device__ __forceinline__ void cweno2d(R u0, const R* ux, const R* uy, R upp, R
     const R yyyR4 = r1_6 * (u_jm1 - u_jp1) + r1_12 * (u_jp2 - u_jm2);
     const R xxyR4 = R(0.25) * (-u_im1jm1 + u_im1jp1 - u_ip1jm1 + u_ip1jp1) + R(0.5) * (u_jm1 - u_jp1);
     const R xyyR4 = R(0.5) * (u_im1 - u_ip1) + R(0.25) * (u_ip1jp1 - u_im1jm1 - u_im1jp1 + u_ip1jm1);
+    if (linear) {  // the optimal-weight limit: the R4 polynomial itself
+        cf[0] = u0;
+        cf[1] = xR4; cf[2] = yR4; cf[3] = xxR4; cf[4] = yyR4; cf[5] = xyR4;
+        cf[6] = xxxR4; cf[7] = yyyR4; cf[8] = xxyR4; cf[9] = xyyR4;
+        return;
+    }
     const R IS4 = (xR4 + R(0.1) * xxxR4) * (xR4 + R(0.1) * xxxR4) + r13_3 * (xxR4 * xxR4 + yyR4 * yyR4) +
                   (yR4 + R(0.1) * yyyR4) * (yR4 + R(0.1) * yyyR4) + R(39.05) * (xxxR4 * xxxR4 + yyyR4 * yyyR4) +
                   r7_6 * xyR4 * xyR4 + R(4.7) * (xxyR4 * xxyR4 + xyyR4 * xyyR4);

@@ -293,14 +293,15 @@ class Multiphase2D:
 
     def __init__(self, nx, ny, h, x_min=0.0, y_min=0.0, CFL=0.9, boundaries=(L.BC_TRANSMISSIVE,) * 4,
                  model=L.MP_DI4, eos=(4.4, 6000.0, 1.4, 0.0), stepper=L.STEP_SSPRK43, precision=L.PREC_FP64,
-                 dt_mode=L.DT_MONITOR):
+                 dt_mode=L.DT_MONITOR, recon=L.RECON_CWENO4):
         p = L.Mp2dParams()
         p.nx, p.ny, p.x_min, p.y_min, p.h, p.cfl = nx, ny, x_min, y_min, h, CFL
         for q in range(4):
             p.bc[q] = int(boundaries[q])
         p.model = model
         p.g1, p.p1, p.g2, p.p2 = eos
-        p.stepper, p.precision, p.dt_mode = stepper, precision, dt_mode
+        p.stepper, p.precision, p.dt_mode, p.recon = stepper, precision, dt_mode, recon
+        self.nx, self.ny = nx, ny
         self.nv = 5 if model == L.MP_DI4 else 6
         self.shape = (ny, nx, self.nv)
         self.dt = 0.0
@@ -352,3 +353,27 @@ class Multiphase2D:
 
     def sync(self):
         check(L.lib().hype_mp2d_sync(self._h), "hype_mp2d_sync")
+
+    # learned troubled-cell indicator (no counterpart in the reference)
+    def set_mlp(self, params, prob_threshold=0.5):
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        check(L.lib().hype_mp2d_set_mlp(self._h, params.ctypes.data_as(L.F), float(prob_threshold)), "hype_mp2d_set_mlp")
+
+    def set_recon(self, recon):
+        check(L.lib().hype_mp2d_set_recon(self._h, int(recon)), "hype_mp2d_set_recon")
+
+    def indicator_stats(self, reset=False):
+        """owned-cell reconstructions flagged by the network since the last reset"""
+        f = C.c_longlong()
+        check(L.lib().hype_mp2d_indicator_stats(self._h, C.byref(f), int(reset)), "hype_mp2d_indicator_stats")
+        return f.value
+
+    def sample_features(self, stride=1):
+        """(X[n][3][25], D[n]) of every stride-th owned cell of the resident state"""
+        n = (self.nx * self.ny + stride - 1) // stride
+        X = np.empty((n, 3, 25), dtype=np.float32)
+        Dv = np.empty(n, dtype=np.float32)
+        ns = C.c_longlong()
+        check(L.lib().hype_mp2d_sample_features(self._h, int(stride), X.ctypes.data_as(L.F), Dv.ctypes.data_as(L.F),
+                                                C.byref(ns)), "hype_mp2d_sample_features")
+        return X, Dv

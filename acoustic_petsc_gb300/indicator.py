@@ -42,7 +42,9 @@ def init_params(seed: int = 0) -> np.ndarray:
 
 
 def sample(solver, stride: int = 1):
-    """(X[n][3][25], D[n]) from the solver's resident state."""
+    """(X[n][3][25], D[n]) from the solver's resident state (3D Euler or 2D multiphase)."""
+    if hasattr(solver, "sample_features"):
+        return solver.sample_features(stride)
     n = (solver.ctx.N_x * solver.ctx.N_y * solver.ctx.N_z + stride - 1) // stride
     X = np.empty((n, 3, NIN), dtype=np.float32)
     D = np.empty(n, dtype=np.float32)

@@ -533,10 +533,88 @@ def run_blast(args, ws, rank, local, n=512, ntrain=64, tau=0.01, prob=0.2):
             "gpu_launches": launches, "clocks": clocks}
 
 
+def run_mp2d_learned(args, ws, rank, local, n=1024, ntrain=256, tau=1e-4, prob=0.2):
+    """Config 3 with the learned indicator: Kapila 1024^2 shock-bubble, FP64 state, FP32
+    reconstruction/flux; plain CWENO4 vs the indicator-gated form (network trained on the
+    GPU on labels from a 256^2 run of the same problem) vs plain FP64, on the same GPU."""
+    import torch
+
+    import acoustic_petsc_gb300 as H
+    from acoustic_petsc_gb300 import indicator, workloads
+
+    L = H.lib()
+    H._lib.check(L.hype_set_device(local), "hype_set_device")
+    torch.cuda.set_device(local)
+    Lc = H._lib
+
+    def solver(nn, precision, recon=Lc.RECON_CWENO4):
+        U, h = workloads.kapila_bubble(nn, model=1)
+        m = H.Multiphase2D(nn, nn, h, CFL=0.4, boundaries=(2, 2, 2, 2), model=Lc.MP_KAPILA5, eos=workloads.KAPILA_EOS,
+                           stepper=Lc.STEP_SSPRK43, precision=precision, recon=recon)
+        m.set_state(U)
+        return m, U
+
+    tr, _ = solver(ntrain, Lc.PREC_FP64)
+    Xs, Ds = [], []
+    for _ in range(6):
+        tr.step(40)
+        X, D = indicator.sample(tr)
+        Xs.append(X)
+        Ds.append(D)
+    tr.close()
+    X, D = np.concatenate(Xs), np.concatenate(Ds)
+    y = indicator.labels(D, tau)
+    t0 = time.perf_counter()
+    params, loss = indicator.train(X, y, epochs=10, batch=4096, lr=3e-3, seed=0)
+    t_train = time.perf_counter() - t0
+    recall, precision, flagged_train = indicator.recall_precision(indicator.score(X, params), y, prob)
+    res = {}
+    clocks, launches = None, 0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for form, prec, recon in (("plain_fp32", Lc.PREC_FP32, Lc.RECON_CWENO4), ("learned_fp32", Lc.PREC_FP32, Lc.RECON_LEARNED),
+                              ("plain_fp64", Lc.PREC_FP64, Lc.RECON_CWENO4)):
+        m, _ = solver(n, prec, recon)
+        if recon == Lc.RECON_LEARNED:
+            m.set_mlp(params, prob)
+        m.step(max(args.warmup, 3))
+        m.indicator_stats(reset=True)
+        stream = torch.cuda.ExternalStream(L.hype_mp2d_stream(m._h))
+        l0 = H.launches()
+        torch.cuda.synchronize()
+        with Clocks(_gpu_index(local)) as clk:
+            e0.record(stream)
+            m.step(args.steps)
+            e1.record(stream)
+            e1.synchronize()
+        ms = _max_over_ranks(ws, e0.elapsed_time(e1))
+        res[form] = {"value": ws * n * n * args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
+                     "flagged_per_cell_stage": m.indicator_stats() / (4.0 * n * n * args.steps),
+                     "minmod_fallback_cells": m.fallback_cells}
+        if form == "learned_fp32":
+            clocks, launches = clk.summary(), H.launches() - l0
+        m.close()
+    v = res["learned_fp32"]["value"]
+    peak, kind = _peaks()
+    return {"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": res["learned_fp32"]["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 state / f32 recon+flux, bf16 indicator",
+            "data": "synthetic: shock-driven air bubble in water (stiffened gases), 1e8 Pa step at x < 0.2",
+            "config": {"workload": f"kapila2d_{n}_learned_indicator", "grid": [n, n], "cfl": 0.4,
+                       "scheme": "primitive CWENO4 + 8-node PAD/minmod + rotated HLLC + SSPRK(4,3)",
+                       "indicator": {"train_grid": ntrain, "samples": int(X.shape[0]), "tau": tau,
+                                     "prob_threshold": prob, "train_s": t_train, "final_loss": loss,
+                                     "recall": recall, "precision": precision, "flagged_train": flagged_train}},
+            "forms": res, "speedup_vs_plain_fp32": v / res["plain_fp32"]["value"],
+            "speedup_vs_plain_fp64": v / res["plain_fp64"]["value"],
+            "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None, "traffic": None},
+            "gpu_launches": launches, "clocks": clocks}
+
+
 WORKLOADS = {
     "blast512": run_blast,
     "blast256": lambda a, *r: run_blast(a, *r, n=256),
     "kapila1024": lambda a, *r: run_mp2d(a, *r, precision=0),
+    "kapila1024_learned": run_mp2d_learned,
     "kapila1024_fp32": lambda a, *r: run_mp2d(a, *r, precision=1),
     "euler256_hllc": lambda a, *r: run_euler(a, *r, precision=0, recon=0, flux=1),
     "euler256": lambda a, *r: run_euler(a, *r, precision=0, recon=0),

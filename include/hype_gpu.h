@@ -202,6 +202,9 @@ typedef struct {
     int stepper;                /* HYPE_STEP_* */
     int precision;              /* HYPE_PREC_*: FP32 = reconstruction + flux in FP32, EOS and state in FP64 */
     int dt_mode;                /* HYPE_DT_* (dt = CFL h / (2 s_max), 2d/weno4/bubble/rhs_function.c:385) */
+    int recon;                  /* HYPE_RECON_CWENO4, or HYPE_RECON_LEARNED (hype_mp2d_set_mlp): the network
+                                   scores each cell from its x and y stencils; flagged cells take CWENO4, the
+                                   others its R4 limit, R4 failing the admissibility nodes is redone with CWENO4 */
 } hype_mp2d_params;
 
 int hype_mp2d_create(const hype_mp2d_params* p, hype_mp2d** out);
@@ -217,6 +220,18 @@ int hype_mp2d_download(hype_mp2d* m, double* U_aos);
 int hype_mp2d_step(hype_mp2d* m, int nsteps, double* t_inout, double* dt_inout, long long* fallback_cells);
 int hype_mp2d_sync(hype_mp2d* m);
 void* hype_mp2d_stream(hype_mp2d* m);
+/* learned indicator of the 2D models (network layout as hype_mlp_*; inputs: the
+ * normalised 5-point stencils of mixture density, normal and tangential velocity,
+ * pressure and volume fraction along x and along y) */
+int hype_mp2d_set_mlp(hype_mp2d* m, const float* params, float prob_threshold);
+int hype_mp2d_set_recon(hype_mp2d* m, int recon);
+/* owned-cell reconstructions the network flagged (full CWENO4) since the last reset */
+int hype_mp2d_indicator_stats(hype_mp2d* m, long long* flagged, int reset);
+/* training samples from the resident state: every stride-th owned cell, its features
+ * X[s][3][25] (x, y, y: the training kernels take three directions) and D[s], the
+ * largest change the nonlinear CWENO4 weights make to one of its 8 face traces relative
+ * to the R4 polynomial, in units of the variable's magnitude in the cell */
+int hype_mp2d_sample_features(hype_mp2d* m, long long stride, float* X, float* D, long long* ns);
 
 /* ============================================================ CTCS acoustics */
 /* Drop-in for CTCS(DM, Vec Pold, Vec Pcurr, Vec Pnew, AppCtx*)

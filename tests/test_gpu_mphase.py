@@ -69,3 +69,74 @@ def test_kapila_fp32_recon_flux_error_stated(hype, oracle):
     l1 = float(np.abs(rho - rho_o).mean() / np.abs(rho_o).mean())
     print(f"Kapila FP32 recon/flux: L1(rho) rel err {l1:.2e} after 12 steps, state rel {rel(m.get_state(), Uo):.2e}")
     assert l1 <= 1e-3
+
+
+def _kapila_solver(hype, n, precision=0, recon=0):
+    from acoustic_petsc_gb300 import workloads as W
+
+    U, h = W.kapila_bubble(n, model=1)
+    L = hype._lib
+    m = hype.Multiphase2D(n, n, h, CFL=0.4, boundaries=(2, 2, 2, 2), model=L.MP_KAPILA5, eos=W.KAPILA_EOS,
+                          stepper=L.STEP_SSPRK43, precision=precision, recon=recon)
+    m.set_state(U)
+    return m
+
+
+def _kapila_training(hype, n=96, tau=1e-4):
+    """labels: tau = 1e-4 of the variable's magnitude; in units of p + pi (pi = 6e8 Pa for
+    water) the 1e8 Pa shock is weak and the nonlinear weights move traces by ~1e-3 at most"""
+    from acoustic_petsc_gb300 import indicator
+
+    m = _kapila_solver(hype, n)
+    Xs, Ds = [], []
+    for _ in range(6):
+        m.step(15)
+        X, D = indicator.sample(m)
+        Xs.append(X)
+        Ds.append(D)
+    m.close()
+    X, D = np.concatenate(Xs), np.concatenate(Ds)
+    y = indicator.labels(D, tau)
+    p, loss = indicator.train(X, y, epochs=20, batch=2048, lr=3e-3, seed=0)
+    return p, X, y
+
+
+def test_kapila_learned_indicator_trains_on_solver_labels(hype):
+    """2D learned indicator (config 3): labels from the solver's own CWENO4 weights, training on the GPU"""
+    from acoustic_petsc_gb300 import indicator
+
+    p, X, y = _kapila_training(hype)
+    assert 0.0 < y.mean() < 0.5
+    recall, precision, flagged = indicator.recall_precision(indicator.score(X, p), y, 0.2)
+    print(f"Kapila indicator: recall {recall:.3f} precision {precision:.3f} flagged {flagged:.3f} labels {y.mean():.3f}")
+    assert recall >= 0.9 and flagged <= 0.6
+
+
+def test_kapila_learned_gain_at_equal_error(hype):
+    """FP32-flux forms on the 64^2 shock-bubble problem against a 128^2 FP64 run of the same
+    problem (block averages of the mixture density): the learned form stays within 1.05x of
+    plain CWENO4's L1 error while most cells take the R4 path."""
+    L = hype._lib
+    p, _, _ = _kapila_training(hype)
+    n = 64
+    ref = _kapila_solver(hype, 2 * n)
+    plain = _kapila_solver(hype, n, precision=L.PREC_FP32)
+    learned = _kapila_solver(hype, n, precision=L.PREC_FP32, recon=L.RECON_LEARNED)
+    learned.set_mlp(p, 0.2)
+    learned.indicator_stats(reset=True)
+    T = 2.0e-4
+    steps = {}
+    for name, m in (("ref", ref), ("plain", plain), ("learned", learned)):
+        steps[name] = 0
+        while m.t < T:
+            m.step(1)
+            steps[name] += 1
+    rho = lambda U: U[..., 0] + U[..., 1]  # noqa: E731
+    r_ref = rho(ref.get_state()).reshape(n, 2, n, 2).mean(axis=(1, 3))
+    e_plain = np.abs(rho(plain.get_state()) - r_ref).mean() / np.abs(r_ref).mean()
+    e_learn = np.abs(rho(learned.get_state()) - r_ref).mean() / np.abs(r_ref).mean()
+    frac = learned.indicator_stats() / (n * n * 4.0 * steps["learned"])
+    print(f"Kapila L1(rho) vs 2x FP64: plain FP32 {e_plain:.3e} learned FP32 {e_learn:.3e}; flagged/cell-stage {frac:.3f}; "
+          f"minmod fallbacks {learned.fallback_cells}")
+    assert e_learn <= 1.05 * e_plain
+    assert frac < 0.5
