@@ -39,7 +39,10 @@ SYMBOLS = [
     "hype_probe_fma_peak", "hype_euler_rhs_noalloc", "hype_euler_noalloc_max_ext",
     "hype_mp2d_create", "hype_mp2d_destroy", "hype_mp2d_rhs", "hype_mp2d_upload", "hype_mp2d_download",
     "hype_mp2d_step", "hype_mp2d_sync", "hype_mp2d_stream", "hype_mp2d_set_mlp", "hype_mp2d_set_recon",
-    "hype_mp2d_indicator_stats", "hype_mp2d_sample_features",
+    "hype_mp2d_indicator_stats", "hype_mp2d_sample_features", "hype_euler_get_params", "hype_mp2d_get_params",
+    "hype_write_petsc_vec", "hype_read_petsc_vec", "hype_write_vtk", "hype_euler_write_restart",
+    "hype_euler_read_restart", "hype_euler_write_vtk", "hype_mp2d_write_restart", "hype_mp2d_read_restart",
+    "hype_mp2d_write_vtk",
     "hype_euler_set_mlp", "hype_euler_set_recon", "hype_euler_indicator_stats", "hype_euler_sample_features",
     "hype_mlp_nparam", "hype_mlp_score", "hype_mlp_grad", "hype_mlp_train", "hype_euler_shadow_step",
 ]
@@ -151,6 +154,18 @@ def lib():
         "hype_mp2d_set_recon": ([V, C.c_int], C.c_int),
         "hype_mp2d_indicator_stats": ([V, P(C.c_longlong), C.c_int], C.c_int),
         "hype_mp2d_sample_features": ([V, C.c_longlong, F, F, P(C.c_longlong)], C.c_int),
+        "hype_euler_get_params": ([V, P(EulerParams)], C.c_int),
+        "hype_mp2d_get_params": ([V, P(Mp2dParams)], C.c_int),
+        "hype_write_petsc_vec": ([C.c_char_p, D, C.c_longlong, C.c_int], C.c_int),
+        "hype_read_petsc_vec": ([C.c_char_p, D, C.c_longlong], C.c_int),
+        "hype_write_vtk": ([C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                            C.c_double, C.c_int, P(C.c_char_p), D], C.c_int),
+        "hype_euler_write_restart": ([V, C.c_char_p], C.c_int),
+        "hype_euler_read_restart": ([V, C.c_char_p], C.c_int),
+        "hype_euler_write_vtk": ([V, C.c_char_p], C.c_int),
+        "hype_mp2d_write_restart": ([V, C.c_char_p], C.c_int),
+        "hype_mp2d_read_restart": ([V, C.c_char_p], C.c_int),
+        "hype_mp2d_write_vtk": ([V, C.c_char_p], C.c_int),
         "hype_euler_set_mlp": ([V, F, C.c_float], C.c_int),
         "hype_euler_set_recon": ([V, C.c_int], C.c_int),
         "hype_euler_indicator_stats": ([V, P(C.c_longlong), P(C.c_longlong), C.c_int], C.c_int),
@@ -178,7 +193,7 @@ def errstr(code: int) -> str:
 
 def check(code: int, where: str) -> None:
     if code != HYPE_OK:
-        detail = lib().hype_last_error().decode() if code == HYPE_ERR_CUDA else ""
+        detail = lib().hype_last_error().decode() if code in (HYPE_ERR_CUDA, HYPE_ERR_ARG) else ""
         raise HypeError(code, where, detail)
 
 

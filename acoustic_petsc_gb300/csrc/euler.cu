@@ -846,6 +846,12 @@ extern "C" int hype_euler_rhs_device(hype_euler* e, double t, const double* dU, 
     return rhs_core(e, dU, dRHS, dt_out);
 }
 
+extern "C" int hype_euler_get_params(const hype_euler* e, hype_euler_params* out) {
+    if (!e || !out) return HYPE_ERR_ARG;
+    *out = e->p;
+    return HYPE_OK;
+}
+
 extern "C" int hype_euler_upload(hype_euler* e, const double* U_aos) {
     if (!e || !U_aos) return HYPE_ERR_ARG;
     int rc = h2d_aos(e, U_aos, e->U);

@@ -576,6 +576,12 @@ extern "C" int hype_mp2d_rhs(hype_mp2d* m, double t, const double* U_aos, double
     return m->hs->bad == ~0ull ? HYPE_OK : HYPE_ERR_STATE;
 }
 
+extern "C" int hype_mp2d_get_params(const hype_mp2d* m, hype_mp2d_params* out) {
+    if (!m || !out) return HYPE_ERR_ARG;
+    *out = m->p;
+    return HYPE_OK;
+}
+
 extern "C" int hype_mp2d_upload(hype_mp2d* m, const double* U_aos) {
     if (!m || !U_aos) return HYPE_ERR_ARG;
     int rc = mp_h2d(m, U_aos, m->U);

@@ -13,6 +13,7 @@ Arrays use the DMDA layout: AoS ``[k][j][i][c]`` for HyPE states, ``[j][i]`` or
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -27,6 +28,31 @@ def _dp(a: np.ndarray):
     if a.dtype != np.float64 or not a.flags.c_contiguous:
         raise ValueError("arrays must be C-contiguous float64")
     return a.ctypes.data_as(_D)
+
+
+def write_petsc_vec(path, v, block_size=1):
+    """PETSc binary Vec record of v (what VecView on a binary viewer writes)"""
+    v = np.ascontiguousarray(v, dtype=np.float64).ravel()
+    check(L.lib().hype_write_petsc_vec(os.fsencode(path), _dp(v), v.size, int(block_size)), "hype_write_petsc_vec")
+
+
+def read_petsc_vec(path, n):
+    """n values of a PETSc binary Vec record (what VecLoad reads)"""
+    v = np.empty(int(n))
+    check(L.lib().hype_read_petsc_vec(os.fsencode(path), _dp(v), v.size), "hype_read_petsc_vec")
+    return v
+
+
+def write_vtk(path, aos, h, origin=(0.0, 0.0, 0.0), names=None, title="HyPE solution"):
+    """legacy VTK 2.0 ASCII file of a cell-centred [k][j][i][c] (or [j][i][c]) array"""
+    aos = np.ascontiguousarray(aos, dtype=np.float64)
+    shp = aos.shape[:-1]
+    nz, ny, nx = (1,) + shp if len(shp) == 2 else shp
+    nc = aos.shape[-1]
+    names = names or [f"c{q}" for q in range(nc)]
+    arr = (C.c_char_p * nc)(*[n.encode() for n in names])
+    check(L.lib().hype_write_vtk(os.fsencode(path), title.encode(), nx, ny, nz, origin[0], origin[1], origin[2], h, nc, arr,
+                                 _dp(aos)), "hype_write_vtk")
 
 
 @dataclass
@@ -108,6 +134,16 @@ class EulerSolver:
         check(L.lib().hype_euler_download(self._h, _dp(U)), "hype_euler_download")
         return U
 
+
+    def write_restart(self, path):
+        """the resident state as a PETSc binary Vec (restart1.bin of the reference's monitor)"""
+        check(L.lib().hype_euler_write_restart(self._h, os.fsencode(path)), "hype_euler_write_restart")
+
+    def read_restart(self, path):
+        check(L.lib().hype_euler_read_restart(self._h, os.fsencode(path)), "hype_euler_read_restart")
+
+    def write_vtk(self, path):
+        check(L.lib().hype_euler_write_vtk(self._h, os.fsencode(path)), "hype_euler_write_vtk")
     def step(self, nsteps: int, dt: float | None = None) -> L.Status:
         """nsteps of SSPRK(4,3) on the resident state (TSSolve with TSSSP RKS3, 4 stages)."""
         t = C.c_double(self.t)
@@ -343,6 +379,16 @@ class Multiphase2D:
         check(L.lib().hype_mp2d_download(self._h, _dp(U)), "hype_mp2d_download")
         return U
 
+
+    def write_restart(self, path):
+        """the resident state as a PETSc binary Vec"""
+        check(L.lib().hype_mp2d_write_restart(self._h, os.fsencode(path)), "hype_mp2d_write_restart")
+
+    def read_restart(self, path):
+        check(L.lib().hype_mp2d_read_restart(self._h, os.fsencode(path)), "hype_mp2d_read_restart")
+
+    def write_vtk(self, path):
+        check(L.lib().hype_mp2d_write_vtk(self._h, os.fsencode(path)), "hype_mp2d_write_vtk")
     def step(self, nsteps, dt=None):
         t = C.c_double(self.t)
         d = C.c_double(self.next_dt if dt is None else dt)

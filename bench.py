@@ -691,10 +691,10 @@ def main():
             out["cpu_baseline"] = {"value": n * n * 4 / d, "unit": "cell-updates/s", "cores": O.threads(),
                                    "kind": "port", "sample": f"4 SSPRK(4,3) steps of the {n}^2 version ({d:.1f} s)"}
         elif args.workload.startswith("euler"):
-            n = 96 if args.workload != "euler64" else 48
-            r, cores, kind, d = cpu_euler_rate(n, 2, use_ref=False)
+            n = 160 if args.workload != "euler64" else 48
+            r, cores, kind, d = cpu_euler_rate(n, 3, use_ref=False)
             out["cpu_baseline"] = {"value": r, "unit": "cell-updates/s", "cores": cores, "kind": kind,
-                                   "sample": f"2 SSPRK(4,3) steps of a {n}^3 periodic pulse grid ({d:.1f} s wall)"}
+                                   "sample": f"3 SSPRK(4,3) steps of a {n}^3 periodic pulse grid ({d:.1f} s wall)"}
         else:
             r, cores, kind, d = cpu_ctcs_rate(512, 300)
             out["cpu_baseline"] = {"value": r, "unit": "cell-updates/s", "cores": cores, "kind": kind,

@@ -98,6 +98,8 @@ typedef struct {
 /* Create a solver context and its device buffers. */
 int hype_euler_create(const hype_euler_params* p, hype_euler** out);
 void hype_euler_destroy(hype_euler* e);
+/* the parameters the context was created with (recon reflects hype_euler_set_recon) */
+int hype_euler_get_params(const hype_euler* e, hype_euler_params* out);
 
 /* Drop-in for RHSFunction(TS ts, PetscReal t, Vec U, Vec RHS, void* ctx)
  * (3d/weno3/Euler/hype.h:291 declaration; body 3d/weno4/Navier-Stokes-3D/rhs_function.c:12-443):
@@ -209,6 +211,7 @@ typedef struct {
 
 int hype_mp2d_create(const hype_mp2d_params* p, hype_mp2d** out);
 void hype_mp2d_destroy(hype_mp2d* m);
+int hype_mp2d_get_params(const hype_mp2d* m, hype_mp2d_params* out);
 /* Drop-in for the 2D RHSFunction (2d/weno4/bubble/rhs_function.c:12): primitive
  * CWENO4 with the 8-node admissibility check and minmod fallback, rotated HLLC,
  * divergence with the non-conservative volume-fraction term; host AoS [j][i][nv]. */
@@ -232,6 +235,27 @@ int hype_mp2d_indicator_stats(hype_mp2d* m, long long* flagged, int reset);
  * largest change the nonlinear CWENO4 weights make to one of its 8 face traces relative
  * to the R4 polynomial, in units of the variable's magnitude in the cell */
 int hype_mp2d_sample_features(hype_mp2d* m, long long stride, float* X, float* D, long long* ns);
+
+/* ============================================================ restart and output files */
+/* PETSc binary Vec record (what VecView on a binary viewer writes and VecLoad reads:
+ * int32 class id 1211214, int32 length, big-endian doubles; the reference's restart1.bin /
+ * restart2.bin, 3d/weno3/Euler/monitor_function.c:46-62, read back at hype.c:147-155);
+ * block_size > 1 also writes "<path>.info" with -vecload_block_size, as PETSc does for
+ * a multi-component DMDA vector. */
+int hype_write_petsc_vec(const char* path, const double* v, long long n, int block_size);
+int hype_read_petsc_vec(const char* path, double* v, long long n);
+/* legacy VTK 2.0 ASCII, STRUCTURED_POINTS on the cell centres, one SCALARS section per
+ * component of the interleaved [k][j][i][c] array aos (the reference's sol-*.vtk,
+ * hype.c:202-208, is PETSc's ASCII_VTK view of the same DMDA vector) */
+int hype_write_vtk(const char* path, const char* title, int nx, int ny, int nz, double x0, double y0, double z0, double h,
+                   int ncomp, const char* const* names, const double* aos);
+/* the resident state of a context, in the DMDA natural order [k][j][i][c] */
+int hype_euler_write_restart(hype_euler* e, const char* path);
+int hype_euler_read_restart(hype_euler* e, const char* path);
+int hype_euler_write_vtk(hype_euler* e, const char* path);
+int hype_mp2d_write_restart(hype_mp2d* m, const char* path);
+int hype_mp2d_read_restart(hype_mp2d* m, const char* path);
+int hype_mp2d_write_vtk(hype_mp2d* m, const char* path);
 
 /* ============================================================ CTCS acoustics */
 /* Drop-in for CTCS(DM, Vec Pold, Vec Pcurr, Vec Pnew, AppCtx*)

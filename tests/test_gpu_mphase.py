@@ -140,3 +140,17 @@ def test_kapila_learned_gain_at_equal_error(hype):
           f"minmod fallbacks {learned.fallback_cells}")
     assert e_learn <= 1.05 * e_plain
     assert frac < 0.5
+
+
+def test_multiphase_restart_round_trip(hype, tmp_path):
+    L = hype._lib
+    m = _kapila_solver(hype, 40)
+    m.step(5)
+    m.write_restart(tmp_path / "restart1.bin")
+    assert (tmp_path / "restart1.bin.info").read_text().strip() == "-vecload_block_size 6"
+    k = _kapila_solver(hype, 40)
+    k.read_restart(tmp_path / "restart1.bin")
+    assert np.array_equal(k.get_state(), m.get_state())
+    m.write_vtk(tmp_path / "sol.vtk")
+    assert (tmp_path / "sol.vtk").read_text().splitlines()[4] == "DIMENSIONS 40 40 1"
+    assert L.MP_KAPILA5 == 1
