@@ -17,7 +17,7 @@ I = C.POINTER(C.c_int)
 F = C.POINTER(C.c_float)
 
 HYPE_OK, HYPE_ERR_ARG, HYPE_ERR_STATE, HYPE_ERR_CUDA, HYPE_ERR_NOMEM, HYPE_ERR_UNSUPPORTED = range(6)
-BC_PERIODIC, BC_REFLECTIVE, BC_TRANSMISSIVE, BC_ZERO = range(4)
+BC_PERIODIC, BC_REFLECTIVE, BC_TRANSMISSIVE, BC_ZERO, BC_ADIABATIC = range(5)
 RECON_CWENO4, RECON_LINEAR4, RECON_LEARNED, RECON_WENO3 = 0, 1, 2, 3
 PREC_FP64, PREC_FP32 = 0, 1
 DT_MONITOR, DT_FROZEN, DT_FIXED = 0, 1, 2
@@ -42,7 +42,8 @@ SYMBOLS = [
     "hype_mp2d_indicator_stats", "hype_mp2d_sample_features", "hype_euler_get_params", "hype_mp2d_get_params",
     "hype_write_petsc_vec", "hype_read_petsc_vec", "hype_write_vtk", "hype_euler_write_restart",
     "hype_euler_read_restart", "hype_euler_write_vtk", "hype_mp2d_write_restart", "hype_mp2d_read_restart",
-    "hype_mp2d_write_vtk",
+    "hype_mp2d_write_vtk", "hype_acoustic_create", "hype_acoustic_destroy", "hype_acoustic_upload",
+    "hype_acoustic_download", "hype_acoustic_rhs", "hype_acoustic_step", "hype_acoustic_sync", "hype_acoustic_stream",
     "hype_euler_set_mlp", "hype_euler_set_recon", "hype_euler_indicator_stats", "hype_euler_sample_features",
     "hype_mlp_nparam", "hype_mlp_score", "hype_mlp_grad", "hype_mlp_train", "hype_euler_shadow_step",
 ]
@@ -70,6 +71,12 @@ class Mp2dParams(C.Structure):
                 ("cfl", C.c_double), ("bc", C.c_int * 4), ("model", C.c_int), ("g1", C.c_double), ("p1", C.c_double),
                 ("g2", C.c_double), ("p2", C.c_double), ("stepper", C.c_int), ("precision", C.c_int),
                 ("dt_mode", C.c_int), ("recon", C.c_int)]
+
+
+class AcousticParams(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("x_min", C.c_double), ("y_min", C.c_double),
+                ("z_min", C.c_double), ("h", C.c_double), ("c", C.c_double), ("dt", C.c_double), ("bc", C.c_int * 6),
+                ("recon", C.c_int)]
 
 
 class Status(C.Structure):
@@ -166,6 +173,14 @@ def lib():
         "hype_mp2d_write_restart": ([V, C.c_char_p], C.c_int),
         "hype_mp2d_read_restart": ([V, C.c_char_p], C.c_int),
         "hype_mp2d_write_vtk": ([V, C.c_char_p], C.c_int),
+        "hype_acoustic_create": ([P(AcousticParams), P(V)], C.c_int),
+        "hype_acoustic_destroy": ([V], None),
+        "hype_acoustic_upload": ([V, D], C.c_int),
+        "hype_acoustic_download": ([V, D], C.c_int),
+        "hype_acoustic_rhs": ([V, D, D], C.c_int),
+        "hype_acoustic_step": ([V, C.c_int, C.c_double, D, I], C.c_int),
+        "hype_acoustic_sync": ([V], C.c_int),
+        "hype_acoustic_stream": ([V], C.c_void_p),
         "hype_euler_set_mlp": ([V, F, C.c_float], C.c_int),
         "hype_euler_set_recon": ([V, C.c_int], C.c_int),
         "hype_euler_indicator_stats": ([V, P(C.c_longlong), P(C.c_longlong), C.c_int], C.c_int),

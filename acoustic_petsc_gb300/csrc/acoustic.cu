@@ -1,0 +1,347 @@
+// acoustic.cu -- the acoustic finite-volume path of HyPE (3d/weno4/plane_wave):
+// the wave equation u_tt = c^2 lap u as the first-order system (u, v = u_t),
+//   du/dt = v,   dv/dt = c^2 div grad u,
+// with cell averages of u reconstructed by CWENO4 (the reference runs its optimal-
+// weight limit, gammaHi = 1: the R4 polynomial), the normal gradient of the
+// polynomial at the 2x2 Gauss points of every face, the central flux
+// c^2 (grad_L + grad_R) . n / 2 (pde.c:12-34), and SSPRK(4,3) with a fixed dt.
+//
+// Per RHS evaluation (rhs_function.c:12-345):
+//   k_ac_ghost   u with 3 ghost layers: periodic wrap, or the adiabatic wall's odd
+//                mirror u_ghost = -u (rhs_function.c:43-131);
+//   k_ac_recon   per extended cell: the 33-point stencil, CWENO4 / R4 coefficients,
+//                the 24 face-normal gradients (evaluate_grad, reconstruction.c:25-34);
+//   k_ac_faces   per face: 4 Gauss points of the central flux (:176-287);
+//   k_ac_update  RHS (v, (1/h) sum of flux differences) fused with the stage
+//                combination (:289-300).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include "euler_kernels.cuh"
+
+namespace hype {
+namespace acoustic {
+
+using euler::NTR;
+
+struct Geo {
+    int nx, ny, nz;
+    int bc[6];
+    long long N, NE;  // owned cells, extended cells (n+2)^3
+    int ex;           // extended x extent
+    int gx, gy;       // ghosted extents (n + 6)
+    long long GN;     // ghosted cells
+};
+
+constexpr int GW = 3;
+
+__device__ __forceinline__ long long ext_index(const Geo& g, int i, int j, int k) {
+    return ((long long)(k + 1) * (g.ny + 2) + (j + 1)) * (long long)g.ex + (i + 1);
+}
+__device__ __forceinline__ long long ghost_index(const Geo& g, int i, int j, int k) {
+    return ((long long)(k + GW) * g.gy + (j + GW)) * g.gx + (i + GW);
+}
+
+// the boundary map of one axis: periodic wrap, or the mirror of the adiabatic wall
+// (whose ghost value is the negated mirror value)
+__device__ __forceinline__ int amap(int i, int n, int blo, int bhi, int* flip) {
+    return bmap(i, n, blo == HYPE_BC_PERIODIC ? HYPE_BC_PERIODIC : HYPE_BC_REFLECTIVE,
+                bhi == HYPE_BC_PERIODIC ? HYPE_BC_PERIODIC : HYPE_BC_REFLECTIVE, flip);
+}
+
+__global__ void __launch_bounds__(128) k_ac_ghost(const double* __restrict__ U, double* __restrict__ G, Geo g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - GW;
+    const int j = blockIdx.y - GW, k = blockIdx.z - GW;
+    if (i >= g.nx + GW) return;
+    int fi = 0, fj = 0, fk = 0;
+    const int mi = amap(i, g.nx, g.bc[0], g.bc[1], &fi);
+    const int mj = amap(j, g.ny, g.bc[2], g.bc[3], &fj);
+    const int mk = amap(k, g.nz, g.bc[4], g.bc[5], &fk);
+    const double v = __ldg(U + ((long long)mk * g.ny + mj) * g.nx + mi);  // component u
+    G[ghost_index(g, i, j, k)] = ((fi + fj + fk) & 1) ? -v : v;
+}
+
+// gradient component D of the 20-term polynomial at (x, y, z), times h
+template <int D>
+__device__ __forceinline__ double grad_poly(const double* c, double x, double y, double z) {
+    constexpr double r1_12 = 1. / 12., r3_20 = 3. / 20.;
+    if (D == 0)
+        return c[1] + 2.0 * c[4] * x + c[7] * y + c[9] * z + c[10] * (3.0 * x * x - r3_20) + 2.0 * c[13] * x * y +
+               c[14] * (y * y - r1_12) + 2.0 * c[17] * x * z + c[18] * (z * z - r1_12) + c[19] * y * z;
+    if (D == 1)
+        return c[2] + 2.0 * c[5] * y + c[7] * x + c[8] * z + c[11] * (3.0 * y * y - r3_20) + c[13] * (x * x - r1_12) +
+               2.0 * c[14] * x * y + 2.0 * c[15] * y * z + c[16] * (z * z - r1_12) + c[19] * x * z;
+    return c[3] + 2.0 * c[6] * z + c[8] * y + c[9] * x + c[12] * (3.0 * z * z - r3_20) + c[15] * (y * y - r1_12) +
+           2.0 * c[16] * y * z + c[17] * (x * x - r1_12) + 2.0 * c[18] * x * z + c[19] * x * y;
+}
+
+// T[face][gp][extended cell]: the face-normal gradient (times h) at the 4 Gauss points
+// of the 6 faces; Gauss point q = 2 (t1 > 0) + (t2 > 0), (t1, t2) the remaining axes
+__global__ void __launch_bounds__(128) k_ac_recon(const double* __restrict__ G, double* __restrict__ T, Geo g, int linear) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+    const int k = blockIdx.z - 1;
+    if (i > g.nx || j > g.ny) return;
+    const int gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny), gk = (k < 0 || k >= g.nz);
+    if (gi + gj + gk > 1) return;
+    const double* p = G + ghost_index(g, i, j, k);
+    const int sy = g.gx, sz = g.gx * g.gy;
+    double s[33], cf[20];
+    s[0] = __ldg(p);
+#pragma unroll
+    for (int o = 0; o < 4; ++o) {
+        const int off = (o == 0) ? -2 : (o == 1) ? -1 : (o == 2) ? 1 : 2;
+        s[euler::S1(0, off)] = __ldg(p + off);
+        s[euler::S1(1, off)] = __ldg(p + off * sy);
+        s[euler::S1(2, off)] = __ldg(p + off * sz);
+    }
+#pragma unroll
+    for (int sa = 0; sa < 2; ++sa)
+#pragma unroll
+        for (int sb = 0; sb < 2; ++sb) {
+            s[euler::SQ(0, sa, 1, sb)] = __ldg(p + (2 * sa - 1) + (2 * sb - 1) * sy);
+            s[euler::SQ(1, sa, 2, sb)] = __ldg(p + (2 * sa - 1) * sy + (2 * sb - 1) * sz);
+            s[euler::SQ(0, sa, 2, sb)] = __ldg(p + (2 * sa - 1) + (2 * sb - 1) * sz);
+        }
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int d = 0; d < 2; ++d) s[euler::SO(a, b, d)] = __ldg(p + (2 * a - 1) + (2 * b - 1) * sy + (2 * d - 1) * sz);
+    euler::cweno4<double>(s, linear != 0, cf);
+    const long long e = ext_index(g, i, j, k);
+    constexpr double gp = euler::GPT;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const double t1 = (q & 2) ? gp : -gp, t2 = (q & 1) ? gp : -gp;
+        T[(long long)(0 * 4 + q) * g.NE + e] = grad_poly<0>(cf, -0.5, t1, t2);
+        T[(long long)(1 * 4 + q) * g.NE + e] = grad_poly<0>(cf, 0.5, t1, t2);
+        T[(long long)(2 * 4 + q) * g.NE + e] = grad_poly<1>(cf, t1, -0.5, t2);
+        T[(long long)(3 * 4 + q) * g.NE + e] = grad_poly<1>(cf, t1, 0.5, t2);
+        T[(long long)(4 * 4 + q) * g.NE + e] = grad_poly<2>(cf, t1, t2, -0.5);
+        T[(long long)(5 * 4 + q) * g.NE + e] = grad_poly<2>(cf, t1, t2, 0.5);
+    }
+}
+
+// face flux sum_q w_q c^2 (gL + gR) / 2, w_q = 1/4 (the gradients carry a factor h
+// that the divergence's 1/h^2 removes)
+template <int D>
+__global__ void __launch_bounds__(128) k_ac_faces(const double* __restrict__ T, double* __restrict__ F, Geo g, double c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    const int fx = g.nx + (D == 0), fy = g.ny + (D == 1);
+    if (i >= fx || j >= fy) return;
+    const long long eR = ext_index(g, i, j, k);
+    const long long eL = ext_index(g, i - (D == 0), j - (D == 1), k - (D == 2));
+    double flux = 0.0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const double gL = T[(long long)((2 * D + 1) * 4 + q) * g.NE + eL];
+        const double gR = T[(long long)((2 * D) * 4 + q) * g.NE + eR];
+        flux += 0.25 * (0.5 * (c2 * gR + c2 * gL));
+    }
+    F[((long long)k * fy + j) * fx + i] = flux;
+}
+
+struct Stage {
+    double a, b, c;  // out = a U + b W + (c dt) L, or (rhs_only) out = L
+    int rhs_only;
+};
+
+// U, W, out: SoA [2][N]; L = (v, (1/h^2) sum of face-flux differences)
+__global__ void __launch_bounds__(256) k_ac_update(const double* __restrict__ Fx, const double* __restrict__ Fy,
+                                                   const double* __restrict__ Fz, const double* __restrict__ U,
+                                                   const double* __restrict__ W, double* __restrict__ out, Geo g,
+                                                   double r1_h2, Stage st, double dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= g.nx || j >= g.ny) return;
+    const long long cell = ((long long)k * g.ny + j) * g.nx + i;
+    const long long ix = ((long long)k * g.ny + j) * (g.nx + 1) + i;
+    const long long iy = ((long long)k * (g.ny + 1) + j) * g.nx + i;
+    const long long iz = cell;
+    const double div = r1_h2 * (Fx[ix + 1] - Fx[ix]) + r1_h2 * (Fy[iy + g.nx] - Fy[iy]) +
+                       r1_h2 * (Fz[iz + (long long)g.nx * g.ny] - Fz[iz]);
+    const double L[2] = {W[g.N + cell], div};
+    const double cdt = st.c * dt;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        double v;
+        if (st.rhs_only) v = L[c];
+        else if (st.a != 0.0) v = st.a * U[c * g.N + cell] + st.b * W[c * g.N + cell] + cdt * L[c];
+        else v = W[c * g.N + cell] + cdt * L[c];
+        out[c * g.N + cell] = v;
+    }
+}
+
+__global__ void k_ac_aos2soa(const double* __restrict__ a, double* __restrict__ s, long long N) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= N) return;
+    s[q] = a[2 * q];
+    s[N + q] = a[2 * q + 1];
+}
+__global__ void k_ac_soa2aos(const double* __restrict__ s, double* __restrict__ a, long long N) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= N) return;
+    a[2 * q] = s[q];
+    a[2 * q + 1] = s[N + q];
+}
+
+}  // namespace acoustic
+}  // namespace hype
+
+using namespace hype;
+using namespace hype::acoustic;
+
+struct hype_acoustic {
+    hype_acoustic_params p;
+    Geo g;
+    cudaStream_t stream = nullptr;
+    double *U = nullptr, *W = nullptr, *L = nullptr, *S = nullptr, *Gh = nullptr, *T = nullptr;
+    double *Fx = nullptr, *Fy = nullptr, *Fz = nullptr, *aos = nullptr;
+};
+
+static int ac_rhs(hype_acoustic* a, const double* Win) {
+    const Geo& g = a->g;
+    k_ac_ghost<<<dim3(cdiv(g.gx, 128), g.gy, g.nz + 2 * GW), 128, 0, a->stream>>>(Win, a->Gh, g);
+    k_ac_recon<<<dim3(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2), dim3(32, 4), 0, a->stream>>>(
+        a->Gh, a->T, g, a->p.recon == HYPE_RECON_LINEAR4);
+    const double c2 = a->p.c * a->p.c;
+    const dim3 bf(32, 4);
+    k_ac_faces<0><<<dim3(cdiv(g.nx + 1, 32), cdiv(g.ny, 4), g.nz), bf, 0, a->stream>>>(a->T, a->Fx, g, c2);
+    k_ac_faces<1><<<dim3(cdiv(g.nx, 32), cdiv(g.ny + 1, 4), g.nz), bf, 0, a->stream>>>(a->T, a->Fy, g, c2);
+    k_ac_faces<2><<<dim3(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz + 1), bf, 0, a->stream>>>(a->T, a->Fz, g, c2);
+    HYPE_LAUNCHED(5);
+    return HYPE_OK;
+}
+
+static int ac_update(hype_acoustic* a, const double* U, const double* W, double* out, Stage st, double dt) {
+    const Geo& g = a->g;
+    k_ac_update<<<dim3(cdiv(g.nx, 32), cdiv(g.ny, 8), g.nz), dim3(32, 8), 0, a->stream>>>(
+        a->Fx, a->Fy, a->Fz, U, W, out, g, 1.0 / (a->p.h * a->p.h), st, dt);
+    HYPE_LAUNCHED(1);
+    return HYPE_OK;
+}
+
+extern "C" int hype_acoustic_create(const hype_acoustic_params* p, hype_acoustic** out) {
+    if (!p || !out) return HYPE_ERR_ARG;
+    *out = nullptr;
+    if (p->nx < 3 || p->ny < 3 || p->nz < 3 || !(p->h > 0) || !(p->c > 0) || !(p->dt > 0)) return HYPE_ERR_ARG;
+    for (int f = 0; f < 6; ++f)
+        if (p->bc[f] != HYPE_BC_PERIODIC && p->bc[f] != HYPE_BC_ADIABATIC) return HYPE_ERR_ARG;
+    for (int d = 0; d < 3; ++d)
+        if ((p->bc[2 * d] == HYPE_BC_PERIODIC) != (p->bc[2 * d + 1] == HYPE_BC_PERIODIC)) return HYPE_ERR_ARG;
+    if (p->recon != HYPE_RECON_LINEAR4 && p->recon != HYPE_RECON_CWENO4) return HYPE_ERR_ARG;
+    hype_acoustic* a = new hype_acoustic();
+    a->p = *p;
+    Geo& g = a->g;
+    g.nx = p->nx; g.ny = p->ny; g.nz = p->nz;
+    for (int f = 0; f < 6; ++f) g.bc[f] = p->bc[f];
+    g.N = (long long)p->nx * p->ny * p->nz;
+    g.NE = (long long)(p->nx + 2) * (p->ny + 2) * (p->nz + 2);
+    g.ex = p->nx + 2;
+    g.gx = p->nx + 2 * GW;
+    g.gy = p->ny + 2 * GW;
+    g.GN = (long long)g.gx * g.gy * (p->nz + 2 * GW);
+    const size_t sN = sizeof(double) * 2 * (size_t)g.N;
+    cudaError_t ce = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking);
+    double** bufs[] = {&a->U, &a->W, &a->L, &a->S, &a->aos};
+    for (auto b : bufs)
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)b, sN);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&a->Gh, sizeof(double) * (size_t)g.GN);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&a->T, sizeof(double) * NTR * (size_t)g.NE);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&a->Fx, sizeof(double) * (size_t)(p->nx + 1) * p->ny * p->nz);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&a->Fy, sizeof(double) * (size_t)p->nx * (p->ny + 1) * p->nz);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&a->Fz, sizeof(double) * (size_t)p->nx * p->ny * (p->nz + 1));
+    if (ce != cudaSuccess) {
+        set_last_error("hype_acoustic_create", ce);
+        hype_acoustic_destroy(a);
+        return ce == cudaErrorMemoryAllocation ? HYPE_ERR_NOMEM : HYPE_ERR_CUDA;
+    }
+    *out = a;
+    return HYPE_OK;
+}
+
+extern "C" void hype_acoustic_destroy(hype_acoustic* a) {
+    if (!a) return;
+    if (a->stream) cudaStreamSynchronize(a->stream);
+    cudaFree(a->U); cudaFree(a->W); cudaFree(a->L); cudaFree(a->S); cudaFree(a->aos); cudaFree(a->Gh); cudaFree(a->T);
+    cudaFree(a->Fx); cudaFree(a->Fy); cudaFree(a->Fz);
+    if (a->stream) cudaStreamDestroy(a->stream);
+    delete a;
+}
+
+static int ac_h2d(hype_acoustic* a, const double* aos, double* soa) {
+    const long long N = a->g.N;
+    HYPE_CK(cudaMemcpyAsync(a->aos, aos, sizeof(double) * 2 * N, cudaMemcpyHostToDevice, a->stream));
+    k_ac_aos2soa<<<cdiv(N, 256), 256, 0, a->stream>>>(a->aos, soa, N);
+    HYPE_LAUNCHED(1);
+    return HYPE_OK;
+}
+
+static int ac_d2h(hype_acoustic* a, const double* soa, double* aos) {
+    const long long N = a->g.N;
+    k_ac_soa2aos<<<cdiv(N, 256), 256, 0, a->stream>>>(soa, a->aos, N);
+    HYPE_LAUNCHED(1);
+    HYPE_CK(cudaMemcpyAsync(aos, a->aos, sizeof(double) * 2 * N, cudaMemcpyDeviceToHost, a->stream));
+    HYPE_CK(cudaStreamSynchronize(a->stream));
+    return HYPE_OK;
+}
+
+extern "C" int hype_acoustic_upload(hype_acoustic* a, const double* U_aos) {
+    if (!a || !U_aos) return HYPE_ERR_ARG;
+    int rc = ac_h2d(a, U_aos, a->U);
+    if (rc) return rc;
+    HYPE_CK(cudaStreamSynchronize(a->stream));
+    return HYPE_OK;
+}
+
+extern "C" int hype_acoustic_download(hype_acoustic* a, double* U_aos) {
+    if (!a || !U_aos) return HYPE_ERR_ARG;
+    return ac_d2h(a, a->U, U_aos);
+}
+
+extern "C" int hype_acoustic_rhs(hype_acoustic* a, const double* U_aos, double* RHS_aos) {
+    if (!a || !U_aos || !RHS_aos) return HYPE_ERR_ARG;
+    int rc = ac_h2d(a, U_aos, a->S);
+    if (rc || (rc = ac_rhs(a, a->S))) return rc;
+    if ((rc = ac_update(a, a->S, a->S, a->L, Stage{0.0, 0.0, 0.0, 1}, 0.0))) return rc;
+    return ac_d2h(a, a->L, RHS_aos);
+}
+
+// SSPRK(4,3) steps of dt from *t_inout; a positive t_final shortens the step that
+// would pass it so that the run ends on t_final (TS_EXACTFINALTIME_MATCHSTEP)
+// and stops there.  Returns the number of steps taken in *steps_taken.
+extern "C" int hype_acoustic_step(hype_acoustic* a, int nsteps, double t_final, double* t_inout, int* steps_taken) {
+    if (!a || !t_inout || nsteps < 0) return HYPE_ERR_ARG;
+    double t = *t_inout;
+    int s = 0;
+    const Stage s12{0.0, 1.0, 0.5, 0}, s3{2.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 0};
+    for (; s < nsteps; ++s) {
+        if (t_final > 0.0 && t >= t_final) break;
+        double dt = a->p.dt;
+        if (t_final > 0.0 && t + dt > t_final) dt = t_final - t;
+        int rc;
+        if ((rc = ac_rhs(a, a->U)) || (rc = ac_update(a, a->U, a->U, a->W, s12, dt))) return rc;  // u1 = u + dt/2 L(u)
+        if ((rc = ac_rhs(a, a->W)) || (rc = ac_update(a, a->U, a->W, a->W, s12, dt))) return rc;  // u2 = u1 + dt/2 L(u1)
+        if ((rc = ac_rhs(a, a->W)) || (rc = ac_update(a, a->U, a->W, a->W, s3, dt))) return rc;  // u3 = 2/3 u + u2/3 + dt/6 L(u2)
+        if ((rc = ac_rhs(a, a->W)) || (rc = ac_update(a, a->U, a->W, a->U, s12, dt))) return rc;  // u3 + dt/2 L(u3)
+        t += dt;
+    }
+    HYPE_CK(cudaStreamSynchronize(a->stream));
+    *t_inout = t;
+    if (steps_taken) *steps_taken = s;
+    return HYPE_OK;
+}
+
+extern "C" int hype_acoustic_sync(hype_acoustic* a) {
+    if (!a) return HYPE_ERR_ARG;
+    HYPE_CK(cudaStreamSynchronize(a->stream));
+    return HYPE_OK;
+}
+
+extern "C" void* hype_acoustic_stream(hype_acoustic* a) { return a ? (void*)a->stream : nullptr; }

@@ -423,3 +423,61 @@ class Multiphase2D:
         check(L.lib().hype_mp2d_sample_features(self._h, int(stride), X.ctypes.data_as(L.F), Dv.ctypes.data_as(L.F),
                                                 C.byref(ns)), "hype_mp2d_sample_features")
         return X, Dv
+
+
+class AcousticFV3D:
+    """The acoustic finite-volume path of 3d/weno4/plane_wave: u_tt = c^2 lap u as
+    (u, v = u_t) with CWENO4 (default: its R4 limit, as the reference runs it)
+    face-normal gradients, a central flux and SSPRK(4,3) with a fixed dt."""
+
+    def __init__(self, N_x, N_y, N_z, h, dt, c=1.0, x_min=0.0, y_min=0.0, z_min=0.0,
+                 boundaries=(L.BC_PERIODIC,) * 6, recon=L.RECON_LINEAR4):
+        p = L.AcousticParams()
+        p.nx, p.ny, p.nz = N_x, N_y, N_z
+        p.x_min, p.y_min, p.z_min, p.h, p.c, p.dt = x_min, y_min, z_min, h, c, dt
+        for q in range(6):
+            p.bc[q] = int(boundaries[q])
+        p.recon = recon
+        self.shape = (N_z, N_y, N_x, 2)
+        self.t = 0.0
+        self._h = C.c_void_p()
+        check(L.lib().hype_acoustic_create(C.byref(p), C.byref(self._h)), "hype_acoustic_create")
+
+    def close(self):
+        if self._h:
+            L.lib().hype_acoustic_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def RHSFunction(self, t, U, RHS=None):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        if U.shape != self.shape:
+            raise ValueError(f"U must have shape {self.shape}")
+        if RHS is None:
+            RHS = np.empty_like(U)
+        check(L.lib().hype_acoustic_rhs(self._h, _dp(U), _dp(RHS)), "RHSFunction")
+        return RHS
+
+    def set_state(self, U):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        check(L.lib().hype_acoustic_upload(self._h, _dp(U)), "hype_acoustic_upload")
+
+    def get_state(self):
+        U = np.empty(self.shape)
+        check(L.lib().hype_acoustic_download(self._h, _dp(U)), "hype_acoustic_download")
+        return U
+
+    def step(self, nsteps, t_final=0.0):
+        """up to nsteps steps; t_final > 0 ends the run exactly on t_final
+        (TS_EXACTFINALTIME_MATCHSTEP). Returns the steps taken."""
+        t = C.c_double(self.t)
+        n = C.c_int(0)
+        check(L.lib().hype_acoustic_step(self._h, int(nsteps), float(t_final), C.byref(t), C.byref(n)),
+              "hype_acoustic_step")
+        self.t = t.value
+        return n.value

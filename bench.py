@@ -610,11 +610,59 @@ def run_mp2d_learned(args, ws, rank, local, n=1024, ntrain=256, tau=1e-4, prob=0
             "gpu_launches": launches, "clocks": clocks}
 
 
+def run_acoustic(args, ws, rank, local, n=256):
+    """acoustic FV path of 3d/weno4/plane_wave: the plane wave k = (1,1,1) on [0, 2 pi]^3,
+    periodic, R4 face gradients + central flux, SSPRK(4,3) with dt = h CFL / 3, CFL 0.5"""
+    import math
+
+    import torch
+
+    import acoustic_petsc_gb300 as H
+
+    L = H.lib()
+    H._lib.check(L.hype_set_device(local), "hype_set_device")
+    torch.cuda.set_device(local)
+    h = 2 * math.pi / n
+    s = H.AcousticFV3D(n, n, n, h, h * 0.5 / 3.0)
+    x = (np.arange(n) + 0.5) * h
+    ph = x[:, None, None] + x[None, :, None] + x[None, None, :]
+    U0 = np.stack([np.sin(ph), -math.sqrt(3.0) * np.cos(ph)], -1)
+    s.set_state(U0)
+    s.step(max(args.warmup, 3))
+    stream = torch.cuda.ExternalStream(L.hype_acoustic_stream(s._h))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = H.launches()
+    _barrier(ws)
+    torch.cuda.synchronize()
+    with Clocks(_gpu_index(local)) as clk:
+        e0.record(stream)
+        s.step(args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    launches = H.launches() - l0
+    ms = _max_over_ranks(ws, e0.elapsed_time(e1))
+    cells = n**3
+    value = ws * cells * args.steps / (ms * 1e-3)
+    peak, kind = _peaks()
+    bytes_cu = 4 * 32 + 16  # per stage read + write (u, v), one extra read of u^n per step
+    ach = bytes_cu * cells * args.steps / (ms * 1e-3) / 1e9
+    s.close()
+    return {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic plane wave sin(x+y+z), exact cell-centre values",
+            "config": {"workload": f"acoustic_fv_plane_wave_{n}", "grid": [n, n, n], "cfl": 0.5,
+                       "scheme": "R4 face gradients + central flux + SSPRK(4,3), 3d/weno4/plane_wave"},
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "traffic": None},
+            "gpu_launches": launches, "clocks": clk.summary()}
+
+
 WORKLOADS = {
     "blast512": run_blast,
     "blast256": lambda a, *r: run_blast(a, *r, n=256),
     "kapila1024": lambda a, *r: run_mp2d(a, *r, precision=0),
     "kapila1024_learned": run_mp2d_learned,
+    "acoustic256": run_acoustic,
     "kapila1024_fp32": lambda a, *r: run_mp2d(a, *r, precision=1),
     "euler256_hllc": lambda a, *r: run_euler(a, *r, precision=0, recon=0, flux=1),
     "euler256": lambda a, *r: run_euler(a, *r, precision=0, recon=0),

@@ -41,6 +41,7 @@ extern "C" {
 #define HYPE_BC_REFLECTIVE 1
 #define HYPE_BC_TRANSMISSIVE 2
 #define HYPE_BC_ZERO 3
+#define HYPE_BC_ADIABATIC 4 /* acoustic wall: the ghost value is the negated mirror value (3d/weno4/plane_wave) */
 
 /* reconstruction */
 #define HYPE_RECON_CWENO4 0  /* nonlinear CWENO4, gammaHi=gammaLo=0.85
@@ -235,6 +236,36 @@ int hype_mp2d_indicator_stats(hype_mp2d* m, long long* flagged, int reset);
  * largest change the nonlinear CWENO4 weights make to one of its 8 face traces relative
  * to the R4 polynomial, in units of the variable's magnitude in the cell */
 int hype_mp2d_sample_features(hype_mp2d* m, long long stride, float* X, float* D, long long* ns);
+
+/* ============================================================ acoustic finite volume */
+/* The acoustic path of 3d/weno4/plane_wave: u_tt = c^2 lap u as (u, v = u_t),
+ * du/dt = v, dv/dt = c^2 div grad u; CWENO4 reconstruction of u (the reference runs
+ * its optimal-weight limit, gammaHi = 1, reconstruction.c:38-44: HYPE_RECON_LINEAR4),
+ * face-normal gradients at the 2x2 face Gauss points (evaluate_grad,
+ * reconstruction.c:25-34), central flux c^2 (grad_L + grad_R).n/2 (pde.c:12-34),
+ * SSPRK(4,3) with a fixed dt. State: host AoS [k][j][i][2] = (u, v). */
+typedef struct hype_acoustic hype_acoustic;
+
+typedef struct {
+    int nx, ny, nz;
+    double x_min, y_min, z_min, h;
+    double c;   /* wave speed */
+    double dt;  /* fixed time step (hype.c:56: h CFL / (3 c)) */
+    int bc[6];  /* HYPE_BC_PERIODIC or HYPE_BC_ADIABATIC */
+    int recon;  /* HYPE_RECON_LINEAR4 (the reference's setting) or HYPE_RECON_CWENO4 */
+} hype_acoustic_params;
+
+int hype_acoustic_create(const hype_acoustic_params* p, hype_acoustic** out);
+void hype_acoustic_destroy(hype_acoustic* a);
+int hype_acoustic_upload(hype_acoustic* a, const double* U_aos);
+int hype_acoustic_download(hype_acoustic* a, double* U_aos);
+/* Drop-in for its RHSFunction (3d/weno4/plane_wave/rhs_function.c:12-345) */
+int hype_acoustic_rhs(hype_acoustic* a, const double* U_aos, double* RHS_aos);
+/* up to nsteps steps from *t_inout; t_final > 0 shortens the step that would pass it
+ * and stops there (TS_EXACTFINALTIME_MATCHSTEP, hype.c:178) */
+int hype_acoustic_step(hype_acoustic* a, int nsteps, double t_final, double* t_inout, int* steps_taken);
+int hype_acoustic_sync(hype_acoustic* a);
+void* hype_acoustic_stream(hype_acoustic* a);
 
 /* ============================================================ restart and output files */
 /* PETSc binary Vec record (what VecView on a binary viewer writes and VecLoad reads:

@@ -981,3 +981,237 @@ long orc_positivity_fallbacks(int reset) {
     if (reset) g_fallbacks = 0;
     return v;
 }
+
+/* ============================================================ acoustic FV (plane_wave)
+ * RHSFunction            3d/weno4/plane_wave/rhs_function.c:12-345 (adiabatic ghosts
+ *                        :43-131, reconstruction + face gradients :135-214, central
+ *                        fluxes :216-287, RHS :289-300)
+ * weno() with gammaHi=1  3d/weno4/plane_wave/reconstruction.c:38-259 (all R3 weights
+ *                        zero: the coefficients are the R4 ones, bit for bit)
+ * evaluate_grad          3d/weno4/plane_wave/reconstruction.c:25-34
+ * PDEFlux, RiemannSolver 3d/weno4/plane_wave/pde.c:12-34 */
+static void ac_eval_grad(const double* c, double x, double y, double z, double h, double* gx, double* gy, double* gz) {
+    *gx = (c[1] + 2.0 * c[4] * x + c[7] * y + c[9] * z + c[10] * (3.0 * x * x - R3_20) + 2.0 * c[13] * x * y +
+           c[14] * (y * y - R1_12) + 2.0 * c[17] * x * z + c[18] * (z * z - R1_12) + c[19] * y * z) / h;
+    *gy = (c[2] + 2.0 * c[5] * y + c[7] * x + c[8] * z + c[11] * (3.0 * y * y - R3_20) + c[13] * (x * x - R1_12) +
+           2.0 * c[14] * x * y + 2.0 * c[15] * y * z + c[16] * (z * z - R1_12) + c[19] * x * z) / h;
+    *gz = (c[3] + 2.0 * c[6] * z + c[8] * y + c[9] * x + c[12] * (3.0 * z * z - R3_20) + c[15] * (y * y - R1_12) +
+           2.0 * c[16] * y * z + c[17] * (x * x - R1_12) + 2.0 * c[18] * x * z + c[19] * x * y) / h;
+}
+
+typedef struct {
+    const orc_acoustic_cfg* g;
+    int gx, gy;
+    double* pad; /* u with 3 ghost layers */
+} AcPad;
+
+static inline double acp(const AcPad* P, int i, int j, int k) {
+    return P->pad[((size_t)(k + 3) * P->gy + (j + 3)) * P->gx + (i + 3)];
+}
+
+static int ac_map(int i, int n, int blo, int bhi, int* flip) {
+    if (i < 0) {
+        if (blo == 0) return i + n;
+        *flip ^= 1;
+        return -1 - i;
+    }
+    if (i >= n) {
+        if (bhi == 0) return i - n;
+        *flip ^= 1;
+        return 2 * n - 1 - i;
+    }
+    return i;
+}
+
+static void ac_build_pad(AcPad* P, const orc_acoustic_cfg* g, const double* U) {
+    const int nx = g->nx, ny = g->ny, nz = g->nz;
+    P->g = g;
+    P->gx = nx + 6;
+    P->gy = ny + 6;
+#pragma omp parallel for schedule(static) collapse(2)
+    for (int k = -3; k < nz + 3; ++k)
+        for (int j = -3; j < ny + 3; ++j)
+            for (int i = -3; i < nx + 3; ++i) {
+                int f = 0;
+                const int mi = ac_map(i, nx, g->bc[0], g->bc[1], &f);
+                const int mj = ac_map(j, ny, g->bc[2], g->bc[3], &f);
+                const int mk = ac_map(k, nz, g->bc[4], g->bc[5], &f);
+                const double v = U[(((size_t)mk * ny + mj) * nx + mi) * 2];
+                P->pad[((size_t)(k + 3) * P->gy + (j + 3)) * P->gx + (i + 3)] = f ? -v : v;
+            }
+}
+
+/* the 24 normal gradients of one cell: g[face * 4 + q] (faces -x,+x,-y,+y,-z,+z) */
+static void ac_cell_grads(const AcPad* P, int i, int j, int k, double* gn) {
+    const orc_acoustic_cfg* g = P->g;
+    Stencil s;
+    s.c = acp(P, i, j, k);
+    for (int d = 0; d < 3; ++d) {
+        const int ex = d == 0, ey = d == 1, ez = d == 2;
+        s.m2[d] = acp(P, i - 2 * ex, j - 2 * ey, k - 2 * ez);
+        s.m1[d] = acp(P, i - ex, j - ey, k - ez);
+        s.p1[d] = acp(P, i + ex, j + ey, k + ez);
+        s.p2[d] = acp(P, i + 2 * ex, j + 2 * ey, k + 2 * ez);
+    }
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            if (a == b) continue;
+            for (int sa = 0; sa < 2; ++sa)
+                for (int sb = 0; sb < 2; ++sb) {
+                    int off[3] = {0, 0, 0};
+                    off[a] = 2 * sa - 1;
+                    off[b] = 2 * sb - 1;
+                    s.q[a][b][sa][sb] = acp(P, i + off[0], j + off[1], k + off[2]);
+                }
+        }
+    for (int sx = 0; sx < 2; ++sx)
+        for (int sy = 0; sy < 2; ++sy)
+            for (int sz = 0; sz < 2; ++sz) s.o[sx][sy][sz] = acp(P, i + 2 * sx - 1, j + 2 * sy - 1, k + 2 * sz - 1);
+    double coef[20], gx, gy, gz;
+    cweno4(&s, 0.85, g->recon == 1, coef);
+    for (int q = 0; q < 4; ++q) {
+        ac_eval_grad(coef, -0.5, GPX[q], GPY[q], g->h, &gx, &gy, &gz); gn[0 * 4 + q] = gx;
+        ac_eval_grad(coef, 0.5, GPX[q], GPY[q], g->h, &gx, &gy, &gz);  gn[1 * 4 + q] = gx;
+        ac_eval_grad(coef, GPX[q], -0.5, GPY[q], g->h, &gx, &gy, &gz); gn[2 * 4 + q] = gy;
+        ac_eval_grad(coef, GPX[q], 0.5, GPY[q], g->h, &gx, &gy, &gz);  gn[3 * 4 + q] = gy;
+        ac_eval_grad(coef, GPX[q], GPY[q], -0.5, g->h, &gx, &gy, &gz); gn[4 * 4 + q] = gz;
+        ac_eval_grad(coef, GPX[q], GPY[q], 0.5, g->h, &gx, &gy, &gz);  gn[5 * 4 + q] = gz;
+    }
+}
+
+/* sum_q w_q RiemannSolver: 0.5 (FR + FL), F = c^2 (grad . n); the tangential products
+ * of PDEFlux are exact zeros */
+static double ac_face_flux(const double* gL, int fl, const double* gR, int fr, double c) {
+    double flux = 0.0;
+    for (int q = 0; q < 4; ++q) {
+        const double FL = c * c * (gL[fl * 4 + q] * 1.0 + 0.0 + 0.0);
+        const double FR = c * c * (gR[fr * 4 + q] * 1.0 + 0.0 + 0.0);
+        flux += 0.25 * (0.5 * (FR + FL));
+    }
+    return flux;
+}
+
+int orc_acoustic_rhs(const orc_acoustic_cfg* g, const double* U, double* RHS) {
+    const int nx = g->nx, ny = g->ny, nz = g->nz;
+#ifdef _OPENMP
+    if (g->nthreads > 0) omp_set_num_threads(g->nthreads);
+#endif
+    AcPad P;
+    P.pad = (double*)malloc(sizeof(double) * (size_t)(nx + 6) * (ny + 6) * (nz + 6));
+    const int tx = nx + 2, ty = ny + 2, tz = nz + 2;
+    double* GR = (double*)malloc(sizeof(double) * 24 * (size_t)tx * ty * tz);
+    if (!P.pad || !GR) return 3;
+    ac_build_pad(&P, g, U);
+#define ACG(i, j, k) (GR + (((size_t)((k) + 1) * ty + ((j) + 1)) * tx + ((i) + 1)) * 24)
+#pragma omp parallel for schedule(static) collapse(2)
+    for (int k = -1; k <= nz; ++k)
+        for (int j = -1; j <= ny; ++j)
+            for (int i = -1; i <= nx; ++i) {
+                const int gi = (i < 0 || i >= nx), gj = (j < 0 || j >= ny), gk = (k < 0 || k >= nz);
+                if (gi + gj + gk > 1) continue;
+                ac_cell_grads(&P, i, j, k, ACG(i, j, k));
+            }
+    const double r1_h = 1. / g->h;
+#pragma omp parallel for schedule(static) collapse(2)
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const double Fm = ac_face_flux(ACG(i - 1, j, k), 1, ACG(i, j, k), 0, g->c);
+                const double Fp = ac_face_flux(ACG(i, j, k), 1, ACG(i + 1, j, k), 0, g->c);
+                const double Gm = ac_face_flux(ACG(i, j - 1, k), 3, ACG(i, j, k), 2, g->c);
+                const double Gp = ac_face_flux(ACG(i, j, k), 3, ACG(i, j + 1, k), 2, g->c);
+                const double Hm = ac_face_flux(ACG(i, j, k - 1), 5, ACG(i, j, k), 4, g->c);
+                const double Hp = ac_face_flux(ACG(i, j, k), 5, ACG(i, j, k + 1), 4, g->c);
+                const size_t cell = ((size_t)k * ny + j) * nx + i;
+                RHS[cell * 2 + 0] = U[cell * 2 + 1];
+                RHS[cell * 2 + 1] = r1_h * (Fp - Fm) + r1_h * (Gp - Gm) + r1_h * (Hp - Hm);
+            }
+#undef ACG
+    free(P.pad);
+    free(GR);
+    return 0;
+}
+
+int orc_acoustic_run(const orc_acoustic_cfg* g, int nsteps, double dt, double t_final, double* U, double* t_inout,
+                     int* steps_taken) {
+    const size_t n = (size_t)g->nx * g->ny * g->nz * 2;
+    double* W = (double*)malloc(sizeof(double) * n);
+    double* L = (double*)malloc(sizeof(double) * n);
+    if (!W || !L) return 3;
+    double t = *t_inout;
+    int s = 0;
+    for (; s < nsteps; ++s) {
+        if (t_final > 0.0 && t >= t_final) break;
+        double h = dt;
+        if (t_final > 0.0 && t + h > t_final) h = t_final - t;
+        /* SSP RKS3, 4 stages (Ketcheson 2008, low-storage form as PETSc's TSSSP;
+         * the same operation order as orc_euler_run) */
+        const double dtr = h / 2;
+        const double a3 = 1.0 * 2 / (2 * 2 - 1.0), b3 = (2 - 1.0) * h / (2 * (2 * 2 - 1)), c3 = (2 - 1.0) / (2 * 2 - 1);
+        orc_acoustic_rhs(g, U, L);
+        for (size_t q = 0; q < n; ++q) W[q] = U[q] + dtr * L[q];
+        orc_acoustic_rhs(g, W, L);
+        for (size_t q = 0; q < n; ++q) W[q] = W[q] + dtr * L[q];
+        orc_acoustic_rhs(g, W, L);
+        for (size_t q = 0; q < n; ++q) W[q] = a3 * U[q] + b3 * L[q] + c3 * W[q];
+        orc_acoustic_rhs(g, W, L);
+        for (size_t q = 0; q < n; ++q) U[q] = W[q] + dtr * L[q];
+        t += h;
+    }
+    free(W);
+    free(L);
+    *t_inout = t;
+    if (steps_taken) *steps_taken = s;
+    return 0;
+}
+
+static const double AC_XGP5[5] = {0.0000000000000000, -0.2692346550528416, 0.2692346550528416, -0.4530899229693320,
+                                  0.4530899229693320};
+static const double AC_WGP5[5] = {0.28444444444444444, 0.23931433524968326, 0.23931433524968326, 0.11846344252809456,
+                                  0.11846344252809456};
+
+/* cell (i,j,k): the corner x_min + i h of the periodic DMDA's uniform coordinates, and
+ * the reference's quadrature offsets l*h*x_gp5[l] (initialize_solution.c:56-58) */
+static void ac_project(const orc_acoustic_cfg* g, int i, int j, int k, double t, int exact, double* out) {
+    const double h = g->h, pi2 = 2.0 * 3.14159265358979323846;
+    const double xc = (g->xmin + 0.5 * h + i * (pi2 / g->nx)) - 0.5 * h;
+    const double yc = (g->ymin + 0.5 * h + j * (pi2 / g->ny)) - 0.5 * h;
+    const double zc = (g->zmin + 0.5 * h + k * (pi2 / g->nz)) - 0.5 * h;
+    const double omega = 1.0 * sqrt(1.0 * 1.0 + 1.0 * 1.0 + 1.0 * 1.0);
+    double a0 = 0.0, a1 = 0.0;
+    for (int l = 0; l < 5; l++)
+        for (int m = 0; m < 5; m++)
+            for (int n = 0; n < 5; ++n) {
+                const double x = xc + (double)l * h * AC_XGP5[l];
+                const double y = yc + (double)m * h * AC_XGP5[m];
+                const double z = zc + (double)n * h * AC_XGP5[n];
+                const double ph = exact ? 1.0 * x + 1.0 * y + 1.0 * z - omega * t : 1.0 * x + 1.0 * y + 1.0 * z;
+                const double w = AC_WGP5[l] * AC_WGP5[m] * AC_WGP5[n];
+                a0 += w * sin(ph);
+                a1 += w * (-omega * cos(ph));
+            }
+    out[0] = a0;
+    out[1] = a1;
+}
+
+void orc_acoustic_plane_wave_ic(const orc_acoustic_cfg* g, double* U) {
+#pragma omp parallel for schedule(static) collapse(2)
+    for (int k = 0; k < g->nz; ++k)
+        for (int j = 0; j < g->ny; ++j)
+            for (int i = 0; i < g->nx; ++i) ac_project(g, i, j, k, 0.0, 0, U + (((size_t)k * g->ny + j) * g->nx + i) * 2);
+}
+
+void orc_acoustic_plane_wave_errors(const orc_acoustic_cfg* g, const double* U, double t, double* l2, double* linf) {
+    double s2 = 0.0, mx = 0.0;
+    for (int k = 0; k < g->nz; ++k)
+        for (int j = 0; j < g->ny; ++j)
+            for (int i = 0; i < g->nx; ++i) {
+                double e[2];
+                ac_project(g, i, j, k, t, 1, e);
+                const double d = e[0] - U[(((size_t)k * g->ny + j) * g->nx + i) * 2];
+                s2 += d * d;
+                if (fabs(d) > mx) mx = fabs(d);
+            }
+    *l2 = sqrt(s2) * pow(g->h, 1.5);
+    *linf = mx;
+}

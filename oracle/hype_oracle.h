@@ -96,6 +96,27 @@ void orc_mp_prim2cons(int model, const double* eos4, const double* V, double* Q)
 void orc_cweno4_2d(double u0, const double* ux, const double* uy, double upp, double upm, double ump, double umm,
                    double* coeffs);
 
+/* Acoustic FV path of 3d/weno4/plane_wave: state AoS [k][j][i][2] = (u, u_t);
+ * bc[6]: 0 periodic, 4 adiabatic (odd mirror of u); recon: 1 = the R4 polynomial
+ * (the reference's gammaHi = 1), 0 = CWENO4 with gamma 0.85. */
+typedef struct {
+    int nx, ny, nz;
+    double xmin, ymin, zmin, h, c;
+    int bc[6];
+    int recon;
+    int nthreads;
+} orc_acoustic_cfg;
+int orc_acoustic_rhs(const orc_acoustic_cfg* g, const double* U, double* RHS);
+/* SSP RKS3 / 4 stages with fixed dt from *t_inout; t_final > 0: the step that would
+ * pass it is shortened (TS_EXACTFINALTIME_MATCHSTEP) and the run stops there */
+int orc_acoustic_run(const orc_acoustic_cfg* g, int nsteps, double dt, double t_final, double* U, double* t_inout,
+                     int* steps_taken);
+/* the plane wave of 3d/weno4/plane_wave/initial_condition.c (k = (1,1,1)) projected
+ * as initialize_solution.c does, and error_norms.c's L2/Linf of u against the exact
+ * solution at time t, both with the reference's 3D Gauss-point offsets l*h*x_gp5[l] */
+void orc_acoustic_plane_wave_ic(const orc_acoustic_cfg* g, double* U);
+void orc_acoustic_plane_wave_errors(const orc_acoustic_cfg* g, const double* U, double t, double* l2, double* linf);
+
 /* OpenMP threads the restatement runs with */
 int orc_threads(void);
 

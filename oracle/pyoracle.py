@@ -72,6 +72,13 @@ def lib():
             build()
         L = C.CDLL(path)
         L.orc_euler_rhs.argtypes = [C.POINTER(EulerCfg), D, D, D, C.POINTER(C.c_long)]
+        L.orc_acoustic_rhs.argtypes = [C.POINTER(AcousticCfg), D, D]
+        L.orc_acoustic_run.argtypes = [C.POINTER(AcousticCfg), C.c_int, C.c_double, C.c_double, D, D,
+                                       C.POINTER(C.c_int)]
+        L.orc_acoustic_plane_wave_ic.argtypes = [C.POINTER(AcousticCfg), D]
+        L.orc_acoustic_plane_wave_ic.restype = None
+        L.orc_acoustic_plane_wave_errors.argtypes = [C.POINTER(AcousticCfg), D, C.c_double, D, D]
+        L.orc_acoustic_plane_wave_errors.restype = None
         L.orc_euler_run.argtypes = [C.POINTER(EulerCfg), C.c_int, C.c_int, D, D, D, C.POINTER(C.c_long)]
         L.orc_ctcs2d_plane.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, D, D, D]
         L.orc_ctcs_pointsrc.argtypes = [C.POINTER(CtcsCfg), D, C.c_int, D, D, D, D]
@@ -200,6 +207,82 @@ def ref_euler_run(cfg: EulerCfg, U, nsteps, dt_mode=0, dt=0.0):
     rc = run(cfg.nx, cfg.ny, cfg.nz, cfg.xmin, cfg.ymin, cfg.zmin, cfg.h, cfg.cfl, bc, nsteps, dt_mode, _dp(U),
              C.byref(t), C.byref(d))
     return U, t.value, d.value, rc
+
+
+# ---------------------------------------------------------------- acoustic FV (plane_wave)
+class AcousticCfg(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("xmin", C.c_double), ("ymin", C.c_double),
+                ("zmin", C.c_double), ("h", C.c_double), ("c", C.c_double), ("bc", C.c_int * 6), ("recon", C.c_int),
+                ("nthreads", C.c_int)]
+
+
+def acoustic_cfg(n, h, bc=(0,) * 6, recon=1, c=1.0, nthreads=0):
+    nx, ny, nz = (n, n, n) if isinstance(n, int) else n
+    g = AcousticCfg()
+    g.nx, g.ny, g.nz, g.h, g.c = nx, ny, nz, h, c
+    for q in range(6):
+        g.bc[q] = bc[q]
+    g.recon, g.nthreads = recon, nthreads
+    return g
+
+
+def acoustic_rhs(cfg, U):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    lib().orc_acoustic_rhs(C.byref(cfg), _dp(U), _dp(R))
+    return R
+
+
+def acoustic_run(cfg, U, nsteps, dt, t_final=0.0):
+    U = np.array(U, dtype=np.float64, order="C", copy=True)
+    t = C.c_double(0.0)
+    n = C.c_int(0)
+    lib().orc_acoustic_run(C.byref(cfg), int(nsteps), float(dt), float(t_final), _dp(U), C.byref(t), C.byref(n))
+    return U, t.value, n.value
+
+
+def plane_wave_ic(cfg):
+    U = np.zeros((cfg.nz, cfg.ny, cfg.nx, 2))
+    lib().orc_acoustic_plane_wave_ic(C.byref(cfg), _dp(U))
+    return U
+
+
+def plane_wave_errors(cfg, U, t):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    l2, li = C.c_double(), C.c_double()
+    lib().orc_acoustic_plane_wave_errors(C.byref(cfg), _dp(U), float(t), C.byref(l2), C.byref(li))
+    return l2.value, li.value
+
+
+_ref_acoustic = None
+
+
+def _ref_acoustic_lib():
+    global _ref_acoustic
+    if _ref_acoustic is None:
+        L = C.CDLL(os.path.join(HERE, "_ref", "libref_acoustic.so"))
+        IP = C.POINTER(C.c_int)
+        L.ref_acoustic_rhs.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, IP, D, D]
+        L.ref_acoustic_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, IP, C.c_int, C.c_double, C.c_double, D, D]
+        _ref_acoustic = L
+    return _ref_acoustic
+
+
+def ref_acoustic_rhs(cfg, U):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    bc = (C.c_int * 6)(*cfg.bc)
+    _ref_acoustic_lib().ref_acoustic_rhs(cfg.nx, cfg.ny, cfg.nz, cfg.h, bc, _dp(U), _dp(R))
+    return R
+
+
+def ref_acoustic_run(cfg, U, nsteps, dt, t_final=0.0):
+    U = np.array(U, dtype=np.float64, order="C", copy=True)
+    t = C.c_double(0.0)
+    bc = (C.c_int * 6)(*cfg.bc)
+    _ref_acoustic_lib().ref_acoustic_run(cfg.nx, cfg.ny, cfg.nz, cfg.h, bc, int(nsteps), float(dt), float(t_final),
+                                         _dp(U), C.byref(t))
+    return U, t.value
 
 
 def ref_ctcs2d_run(p_old, p, h, c0, dt, zero_bc, nsteps):

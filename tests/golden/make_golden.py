@@ -16,6 +16,9 @@ tree is available; the GPU machine has none, so the fixtures are committed).
 * ref_euler_*_weno3.npz -- the same for the third-order WENO Euler program
                            3d/weno3/Euler (its rhs_function.c, reconstruction.c,
                            pde.c), stepped with its monitor disabled (fixed dt)
+* ref_acoustic_*.npz    -- the acoustic FV RHS of 3d/weno4/plane_wave (R4 face
+                           gradients, central flux) and 3 SSP RKS3 steps of it, under
+                           periodic, adiabatic and mixed walls
 * ref_ctcs2d.npz        -- the reference's CTCS() (2d/ctcs/plane_wave/wave.c)
                            on a zero-exterior grid
 * ref_bubble_*.npz      -- the reference's 2D diffuse-interface RHSFunction
@@ -92,6 +95,14 @@ def main():
         assert rc3 == 0
         np.savez_compressed(os.path.join(HERE, f"ref_euler_{name}_weno3.npz"), U=U, RHS=R, dt=dt, U3=U3, t3=t3,
                             dt3=dt3, bc=np.array(bc), n=n, cfl=0.4, flux=0, recon=3, dt_mode=1)
+    for name, bc, seed in (("periodic", (0,) * 6, 31), ("adiabatic", (4,) * 6, 32), ("mixed", (4, 4, 0, 0, 4, 4), 33)):
+        shape = (7, 6, 5)
+        cfg = O.acoustic_cfg(shape, 0.3, bc=bc)
+        U = np.random.default_rng(seed).standard_normal((shape[2], shape[1], shape[0], 2))
+        R = O.ref_acoustic_rhs(cfg, U)
+        U3, t3 = O.ref_acoustic_run(cfg, U, 3, 0.01)
+        np.savez_compressed(os.path.join(HERE, f"ref_acoustic_{name}.npz"), U=U, RHS=R, U3=U3, t3=t3, dt=0.01, h=0.3,
+                            shape=np.array(shape), bc=np.array(bc))
     n = 32
     x = -1 + np.arange(n) * (2.0 / n)
     Xg, Yg = np.meshgrid(x, x)

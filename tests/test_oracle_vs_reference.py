@@ -112,3 +112,16 @@ def test_point_source_program_reproduces_p_dat(oracle):
 
     with open(os.path.join(GOLDEN, "point_source_p.dat")) as f:
         assert oracle.ref_point_source_trace() == f.read()
+
+
+@pytest.mark.parametrize("bc", [(0,) * 6, (4,) * 6, (4, 0, 0, 0, 0, 4)[0:1] * 2 + (0, 0, 4, 4)])
+def test_acoustic_fv_bitwise(oracle, bc):
+    """the acoustic FV path of 3d/weno4/plane_wave, including TS_EXACTFINALTIME_MATCHSTEP"""
+    _need_ref(oracle)
+    rng = np.random.default_rng(41)
+    cfg = oracle.acoustic_cfg((6, 7, 5), 0.21, bc=bc)
+    U = rng.standard_normal((5, 7, 6, 2))
+    assert np.array_equal(oracle.acoustic_rhs(cfg, U), oracle.ref_acoustic_rhs(cfg, U))
+    a = oracle.acoustic_run(cfg, U, 100, 0.013, t_final=0.05)
+    b = oracle.ref_acoustic_run(cfg, U, 100, 0.013, t_final=0.05)
+    assert np.array_equal(a[0], b[0]) and a[1] == b[1] == 0.05 and a[2] == 4
