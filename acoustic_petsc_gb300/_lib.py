@@ -46,6 +46,7 @@ SYMBOLS = [
     "hype_acoustic_download", "hype_acoustic_rhs", "hype_acoustic_step", "hype_acoustic_sync", "hype_acoustic_stream",
     "hype_euler_set_mlp", "hype_euler_set_recon", "hype_euler_indicator_stats", "hype_euler_sample_features",
     "hype_mlp_nparam", "hype_mlp_score", "hype_mlp_grad", "hype_mlp_train", "hype_euler_shadow_step",
+    "hype_euler_monitor",
 ]
 
 
@@ -63,7 +64,7 @@ class EulerParams(C.Structure):
                 ("x_min", C.c_double), ("y_min", C.c_double), ("z_min", C.c_double), ("h", C.c_double),
                 ("cfl", C.c_double), ("gamma", C.c_double), ("bc", C.c_int * 6),
                 ("recon", C.c_int), ("precision", C.c_int), ("dt_mode", C.c_int), ("flux", C.c_int),
-                ("positivity", C.c_int)]
+                ("positivity", C.c_int), ("mu", C.c_double), ("prandtl", C.c_double), ("cv", C.c_double)]
 
 
 class Mp2dParams(C.Structure):
@@ -142,6 +143,7 @@ def lib():
         "hype_launch_count": ([], C.c_longlong),
         "hype_version": ([], C.c_char_p),
         "hype_euler_stream": ([V], C.c_void_p),
+        "hype_euler_monitor": ([V, D, D], C.c_int),
         "hype_euler_profile": ([V, C.c_int], C.c_int),
         "hype_euler_profile_read": ([V, D, P(C.c_longlong)], C.c_int),
         "hype_set_device": ([C.c_int], C.c_int),

@@ -19,6 +19,8 @@
 
 #include <string.h>
 
+#include <algorithm>
+
 #include <vector>
 
 #include "euler_kernels.cuh"
@@ -58,6 +60,12 @@ struct DevScalars {
     double t;
     unsigned long long bad;  // first inadmissible cell (ULLONG_MAX: none)
     long long rhs_evals;
+    unsigned long long smaxv_bits[6];  // viscous wave speeds, same slots
+};
+
+// viscosity of the Navier-Stokes terms (mu = 0: Euler)
+struct Visc {
+    double mu, pr, cv, r1_h;
 };
 
 __device__ __forceinline__ long long ext_index(const Geo& g, int i, int j, int k) {
@@ -272,7 +280,7 @@ __device__ __forceinline__ void store_first_order_g(const R* __restrict__ G, R* 
 template <typename R>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1)
     k_recon(const R* __restrict__ G, R* __restrict__ T, Geo g, int recon, int pad, double gm1,
-            unsigned long long* __restrict__ counters) {
+            unsigned long long* __restrict__ counters, double* __restrict__ C4 = nullptr) {
     extern __shared__ float ck_dyn[];
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
@@ -292,6 +300,17 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1)
         if (recon == HYPE_RECON_WENO3) weno3<R>(s, cf);
         else cweno4<R>(s, recon == HYPE_RECON_LINEAR4, cf);
         store_traces<R>(T, g, e, c, cf, ckp);
+        if (sizeof(R) == sizeof(double) && C4) {  // the R4 polynomial, whose gradients the viscous fluxes take
+            R r4[20];
+            if (recon == HYPE_RECON_LINEAR4) {
+#pragma unroll
+                for (int q = 0; q < 20; ++q) r4[q] = cf[q];
+            } else {
+                cweno4<R>(s, true, r4);
+            }
+#pragma unroll
+            for (int q = 0; q < 20; ++q) C4[((long long)c * 20 + q) * g.NE + e] = (double)r4[q];
+        }
     }
     if (pad && !(f32 ? ck.ok : traces_admissible<R>(T, g, e, gm1))) {
         store_first_order_g<R>(G, T, g, ge, e);
@@ -434,14 +453,15 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long* a, double v) 
 
 // Face fluxes of direction D.  Face index (i,j,k) is the face on the low side of
 // cell (i,j,k); along D it runs to n (the high face of the last cell).
-template <typename R, int D, int FLUX>
+template <typename R, int D, int FLUX, bool VISC = false>
 __global__ void __launch_bounds__(128) k_faces(const R* __restrict__ T, double* __restrict__ F, Geo g, double gamma,
-                                               DevScalars* __restrict__ ds, int slot) {
+                                               DevScalars* __restrict__ ds, int slot, const double* __restrict__ C4 = nullptr,
+                                               Visc vp = Visc{0.0, 1.0, 2.5, 0.0}) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
     const int fx = g.nx + (D == 0), fy = g.ny + (D == 1);
-    double smax = 0.0;
+    double smax = 0.0, smaxv = 0.0;
     bool bad = false;
     const bool active = (i < fx && j < fy);
     if (active) {
@@ -451,7 +471,8 @@ __global__ void __launch_bounds__(128) k_faces(const R* __restrict__ T, double* 
 #pragma unroll
         for (int c = 0; c < NV; ++c) acc[c] = R(0);
         const R gm = (R)gamma, gm1 = (R)(gamma - 1.0);
-#pragma unroll
+        constexpr int kGpUnroll = VISC ? 1 : 4;  // the viscous body is large enough without unrolling
+#pragma unroll kGpUnroll
         for (int gp = 0; gp < 4; ++gp) {
             R QL[NV], QR[NV], fl[NV];
 #pragma unroll
@@ -461,8 +482,34 @@ __global__ void __launch_bounds__(128) k_faces(const R* __restrict__ T, double* 
             }
             const R s = face_solver<R, D, FLUX>(QL, QR, gm, gm1, fl, bad);
             smax = fmax(smax, (double)s);
+            if constexpr (VISC) {
+                // the gradients of both cells' R4 polynomials at this Gauss point
+                // (evaluate_grad at the face, Navier-Stokes-3D/rhs_function.c:224-270)
+                constexpr double gp5 = GPT;
+                const double t1 = (gp & 2) ? gp5 : -gp5, t2 = (gp & 1) ? gp5 : -gp5;
+                double GL[NV][3], GR[NV][3];
+                const double xl = D == 0 ? 0.5 : t1, yl = D == 1 ? 0.5 : (D == 0 ? t1 : t2), zl = D == 2 ? 0.5 : t2;
+                const double xr = D == 0 ? -0.5 : t1, yr = D == 1 ? -0.5 : (D == 0 ? t1 : t2), zr = D == 2 ? -0.5 : t2;
 #pragma unroll
-            for (int c = 0; c < NV; ++c) acc[c] += R(0.25) * fl[c];
+                for (int c = 0; c < NV; ++c) {
+                    poly_grad_ld(C4 + (long long)c * 20 * g.NE + eL, g.NE, xl, yl, zl, vp.r1_h, GL[c]);
+                    poly_grad_ld(C4 + (long long)c * 20 * g.NE + eR, g.NE, xr, yr, zr, vp.r1_h, GR[c]);
+                }
+                double QLd[NV], QRd[NV], FLv[NV], FRv[NV];
+#pragma unroll
+                for (int c = 0; c < NV; ++c) {
+                    QLd[c] = (double)QL[c];
+                    QRd[c] = (double)QR[c];
+                }
+                const double sl = visc_flux<D>(QLd, GL, gamma, vp.mu, vp.pr, vp.cv, FLv);
+                const double sr = visc_flux<D>(QRd, GR, gamma, vp.mu, vp.pr, vp.cv, FRv);
+                smaxv = fmax(smaxv, fmax(sl, sr));
+#pragma unroll
+                for (int c = 0; c < NV; ++c) acc[c] += R(0.25) * (fl[c] + (R)(0.5 * (FRv[c] + FLv[c])));
+            } else {
+#pragma unroll
+                for (int c = 0; c < NV; ++c) acc[c] += R(0.25) * fl[c];
+            }
         }
         const long long nf = (long long)fx * fy * (g.nz + (D == 2));
         const long long f = ((long long)k * fy + j) * fx + i;
@@ -477,6 +524,11 @@ __global__ void __launch_bounds__(128) k_faces(const R* __restrict__ T, double* 
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, o));
     if ((threadIdx.x & 31) == 0 && smax > 0.0) atomic_max_pos(&ds->smax_bits[slot], smax);
+    if constexpr (VISC) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) smaxv = fmax(smaxv, __shfl_xor_sync(0xffffffffu, smaxv, o));
+        if ((threadIdx.x & 31) == 0 && smaxv > 0.0) atomic_max_pos(&ds->smaxv_bits[slot], smaxv);
+    }
 }
 
 // stage combination: out = a*U + b*W + (c*dt)*L   (L = divergence of the face fluxes)
@@ -518,19 +570,23 @@ __global__ void __launch_bounds__(256) k_update(const double* __restrict__ Fx, c
 // dt from the largest wave speed, rounded as each reference program does:
 // (1/3) (CFL h) / s_max (3d/weno4/Navier-Stokes-3D/rhs_function.c:438-440) or
 // (CFL h) / (3 s_max) (3d/weno3/Euler/rhs_function.c:383)
-__host__ __device__ inline double cfl_dt(double cfl_h, double smax, int recon) {
+// and, with viscosity, (1/3) (CFL h) / (s_max + 2 s_visc / h) (Navier-Stokes-3D/rhs_function.c:438)
+__host__ __device__ inline double cfl_dt(double cfl_h, double smax, int recon, double smaxv = 0.0, double r1_h = 0.0,
+                                         bool visc = false) {
+    if (visc) return (1.0 / 3.0) * cfl_h / (smax + (r1_h * smaxv) * 2.0);
     return recon == HYPE_RECON_WENO3 ? cfl_h / (3.0 * smax) : (1.0 / 3.0) * cfl_h / (smax + 0.0);
 }
 
 // dt of the coming step and the time update (one thread)
 __global__ void k_begin_step(DevScalars* ds, int dt_mode, int src_slot, int use_src, int reset_stages, double cfl_h,
-                             int recon) {
+                             int recon, double r1_h, int visc) {
     if (use_src && dt_mode != HYPE_DT_FIXED) {
         const double smax = __longlong_as_double((long long)ds->smax_bits[src_slot]);
-        ds->dt = cfl_dt(cfl_h, smax, recon);
+        const double smaxv = __longlong_as_double((long long)ds->smaxv_bits[src_slot]);
+        ds->dt = cfl_dt(cfl_h, smax, recon, smaxv, r1_h, visc != 0);
     }
     if (reset_stages)
-        for (int s = 0; s < 4; ++s) ds->smax_bits[s] = 0ull;
+        for (int s = 0; s < 4; ++s) ds->smax_bits[s] = ds->smaxv_bits[s] = 0ull;
     ds->t += ds->dt;
 }
 
@@ -554,6 +610,7 @@ __global__ void k_l1(const double* __restrict__ a, const double* __restrict__ b,
 
 __global__ void k_reset_slot(DevScalars* ds, int slot) {
     ds->smax_bits[slot] = 0ull;
+    ds->smaxv_bits[slot] = 0ull;
     ds->bad = ~0ull;
 }
 
@@ -571,6 +628,98 @@ __global__ void k_soa_to_aos(const double* __restrict__ s, double* __restrict__ 
     const long long cell = q / NV;
     const int c = (int)(q - cell * NV);
     a[q] = s[c * N + cell];
+}
+
+// ---------------------------------------------------------------- monitor diagnostics
+// KineticEnergy (3d/weno4/Navier-Stokes-3D/kinetic_energy.c:11-44): sum of
+// h^3 (|rho u|^2 / 2 rho); Dissipation (dissipation.c:11-67): sum over cells of
+// tau : grad v with central velocity differences and the Stokes stress of viscosity
+// mu.  Neighbours across a non-periodic face are the context's ghost values of the
+// state.  Deterministic: one partial pair per block, then one block sums the
+// partials in a fixed order.
+constexpr int kMonThreads = 256;
+
+__device__ __forceinline__ void block_sum2(double& a, double& b, double* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) {
+        sh[2 * w] = a;
+        sh[2 * w + 1] = b;
+    }
+    __syncthreads();
+    if (w == 0) {
+        a = l < (int)(blockDim.x >> 5) ? sh[2 * l] : 0.0;
+        b = l < (int)(blockDim.x >> 5) ? sh[2 * l + 1] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+        }
+    }
+}
+
+__device__ __forceinline__ void vel_at(const double* __restrict__ U, const Geo& g, int i, int j, int k, double* v) {
+    int fi = 0, fj = 0, fk = 0;
+    const int mi = bmap(i, g.nx, g.bc[0], g.bc[1], &fi);
+    const int mj = bmap(j, g.ny, g.bc[2], g.bc[3], &fj);
+    const int mk = bmap(k, g.nz, g.bc[4], g.bc[5], &fk);
+    const long long q = ((long long)mk * g.ny + mj) * g.nx + mi;
+    const double rho = __ldg(U + q);
+    v[0] = (fi ? -1.0 : 1.0) * __ldg(U + g.N + q) / rho;
+    v[1] = (fj ? -1.0 : 1.0) * __ldg(U + 2 * g.N + q) / rho;
+    v[2] = (fk ? -1.0 : 1.0) * __ldg(U + 3 * g.N + q) / rho;
+}
+
+__global__ void __launch_bounds__(kMonThreads) k_monitor(const double* __restrict__ U, Geo g, double vol, double r1_2h,
+                                                         double mu, double* __restrict__ part) {
+    __shared__ double sh[2 * (kMonThreads / 32)];
+    double ke = 0.0, dr = 0.0;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < g.N; q += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % g.nx), j = (int)((q / g.nx) % g.ny), k = (int)(q / ((long long)g.nx * g.ny));
+        const double rho = __ldg(U + q), mx = __ldg(U + g.N + q), my = __ldg(U + 2 * g.N + q), mz = __ldg(U + 3 * g.N + q);
+        ke += vol * 0.5 * (mx * mx + my * my + mz * mz) / rho;
+        double a[3], b[3], vg[3][3];  // vg[a][b]: d(velocity a)/d(x_b)
+        vel_at(U, g, i + 1, j, k, a);
+        vel_at(U, g, i - 1, j, k, b);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vg[c][0] = r1_2h * (a[c] - b[c]);
+        vel_at(U, g, i, j + 1, k, a);
+        vel_at(U, g, i, j - 1, k, b);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vg[c][1] = r1_2h * (a[c] - b[c]);
+        vel_at(U, g, i, j, k + 1, a);
+        vel_at(U, g, i, j, k - 1, b);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vg[c][2] = r1_2h * (a[c] - b[c]);
+        const double div_v = -(2.0 / 3.0) * mu * (vg[0][0] + vg[1][1] + vg[2][2]);
+        const double txx = div_v + 2.0 * mu * vg[0][0], txy = mu * (vg[0][1] + vg[1][0]), txz = mu * (vg[0][2] + vg[2][0]);
+        const double tyy = div_v + 2.0 * mu * vg[1][1], tyz = mu * (vg[1][2] + vg[2][1]), tzz = div_v + 2.0 * mu * vg[2][2];
+        dr += (txx * vg[0][0] + txy * vg[0][1] + txz * vg[0][2]) + (txy * vg[1][0] + tyy * vg[1][1] + tyz * vg[1][2]) +
+              (txz * vg[2][0] + tyz * vg[2][1] + tzz * vg[2][2]);
+    }
+    block_sum2(ke, dr, sh);
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = ke;
+        part[2 * blockIdx.x + 1] = dr;
+    }
+}
+
+__global__ void __launch_bounds__(kMonThreads) k_monitor_sum(const double* __restrict__ part, int nblk, double* out) {
+    __shared__ double sh[2 * (kMonThreads / 32)];
+    double ke = 0.0, dr = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+        ke += part[2 * b];
+        dr += part[2 * b + 1];
+    }
+    block_sum2(ke, dr, sh);
+    if (threadIdx.x == 0) {
+        out[0] = ke;
+        out[1] = dr;
+    }
 }
 
 }  // namespace euler
@@ -599,6 +748,8 @@ struct hype_euler {
     double* Fz = nullptr;
     double* stage_aos = nullptr;  // device AoS staging
     void* G = nullptr;            // ghosted stage input in the reconstruction's precision
+    double* C4 = nullptr;         // viscous runs: R4 coefficients [5][20][ext cells] for the face gradients
+    double* mon = nullptr;        // monitor partial sums (2 per block) and the result pair
     DevScalars* ds = nullptr;
     DevScalars* hs = nullptr;  // pinned host copy
     double* pin = nullptr;     // pinned host staging for AoS transfers
@@ -632,15 +783,15 @@ static void prof_mark(hype_euler* e, int kind, bool start) {
     }
 }
 
-template <typename R, int FLUX>
+template <typename R, int FLUX, bool VISC = false>
 static void launch_faces_t(const Geo& g, const void* T, double* Fx, double* Fy, double* Fz, double gamma, DevScalars* ds,
-                           int slot, cudaStream_t st) {
+                           int slot, cudaStream_t st, const double* C4 = nullptr, Visc vp = Visc{0.0, 1.0, 2.5, 0.0}) {
     const dim3 bf(32, 4);
     const dim3 gx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4), g.nz), gy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4), g.nz),
         gz(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz + 1);
-    k_faces<R, 0, FLUX><<<gx, bf, 0, st>>>((const R*)T, Fx, g, gamma, ds, slot);
-    k_faces<R, 1, FLUX><<<gy, bf, 0, st>>>((const R*)T, Fy, g, gamma, ds, slot);
-    k_faces<R, 2, FLUX><<<gz, bf, 0, st>>>((const R*)T, Fz, g, gamma, ds, slot);
+    k_faces<R, 0, FLUX, VISC><<<gx, bf, 0, st>>>((const R*)T, Fx, g, gamma, ds, slot, C4, vp);
+    k_faces<R, 1, FLUX, VISC><<<gy, bf, 0, st>>>((const R*)T, Fy, g, gamma, ds, slot, C4, vp);
+    k_faces<R, 2, FLUX, VISC><<<gz, bf, 0, st>>>((const R*)T, Fz, g, gamma, ds, slot, C4, vp);
 }
 
 // the three face-flux launches of one RHS, for the context's precision and flux
@@ -682,11 +833,20 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
                                                         e->mlp_cnt);
     } else {
         k_recon<double><<<gr, br, 0, e->stream>>>((const double*)e->G, (double*)e->T, g, rec, e->p.positivity, gm1,
-                                                  e->mlp_cnt);
+                                                  e->mlp_cnt, e->C4);
     }
     prof_mark(e, 0, false);
     prof_mark(e, 1, true);
-    launch_faces(e->g, e->T, e->Fx, e->Fy, e->Fz, e->p.gamma, e->ds, slot, f32, e->p.flux, e->stream);
+    if (e->C4) {
+        // Navier-Stokes: the inviscid flux plus the average of both sides' viscous fluxes
+        const Visc vp{e->p.mu, e->p.prandtl, e->p.cv, 1.0 / e->p.h};
+        const auto lf = e->p.flux == HYPE_FLUX_HLLC      ? launch_faces_t<double, HYPE_FLUX_HLLC, true>
+                        : e->p.flux == HYPE_FLUX_ROTHLLC ? launch_faces_t<double, HYPE_FLUX_ROTHLLC, true>
+                                                         : launch_faces_t<double, HYPE_FLUX_RUSANOV, true>;
+        lf(e->g, e->T, e->Fx, e->Fy, e->Fz, e->p.gamma, e->ds, slot, e->stream, e->C4, vp);
+    } else {
+        launch_faces(e->g, e->T, e->Fx, e->Fy, e->Fz, e->p.gamma, e->ds, slot, f32, e->p.flux, e->stream);
+    }
     prof_mark(e, 1, false);
     HYPE_LAUNCHED(4);
     return HYPE_OK;
@@ -715,6 +875,11 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
     if (p->dt_mode < HYPE_DT_MONITOR || p->dt_mode > HYPE_DT_FIXED) return HYPE_ERR_ARG;
     if (p->flux < HYPE_FLUX_RUSANOV || p->flux > HYPE_FLUX_ROTHLLC) return HYPE_ERR_ARG;
     if (p->positivity != 0 && p->positivity != 1) return HYPE_ERR_ARG;
+    // viscosity: FP64 only, with the CWENO4 / R4 / WENO3 traces (the gradients always come from R4)
+    const bool visc = p->mu != 0.0;
+    if (visc && (!(p->mu > 0.0) || !(p->prandtl > 0.0) || !(p->cv > 0.0) || p->precision != HYPE_PREC_FP64 ||
+                 p->recon == HYPE_RECON_LEARNED))
+        return HYPE_ERR_ARG;
     hype_euler* e = new hype_euler();
     e->p = *p;
     Geo& g = e->g;
@@ -756,6 +921,7 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
     ALLOC(e->ds, sizeof(DevScalars));
     ALLOC(e->mlp_cnt, 2 * sizeof(unsigned long long));
     ALLOC(e->G, (p->precision == HYPE_PREC_FP32 ? sizeof(float) : sizeof(double)) * NV * (size_t)g.GN);
+    if (visc) ALLOC(e->C4, sizeof(double) * NV * 20 * (size_t)g.NE);
 #undef ALLOC
     ce = cudaMemset(e->mlp_cnt, 0, 2 * sizeof(unsigned long long));
     if (ce != cudaSuccess) {
@@ -784,7 +950,7 @@ extern "C" void hype_euler_destroy(hype_euler* e) {
     if (e->stream) cudaStreamSynchronize(e->stream);
     cudaFree(e->U); cudaFree(e->W); cudaFree(e->L); cudaFree(e->S); cudaFree(e->T);
     cudaFree(e->Fx); cudaFree(e->Fy); cudaFree(e->Fz); cudaFree(e->stage_aos); cudaFree(e->ds); cudaFree(e->G);
-    cudaFree(e->mlp); cudaFree(e->mlp_cnt);
+    cudaFree(e->mlp); cudaFree(e->mlp_cnt); cudaFree(e->C4); cudaFree(e->mon);
     if (e->hs) cudaFreeHost(e->hs);
     for (auto x : e->ev) cudaEventDestroy(x);
     if (e->stream) cudaStreamDestroy(e->stream);
@@ -822,7 +988,8 @@ static int rhs_core(hype_euler* e, const double* dU, double* dRHS, double* dt_ou
     if ((rc = launch_update(e, nullptr, nullptr, dRHS, st))) return rc;
     if ((rc = read_scalars(e))) return rc;
     const double smax = bits_to_double(e->hs->smax_bits[4]);
-    if (dt_out) *dt_out = cfl_dt(e->p.cfl * e->p.h, smax, e->p.recon);
+    const double smaxv = bits_to_double(e->hs->smaxv_bits[4]);
+    if (dt_out) *dt_out = cfl_dt(e->p.cfl * e->p.h, smax, e->p.recon, smaxv, 1.0 / e->p.h, e->C4 != nullptr);
     if (e->hs->bad != ~0ull) return HYPE_ERR_STATE;
     return HYPE_OK;
 }
@@ -898,12 +1065,13 @@ extern "C" int hype_euler_step(hype_euler* e, int nsteps, double* t_inout, doubl
         if (s == 0 && first_from_rhs) {
             // the initial RHS call of hype.c:175 is this step's first stage RHS
             if ((rc = launch_rhs(e, e->U, 0))) return rc;
-            k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 0, 1, 0, cfl_h, e->p.recon);
+            k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 0, 1, 0, cfl_h, e->p.recon, 1.0 / e->p.h, e->C4 != nullptr);
             HYPE_LAUNCHED(1);
         } else {
             // dt: MONITOR refreshes it from the last stage of the previous step
             const int use_src = (mode == HYPE_DT_MONITOR) && s > 0;
-            k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 3, use_src, 1, cfl_h, e->p.recon);
+            k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 3, use_src, 1, cfl_h, e->p.recon, 1.0 / e->p.h,
+                                                 e->C4 != nullptr);
             HYPE_LAUNCHED(1);
             if ((rc = launch_rhs(e, e->U, 0))) return rc;
         }
@@ -919,7 +1087,8 @@ extern "C" int hype_euler_step(hype_euler* e, int nsteps, double* t_inout, doubl
     *t_inout = e->hs->t;
     const double smax3 = bits_to_double(e->hs->smax_bits[3]);
     if (nsteps > 0 && mode == HYPE_DT_MONITOR)
-        *dt_inout = cfl_dt(cfl_h, smax3, e->p.recon);
+        *dt_inout = cfl_dt(cfl_h, smax3, e->p.recon, bits_to_double(e->hs->smaxv_bits[3]), 1.0 / e->p.h,
+                           e->C4 != nullptr);
     else
         *dt_inout = e->hs->dt;
     if (st) {
@@ -931,6 +1100,23 @@ extern "C" int hype_euler_step(hype_euler* e, int nsteps, double* t_inout, doubl
 }
 
 extern "C" void* hype_euler_stream(hype_euler* e) { return e ? (void*)e->stream : nullptr; }
+
+extern "C" int hype_euler_monitor(hype_euler* e, double* ke, double* dissipation) {
+    if (!e || !ke || !dissipation) return HYPE_ERR_ARG;
+    constexpr int kMaxBlocks = 152 * 8;
+    const int nblk = (int)std::min<long long>(kMaxBlocks, (e->g.N + kMonThreads - 1) / kMonThreads);
+    if (!e->mon) HYPE_CK(cudaMalloc((void**)&e->mon, sizeof(double) * (2 * kMaxBlocks + 2)));
+    const double h = e->p.h;
+    k_monitor<<<nblk, kMonThreads, 0, e->stream>>>(e->U, e->g, h * h * h, 0.5 / h, e->p.mu, e->mon);
+    k_monitor_sum<<<1, kMonThreads, 0, e->stream>>>(e->mon, nblk, e->mon + 2 * kMaxBlocks);
+    HYPE_LAUNCHED(2);
+    double r[2];
+    HYPE_CK(cudaMemcpyAsync(r, e->mon + 2 * kMaxBlocks, sizeof(r), cudaMemcpyDeviceToHost, e->stream));
+    HYPE_CK(cudaStreamSynchronize(e->stream));
+    *ke = r[0];
+    *dissipation = r[1];
+    return HYPE_OK;
+}
 
 extern "C" int hype_euler_set_mlp(hype_euler* e, const float* params, float prob_threshold) {
     if (!e || !params || !(prob_threshold > 0.0f) || !(prob_threshold < 1.0f)) return HYPE_ERR_ARG;
@@ -958,6 +1144,7 @@ extern "C" int hype_euler_indicator_stats(hype_euler* e, long long* flagged, lon
 
 extern "C" int hype_euler_set_recon(hype_euler* e, int recon) {
     if (!e || recon < HYPE_RECON_CWENO4 || recon > HYPE_RECON_WENO3) return HYPE_ERR_ARG;
+    if (e->C4 && recon == HYPE_RECON_LEARNED) return HYPE_ERR_ARG;  // the viscous path keeps the R4 coefficients
     HYPE_CK(cudaStreamSynchronize(e->stream));
     e->p.recon = recon;
     return HYPE_OK;
@@ -1060,6 +1247,10 @@ extern "C" int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* 
     if (p->recon != HYPE_RECON_CWENO4 && p->recon != HYPE_RECON_LINEAR4 && p->recon != HYPE_RECON_WENO3) return HYPE_ERR_ARG;
     if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32) return HYPE_ERR_ARG;
     if (p->flux < HYPE_FLUX_RUSANOV || p->flux > HYPE_FLUX_ROTHLLC) return HYPE_ERR_ARG;
+    if (p->mu != 0.0) {
+        set_last_error("hype_euler_rhs_noalloc: the viscous terms need a context (hype_euler_create)", cudaErrorInvalidValue);
+        return HYPE_ERR_UNSUPPORTED;
+    }
     const long long ne = (long long)(p->nx + 2) * (p->ny + 2) * (p->nz + 2);
     if (ne > kNoAllocMaxExt) {
         set_last_error("hype_euler_rhs_noalloc: grid exceeds the fixed scratch ((nx+2)(ny+2)(nz+2) > 5832)",

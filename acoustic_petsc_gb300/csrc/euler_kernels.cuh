@@ -430,6 +430,77 @@ __device__ __forceinline__ R rusanov(const R* QL, const R* QR, R gamma, R gm1, R
     return s;
 }
 
+// ---------------------------------------------------------------- viscous fluxes
+// gradient (times h) of the 20-term polynomial at (x, y, z): evaluate_grad of
+// 3d/weno4/Navier-Stokes-3D/reconstruction.c:24-35 without its final division by h
+__host__ __device__ __forceinline__ void poly_grad(const double* c, double x, double y, double z, double* g) {
+    constexpr double r1_12 = 1. / 12., r3_20 = 3. / 20.;
+    g[0] = c[1] + 2.0 * c[4] * x + c[7] * y + c[9] * z + c[10] * (3.0 * x * x - r3_20) + 2.0 * c[13] * x * y +
+           c[14] * (y * y - r1_12) + 2.0 * c[17] * x * z + c[18] * (z * z - r1_12) + c[19] * y * z;
+    g[1] = c[2] + 2.0 * c[5] * y + c[7] * x + c[8] * z + c[11] * (3.0 * y * y - r3_20) + c[13] * (x * x - r1_12) +
+           2.0 * c[14] * x * y + 2.0 * c[15] * y * z + c[16] * (z * z - r1_12) + c[19] * x * z;
+    g[2] = c[3] + 2.0 * c[6] * z + c[8] * y + c[9] * x + c[12] * (3.0 * z * z - r3_20) + c[15] * (y * y - r1_12) +
+           2.0 * c[16] * y * z + c[17] * (x * x - r1_12) + 2.0 * c[18] * x * z + c[19] * x * y;
+}
+
+// the same from coefficients in global memory (c[q] at p[q * stride]), times 1/h; each
+// coefficient is loaded where it is used, so that the 19 live values of a full
+// coefficient set are never held at once
+__device__ __forceinline__ void poly_grad_ld(const double* __restrict__ p, long long stride, double x, double y, double z,
+                                             double r1_h, double* g) {
+    constexpr double r1_12 = 1. / 12., r3_20 = 3. / 20.;
+    auto C = [&](int q) { return __ldg(p + q * stride); };
+    const double xx = 3.0 * x * x - r3_20, yy = 3.0 * y * y - r3_20, zz = 3.0 * z * z - r3_20;
+    const double x2 = x * x - r1_12, y2 = y * y - r1_12, z2 = z * z - r1_12;
+    double gx = C(1) + 2.0 * C(4) * x + C(7) * y + C(9) * z + C(10) * xx;
+    double gy = C(2) + 2.0 * C(5) * y + C(7) * x + C(8) * z + C(11) * yy;
+    double gz = C(3) + 2.0 * C(6) * z + C(8) * y + C(9) * x + C(12) * zz;
+    const double c13 = C(13), c14 = C(14), c15 = C(15), c16 = C(16), c17 = C(17), c18 = C(18), c19 = C(19);
+    gx += 2.0 * c13 * x * y + c14 * y2 + 2.0 * c17 * x * z + c18 * z2 + c19 * y * z;
+    gy += c13 * x2 + 2.0 * c14 * x * y + 2.0 * c15 * y * z + c16 * z2 + c19 * x * z;
+    gz += c15 * y2 + 2.0 * c16 * y * z + c17 * x2 + 2.0 * c18 * x * z + c19 * x * y;
+    g[0] = gx * r1_h;
+    g[1] = gy * r1_h;
+    g[2] = gz * r1_h;
+}
+
+// PDEViscFlux (3d/weno4/Navier-Stokes-3D/pde.c:90-162) across a face of normal axis D:
+// Newtonian stress with Stokes' hypothesis and Fourier heat flux k = Cv mu gamma / Pr,
+// with the program's velocity gradients u_x = (rho u)_x - u rho_x / rho (:118-130);
+// returns the viscous speed max(4 mu / (3 rho), gamma mu / (Pr rho))
+template <int D>
+__device__ __forceinline__ double visc_flux(const double* Q, const double (*G)[3], double gamma, double mu, double pr,
+                                            double cv, double* F) {
+    const double rho = Q[0], rho2 = Q[0] * Q[0], irho = 1.0 / Q[0];
+    const double u = irho * Q[1], v = irho * Q[2], w = irho * Q[3];
+    const double rhou = Q[1], rhov = Q[2], rhow = Q[3], e = Q[4];
+    const double k = cv * mu * gamma / pr;
+    const double m2 = rhou * rhou + rhov * rhov + rhow * rhow;
+    double vg[3][3], T[3];  // vg[a][b]: d(velocity a)/d(x_b)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+        const double rb = G[0][b];
+        vg[0][b] = G[1][b] - u * rb / rho;
+        vg[1][b] = G[2][b] - v * rb / rho;
+        vg[2][b] = G[3][b] - w * rb / rho;
+        T[b] = (-(gamma - 1.0) * rb / rho2) * (e - 0.5 * m2 / rho) +
+               ((gamma - 1.0) / rho) * (G[4][b] - (rhou * G[1][b] + rhov * G[2][b] + rhow * G[3][b]) / rho +
+                                        0.5 * m2 * rb / rho2);
+    }
+    const double div_v = -(2.0 / 3.0) * mu * (vg[0][0] + vg[1][1] + vg[2][2]);
+    const double tdd = div_v + 2.0 * mu * vg[D][D];                  // tau_DD
+    const double t0 = D == 0 ? tdd : mu * (vg[0][D] + vg[D][0]);     // tau_xD
+    const double t1 = D == 1 ? tdd : mu * (vg[1][D] + vg[D][1]);     // tau_yD
+    const double t2 = D == 2 ? tdd : mu * (vg[2][D] + vg[D][2]);     // tau_zD
+    F[0] = 0.0;
+    F[1] = -t0;
+    F[2] = -t1;
+    F[3] = -t2;
+    F[4] = -(u * t0 + v * t1 + w * t2 - (-k * T[D]));
+    const double a = (4. / 3.) * mu / Q[0], b = gamma * mu / (pr * Q[0]);
+    return a > b ? a : b;
+}
+
 // ---------------------------------------------------------------- HLLC family
 // PDEConsFlux with a general unit normal (Navier-Stokes-3D/pde.c:40-88)
 template <typename R>

@@ -74,6 +74,11 @@ class AppCtx:
     dt_mode: int = L.DT_MONITOR
     flux: int = L.FLUX_RUSANOV
     positivity: int = 0  # 1: first-order fallback on inadmissible face traces
+    # Navier-Stokes constants (3d/weno4/Navier-Stokes-3D/hype.h:38-41: C_V 2.5, PR 1.0, MU_0 0.01);
+    # mu = 0 is the Euler system
+    mu: float = 0.0
+    prandtl: float = 1.0
+    cv: float = 2.5
     dt: float = 0.0  # the reference's Ctx->dt output of RHSFunction
 
     def params(self) -> L.EulerParams:
@@ -85,6 +90,7 @@ class AppCtx:
             p.bc[q] = int(self.boundaries[q])
         p.recon, p.precision, p.dt_mode, p.flux = self.recon, self.precision, self.dt_mode, self.flux
         p.positivity = self.positivity
+        p.mu, p.prandtl, p.cv = self.mu, self.prandtl, self.cv
         return p
 
 
@@ -156,6 +162,14 @@ class EulerSolver:
 
     def device_state_ptr(self) -> int:
         return int(L.lib().hype_euler_state_device(self._h))
+
+    def monitor(self) -> tuple[float, float]:
+        """(KineticEnergy, Dissipation) of the resident state: the two numbers the
+        reference's MonitorFunction writes to ke.csv every 10 steps
+        (3d/weno4/Navier-Stokes-3D/monitor_function.c:77-85)."""
+        ke, dr = C.c_double(), C.c_double()
+        check(L.lib().hype_euler_monitor(self._h, C.byref(ke), C.byref(dr)), "hype_euler_monitor")
+        return ke.value, dr.value
 
     # ---- learned troubled-cell indicator (no counterpart in the reference) ----
     def set_mlp(self, params: np.ndarray, prob_threshold: float = 0.2) -> None:

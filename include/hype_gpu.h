@@ -88,6 +88,14 @@ typedef struct {
                                       3d/weno4/Viscous-Multiphase-Fourth-Order/rhs_function.c:297-305, checked
                                       at the 24 face Gauss-point traces the flux uses; counted in
                                       hype_euler_indicator_stats */
+    /* Navier-Stokes terms (3d/weno4/Navier-Stokes-3D/pde.c:90-162, PDEViscFlux): mu = 0 is the Euler
+     * system; mu > 0 adds at every face Gauss point the average of both sides' viscous fluxes, built
+     * from the gradients of the cells' R4 polynomials, and the viscous speed enters dt as
+     * (1/3) CFL h / (s_max + 2 s_visc / h) (Navier-Stokes-3D/rhs_function.c:438).  FP64 only, not
+     * with HYPE_RECON_LEARNED nor hype_euler_rhs_noalloc. */
+    double mu;      /* dynamic viscosity (MU_0 = 0.01, Navier-Stokes-3D/hype.h:41) */
+    double prandtl; /* Prandtl number (PR = 1.0, hype.h:40); conductivity k = cv mu gamma / prandtl */
+    double cv;      /* specific heat at constant volume (C_V = 2.5, hype.h:38) */
 } hype_euler_params;
 
 typedef struct {
@@ -131,6 +139,14 @@ int hype_euler_sync(hype_euler* e);
 /* The context's CUDA stream (a cudaStream_t), for callers that record their own
  * events or order their own work after the solver's. */
 void* hype_euler_stream(hype_euler* e);
+
+/* The monitor's diagnostics of the resident state (computed on the device, summed in a
+ * fixed order): *ke = KineticEnergy, sum of h^3 |rho u|^2 / (2 rho)
+ * (3d/weno4/Navier-Stokes-3D/kinetic_energy.c:11-44), *dissipation = Dissipation, the sum
+ * of tau : grad v with central velocity differences and viscosity params.mu
+ * (dissipation.c:11-67; neighbours across a non-periodic face are the context's ghost
+ * values of this state). */
+int hype_euler_monitor(hype_euler* e, double* ke, double* dissipation);
 
 /* Per-kernel timing: while enabled, every kernel the context launches is
  * bracketed by CUDA events on its stream; read returns the summed milliseconds

@@ -725,8 +725,16 @@ static void gather(const Padded* P, int i, int j, int k, int c, Stencil* s) {
             for (int sz = 0; sz < 2; ++sz) s->o[sx][sy][sz] = padp(P, i + 2 * sx - 1, j + 2 * sy - 1, k + 2 * sz - 1)[c];
 }
 
-/* traces of one cell: tr[c*NTR + f*4 + g], faces 0..5 = -x,+x,-y,+y,-z,+z */
+/* traces of one cell: tr[c*NTR + f*4 + g], faces 0..5 = -x,+x,-y,+y,-z,+z; with viscosity
+ * followed by the gradients of the R4 polynomial at the same points,
+ * tr[NV*NTR + (c*NTR + f*4 + g)*3 + d] (evaluate_grad, Navier-Stokes-3D/reconstruction.c:24-35).
+ * The Navier-Stokes-3D program itself reconstructs with R4 (recon 1): its weno() has the
+ * whole CWENO combination inside a comment (reconstruction.c:159-308) and copies u_coeffs
+ * into coeffs (:310-312). */
 static void cell_traces_raw(const Padded* P, int i, int j, int k, double gam, int recon, double* tr);
+static void ac_eval_grad(const double* c, double x, double y, double z, double h, double* gx, double* gy, double* gz);
+static int g_visc = 0;          /* set per RHS call: viscous fluxes on */
+static double g_visc_h = 1.0;   /* grid spacing for the gradients */
 
 /* optional first-order fallback (positivity = 1): when a face trace has rho < 1e-14
  * or p < 1e-12 the cell is reconstructed at first order, the rule of
@@ -773,6 +781,19 @@ static void cell_traces_raw(const Padded* P, int i, int j, int k, double gam, in
             continue;
         }
         cweno4(&s, gam, recon == 1, coef);
+        if (g_visc) { /* u_coeffs: the R4 polynomial (Navier-Stokes-3D/reconstruction.c:138-157) */
+            double r4[20];
+            cweno4(&s, gam, 1, r4);
+            double* gr = tr + NV * NTR + (size_t)c * NTR * 3;
+            for (int g = 0; g < 4; ++g) {
+                ac_eval_grad(r4, -0.5, GPX[g], GPY[g], g_visc_h, &gr[(0 * 4 + g) * 3], &gr[(0 * 4 + g) * 3 + 1], &gr[(0 * 4 + g) * 3 + 2]);
+                ac_eval_grad(r4, 0.5, GPX[g], GPY[g], g_visc_h, &gr[(1 * 4 + g) * 3], &gr[(1 * 4 + g) * 3 + 1], &gr[(1 * 4 + g) * 3 + 2]);
+                ac_eval_grad(r4, GPX[g], -0.5, GPY[g], g_visc_h, &gr[(2 * 4 + g) * 3], &gr[(2 * 4 + g) * 3 + 1], &gr[(2 * 4 + g) * 3 + 2]);
+                ac_eval_grad(r4, GPX[g], 0.5, GPY[g], g_visc_h, &gr[(3 * 4 + g) * 3], &gr[(3 * 4 + g) * 3 + 1], &gr[(3 * 4 + g) * 3 + 2]);
+                ac_eval_grad(r4, GPX[g], GPY[g], -0.5, g_visc_h, &gr[(4 * 4 + g) * 3], &gr[(4 * 4 + g) * 3 + 1], &gr[(4 * 4 + g) * 3 + 2]);
+                ac_eval_grad(r4, GPX[g], GPY[g], 0.5, g_visc_h, &gr[(5 * 4 + g) * 3], &gr[(5 * 4 + g) * 3 + 1], &gr[(5 * 4 + g) * 3 + 2]);
+            }
+        }
         for (int g = 0; g < 4; ++g) {
             t[0 * 4 + g] = orc_eval_poly3(-0.5, GPX[g], GPY[g], coef);
             t[1 * 4 + g] = orc_eval_poly3(0.5, GPX[g], GPY[g], coef);
@@ -785,10 +806,76 @@ static void cell_traces_raw(const Padded* P, int i, int j, int k, double gam, in
     (void)GP;
 }
 
+/* PDEViscFlux (Navier-Stokes-3D/pde.c:90-162), operation for operation, including its
+ * velocity gradients u_x = rhou_x - u rho_x / rho (:118-130); returns the viscous speed */
+static double orc_visc_flux(const double* Q, const double G[NV][3], double nx, double ny, double nz, double gamma,
+                            double mu0, double pr, double cv, double* F) {
+    double rho, rho2, irho, u, v, w, p, mu, k, rho_x, rhou_x, rhov_x, rhow_x, e_x, rho_y, rhou_y, rhov_y, rhow_y, e_y, rho_z,
+        rhou_z, rhov_z, rhow_z, e_z, e;
+    double rhou, rhov, rhow;
+    double u_x, u_y, u_z, v_x, v_y, v_z, w_x, w_y, w_z, T_x, T_y, T_z, div_v;
+    double tau_xx, tau_xy, tau_xz, tau_yz, tau_yy, tau_zz, q_x, q_y, q_z;
+    rho = Q[0]; rho2 = Q[0] * Q[0]; irho = 1.0 / Q[0];
+    u = irho * Q[1];
+    v = irho * Q[2];
+    w = irho * Q[3];
+    rhou = Q[1];
+    rhov = Q[2];
+    rhow = Q[3];
+    e = Q[4];
+    p = (gamma - 1.0) * (e - 0.5 * rho * (u * u + v * v + w * w));
+    (void)p;
+    mu = mu0;
+    k = cv * mu * gamma / pr;
+    rho_x = G[0][0]; rho_y = G[0][1]; rho_z = G[0][2];
+    rhou_x = G[1][0]; rhou_y = G[1][1]; rhou_z = G[1][2];
+    rhov_x = G[2][0]; rhov_y = G[2][1]; rhov_z = G[2][2];
+    rhow_x = G[3][0]; rhow_y = G[3][1]; rhow_z = G[3][2];
+    e_x = G[4][0]; e_y = G[4][1]; e_z = G[4][2];
+    u_x = rhou_x - u * rho_x / rho;
+    v_x = rhov_x - v * rho_x / rho;
+    w_x = rhow_x - w * rho_x / rho;
+    T_x = (-(gamma - 1.0) * rho_x / rho2) * (e - 0.5 * (rhou * rhou + rhov * rhov + rhow * rhow) / rho) +
+          ((gamma - 1.0) / rho) * (e_x - (rhou * rhou_x + rhov * rhov_x + rhow * rhow_x) / rho +
+                                   0.5 * (rhou * rhou + rhov * rhov + rhow * rhow) * rho_x / rho2);
+    u_y = rhou_y - u * rho_y / rho;
+    v_y = rhov_y - v * rho_y / rho;
+    w_y = rhow_y - w * rho_y / rho;
+    T_y = (-(gamma - 1.0) * rho_y / rho2) * (e - 0.5 * (rhou * rhou + rhov * rhov + rhow * rhow) / rho) +
+          ((gamma - 1.0) / rho) * (e_y - (rhou * rhou_y + rhov * rhov_y + rhow * rhow_y) / rho +
+                                   0.5 * (rhou * rhou + rhov * rhov + rhow * rhow) * rho_y / rho2);
+    u_z = rhou_z - u * rho_z / rho;
+    v_z = rhov_z - v * rho_z / rho;
+    w_z = rhow_z - w * rho_z / rho;
+    T_z = (-(gamma - 1.0) * rho_z / rho2) * (e - 0.5 * (rhou * rhou + rhov * rhov + rhow * rhow) / rho) +
+          ((gamma - 1.0) / rho) * (e_z - (rhou * rhou_z + rhov * rhov_z + rhow * rhow_z) / rho +
+                                   0.5 * (rhou * rhou + rhov * rhov + rhow * rhow) * rho_z / rho2);
+    div_v = -(2.0 / 3.0) * mu * (u_x + v_y + w_z);
+    tau_xx = div_v + 2.0 * mu * u_x;
+    tau_xy = mu * (u_y + v_x);
+    tau_xz = mu * (u_z + w_x);
+    tau_yy = div_v + 2.0 * mu * v_y;
+    tau_yz = mu * (v_z + w_y);
+    tau_zz = div_v + 2.0 * mu * w_z;
+    q_x = -k * T_x;
+    q_y = -k * T_y;
+    q_z = -k * T_z;
+    F[0] = 0.0;
+    F[1] = -(nx * tau_xx + ny * tau_xy + nz * tau_xz);
+    F[2] = -(nx * tau_xy + ny * tau_yy + nz * tau_yz);
+    F[3] = -(nx * tau_xz + ny * tau_yz + nz * tau_zz);
+    F[4] = -(nx * (u * tau_xx + v * tau_xy + w * tau_xz - q_x) + ny * (u * tau_xy + v * tau_yy + w * tau_yz - q_y) +
+             nz * (u * tau_xz + v * tau_yz + w * tau_zz - q_z));
+    const double a = (4. / 3.) * mu / Q[0], b = gamma * mu / (pr * Q[0]);
+    return a > b ? a : b;
+}
+
 /* face flux from the left cell's trace set (face fl) and the right cell's (face fr) */
 static int g_flux_kind = 0; /* set per RHS call: 0 Rusanov, 1 HLLC, 2 rotated HLLC */
+static double g_mu = 0.0, g_pr = 1.0, g_cv = 2.5;
 
-static inline double face_flux(const double* trL, int fl, const double* trR, int fr, int dir, double gamma, double* F, int* bad) {
+static inline double face_flux(const double* trL, int fl, const double* trR, int fr, int dir, double gamma, double* F, int* bad,
+                               double* smax_visc) {
     double smax = 0.0;
     for (int c = 0; c < NV; ++c) F[c] = 0.0;
     for (int g = 0; g < 4; ++g) {
@@ -806,10 +893,29 @@ static inline double face_flux(const double* trL, int fl, const double* trR, int
                                    : orc_rothllc(QL, QR, nx, ny, nz, gamma, fl5, bad);
         }
         if (s > smax) smax = s;
-        for (int c = 0; c < NV; ++c) F[c] += 0.25 * fl5[c];
+        if (g_visc) { /* PDEViscRiemannSolver (pde.c:386-404) and rhs_function.c:310-316 */
+            const double nx = dir == 0 ? 1.0 : 0.0, ny = dir == 1 ? 1.0 : 0.0, nz = dir == 2 ? 1.0 : 0.0;
+            double GL[NV][3], GR[NV][3], FL[NV], FR[NV], fv[NV];
+            for (int c = 0; c < NV; ++c)
+                for (int d = 0; d < 3; ++d) {
+                    GL[c][d] = trL[NV * NTR + (c * NTR + fl * 4 + g) * 3 + d];
+                    GR[c][d] = trR[NV * NTR + (c * NTR + fr * 4 + g) * 3 + d];
+                }
+            const double sl = orc_visc_flux(QL, GL, nx, ny, nz, gamma, g_mu, g_pr, g_cv, FL);
+            const double sr = orc_visc_flux(QR, GR, nx, ny, nz, gamma, g_mu, g_pr, g_cv, FR);
+            const double sv = sl > sr ? sl : sr;
+            for (int c = 0; c < NV; ++c) fv[c] = 0.5 * (FR[c] + FL[c]);
+            if (sv > *smax_visc) *smax_visc = sv;
+            for (int c = 0; c < NV; ++c) F[c] += 0.25 * (fl5[c] + fv[c]);
+        } else {
+            for (int c = 0; c < NV; ++c) F[c] += 0.25 * fl5[c];
+        }
     }
     return smax;
 }
+
+static double g_last_smax_visc = 0.0;
+double orc_euler_last_smax_visc(void) { return g_last_smax_visc; }
 
 int orc_euler_rhs(const orc_euler_cfg* g, const double* U, double* RHS, double* smax_out, long* bad_out) {
     const int nx = g->nx, ny = g->ny, nz = g->nz;
@@ -818,6 +924,12 @@ int orc_euler_rhs(const orc_euler_cfg* g, const double* U, double* RHS, double* 
     const double r1_h = 1. / (g->h);
     g_flux_kind = g->flux;
     g_positivity = g->positivity;
+    g_visc = g->mu > 0.0;
+    g_visc_h = g->h;
+    g_mu = g->mu;
+    g_pr = g->prandtl;
+    g_cv = g->cv;
+    const size_t REC = (size_t)NV * NTR * (g_visc ? 4 : 1);
 #ifdef _OPENMP
     if (g->nthreads > 0) omp_set_num_threads(g->nthreads);
 #endif
@@ -827,7 +939,7 @@ int orc_euler_rhs(const orc_euler_cfg* g, const double* U, double* RHS, double* 
     build_padded(&P, g, U);
     /* traces for two planes (k-1, k), cells i,j in [-1, n] */
     const int tx = nx + 2, ty = ny + 2;
-    const size_t plane = (size_t)tx * ty * NV * NTR;
+    const size_t plane = (size_t)tx * ty * REC;
     double* T[2];
     T[0] = (double*)malloc(sizeof(double) * plane);
     T[1] = (double*)malloc(sizeof(double) * plane);
@@ -838,9 +950,9 @@ int orc_euler_rhs(const orc_euler_cfg* g, const double* U, double* RHS, double* 
     double* F = (double*)malloc(sizeof(double) * (size_t)(nx + 1) * ny * NV);
     double* G = (double*)malloc(sizeof(double) * (size_t)nx * (ny + 1) * NV);
     if (!T[0] || !T[1] || !H[0] || !H[1] || !F || !G) return 3;
-    double smax = 0.0;
+    double smax = 0.0, smax_v = 0.0;
     long bad = -1;
-#define TR(buf, i, j) ((buf) + ((size_t)((j) + 1) * tx + ((i) + 1)) * NV * NTR)
+#define TR(buf, i, j) ((buf) + ((size_t)((j) + 1) * tx + ((i) + 1)) * REC)
     for (int k = -1; k <= nz; ++k) {
         double* Tk = T[(k + 2) & 1];
         double* Tkm1 = T[(k + 1) & 1];
@@ -859,45 +971,53 @@ int orc_euler_rhs(const orc_euler_cfg* g, const double* U, double* RHS, double* 
         if (k < 0) continue;
         double* Hk = H[k & 1];      /* face k-1/2 */
         double* Hkm1 = H[(k + 1) & 1]; /* face k-3/2 (from the previous plane) */
-        double smax_k = 0.0;
+        double smax_k = 0.0, smaxv_k = 0.0;
         int bad_k = 0;
         /* z faces between plane k-1 and k (for k == nz: the top face of plane nz-1) */
-#pragma omp parallel for schedule(static) reduction(max : smax_k) reduction(| : bad_k)
+#pragma omp parallel for schedule(static) reduction(max : smax_k, smaxv_k) reduction(| : bad_k)
         for (int j = 0; j < ny; ++j)
             for (int i = 0; i < nx; ++i) {
                 int b = 0;
-                double s = face_flux(TR(Tkm1, i, j), 5, TR(Tk, i, j), 4, 2, g->gamma, Hk + ((size_t)j * nx + i) * NV, &b);
+                double sv = 0.0;
+                double s = face_flux(TR(Tkm1, i, j), 5, TR(Tk, i, j), 4, 2, g->gamma, Hk + ((size_t)j * nx + i) * NV, &b, &sv);
                 if (s > smax_k) smax_k = s;
+                if (sv > smaxv_k) smaxv_k = sv;
                 bad_k |= b;
             }
         if (bad_k && bad < 0) bad = (long)k * nx * ny;
         if (smax_k > smax) smax = smax_k;
+        if (smaxv_k > smax_v) smax_v = smaxv_k;
         if (k == 0) continue;
         /* plane kk = k-1 is complete: x and y faces, then the divergence */
         const int kk = k - 1;
         double* Tc = Tkm1;
-        double smax_p = 0.0;
+        double smax_p = 0.0, smaxv_p = 0.0;
         int bad_p = 0;
-#pragma omp parallel for schedule(static) reduction(max : smax_p) reduction(| : bad_p)
+#pragma omp parallel for schedule(static) reduction(max : smax_p, smaxv_p) reduction(| : bad_p)
         for (int j = 0; j < ny; ++j) {
             for (int i = 0; i <= nx; ++i) {
                 int b = 0;
-                double s = face_flux(TR(Tc, i - 1, j), 1, TR(Tc, i, j), 0, 0, g->gamma, F + ((size_t)j * (nx + 1) + i) * NV, &b);
+                double sv = 0.0;
+                double s = face_flux(TR(Tc, i - 1, j), 1, TR(Tc, i, j), 0, 0, g->gamma, F + ((size_t)j * (nx + 1) + i) * NV, &b, &sv);
                 if (s > smax_p) smax_p = s;
+                if (sv > smaxv_p) smaxv_p = sv;
                 bad_p |= b;
             }
         }
-#pragma omp parallel for schedule(static) reduction(max : smax_p) reduction(| : bad_p)
+#pragma omp parallel for schedule(static) reduction(max : smax_p, smaxv_p) reduction(| : bad_p)
         for (int j = 0; j <= ny; ++j) {
             for (int i = 0; i < nx; ++i) {
                 int b = 0;
-                double s = face_flux(TR(Tc, i, j - 1), 3, TR(Tc, i, j), 2, 1, g->gamma, G + ((size_t)j * nx + i) * NV, &b);
+                double sv = 0.0;
+                double s = face_flux(TR(Tc, i, j - 1), 3, TR(Tc, i, j), 2, 1, g->gamma, G + ((size_t)j * nx + i) * NV, &b, &sv);
                 if (s > smax_p) smax_p = s;
+                if (sv > smaxv_p) smaxv_p = sv;
                 bad_p |= b;
             }
         }
         if (bad_p && bad < 0) bad = (long)kk * nx * ny;
         if (smax_p > smax) smax = smax_p;
+        if (smaxv_p > smax_v) smax_v = smaxv_p;
 #pragma omp parallel for schedule(static)
         for (int j = 0; j < ny; ++j)
             for (int i = 0; i < nx; ++i) {
@@ -917,6 +1037,7 @@ int orc_euler_rhs(const orc_euler_cfg* g, const double* U, double* RHS, double* 
     free(T[0]); free(T[1]); free(H[0]); free(H[1]); free(F); free(G);
     if (smax_out) *smax_out = smax;
     if (bad_out) *bad_out = bad;
+    g_last_smax_visc = smax_v;
     return bad >= 0 ? 2 : 0;
 }
 
@@ -924,6 +1045,8 @@ int orc_euler_rhs(const orc_euler_cfg* g, const double* U, double* RHS, double* 
 /* (1/3)(CFL h)/s_max: 3d/weno4/Navier-Stokes-3D/rhs_function.c:438-440;
  * (CFL h)/(3 s_max): 3d/weno3/Euler/rhs_function.c:383 (the WENO3 program) */
 static inline double euler_dt(const orc_euler_cfg* g, double smax) {
+    if (g->mu > 0.0) /* rhs_function.c:438 with the viscous speed of the last RHS call */
+        return (1.0 / 3.0) * (g->cfl * g->h) / (smax + ((1. / g->h) * g_last_smax_visc) * 2.0);
     return g->recon == 3 ? (g->cfl * g->h) / (3.0 * smax) : (1.0 / 3.0) * (g->cfl * g->h) / (smax + 0.0);
 }
 
@@ -940,7 +1063,9 @@ int orc_euler_run(const orc_euler_cfg* g, int nsteps, int dt_mode, double* U, do
     rc = orc_euler_rhs(g, U, F, &smax, bad);
     if (rc) goto out;
     double dt_last = euler_dt(g, smax);
-    dt = (dt_mode == 2) ? *dt_inout : dt_last;
+    /* dt_mode 2: the given dt throughout; dt_mode 3: monitor semantics continued from an
+     * earlier call (its first step takes the dt that call handed back) */
+    dt = (dt_mode == 2 || dt_mode == 3) ? *dt_inout : dt_last;
     for (int s = 0; s < nsteps; ++s) {
         /* stage 1: u1 = u + dt/2 F(u) */
         if (s > 0) rc = orc_euler_rhs(g, U, F, &smax, bad);
@@ -966,7 +1091,7 @@ int orc_euler_run(const orc_euler_cfg* g, int nsteps, int dt_mode, double* U, do
         for (size_t q = 0; q < n; ++q) U[q] = u1[q] + dtr * F[q];
         t += dt;
         dt_last = euler_dt(g, smax);
-        if (dt_mode == 0) dt = dt_last;
+        if (dt_mode == 0 || dt_mode == 3) dt = dt_last;
     }
 out:
     free(u1);
@@ -1214,4 +1339,94 @@ void orc_acoustic_plane_wave_errors(const orc_acoustic_cfg* g, const double* U, 
             }
     *l2 = sqrt(s2) * pow(g->h, 1.5);
     *linf = mx;
+}
+
+/* ============================================================ Taylor-Green vortex (Navier-Stokes-3D)
+ * InitialCondition    3d/weno4/Navier-Stokes-3D/initial_condition.c (rho 1, p 100/gamma,
+ *                     primitive -> conserved by PDEPrim2Cons, pde.c:24-34)
+ * InitializeSolution  initialize_solution.c: 5^3 Gauss sum at the offsets l*h*x_gp5[l]
+ *                     from the cell corner, the corner taken from the periodic DMDA's
+ *                     uniform coordinates (hype.c:114-116)
+ * KineticEnergy       kinetic_energy.c:10-36
+ * Dissipation         dissipation.c:10-70 (central differences of the velocity) */
+static void tgv_cons(double gamma, double x, double y, double z, double* Q) {
+    const double rho_0 = 1.0, p_0 = 100.0 / gamma;
+    double V[5];
+    V[0] = rho_0;
+    V[1] = sin(x) * cos(y) * cos(z);
+    V[2] = -cos(x) * sin(y) * cos(z);
+    V[3] = 0.0;
+    V[4] = p_0 + (rho_0 / 16.0) * (cos(2.0 * z) + 2.0) * (cos(2.0 * x) + cos(2.0 * y) - 2.0);
+    const double e = V[4] / (gamma - 1.0);
+    const double k = 0.5 * V[0] * (V[1] * V[1] + V[2] * V[2] + V[3] * V[3]);
+    Q[0] = V[0];
+    Q[1] = V[0] * V[1];
+    Q[2] = V[0] * V[2];
+    Q[3] = V[0] * V[3];
+    Q[4] = k + e;
+}
+
+void orc_tgv_ic(const orc_euler_cfg* g, double* U) {
+    const double h = g->h;
+    /* DMDASetUniformCoordinates(da, x_min + h/2, x_max + h/2, ...) on periodic axes */
+    const double x0 = g->xmin + 0.5 * h, y0 = g->ymin + 0.5 * h, z0 = g->zmin + 0.5 * h;
+    const double hx = ((g->xmin + g->nx * h + 0.5 * h) - x0) / g->nx;
+    const double hy = ((g->ymin + g->ny * h + 0.5 * h) - y0) / g->ny;
+    const double hz = ((g->zmin + g->nz * h + 0.5 * h) - z0) / g->nz;
+#pragma omp parallel for schedule(static) collapse(2)
+    for (int k = 0; k < g->nz; ++k)
+        for (int j = 0; j < g->ny; ++j)
+            for (int i = 0; i < g->nx; ++i) {
+                const double xc = (x0 + hx * i) - 0.5 * h, yc = (y0 + hy * j) - 0.5 * h, zc = (z0 + hz * k) - 0.5 * h;
+                double integral[5] = {0, 0, 0, 0, 0};
+                for (int l = 0; l < 5; l++)
+                    for (int m = 0; m < 5; m++)
+                        for (int n = 0; n < 5; ++n) {
+                            double Q0[5];
+                            tgv_cons(g->gamma, xc + (double)l * h * AC_XGP5[l], yc + (double)m * h * AC_XGP5[m],
+                                     zc + (double)n * h * AC_XGP5[n], Q0);
+                            for (int c = 0; c < 5; ++c) integral[c] += AC_WGP5[l] * AC_WGP5[m] * AC_WGP5[n] * Q0[c];
+                        }
+                double* u = U + (((size_t)k * g->ny + j) * g->nx + i) * 5;
+                for (int c = 0; c < 5; ++c) u[c] = integral[c];
+            }
+}
+
+double orc_kinetic_energy(const orc_euler_cfg* g, const double* U) {
+    const double h = g->h, vol = h * h * h;
+    double ke = 0.0;
+    for (size_t q = 0; q < (size_t)g->nx * g->ny * g->nz; ++q) {
+        const double* u = U + q * 5;
+        ke += vol * 0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0];
+    }
+    return ke;
+}
+
+double orc_dissipation(const orc_euler_cfg* g, const double* U) {
+    const int nx = g->nx, ny = g->ny, nz = g->nz;
+    const double r1_2h = 0.5 / g->h, mu = g->mu;
+#define TGV_U(i, j, k, c) U[((((size_t)(((k) + nz) % nz) * ny + (((j) + ny) % ny)) * nx + (((i) + nx) % nx)) * 5) + (c)]
+#define VEL(i, j, k, c) (TGV_U(i, j, k, c) / TGV_U(i, j, k, 0))
+    double dr = 0.0;
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const double u_x = r1_2h * (VEL(i + 1, j, k, 1) - VEL(i - 1, j, k, 1));
+                const double u_y = r1_2h * (VEL(i, j + 1, k, 1) - VEL(i, j - 1, k, 1));
+                const double u_z = r1_2h * (VEL(i, j, k + 1, 1) - VEL(i, j, k - 1, 1));
+                const double v_x = r1_2h * (VEL(i + 1, j, k, 2) - VEL(i - 1, j, k, 2));
+                const double v_y = r1_2h * (VEL(i, j + 1, k, 2) - VEL(i, j - 1, k, 2));
+                const double v_z = r1_2h * (VEL(i, j, k + 1, 2) - VEL(i, j, k - 1, 2));
+                const double w_x = r1_2h * (VEL(i + 1, j, k, 3) - VEL(i - 1, j, k, 3));
+                const double w_y = r1_2h * (VEL(i, j + 1, k, 3) - VEL(i, j - 1, k, 3));
+                const double w_z = r1_2h * (VEL(i, j, k + 1, 3) - VEL(i, j, k - 1, 3));
+                const double div_v = -(2.0 / 3.0) * mu * (u_x + v_y + w_z);
+                const double tau_xx = div_v + 2.0 * mu * u_x, tau_xy = mu * (u_y + v_x), tau_xz = mu * (u_z + w_x);
+                const double tau_yy = div_v + 2.0 * mu * v_y, tau_yz = mu * (v_z + w_y), tau_zz = div_v + 2.0 * mu * w_z;
+                dr += (tau_xx * u_x + tau_xy * u_y + tau_xz * u_z) + (tau_xy * v_x + tau_yy * v_y + tau_yz * v_z) +
+                      (tau_xz * w_x + tau_yz * w_y + tau_zz * w_z);
+            }
+#undef VEL
+#undef TGV_U
+    return dr;
 }

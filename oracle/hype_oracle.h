@@ -59,12 +59,22 @@ typedef struct {
     int nthreads;
     int flux;  /* 0 = Rusanov (LLF), 1 = HLLC, 2 = rotated HLLC (Navier-Stokes-3D/pde.c:164-384) */
     int positivity; /* 1: first-order fallback of cells with an inadmissible face trace */
+    double mu, prandtl, cv; /* mu > 0: viscous fluxes of Navier-Stokes-3D/pde.c:90-162,386-404 */
 } orc_euler_cfg;
 long orc_positivity_fallbacks(int reset);
 int orc_euler_rhs(const orc_euler_cfg* cfg, const double* U, double* RHS, double* smax_out, long* bad);
+/* the largest viscous wave speed of the last orc_euler_rhs call (0 without viscosity) */
+double orc_euler_last_smax_visc(void);
+/* Taylor-Green vortex of 3d/weno4/Navier-Stokes-3D/initial_condition.c projected as its
+ * initialize_solution.c does (its 3D Gauss-point offsets), and the diagnostics that its
+ * monitor writes to ke.csv: kinetic_energy.c and dissipation.c */
+void orc_tgv_ic(const orc_euler_cfg* cfg, double* U);
+double orc_kinetic_energy(const orc_euler_cfg* cfg, const double* U);
+double orc_dissipation(const orc_euler_cfg* cfg, const double* U);
 /* SSPRK(4,3) steps with dt semantics: dt_mode 0 -> dt refreshed each step from
  * the last stage RHS (Navier-Stokes-3D monitor), 1 -> frozen at the initial RHS
- * value, 2 -> *dt_inout for every step.  Returns 0 or the RHS error. */
+ * value, 2 -> *dt_inout for every step, 3 -> as 0, continuing an earlier call: the
+ * first step takes *dt_inout (the dt that call handed back).  Returns 0 or the RHS error. */
 int orc_euler_run(const orc_euler_cfg* cfg, int nsteps, int dt_mode, double* U, double* t_inout, double* dt_inout, long* bad);
 
 /* Single-cell CWENO4 coefficients from the 33-point stencil in the reference's

@@ -271,6 +271,7 @@ PetscErrorCode DMDestroy(DM* da) {
     if (!da || !*da) return 0;
     for (int i = 0; i < 8; ++i) VecDestroy(&(*da)->localpool[i]);
     VecDestroy(&(*da)->coords);
+    if ((*da)->cdm) DMDestroy(&(*da)->cdm);
     free(*da);
     *da = NULL;
     return 0;
@@ -394,13 +395,35 @@ PetscErrorCode DMDAVecRestoreArray(DM d, Vec v, void* array) { (void)d; (void)v;
 PetscErrorCode DMDAVecGetArrayRead(DM d, Vec v, void* array) { return DMDAVecGetArray(d, v, array); }
 PetscErrorCode DMDAVecRestoreArrayRead(DM d, Vec v, void* array) { return DMDAVecRestoreArray(d, v, array); }
 
+/* uniform coordinates (PETSc manual, DMDASetUniformCoordinates): node i of an axis is
+ * x0 + i h with h = (x1 - x0)/M on a periodic axis and (x1 - x0)/(M - 1) otherwise,
+ * stored interleaved (dof = dim) in a global vector of a coordinate DMDA */
 PetscErrorCode DMDASetUniformCoordinates(DM d, PetscReal x0, PetscReal x1, PetscReal y0, PetscReal y1, PetscReal z0, PetscReal z1) {
     d->cmin[0] = x0; d->cmax[0] = x1;
     d->cmin[1] = y0; d->cmax[1] = y1;
     d->cmin[2] = z0; d->cmax[2] = z1;
+    if (d->cdm) DMDestroy(&d->cdm);
+    VecDestroy(&d->coords);
+    d->cdm = dm_new(d->dim, d->bx, d->by, d->bz, d->st, d->M, d->N, d->P, d->dim, d->sw);
+    DMCreateGlobalVector(d->cdm, &d->coords);
+    const int n[3] = {d->M, d->N, d->P};
+    const DMBoundaryType b[3] = {d->bx, d->by, d->bz};
+    double h[3];
+    for (int a = 0; a < 3; ++a) {
+        const double L = d->cmax[a] - d->cmin[a];
+        h[a] = (b[a] == DM_BOUNDARY_PERIODIC) ? L / n[a] : (n[a] > 1 ? L / (n[a] - 1) : 0.0);
+    }
+    long q = 0;
+    for (int k = 0; k < (d->dim >= 3 ? d->P : 1); ++k)
+        for (int j = 0; j < (d->dim >= 2 ? d->N : 1); ++j)
+            for (int i = 0; i < d->M; ++i) {
+                d->coords->a[q++] = d->cmin[0] + i * h[0];
+                if (d->dim >= 2) d->coords->a[q++] = d->cmin[1] + j * h[1];
+                if (d->dim >= 3) d->coords->a[q++] = d->cmin[2] + k * h[2];
+            }
     return 0;
 }
-PetscErrorCode DMGetCoordinateDM(DM d, DM* cda) { *cda = d; return 0; }
+PetscErrorCode DMGetCoordinateDM(DM d, DM* cda) { *cda = d->cdm ? d->cdm : d; return 0; }
 PetscErrorCode DMGetCoordinates(DM d, Vec* c) { *c = d->coords; return 0; }
 PetscErrorCode DMGetCoordinatesLocal(DM d, Vec* c) { *c = d->coords; return 0; }
 PetscErrorCode DMDASetFieldName(DM d, PetscInt nf, const char* name) { (void)d; (void)nf; (void)name; return 0; }

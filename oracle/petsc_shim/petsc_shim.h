@@ -123,6 +123,7 @@ struct _p_DM {
     Vec localpool[8];
     int localused[8];
     Vec coords;
+    DM cdm;  /* coordinate DMDA (dof = dim), made by DMDASetUniformCoordinates */
     double cmin[3], cmax[3];
 };
 

@@ -44,7 +44,7 @@ class EulerCfg(C.Structure):
                 ("xmin", C.c_double), ("ymin", C.c_double), ("zmin", C.c_double),
                 ("h", C.c_double), ("cfl", C.c_double), ("gamma", C.c_double),
                 ("bc", C.c_int * 6), ("recon", C.c_int), ("nthreads", C.c_int), ("flux", C.c_int),
-                ("positivity", C.c_int)]
+                ("positivity", C.c_int), ("mu", C.c_double), ("prandtl", C.c_double), ("cv", C.c_double)]
 
 
 class CtcsCfg(C.Structure):
@@ -73,6 +73,14 @@ def lib():
         L = C.CDLL(path)
         L.orc_euler_rhs.argtypes = [C.POINTER(EulerCfg), D, D, D, C.POINTER(C.c_long)]
         L.orc_acoustic_rhs.argtypes = [C.POINTER(AcousticCfg), D, D]
+        L.orc_euler_last_smax_visc.argtypes = []
+        L.orc_euler_last_smax_visc.restype = C.c_double
+        L.orc_tgv_ic.argtypes = [C.POINTER(EulerCfg), D]
+        L.orc_tgv_ic.restype = None
+        L.orc_kinetic_energy.argtypes = [C.POINTER(EulerCfg), D]
+        L.orc_kinetic_energy.restype = C.c_double
+        L.orc_dissipation.argtypes = [C.POINTER(EulerCfg), D]
+        L.orc_dissipation.restype = C.c_double
         L.orc_acoustic_run.argtypes = [C.POINTER(AcousticCfg), C.c_int, C.c_double, C.c_double, D, D,
                                        C.POINTER(C.c_int)]
         L.orc_acoustic_plane_wave_ic.argtypes = [C.POINTER(AcousticCfg), D]
@@ -99,7 +107,8 @@ def threads() -> int:
     return lib().orc_threads()
 
 
-def euler_cfg(n, h, cfl=0.4, gamma=1.4, bc=(0,) * 6, origin=(0.0, 0.0, 0.0), recon=0, nthreads=0, flux=0,
+def euler_cfg(n, h, cfl=0.4, gamma=1.4, bc=(0,) * 6, origin=(0.0, 0.0, 0.0), recon=0, nthreads=0, flux=0, mu=0.0,
+              prandtl=1.0, cv=2.5,
               positivity=0):
     nx, ny, nz = (n, n, n) if isinstance(n, int) else n
     c = EulerCfg()
@@ -109,6 +118,7 @@ def euler_cfg(n, h, cfl=0.4, gamma=1.4, bc=(0,) * 6, origin=(0.0, 0.0, 0.0), rec
     for q in range(6):
         c.bc[q] = bc[q]
     c.recon, c.nthreads, c.flux, c.positivity = recon, nthreads, flux, positivity
+    c.mu, c.prandtl, c.cv = mu, prandtl, cv
     return c
 
 
@@ -120,6 +130,24 @@ def euler_rhs(cfg: EulerCfg, U: np.ndarray):
     bad = C.c_long(-1)
     rc = lib().orc_euler_rhs(C.byref(cfg), _dp(U), _dp(R), C.byref(smax), C.byref(bad))
     return R, smax.value, rc, bad.value
+
+
+def last_smax_visc() -> float:
+    return lib().orc_euler_last_smax_visc()
+
+
+def tgv_ic(cfg: EulerCfg) -> np.ndarray:
+    U = np.zeros((cfg.nz, cfg.ny, cfg.nx, 5))
+    lib().orc_tgv_ic(C.byref(cfg), _dp(U))
+    return U
+
+
+def kinetic_energy(cfg: EulerCfg, U) -> float:
+    return lib().orc_kinetic_energy(C.byref(cfg), _dp(np.ascontiguousarray(U, dtype=np.float64)))
+
+
+def dissipation(cfg: EulerCfg, U) -> float:
+    return lib().orc_dissipation(C.byref(cfg), _dp(np.ascontiguousarray(U, dtype=np.float64)))
 
 
 def euler_run(cfg: EulerCfg, U: np.ndarray, nsteps: int, dt_mode: int = 0, dt: float = 0.0):
@@ -175,6 +203,11 @@ def _ref_euler_fns(cfg):
         if cfg.flux != 0:
             raise ValueError("the WENO3 reference program has the Rusanov flux only")
         key, name, pre = "w3", "libref_euler_w3.so", "ref_euler_w3_"
+    elif cfg.mu > 0.0:
+        if cfg.recon != 1 or cfg.flux != 0 or cfg.mu != 0.01 or cfg.prandtl != 1.0 or cfg.cv != 2.5:
+            raise ValueError("the Navier-Stokes-3D reference program reconstructs with R4, has the Rusanov flux and "
+                             "mu 0.01, Pr 1, Cv 2.5")
+        key, name, pre = "ns3d", "libref_ns3d.so", "ref_ns3d_"
     else:
         key, name, pre = cfg.flux, _REF_FLUX_LIB[cfg.flux], "ref_euler_"
     if key not in _ref_euler_libs:

@@ -21,11 +21,13 @@
  * reconstruction.c:12-177, pde.c:40-106, array.c; set-up of hype.c:96-196) it
  * drives the third-order WENO Euler program instead, which has no viscous terms
  * and no gradient traces; its entry points are then renamed by the Makefile.
+ * Built with -DREF_NS3D it keeps the program's own viscous Riemann solver and its own
+ * reconstruction.c: the whole Navier-Stokes RHS.
  */
 #include "hype.h"
 #include <setjmp.h>
 
-#ifndef REF_WENO3
+#if !defined(REF_WENO3) && !defined(REF_NS3D)
 /* Zero viscous flux: replaces PDEViscRiemannSolver (pde.c:386-404). */
 PetscReal PDEViscRiemannSolver(const Field* QL, PetscReal grad_QL[nVar][DIM], const Field* QR, PetscReal grad_QR[nVar][DIM],
                                const PetscReal nx, const PetscReal ny, const PetscReal nz, Field* Flux) {

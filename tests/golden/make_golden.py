@@ -19,6 +19,14 @@ tree is available; the GPU machine has none, so the fixtures are committed).
 * ref_acoustic_*.npz    -- the acoustic FV RHS of 3d/weno4/plane_wave (R4 face
                            gradients, central flux) and 3 SSP RKS3 steps of it, under
                            periodic, adiabatic and mixed walls
+* ref_ns3d_*.npz        -- the viscous RHS of 3d/weno4/Navier-Stokes-3D as shipped (R4
+                           values and gradients, Rusanov + averaged PDEViscFlux,
+                           mu 0.01, Pr 1, Cv 2.5) and 3 steps of it with the
+                           program's own dt (viscous speed included)
+* ns3d_tgv_ke.csv       -- the reference's checked-in kinetic energy / dissipation
+                           history of its 32^3 Taylor-Green run
+                           (3d/weno4/Navier-Stokes-3D/ke.csv: t, KE, dissipation every
+                           10 steps)
 * ref_ctcs2d.npz        -- the reference's CTCS() (2d/ctcs/plane_wave/wave.c)
                            on a zero-exterior grid
 * ref_bubble_*.npz      -- the reference's 2D diffuse-interface RHSFunction
@@ -58,6 +66,22 @@ def euler_case(n, seed, bc, amp=0.2, sig=0.15, vel=0.05):
 
 CASES = [("periodic", 8, 11, (0, 0, 0, 0, 0, 0)), ("walls", 8, 12, (1, 1, 2, 2, 1, 2)),
          ("mixed", 9, 13, (2, 2, 0, 0, 1, 1))]
+
+
+def ns3d_fixtures():
+    """the Navier-Stokes-3D fixtures (viscous RHS, 3 steps, the Taylor-Green history)"""
+    for name, n, seed, bc in CASES:
+        cfg = O.euler_cfg(n, 1.0 / n, cfl=0.4, bc=bc, recon=1, mu=0.01)
+        U = euler_case(n, seed + 200, bc, vel=0.1)
+        R, dt, rc = O.ref_euler_rhs(cfg, U)
+        assert rc == 0
+        U3, t3, dt3, rc3 = O.ref_euler_run(cfg, U, 3)
+        assert rc3 == 0
+        np.savez_compressed(os.path.join(HERE, f"ref_ns3d_{name}.npz"), U=U, RHS=R, dt=dt, U3=U3, t3=t3, dt3=dt3,
+                            bc=np.array(bc), n=n, cfl=0.4, flux=0, recon=1, mu=0.01, prandtl=1.0, cv=2.5)
+    with open(os.path.join(REF, "3d/weno4/Navier-Stokes-3D/ke.csv")) as f, \
+            open(os.path.join(HERE, "ns3d_tgv_ke.csv"), "w") as g:
+        g.write(f.read())
 
 
 def main():
@@ -103,6 +127,7 @@ def main():
         U3, t3 = O.ref_acoustic_run(cfg, U, 3, 0.01)
         np.savez_compressed(os.path.join(HERE, f"ref_acoustic_{name}.npz"), U=U, RHS=R, U3=U3, t3=t3, dt=0.01, h=0.3,
                             shape=np.array(shape), bc=np.array(bc))
+    ns3d_fixtures()
     n = 32
     x = -1 + np.arange(n) * (2.0 / n)
     Xg, Yg = np.meshgrid(x, x)

@@ -124,3 +124,57 @@ def test_acoustic_fv_reproduces_published_convergence_table():
         l2, linf = O.plane_wave_errors(cfg, U, t)
         assert abs(t - 1.0) < 1e-15
         assert abs(l2 - table[n][0]) <= 2e-3 * table[n][0] and abs(linf - table[n][1]) <= 2e-3 * table[n][1]
+
+
+# ---------------------------------------------------------------- Navier-Stokes-3D
+NS_NAMES = ["periodic", "walls", "mixed"]
+
+
+def _ns_cfg(oracle, z):
+    n = int(z["n"])
+    return oracle.euler_cfg(n, 1.0 / n, cfl=float(z["cfl"]), bc=tuple(int(b) for b in z["bc"]), recon=int(z["recon"]),
+                            mu=float(z["mu"]), prandtl=float(z["prandtl"]), cv=float(z["cv"]))
+
+
+@pytest.mark.parametrize("name", NS_NAMES)
+def test_ns3d_rhs_and_steps_match_reference_bitwise(oracle, name):
+    """the viscous RHS (R4 values and gradients, Rusanov + averaged PDEViscFlux) and its
+    dt (1/3) CFL h / (s_max + 2 s_visc / h) (Navier-Stokes-3D/rhs_function.c:438)"""
+    z = np.load(os.path.join(GOLDEN, f"ref_ns3d_{name}.npz"))
+    cfg = _ns_cfg(oracle, z)
+    R, smax, rc, bad = oracle.euler_rhs(cfg, z["U"])
+    assert rc == 0 and bad == -1
+    assert np.array_equal(R, z["RHS"])
+    sv = oracle.last_smax_visc()
+    assert sv > 0
+    assert (1.0 / 3.0) * (cfg.cfl * cfg.h) / (smax + ((1.0 / cfg.h) * sv) * 2.0) == float(z["dt"])
+    U3, t3, dt3, rc = oracle.euler_run(cfg, z["U"], 3)
+    assert rc == 0
+    assert np.array_equal(U3, z["U3"])
+    assert t3 == float(z["t3"]) and dt3 == float(z["dt3"])
+
+
+def tgv_cfg(oracle, n=32):
+    """the reference's Taylor-Green set-up (Navier-Stokes-3D/hype.c:33-55): [-pi, pi]^3,
+    32^3 cells, CFL 0.6, periodic, R4, Rusanov, mu 0.01"""
+    h = 2.0 * np.pi / n
+    return oracle.euler_cfg(n, h, cfl=0.6, origin=(-np.pi,) * 3, recon=1, mu=0.01)
+
+
+def test_ns3d_taylor_green_reproduces_ke_csv(oracle):
+    """the reference's checked-in history ke.csv (t, KE, dissipation every 10 steps,
+    printed %.8e) from the checker's Taylor-Green start: rows 0-3 to print precision"""
+    ke = np.loadtxt(os.path.join(GOLDEN, "ns3d_tgv_ke.csv"), delimiter=",")
+    cfg = tgv_cfg(oracle)
+    U = oracle.tgv_ic(cfg)
+    assert abs(oracle.kinetic_energy(cfg, U) - ke[0, 1]) <= 1e-8 * ke[0, 1]
+    assert abs(oracle.dissipation(cfg, U) - ke[0, 2]) <= 1e-8 * ke[0, 2]
+    t, dt = 0.0, 0.0
+    for r in range(1, 4):
+        U, dtt, dt, rc = oracle.euler_run(cfg, U, 10, dt_mode=3 if r > 1 else 0, dt=dt)
+        assert rc == 0
+        t += dtt
+        assert abs(t - ke[r, 0]) <= 1e-8 * ke[r, 0]
+        assert abs(oracle.kinetic_energy(cfg, U) - ke[r, 1]) <= 1e-8 * ke[r, 1]
+        assert abs(oracle.dissipation(cfg, U) - ke[r, 2]) <= 1e-8 * ke[r, 2]
+

@@ -125,3 +125,22 @@ def test_acoustic_fv_bitwise(oracle, bc):
     a = oracle.acoustic_run(cfg, U, 100, 0.013, t_final=0.05)
     b = oracle.ref_acoustic_run(cfg, U, 100, 0.013, t_final=0.05)
     assert np.array_equal(a[0], b[0]) and a[1] == b[1] == 0.05 and a[2] == 4
+
+
+@pytest.mark.parametrize("bc", [(0,) * 6, (1, 1, 2, 2, 1, 1), (2, 1, 0, 0, 1, 2)])
+def test_ns3d_rhs_and_run_bitwise(oracle, bc):
+    """the viscous Navier-Stokes-3D program (R4, Rusanov, mu 0.01, Pr 1, Cv 2.5)"""
+    _need_ref(oracle)
+    n = 7
+    cfg = oracle.euler_cfg(n, 1.0 / n, cfl=0.4, bc=bc, recon=1, mu=0.01)
+    U = _state(n, 9)
+    R1, smax, rc, _ = oracle.euler_rhs(cfg, U)
+    R2, dt2, rc2 = oracle.ref_euler_rhs(cfg, U)
+    assert rc == rc2 == 0
+    assert np.array_equal(R1, R2)
+    assert (1.0 / 3.0) * (cfg.cfl * cfg.h) / (smax + ((1.0 / cfg.h) * oracle.last_smax_visc()) * 2.0) == dt2
+    U1, t1, d1, r1 = oracle.euler_run(cfg, U, 2)
+    U2, t2, d2, r2 = oracle.ref_euler_run(cfg, U, 2)
+    assert r1 == r2 == 0
+    assert np.array_equal(U1, U2) and t1 == t2 and d1 == d2
+
