@@ -36,6 +36,24 @@ def euler_pulse(n: int = 256, gamma: float = 1.4, amp: float = 1e-3, sigma: floa
     return U
 
 
+def taylor_green(n: int = 256, gamma: float = 1.4) -> np.ndarray:
+    """The Taylor-Green vortex of 3d/weno4/Navier-Stokes-3D/initial_condition.c:9-31 on
+    [-pi, pi]^3 (rho 1, u = sin x cos y cos z, v = -cos x sin y cos z, w = 0,
+    p = 100/gamma + (cos 2z + 2)(cos 2x + cos 2y - 2)/16) at the cell centres, AoS
+    [k][j][i][5]."""
+    h = 2.0 * math.pi / n
+    x = -math.pi + (np.arange(n) + 0.5) * h
+    sx, cx, c2 = np.sin(x), np.cos(x), np.cos(2.0 * x)
+    U = np.empty((n, n, n, 5))
+    U[..., 0] = 1.0
+    U[..., 1] = sx[None, None, :] * cx[None, :, None] * cx[:, None, None]
+    U[..., 2] = -cx[None, None, :] * sx[None, :, None] * cx[:, None, None]
+    U[..., 3] = 0.0
+    p = 100.0 / gamma + (1.0 / 16.0) * (c2[:, None, None] + 2.0) * (c2[None, None, :] + c2[None, :, None] - 2.0)
+    U[..., 4] = p / (gamma - 1.0) + 0.5 * (U[..., 1] ** 2 + U[..., 2] ** 2)
+    return U
+
+
 def euler_blast(n: int = 512, gamma: float = 1.4, seed: int = 2024, p_ratio: float = 10.0, rho_ratio: float = 8.0,
                 r0: float = 0.1, pert: float = 1e-3) -> np.ndarray:
     """Spherical blast on [0,1]^3 (cell-centre values): inside r < r0 p = 10 p0, rho = 8 rho0;

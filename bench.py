@@ -23,6 +23,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -40,6 +41,9 @@ import numpy as np  # noqa: E402
 # combination -> 4*80 + 40 = 360 B per cell-update, 90 B per cell-stage.
 EULER_BYTES_PER_CELL_STAGE = 90.0
 EULER_BYTES_PER_CELL_UPDATE = 360.0
+# Navier-Stokes: the R4 coefficients (5 x 20 doubles) written by the reconstruction and
+# read back by the face kernels, 1600 B more per cell-stage
+NS_COEF_BYTES_PER_CELL_STAGE = 1600.0
 # CTCS: read p^n, p^{n-1}, write p^{n+1}: 24 B per cell-update
 CTCS_BYTES_PER_CELL_UPDATE = 24.0
 
@@ -205,7 +209,7 @@ FLUX_TAG = {0: "rusanov", 1: "hllc", 2: "rothllc"}
 FLUX_NAME = {0: "Rusanov", 1: "HLLC", 2: "rotated HLLC"}
 
 
-def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0):
+def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscous=False):
     import torch
 
     import acoustic_petsc_gb300 as H
@@ -214,8 +218,13 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0):
     L = H.lib()
     H._lib.check(L.hype_set_device(local), "hype_set_device")
     torch.cuda.set_device(local)
-    U0 = workloads.euler_pulse(n)
-    ctx = H.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, precision=precision, recon=recon, flux=flux)
+    if viscous:  # the Taylor-Green run of 3d/weno4/Navier-Stokes-3D (hype.c:33-55) at n^3
+        U0 = workloads.taylor_green(n)
+        ctx = H.AppCtx(N_x=n, N_y=n, N_z=n, h=2.0 * math.pi / n, x_min=-math.pi, y_min=-math.pi, z_min=-math.pi,
+                       CFL=0.6, precision=precision, recon=recon, flux=flux, mu=0.01, prandtl=1.0, cv=2.5)
+    else:
+        U0 = workloads.euler_pulse(n)
+        ctx = H.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, precision=precision, recon=recon, flux=flux)
     s = H.EulerSolver(ctx)
     s.set_state(U0)
     s.step(max(args.warmup, 3))
@@ -244,9 +253,11 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0):
     # ---- the stage (recon + faces + update) as the dominant unit of work
     stages = max(prof_n[0], 1)
     t_stage = (prof_ms[0] + prof_ms[1] + prof_ms[2]) / stages * 1e-3
-    achieved_gbs = EULER_BYTES_PER_CELL_STAGE * cells / t_stage / 1e9
+    # the viscous path also writes and reads the 100 R4 coefficients of each cell
+    bytes_stage = EULER_BYTES_PER_CELL_STAGE + (NS_COEF_BYTES_PER_CELL_STAGE if viscous else 0.0)
+    achieved_gbs = bytes_stage * cells / t_stage / 1e9
     peak, peak_kind = _peaks()
-    tag = {0: "fp64", 1: "fp32"}[precision] + ("_linear" if recon else "")
+    tag = {0: "fp64", 1: "fp32"}[precision] + ("_linear" if recon else "") + ("_ns" if viscous else "")
     traffic = _profile_figure(f"euler_stage_{tag}.txt", "dram_bytes_per_cell_stage")
     flops_cell = _profile_figure(f"euler_stage_{tag}.txt", "fp_flops_per_cell_stage")
     fpeak = C.c_double()
@@ -254,7 +265,7 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0):
     roof = {"kernel": "RK stage = k_recon + k_faces x3 + k_update (per-stage average)", "bound": "hbm",
             "achieved": achieved_gbs, "peak": peak, "unit": "GB/s", "frac": achieved_gbs / peak,
             "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-            "traffic": traffic * cells if traffic else None, "algorithmic_bytes": EULER_BYTES_PER_CELL_STAGE * cells,
+            "traffic": traffic * cells if traffic else None, "algorithmic_bytes": bytes_stage * cells,
             "per_kernel_ms": {"recon": prof_ms[0] / stages, "faces": prof_ms[1] / stages,
                               "update": prof_ms[2] / stages}}
     alu = None
@@ -293,9 +304,13 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0):
         "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == 0 else "f64 state / f32 recon+flux",
-        "data": "synthetic: Gaussian acoustic pulse dp = 1e-3 exp(-r^2/(2*0.04^2)), 5^3-Gauss cell averages",
-        "config": {"workload": f"euler3d_{RECON_TAG[recon]}_{FLUX_TAG[flux]}_ssprk43_{n}",
-                   "cells": cells, "grid": [n, n, n], "domain": "[0,1]^3 periodic", "cfl": 0.4, "gamma": 1.4,
+        "data": ("synthetic: Taylor-Green vortex of initial_condition.c at the cell centres" if viscous else
+                 "synthetic: Gaussian acoustic pulse dp = 1e-3 exp(-r^2/(2*0.04^2)), 5^3-Gauss cell averages"),
+        "config": {"workload": (f"ns3d_tgv_{RECON_TAG[recon]}_{FLUX_TAG[flux]}_ssprk43_{n}" if viscous else
+                                f"euler3d_{RECON_TAG[recon]}_{FLUX_TAG[flux]}_ssprk43_{n}"),
+                   "cells": cells, "grid": [n, n, n], "domain": "[-pi,pi]^3 periodic" if viscous else "[0,1]^3 periodic",
+                   "cfl": 0.6 if viscous else 0.4, "gamma": 1.4,
+                   "viscosity": {"mu": 0.01, "prandtl": 1.0, "cv": 2.5} if viscous else None,
                    "reconstruction": RECON_NAME[recon], "flux": FLUX_NAME[flux],
                    "time": "SSPRK(4,3) (PETSc TSSSP RKS3, 4 stages), dt from the last stage (monitor semantics)",
                    "parallelism": "replicas" if ws > 1 else "single GPU",
@@ -670,6 +685,7 @@ WORKLOADS = {
     "euler256_linear": lambda a, *r: run_euler(a, *r, precision=0, recon=1),
     "euler256_fp32_linear": lambda a, *r: run_euler(a, *r, precision=1, recon=1),
     "euler256_weno3": lambda a, *r: run_euler(a, *r, precision=0, recon=3),
+    "ns256_tgv": lambda a, *r: run_euler(a, *r, precision=0, recon=1, viscous=True),
     "euler64": lambda a, *r: run_euler(a, *r, precision=0, recon=0, n=64),
     "euler128": lambda a, *r: run_euler(a, *r, precision=0, recon=0, n=128),
     "euler128_fp32": lambda a, *r: run_euler(a, *r, precision=1, recon=0, n=128),
@@ -738,6 +754,21 @@ def main():
             d = time.perf_counter() - t0
             out["cpu_baseline"] = {"value": n * n * 4 / d, "unit": "cell-updates/s", "cores": O.threads(),
                                    "kind": "port", "sample": f"4 SSPRK(4,3) steps of the {n}^2 version ({d:.1f} s)"}
+        elif args.workload.startswith("ns"):
+            from acoustic_petsc_gb300 import workloads
+            from oracle import pyoracle as O
+
+            O.build(None)
+            n = 96
+            cfg = O.euler_cfg(n, 2.0 * math.pi / n, cfl=0.6, origin=(-math.pi,) * 3, recon=1, mu=0.01,
+                              nthreads=os.cpu_count() or 1)
+            U0 = workloads.taylor_green(n)
+            O.euler_run(cfg, U0, 1)
+            t0 = time.perf_counter()
+            O.euler_run(cfg, U0, 2)
+            d = time.perf_counter() - t0
+            out["cpu_baseline"] = {"value": n**3 * 2 / d, "unit": "cell-updates/s", "cores": O.threads(),
+                                   "kind": "port", "sample": f"2 SSPRK(4,3) steps of the {n}^3 Taylor-Green run ({d:.1f} s)"}
         elif args.workload.startswith("euler"):
             n = 160 if args.workload != "euler64" else 48
             r, cores, kind, d = cpu_euler_rate(n, 3, use_ref=False)
