@@ -65,7 +65,7 @@ struct DevScalars {
 
 // viscosity of the Navier-Stokes terms (mu = 0: Euler)
 struct Visc {
-    double mu, pr, cv, r1_h;
+    double mu, kc, vmax, r1_h;  // viscosity, cv mu gamma / Pr, max(4 mu / 3, gamma mu / Pr), 1 / h
 };
 
 __device__ __forceinline__ long long ext_index(const Geo& g, int i, int j, int k) {
@@ -456,7 +456,7 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long* a, double v) 
 template <typename R, int D, int FLUX, bool VISC = false>
 __global__ void __launch_bounds__(128) k_faces(const R* __restrict__ T, double* __restrict__ F, Geo g, double gamma,
                                                DevScalars* __restrict__ ds, int slot, const double* __restrict__ C4 = nullptr,
-                                               Visc vp = Visc{0.0, 1.0, 2.5, 0.0}) {
+                                               Visc vp = Visc{0.0, 0.0, 0.0, 0.0}) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
@@ -501,8 +501,8 @@ __global__ void __launch_bounds__(128) k_faces(const R* __restrict__ T, double* 
                     QLd[c] = (double)QL[c];
                     QRd[c] = (double)QR[c];
                 }
-                const double sl = visc_flux<D>(QLd, GL, gamma, vp.mu, vp.pr, vp.cv, FLv);
-                const double sr = visc_flux<D>(QRd, GR, gamma, vp.mu, vp.pr, vp.cv, FRv);
+                const double sl = visc_flux<D>(QLd, GL, gamma - 1.0, vp.mu, vp.kc, vp.vmax, FLv);
+                const double sr = visc_flux<D>(QRd, GR, gamma - 1.0, vp.mu, vp.kc, vp.vmax, FRv);
                 smaxv = fmax(smaxv, fmax(sl, sr));
 #pragma unroll
                 for (int c = 0; c < NV; ++c) acc[c] += R(0.25) * (fl[c] + (R)(0.5 * (FRv[c] + FLv[c])));
@@ -785,7 +785,7 @@ static void prof_mark(hype_euler* e, int kind, bool start) {
 
 template <typename R, int FLUX, bool VISC = false>
 static void launch_faces_t(const Geo& g, const void* T, double* Fx, double* Fy, double* Fz, double gamma, DevScalars* ds,
-                           int slot, cudaStream_t st, const double* C4 = nullptr, Visc vp = Visc{0.0, 1.0, 2.5, 0.0}) {
+                           int slot, cudaStream_t st, const double* C4 = nullptr, Visc vp = Visc{0.0, 0.0, 0.0, 0.0}) {
     const dim3 bf(32, 4);
     const dim3 gx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4), g.nz), gy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4), g.nz),
         gz(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz + 1);
@@ -839,7 +839,8 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
     prof_mark(e, 1, true);
     if (e->C4) {
         // Navier-Stokes: the inviscid flux plus the average of both sides' viscous fluxes
-        const Visc vp{e->p.mu, e->p.prandtl, e->p.cv, 1.0 / e->p.h};
+        const double mu = e->p.mu, g = e->p.gamma;
+        const Visc vp{mu, e->p.cv * mu * g / e->p.prandtl, std::max((4. / 3.) * mu, g * mu / e->p.prandtl), 1.0 / e->p.h};
         const auto lf = e->p.flux == HYPE_FLUX_HLLC      ? launch_faces_t<double, HYPE_FLUX_HLLC, true>
                         : e->p.flux == HYPE_FLUX_ROTHLLC ? launch_faces_t<double, HYPE_FLUX_ROTHLLC, true>
                                                          : launch_faces_t<double, HYPE_FLUX_RUSANOV, true>;

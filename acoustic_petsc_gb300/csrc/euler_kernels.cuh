@@ -469,23 +469,24 @@ __device__ __forceinline__ void poly_grad_ld(const double* __restrict__ p, long 
 // with the program's velocity gradients u_x = (rho u)_x - u rho_x / rho (:118-130);
 // returns the viscous speed max(4 mu / (3 rho), gamma mu / (Pr rho))
 template <int D>
-__device__ __forceinline__ double visc_flux(const double* Q, const double (*G)[3], double gamma, double mu, double pr,
-                                            double cv, double* F) {
-    const double rho = Q[0], rho2 = Q[0] * Q[0], irho = 1.0 / Q[0];
+__device__ __forceinline__ double visc_flux(const double* Q, const double (*G)[3], double gm1, double mu, double kc,
+                                            double vmax, double* F) {
+    // kc = cv mu gamma / Pr (heat conductivity), vmax = max(4 mu / 3, gamma mu / Pr); the
+    // divisions by rho of the reference's expressions are products with 1/rho here
+    const double irho = 1.0 / Q[0], irho2 = irho * irho;
     const double u = irho * Q[1], v = irho * Q[2], w = irho * Q[3];
     const double rhou = Q[1], rhov = Q[2], rhow = Q[3], e = Q[4];
-    const double k = cv * mu * gamma / pr;
     const double m2 = rhou * rhou + rhov * rhov + rhow * rhow;
     double vg[3][3], T[3];  // vg[a][b]: d(velocity a)/d(x_b)
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
-        const double rb = G[0][b];
-        vg[0][b] = G[1][b] - u * rb / rho;
-        vg[1][b] = G[2][b] - v * rb / rho;
-        vg[2][b] = G[3][b] - w * rb / rho;
-        T[b] = (-(gamma - 1.0) * rb / rho2) * (e - 0.5 * m2 / rho) +
-               ((gamma - 1.0) / rho) * (G[4][b] - (rhou * G[1][b] + rhov * G[2][b] + rhow * G[3][b]) / rho +
-                                        0.5 * m2 * rb / rho2);
+        const double rb = G[0][b] * irho;
+        vg[0][b] = G[1][b] - u * rb;
+        vg[1][b] = G[2][b] - v * rb;
+        vg[2][b] = G[3][b] - w * rb;
+        T[b] = (-gm1 * rb * irho) * (e - 0.5 * m2 * irho) +
+               (gm1 * irho) * (G[4][b] - (rhou * G[1][b] + rhov * G[2][b] + rhow * G[3][b]) * irho +
+                               0.5 * m2 * rb * irho);
     }
     const double div_v = -(2.0 / 3.0) * mu * (vg[0][0] + vg[1][1] + vg[2][2]);
     const double tdd = div_v + 2.0 * mu * vg[D][D];                  // tau_DD
@@ -496,9 +497,8 @@ __device__ __forceinline__ double visc_flux(const double* Q, const double (*G)[3
     F[1] = -t0;
     F[2] = -t1;
     F[3] = -t2;
-    F[4] = -(u * t0 + v * t1 + w * t2 - (-k * T[D]));
-    const double a = (4. / 3.) * mu / Q[0], b = gamma * mu / (pr * Q[0]);
-    return a > b ? a : b;
+    F[4] = -(u * t0 + v * t1 + w * t2 + kc * T[D]);
+    return vmax * irho;
 }
 
 // ---------------------------------------------------------------- HLLC family

@@ -218,6 +218,7 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
     L = H.lib()
     H._lib.check(L.hype_set_device(local), "hype_set_device")
     torch.cuda.set_device(local)
+    n = args.grid or n
     if viscous:  # the Taylor-Green run of 3d/weno4/Navier-Stokes-3D (hype.c:33-55) at n^3
         U0 = workloads.taylor_green(n)
         ctx = H.AppCtx(N_x=n, N_y=n, N_z=n, h=2.0 * math.pi / n, x_min=-math.pi, y_min=-math.pi, z_min=-math.pi,
@@ -314,7 +315,7 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
                    "reconstruction": RECON_NAME[recon], "flux": FLUX_NAME[flux],
                    "time": "SSPRK(4,3) (PETSc TSSSP RKS3, 4 stages), dt from the last stage (monitor semantics)",
                    "parallelism": "replicas" if ws > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (state 5*8*256^3 B = 671 MB > 129 MB); no flush"},
+                   "l2": f"inputs larger than L2 (state 5*8*{n}^3 B = {5 * 8 * n**3 / 1e6:.0f} MB vs 129 MB); no flush"},
         "roofline": roof, "gpu_launches": launches, "clocks": clocks, "e2e": e2e,
     }
     if alu:
@@ -730,6 +731,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="euler256", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", type=int, default=0,
+                    help="cells per axis of the 3D Euler / Navier-Stokes workloads (default 256; smaller for profiling)")
     args = ap.parse_args()
     ws, rank, local = _dist()
     if args.impl == "reference":
