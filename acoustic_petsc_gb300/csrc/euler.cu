@@ -20,6 +20,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include <vector>
 
@@ -280,7 +281,7 @@ __device__ __forceinline__ void store_first_order_g(const R* __restrict__ G, R* 
 template <typename R>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1)
     k_recon(const R* __restrict__ G, R* __restrict__ T, Geo g, int recon, int pad, double gm1,
-            unsigned long long* __restrict__ counters, double* __restrict__ C4 = nullptr) {
+            unsigned long long* __restrict__ counters, double* __restrict__ C4 = nullptr, double c4_scale = 1.0) {
     extern __shared__ float ck_dyn[];
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
@@ -309,7 +310,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1)
                 cweno4<R>(s, true, r4);
             }
 #pragma unroll
-            for (int q = 0; q < 20; ++q) C4[((long long)c * 20 + q) * g.NE + e] = (double)r4[q];
+            for (int q = 0; q < 20; ++q) C4[((long long)c * 20 + q) * g.NE + e] = (double)r4[q] * c4_scale;
         }
     }
     if (pad && !(f32 ? ck.ok : traces_admissible<R>(T, g, e, gm1))) {
@@ -451,6 +452,42 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long* a, double v) 
     atomicMax(a, (unsigned long long)__double_as_longlong(v));
 }
 
+// The viscous fluxes of one face side at its 4 Gauss points, 0.125 F_v each, added to
+// av: NS = +1 for the low cell's high face, -1 for the high cell's low face.  The
+// traces come from T, the gradients from the cell's R4 coefficients (stored times 1/h).
+template <int D, int NS>
+__device__ __forceinline__ double visc_side(const double* __restrict__ T, const double* __restrict__ C4, const Geo& g,
+                                            long long e, double gamma, const Visc& vp, double* av) {
+    FaceGrad fg[NV][3];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        const double* p = C4 + (long long)c * 20 * g.NE + e;
+        fg[c][0] = face_grad<D, NS, 0>(p, g.NE);
+        fg[c][1] = face_grad<D, NS, 1>(p, g.NE);
+        fg[c][2] = face_grad<D, NS, 2>(p, g.NE);
+    }
+    constexpr int face = 2 * D + (NS > 0 ? 1 : 0);
+    double sv = 0.0;
+    auto at = [&](auto gpc) {
+        constexpr int gp = decltype(gpc)::value;
+        double Q[NV], G[NV][3], Fv[NV];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            Q[c] = __ldg(T + ((long long)c * NTR + face * 4 + gp) * g.NE + e);
+#pragma unroll
+            for (int b = 0; b < 3; ++b) G[c][b] = fg_eval<gp>(fg[c][b]);
+        }
+        sv = fmax(sv, visc_flux<D>(Q, G, gamma - 1.0, vp.mu, vp.kc, vp.vmax, Fv));
+#pragma unroll
+        for (int c = 0; c < NV; ++c) av[c] = fma(0.125, Fv[c], av[c]);
+    };
+    at(std::integral_constant<int, 0>{});
+    at(std::integral_constant<int, 1>{});
+    at(std::integral_constant<int, 2>{});
+    at(std::integral_constant<int, 3>{});
+    return sv;
+}
+
 // Face fluxes of direction D.  Face index (i,j,k) is the face on the low side of
 // cell (i,j,k); along D it runs to n (the high face of the last cell).
 template <typename R, int D, int FLUX, bool VISC = false>
@@ -471,8 +508,7 @@ __global__ void __launch_bounds__(128) k_faces(const R* __restrict__ T, double* 
 #pragma unroll
         for (int c = 0; c < NV; ++c) acc[c] = R(0);
         const R gm = (R)gamma, gm1 = (R)(gamma - 1.0);
-        constexpr int kGpUnroll = VISC ? 1 : 4;  // the viscous body is large enough without unrolling
-#pragma unroll kGpUnroll
+#pragma unroll
         for (int gp = 0; gp < 4; ++gp) {
             R QL[NV], QR[NV], fl[NV];
 #pragma unroll
@@ -482,34 +518,19 @@ __global__ void __launch_bounds__(128) k_faces(const R* __restrict__ T, double* 
             }
             const R s = face_solver<R, D, FLUX>(QL, QR, gm, gm1, fl, bad);
             smax = fmax(smax, (double)s);
-            if constexpr (VISC) {
-                // the gradients of both cells' R4 polynomials at this Gauss point
-                // (evaluate_grad at the face, Navier-Stokes-3D/rhs_function.c:224-270)
-                constexpr double gp5 = GPT;
-                const double t1 = (gp & 2) ? gp5 : -gp5, t2 = (gp & 1) ? gp5 : -gp5;
-                double GL[NV][3], GR[NV][3];
-                const double xl = D == 0 ? 0.5 : t1, yl = D == 1 ? 0.5 : (D == 0 ? t1 : t2), zl = D == 2 ? 0.5 : t2;
-                const double xr = D == 0 ? -0.5 : t1, yr = D == 1 ? -0.5 : (D == 0 ? t1 : t2), zr = D == 2 ? -0.5 : t2;
 #pragma unroll
-                for (int c = 0; c < NV; ++c) {
-                    poly_grad_ld(C4 + (long long)c * 20 * g.NE + eL, g.NE, xl, yl, zl, vp.r1_h, GL[c]);
-                    poly_grad_ld(C4 + (long long)c * 20 * g.NE + eR, g.NE, xr, yr, zr, vp.r1_h, GR[c]);
-                }
-                double QLd[NV], QRd[NV], FLv[NV], FRv[NV];
+            for (int c = 0; c < NV; ++c) acc[c] += R(0.25) * fl[c];
+        }
+        if constexpr (VISC) {
+            // PDEViscRiemannSolver (Navier-Stokes-3D/pde.c:386-404): 0.5 (F_v(L) + F_v(R)) at
+            // each Gauss point, weight 0.25, added to the inviscid flux (rhs_function.c:310-316)
+            double av[NV];
 #pragma unroll
-                for (int c = 0; c < NV; ++c) {
-                    QLd[c] = (double)QL[c];
-                    QRd[c] = (double)QR[c];
-                }
-                const double sl = visc_flux<D>(QLd, GL, gamma - 1.0, vp.mu, vp.kc, vp.vmax, FLv);
-                const double sr = visc_flux<D>(QRd, GR, gamma - 1.0, vp.mu, vp.kc, vp.vmax, FRv);
-                smaxv = fmax(smaxv, fmax(sl, sr));
+            for (int c = 0; c < NV; ++c) av[c] = 0.0;
+            smaxv = visc_side<D, 1>((const double*)T, C4, g, eL, gamma, vp, av);
+            smaxv = fmax(smaxv, visc_side<D, -1>((const double*)T, C4, g, eR, gamma, vp, av));
 #pragma unroll
-                for (int c = 0; c < NV; ++c) acc[c] += R(0.25) * (fl[c] + (R)(0.5 * (FRv[c] + FLv[c])));
-            } else {
-#pragma unroll
-                for (int c = 0; c < NV; ++c) acc[c] += R(0.25) * fl[c];
-            }
+            for (int c = 0; c < NV; ++c) acc[c] += (R)av[c];
         }
         const long long nf = (long long)fx * fy * (g.nz + (D == 2));
         const long long f = ((long long)k * fy + j) * fx + i;
@@ -833,7 +854,7 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
                                                         e->mlp_cnt);
     } else {
         k_recon<double><<<gr, br, 0, e->stream>>>((const double*)e->G, (double*)e->T, g, rec, e->p.positivity, gm1,
-                                                  e->mlp_cnt, e->C4);
+                                                  e->mlp_cnt, e->C4, 1.0 / e->p.h);
     }
     prof_mark(e, 0, false);
     prof_mark(e, 1, true);

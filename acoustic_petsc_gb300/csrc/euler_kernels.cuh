@@ -431,37 +431,91 @@ __device__ __forceinline__ R rusanov(const R* QL, const R* QR, R gamma, R gm1, R
 }
 
 // ---------------------------------------------------------------- viscous fluxes
-// gradient (times h) of the 20-term polynomial at (x, y, z): evaluate_grad of
-// 3d/weno4/Navier-Stokes-3D/reconstruction.c:24-35 without its final division by h
-__host__ __device__ __forceinline__ void poly_grad(const double* c, double x, double y, double z, double* g) {
-    constexpr double r1_12 = 1. / 12., r3_20 = 3. / 20.;
-    g[0] = c[1] + 2.0 * c[4] * x + c[7] * y + c[9] * z + c[10] * (3.0 * x * x - r3_20) + 2.0 * c[13] * x * y +
-           c[14] * (y * y - r1_12) + 2.0 * c[17] * x * z + c[18] * (z * z - r1_12) + c[19] * y * z;
-    g[1] = c[2] + 2.0 * c[5] * y + c[7] * x + c[8] * z + c[11] * (3.0 * y * y - r3_20) + c[13] * (x * x - r1_12) +
-           2.0 * c[14] * x * y + 2.0 * c[15] * y * z + c[16] * (z * z - r1_12) + c[19] * x * z;
-    g[2] = c[3] + 2.0 * c[6] * z + c[8] * y + c[9] * x + c[12] * (3.0 * z * z - r3_20) + c[15] * (y * y - r1_12) +
-           2.0 * c[16] * y * z + c[17] * (x * x - r1_12) + 2.0 * c[18] * x * z + c[19] * x * y;
+// The gradient of a cell's R4 polynomial on one of its faces (normal axis D, side
+// NS = +1 for the high face x_D = +1/2, -1 for the low face) is, in the two
+// tangential coordinates, g(t1, t2) = P + Q t1 + R t2 + S t1 t2 once the squares
+// t1^2 = t2^2 = GPT^2 of the 2x2 Gauss points are folded into P (the gradient of
+// evaluate_grad, Navier-Stokes-3D/reconstruction.c:24-35, at the face points of
+// rhs_function.c:224-270).  Built once per face side from the coefficients, it costs
+// 3 FMAs per Gauss point.  The tangential axes are the two other axes in increasing
+// order, as for the traces.
+struct FaceGrad {
+    double p, q, r, s;
+};
+
+// adds c k x^EX y^EY z^EZ to f
+template <int D, int NS, int EX, int EY, int EZ>
+__device__ __forceinline__ void fg_term(FaceGrad& f, double c, double k) {
+    constexpr int eD = D == 0 ? EX : (D == 1 ? EY : EZ);
+    constexpr int e1 = D == 0 ? EY : EX, e2 = D == 2 ? EY : EZ;
+    constexpr double n = 0.5 * NS;
+    constexpr double nf = eD == 0 ? 1.0 : (eD == 1 ? n : n * n);
+    if constexpr (e1 == 2 || e2 == 2) f.p = fma(c, k * (nf * G2), f.p);
+    else if constexpr (e1 == 0 && e2 == 0) f.p = fma(c, k * nf, f.p);
+    else if constexpr (e1 == 1 && e2 == 0) f.q = fma(c, k * nf, f.q);
+    else if constexpr (e1 == 0 && e2 == 1) f.r = fma(c, k * nf, f.r);
+    else f.s = fma(c, k * nf, f.s);
 }
 
-// the same from coefficients in global memory (c[q] at p[q * stride]), times 1/h; each
-// coefficient is loaded where it is used, so that the 19 live values of a full
-// coefficient set are never held at once
-__device__ __forceinline__ void poly_grad_ld(const double* __restrict__ p, long long stride, double x, double y, double z,
-                                             double r1_h, double* g) {
-    constexpr double r1_12 = 1. / 12., r3_20 = 3. / 20.;
-    auto C = [&](int q) { return __ldg(p + q * stride); };
-    const double xx = 3.0 * x * x - r3_20, yy = 3.0 * y * y - r3_20, zz = 3.0 * z * z - r3_20;
-    const double x2 = x * x - r1_12, y2 = y * y - r1_12, z2 = z * z - r1_12;
-    double gx = C(1) + 2.0 * C(4) * x + C(7) * y + C(9) * z + C(10) * xx;
-    double gy = C(2) + 2.0 * C(5) * y + C(7) * x + C(8) * z + C(11) * yy;
-    double gz = C(3) + 2.0 * C(6) * z + C(8) * y + C(9) * x + C(12) * zz;
-    const double c13 = C(13), c14 = C(14), c15 = C(15), c16 = C(16), c17 = C(17), c18 = C(18), c19 = C(19);
-    gx += 2.0 * c13 * x * y + c14 * y2 + 2.0 * c17 * x * z + c18 * z2 + c19 * y * z;
-    gy += c13 * x2 + 2.0 * c14 * x * y + 2.0 * c15 * y * z + c16 * z2 + c19 * x * z;
-    gz += c15 * y2 + 2.0 * c16 * y * z + c17 * x2 + 2.0 * c18 * x * z + c19 * x * y;
-    g[0] = gx * r1_h;
-    g[1] = gy * r1_h;
-    g[2] = gz * r1_h;
+// component B of the gradient of the 20-term polynomial whose coefficient q is at p[q * st]
+template <int D, int NS, int B>
+__device__ __forceinline__ FaceGrad face_grad(const double* __restrict__ p, long long st) {
+    auto C = [&](int q) { return __ldg(p + q * st); };
+    FaceGrad f{0.0, 0.0, 0.0, 0.0};
+    if constexpr (B == 0) {  // d/dx
+        fg_term<D, NS, 0, 0, 0>(f, C(1), 1.0);
+        fg_term<D, NS, 1, 0, 0>(f, C(4), 2.0);
+        fg_term<D, NS, 0, 1, 0>(f, C(7), 1.0);
+        fg_term<D, NS, 0, 0, 1>(f, C(9), 1.0);
+        const double c10 = C(10), c14 = C(14), c18 = C(18);
+        fg_term<D, NS, 2, 0, 0>(f, c10, 3.0);
+        fg_term<D, NS, 0, 0, 0>(f, c10, -R3_20);
+        fg_term<D, NS, 1, 1, 0>(f, C(13), 2.0);
+        fg_term<D, NS, 0, 2, 0>(f, c14, 1.0);
+        fg_term<D, NS, 0, 0, 0>(f, c14, -R1_12);
+        fg_term<D, NS, 1, 0, 1>(f, C(17), 2.0);
+        fg_term<D, NS, 0, 0, 2>(f, c18, 1.0);
+        fg_term<D, NS, 0, 0, 0>(f, c18, -R1_12);
+        fg_term<D, NS, 0, 1, 1>(f, C(19), 1.0);
+    } else if constexpr (B == 1) {  // d/dy
+        fg_term<D, NS, 0, 0, 0>(f, C(2), 1.0);
+        fg_term<D, NS, 0, 1, 0>(f, C(5), 2.0);
+        fg_term<D, NS, 1, 0, 0>(f, C(7), 1.0);
+        fg_term<D, NS, 0, 0, 1>(f, C(8), 1.0);
+        const double c11 = C(11), c13 = C(13), c16 = C(16);
+        fg_term<D, NS, 0, 2, 0>(f, c11, 3.0);
+        fg_term<D, NS, 0, 0, 0>(f, c11, -R3_20);
+        fg_term<D, NS, 2, 0, 0>(f, c13, 1.0);
+        fg_term<D, NS, 0, 0, 0>(f, c13, -R1_12);
+        fg_term<D, NS, 1, 1, 0>(f, C(14), 2.0);
+        fg_term<D, NS, 0, 1, 1>(f, C(15), 2.0);
+        fg_term<D, NS, 0, 0, 2>(f, c16, 1.0);
+        fg_term<D, NS, 0, 0, 0>(f, c16, -R1_12);
+        fg_term<D, NS, 1, 0, 1>(f, C(19), 1.0);
+    } else {  // d/dz
+        fg_term<D, NS, 0, 0, 0>(f, C(3), 1.0);
+        fg_term<D, NS, 0, 0, 1>(f, C(6), 2.0);
+        fg_term<D, NS, 0, 1, 0>(f, C(8), 1.0);
+        fg_term<D, NS, 1, 0, 0>(f, C(9), 1.0);
+        const double c12 = C(12), c15 = C(15), c17 = C(17);
+        fg_term<D, NS, 0, 0, 2>(f, c12, 3.0);
+        fg_term<D, NS, 0, 0, 0>(f, c12, -R3_20);
+        fg_term<D, NS, 0, 2, 0>(f, c15, 1.0);
+        fg_term<D, NS, 0, 0, 0>(f, c15, -R1_12);
+        fg_term<D, NS, 0, 1, 1>(f, C(16), 2.0);
+        fg_term<D, NS, 2, 0, 0>(f, c17, 1.0);
+        fg_term<D, NS, 0, 0, 0>(f, c17, -R1_12);
+        fg_term<D, NS, 1, 0, 1>(f, C(18), 2.0);
+        fg_term<D, NS, 1, 1, 0>(f, C(19), 1.0);
+    }
+    return f;
+}
+
+// the value at Gauss point gp (t1 = -/+GPT for gp & 2, t2 = -/+GPT for gp & 1)
+template <int GP>
+__device__ __forceinline__ double fg_eval(const FaceGrad& f) {
+    constexpr double s1 = (GP & 2) ? GPT : -GPT, s2 = (GP & 1) ? GPT : -GPT;
+    return fma(f.s, s1 * s2, fma(f.r, s2, fma(f.q, s1, f.p)));
 }
 
 // PDEViscFlux (3d/weno4/Navier-Stokes-3D/pde.c:90-162) across a face of normal axis D:
