@@ -259,8 +259,9 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
     achieved_gbs = bytes_stage * cells / t_stage / 1e9
     peak, peak_kind = _peaks()
     tag = {0: "fp64", 1: "fp32"}[precision] + ("_linear" if recon else "") + ("_ns" if viscous else "")
-    traffic = _profile_figure(f"euler_stage_{tag}.txt", "dram_bytes_per_cell_stage")
-    flops_cell = _profile_figure(f"euler_stage_{tag}.txt", "fp_flops_per_cell_stage")
+    prof_file = "ns3d_tgv_stage_fp64.txt" if viscous else f"euler_stage_{tag}.txt"
+    traffic = _profile_figure(prof_file, "dram_bytes_per_cell_stage")
+    flops_cell = _profile_figure(prof_file, "fp_flops_per_cell_stage")
     fpeak = C.c_double()
     H._lib.check(L.hype_probe_fma_peak(precision, C.byref(fpeak)), "probe")
     roof = {"kernel": "RK stage = k_recon + k_faces x3 + k_update (per-stage average)", "bound": "hbm",
