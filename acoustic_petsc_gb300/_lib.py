@@ -46,7 +46,9 @@ SYMBOLS = [
     "hype_acoustic_download", "hype_acoustic_rhs", "hype_acoustic_step", "hype_acoustic_sync", "hype_acoustic_stream",
     "hype_euler_set_mlp", "hype_euler_set_recon", "hype_euler_indicator_stats", "hype_euler_sample_features",
     "hype_mlp_nparam", "hype_mlp_score", "hype_mlp_grad", "hype_mlp_train", "hype_euler_shadow_step",
-    "hype_euler_monitor",
+    "hype_euler_monitor", "hype_acoustic2d_create", "hype_acoustic2d_destroy", "hype_acoustic2d_upload",
+    "hype_acoustic2d_download", "hype_acoustic2d_rhs", "hype_acoustic2d_step", "hype_acoustic2d_sync",
+    "hype_acoustic2d_stream",
 ]
 
 
@@ -82,6 +84,11 @@ class AcousticParams(C.Structure):
 
 class Status(C.Structure):
     _fields_ = [("bad_cell", C.c_longlong), ("smax", C.c_double), ("rhs_evals", C.c_longlong)]
+
+
+class Acoustic2dParams(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("x_min", C.c_double), ("y_min", C.c_double), ("h", C.c_double),
+                ("c", C.c_double), ("dt", C.c_double), ("bc", C.c_int * 4), ("stepper", C.c_int)]
 
 
 class CtcsParams(C.Structure):
@@ -183,6 +190,14 @@ def lib():
         "hype_acoustic_step": ([V, C.c_int, C.c_double, D, I], C.c_int),
         "hype_acoustic_sync": ([V], C.c_int),
         "hype_acoustic_stream": ([V], C.c_void_p),
+        "hype_acoustic2d_create": ([P(Acoustic2dParams), P(V)], C.c_int),
+        "hype_acoustic2d_destroy": ([V], None),
+        "hype_acoustic2d_upload": ([V, D], C.c_int),
+        "hype_acoustic2d_download": ([V, D], C.c_int),
+        "hype_acoustic2d_rhs": ([V, D, D], C.c_int),
+        "hype_acoustic2d_step": ([V, C.c_int, C.c_double, D, I], C.c_int),
+        "hype_acoustic2d_sync": ([V], C.c_int),
+        "hype_acoustic2d_stream": ([V], C.c_void_p),
         "hype_euler_set_mlp": ([V, F, C.c_float], C.c_int),
         "hype_euler_set_recon": ([V, C.c_int], C.c_int),
         "hype_euler_indicator_stats": ([V, P(C.c_longlong), P(C.c_longlong), C.c_int], C.c_int),

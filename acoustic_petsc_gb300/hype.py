@@ -495,3 +495,63 @@ class AcousticFV3D:
               "hype_acoustic_step")
         self.t = t.value
         return n.value
+
+
+
+class AcousticFV2D:
+    """The 2D acoustic finite-volume program of 2d/weno4/standing_wave: (u, v = u_t) with
+    the 2D R4 polynomial's edge-normal gradients, the averaged flux and SSP RK104 (the
+    program's) or RKS3/4 stages with a fixed dt; bit-identical to the reference."""
+
+    def __init__(self, N_x, N_y, h, dt, c=1.0, x_min=0.0, y_min=0.0, boundaries=(L.BC_ADIABATIC,) * 4,
+                 stepper=L.STEP_SSPRK104):
+        p = L.Acoustic2dParams()
+        p.nx, p.ny, p.x_min, p.y_min, p.h, p.c, p.dt = N_x, N_y, x_min, y_min, h, c, dt
+        for q in range(4):
+            p.bc[q] = int(boundaries[q])
+        p.stepper = stepper
+        self.shape = (N_y, N_x, 2)
+        self.t = 0.0
+        self._h = C.c_void_p()
+        check(L.lib().hype_acoustic2d_create(C.byref(p), C.byref(self._h)), "hype_acoustic2d_create")
+
+    def close(self):
+        if self._h:
+            L.lib().hype_acoustic2d_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def RHSFunction(self, t, U, RHS=None):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        if U.shape != self.shape:
+            raise ValueError(f"U must have shape {self.shape}")
+        if RHS is None:
+            RHS = np.empty_like(U)
+        check(L.lib().hype_acoustic2d_rhs(self._h, _dp(U), _dp(RHS)), "RHSFunction")
+        return RHS
+
+    def set_state(self, U):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        if U.shape != self.shape:
+            raise ValueError(f"U must have shape {self.shape}")
+        check(L.lib().hype_acoustic2d_upload(self._h, _dp(U)), "hype_acoustic2d_upload")
+
+    def get_state(self):
+        U = np.empty(self.shape)
+        check(L.lib().hype_acoustic2d_download(self._h, _dp(U)), "hype_acoustic2d_download")
+        return U
+
+    def step(self, nsteps, t_final=0.0):
+        """up to nsteps steps; t_final > 0 ends the run exactly on t_final
+        (TS_EXACTFINALTIME_MATCHSTEP). Returns the steps taken."""
+        t = C.c_double(self.t)
+        n = C.c_int(0)
+        check(L.lib().hype_acoustic2d_step(self._h, int(nsteps), float(t_final), C.byref(t), C.byref(n)),
+              "hype_acoustic2d_step")
+        self.t = t.value
+        return n.value

@@ -283,6 +283,34 @@ int hype_acoustic_step(hype_acoustic* a, int nsteps, double t_final, double* t_i
 int hype_acoustic_sync(hype_acoustic* a);
 void* hype_acoustic_stream(hype_acoustic* a);
 
+/* ---- 2D acoustic FV: 2d/weno4/standing_wave ----
+ * The same system in 2D: state AoS [j][i][2] = (u, u_t); the 2D R4 polynomial of u
+ * (weno(), reconstruction.c:108-125), its normal gradient at 2 Gauss points per edge,
+ * the averaged flux c^2 grad u . n (pde.c:12-34), RK104 (hype.c:211) or RKS3/4 stages.
+ * Results equal the reference program's bit for bit. */
+typedef struct hype_acoustic2d hype_acoustic2d;
+
+typedef struct {
+    int nx, ny;
+    double x_min, y_min, h;
+    double c;    /* wave speed (wave_speed, hype.h:38) */
+    double dt;   /* fixed time step (hype.c:50: h CFL / (2 c)) */
+    int bc[4];   /* HYPE_BC_PERIODIC or HYPE_BC_ADIABATIC: left, right, bottom, top */
+    int stepper; /* HYPE_STEP_SSPRK104 (the program's) or HYPE_STEP_SSPRK43 */
+} hype_acoustic2d_params;
+
+int hype_acoustic2d_create(const hype_acoustic2d_params* p, hype_acoustic2d** out);
+void hype_acoustic2d_destroy(hype_acoustic2d* a);
+int hype_acoustic2d_upload(hype_acoustic2d* a, const double* U_aos);
+int hype_acoustic2d_download(hype_acoustic2d* a, double* U_aos);
+/* Drop-in for its RHSFunction (2d/weno4/standing_wave/rhs_function.c:12-258) */
+int hype_acoustic2d_rhs(hype_acoustic2d* a, const double* U_aos, double* RHS_aos);
+/* up to nsteps steps from *t_inout; t_final > 0 shortens the step that would pass it
+ * and stops there (TS_EXACTFINALTIME_MATCHSTEP, hype.c:208) */
+int hype_acoustic2d_step(hype_acoustic2d* a, int nsteps, double t_final, double* t_inout, int* steps_taken);
+int hype_acoustic2d_sync(hype_acoustic2d* a);
+void* hype_acoustic2d_stream(hype_acoustic2d* a);
+
 /* ============================================================ restart and output files */
 /* PETSc binary Vec record (what VecView on a binary viewer writes and VecLoad reads:
  * int32 class id 1211214, int32 length, big-endian doubles; the reference's restart1.bin /

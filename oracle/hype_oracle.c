@@ -1430,3 +1430,245 @@ double orc_dissipation(const orc_euler_cfg* g, const double* U) {
 #undef TGV_U
     return dr;
 }
+
+
+/* ============================================================ 2D acoustic FV (standing_wave)
+ * RHSFunction              2d/weno4/standing_wave/rhs_function.c:12-258 (adiabatic ghosts
+ *                          :46-95, reconstruction + face gradients :97-150, fluxes
+ *                          :152-205, RHS :207-216)
+ * weno()                   2d/weno4/standing_wave/reconstruction.c:108-125 (the R4 polynomial)
+ * basis_grad tables        reconstruction.c:50-100, filled as hype.c:137-166 fills them
+ * PDEFlux, LLFRiemannSolver pde.c:12-34
+ * SSP RK104                PETSc TSSSP RK104 (Ketcheson 2008), restated in oracle/petsc_shim
+ * InitializeSolution, ErrorNorms  initialize_solution.c:10-68, post_process.c:80-152 */
+static void sw_basis_grad(double x, double y, int n, double* gx, double* gy) {
+    switch (n) {
+        case 1: *gx = 1.0; *gy = 0.0; break;
+        case 2: *gx = 0.0; *gy = 1.0; break;
+        case 3: *gx = 2.0 * x; *gy = 0.0; break;
+        case 4: *gx = 0.0; *gy = 2.0 * y; break;
+        case 5: *gx = y; *gy = x; break;
+        case 6: *gx = 3.0 * x * x - 3. / 20.; *gy = 0.0; break;
+        case 7: *gx = 0.0; *gy = 3.0 * y * y - 3. / 20.; break;
+        case 8: *gx = 2.0 * x * y; *gy = (x * x - 1. / 12.); break;
+        case 9: *gx = (y * y - 1. / 12.); *gy = 2.0 * x * y; break;
+        default: *gx = 0.0; *gy = 0.0;
+    }
+}
+
+static const double SW_GP2[2] = {-0.28867513459481287, 0.28867513459481287};
+
+/* phi[f][q][k][d]: the basis gradients at Gauss point q of edge f (left, right, bottom, top) */
+static void sw_tables(double phi[4][2][10][2]) {
+    for (int q = 0; q < 2; ++q)
+        for (int k = 0; k < 10; ++k) {
+            sw_basis_grad(-0.5, SW_GP2[q], k, &phi[0][q][k][0], &phi[0][q][k][1]);
+            sw_basis_grad(0.5, SW_GP2[q], k, &phi[1][q][k][0], &phi[1][q][k][1]);
+            sw_basis_grad(SW_GP2[q], -0.5, k, &phi[2][q][k][0], &phi[2][q][k][1]);
+            sw_basis_grad(SW_GP2[q], 0.5, k, &phi[3][q][k][0], &phi[3][q][k][1]);
+        }
+}
+
+/* u of cell (i, j) with the program's ghost values: periodic wrap, or the wall's odd mirror */
+static double sw_u(const orc_sw2d_cfg* g, const double* U, int i, int j) {
+    double s = 1.0;
+    if (i < 0 || i >= g->nx) {
+        if (g->bc[i < 0 ? 0 : 1] == 0) i = (i + g->nx) % g->nx;
+        else { i = i < 0 ? -1 - i : 2 * (g->nx - 1) - i + 1; s = -s; }
+    }
+    if (j < 0 || j >= g->ny) {
+        if (g->bc[j < 0 ? 2 : 3] == 0) j = (j + g->ny) % g->ny;
+        else { j = j < 0 ? -1 - j : 2 * (g->ny - 1) - j + 1; s = -s; }
+    }
+    const double v = U[((size_t)j * g->nx + i) * 2];
+    return s < 0 ? -v : v;
+}
+
+int orc_sw2d_rhs(const orc_sw2d_cfg* g, const double* U, double* RHS) {
+    const int nx = g->nx, ny = g->ny, ex = nx + 2;
+    const double r1_h = 1. / (g->h);
+    static const double r41_60 = 41. / 60., r11_120 = 11. / 120., r1_6 = 1. / 6., r1_12 = 1. / 12.;
+    double phi[4][2][10][2];
+    sw_tables(phi);
+    /* gr[((j+1)*ex + (i+1))*16 + (f*2+q)*2 + d]: the r1_h-scaled gradients */
+    double* gr = (double*)malloc(sizeof(double) * (size_t)ex * (ny + 2) * 16);
+    double* F = (double*)malloc(sizeof(double) * (size_t)(nx + 1) * ny);
+    double* G = (double*)malloc(sizeof(double) * (size_t)nx * (ny + 1));
+    if (!gr || !F || !G) return 3;
+#pragma omp parallel for schedule(static)
+    for (int j = -1; j < ny + 1; ++j)
+        for (int i = -1; i < nx + 1; ++i) {
+            const double u_0 = sw_u(g, U, i, j);
+            const double u_ip1 = sw_u(g, U, i + 1, j), u_jp1 = sw_u(g, U, i, j + 1), u_ip1jp1 = sw_u(g, U, i + 1, j + 1);
+            const double u_im1 = sw_u(g, U, i - 1, j), u_jm1 = sw_u(g, U, i, j - 1), u_ip1jm1 = sw_u(g, U, i + 1, j - 1);
+            const double u_ip2 = sw_u(g, U, i + 2, j), u_jp2 = sw_u(g, U, i, j + 2), u_im1jp1 = sw_u(g, U, i - 1, j + 1);
+            const double u_im2 = sw_u(g, U, i - 2, j), u_jm2 = sw_u(g, U, i, j - 2), u_im1jm1 = sw_u(g, U, i - 1, j - 1);
+            double c[10];
+            c[0] = u_0;
+            c[1] = r41_60 * (-u_im1 + u_ip1) + r11_120 * (u_im2 - u_ip2);
+            c[2] = r41_60 * (-u_jm1 + u_jp1) + r11_120 * (u_jm2 - u_jp2);
+            c[3] = -u_0 + 0.5 * (u_im1 + u_ip1);
+            c[4] = -u_0 + 0.5 * (u_jm1 + u_jp1);
+            c[5] = 0.25 * (u_im1jm1 - u_im1jp1 - u_ip1jm1 + u_ip1jp1);
+            c[6] = r1_6 * (u_im1 - u_ip1) + r1_12 * (u_ip2 - u_im2);
+            c[7] = r1_6 * (u_jm1 - u_jp1) + r1_12 * (u_jp2 - u_jm2);
+            c[8] = 0.25 * (-u_im1jm1 + u_im1jp1 - u_ip1jm1 + u_ip1jp1) + 0.5 * (u_jm1 - u_jp1);
+            c[9] = 0.5 * (u_im1 - u_ip1) + 0.25 * (u_ip1jp1 - u_im1jm1 - u_im1jp1 + u_ip1jm1);
+            double* o = gr + ((size_t)(j + 1) * ex + (i + 1)) * 16;
+            for (int f = 0; f < 4; ++f)
+                for (int q = 0; q < 2; ++q) {
+                    double gx = 0.0, gy = 0.0;
+                    for (int k = 0; k < 10; ++k) {
+                        gx += c[k] * phi[f][q][k][0];
+                        gy += c[k] * phi[f][q][k][1];
+                    }
+                    o[(f * 2 + q) * 2] = r1_h * gx;
+                    o[(f * 2 + q) * 2 + 1] = r1_h * gy;
+                }
+        }
+    const double c2 = g->c * g->c;
+#define SWG(i, j, f, q, d) gr[((size_t)((j) + 1) * ex + ((i) + 1)) * 16 + ((f) * 2 + (q)) * 2 + (d)]
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx + 1; ++i) {
+            double flux = 0.0;
+            for (int q = 0; q < 2; ++q) {
+                const double FL = c2 * (SWG(i - 1, j, 1, q, 0) * 1.0 + SWG(i - 1, j, 1, q, 1) * 0.0);
+                const double FR = c2 * (SWG(i, j, 0, q, 0) * 1.0 + SWG(i, j, 0, q, 1) * 0.0);
+                flux += 0.5 * (0.5 * (FR + FL));
+            }
+            F[(size_t)j * (nx + 1) + i] = flux;
+        }
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < ny + 1; ++j)
+        for (int i = 0; i < nx; ++i) {
+            double flux = 0.0;
+            for (int q = 0; q < 2; ++q) {
+                const double FL = c2 * (SWG(i, j - 1, 3, q, 0) * 0.0 + SWG(i, j - 1, 3, q, 1) * 1.0);
+                const double FR = c2 * (SWG(i, j, 2, q, 0) * 0.0 + SWG(i, j, 2, q, 1) * 1.0);
+                flux += 0.5 * (0.5 * (FR + FL));
+            }
+            G[(size_t)j * nx + i] = flux;
+        }
+#undef SWG
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const size_t q = (size_t)j * nx + i;
+            RHS[q * 2] = U[q * 2 + 1];
+            RHS[q * 2 + 1] = r1_h * (F[(size_t)j * (nx + 1) + i + 1] - F[(size_t)j * (nx + 1) + i]) +
+                             r1_h * (G[(size_t)(j + 1) * nx + i] - G[(size_t)j * nx + i]);
+        }
+    free(gr);
+    free(F);
+    free(G);
+    return 0;
+}
+
+int orc_sw2d_run(const orc_sw2d_cfg* g, int stepper, int nsteps, double dt, double t_final, double* U, double* t_inout,
+                 int* steps_taken) {
+    const size_t n = (size_t)g->nx * g->ny * 2;
+    double* W0 = (double*)malloc(sizeof(double) * n);
+    double* W1 = (double*)malloc(sizeof(double) * n);
+    double* L = (double*)malloc(sizeof(double) * n);
+    if (!W0 || !W1 || !L) return 3;
+    double t = *t_inout;
+    int s = 0;
+    for (; s < nsteps; ++s) {
+        if (t_final > 0.0 && t >= t_final) break;
+        double h = dt;
+        if (t_final > 0.0 && t + h > t_final) h = t_final - t;
+        if (stepper == 1) {
+            /* SSP RK104, low-storage: five stages of dt/6 on w0, w1 = 9/25 w0 + 1/25 w1,
+             * w0 = 15 w1 - 5 w0, four stages of dt/6, u = 3/5 w0 + dt/10 L(w0) + w1 */
+            memcpy(W0, U, sizeof(double) * n);
+            memcpy(W1, U, sizeof(double) * n);
+            int i = 0;
+            for (; i < 5; ++i) {
+                orc_sw2d_rhs(g, W0, L);
+                for (size_t q = 0; q < n; ++q) W0[q] = W0[q] + h / 6 * L[q];
+            }
+            for (size_t q = 0; q < n; ++q) W1[q] = 9.0 / 25 * W0[q] + 1.0 / 25 * W1[q];
+            for (size_t q = 0; q < n; ++q) W0[q] = 15 * W1[q] + -5 * W0[q];
+            for (; i < 9; ++i) {
+                orc_sw2d_rhs(g, W0, L);
+                for (size_t q = 0; q < n; ++q) W0[q] = W0[q] + h / 6 * L[q];
+            }
+            orc_sw2d_rhs(g, W0, L);
+            for (size_t q = 0; q < n; ++q) U[q] = 3.0 / 5 * W0[q] + h / 10 * L[q] + 1 * W1[q];
+        } else {
+            const double dtr = h / 2;
+            const double a3 = 1.0 * 2 / (2 * 2 - 1.0), b3 = (2 - 1.0) * h / (2 * (2 * 2 - 1)), c3 = (2 - 1.0) / (2 * 2 - 1);
+            orc_sw2d_rhs(g, U, L);
+            for (size_t q = 0; q < n; ++q) W0[q] = U[q] + dtr * L[q];
+            orc_sw2d_rhs(g, W0, L);
+            for (size_t q = 0; q < n; ++q) W0[q] = W0[q] + dtr * L[q];
+            orc_sw2d_rhs(g, W0, L);
+            for (size_t q = 0; q < n; ++q) W0[q] = a3 * U[q] + b3 * L[q] + c3 * W0[q];
+            orc_sw2d_rhs(g, W0, L);
+            for (size_t q = 0; q < n; ++q) U[q] = W0[q] + dtr * L[q];
+        }
+        t += h;
+    }
+    free(W0);
+    free(W1);
+    free(L);
+    *t_inout = t;
+    if (steps_taken) *steps_taken = s;
+    return 0;
+}
+
+/* the DMDA's cell-centre coordinate of index i on an axis: DMDASetUniformCoordinates over
+ * [lo + h/2, hi - h/2], spacing (span)/n periodic, (span)/(n-1) otherwise */
+static double sw_coord(double lo, double hi, double h, int n, int periodic, int i) {
+    const double a = lo + 0.5 * h, b = hi - 0.5 * h;
+    const double hh = periodic ? (b - a) / n : (b - a) / (n - 1);
+    return a + i * hh;
+}
+
+static void sw_project(const orc_sw2d_cfg* g, int i, int j, double t, int exact, double* out) {
+    const double h = g->h;
+    const double xc = sw_coord(g->xmin, g->xmax, h, g->nx, g->bc[0] == 0, i);
+    const double yc = sw_coord(g->ymin, g->ymax, h, g->ny, g->bc[2] == 0, j);
+    const double kx = 2 * 3.14159265358979323846, ky = 2 * 3.14159265358979323846;
+    const double omega = g->c * sqrt(kx * kx + ky * ky);
+    double a0 = 0.0, a1 = 0.0;
+    for (int l = 0; l < 5; l++)
+        for (int m = 0; m < 5; m++) {
+            const double x = xc + h * AC_XGP5[l], y = yc + h * AC_XGP5[m];
+            const double w = AC_WGP5[l] * AC_WGP5[m];
+            if (exact) {
+                a0 += w * (sin(kx * x) * sin(ky * y) * cos(omega * t));
+                a1 += w * (-omega * sin(kx * x) * sin(ky * y) * sin(omega * t));
+            } else {
+                a0 += w * (sin(kx * x) * sin(ky * y));
+                a1 += w * 0.0;
+            }
+        }
+    out[0] = a0;
+    out[1] = a1;
+}
+
+void orc_sw2d_ic(const orc_sw2d_cfg* g, double* U) {
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < g->ny; ++j)
+        for (int i = 0; i < g->nx; ++i) sw_project(g, i, j, 0.0, 0, U + ((size_t)j * g->nx + i) * 2);
+}
+
+void orc_sw2d_errors(const orc_sw2d_cfg* g, const double* U, double t, double* l2, double* linf) {
+    /* U_exact - U over the vector with the u_t entries zeroed in both (post_process.c:118-149) */
+    double s2 = 0.0, mx = 0.0;
+    for (int j = 0; j < g->ny; ++j)
+        for (int i = 0; i < g->nx; ++i) {
+            double e[2];
+            sw_project(g, i, j, t, 1, e);
+            const size_t q = ((size_t)j * g->nx + i) * 2;
+            const double d0 = e[0] + -1.0 * U[q], d1 = 0.0 + -1.0 * 0.0;
+            s2 += d0 * d0;
+            s2 += d1 * d1;
+            if (fabs(d0) > mx) mx = fabs(d0);
+            if (fabs(d1) > mx) mx = fabs(d1);
+        }
+    *l2 = sqrt(s2) / ((double)g->nx);
+    *linf = mx;
+}

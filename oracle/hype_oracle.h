@@ -127,6 +127,23 @@ int orc_acoustic_run(const orc_acoustic_cfg* g, int nsteps, double dt, double t_
 void orc_acoustic_plane_wave_ic(const orc_acoustic_cfg* g, double* U);
 void orc_acoustic_plane_wave_errors(const orc_acoustic_cfg* g, const double* U, double t, double* l2, double* linf);
 
+/* 2D acoustic FV program of 2d/weno4/standing_wave: state AoS [j][i][2] = (u, u_t);
+ * bc[4]: 0 periodic, 4 adiabatic wall (odd mirror of u); the 2D R4 polynomial (10
+ * coefficients), its normal gradients at 2 Gauss points per edge, the averaged flux
+ * c^2 grad u . n, RHS (u_t, div). stepper 0: SSP RKS3 / 4 stages, 1: SSP RK104. */
+typedef struct {
+    int nx, ny;
+    double xmin, ymin, xmax, ymax, h, c;
+    int bc[4];
+} orc_sw2d_cfg;
+int orc_sw2d_rhs(const orc_sw2d_cfg* g, const double* U, double* RHS);
+int orc_sw2d_run(const orc_sw2d_cfg* g, int stepper, int nsteps, double dt, double t_final, double* U, double* t_inout,
+                 int* steps_taken);
+/* sin(2 pi x) sin(2 pi y) at the 5x5 Gauss points of the cell-centre coordinates of the
+ * program's DMDA (initialize_solution.c), and ErrorNorms (post_process.c) at time t */
+void orc_sw2d_ic(const orc_sw2d_cfg* g, double* U);
+void orc_sw2d_errors(const orc_sw2d_cfg* g, const double* U, double t, double* l2, double* linf);
+
 /* OpenMP threads the restatement runs with */
 int orc_threads(void);
 

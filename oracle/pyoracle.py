@@ -88,6 +88,13 @@ def lib():
         L.orc_acoustic_plane_wave_errors.argtypes = [C.POINTER(AcousticCfg), D, C.c_double, D, D]
         L.orc_acoustic_plane_wave_errors.restype = None
         L.orc_euler_run.argtypes = [C.POINTER(EulerCfg), C.c_int, C.c_int, D, D, D, C.POINTER(C.c_long)]
+        L.orc_sw2d_rhs.argtypes = [C.POINTER(Sw2dCfg), D, D]
+        L.orc_sw2d_run.argtypes = [C.POINTER(Sw2dCfg), C.c_int, C.c_int, C.c_double, C.c_double, D, D,
+                                   C.POINTER(C.c_int)]
+        L.orc_sw2d_ic.argtypes = [C.POINTER(Sw2dCfg), D]
+        L.orc_sw2d_ic.restype = None
+        L.orc_sw2d_errors.argtypes = [C.POINTER(Sw2dCfg), D, C.c_double, D, D]
+        L.orc_sw2d_errors.restype = None
         L.orc_ctcs2d_plane.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, D, D, D]
         L.orc_ctcs_pointsrc.argtypes = [C.POINTER(CtcsCfg), D, C.c_int, D, D, D, D]
         L.orc_ctcs_monopole.argtypes = [C.POINTER(MonoCfg), C.c_int, D, D, D]
@@ -316,6 +323,99 @@ def ref_acoustic_run(cfg, U, nsteps, dt, t_final=0.0):
     _ref_acoustic_lib().ref_acoustic_run(cfg.nx, cfg.ny, cfg.nz, cfg.h, bc, int(nsteps), float(dt), float(t_final),
                                          _dp(U), C.byref(t))
     return U, t.value
+
+
+# ---------------------------------------------------------------- 2D acoustic FV (standing_wave)
+class Sw2dCfg(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("xmin", C.c_double), ("ymin", C.c_double), ("xmax", C.c_double),
+                ("ymax", C.c_double), ("h", C.c_double), ("c", C.c_double), ("bc", C.c_int * 4)]
+
+
+def sw2d_cfg(nx, ny, h, xmin=0.0, ymin=0.0, bc=(4,) * 4, c=1.0, xmax=None, ymax=None):
+    g = Sw2dCfg()
+    g.nx, g.ny, g.h, g.c = nx, ny, h, c
+    g.xmin, g.ymin = xmin, ymin
+    g.xmax = xmin + nx * h if xmax is None else xmax
+    g.ymax = ymin + ny * h if ymax is None else ymax
+    for q in range(4):
+        g.bc[q] = bc[q]
+    return g
+
+
+def standing_wave_cfg(N):
+    """the 2d/weno4/standing_wave program's set-up (hype.c:30-50): [-1,1]^2, adiabatic walls"""
+    return sw2d_cfg(N, N, (1.0 - -1.0) / N, -1.0, -1.0, (4,) * 4, 1.0, 1.0, 1.0)
+
+
+def sw2d_rhs(cfg, U):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    lib().orc_sw2d_rhs(C.byref(cfg), _dp(U), _dp(R))
+    return R
+
+
+def sw2d_run(cfg, U, nsteps, dt, t_final=0.0, stepper=1):
+    U = np.array(U, dtype=np.float64, order="C", copy=True)
+    t = C.c_double(0.0)
+    n = C.c_int(0)
+    lib().orc_sw2d_run(C.byref(cfg), int(stepper), int(nsteps), float(dt), float(t_final), _dp(U), C.byref(t),
+                       C.byref(n))
+    return U, t.value, n.value
+
+
+def sw2d_ic(cfg):
+    U = np.zeros((cfg.ny, cfg.nx, 2))
+    lib().orc_sw2d_ic(C.byref(cfg), _dp(U))
+    return U
+
+
+def sw2d_errors(cfg, U, t):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    l2, li = C.c_double(), C.c_double()
+    lib().orc_sw2d_errors(C.byref(cfg), _dp(U), float(t), C.byref(l2), C.byref(li))
+    return l2.value, li.value
+
+
+_ref_sw2d = None
+
+
+def _ref_sw2d_lib():
+    global _ref_sw2d
+    if _ref_sw2d is None:
+        L = C.CDLL(os.path.join(HERE, "_ref", "libref_sw2d.so"))
+        IP = C.POINTER(C.c_int)
+        L.ref_sw2d_rhs.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, IP, D, D]
+        L.ref_sw2d_run.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, IP, C.c_int, C.c_int,
+                                   C.c_double, C.c_double, D, D]
+        L.ref_sw2d_program.argtypes = [C.c_int, D, D, D, D]
+        _ref_sw2d = L
+    return _ref_sw2d
+
+
+def ref_sw2d_rhs(cfg, U):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    bc = (C.c_int * 4)(*cfg.bc)
+    _ref_sw2d_lib().ref_sw2d_rhs(cfg.nx, cfg.ny, cfg.xmin, cfg.ymin, cfg.h, bc, _dp(U), _dp(R))
+    return R
+
+
+def ref_sw2d_run(cfg, U, nsteps, dt, t_final=0.0, stepper=1):
+    U = np.array(U, dtype=np.float64, order="C", copy=True)
+    t = C.c_double(0.0)
+    bc = (C.c_int * 4)(*cfg.bc)
+    _ref_sw2d_lib().ref_sw2d_run(cfg.nx, cfg.ny, cfg.xmin, cfg.ymin, cfg.h, bc, int(stepper), int(nsteps), float(dt),
+                                 float(t_final), _dp(U), C.byref(t))
+    return U, t.value
+
+
+def ref_sw2d_program(N):
+    """the whole standing-wave program at N x N: (l2, linf, U0, U_final)"""
+    U0 = np.zeros((N, N, 2))
+    U1 = np.zeros((N, N, 2))
+    l2, li = C.c_double(), C.c_double()
+    _ref_sw2d_lib().ref_sw2d_program(int(N), C.byref(l2), C.byref(li), _dp(U0), _dp(U1))
+    return l2.value, li.value, U0, U1
 
 
 def ref_ctcs2d_run(p_old, p, h, c0, dt, zero_bc, nsteps):

@@ -27,6 +27,9 @@ tree is available; the GPU machine has none, so the fixtures are committed).
                            history of its 32^3 Taylor-Green run
                            (3d/weno4/Navier-Stokes-3D/ke.csv: t, KE, dissipation every
                            10 steps)
+* ref_sw2d_*.npz        -- the 2D acoustic FV RHS of 2d/weno4/standing_wave and 3 steps of
+                           it with SSP RK104 and with RKS3/4 stages, under periodic,
+                           adiabatic and mixed walls
 * ref_ctcs2d.npz        -- the reference's CTCS() (2d/ctcs/plane_wave/wave.c)
                            on a zero-exterior grid
 * ref_bubble_*.npz      -- the reference's 2D diffuse-interface RHSFunction
@@ -84,6 +87,19 @@ def ns3d_fixtures():
         g.write(f.read())
 
 
+def sw2d_fixtures():
+    """the 2d/weno4/standing_wave fixtures (RHS, 3 RK104 steps, 3 RKS3/4 steps)"""
+    for name, bc, seed in (("periodic", (0,) * 4, 41), ("adiabatic", (4,) * 4, 42), ("mixed", (4, 4, 0, 0), 43)):
+        nx, ny, h = 9, 7, 0.3
+        cfg = O.sw2d_cfg(nx, ny, h, -0.2, 0.1, bc)
+        U = np.random.default_rng(seed).standard_normal((ny, nx, 2))
+        R = O.ref_sw2d_rhs(cfg, U)
+        U104, t104 = O.ref_sw2d_run(cfg, U, 3, 0.01, stepper=1)
+        U43, t43 = O.ref_sw2d_run(cfg, U, 3, 0.01, stepper=0)
+        np.savez_compressed(os.path.join(HERE, f"ref_sw2d_{name}.npz"), U=U, RHS=R, U104=U104, t104=t104, U43=U43,
+                            t43=t43, dt=0.01, h=h, xmin=-0.2, ymin=0.1, nx=nx, ny=ny, bc=np.array(bc))
+
+
 def main():
     O.build(REF)
     src = os.path.join(REF, "3d/ctcs/point_source/results/p.dat")
@@ -128,6 +144,7 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"ref_acoustic_{name}.npz"), U=U, RHS=R, U3=U3, t3=t3, dt=0.01, h=0.3,
                             shape=np.array(shape), bc=np.array(bc))
     ns3d_fixtures()
+    sw2d_fixtures()
     n = 32
     x = -1 + np.arange(n) * (2.0 / n)
     Xg, Yg = np.meshgrid(x, x)

@@ -178,3 +178,36 @@ def test_ns3d_taylor_green_reproduces_ke_csv(oracle):
         assert abs(oracle.kinetic_energy(cfg, U) - ke[r, 1]) <= 1e-8 * ke[r, 1]
         assert abs(oracle.dissipation(cfg, U) - ke[r, 2]) <= 1e-8 * ke[r, 2]
 
+
+# ---------------------------------------------------------------- 2D standing wave
+def _sw2d_cfg(oracle, z):
+    return oracle.sw2d_cfg(int(z["nx"]), int(z["ny"]), float(z["h"]), float(z["xmin"]), float(z["ymin"]),
+                           tuple(int(b) for b in z["bc"]))
+
+
+@pytest.mark.parametrize("name", ["periodic", "adiabatic", "mixed"])
+def test_sw2d_rhs_and_steps_match_reference_bitwise(oracle, name):
+    """the 2D acoustic RHS of 2d/weno4/standing_wave and 3 steps with RK104 and RKS3/4"""
+    z = np.load(os.path.join(GOLDEN, f"ref_sw2d_{name}.npz"))
+    cfg = _sw2d_cfg(oracle, z)
+    assert np.array_equal(oracle.sw2d_rhs(cfg, z["U"]), z["RHS"])
+    U, t, n = oracle.sw2d_run(cfg, z["U"], 3, float(z["dt"]), stepper=1)
+    assert np.array_equal(U, z["U104"]) and t == float(z["t104"]) and n == 3
+    U, t, n = oracle.sw2d_run(cfg, z["U"], 3, float(z["dt"]), stepper=0)
+    assert np.array_equal(U, z["U43"]) and t == float(z["t43"])
+
+
+@pytest.mark.parametrize("N", [16, 32, 64])
+def test_sw2d_program_reproduces_error_dat(oracle, N):
+    """the whole standing-wave program (hype.c: projected initial condition, RK104 with
+    dt = h CFL / 2 to t = 1 with the last step matched, ErrorNorms) against the
+    reference's checked-in results/Error.dat, digit for digit as printed (%.7e)"""
+    with open(os.path.join(GOLDEN, "accuracy_tables.json")) as f:
+        rows = {int(r[0]): r for r in json.load(f)["standing_wave_2d_Error_dat"]}
+    cfg = oracle.standing_wave_cfg(N)
+    U0 = oracle.sw2d_ic(cfg)
+    U, t, n = oracle.sw2d_run(cfg, U0, 1 << 30, 0.5 * cfg.h * 0.5 / 1.0, t_final=1.0, stepper=1)
+    assert t == 1.0
+    l2, linf = oracle.sw2d_errors(cfg, U, 1.0)
+    assert "%.7e %.7e" % (l2, linf) == "%.7e %.7e" % (rows[N][1], rows[N][2])
+

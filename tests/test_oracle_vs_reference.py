@@ -144,3 +144,26 @@ def test_ns3d_rhs_and_run_bitwise(oracle, bc):
     assert r1 == r2 == 0
     assert np.array_equal(U1, U2) and t1 == t2 and d1 == d2
 
+
+@pytest.mark.parametrize("bc", [(0,) * 4, (4,) * 4, (0, 0, 4, 4)])
+def test_sw2d_rhs_and_run_bitwise(oracle, bc):
+    """2d/weno4/standing_wave: RHS and RK104 / RKS3 steps on a fresh seeded state"""
+    _need_ref(oracle)
+    cfg = oracle.sw2d_cfg(11, 8, 0.17, 0.3, -0.4, bc)
+    U = np.random.default_rng(77).standard_normal((8, 11, 2))
+    assert np.array_equal(oracle.sw2d_rhs(cfg, U), oracle.ref_sw2d_rhs(cfg, U))
+    for stepper in (0, 1):
+        a = oracle.sw2d_run(cfg, U, 4, 0.02, stepper=stepper)
+        b = oracle.ref_sw2d_run(cfg, U, 4, 0.02, stepper=stepper)
+        assert np.array_equal(a[0], b[0]) and a[1] == b[1]
+
+
+def test_sw2d_program_initial_and_final_states_bitwise(oracle):
+    _need_ref(oracle)
+    l2, li, U0, U1 = oracle.ref_sw2d_program(16)
+    cfg = oracle.standing_wave_cfg(16)
+    assert np.array_equal(oracle.sw2d_ic(cfg), U0)
+    U, t, n = oracle.sw2d_run(cfg, U0, 1 << 30, 0.5 * cfg.h * 0.5 / 1.0, t_final=1.0, stepper=1)
+    assert np.array_equal(U, U1)
+    assert oracle.sw2d_errors(cfg, U, 1.0) == (l2, li)
+
