@@ -32,11 +32,48 @@ struct Geo {
     int ex;           // nx + 2
 };
 
-// the normal component of the basis gradients, tab[f][q][k]: f = left, right, bottom,
-// top edge, q = Gauss point, k = basis function
-struct Tables {
-    double t[4][2][10];
-};
+// basis_grad (reconstruction.c:50-100), the component along axis d
+__host__ __device__ constexpr double basis_grad_axis(double x, double y, int n, int d) {
+    double gx = 0.0, gy = 0.0;
+    switch (n) {
+        case 1: gx = 1.0; break;
+        case 2: gy = 1.0; break;
+        case 3: gx = 2.0 * x; break;
+        case 4: gy = 2.0 * y; break;
+        case 5: gx = y; gy = x; break;
+        case 6: gx = 3.0 * x * x - 3. / 20.; break;
+        case 7: gy = 3.0 * y * y - 3. / 20.; break;
+        case 8: gx = 2.0 * x * y; gy = (x * x - 1. / 12.); break;
+        case 9: gx = (y * y - 1. / 12.); gy = 2.0 * x * y; break;
+        default: break;
+    }
+    return d == 0 ? gx : gy;
+}
+
+// the 2-point Gauss abscissae on [-1/2, 1/2] (x_gp2, hype.h:56)
+__host__ __device__ constexpr double gp2(int q) { return q == 0 ? -0.28867513459481287 : 0.28867513459481287; }
+
+// the normal component of the basis gradient at Gauss point q of edge f (left, right,
+// bottom, top) for basis k, as the program fills its tables (hype.c:137-166)
+__host__ __device__ constexpr double tab(int f, int q, int k) {
+    return f == 0 ? basis_grad_axis(-0.5, gp2(q), k, 0)
+         : f == 1 ? basis_grad_axis(0.5, gp2(q), k, 0)
+         : f == 2 ? basis_grad_axis(gp2(q), -0.5, k, 1)
+                  : basis_grad_axis(gp2(q), 0.5, k, 1);
+}
+
+// sum_k c[k] tab(f, q, k) in the program's order (rhs_function.c:139-146), the terms
+// whose table entry is zero left out: they add a signed zero, which changes no value
+template <int F, int Q, int K = 0>
+__device__ __forceinline__ double edge_grad(const double* c, double acc) {
+    if constexpr (K == 10) {
+        return acc;
+    } else {
+        constexpr double w = tab(F, Q, K);
+        if constexpr (w == 0.0) return edge_grad<F, Q, K + 1>(c, acc);
+        else return edge_grad<F, Q, K + 1>(c, acc + c[K] * w);
+    }
+}
 
 // the program's ghost value map of one axis: periodic wrap, or the wall mirror (odd in u)
 __device__ __forceinline__ int sw_map(int i, int n, int blo, int bhi, double& s) {
@@ -62,17 +99,28 @@ __device__ __forceinline__ double sw_u(const double* __restrict__ u, const Geo& 
 }
 
 // T[(f*2+q)][extended cell]: (1/h) times the normal gradient at Gauss point q of edge f
-__global__ void __launch_bounds__(256) k_sw_recon(const double* __restrict__ u, double* __restrict__ T, Geo g, Tables tb,
+__global__ void __launch_bounds__(256) k_sw_recon(const double* __restrict__ u, double* __restrict__ T, Geo g,
                                                   double r1_h) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
     if (i > g.nx || j > g.ny) return;
     constexpr double r41_60 = 41. / 60., r11_120 = 11. / 120., r1_6 = 1. / 6., r1_12 = 1. / 12.;
-    const double u_0 = sw_u(u, g, i, j);
-    const double u_ip1 = sw_u(u, g, i + 1, j), u_jp1 = sw_u(u, g, i, j + 1), u_ip1jp1 = sw_u(u, g, i + 1, j + 1);
-    const double u_im1 = sw_u(u, g, i - 1, j), u_jm1 = sw_u(u, g, i, j - 1), u_ip1jm1 = sw_u(u, g, i + 1, j - 1);
-    const double u_ip2 = sw_u(u, g, i + 2, j), u_jp2 = sw_u(u, g, i, j + 2), u_im1jp1 = sw_u(u, g, i - 1, j + 1);
-    const double u_im2 = sw_u(u, g, i - 2, j), u_jm2 = sw_u(u, g, i, j - 2), u_im1jm1 = sw_u(u, g, i - 1, j - 1);
+    double u_0, u_ip1, u_jp1, u_ip1jp1, u_im1, u_jm1, u_ip1jm1, u_ip2, u_jp2, u_im1jp1, u_im2, u_jm2, u_im1jm1;
+    if (i >= 2 && i < g.nx - 2 && j >= 2 && j < g.ny - 2) {  // no ghost value in the stencil
+        const double* p = u + (long long)j * g.nx + i;
+        const int sy = g.nx;
+        u_0 = __ldg(p);
+        u_ip1 = __ldg(p + 1), u_jp1 = __ldg(p + sy), u_ip1jp1 = __ldg(p + sy + 1);
+        u_im1 = __ldg(p - 1), u_jm1 = __ldg(p - sy), u_ip1jm1 = __ldg(p - sy + 1);
+        u_ip2 = __ldg(p + 2), u_jp2 = __ldg(p + 2 * sy), u_im1jp1 = __ldg(p + sy - 1);
+        u_im2 = __ldg(p - 2), u_jm2 = __ldg(p - 2 * sy), u_im1jm1 = __ldg(p - sy - 1);
+    } else {
+        u_0 = sw_u(u, g, i, j);
+        u_ip1 = sw_u(u, g, i + 1, j), u_jp1 = sw_u(u, g, i, j + 1), u_ip1jp1 = sw_u(u, g, i + 1, j + 1);
+        u_im1 = sw_u(u, g, i - 1, j), u_jm1 = sw_u(u, g, i, j - 1), u_ip1jm1 = sw_u(u, g, i + 1, j - 1);
+        u_ip2 = sw_u(u, g, i + 2, j), u_jp2 = sw_u(u, g, i, j + 2), u_im1jp1 = sw_u(u, g, i - 1, j + 1);
+        u_im2 = sw_u(u, g, i - 2, j), u_jm2 = sw_u(u, g, i, j - 2), u_im1jm1 = sw_u(u, g, i - 1, j - 1);
+    }
     double c[10];
     c[0] = u_0;
     c[1] = r41_60 * (-u_im1 + u_ip1) + r11_120 * (u_im2 - u_ip2);
@@ -85,13 +133,14 @@ __global__ void __launch_bounds__(256) k_sw_recon(const double* __restrict__ u, 
     c[8] = 0.25 * (-u_im1jm1 + u_im1jp1 - u_ip1jm1 + u_ip1jp1) + 0.5 * (u_jm1 - u_jp1);
     c[9] = 0.5 * (u_im1 - u_ip1) + 0.25 * (u_ip1jp1 - u_im1jm1 - u_im1jp1 + u_ip1jm1);
     const long long e = (long long)(j + 1) * g.ex + (i + 1);
-#pragma unroll
-    for (int fq = 0; fq < 8; ++fq) {
-        double gn = 0.0;
-#pragma unroll
-        for (int k = 0; k < 10; ++k) gn += c[k] * tb.t[fq >> 1][fq & 1][k];
-        T[(long long)fq * g.NE + e] = r1_h * gn;
-    }
+    T[0 * g.NE + e] = r1_h * edge_grad<0, 0>(c, 0.0);
+    T[1 * g.NE + e] = r1_h * edge_grad<0, 1>(c, 0.0);
+    T[2 * g.NE + e] = r1_h * edge_grad<1, 0>(c, 0.0);
+    T[3 * g.NE + e] = r1_h * edge_grad<1, 1>(c, 0.0);
+    T[4 * g.NE + e] = r1_h * edge_grad<2, 0>(c, 0.0);
+    T[5 * g.NE + e] = r1_h * edge_grad<2, 1>(c, 0.0);
+    T[6 * g.NE + e] = r1_h * edge_grad<3, 0>(c, 0.0);
+    T[7 * g.NE + e] = r1_h * edge_grad<3, 1>(c, 0.0);
 }
 
 struct Stage {
@@ -159,35 +208,20 @@ __global__ void k_sw_soa2aos(const double* __restrict__ s, double* __restrict__ 
     a[2 * q + 1] = s[N + q];
 }
 
-// basis_grad (reconstruction.c:50-100), the component along axis d
-static double basis_grad_axis(double x, double y, int n, int d) {
-    double gx = 0.0, gy = 0.0;
-    switch (n) {
-        case 1: gx = 1.0; break;
-        case 2: gy = 1.0; break;
-        case 3: gx = 2.0 * x; break;
-        case 4: gy = 2.0 * y; break;
-        case 5: gx = y; gy = x; break;
-        case 6: gx = 3.0 * x * x - 3. / 20.; break;
-        case 7: gy = 3.0 * y * y - 3. / 20.; break;
-        case 8: gx = 2.0 * x * y; gy = (x * x - 1. / 12.); break;
-        case 9: gx = (y * y - 1. / 12.); gy = 2.0 * x * y; break;
-        default: break;
-    }
-    return d == 0 ? gx : gy;
-}
-
-static Tables make_tables() {
-    constexpr double gp[2] = {-0.28867513459481287, 0.28867513459481287};
-    Tables tb;
+// the table as the program computes it at run time (hype.c:137-166), for the check that
+// the compile-time table used by the kernels is the same, bit for bit
+static bool tables_match() {
+    const volatile double gp[2] = {gp2(0), gp2(1)};
     for (int q = 0; q < 2; ++q)
         for (int k = 0; k < 10; ++k) {
-            tb.t[0][q][k] = basis_grad_axis(-0.5, gp[q], k, 0);
-            tb.t[1][q][k] = basis_grad_axis(0.5, gp[q], k, 0);
-            tb.t[2][q][k] = basis_grad_axis(gp[q], -0.5, k, 1);
-            tb.t[3][q][k] = basis_grad_axis(gp[q], 0.5, k, 1);
+            const double x[4] = {-0.5, 0.5, gp[q], gp[q]}, y[4] = {gp[q], gp[q], -0.5, 0.5};
+            for (int f = 0; f < 4; ++f) {
+                const double run = basis_grad_axis(x[f], y[f], k, f < 2 ? 0 : 1);
+                const double ct = tab(f, q, k);
+                if (memcmp(&run, &ct, sizeof(double)) != 0 && !(run == 0.0 && ct == 0.0)) return false;
+            }
         }
-    return tb;
+    return true;
 }
 
 }  // namespace acoustic2d
@@ -199,7 +233,6 @@ using namespace hype::acoustic2d;
 struct hype_acoustic2d {
     hype_acoustic2d_params p;
     Geo g;
-    Tables tb;
     cudaStream_t stream = nullptr;
     double *U = nullptr, *W0 = nullptr, *W1 = nullptr, *S = nullptr, *L = nullptr, *T = nullptr, *aos = nullptr;
 };
@@ -207,8 +240,7 @@ struct hype_acoustic2d {
 static int sw_rhs_stage(hype_acoustic2d* a, const double* Win, const double* X, const double* Y, double* out, Stage st,
                         double dt) {
     const Geo& g = a->g;
-    k_sw_recon<<<dim3(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 8)), dim3(32, 8), 0, a->stream>>>(Win, a->T, g, a->tb,
-                                                                                           1. / (a->p.h));
+    k_sw_recon<<<dim3(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 8)), dim3(32, 8), 0, a->stream>>>(Win, a->T, g, 1. / (a->p.h));
     k_sw_update<<<dim3(cdiv(g.nx, 32), cdiv(g.ny, 8)), dim3(32, 8), 0, a->stream>>>(
         a->T, Win, X, Y, out, g, a->p.c * a->p.c, 1. / (a->p.h), st, dt);
     HYPE_LAUNCHED(2);
@@ -224,6 +256,11 @@ extern "C" int hype_acoustic2d_create(const hype_acoustic2d_params* p, hype_acou
     for (int d = 0; d < 2; ++d)
         if ((p->bc[2 * d] == HYPE_BC_PERIODIC) != (p->bc[2 * d + 1] == HYPE_BC_PERIODIC)) return HYPE_ERR_ARG;
     if (p->stepper != HYPE_STEP_SSPRK43 && p->stepper != HYPE_STEP_SSPRK104) return HYPE_ERR_ARG;
+    if (!tables_match()) {
+        set_last_error("hype_acoustic2d_create: compile-time basis-gradient table differs from the run-time one",
+                       cudaSuccess);
+        return HYPE_ERR_UNSUPPORTED;
+    }
     hype_acoustic2d* a = new hype_acoustic2d();
     a->p = *p;
     Geo& g = a->g;
@@ -233,7 +270,6 @@ extern "C" int hype_acoustic2d_create(const hype_acoustic2d_params* p, hype_acou
     g.N = (long long)p->nx * p->ny;
     g.ex = p->nx + 2;
     g.NE = (long long)(p->nx + 2) * (p->ny + 2);
-    a->tb = make_tables();
     const size_t sN = sizeof(double) * 2 * (size_t)g.N;
     cudaError_t ce = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking);
     if (ce == cudaSuccess) ce = cudaMalloc((void**)&a->U, sN);

@@ -674,6 +674,72 @@ def run_acoustic(args, ws, rank, local, n=256):
             "gpu_launches": launches, "clocks": clk.summary()}
 
 
+def run_sw2d(args, ws, rank, local, n=4096):
+    """2D acoustic FV program of 2d/weno4/standing_wave at n^2: sin(2 pi x) sin(2 pi y) on
+    [-1,1]^2, adiabatic walls, R4 edge gradients + averaged flux, SSP RK104 with
+    dt = h CFL / 2, CFL 0.5"""
+    import torch
+
+    import acoustic_petsc_gb300 as H
+
+    L = H.lib()
+    H._lib.check(L.hype_set_device(local), "hype_set_device")
+    torch.cuda.set_device(local)
+    n = args.grid or n
+    h = 2.0 / n
+    s = H.AcousticFV2D(n, n, h, 0.5 * h * 0.5, x_min=-1.0, y_min=-1.0)
+    x = -1.0 + (np.arange(n) + 0.5) * h
+    U0 = np.zeros((n, n, 2))
+    U0[..., 0] = np.sin(2 * math.pi * x)[None, :] * np.sin(2 * math.pi * x)[:, None]
+    s.set_state(U0)
+    s.step(max(args.warmup, 3))
+    stream = torch.cuda.ExternalStream(L.hype_acoustic2d_stream(s._h))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = H.launches()
+    _barrier(ws)
+    torch.cuda.synchronize()
+    with Clocks(_gpu_index(local)) as clk:
+        e0.record(stream)
+        s.step(args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    launches = H.launches() - l0
+    ms = _max_over_ranks(ws, e0.elapsed_time(e1))
+    cells = n * n
+    value = ws * cells * args.steps / (ms * 1e-3)
+    peak, kind = _peaks()
+    # per RK104 step and cell: 10 stages of read + write (u, v), the two combinations
+    # (read 2 states, write 1) and the final read of the second register
+    bytes_cu = 10 * 32 + 2 * 48 + 16
+    ach = bytes_cu * cells * args.steps / (ms * 1e-3) / 1e9
+    # end to end: host state in, one step, host state out (pinned buffers)
+    host = torch.empty((n, n, 2), dtype=torch.float64, pin_memory=True)
+    hv = host.numpy()
+    hv[...] = U0
+    ke = max(1, min(3, args.steps))
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        s.set_state(hv)
+        s.step(1)
+        H._lib.check(L.hype_acoustic2d_download(s._h, hv.ctypes.data_as(H._lib.D)), "download")
+    wall = time.perf_counter() - t0
+    ms_e2e = _max_over_ranks(ws, wall * 1e3)
+    s.close()
+    nb = cells * 2 * 8
+    return {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic standing wave sin(2 pi x) sin(2 pi y), cell centres",
+            "config": {"workload": f"acoustic_fv_standing_wave_{n}", "grid": [n, n], "cfl": 0.5,
+                       "scheme": "2D R4 edge gradients + averaged flux + SSP RK104, 2d/weno4/standing_wave",
+                       "l2": f"state 2*8*{n}^2 B = {16 * cells / 1e6:.0f} MB vs 129 MB; no flush"},
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "algorithmic_bytes_per_cell_update": bytes_cu, "traffic": None},
+            "e2e": {"value": ws * cells * ke / (ms_e2e * 1e-3), "unit": "cell-updates/s", "h2d_bytes_per_step": nb,
+                    "d2h_bytes_per_step": nb, "steps": ke,
+                    "path": "AcousticFV2D.set_state -> step(1) -> get_state"},
+            "gpu_launches": launches, "clocks": clk.summary()}
+
+
 WORKLOADS = {
     "blast512": run_blast,
     "blast256": lambda a, *r: run_blast(a, *r, n=256),
@@ -691,6 +757,7 @@ WORKLOADS = {
     "euler64": lambda a, *r: run_euler(a, *r, precision=0, recon=0, n=64),
     "euler128": lambda a, *r: run_euler(a, *r, precision=0, recon=0, n=128),
     "euler128_fp32": lambda a, *r: run_euler(a, *r, precision=1, recon=0, n=128),
+    "sw2d4096": run_sw2d,
     "ctcs512": run_ctcs,
     "batch256": run_batch,
 }
@@ -758,6 +825,19 @@ def main():
             d = time.perf_counter() - t0
             out["cpu_baseline"] = {"value": n * n * 4 / d, "unit": "cell-updates/s", "cores": O.threads(),
                                    "kind": "port", "sample": f"4 SSPRK(4,3) steps of the {n}^2 version ({d:.1f} s)"}
+        elif args.workload.startswith("sw2d"):
+            from oracle import pyoracle as O
+
+            O.build(None)
+            n = 1024
+            cfg = O.sw2d_cfg(n, n, 2.0 / n, -1.0, -1.0, (4,) * 4, 1.0, 1.0, 1.0)
+            U0 = O.sw2d_ic(cfg)
+            O.sw2d_run(cfg, U0, 1, 0.5 * cfg.h * 0.5)
+            t0 = time.perf_counter()
+            O.sw2d_run(cfg, U0, 10, 0.5 * cfg.h * 0.5)
+            d = time.perf_counter() - t0
+            out["cpu_baseline"] = {"value": n * n * 10 / d, "unit": "cell-updates/s", "cores": O.threads(),
+                                   "kind": "port", "sample": f"10 RK104 steps of the {n}^2 standing wave ({d:.1f} s)"}
         elif args.workload.startswith("ns"):
             from acoustic_petsc_gb300 import workloads
             from oracle import pyoracle as O
