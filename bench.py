@@ -9,8 +9,12 @@ cell-updates/s (cells x steps / s).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl reference]
 
 Other workloads (--workload): euler256_fp32 (FP32 reconstruction/flux, FP64
-state), euler256_linear (optimal-weight linear reconstruction), ctcs512 (2D
-CTCS 512^2), batch256 (256 batched monopole CTCS instances).
+state), euler256_linear (optimal-weight linear reconstruction), euler256_weno3,
+euler256_hllc, ns256_tgv (viscous Taylor-Green), acoustic256 (3D acoustic FV),
+sw2d4096 (2D standing wave, RK104), kapila1024[_fp32|_learned], blast256/512,
+ctcs512 (2D CTCS 512^2), batch256 (256 batched monopole CTCS instances).
+--grid N sets the cells per axis of the 3D Euler / Navier-Stokes and 2D acoustic
+workloads (small cases for profiling).
 
 N > 1 (torchrun): replicas only -- each rank runs the same workload on its own
 GPU, no data exchange; value = all ranks' cell-updates / max time.
