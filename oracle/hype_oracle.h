@@ -144,6 +144,30 @@ int orc_sw2d_run(const orc_sw2d_cfg* g, int stepper, int nsteps, double dt, doub
 void orc_sw2d_ic(const orc_sw2d_cfg* g, double* U);
 void orc_sw2d_errors(const orc_sw2d_cfg* g, const double* U, double t, double* l2, double* linf);
 
+/* 3D primitive-variable multiphase RHS of 3d/weno4/Viscous-Multiphase-Fourth-Order
+ * (RHSFunctionPrimitive): Q = (rho, rho u, rho v, rho w, E, phi), mixture EOS of two
+ * stiffened gases (g1, p1) / (g2, p2) mixed by phi, CWENO4 of the primitive variables,
+ * 33-node admissibility check with first-order fallback, rotated HLLC with the
+ * non-conservative phi term, and the viscous speed (4/3)(phi mu1 + (1-phi) mu2)/rho in
+ * dt (the program's viscous flux itself is not defined, see mphase3d_oracle.c).
+ * bc[6]: 0 periodic, 1 reflective, 2 transmissive. */
+typedef struct {
+    int nx, ny, nz;
+    double h, cfl;
+    int bc[6];
+    double g1, p1, g2, p2, mu1, mu2;
+    int nthreads;
+} orc_mp3d_cfg;
+void orc_mp3d_cons2prim(const orc_mp3d_cfg* e, const double* Q, double* V);
+void orc_mp3d_prim2cons(const orc_mp3d_cfg* e, const double* V, double* Q);
+double orc_mp3d_rothllc(const orc_mp3d_cfg* e, const double* VL, const double* VR, double nx, double ny, double nz,
+                        double* Flux, int* bad);
+/* returns 0, or 2 for an inadmissible face state (the reference aborts) */
+int orc_mp3d_rhs(const orc_mp3d_cfg* e, const double* U, double* RHS, double* dt_out, double* smax_out,
+                 double* smaxv_out);
+int orc_mp3d_run(const orc_mp3d_cfg* e, int nsteps, int dt_mode, double* U, double* t_inout, double* dt_inout);
+long orc_mp3d_fallbacks(int reset);
+
 /* OpenMP threads the restatement runs with */
 int orc_threads(void);
 

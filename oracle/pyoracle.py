@@ -88,6 +88,14 @@ def lib():
         L.orc_acoustic_plane_wave_errors.argtypes = [C.POINTER(AcousticCfg), D, C.c_double, D, D]
         L.orc_acoustic_plane_wave_errors.restype = None
         L.orc_euler_run.argtypes = [C.POINTER(EulerCfg), C.c_int, C.c_int, D, D, D, C.POINTER(C.c_long)]
+        L.orc_mp3d_rhs.argtypes = [C.POINTER(Mp3dCfg), D, D, D, D, D]
+        L.orc_mp3d_run.argtypes = [C.POINTER(Mp3dCfg), C.c_int, C.c_int, D, D, D]
+        L.orc_mp3d_fallbacks.argtypes = [C.c_int]
+        L.orc_mp3d_fallbacks.restype = C.c_long
+        L.orc_mp3d_prim2cons.argtypes = [C.POINTER(Mp3dCfg), D, D]
+        L.orc_mp3d_prim2cons.restype = None
+        L.orc_mp3d_cons2prim.argtypes = [C.POINTER(Mp3dCfg), D, D]
+        L.orc_mp3d_cons2prim.restype = None
         L.orc_sw2d_rhs.argtypes = [C.POINTER(Sw2dCfg), D, D]
         L.orc_sw2d_run.argtypes = [C.POINTER(Sw2dCfg), C.c_int, C.c_int, C.c_double, C.c_double, D, D,
                                    C.POINTER(C.c_int)]
@@ -323,6 +331,87 @@ def ref_acoustic_run(cfg, U, nsteps, dt, t_final=0.0):
     _ref_acoustic_lib().ref_acoustic_run(cfg.nx, cfg.ny, cfg.nz, cfg.h, bc, int(nsteps), float(dt), float(t_final),
                                          _dp(U), C.byref(t))
     return U, t.value
+
+
+# ---------------------------------------------------------------- 3D primitive multiphase
+class Mp3dCfg(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("h", C.c_double), ("cfl", C.c_double),
+                ("bc", C.c_int * 6), ("g1", C.c_double), ("p1", C.c_double), ("g2", C.c_double), ("p2", C.c_double),
+                ("mu1", C.c_double), ("mu2", C.c_double), ("nthreads", C.c_int)]
+
+
+# the constants compiled into 3d/weno4/Viscous-Multiphase-Fourth-Order (hype.h:37-42)
+MP3D_EOS = (1.4, 0.0, 1.6, 0.0)
+MP3D_MU = (1.4, 1.6)
+
+
+def mp3d_cfg(n, h, cfl=0.9, bc=(2,) * 6, eos=MP3D_EOS, mu=MP3D_MU, nthreads=0):
+    nx, ny, nz = (n, n, n) if isinstance(n, int) else n
+    c = Mp3dCfg()
+    c.nx, c.ny, c.nz, c.h, c.cfl = nx, ny, nz, h, cfl
+    for q in range(6):
+        c.bc[q] = bc[q]
+    c.g1, c.p1, c.g2, c.p2 = eos
+    c.mu1, c.mu2 = mu
+    c.nthreads = nthreads
+    return c
+
+
+def mp3d_rhs(cfg, U):
+    """(RHS, dt, s_max_c, s_max_v, status)"""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    dt, sc, sv = C.c_double(), C.c_double(), C.c_double()
+    rc = lib().orc_mp3d_rhs(C.byref(cfg), _dp(U), _dp(R), C.byref(dt), C.byref(sc), C.byref(sv))
+    return R, dt.value, sc.value, sv.value, rc
+
+
+def mp3d_run(cfg, U, nsteps, dt_mode=0, dt=0.0):
+    U = np.array(U, dtype=np.float64, order="C", copy=True)
+    t = C.c_double(0.0)
+    d = C.c_double(dt)
+    rc = lib().orc_mp3d_run(C.byref(cfg), int(nsteps), int(dt_mode), _dp(U), C.byref(t), C.byref(d))
+    return U, t.value, d.value, rc
+
+
+def mp3d_prim2cons(cfg, V):
+    V = np.ascontiguousarray(V, dtype=np.float64)
+    Q = np.empty_like(V)
+    for idx in np.ndindex(V.shape[:-1]):
+        lib().orc_mp3d_prim2cons(C.byref(cfg), _dp(np.ascontiguousarray(V[idx])), _dp(Q[idx]))
+    return Q
+
+
+_ref_mp3d = None
+
+
+def _ref_mp3d_lib():
+    global _ref_mp3d
+    if _ref_mp3d is None:
+        L = C.CDLL(os.path.join(HERE, "_ref", "libref_mp3d.so"))
+        IP = C.POINTER(C.c_int)
+        L.ref_mp3d_rhs.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, IP, D, D, D]
+        L.ref_mp3d_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, IP, C.c_int, C.c_int, D, D, D]
+        _ref_mp3d = L
+    return _ref_mp3d
+
+
+def ref_mp3d_rhs(cfg, U):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    dt = C.c_double()
+    bc = (C.c_int * 6)(*cfg.bc)
+    rc = _ref_mp3d_lib().ref_mp3d_rhs(cfg.nx, cfg.ny, cfg.nz, cfg.h, cfg.cfl, bc, _dp(U), _dp(R), C.byref(dt))
+    return R, dt.value, rc
+
+
+def ref_mp3d_run(cfg, U, nsteps, dt_mode=0):
+    U = np.array(U, dtype=np.float64, order="C", copy=True)
+    t, dt = C.c_double(), C.c_double()
+    bc = (C.c_int * 6)(*cfg.bc)
+    rc = _ref_mp3d_lib().ref_mp3d_run(cfg.nx, cfg.ny, cfg.nz, cfg.h, cfg.cfl, bc, int(nsteps), int(dt_mode), _dp(U),
+                                      C.byref(t), C.byref(dt))
+    return U, t.value, dt.value, rc
 
 
 # ---------------------------------------------------------------- 2D acoustic FV (standing_wave)

@@ -30,6 +30,11 @@ tree is available; the GPU machine has none, so the fixtures are committed).
 * ref_sw2d_*.npz        -- the 2D acoustic FV RHS of 2d/weno4/standing_wave and 3 steps of
                            it with SSP RK104 and with RKS3/4 stages, under periodic,
                            adiabatic and mixed walls
+* ref_mp3d_*.npz        -- the 3D primitive-variable multiphase RHS of
+                           3d/weno4/Viscous-Multiphase-Fourth-Order (RHSFunctionPrimitive:
+                           primitive CWENO4, 33-node PAD fallback, rotated HLLC, phi term,
+                           viscous speed in dt) and 3 SSP RKS3/4 steps of it; "sharp"
+                           trips the fallback
 * ref_ctcs2d.npz        -- the reference's CTCS() (2d/ctcs/plane_wave/wave.c)
                            on a zero-exterior grid
 * ref_bubble_*.npz      -- the reference's 2D diffuse-interface RHSFunction
@@ -100,6 +105,40 @@ def sw2d_fixtures():
                             t43=t43, dt=0.01, h=h, xmin=-0.2, ymin=0.1, nx=nx, ny=ny, bc=np.array(bc))
 
 
+def mp3d_state(cfg, n, seed, sharp=False):
+    """a gas bubble (phi = 0) in the other phase with random velocities and pressure"""
+    nx, ny, nz = n
+    rng = np.random.default_rng(seed)
+    h = cfg.h
+    z, y, x = ((np.arange(m) + 0.5) * h for m in (nz, ny, nx))
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    r = np.sqrt((X - 0.5 * nx * h) ** 2 + (Y - 0.5 * ny * h) ** 2 + (Z - 0.5 * nz * h) ** 2)
+    w = 0.02 if sharp else 0.15
+    phi = 0.5 * (1 + np.tanh((r - 0.25 * nz * h) / (w * nz * h)))
+    V = np.zeros((nz, ny, nx, 6))
+    V[..., 0] = 0.138 + (1.0 - 0.138) * phi + 0.01 * rng.random((nz, ny, nx))
+    V[..., 1:4] = 0.05 * rng.standard_normal((nz, ny, nx, 3))
+    V[..., 4] = 1.0 + 0.1 * rng.random((nz, ny, nx))
+    V[..., 5] = phi
+    return O.mp3d_prim2cons(cfg, V)
+
+
+def mp3d_fixtures():
+    """the Viscous-Multiphase-Fourth-Order fixtures (RHS + dt, 3 steps)"""
+    n = (7, 6, 8)
+    for name, bc, seed, sharp in (("transmissive", (2,) * 6, 51, False), ("periodic", (0,) * 6, 52, False),
+                                  ("walls", (1, 1, 2, 2, 1, 1), 53, False), ("sharp", (2,) * 6, 54, True)):
+        cfg = O.mp3d_cfg(n, 1.0 / 8, cfl=0.9, bc=bc)
+        U = mp3d_state(cfg, n, seed, sharp)
+        R, dt, rc = O.ref_mp3d_rhs(cfg, U)
+        assert rc == 0
+        U3, t3, dt3, rc3 = O.ref_mp3d_run(cfg, U, 3)
+        assert rc3 == 0
+        np.savez_compressed(os.path.join(HERE, f"ref_mp3d_{name}.npz"), U=U, RHS=R, dt=dt, U3=U3, t3=t3, dt3=dt3,
+                            n=np.array(n), h=1.0 / 8, cfl=0.9, bc=np.array(bc), eos=np.array(O.MP3D_EOS),
+                            mu=np.array(O.MP3D_MU))
+
+
 def main():
     O.build(REF)
     src = os.path.join(REF, "3d/ctcs/point_source/results/p.dat")
@@ -145,6 +184,7 @@ def main():
                             shape=np.array(shape), bc=np.array(bc))
     ns3d_fixtures()
     sw2d_fixtures()
+    mp3d_fixtures()
     n = 32
     x = -1 + np.arange(n) * (2.0 / n)
     Xg, Yg = np.meshgrid(x, x)

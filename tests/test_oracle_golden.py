@@ -211,3 +211,27 @@ def test_sw2d_program_reproduces_error_dat(oracle, N):
     l2, linf = oracle.sw2d_errors(cfg, U, 1.0)
     assert "%.7e %.7e" % (l2, linf) == "%.7e %.7e" % (rows[N][1], rows[N][2])
 
+
+# ---------------------------------------------------------------- 3D primitive multiphase
+def _mp3d_cfg(oracle, z):
+    return oracle.mp3d_cfg(tuple(int(v) for v in z["n"]), float(z["h"]), cfl=float(z["cfl"]),
+                           bc=tuple(int(b) for b in z["bc"]), eos=tuple(float(v) for v in z["eos"]),
+                           mu=tuple(float(v) for v in z["mu"]))
+
+
+@pytest.mark.parametrize("name", ["transmissive", "periodic", "walls", "sharp"])
+def test_mp3d_rhs_and_steps_match_reference_bitwise(oracle, name):
+    """RHSFunctionPrimitive of 3d/weno4/Viscous-Multiphase-Fourth-Order: primitive CWENO4,
+    the 33-node admissibility fallback ("sharp"), rotated HLLC with the phi term, and its
+    dt with the viscous speed; then 3 SSP RKS3/4 steps with the program's dt updates"""
+    z = np.load(os.path.join(GOLDEN, f"ref_mp3d_{name}.npz"))
+    cfg = _mp3d_cfg(oracle, z)
+    oracle.lib().orc_mp3d_fallbacks(1)
+    R, dt, sc, sv, rc = oracle.mp3d_rhs(cfg, z["U"])
+    assert rc == 0
+    assert np.array_equal(R, z["RHS"]) and dt == float(z["dt"])
+    assert (oracle.lib().orc_mp3d_fallbacks(1) > 0) == (name == "sharp")
+    U3, t3, dt3, rc = oracle.mp3d_run(cfg, z["U"], 3)
+    assert rc == 0
+    assert np.array_equal(U3, z["U3"]) and t3 == float(z["t3"]) and dt3 == float(z["dt3"])
+

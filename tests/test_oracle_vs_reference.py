@@ -1,6 +1,8 @@
 """Restatement vs the reference compiled in place through the PETSc shim, on
 fresh seeded inputs (skipped where the reference tree was not available at
 build time, e.g. on the GPU machine: the committed golden fixtures cover it there)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -166,4 +168,25 @@ def test_sw2d_program_initial_and_final_states_bitwise(oracle):
     U, t, n = oracle.sw2d_run(cfg, U0, 1 << 30, 0.5 * cfg.h * 0.5 / 1.0, t_final=1.0, stepper=1)
     assert np.array_equal(U, U1)
     assert oracle.sw2d_errors(cfg, U, 1.0) == (l2, li)
+
+
+@pytest.mark.parametrize("bc", [(2,) * 6, (0,) * 6, (1, 2, 0, 0, 2, 1)])
+def test_mp3d_rhs_and_run_bitwise(oracle, bc):
+    """3d/weno4/Viscous-Multiphase-Fourth-Order (RHSFunctionPrimitive) on fresh states"""
+    _need_ref(oracle)
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_golden import mp3d_state
+
+    n = (6, 7, 5)
+    cfg = oracle.mp3d_cfg(n, 0.1, cfl=0.8, bc=bc)
+    U = mp3d_state(cfg, n, 61)
+    R1, dt1, _, _, rc1 = oracle.mp3d_rhs(cfg, U)
+    R2, dt2, rc2 = oracle.ref_mp3d_rhs(cfg, U)
+    assert rc1 == rc2 == 0
+    assert np.array_equal(R1, R2) and dt1 == dt2
+    U1, t1, d1, r1 = oracle.mp3d_run(cfg, U, 2)
+    U2, t2, d2, r2 = oracle.ref_mp3d_run(cfg, U, 2)
+    assert r1 == r2 == 0
+    assert np.array_equal(U1, U2) and t1 == t2 and d1 == d2
 
