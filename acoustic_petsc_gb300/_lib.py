@@ -48,7 +48,8 @@ SYMBOLS = [
     "hype_mlp_nparam", "hype_mlp_score", "hype_mlp_grad", "hype_mlp_train", "hype_euler_shadow_step",
     "hype_euler_monitor", "hype_acoustic2d_create", "hype_acoustic2d_destroy", "hype_acoustic2d_upload",
     "hype_acoustic2d_download", "hype_acoustic2d_rhs", "hype_acoustic2d_step", "hype_acoustic2d_sync",
-    "hype_acoustic2d_stream",
+    "hype_acoustic2d_stream", "hype_mp3d_create", "hype_mp3d_destroy", "hype_mp3d_get_params", "hype_mp3d_rhs",
+    "hype_mp3d_upload", "hype_mp3d_download", "hype_mp3d_step", "hype_mp3d_sync", "hype_mp3d_stream",
 ]
 
 
@@ -84,6 +85,13 @@ class AcousticParams(C.Structure):
 
 class Status(C.Structure):
     _fields_ = [("bad_cell", C.c_longlong), ("smax", C.c_double), ("rhs_evals", C.c_longlong)]
+
+
+class Mp3dParams(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("x_min", C.c_double), ("y_min", C.c_double),
+                ("z_min", C.c_double), ("h", C.c_double), ("cfl", C.c_double), ("bc", C.c_int * 6),
+                ("g1", C.c_double), ("p1", C.c_double), ("g2", C.c_double), ("p2", C.c_double), ("mu1", C.c_double),
+                ("mu2", C.c_double), ("dt_mode", C.c_int)]
 
 
 class Acoustic2dParams(C.Structure):
@@ -198,6 +206,15 @@ def lib():
         "hype_acoustic2d_step": ([V, C.c_int, C.c_double, D, I], C.c_int),
         "hype_acoustic2d_sync": ([V], C.c_int),
         "hype_acoustic2d_stream": ([V], C.c_void_p),
+        "hype_mp3d_create": ([P(Mp3dParams), P(V)], C.c_int),
+        "hype_mp3d_destroy": ([V], None),
+        "hype_mp3d_get_params": ([V, P(Mp3dParams)], C.c_int),
+        "hype_mp3d_rhs": ([V, C.c_double, D, D, D], C.c_int),
+        "hype_mp3d_upload": ([V, D], C.c_int),
+        "hype_mp3d_download": ([V, D], C.c_int),
+        "hype_mp3d_step": ([V, C.c_int, D, D, P(C.c_longlong)], C.c_int),
+        "hype_mp3d_sync": ([V], C.c_int),
+        "hype_mp3d_stream": ([V], C.c_void_p),
         "hype_euler_set_mlp": ([V, F, C.c_float], C.c_int),
         "hype_euler_set_recon": ([V, C.c_int], C.c_int),
         "hype_euler_indicator_stats": ([V, P(C.c_longlong), P(C.c_longlong), C.c_int], C.c_int),

@@ -283,6 +283,42 @@ int hype_acoustic_step(hype_acoustic* a, int nsteps, double t_final, double* t_i
 int hype_acoustic_sync(hype_acoustic* a);
 void* hype_acoustic_stream(hype_acoustic* a);
 
+/* ============================================================ 3D multiphase */
+/* The primitive-variable multiphase RHS of 3d/weno4/Viscous-Multiphase-Fourth-Order
+ * (RHSFunctionPrimitive, rhs_function.c:56-570): Q = (rho, rho u, rho v, rho w, E, phi),
+ * AoS [k][j][i][6]; the mixture of two stiffened gases (g, p_inf) mixed by phi
+ * (pde.c:9-45); CWENO4 of the primitive variables with the 33-node density / pressure
+ * check and first order on failure; rotated HLLC (pde.c:383-440) with the
+ * non-conservative phi equation; SSP RKS3/4 stages; dt = (1/3) CFL h / (s_max +
+ * 2 s_visc / h) with s_visc = (4/3)(phi mu1 + (1 - phi) mu2)/rho (rhs_function.c:559).
+ * The program's viscous flux reads gradients its weno() never writes (zero when its
+ * automatic variables start at zero): no viscous flux is applied, only its speed
+ * limits dt (mu1 = mu2 = 0 for the inviscid CFL limit). */
+typedef struct hype_mp3d hype_mp3d;
+
+typedef struct {
+    int nx, ny, nz;
+    double x_min, y_min, z_min, h;
+    double cfl;
+    int bc[6];                  /* HYPE_BC_PERIODIC / REFLECTIVE / TRANSMISSIVE */
+    double g1, p1, g2, p2;      /* phase EOS (hype.h:39-42 of the program: 1.4, 0, 1.6, 0) */
+    double mu1, mu2;            /* phase viscosities of the dt limit (MU_1 1.4, MU_2 1.6) */
+    int dt_mode;                /* HYPE_DT_* */
+} hype_mp3d_params;
+
+int hype_mp3d_create(const hype_mp3d_params* p, hype_mp3d** out);
+void hype_mp3d_destroy(hype_mp3d* m);
+int hype_mp3d_get_params(const hype_mp3d* m, hype_mp3d_params* out);
+/* Drop-in for RHSFunctionPrimitive (rhs_function.c:56); *dt_out: the Ctx->dt it sets */
+int hype_mp3d_rhs(hype_mp3d* m, double t, const double* U_aos, double* RHS_aos, double* dt_out);
+int hype_mp3d_upload(hype_mp3d* m, const double* U_aos);
+int hype_mp3d_download(hype_mp3d* m, double* U_aos);
+/* nsteps of SSP RKS3/4 stages on the resident state (dt semantics as hype_euler_step);
+ * *fallback_cells: owned-cell reconstructions that fell back to first order */
+int hype_mp3d_step(hype_mp3d* m, int nsteps, double* t_inout, double* dt_inout, long long* fallback_cells);
+int hype_mp3d_sync(hype_mp3d* m);
+void* hype_mp3d_stream(hype_mp3d* m);
+
 /* ---- 2D acoustic FV: 2d/weno4/standing_wave ----
  * The same system in 2D: state AoS [j][i][2] = (u, u_t); the 2D R4 polynomial of u
  * (weno(), reconstruction.c:108-125), its normal gradient at 2 Gauss points per edge,
