@@ -163,3 +163,38 @@ def kapila_bubble(n: int = 1024, model: int = 1, smear: float = 2.0, eps: float 
         V[..., 3] = p
         V[..., 4] = a_water
     return _prim2cons_mp(model, KAPILA_EOS, V), h
+
+
+MP3D_EOS = (1.4, 0.0, 1.6, 0.0)  # 3d/weno4/Viscous-Multiphase-Fourth-Order/hype.h:39-42
+
+
+def mp3d_prim2cons(V: np.ndarray, eos=MP3D_EOS) -> np.ndarray:
+    """PDEPrim2Cons of the 3D multiphase program (pde.c:27-45), vectorised"""
+    g1, p1, g2, p2 = eos
+    phi = V[..., 5]
+    g = 1.0 + (g1 - 1.0) * (g2 - 1.0) / ((1.0 - phi) * (g1 - 1.0) + phi * (g2 - 1.0))
+    pinf = ((g - 1.0) / g) * (g1 * p1 * phi / (g1 - 1.0) + g2 * p2 * (1.0 - phi) / (g2 - 1.0))
+    Q = np.empty_like(V)
+    Q[..., 0] = V[..., 0]
+    Q[..., 1:4] = V[..., 0:1] * V[..., 1:4]
+    Q[..., 4] = 0.5 * V[..., 0] * (V[..., 1] ** 2 + V[..., 2] ** 2 + V[..., 3] ** 2) + (V[..., 4] + g * pinf) / (g - 1.0)
+    Q[..., 5] = phi
+    return Q
+
+
+def mp3d_layers(nx: int, ny: int, nz: int, eos=MP3D_EOS, width: float = 0.02) -> np.ndarray:
+    """the layered set-up of 3d/weno4/Viscous-Multiphase-Fourth-Order/initial_condition.c on
+    z in [-1/2, 1/2]: a shocked layer (rho 1.3765, w 0.3948, p 1.57) below z = -0.25, the same
+    phase at rest, a light-gas layer (rho 0.138, phi 0) for |z| < 0.1, the phase at rest above;
+    the interfaces smoothed over `width`; AoS [k][j][i][6]"""
+    z = -0.5 + (np.arange(nz) + 0.5) / nz
+    s = lambda a: 0.5 * (1.0 + np.tanh(a / width))
+    w_shock = 1.0 - s(z + 0.25)
+    w_gas = s(z + 0.1) * (1.0 - s(z - 0.1))
+    V = np.zeros((nz, ny, nx, 6))
+    V[..., 0] = (1.0 + 0.3765 * w_shock - 0.862 * w_gas)[:, None, None]
+    V[..., 3] = (0.3948 * w_shock)[:, None, None]
+    V[..., 4] = (1.0 + 0.57 * w_shock)[:, None, None]
+    V[..., 5] = (1.0 - w_gas)[:, None, None]
+    return mp3d_prim2cons(V, eos)
+

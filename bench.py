@@ -11,7 +11,7 @@ cell-updates/s (cells x steps / s).
 Other workloads (--workload): euler256_fp32 (FP32 reconstruction/flux, FP64
 state), euler256_linear (optimal-weight linear reconstruction), euler256_weno3,
 euler256_hllc, ns256_tgv (viscous Taylor-Green), acoustic256 (3D acoustic FV),
-sw2d4096 (2D standing wave, RK104), kapila1024[_fp32|_learned], blast256/512,
+sw2d4096 (2D standing wave, RK104), mp3d256 (3D primitive multiphase), kapila1024[_fp32|_learned], blast256/512,
 ctcs512 (2D CTCS 512^2), batch256 (256 batched monopole CTCS instances).
 --grid N sets the cells per axis of the 3D Euler / Navier-Stokes and 2D acoustic
 workloads (small cases for profiling).
@@ -744,6 +744,68 @@ def run_sw2d(args, ws, rank, local, n=4096):
             "gpu_launches": launches, "clocks": clk.summary()}
 
 
+def run_mp3d(args, ws, rank, local, n=256):
+    """3D primitive multiphase (3d/weno4/Viscous-Multiphase-Fourth-Order) at n^3: the program's
+    layered shock / gas-layer set-up along z, transmissive, CFL 0.9, its EOS and viscous dt limit"""
+    import torch
+
+    import acoustic_petsc_gb300 as H
+    from acoustic_petsc_gb300 import workloads
+
+    L = H.lib()
+    H._lib.check(L.hype_set_device(local), "hype_set_device")
+    torch.cuda.set_device(local)
+    n = args.grid or n
+    h = 1.0 / n
+    U0 = workloads.mp3d_layers(n, n, n)
+    s = H.Multiphase3D(n, n, n, h, CFL=0.9, x_min=-0.5, y_min=-0.5, z_min=-0.5)
+    s.set_state(U0)
+    s.step(max(args.warmup, 3))
+    stream = torch.cuda.ExternalStream(L.hype_mp3d_stream(s._h))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = H.launches()
+    _barrier(ws)
+    torch.cuda.synchronize()
+    with Clocks(_gpu_index(local)) as clk:
+        e0.record(stream)
+        s.step(args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    launches = H.launches() - l0
+    ms = _max_over_ranks(ws, e0.elapsed_time(e1))
+    cells = n**3
+    value = ws * cells * args.steps / (ms * 1e-3)
+    peak, kind = _peaks()
+    bytes_cu = 4 * 96 + 48  # per stage read + write of 6 doubles, one extra read of u^n per step
+    ach = bytes_cu * cells * args.steps / (ms * 1e-3) / 1e9
+    host = torch.empty((n, n, n, 6), dtype=torch.float64, pin_memory=True)
+    hv = host.numpy()
+    hv[...] = U0
+    ke = max(1, min(2, args.steps))
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        s.set_state(hv)
+        s.step(1)
+        H._lib.check(L.hype_mp3d_download(s._h, hv.ctypes.data_as(H._lib.D)), "download")
+    wall = time.perf_counter() - t0
+    ms_e2e = _max_over_ranks(ws, wall * 1e3)
+    s.close()
+    nb = cells * 6 * 8
+    return {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: the program's z-layered shock / light-gas set-up, interfaces smoothed over 0.02",
+            "config": {"workload": f"mphase3d_layers_{n}", "grid": [n, n, n], "cfl": 0.9,
+                       "scheme": "primitive CWENO4 + 33-node PAD + rotated HLLC + SSPRK(4,3), "
+                                 "3d/weno4/Viscous-Multiphase-Fourth-Order",
+                       "l2": f"state 6*8*{n}^3 B = {48 * cells / 1e6:.0f} MB vs 129 MB; no flush"},
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "algorithmic_bytes_per_cell_update": bytes_cu, "traffic": None},
+            "e2e": {"value": ws * cells * ke / (ms_e2e * 1e-3), "unit": "cell-updates/s", "h2d_bytes_per_step": nb,
+                    "d2h_bytes_per_step": nb, "steps": ke, "path": "Multiphase3D.set_state -> step(1) -> get_state"},
+            "gpu_launches": launches, "clocks": clk.summary()}
+
+
 WORKLOADS = {
     "blast512": run_blast,
     "blast256": lambda a, *r: run_blast(a, *r, n=256),
@@ -762,6 +824,7 @@ WORKLOADS = {
     "euler128": lambda a, *r: run_euler(a, *r, precision=0, recon=0, n=128),
     "euler128_fp32": lambda a, *r: run_euler(a, *r, precision=1, recon=0, n=128),
     "sw2d4096": run_sw2d,
+    "mp3d256": run_mp3d,
     "ctcs512": run_ctcs,
     "batch256": run_batch,
 }
@@ -829,6 +892,20 @@ def main():
             d = time.perf_counter() - t0
             out["cpu_baseline"] = {"value": n * n * 4 / d, "unit": "cell-updates/s", "cores": O.threads(),
                                    "kind": "port", "sample": f"4 SSPRK(4,3) steps of the {n}^2 version ({d:.1f} s)"}
+        elif args.workload.startswith("mp3d"):
+            from acoustic_petsc_gb300 import workloads
+            from oracle import pyoracle as O
+
+            O.build(None)
+            n = 48
+            cfg = O.mp3d_cfg(n, 1.0 / n, cfl=0.9, bc=(2,) * 6, nthreads=os.cpu_count() or 1)
+            U0 = workloads.mp3d_layers(n, n, n)
+            O.mp3d_run(cfg, U0, 1)
+            t0 = time.perf_counter()
+            O.mp3d_run(cfg, U0, 2)
+            d = time.perf_counter() - t0
+            out["cpu_baseline"] = {"value": n**3 * 2 / d, "unit": "cell-updates/s", "cores": O.threads(),
+                                   "kind": "port", "sample": f"2 SSPRK(4,3) steps of the {n}^3 layered set-up ({d:.1f} s)"}
         elif args.workload.startswith("sw2d"):
             from oracle import pyoracle as O
 
