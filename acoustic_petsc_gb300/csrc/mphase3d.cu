@@ -81,144 +81,139 @@ __device__ __forceinline__ void cons2prim(const Eos& e, const double* Q, double*
     V[5] = Q[5];
 }
 
-// PDEConsFluxPrim (pde.c:142-202) with PDEPrim2Cons's E; bad on inadmissible input
-__device__ __forceinline__ double cons_flux_prim(const Eos& e, const double* V, double nx, double ny, double nz, double* F,
-                                                 double& E, bool& bad) {
-    const double phi = V[5];
-    const double g = mix_g(e, phi);
-    const double P_inf = mix_pinf(e, g, phi);
-    const double rho = V[0], u = V[1], v = V[2], w = V[3], p = V[4];
-    const double en = (p + g * P_inf) / (g - 1.0);
-    E = 0.5 * rho * (u * u + v * v + w * w) + en;
-    const double un = nx * u + ny * v + nz * w;
-    if (rho < RHO_FLOOR || (p + P_inf) < PRS_FLOOR) bad = true;
-    F[0] = rho * un;
-    F[1] = rho * u * un + p * nx;
-    F[2] = rho * v * un + p * ny;
-    F[3] = rho * w * un + p * nz;
-    F[4] = (E + p) * un;
-    F[5] = phi * un;
-    F[6] = 0.0;
-    return fabs(un) + sqrt(g * (p + P_inf) / rho);
+// One side of a face: the primitive trace and what PDEConsFluxPrim / PDEPrim2Cons derive
+// from it that does not depend on the normal (pde.c:142-202, 27-45): mixture gamma and
+// P_inf, total energy, sound speed.  Computed once per trace instead of once per HLLC
+// evaluation (the rotated solver makes three).
+struct Side {
+    double rho, u, v, w, p, phi, E, a;
+};
+
+__device__ __forceinline__ Side make_side(const Eos& e, const double* V, bool& bad) {
+    Side s;
+    s.rho = V[0]; s.u = V[1]; s.v = V[2]; s.w = V[3]; s.p = V[4]; s.phi = V[5];
+    const double g = mix_g(e, s.phi);
+    const double P_inf = mix_pinf(e, g, s.phi);
+    s.E = 0.5 * s.rho * (s.u * s.u + s.v * s.v + s.w * s.w) + (s.p + g * P_inf) / (g - 1.0);
+    if (s.rho < RHO_FLOOR || (s.p + P_inf) < PRS_FLOOR) bad = true;
+    s.a = sqrt(g * (s.p + P_inf) / s.rho);
+    return s;
 }
 
-// the tangent pair of Miller and Colella for the unit normal n; rot selects the form of
-// t2z that PDErotHLLCRiemannSolver uses (pde.c:407-422) instead of PDEHLLCRiemannSolver's (:296-312)
-__device__ __forceinline__ void tangents(double nx, double ny, double nz, bool rot, double* t1, double* t2) {
-    if (fabs(ny + nz) > fabs(ny - nz)) {
-        const double il = 1.0 / sqrt(2.0 * (1.0 + nz * (ny - nx) + nx * ny));
-        t1[0] = (ny + nz) * il; t1[1] = (nz - nx) * il; t1[2] = -(nx + ny) * il;
-        t2[0] = (nx * (nz - ny) - ny * ny - nz * nz) * il;
-        t2[1] = (ny * (nx + nz) + nx * nx + nz * nz) * il;
-        t2[2] = ((rot ? nz * (nx - ny) : nz * (nx - nz)) - nx * nx - ny * ny) * il;
-    } else {
-        const double il = 1.0 / sqrt(2.0 * (1.0 - nx * ny - nx * nz - ny * nz));
-        t1[0] = (ny - nz) * il; t1[1] = (nz - nx) * il; t1[2] = (nx - ny) * il;
-        t2[0] = (nx * (ny + nz) - ny * ny - nz * nz) * il;
-        t2[1] = (ny * (nx + nz) - nx * nx - nz * nz) * il;
-        t2[2] = (nz * (nx + ny) - nx * nx - ny * ny) * il;
-    }
-}
-
-// PDEHLLCRiemannSolver (pde.c:273-379) for a unit normal n, 7 flux components
-__device__ __forceinline__ double hllc7(const Eos& e, const double* VL, const double* VR, double nx, double ny, double nz,
-                                        double* Flux, bool& bad) {
-    double FL[MF], FR[MF], t1[3], t2[3], E_L, E_R;
-    const double smaxl = cons_flux_prim(e, VL, nx, ny, nz, FL, E_L, bad);
-    const double smaxr = cons_flux_prim(e, VR, nx, ny, nz, FR, E_R, bad);
-    tangents(nx, ny, nz, false, t1, t2);
-    // inverse of the rotation [n; t1; t2] (invert3x3matrix, pde.c:255-271)
-    const double M[3][3] = {{nx, ny, nz}, {t1[0], t1[1], t1[2]}, {t2[0], t2[1], t2[2]}};
-    const double t4 = M[0][0] * M[1][1], t6 = M[0][0] * M[1][2], t8 = M[0][1] * M[1][0], t00 = M[0][2] * M[1][0],
-                 t01 = M[0][1] * M[2][0], t04 = M[0][2] * M[2][0],
-                 t07 = 1.0 / (t4 * M[2][2] - t6 * M[2][1] - t8 * M[2][2] + t00 * M[2][1] + t01 * M[1][2] - t04 * M[1][1]);
-    double iM[3][3];
-    iM[0][0] = (M[1][1] * M[2][2] - M[1][2] * M[2][1]) * t07;
-    iM[0][1] = -(M[0][1] * M[2][2] - M[0][2] * M[2][1]) * t07;
-    iM[0][2] = -(-M[0][1] * M[1][2] + M[0][2] * M[1][1]) * t07;
-    iM[1][0] = -(M[1][0] * M[2][2] - M[1][2] * M[2][0]) * t07;
-    iM[1][1] = (M[0][0] * M[2][2] - t04) * t07;
-    iM[1][2] = -(t6 - t00) * t07;
-    iM[2][0] = -(-M[1][0] * M[2][1] + M[1][1] * M[2][0]) * t07;
-    iM[2][1] = -(M[0][0] * M[2][1] - t01) * t07;
-    iM[2][2] = (t4 - t8) * t07;
-    const double rho_L = VL[0], P_L = VL[4], rho_R = VR[0], P_R = VR[4];
-    const double un_L = VL[1] * nx + VL[2] * ny + VL[3] * nz, ut1_L = VL[1] * t1[0] + VL[2] * t1[1] + VL[3] * t1[2],
-                 ut2_L = VL[1] * t2[0] + VL[2] * t2[1] + VL[3] * t2[2];
-    const double un_R = VR[1] * nx + VR[2] * ny + VR[3] * nz, ut1_R = VR[1] * t1[0] + VR[2] * t1[1] + VR[3] * t1[2],
-                 ut2_R = VR[1] * t2[0] + VR[2] * t2[1] + VR[3] * t2[2];
-    const double c_L = smaxl - fabs(un_L), c_R = smaxr - fabs(un_R);
-    const double S_L = fmin(un_R - c_R, un_L - c_L);
-    const double S_R = fmax(un_L + c_L, un_R + c_R);
-    const double S_star = (P_R - P_L + rho_L * un_L * (S_L - un_L) - rho_R * un_R * (S_R - un_R)) /
-                          (rho_L * (S_L - un_L) - rho_R * (S_R - un_R));
-    FL[6] = un_L;
-    FR[6] = un_R;
+// PDEHLLCRiemannSolver (pde.c:273-379) for a unit normal n, 7 flux components.  The
+// reference builds the star-state velocity from (S_star, u.t1, u.t2) in its Miller-Colella
+// frame M = [n; t1; t2] and the inverse of M (pde.c:290-323); since M^-1 M u = u, that
+// velocity is u + (S_star - u.n) c with c the first column of M^-1, (t1 x t2) / det M.
+// The frame's t2z of the first branch (pde.c:302) is not the one of n x t1, so M is not
+// orthonormal and c is not n: c is formed from the reference's t1, t2 as they are.
+__device__ __forceinline__ double hllc7(const Side& L, const Side& R, double nx, double ny, double nz, double* Flux) {
+    const double un_L = L.u * nx + L.v * ny + L.w * nz, un_R = R.u * nx + R.v * ny + R.w * nz;
+    const double S_L = fmin(un_R - R.a, un_L - L.a);
+    const double S_R = fmax(un_L + L.a, un_R + R.a);
+    const double S_star = (R.p - L.p + L.rho * un_L * (S_L - un_L) - R.rho * un_R * (S_R - un_R)) /
+                          (L.rho * (S_L - un_L) - R.rho * (S_R - un_R));
     // the reference's branch order (pde.c:368-376); with S_L == 0 and S_star >= 0 it leaves
     // the flux unset, here zero
     const int sel = (S_L > 0.0) ? 0 : (S_star >= 0.0 && S_L < 0.0) ? 1 : (S_star < 0.0 && S_R >= 0.0) ? 2
                                 : (S_R < 0.0) ? 3 : 4;
-    if (sel == 0 || sel == 3) {
-#pragma unroll
-        for (int i = 0; i < MF; ++i) Flux[i] = sel == 0 ? FL[i] : FR[i];
-    } else if (sel == 4) {
+    if (sel == 4) {
 #pragma unroll
         for (int i = 0; i < MF; ++i) Flux[i] = 0.0;
-    } else {
-        // the star state on the side of S_star (pde.c:340-366)
-        const bool left = sel == 1;
-        const double* V = left ? VL : VR;
-        const double* Fs = left ? FL : FR;
-        const double S = left ? S_L : S_R, un_s = left ? un_L : un_R, rho = left ? rho_L : rho_R, P = left ? P_L : P_R;
-        const double Es = left ? E_L : E_R;
-        const double ut1 = left ? ut1_L : ut1_R, ut2 = left ? ut2_L : ut2_R;
-        const double r = (S - un_s) / (S - S_star);
-        const double q0 = rho * (S - un_s) / (S - S_star);
-        const double Qs[MV] = {q0, q0 * (S_star * iM[0][0] + ut1 * iM[0][1] + ut2 * iM[0][2]),
-                               q0 * (S_star * iM[1][0] + ut1 * iM[1][1] + ut2 * iM[1][2]),
-                               q0 * (S_star * iM[2][0] + ut1 * iM[2][1] + ut2 * iM[2][2]),
-                               q0 * ((Es / rho) + (S_star - un_s) * (S_star + P / (rho * (S - un_s)))),
-                               V[5] * (S - un_s) / (S - S_star)};
-        const double Q[MV] = {rho, rho * V[1], rho * V[2], rho * V[3], Es, V[5]};
-#pragma unroll
-        for (int i = 0; i < MV; ++i) Flux[i] = Fs[i] + S * (Qs[i] - Q[i]);
-        Flux[6] = un_s + S * (r - 1.0);
+        return fmax(fabs(un_L) + L.a, fabs(un_R) + R.a);
     }
-    return fmax(smaxl, smaxr);
+    const bool left = sel <= 1;
+    const Side& K = left ? L : R;
+    const double un = left ? un_L : un_R;
+    // the side's flux (PDEConsFluxPrim) and, for the star states, S (Q* - Q)
+    double F[MF];
+    F[0] = K.rho * un;
+    F[1] = K.rho * K.u * un + K.p * nx;
+    F[2] = K.rho * K.v * un + K.p * ny;
+    F[3] = K.rho * K.w * un + K.p * nz;
+    F[4] = (K.E + K.p) * un;
+    F[5] = K.phi * un;
+    F[6] = un;
+    if (sel == 1 || sel == 2) {
+        // the frame of pde.c:290-312 and the first column of its inverse
+        double t1x, t1y, t1z, t2x, t2y, t2z;
+        if (fabs(ny + nz) > fabs(ny - nz)) {
+            const double il = 1.0 / sqrt(2.0 * (1.0 + nz * (ny - nx) + nx * ny));
+            t1x = (ny + nz) * il; t1y = (nz - nx) * il; t1z = -(nx + ny) * il;
+            t2x = (nx * (nz - ny) - ny * ny - nz * nz) * il;
+            t2y = (ny * (nx + nz) + nx * nx + nz * nz) * il;
+            t2z = (nz * (nx - nz) - nx * nx - ny * ny) * il;
+        } else {
+            const double il = 1.0 / sqrt(2.0 * (1.0 - nx * ny - nx * nz - ny * nz));
+            t1x = (ny - nz) * il; t1y = (nz - nx) * il; t1z = (nx - ny) * il;
+            t2x = (nx * (ny + nz) - ny * ny - nz * nz) * il;
+            t2y = (ny * (nx + nz) - nx * nx - nz * nz) * il;
+            t2z = (nz * (nx + ny) - nx * nx - ny * ny) * il;
+        }
+        const double cx = t1y * t2z - t1z * t2y, cy = t1z * t2x - t1x * t2z, cz = t1x * t2y - t1y * t2x;
+        const double idet = 1.0 / (nx * cx + ny * cy + nz * cz);
+        const double S = left ? S_L : S_R;
+        const double isd = 1.0 / (S - S_star);
+        const double q0 = K.rho * (S - un) * isd;
+        const double dn = (S_star - un) * idet;
+        const double Qs[MV] = {q0, q0 * (K.u + dn * cx), q0 * (K.v + dn * cy), q0 * (K.w + dn * cz),
+                               q0 * ((K.E / K.rho) + (S_star - un) * (S_star + K.p / (K.rho * (S - un)))),
+                               K.phi * (S - un) * isd};
+        const double Q[MV] = {K.rho, K.rho * K.u, K.rho * K.v, K.rho * K.w, K.E, K.phi};
+#pragma unroll
+        for (int i = 0; i < MV; ++i) F[i] = F[i] + S * (Qs[i] - Q[i]);
+        F[6] = un + S * (((S - un) * isd) - 1.0);
+    }
+#pragma unroll
+    for (int i = 0; i < MF; ++i) Flux[i] = F[i];
+    return fmax(fabs(un_L) + L.a, fabs(un_R) + R.a);
 }
 
-// PDErotHLLCRiemannSolver (pde.c:383-440): HLLC along the velocity-jump direction and
-// its two tangents, weighted by their projections on the face normal
-__device__ __forceinline__ double rot_hllc7(const Eos& e, const double* VL, const double* VR, double nx, double ny,
-                                            double nz, double* Flux, bool& bad) {
-    const double du = VR[1] - VL[1], dv = VR[2] - VL[2], dw = VR[3] - VL[3];
+// PDErotHLLCRiemannSolver (pde.c:383-440): HLLC along the velocity-jump direction n1 and
+// its two Miller-Colella tangents, weighted by their projections on the face normal
+__device__ __forceinline__ double rot_hllc7(const Side& L, const Side& R, double nx, double ny, double nz, double* Flux) {
+    const double du = R.u - L.u, dv = R.v - L.v, dw = R.w - L.w;
     const double dq = sqrt(du * du + dv * dv + dw * dw);
-    double n1[3];
+    double n1x, n1y, n1z;
     if (dq < 1.0E-10) {
-        n1[0] = nx; n1[1] = ny; n1[2] = nz;
+        n1x = nx; n1y = ny; n1z = nz;
     } else {
-        n1[0] = du / dq; n1[1] = dv / dq; n1[2] = dw / dq;
+        const double idq = 1.0 / dq;
+        n1x = du * idq; n1y = dv * idq; n1z = dw * idq;
     }
-    double a1 = n1[0] * nx + n1[1] * ny + n1[2] * nz;
+    double a1 = n1x * nx + n1y * ny + n1z * nz;
     if (a1 < 0.0) {
-        n1[0] = -n1[0]; n1[1] = -n1[1]; n1[2] = -n1[2]; a1 = -a1;
+        n1x = -n1x; n1y = -n1y; n1z = -n1z; a1 = -a1;
     }
-    double t1[3], t2[3];
-    tangents(n1[0], n1[1], n1[2], true, t1, t2);
-    double a2 = t1[0] * nx + t1[1] * ny + t1[2] * nz;
+    double t1x, t1y, t1z, t2x, t2y, t2z;
+    if (fabs(n1y + n1z) > fabs(n1y - n1z)) {
+        const double il = 1.0 / sqrt(2.0 * (1.0 + n1z * (n1y - n1x) + n1x * n1y));
+        t1x = (n1y + n1z) * il; t1y = (n1z - n1x) * il; t1z = -(n1x + n1y) * il;
+        t2x = (n1x * (n1z - n1y) - n1y * n1y - n1z * n1z) * il;
+        t2y = (n1y * (n1x + n1z) + n1x * n1x + n1z * n1z) * il;
+        t2z = (n1z * (n1x - n1y) - n1x * n1x - n1y * n1y) * il;
+    } else {
+        const double il = 1.0 / sqrt(2.0 * (1.0 - n1x * n1y - n1x * n1z - n1y * n1z));
+        t1x = (n1y - n1z) * il; t1y = (n1z - n1x) * il; t1z = (n1x - n1y) * il;
+        t2x = (n1x * (n1y + n1z) - n1y * n1y - n1z * n1z) * il;
+        t2y = (n1y * (n1x + n1z) - n1x * n1x - n1z * n1z) * il;
+        t2z = (n1z * (n1x + n1y) - n1x * n1x - n1y * n1y) * il;
+    }
+    double a2 = t1x * nx + t1y * ny + t1z * nz;
     if (a2 < 0.0) {
-        t1[0] = -t1[0]; t1[1] = -t1[1]; t1[2] = -t1[2]; a2 = -a2;
+        t1x = -t1x; t1y = -t1y; t1z = -t1z; a2 = -a2;
     }
-    double a3 = t2[0] * nx + t2[1] * ny + t2[2] * nz;
+    double a3 = t2x * nx + t2y * ny + t2z * nz;
     if (a3 < 0.0) {
-        t2[0] = -t2[0]; t2[1] = -t2[1]; t2[2] = -t2[2]; a3 = -a3;
+        t2x = -t2x; t2y = -t2y; t2z = -t2z; a3 = -a3;
     }
-    double F1[MF], F2[MF];
-    const double s1 = hllc7(e, VL, VR, n1[0], n1[1], n1[2], F1, bad);
-    const double s2 = hllc7(e, VL, VR, t1[0], t1[1], t1[2], F2, bad);
+    double F1[MF];
+    const double s1 = hllc7(L, R, n1x, n1y, n1z, F1);
 #pragma unroll
-    for (int c = 0; c < MF; ++c) Flux[c] = a1 * F1[c] + a2 * F2[c];
-    const double s3 = hllc7(e, VL, VR, t2[0], t2[1], t2[2], F1, bad);
+    for (int c = 0; c < MF; ++c) Flux[c] = a1 * F1[c];
+    const double s2 = hllc7(L, R, t1x, t1y, t1z, F1);
+#pragma unroll
+    for (int c = 0; c < MF; ++c) Flux[c] += a2 * F1[c];
+    const double s3 = hllc7(L, R, t2x, t2y, t2z, F1);
 #pragma unroll
     for (int c = 0; c < MF; ++c) Flux[c] += a3 * F1[c];
     return fmax(s1, fmax(s2, s3));
@@ -458,7 +453,8 @@ __global__ void __launch_bounds__(128) k_m3_faces(const double* __restrict__ T, 
                 VL[c] = __ldg(T + ((long long)c * NTR + (2 * D + 1) * 4 + gp) * g.NE + eL);
                 VR[c] = __ldg(T + ((long long)c * NTR + (2 * D) * 4 + gp) * g.NE + eR);
             }
-            const double s = rot_hllc7(e, VL, VR, D == 0 ? 1.0 : 0.0, D == 1 ? 1.0 : 0.0, D == 2 ? 1.0 : 0.0, fc, bad);
+            const Side SL = make_side(e, VL, bad), SR = make_side(e, VR, bad);
+            const double s = rot_hllc7(SL, SR, D == 0 ? 1.0 : 0.0, D == 1 ? 1.0 : 0.0, D == 2 ? 1.0 : 0.0, fc);
             smax = fmax(smax, s);
             if (visc) {  // PDEViscFluxPrim's speed (4/3) mu / rho on both sides
                 const double r4_3 = 4. / 3;
