@@ -168,6 +168,22 @@ int orc_mp3d_rhs(const orc_mp3d_cfg* e, const double* U, double* RHS, double* dt
 int orc_mp3d_run(const orc_mp3d_cfg* e, int nsteps, int dt_mode, double* U, double* t_inout, double* dt_inout);
 long orc_mp3d_fallbacks(int reset);
 
+/* 2D path-conservative RHS of 2d/HyPE-2D with its Kapila five-equation model:
+ * Q = (a1 rho1, a2 rho2, rho u, rho v, E, a1), reconstruction of the conservative
+ * variables of order N (0..3), admissibility at the nodes with first order on failure,
+ * Rusanov flux + Roe-path fluctuation, the non-conservative volume term, and dt =
+ * CFL h / (2 s_max).  bc[4]: 0 periodic, 1 reflective, 2 transmissive. */
+typedef struct {
+    int N, nx, ny;
+    double h, cfl;
+    int bc[4];
+    double g1, p1, g2, p2;
+    int nthreads;
+} orc_h2d_cfg;
+/* returns 0, or 2 for an inadmissible face state (the reference aborts) */
+int orc_h2d_rhs(const orc_h2d_cfg* e, const double* U, double* RHS, double* dt_out);
+int orc_h2d_run(const orc_h2d_cfg* e, int nsteps, double* U, double* t_out, double* dt_out);
+
 /* OpenMP threads the restatement runs with */
 int orc_threads(void);
 

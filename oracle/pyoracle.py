@@ -96,6 +96,8 @@ def lib():
         L.orc_mp3d_prim2cons.restype = None
         L.orc_mp3d_cons2prim.argtypes = [C.POINTER(Mp3dCfg), D, D]
         L.orc_mp3d_cons2prim.restype = None
+        L.orc_h2d_rhs.argtypes = [C.POINTER(H2dCfg), D, D, D]
+        L.orc_h2d_run.argtypes = [C.POINTER(H2dCfg), C.c_int, D, D, D]
         L.orc_sw2d_rhs.argtypes = [C.POINTER(Sw2dCfg), D, D]
         L.orc_sw2d_run.argtypes = [C.POINTER(Sw2dCfg), C.c_int, C.c_int, C.c_double, C.c_double, D, D,
                                    C.POINTER(C.c_int)]
@@ -412,6 +414,96 @@ def ref_mp3d_run(cfg, U, nsteps, dt_mode=0):
     rc = _ref_mp3d_lib().ref_mp3d_run(cfg.nx, cfg.ny, cfg.nz, cfg.h, cfg.cfl, bc, int(nsteps), int(dt_mode), _dp(U),
                                       C.byref(t), C.byref(dt))
     return U, t.value, dt.value, rc
+
+
+# ---------------------------------------------------------------- 2D path-conservative (HyPE-2D)
+class H2dCfg(C.Structure):
+    _fields_ = [("N", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("h", C.c_double), ("cfl", C.c_double),
+                ("bc", C.c_int * 4), ("g1", C.c_double), ("p1", C.c_double), ("g2", C.c_double), ("p2", C.c_double),
+                ("nthreads", C.c_int)]
+
+
+# GAMMA_1, PI_1, GAMMA_2, PI_2 compiled into 2d/HyPE-2D (hype.h:41-44)
+H2D_EOS = (1.4, 0.0, 1.4, 0.0)
+
+
+def h2d_cfg(N, nx, ny, h, cfl=0.9, bc=(2,) * 4, eos=H2D_EOS, nthreads=0):
+    c = H2dCfg()
+    c.N, c.nx, c.ny, c.h, c.cfl = N, nx, ny, h, cfl
+    for q in range(4):
+        c.bc[q] = bc[q]
+    c.g1, c.p1, c.g2, c.p2 = eos
+    c.nthreads = nthreads
+    return c
+
+
+def h2d_rhs(cfg, U):
+    """(RHS, dt, status)"""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    dt = C.c_double()
+    rc = lib().orc_h2d_rhs(C.byref(cfg), _dp(U), _dp(R), C.byref(dt))
+    return R, dt.value, rc
+
+
+def h2d_run(cfg, U, nsteps):
+    """nsteps with the program's stepper for N and the dt of the first RHS: (U, t, dt, status)"""
+    U = np.array(U, dtype=np.float64, order="C", copy=True)
+    t, dt = C.c_double(), C.c_double()
+    rc = lib().orc_h2d_run(C.byref(cfg), int(nsteps), _dp(U), C.byref(t), C.byref(dt))
+    return U, t.value, dt.value, rc
+
+
+_ref_h2d = None
+
+
+def _ref_h2d_lib():
+    global _ref_h2d
+    if _ref_h2d is None:
+        L = C.CDLL(os.path.join(HERE, "_ref", "libref_hype2d_kp5.so"))
+        IP = C.POINTER(C.c_int)
+        L.ref_hype2d_rhs.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, IP, D,
+                                     D, D]
+        L.ref_hype2d_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, IP,
+                                     C.c_int, D, D, D]
+        _ref_h2d = L
+    return _ref_h2d
+
+
+def ref_h2d_rhs(cfg, U):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    dt = C.c_double()
+    bc = (C.c_int * 4)(*cfg.bc)
+    rc = _ref_h2d_lib().ref_hype2d_rhs(cfg.N, cfg.nx, cfg.ny, 0.0, 0.0, cfg.h, cfg.cfl, bc, _dp(U), _dp(R),
+                                       C.byref(dt))
+    return R, dt.value, rc
+
+
+def ref_h2d_run(cfg, U, nsteps):
+    U = np.array(U, dtype=np.float64, order="C", copy=True)
+    t, dt = C.c_double(), C.c_double()
+    bc = (C.c_int * 4)(*cfg.bc)
+    rc = _ref_h2d_lib().ref_hype2d_run(cfg.N, cfg.nx, cfg.ny, 0.0, 0.0, cfg.h, cfg.cfl, bc, int(nsteps), _dp(U),
+                                       C.byref(t), C.byref(dt))
+    return U, t.value, dt.value, rc
+
+
+def kp5_state(nx, ny, seed, sharp=False):
+    """a seeded Kapila state Q = (a1 rho1, a2 rho2, rho u, rho v, E, a1) with EOS (1.4, 0, 1.4, 0):
+    a circular region of phase 1 in phase 2, random velocities and pressures"""
+    rng = np.random.default_rng(seed)
+    y, x = (np.arange(ny) + 0.5) / ny, (np.arange(nx) + 0.5) / nx
+    Y, X = np.meshgrid(y, x, indexing="ij")
+    r = np.sqrt((X - 0.5) ** 2 + (Y - 0.5) ** 2)
+    w = 0.01 if sharp else 0.08
+    a1 = 1e-3 + (1 - 2e-3) * 0.5 * (1 - np.tanh((r - 0.25) / w))
+    r1, r2 = 1.0 + 0.1 * rng.random((ny, nx)), 0.125 + 0.01 * rng.random((ny, nx))
+    u, v = 0.1 * rng.standard_normal((ny, nx)), 0.1 * rng.standard_normal((ny, nx))
+    p = 1.0 + 0.1 * rng.random((ny, nx))
+    rho = a1 * r1 + (1 - a1) * r2
+    Q = np.stack([a1 * r1, (1 - a1) * r2, rho * u, rho * v, p / 0.4 + 0.5 * rho * (u * u + v * v), a1], -1)
+    return Q
 
 
 # ---------------------------------------------------------------- 2D acoustic FV (standing_wave)

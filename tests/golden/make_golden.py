@@ -35,6 +35,10 @@ tree is available; the GPU machine has none, so the fixtures are committed).
                            primitive CWENO4, 33-node PAD fallback, rotated HLLC, phi term,
                            viscous speed in dt) and 3 SSP RKS3/4 steps of it; "sharp"
                            trips the fallback
+* ref_h2d_*.npz         -- the path-conservative RHS of 2d/HyPE-2D with its Kapila model
+                           (order N = 1 and 3, Rusanov + Roe-path fluctuation, volume
+                           term, node admissibility) and 3 steps of its stepper for N;
+                           "sharp" states trip the first-order fallback
 * ref_ctcs2d.npz        -- the reference's CTCS() (2d/ctcs/plane_wave/wave.c)
                            on a zero-exterior grid
 * ref_bubble_*.npz      -- the reference's 2D diffuse-interface RHSFunction
@@ -139,6 +143,21 @@ def mp3d_fixtures():
                             mu=np.array(O.MP3D_MU))
 
 
+def h2d_fixtures():
+    """the 2d/HyPE-2D Kapila fixtures (RHS + dt, 3 steps) for N = 1 and N = 3"""
+    for N in (1, 3):
+        for name, bc, seed, sharp in (("mixed", (2, 2, 0, 0), 71, False), ("sharp", (0, 0, 2, 2), 72, True)):
+            nx, ny, h = 9, 8, 1.0 / 9
+            cfg = O.h2d_cfg(N, nx, ny, h, cfl=0.9, bc=bc)
+            U = O.kp5_state(nx, ny, seed + N, sharp)
+            R, dt, rc = O.ref_h2d_rhs(cfg, U)
+            assert rc == 0
+            U3, t3, dt3, rc3 = O.ref_h2d_run(cfg, U, 3)
+            assert rc3 == 0
+            np.savez_compressed(os.path.join(HERE, f"ref_h2d_n{N}_{name}.npz"), U=U, RHS=R, dt=dt, U3=U3, t3=t3,
+                                N=N, nx=nx, ny=ny, h=h, cfl=0.9, bc=np.array(bc), eos=np.array(O.H2D_EOS))
+
+
 def main():
     O.build(REF)
     src = os.path.join(REF, "3d/ctcs/point_source/results/p.dat")
@@ -185,6 +204,7 @@ def main():
     ns3d_fixtures()
     sw2d_fixtures()
     mp3d_fixtures()
+    h2d_fixtures()
     n = 32
     x = -1 + np.arange(n) * (2.0 / n)
     Xg, Yg = np.meshgrid(x, x)

@@ -235,3 +235,23 @@ def test_mp3d_rhs_and_steps_match_reference_bitwise(oracle, name):
     assert rc == 0
     assert np.array_equal(U3, z["U3"]) and t3 == float(z["t3"]) and dt3 == float(z["dt3"])
 
+
+# ---------------------------------------------------------------- 2d/HyPE-2D (Kapila, path-conservative)
+H2D_NAMES = ["n1_mixed", "n1_sharp", "n3_mixed", "n3_sharp"]
+
+
+@pytest.mark.parametrize("name", H2D_NAMES)
+def test_h2d_rhs_and_steps_match_reference_bitwise(oracle, name):
+    """RHSFunction of 2d/HyPE-2D with the Kapila model: reconstruction of order N, node
+    admissibility with the first-order fallback, Rusanov + Roe-path fluctuation and the
+    volume term; dt = CFL h / (2 s_max); 3 steps of the program's stepper for N"""
+    z = np.load(os.path.join(GOLDEN, f"ref_h2d_{name}.npz"))
+    cfg = oracle.h2d_cfg(int(z["N"]), int(z["nx"]), int(z["ny"]), float(z["h"]), cfl=float(z["cfl"]),
+                         bc=tuple(int(b) for b in z["bc"]), eos=tuple(float(v) for v in z["eos"]))
+    R, dt, rc = oracle.h2d_rhs(cfg, z["U"])
+    assert rc == 0
+    assert np.array_equal(R, z["RHS"]) and dt == float(z["dt"])
+    U3, t3, dt3, rc = oracle.h2d_run(cfg, z["U"], 3)
+    assert rc == 0
+    assert np.array_equal(U3, z["U3"]) and t3 == float(z["t3"])
+
