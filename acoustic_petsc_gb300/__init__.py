@@ -7,10 +7,10 @@ package only binds it (``_lib``) and mirrors the reference's operator interface
 """
 from . import _build, _lib
 from ._lib import HypeError, lib, launches
-from .hype import (AcousticFV2D, AcousticFV3D, AppCtx, BatchLeapfrog, CTCS, EulerSolver, Leapfrog, Monopole, Multiphase2D, Multiphase3D, read_petsc_vec,
+from .hype import (AcousticFV2D, AcousticFV3D, AppCtx, BatchLeapfrog, CTCS, EulerSolver, Leapfrog, Monopole, Multiphase2D, Multiphase3D, PathConservative2D, read_petsc_vec,
                    write_petsc_vec, write_vtk)
 
-__all__ = ["AcousticFV2D", "AcousticFV3D", "AppCtx", "BatchLeapfrog", "CTCS", "EulerSolver", "HypeError", "Leapfrog", "Monopole", "Multiphase2D", "Multiphase3D", "lib", "launches",
+__all__ = ["AcousticFV2D", "AcousticFV3D", "AppCtx", "BatchLeapfrog", "CTCS", "EulerSolver", "HypeError", "Leapfrog", "Monopole", "Multiphase2D", "Multiphase3D", "PathConservative2D", "lib", "launches",
            "build", "read_petsc_vec", "write_petsc_vec", "write_vtk"]
 
 

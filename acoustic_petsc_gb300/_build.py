@@ -16,9 +16,10 @@ LIBDIR = os.path.join(PKG, "lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libhype_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-# per-file extra flags: the CTCS, 2D multiphase and 2D acoustic kernels keep the reference's
+# per-file extra flags: the CTCS, 2D multiphase, 2D acoustic and path-conservative kernels keep the reference's
 # rounding (no FMA contraction): results bit-identical to the CPU restatement
-EXTRA = {"ctcs.cu": ["-fmad=false"], "mphase2d.cu": ["-fmad=false"], "acoustic2d.cu": ["-fmad=false"]}
+EXTRA = {"ctcs.cu": ["-fmad=false"], "mphase2d.cu": ["-fmad=false"], "acoustic2d.cu": ["-fmad=false"],
+         "pc2d.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:

@@ -50,6 +50,8 @@ SYMBOLS = [
     "hype_acoustic2d_download", "hype_acoustic2d_rhs", "hype_acoustic2d_step", "hype_acoustic2d_sync",
     "hype_acoustic2d_stream", "hype_mp3d_create", "hype_mp3d_destroy", "hype_mp3d_get_params", "hype_mp3d_rhs",
     "hype_mp3d_upload", "hype_mp3d_download", "hype_mp3d_step", "hype_mp3d_sync", "hype_mp3d_stream",
+    "hype_pc2d_create", "hype_pc2d_destroy", "hype_pc2d_get_params", "hype_pc2d_rhs", "hype_pc2d_upload",
+    "hype_pc2d_download", "hype_pc2d_step", "hype_pc2d_sync", "hype_pc2d_stream",
 ]
 
 
@@ -85,6 +87,12 @@ class AcousticParams(C.Structure):
 
 class Status(C.Structure):
     _fields_ = [("bad_cell", C.c_longlong), ("smax", C.c_double), ("rhs_evals", C.c_longlong)]
+
+
+class Pc2dParams(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("x_min", C.c_double), ("y_min", C.c_double), ("h", C.c_double),
+                ("cfl", C.c_double), ("bc", C.c_int * 4), ("order", C.c_int), ("g1", C.c_double), ("p1", C.c_double),
+                ("g2", C.c_double), ("p2", C.c_double)]
 
 
 class Mp3dParams(C.Structure):
@@ -215,6 +223,15 @@ def lib():
         "hype_mp3d_step": ([V, C.c_int, D, D, P(C.c_longlong)], C.c_int),
         "hype_mp3d_sync": ([V], C.c_int),
         "hype_mp3d_stream": ([V], C.c_void_p),
+        "hype_pc2d_create": ([P(Pc2dParams), P(V)], C.c_int),
+        "hype_pc2d_destroy": ([V], None),
+        "hype_pc2d_get_params": ([V, P(Pc2dParams)], C.c_int),
+        "hype_pc2d_rhs": ([V, C.c_double, D, D, D], C.c_int),
+        "hype_pc2d_upload": ([V, D], C.c_int),
+        "hype_pc2d_download": ([V, D], C.c_int),
+        "hype_pc2d_step": ([V, C.c_int, D, D, P(C.c_longlong)], C.c_int),
+        "hype_pc2d_sync": ([V], C.c_int),
+        "hype_pc2d_stream": ([V], C.c_void_p),
         "hype_euler_set_mlp": ([V, F, C.c_float], C.c_int),
         "hype_euler_set_recon": ([V, C.c_int], C.c_int),
         "hype_euler_indicator_stats": ([V, P(C.c_longlong), P(C.c_longlong), C.c_int], C.c_int),

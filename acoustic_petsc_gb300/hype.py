@@ -625,3 +625,71 @@ class Multiphase3D:
         self.t, self.next_dt, self.fallback_cells = t.value, d.value, fb.value
         check(rc, "hype_mp3d_step")
 
+
+class PathConservative2D:
+    """The path-conservative 2D scheme of 2d/HyPE-2D (RHSFunction) with its Kapila
+    five-equation model on one GPU: Q = (a1 rho1, a2 rho2, rho u, rho v, E, a1), conservative
+    reconstruction of order N = 0..3, node admissibility with first-order fallback, Rusanov
+    flux + Roe-path fluctuation, the non-conservative volume term and the program's stepper
+    for N; bit-identical to the reference.  The default EOS is the program's compiled-in one
+    (hype.h:41-44: both phases gamma 1.4, pi 0)."""
+
+    def __init__(self, N_x, N_y, h, order=1, CFL=0.9, x_min=0.0, y_min=0.0, boundaries=(L.BC_TRANSMISSIVE,) * 4,
+                 eos=(1.4, 0.0, 1.4, 0.0)):
+        p = L.Pc2dParams()
+        p.nx, p.ny, p.x_min, p.y_min, p.h, p.cfl = N_x, N_y, x_min, y_min, h, CFL
+        for q in range(4):
+            p.bc[q] = int(boundaries[q])
+        p.order = order
+        p.g1, p.p1, p.g2, p.p2 = eos
+        self.shape = (N_y, N_x, 6)
+        self.t = 0.0
+        self.next_dt = 0.0
+        self.dt = 0.0
+        self.fallback_cells = 0
+        self._h = C.c_void_p()
+        check(L.lib().hype_pc2d_create(C.byref(p), C.byref(self._h)), "hype_pc2d_create")
+
+    def close(self):
+        if self._h:
+            L.lib().hype_pc2d_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def RHSFunction(self, t, U, RHS=None):
+        """drop-in for RHSFunction(ts, t, U, RHS, &Ctx): fills RHS and sets self.dt"""
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        if U.shape != self.shape:
+            raise ValueError(f"U must have shape {self.shape}")
+        if RHS is None:
+            RHS = np.empty_like(U)
+        dt = C.c_double(0.0)
+        rc = L.lib().hype_pc2d_rhs(self._h, float(t), _dp(U), _dp(RHS), C.byref(dt))
+        self.dt = dt.value
+        check(rc, "RHSFunction")
+        return RHS
+
+    def set_state(self, U):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        if U.shape != self.shape:
+            raise ValueError(f"U must have shape {self.shape}")
+        check(L.lib().hype_pc2d_upload(self._h, _dp(U)), "hype_pc2d_upload")
+
+    def get_state(self):
+        U = np.empty(self.shape)
+        check(L.lib().hype_pc2d_download(self._h, _dp(U)), "hype_pc2d_download")
+        return U
+
+    def step(self, nsteps, dt=None):
+        t = C.c_double(self.t)
+        d = C.c_double(self.next_dt if dt is None else dt)
+        fb = C.c_longlong(0)
+        rc = L.lib().hype_pc2d_step(self._h, int(nsteps), C.byref(t), C.byref(d), C.byref(fb))
+        self.t, self.next_dt, self.fallback_cells = t.value, d.value, fb.value
+        check(rc, "hype_pc2d_step")
+

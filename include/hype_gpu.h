@@ -283,6 +283,39 @@ int hype_acoustic_step(hype_acoustic* a, int nsteps, double t_final, double* t_i
 int hype_acoustic_sync(hype_acoustic* a);
 void* hype_acoustic_stream(hype_acoustic* a);
 
+/* ============================================================ 2D path-conservative (HyPE-2D) */
+/* The RHS of 2d/HyPE-2D (RHSFunction, rhs_function.c:12-610) with its Kapila
+ * five-equation model (kapila_5eqn.c): Q = (a1 rho1, a2 rho2, rho u, rho v, E, a1), AoS
+ * [j][i][6]; the conservative variables reconstructed to order N = 0..3 (reconstruction.c),
+ * PDECheckPAD at the admissibility nodes with first order on failure, the Rusanov flux plus
+ * the Roe-path fluctuation of riemann.c:13-85, the non-conservative volume term, dt = CFL h /
+ * (2 s_max), and the program's stepper for N (Euler, SSP RKS2/2, RKS3/4, RK104,
+ * hype.c:361-382).  Results equal the reference program's bit for bit. */
+typedef struct hype_pc2d hype_pc2d;
+
+typedef struct {
+    int nx, ny;
+    double x_min, y_min, h;
+    double cfl;
+    int bc[4];              /* HYPE_BC_PERIODIC / REFLECTIVE / TRANSMISSIVE: left, right, bottom, top */
+    int order;              /* N = 0..3 (Ctx.N, hype.c:32) */
+    double g1, p1, g2, p2;  /* phase EOS (GAMMA_1, PI_1, GAMMA_2, PI_2; hype.h:41-44: 1.4, 0, 1.4, 0) */
+} hype_pc2d_params;
+
+int hype_pc2d_create(const hype_pc2d_params* p, hype_pc2d** out);
+void hype_pc2d_destroy(hype_pc2d* m);
+int hype_pc2d_get_params(const hype_pc2d* m, hype_pc2d_params* out);
+/* Drop-in for RHSFunction (rhs_function.c:12); *dt_out: the Ctx->dt it sets */
+int hype_pc2d_rhs(hype_pc2d* m, double t, const double* U_aos, double* RHS_aos, double* dt_out);
+int hype_pc2d_upload(hype_pc2d* m, const double* U_aos);
+int hype_pc2d_download(hype_pc2d* m, double* U_aos);
+/* nsteps of the program's stepper on the resident state; *dt_inout <= 0: dt from the first
+ * RHS, kept for every step as the program keeps it (its monitor does not reset dt);
+ * *fallback_cells: owned-cell reconstructions that fell back to first order */
+int hype_pc2d_step(hype_pc2d* m, int nsteps, double* t_inout, double* dt_inout, long long* fallback_cells);
+int hype_pc2d_sync(hype_pc2d* m);
+void* hype_pc2d_stream(hype_pc2d* m);
+
 /* ============================================================ 3D multiphase */
 /* The primitive-variable multiphase RHS of 3d/weno4/Viscous-Multiphase-Fourth-Order
  * (RHSFunctionPrimitive, rhs_function.c:56-570): Q = (rho, rho u, rho v, rho w, E, phi),
