@@ -198,3 +198,24 @@ def mp3d_layers(nx: int, ny: int, nz: int, eos=MP3D_EOS, width: float = 0.02) ->
     V[..., 5] = (1.0 - w_gas)[:, None, None]
     return mp3d_prim2cons(V, eos)
 
+
+def kapila_drop(n: int, seed: int = 5, width: float = 0.02) -> np.ndarray:
+    """a circular drop of phase 1 (radius 0.25, density 1) in phase 2 (density 0.125) on [0,1]^2
+    with seeded 1 % velocity noise, pressure 1, both phases gamma 1.4 (the EOS compiled into
+    2d/HyPE-2D); volume fraction in [1e-3, 1 - 1e-3]; Kapila conservative variables
+    (a1 rho1, a2 rho2, rho u, rho v, E, a1), AoS [j][i][6]"""
+    rng = np.random.default_rng(seed)
+    x = (np.arange(n) + 0.5) / n
+    r = np.sqrt((x[None, :] - 0.5) ** 2 + (x[:, None] - 0.5) ** 2)
+    a1 = 1e-3 + (1 - 2e-3) * 0.5 * (1 - np.tanh((r - 0.25) / width))
+    u, v = 0.01 * rng.standard_normal((n, n)), 0.01 * rng.standard_normal((n, n))
+    rho = a1 * 1.0 + (1 - a1) * 0.125
+    Q = np.empty((n, n, 6))
+    Q[..., 0] = a1 * 1.0
+    Q[..., 1] = (1 - a1) * 0.125
+    Q[..., 2] = rho * u
+    Q[..., 3] = rho * v
+    Q[..., 4] = 1.0 / 0.4 + 0.5 * rho * (u * u + v * v)
+    Q[..., 5] = a1
+    return Q
+

@@ -11,7 +11,8 @@ cell-updates/s (cells x steps / s).
 Other workloads (--workload): euler256_fp32 (FP32 reconstruction/flux, FP64
 state), euler256_linear (optimal-weight linear reconstruction), euler256_weno3,
 euler256_hllc, ns256_tgv (viscous Taylor-Green), acoustic256 (3D acoustic FV),
-sw2d4096 (2D standing wave, RK104), mp3d256 (3D primitive multiphase), kapila1024[_fp32|_learned], blast256/512,
+sw2d4096 (2D standing wave, RK104), mp3d256 (3D primitive multiphase), pc2d2048 (2d/HyPE-2D path-conservative
+Kapila, order 3), kapila1024[_fp32|_learned], blast256/512,
 ctcs512 (2D CTCS 512^2), batch256 (256 batched monopole CTCS instances).
 --grid N sets the cells per axis of the 3D Euler / Navier-Stokes and 2D acoustic
 workloads (small cases for profiling).
@@ -806,6 +807,70 @@ def run_mp3d(args, ws, rank, local, n=256):
             "gpu_launches": launches, "clocks": clk.summary()}
 
 
+def run_pc2d(args, ws, rank, local, n=2048, order=3):
+    """the path-conservative scheme of 2d/HyPE-2D (Kapila model, order N, Rusanov + Roe-path
+    fluctuation, the program's stepper for N) on an n^2 drop, transmissive, CFL 0.9"""
+    import torch
+
+    import acoustic_petsc_gb300 as H
+    from acoustic_petsc_gb300 import workloads
+
+    L = H.lib()
+    H._lib.check(L.hype_set_device(local), "hype_set_device")
+    torch.cuda.set_device(local)
+    n = args.grid or n
+    U0 = workloads.kapila_drop(n)
+    s = H.PathConservative2D(n, n, 1.0 / n, order=order, CFL=0.9)
+    s.set_state(U0)
+    s.step(max(args.warmup, 3))
+    stream = torch.cuda.ExternalStream(L.hype_pc2d_stream(s._h))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = H.launches()
+    _barrier(ws)
+    torch.cuda.synchronize()
+    with Clocks(_gpu_index(local)) as clk:
+        e0.record(stream)
+        s.step(args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    launches = H.launches() - l0
+    ms = _max_over_ranks(ws, e0.elapsed_time(e1))
+    cells = n * n
+    value = ws * cells * args.steps / (ms * 1e-3)
+    peak, kind = _peaks()
+    stages = {0: 1, 1: 2, 2: 4, 3: 10}[order]
+    bytes_cu = stages * 96 + (2 * 144 + 48 if order == 3 else 48)
+    ach = bytes_cu * cells * args.steps / (ms * 1e-3) / 1e9
+    host = torch.empty((n, n, 6), dtype=torch.float64, pin_memory=True)
+    hv = host.numpy()
+    hv[...] = U0
+    ke = max(1, min(3, args.steps))
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        s.set_state(hv)
+        s.step(1)
+        H._lib.check(L.hype_pc2d_download(s._h, hv.ctypes.data_as(H._lib.D)), "download")
+    wall = time.perf_counter() - t0
+    ms_e2e = _max_over_ranks(ws, wall * 1e3)
+    fb = s.fallback_cells
+    s.close()
+    nb = cells * 6 * 8
+    return {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: Kapila drop (phase 1 in phase 2, gamma 1.4 both), seeded 1 % velocity noise",
+            "config": {"workload": f"pathcons2d_kapila_n{order}_{n}", "grid": [n, n], "cfl": 0.9, "order": order,
+                       "scheme": "2d/HyPE-2D RHSFunction: conservative WENO of order N + node PAD + Rusanov + "
+                                 "Roe-path fluctuation + volume NCP, SSP stepper of N (bit-identical to the reference)",
+                       "fallback_cells_last_step": fb,
+                       "l2": f"state 6*8*{n}^2 B = {48 * cells / 1e6:.0f} MB vs 129 MB; no flush"},
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "algorithmic_bytes_per_cell_update": bytes_cu, "traffic": None},
+            "e2e": {"value": ws * cells * ke / (ms_e2e * 1e-3), "unit": "cell-updates/s", "h2d_bytes_per_step": nb,
+                    "d2h_bytes_per_step": nb, "steps": ke, "path": "PathConservative2D.set_state -> step(1) -> get_state"},
+            "gpu_launches": launches, "clocks": clk.summary()}
+
+
 WORKLOADS = {
     "blast512": run_blast,
     "blast256": lambda a, *r: run_blast(a, *r, n=256),
@@ -825,6 +890,7 @@ WORKLOADS = {
     "euler128_fp32": lambda a, *r: run_euler(a, *r, precision=1, recon=0, n=128),
     "sw2d4096": run_sw2d,
     "mp3d256": run_mp3d,
+    "pc2d2048": run_pc2d,
     "ctcs512": run_ctcs,
     "batch256": run_batch,
 }
@@ -892,6 +958,20 @@ def main():
             d = time.perf_counter() - t0
             out["cpu_baseline"] = {"value": n * n * 4 / d, "unit": "cell-updates/s", "cores": O.threads(),
                                    "kind": "port", "sample": f"4 SSPRK(4,3) steps of the {n}^2 version ({d:.1f} s)"}
+        elif args.workload.startswith("pc2d"):
+            from acoustic_petsc_gb300 import workloads
+            from oracle import pyoracle as O
+
+            O.build(None)
+            n = 512
+            cfg = O.h2d_cfg(3, n, n, 1.0 / n, cfl=0.9, bc=(2,) * 4, nthreads=os.cpu_count() or 1)
+            U0 = workloads.kapila_drop(n)
+            O.h2d_run(cfg, U0, 1)
+            t0 = time.perf_counter()
+            O.h2d_run(cfg, U0, 2)
+            d = time.perf_counter() - t0
+            out["cpu_baseline"] = {"value": n * n * 2 / d, "unit": "cell-updates/s", "cores": O.threads(),
+                                   "kind": "port", "sample": f"2 RK104 steps of the order-3 {n}^2 drop ({d:.1f} s)"}
         elif args.workload.startswith("mp3d"):
             from acoustic_petsc_gb300 import workloads
             from oracle import pyoracle as O
