@@ -13,12 +13,14 @@
 //                the 24 face-normal gradients (evaluate_grad, reconstruction.c:25-34);
 //   k_ac_faces   per face: 4 Gauss points of the central flux (:176-287);
 //   k_ac_update  RHS (v, (1/h) sum of flux differences) fused with the stage
-//                combination (:289-300).
+//                combination (:289-300), plus the point source of 3d/weno4/point_source
+//                (rhs_function.c:337-346: Source(t)/h^3 in one cell, u at the receiver).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
 
 #include "euler_kernels.cuh"
+#include "point_source.cuh"
 
 namespace hype {
 namespace acoustic {
@@ -155,7 +157,7 @@ struct Stage {
 __global__ void __launch_bounds__(256) k_ac_update(const double* __restrict__ Fx, const double* __restrict__ Fy,
                                                    const double* __restrict__ Fz, const double* __restrict__ U,
                                                    const double* __restrict__ W, double* __restrict__ out, Geo g,
-                                                   double r1_h2, Stage st, double dt) {
+                                                   double r1_h2, Stage st, double dt, SourceArgs src) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
@@ -164,8 +166,10 @@ __global__ void __launch_bounds__(256) k_ac_update(const double* __restrict__ Fx
     const long long ix = ((long long)k * g.ny + j) * (g.nx + 1) + i;
     const long long iy = ((long long)k * (g.ny + 1) + j) * g.nx + i;
     const long long iz = cell;
-    const double div = r1_h2 * (Fx[ix + 1] - Fx[ix]) + r1_h2 * (Fy[iy + g.nx] - Fy[iy]) +
-                       r1_h2 * (Fz[iz + (long long)g.nx * g.ny] - Fz[iz]);
+    double div = r1_h2 * (Fx[ix + 1] - Fx[ix]) + r1_h2 * (Fy[iy + g.nx] - Fy[iy]) +
+                 r1_h2 * (Fz[iz + (long long)g.nx * g.ny] - Fz[iz]);
+    if (cell == src.src_cell) div += src.src_val;
+    if (cell == src.rec_cell) *src.slot = W[cell];  // read before out (which may alias W) is written
     const double L[2] = {W[g.N + cell], div};
     const double cdt = st.c * dt;
 #pragma unroll
@@ -203,6 +207,7 @@ struct hype_acoustic {
     cudaStream_t stream = nullptr;
     double *U = nullptr, *W = nullptr, *L = nullptr, *S = nullptr, *Gh = nullptr, *T = nullptr;
     double *Fx = nullptr, *Fy = nullptr, *Fz = nullptr, *aos = nullptr;
+    PointSource ps;
 };
 
 static int ac_rhs(hype_acoustic* a, const double* Win) {
@@ -219,10 +224,11 @@ static int ac_rhs(hype_acoustic* a, const double* Win) {
     return HYPE_OK;
 }
 
-static int ac_update(hype_acoustic* a, const double* U, const double* W, double* out, Stage st, double dt) {
+// t: the time of this RHS evaluation (the point source's argument)
+static int ac_update(hype_acoustic* a, const double* U, const double* W, double* out, Stage st, double dt, double t) {
     const Geo& g = a->g;
     k_ac_update<<<dim3(cdiv(g.nx, 32), cdiv(g.ny, 8), g.nz), dim3(32, 8), 0, a->stream>>>(
-        a->Fx, a->Fy, a->Fz, U, W, out, g, 1.0 / (a->p.h * a->p.h), st, dt);
+        a->Fx, a->Fy, a->Fz, U, W, out, g, 1.0 / (a->p.h * a->p.h), st, dt, source_args(a->ps, t));
     HYPE_LAUNCHED(1);
     return HYPE_OK;
 }
@@ -271,6 +277,7 @@ extern "C" void hype_acoustic_destroy(hype_acoustic* a) {
     if (a->stream) cudaStreamSynchronize(a->stream);
     cudaFree(a->U); cudaFree(a->W); cudaFree(a->L); cudaFree(a->S); cudaFree(a->aos); cudaFree(a->Gh); cudaFree(a->T);
     cudaFree(a->Fx); cudaFree(a->Fy); cudaFree(a->Fz);
+    a->ps.release();
     if (a->stream) cudaStreamDestroy(a->stream);
     delete a;
 }
@@ -305,12 +312,58 @@ extern "C" int hype_acoustic_download(hype_acoustic* a, double* U_aos) {
     return ac_d2h(a, a->U, U_aos);
 }
 
-extern "C" int hype_acoustic_rhs(hype_acoustic* a, const double* U_aos, double* RHS_aos) {
+extern "C" int hype_acoustic_rhs_t(hype_acoustic* a, double t, const double* U_aos, double* RHS_aos) {
     if (!a || !U_aos || !RHS_aos) return HYPE_ERR_ARG;
     int rc = ac_h2d(a, U_aos, a->S);
     if (rc || (rc = ac_rhs(a, a->S))) return rc;
-    if ((rc = ac_update(a, a->S, a->S, a->L, Stage{0.0, 0.0, 0.0, 1}, 0.0))) return rc;
+    if ((rc = ac_update(a, a->S, a->S, a->L, Stage{0.0, 0.0, 0.0, 1}, 0.0, t))) return rc;
     return ac_d2h(a, a->L, RHS_aos);
+}
+
+extern "C" int hype_acoustic_rhs(hype_acoustic* a, const double* U_aos, double* RHS_aos) {
+    return hype_acoustic_rhs_t(a, 0.0, U_aos, RHS_aos);
+}
+
+extern "C" int hype_acoustic_set_point_source(hype_acoustic* a, int isx, int isy, int isz, double f0, int irx, int iry,
+                                              int irz, int trace_capacity) {
+    if (!a || trace_capacity < 0) return HYPE_ERR_ARG;
+    const Geo& g = a->g;
+    const bool src = isx >= 0, rec = irx >= 0;
+    if (src && (isx >= g.nx || isy < 0 || isy >= g.ny || isz < 0 || isz >= g.nz || !(f0 > 0))) return HYPE_ERR_ARG;
+    if (rec && (irx >= g.nx || iry < 0 || iry >= g.ny || irz < 0 || irz >= g.nz)) return HYPE_ERR_ARG;
+    HYPE_CK(cudaStreamSynchronize(a->stream));
+    PointSource& ps = a->ps;
+    ps.release();
+    ps = PointSource();
+    ps.src_on = src;
+    ps.src_cell = src ? ((long long)isz * g.ny + isy) * g.nx + isx : -1;
+    ps.f0 = f0;
+    ps.scale = 1. / ((a->p.h) * (a->p.h) * (a->p.h));  // r1_h3, rhs_function.c:25
+    ps.rec_on = rec;
+    ps.rec_cell = rec ? ((long long)irz * g.ny + iry) * g.nx + irx : -1;
+    if (rec && trace_capacity > 0) {
+        cudaError_t ce = cudaMalloc((void**)&ps.trace, sizeof(double) * (size_t)trace_capacity);
+        if (ce != cudaSuccess) {
+            set_last_error("hype_acoustic_set_point_source", ce);
+            return ce == cudaErrorMemoryAllocation ? HYPE_ERR_NOMEM : HYPE_ERR_CUDA;
+        }
+        ps.capacity = trace_capacity;
+    }
+    return HYPE_OK;
+}
+
+extern "C" int hype_acoustic_trace(hype_acoustic* a, double* t, double* u, int max, long long* count) {
+    if (!a || max < 0 || ((!t || !u) && max > 0)) return HYPE_ERR_ARG;
+    const PointSource& ps = a->ps;
+    const int n = (int)(ps.count < ps.capacity ? ps.count : ps.capacity);
+    const int m = n < max ? n : max;
+    if (m > 0) {
+        HYPE_CK(cudaMemcpyAsync(u, ps.trace, sizeof(double) * m, cudaMemcpyDeviceToHost, a->stream));
+        for (int q = 0; q < m; ++q) t[q] = ps.times[q];
+    }
+    HYPE_CK(cudaStreamSynchronize(a->stream));
+    if (count) *count = ps.count;
+    return HYPE_OK;
 }
 
 // SSPRK(4,3) steps of dt from *t_inout; a positive t_final shortens the step that
@@ -321,15 +374,19 @@ extern "C" int hype_acoustic_step(hype_acoustic* a, int nsteps, double t_final, 
     double t = *t_inout;
     int s = 0;
     const Stage s12{0.0, 1.0, 0.5, 0}, s3{2.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 0};
+    // the stage times of SSP RKS3 with 4 stages (n = 2): c_i = i / (s - n) for i < n (n + 1) / 2,
+    // else (i - n) / (s - n), i.e. t + (0, 1/2, 1, 1/2) dt
+    auto ct = [](int i) { return (i < 2 * (2 + 1) / 2) ? 1.0 * i / (4 - 2) : (1.0 * i - 2) / (4 - 2); };
     for (; s < nsteps; ++s) {
         if (t_final > 0.0 && t >= t_final) break;
         double dt = a->p.dt;
         if (t_final > 0.0 && t + dt > t_final) dt = t_final - t;
         int rc;
-        if ((rc = ac_rhs(a, a->U)) || (rc = ac_update(a, a->U, a->U, a->W, s12, dt))) return rc;  // u1 = u + dt/2 L(u)
-        if ((rc = ac_rhs(a, a->W)) || (rc = ac_update(a, a->U, a->W, a->W, s12, dt))) return rc;  // u2 = u1 + dt/2 L(u1)
-        if ((rc = ac_rhs(a, a->W)) || (rc = ac_update(a, a->U, a->W, a->W, s3, dt))) return rc;  // u3 = 2/3 u + u2/3 + dt/6 L(u2)
-        if ((rc = ac_rhs(a, a->W)) || (rc = ac_update(a, a->U, a->W, a->U, s12, dt))) return rc;  // u3 + dt/2 L(u3)
+        // u1 = u + dt/2 L(u); u2 = u1 + dt/2 L(u1); u3 = 2/3 u + u2/3 + dt/6 L(u2); u3 + dt/2 L(u3)
+        if ((rc = ac_rhs(a, a->U)) || (rc = ac_update(a, a->U, a->U, a->W, s12, dt, t + ct(0) * dt))) return rc;
+        if ((rc = ac_rhs(a, a->W)) || (rc = ac_update(a, a->U, a->W, a->W, s12, dt, t + ct(1) * dt))) return rc;
+        if ((rc = ac_rhs(a, a->W)) || (rc = ac_update(a, a->U, a->W, a->W, s3, dt, t + ct(2) * dt))) return rc;
+        if ((rc = ac_rhs(a, a->W)) || (rc = ac_update(a, a->U, a->W, a->U, s12, dt, t + ct(3) * dt))) return rc;
         t += dt;
     }
     HYPE_CK(cudaStreamSynchronize(a->stream));

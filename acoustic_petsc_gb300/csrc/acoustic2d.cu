@@ -14,13 +14,16 @@
 //                mirror, :46-95), the 10 coefficients and the 8 edge-normal gradients;
 //   k_sw_update  per cell: the 4 edge fluxes from its own and its neighbours'
 //                gradients (each edge computed identically by both of its cells), the
-//                RHS (v, (1/h)(flux differences)) and the Runge-Kutta stage combination.
+//                RHS (v, (1/h)(flux differences)) and the Runge-Kutta stage combination,
+//                plus the line source of 2d/weno4/line_source (rhs_function.c:244-253:
+//                Source(t)/h^2 in one cell, u at the receiver).
 // Operation order follows the reference expression by expression and the file is
 // compiled without FMA contraction, so results equal the reference's bit for bit.
 #include <cuda_runtime.h>
 #include <string.h>
 
 #include "hype_common.cuh"
+#include "point_source.cuh"
 
 namespace hype {
 namespace acoustic2d {
@@ -161,7 +164,7 @@ __device__ __forceinline__ double sw_edge(double c2, double gL0, double gR0, dou
 __global__ void __launch_bounds__(256) k_sw_update(const double* __restrict__ T, const double* __restrict__ W,
                                                    const double* __restrict__ X, const double* __restrict__ Y,
                                                    double* __restrict__ out, Geo g, double c2, double r1_h, Stage st,
-                                                   double dt) {
+                                                   double dt, SourceArgs src) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.nx || j >= g.ny) return;
@@ -174,7 +177,9 @@ __global__ void __launch_bounds__(256) k_sw_update(const double* __restrict__ T,
     // y edges: top edge (f = 3) of the lower cell, bottom edge (f = 2) of the upper one
     const double Gb = sw_edge(c2, t(3, 0, e - g.ex), t(2, 0, e), t(3, 1, e - g.ex), t(2, 1, e));
     const double Gt = sw_edge(c2, t(3, 0, e), t(2, 0, e + g.ex), t(3, 1, e), t(2, 1, e + g.ex));
-    const double L[2] = {__ldg(W + g.N + cell), r1_h * (Fr - Fl) + r1_h * (Gt - Gb)};
+    double L[2] = {__ldg(W + g.N + cell), r1_h * (Fr - Fl) + r1_h * (Gt - Gb)};
+    if (cell == src.src_cell) L[1] += src.src_val;
+    if (cell == src.rec_cell) *src.slot = W[cell];  // read before out (which may alias W) is written
     const double cdt = st.rhs_only ? 0.0 : st.c * dt / st.d;
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
@@ -235,14 +240,16 @@ struct hype_acoustic2d {
     Geo g;
     cudaStream_t stream = nullptr;
     double *U = nullptr, *W0 = nullptr, *W1 = nullptr, *S = nullptr, *L = nullptr, *T = nullptr, *aos = nullptr;
+    PointSource ps;
 };
 
+// t: the time of this RHS evaluation (the line source's argument)
 static int sw_rhs_stage(hype_acoustic2d* a, const double* Win, const double* X, const double* Y, double* out, Stage st,
-                        double dt) {
+                        double dt, double t) {
     const Geo& g = a->g;
     k_sw_recon<<<dim3(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 8)), dim3(32, 8), 0, a->stream>>>(Win, a->T, g, 1. / (a->p.h));
     k_sw_update<<<dim3(cdiv(g.nx, 32), cdiv(g.ny, 8)), dim3(32, 8), 0, a->stream>>>(
-        a->T, Win, X, Y, out, g, a->p.c * a->p.c, 1. / (a->p.h), st, dt);
+        a->T, Win, X, Y, out, g, a->p.c * a->p.c, 1. / (a->p.h), st, dt, source_args(a->ps, t));
     HYPE_LAUNCHED(2);
     return HYPE_OK;
 }
@@ -292,6 +299,7 @@ extern "C" void hype_acoustic2d_destroy(hype_acoustic2d* a) {
     if (!a) return;
     if (a->stream) cudaStreamSynchronize(a->stream);
     cudaFree(a->U); cudaFree(a->W0); cudaFree(a->W1); cudaFree(a->S); cudaFree(a->L); cudaFree(a->aos); cudaFree(a->T);
+    a->ps.release();
     if (a->stream) cudaStreamDestroy(a->stream);
     delete a;
 }
@@ -326,11 +334,57 @@ extern "C" int hype_acoustic2d_download(hype_acoustic2d* a, double* U_aos) {
     return sw_d2h(a, a->U, U_aos);
 }
 
-extern "C" int hype_acoustic2d_rhs(hype_acoustic2d* a, const double* U_aos, double* RHS_aos) {
+extern "C" int hype_acoustic2d_rhs_t(hype_acoustic2d* a, double t, const double* U_aos, double* RHS_aos) {
     if (!a || !U_aos || !RHS_aos) return HYPE_ERR_ARG;
     int rc = sw_h2d(a, U_aos, a->S);
-    if (rc || (rc = sw_rhs_stage(a, a->S, a->S, a->S, a->L, Stage{0.0, 0.0, 0.0, 1.0, 1}, 0.0))) return rc;
+    if (rc || (rc = sw_rhs_stage(a, a->S, a->S, a->S, a->L, Stage{0.0, 0.0, 0.0, 1.0, 1}, 0.0, t))) return rc;
     return sw_d2h(a, a->L, RHS_aos);
+}
+
+extern "C" int hype_acoustic2d_rhs(hype_acoustic2d* a, const double* U_aos, double* RHS_aos) {
+    return hype_acoustic2d_rhs_t(a, 0.0, U_aos, RHS_aos);
+}
+
+extern "C" int hype_acoustic2d_set_point_source(hype_acoustic2d* a, int isx, int isy, double f0, int irx, int iry,
+                                                int trace_capacity) {
+    if (!a || trace_capacity < 0) return HYPE_ERR_ARG;
+    const Geo& g = a->g;
+    const bool src = isx >= 0, rec = irx >= 0;
+    if (src && (isx >= g.nx || isy < 0 || isy >= g.ny || !(f0 > 0))) return HYPE_ERR_ARG;
+    if (rec && (irx >= g.nx || iry < 0 || iry >= g.ny)) return HYPE_ERR_ARG;
+    HYPE_CK(cudaStreamSynchronize(a->stream));
+    PointSource& ps = a->ps;
+    ps.release();
+    ps = PointSource();
+    ps.src_on = src;
+    ps.src_cell = src ? (long long)isy * g.nx + isx : -1;
+    ps.f0 = f0;
+    ps.scale = 1. / ((a->p.h) * (a->p.h));  // r1_h2, rhs_function.c:24
+    ps.rec_on = rec;
+    ps.rec_cell = rec ? (long long)iry * g.nx + irx : -1;
+    if (rec && trace_capacity > 0) {
+        cudaError_t ce = cudaMalloc((void**)&ps.trace, sizeof(double) * (size_t)trace_capacity);
+        if (ce != cudaSuccess) {
+            set_last_error("hype_acoustic2d_set_point_source", ce);
+            return ce == cudaErrorMemoryAllocation ? HYPE_ERR_NOMEM : HYPE_ERR_CUDA;
+        }
+        ps.capacity = trace_capacity;
+    }
+    return HYPE_OK;
+}
+
+extern "C" int hype_acoustic2d_trace(hype_acoustic2d* a, double* t, double* u, int max, long long* count) {
+    if (!a || max < 0 || ((!t || !u) && max > 0)) return HYPE_ERR_ARG;
+    const PointSource& ps = a->ps;
+    const int n = (int)(ps.count < ps.capacity ? ps.count : ps.capacity);
+    const int m = n < max ? n : max;
+    if (m > 0) {
+        HYPE_CK(cudaMemcpyAsync(u, ps.trace, sizeof(double) * m, cudaMemcpyDeviceToHost, a->stream));
+        for (int q = 0; q < m; ++q) t[q] = ps.times[q];
+    }
+    HYPE_CK(cudaStreamSynchronize(a->stream));
+    if (count) *count = ps.count;
+    return HYPE_OK;
 }
 
 extern "C" int hype_acoustic2d_step(hype_acoustic2d* a, int nsteps, double t_final, double* t_inout, int* steps_taken) {
@@ -346,27 +400,30 @@ extern "C" int hype_acoustic2d_step(hype_acoustic2d* a, int nsteps, double t_fin
         if (a->p.stepper == HYPE_STEP_SSPRK104) {
             // SSP RK104, low storage (Ketcheson 2008): five dt/6 stages on w0 = u, then
             // w1 = 9/25 w0 + 1/25 u, w0 = 15 w1 - 5 w0, four dt/6 stages, u = 3/5 w0 + dt/10 L(w0) + w1
+            // stage times t + c_i dt, c = (0, 1, 2, 3, 4, 2, 3, 4, 5, 6) / 6
+            static const double c[10] = {0, 1. / 6, 2. / 6, 3. / 6, 4. / 6, 2. / 6, 3. / 6, 4. / 6, 5. / 6, 1};
             const Stage s6{1.0, 0.0, 1.0, 6.0, 0};
-            if ((rc = sw_rhs_stage(a, a->U, a->U, nullptr, a->W0, s6, h))) return rc;
+            if ((rc = sw_rhs_stage(a, a->U, a->U, nullptr, a->W0, s6, h, t + c[0] * h))) return rc;
             for (int k = 1; k < 5; ++k)
-                if ((rc = sw_rhs_stage(a, a->W0, a->W0, nullptr, a->W0, s6, h))) return rc;
+                if ((rc = sw_rhs_stage(a, a->W0, a->W0, nullptr, a->W0, s6, h, t + c[k] * h))) return rc;
             k_sw_axpby<<<cdiv(n2, 256), 256, 0, a->stream>>>(a->W0, a->U, a->W1, 9.0 / 25, 1.0 / 25, n2);
             k_sw_axpby<<<cdiv(n2, 256), 256, 0, a->stream>>>(a->W1, a->W0, a->W0, 15.0, -5.0, n2);
             HYPE_LAUNCHED(2);
             for (int k = 5; k < 9; ++k)
-                if ((rc = sw_rhs_stage(a, a->W0, a->W0, nullptr, a->W0, s6, h))) return rc;
-            if ((rc = sw_rhs_stage(a, a->W0, a->W0, a->W1, a->U, Stage{3.0 / 5, 1.0, 1.0, 10.0, 0}, h))) return rc;
+                if ((rc = sw_rhs_stage(a, a->W0, a->W0, nullptr, a->W0, s6, h, t + c[k] * h))) return rc;
+            if ((rc = sw_rhs_stage(a, a->W0, a->W0, a->W1, a->U, Stage{3.0 / 5, 1.0, 1.0, 10.0, 0}, h, t + h))) return rc;
         } else {
             // SSP RKS3, 4 stages: u1 = u + dt/2 L(u); u2 = u1 + dt/2 L(u1);
             // u3 = 2/3 u + dt/6 L(u2) + 1/3 u2; u^{n+1} = u3 + dt/2 L(u3)
+            // stage times t + (0, 1/2, 1, 1/2) dt (c_i = i/(s-n), or (i-n)/(s-n) past n(n+1)/2)
             const Stage s2{1.0, 0.0, 1.0, 2.0, 0};
-            if ((rc = sw_rhs_stage(a, a->U, a->U, nullptr, a->W0, s2, h))) return rc;
-            if ((rc = sw_rhs_stage(a, a->W0, a->W0, nullptr, a->W0, s2, h))) return rc;
+            if ((rc = sw_rhs_stage(a, a->U, a->U, nullptr, a->W0, s2, h, t + 1.0 * 0 / (4 - 2) * h))) return rc;
+            if ((rc = sw_rhs_stage(a, a->W0, a->W0, nullptr, a->W0, s2, h, t + 1.0 * 1 / (4 - 2) * h))) return rc;
             if ((rc = sw_rhs_stage(a, a->W0, a->U, a->W0, a->W0,
                                    Stage{1.0 * 2 / (2 * 2 - 1.0), (2 - 1.0) / (2 * 2 - 1), 2 - 1.0, 2.0 * (2 * 2 - 1), 0},
-                                   h)))
+                                   h, t + 1.0 * 2 / (4 - 2) * h)))
                 return rc;
-            if ((rc = sw_rhs_stage(a, a->W0, a->W0, nullptr, a->U, s2, h))) return rc;
+            if ((rc = sw_rhs_stage(a, a->W0, a->W0, nullptr, a->U, s2, h, t + (1.0 * 3 - 2) / (4 - 2) * h))) return rc;
         }
         t += h;
     }

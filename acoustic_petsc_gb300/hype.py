@@ -439,6 +439,17 @@ class Multiphase2D:
         return X, Dv
 
 
+def _trace(fn, handle, capacity):
+    """the stored receiver samples (the first ``capacity`` RHS evaluations) and the count"""
+    count = C.c_longlong(0)
+    check(fn(handle, None, None, 0, C.byref(count)), "receiver_trace")
+    m = min(int(count.value), int(capacity))
+    t = np.empty(m)
+    u = np.empty(m)
+    check(fn(handle, _dp(t), _dp(u), m, C.byref(count)), "receiver_trace")
+    return t, u, int(count.value)
+
+
 class AcousticFV3D:
     """The acoustic finite-volume path of 3d/weno4/plane_wave: u_tt = c^2 lap u as
     (u, v = u_t) with CWENO4 (default: its R4 limit, as the reference runs it)
@@ -456,6 +467,7 @@ class AcousticFV3D:
         self.t = 0.0
         self._h = C.c_void_p()
         check(L.lib().hype_acoustic_create(C.byref(p), C.byref(self._h)), "hype_acoustic_create")
+        self._trace_capacity = 0
 
     def close(self):
         if self._h:
@@ -474,8 +486,25 @@ class AcousticFV3D:
             raise ValueError(f"U must have shape {self.shape}")
         if RHS is None:
             RHS = np.empty_like(U)
-        check(L.lib().hype_acoustic_rhs(self._h, _dp(U), _dp(RHS)), "RHSFunction")
+        check(L.lib().hype_acoustic_rhs_t(self._h, float(t), _dp(U), _dp(RHS)), "RHSFunction")
         return RHS
+
+    def set_point_source(self, source=None, f0=100.0, receiver=None, capacity=0):
+        """the point source and receiver of 3d/weno4/point_source (hype.c:59-64): every RHS
+        evaluation at time t adds Source(t)/h^3 (source.c:11-17, f0 the wavelet's dominant
+        frequency) to the u_t equation of cell ``source`` = (isx, isy, isz) and records u of
+        cell ``receiver`` = (irx, iry, irz) in a trace of up to ``capacity`` samples
+        (rhs_function.c:337-346).  None turns either off."""
+        sx, sy, sz = source if source is not None else (-1, 0, 0)
+        rx, ry, rz = receiver if receiver is not None else (-1, 0, 0)
+        check(L.lib().hype_acoustic_set_point_source(self._h, int(sx), int(sy), int(sz), float(f0), int(rx), int(ry),
+                                                     int(rz), int(capacity)), "set_point_source")
+        self._trace_capacity = int(capacity) if receiver is not None else 0
+
+    def receiver_trace(self):
+        """(t, u) of every recorded RHS evaluation (the columns of results/p.dat) and the
+        number of evaluations seen"""
+        return _trace(L.lib().hype_acoustic_trace, self._h, self._trace_capacity)
 
     def set_state(self, U):
         U = np.ascontiguousarray(U, dtype=np.float64)
@@ -514,6 +543,7 @@ class AcousticFV2D:
         self.t = 0.0
         self._h = C.c_void_p()
         check(L.lib().hype_acoustic2d_create(C.byref(p), C.byref(self._h)), "hype_acoustic2d_create")
+        self._trace_capacity = 0
 
     def close(self):
         if self._h:
@@ -532,8 +562,22 @@ class AcousticFV2D:
             raise ValueError(f"U must have shape {self.shape}")
         if RHS is None:
             RHS = np.empty_like(U)
-        check(L.lib().hype_acoustic2d_rhs(self._h, _dp(U), _dp(RHS)), "RHSFunction")
+        check(L.lib().hype_acoustic2d_rhs_t(self._h, float(t), _dp(U), _dp(RHS)), "RHSFunction")
         return RHS
+
+    def set_point_source(self, source=None, f0=65.0, receiver=None, capacity=0):
+        """the line source and receiver of 2d/weno4/line_source (hype.c:52-55): Source(t)/h^2
+        (source.c:12-18) added to the u_t equation of cell ``source`` = (isx, isy) at every RHS
+        evaluation, u of cell ``receiver`` = (irx, iry) recorded (rhs_function.c:244-253)"""
+        sx, sy = source if source is not None else (-1, 0)
+        rx, ry = receiver if receiver is not None else (-1, 0)
+        check(L.lib().hype_acoustic2d_set_point_source(self._h, int(sx), int(sy), float(f0), int(rx), int(ry),
+                                                       int(capacity)), "set_point_source")
+        self._trace_capacity = int(capacity) if receiver is not None else 0
+
+    def receiver_trace(self):
+        """(t, u) of every recorded RHS evaluation and the number of evaluations seen"""
+        return _trace(L.lib().hype_acoustic2d_trace, self._h, self._trace_capacity)
 
     def set_state(self, U):
         U = np.ascontiguousarray(U, dtype=np.float64)

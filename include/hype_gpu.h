@@ -280,6 +280,20 @@ int hype_acoustic_rhs(hype_acoustic* a, const double* U_aos, double* RHS_aos);
 /* up to nsteps steps from *t_inout; t_final > 0 shortens the step that would pass it
  * and stops there (TS_EXACTFINALTIME_MATCHSTEP, hype.c:178) */
 int hype_acoustic_step(hype_acoustic* a, int nsteps, double t_final, double* t_inout, int* steps_taken);
+/* the RHS at time t (the point source's argument; hype_acoustic_rhs is t = 0) */
+int hype_acoustic_rhs_t(hype_acoustic* a, double t, const double* U_aos, double* RHS_aos);
+/* The point source and receiver of 3d/weno4/point_source (AppCtx isx..irz, hype.c:59-64):
+ * from now on every RHS evaluation at time t adds Source(t) / h^3 to the u_t equation of
+ * cell (isx, isy, isz), Source(t) = -2 (t - t0) f0^2 exp(-f0^2 (t - t0)^2), t0 = 4 / f0
+ * (source.c:11-17, rhs_function.c:337-339; the program's f0 is 100), and records u of cell
+ * (irx, iry, irz) with t (rhs_function.c:342-346, which prints them to results/p.dat) into a
+ * trace of up to trace_capacity samples.  isx < 0: no source; irx < 0: no receiver.  Calling
+ * it again replaces the source and clears the trace. */
+int hype_acoustic_set_point_source(hype_acoustic* a, int isx, int isy, int isz, double f0, int irx, int iry, int irz,
+                                   int trace_capacity);
+/* the receiver trace: t[q], u[q] for q < min(recorded, trace_capacity, max); *count = the RHS
+ * evaluations seen since the receiver was set (also those past the capacity) */
+int hype_acoustic_trace(hype_acoustic* a, double* t, double* u, int max, long long* count);
 int hype_acoustic_sync(hype_acoustic* a);
 void* hype_acoustic_stream(hype_acoustic* a);
 
@@ -377,6 +391,16 @@ int hype_acoustic2d_rhs(hype_acoustic2d* a, const double* U_aos, double* RHS_aos
 /* up to nsteps steps from *t_inout; t_final > 0 shortens the step that would pass it
  * and stops there (TS_EXACTFINALTIME_MATCHSTEP, hype.c:208) */
 int hype_acoustic2d_step(hype_acoustic2d* a, int nsteps, double t_final, double* t_inout, int* steps_taken);
+/* the RHS at time t (hype_acoustic2d_rhs is t = 0) */
+int hype_acoustic2d_rhs_t(hype_acoustic2d* a, double t, const double* U_aos, double* RHS_aos);
+/* The line source and receiver of 2d/weno4/line_source (AppCtx isx, isy, irx, iry,
+ * hype.c:52-55): every RHS evaluation at time t adds Source(t) / h^2 to the u_t equation of
+ * cell (isx, isy) (source.c:12-18 with the program's f0 = 65, rhs_function.c:244-246) and
+ * records u of cell (irx, iry) with t (rhs_function.c:249-253) into a trace of up to
+ * trace_capacity samples; negative isx / irx turn them off; calling it again clears the trace. */
+int hype_acoustic2d_set_point_source(hype_acoustic2d* a, int isx, int isy, double f0, int irx, int iry,
+                                     int trace_capacity);
+int hype_acoustic2d_trace(hype_acoustic2d* a, double* t, double* u, int max, long long* count);
 int hype_acoustic2d_sync(hype_acoustic2d* a);
 void* hype_acoustic2d_stream(hype_acoustic2d* a);
 

@@ -1216,6 +1216,47 @@ static double ac_face_flux(const double* gL, int fl, const double* gR, int fr, d
     return flux;
 }
 
+/* ---------------------------------------------------------------- point source + receiver
+ * 3d/weno4/point_source and 2d/weno4/line_source add to the u_t equation of one cell the
+ * wavelet Source(t) = -2 (t - t0) f0^2 exp(-f0^2 (t - t0)^2), t0 = 4 / f0 (source.c), scaled by
+ * 1/h^3 (3D) or 1/h^2 (2D), at the time t of the RHS call (rhs_function.c:337-340 / :244-246),
+ * and print u at a receiver cell at every RHS call (:342-346 / :249-253).  Off by default. */
+static int g_src_on = 0, g_src[3] = {0, 0, 0}, g_rec_on = 0, g_rec[3] = {0, 0, 0};
+static double g_src_f0 = 100.0, g_src_t = 0.0;
+static double* g_tr_t = NULL;
+static double* g_tr_p = NULL;
+static int g_tr_max = 0, g_tr_n = 0;
+
+void orc_set_point_source(int on, int isx, int isy, int isz, double f0, int rec_on, int irx, int iry, int irz) {
+    g_src_on = on; g_src[0] = isx; g_src[1] = isy; g_src[2] = isz; g_src_f0 = f0;
+    g_rec_on = rec_on; g_rec[0] = irx; g_rec[1] = iry; g_rec[2] = irz;
+}
+
+/* the receiver trace of the following RHS calls goes to (t[q], p[q]), q < max; returns nothing */
+void orc_set_trace_buffer(double* t, double* p, int max) {
+    g_tr_t = t; g_tr_p = p; g_tr_max = max; g_tr_n = 0;
+}
+int orc_trace_count(void) { return g_tr_n; }
+
+static double src_wavelet(double t) {
+    const double f0 = g_src_f0;
+    const double t0 = 4.0 / f0;
+    return -2.0 * (t - t0) * f0 * f0 * exp(-1.0 * f0 * f0 * (t - t0) * (t - t0));
+}
+
+static void rec_sample(double t, double u) {
+    if (g_tr_n < g_tr_max && g_tr_t) {
+        g_tr_t[g_tr_n] = t;
+        g_tr_p[g_tr_n] = u;
+    }
+    ++g_tr_n;
+}
+
+int orc_acoustic_rhs_at(const orc_acoustic_cfg* g, double t, const double* U, double* RHS) {
+    g_src_t = t;
+    return orc_acoustic_rhs(g, U, RHS);
+}
+
 int orc_acoustic_rhs(const orc_acoustic_cfg* g, const double* U, double* RHS) {
     const int nx = g->nx, ny = g->ny, nz = g->nz;
 #ifdef _OPENMP
@@ -1252,6 +1293,11 @@ int orc_acoustic_rhs(const orc_acoustic_cfg* g, const double* U, double* RHS) {
                 RHS[cell * 2 + 1] = r1_h * (Fp - Fm) + r1_h * (Gp - Gm) + r1_h * (Hp - Hm);
             }
 #undef ACG
+    if (g_src_on) {
+        const double r1_h3 = 1. / ((g->h) * (g->h) * (g->h));
+        RHS[(((size_t)g_src[2] * ny + g_src[1]) * nx + g_src[0]) * 2 + 1] += src_wavelet(g_src_t) * r1_h3;
+    }
+    if (g_rec_on) rec_sample(g_src_t, U[(((size_t)g_rec[2] * ny + g_rec[1]) * nx + g_rec[0]) * 2]);
     free(P.pad);
     free(GR);
     return 0;
@@ -1273,13 +1319,14 @@ int orc_acoustic_run(const orc_acoustic_cfg* g, int nsteps, double dt, double t_
          * the same operation order as orc_euler_run) */
         const double dtr = h / 2;
         const double a3 = 1.0 * 2 / (2 * 2 - 1.0), b3 = (2 - 1.0) * h / (2 * (2 * 2 - 1)), c3 = (2 - 1.0) / (2 * 2 - 1);
-        orc_acoustic_rhs(g, U, L);
+        /* stage times of PETSc's RKS3 with 4 stages: t + (0, 1/2, 1, 1/2) h */
+        orc_acoustic_rhs_at(g, t + 1.0 * 0 / (4 - 2) * h, U, L);
         for (size_t q = 0; q < n; ++q) W[q] = U[q] + dtr * L[q];
-        orc_acoustic_rhs(g, W, L);
+        orc_acoustic_rhs_at(g, t + 1.0 * 1 / (4 - 2) * h, W, L);
         for (size_t q = 0; q < n; ++q) W[q] = W[q] + dtr * L[q];
-        orc_acoustic_rhs(g, W, L);
+        orc_acoustic_rhs_at(g, t + 1.0 * 2 / (4 - 2) * h, W, L);
         for (size_t q = 0; q < n; ++q) W[q] = a3 * U[q] + b3 * L[q] + c3 * W[q];
-        orc_acoustic_rhs(g, W, L);
+        orc_acoustic_rhs_at(g, t + (1.0 * 3 - 2) / (4 - 2) * h, W, L);
         for (size_t q = 0; q < n; ++q) U[q] = W[q] + dtr * L[q];
         t += h;
     }
@@ -1484,6 +1531,11 @@ static double sw_u(const orc_sw2d_cfg* g, const double* U, int i, int j) {
     return s < 0 ? -v : v;
 }
 
+int orc_sw2d_rhs_at(const orc_sw2d_cfg* g, double t, const double* U, double* RHS) {
+    g_src_t = t;
+    return orc_sw2d_rhs(g, U, RHS);
+}
+
 int orc_sw2d_rhs(const orc_sw2d_cfg* g, const double* U, double* RHS) {
     const int nx = g->nx, ny = g->ny, ex = nx + 2;
     const double r1_h = 1. / (g->h);
@@ -1559,6 +1611,11 @@ int orc_sw2d_rhs(const orc_sw2d_cfg* g, const double* U, double* RHS) {
             RHS[q * 2 + 1] = r1_h * (F[(size_t)j * (nx + 1) + i + 1] - F[(size_t)j * (nx + 1) + i]) +
                              r1_h * (G[(size_t)(j + 1) * nx + i] - G[(size_t)j * nx + i]);
         }
+    if (g_src_on) {
+        const double r1_h2 = 1. / ((g->h) * (g->h));
+        RHS[((size_t)g_src[1] * nx + g_src[0]) * 2 + 1] += src_wavelet(g_src_t) * r1_h2;
+    }
+    if (g_rec_on) rec_sample(g_src_t, U[((size_t)g_rec[1] * nx + g_rec[0]) * 2]);
     free(gr);
     free(F);
     free(G);
@@ -1583,28 +1640,36 @@ int orc_sw2d_run(const orc_sw2d_cfg* g, int stepper, int nsteps, double dt, doub
              * w0 = 15 w1 - 5 w0, four stages of dt/6, u = 3/5 w0 + dt/10 L(w0) + w1 */
             memcpy(W0, U, sizeof(double) * n);
             memcpy(W1, U, sizeof(double) * n);
+            static const double cst[10] = {0, 1. / 6, 2. / 6, 3. / 6, 4. / 6, 2. / 6, 3. / 6, 4. / 6, 5. / 6, 1};
             int i = 0;
             for (; i < 5; ++i) {
+                g_src_t = t + cst[i] * h;
                 orc_sw2d_rhs(g, W0, L);
                 for (size_t q = 0; q < n; ++q) W0[q] = W0[q] + h / 6 * L[q];
             }
             for (size_t q = 0; q < n; ++q) W1[q] = 9.0 / 25 * W0[q] + 1.0 / 25 * W1[q];
             for (size_t q = 0; q < n; ++q) W0[q] = 15 * W1[q] + -5 * W0[q];
             for (; i < 9; ++i) {
+                g_src_t = t + cst[i] * h;
                 orc_sw2d_rhs(g, W0, L);
                 for (size_t q = 0; q < n; ++q) W0[q] = W0[q] + h / 6 * L[q];
             }
+            g_src_t = t + h;
             orc_sw2d_rhs(g, W0, L);
             for (size_t q = 0; q < n; ++q) U[q] = 3.0 / 5 * W0[q] + h / 10 * L[q] + 1 * W1[q];
         } else {
             const double dtr = h / 2;
             const double a3 = 1.0 * 2 / (2 * 2 - 1.0), b3 = (2 - 1.0) * h / (2 * (2 * 2 - 1)), c3 = (2 - 1.0) / (2 * 2 - 1);
+            g_src_t = t + 1.0 * 0 / (4 - 2) * h;
             orc_sw2d_rhs(g, U, L);
             for (size_t q = 0; q < n; ++q) W0[q] = U[q] + dtr * L[q];
+            g_src_t = t + 1.0 * 1 / (4 - 2) * h;
             orc_sw2d_rhs(g, W0, L);
             for (size_t q = 0; q < n; ++q) W0[q] = W0[q] + dtr * L[q];
+            g_src_t = t + 1.0 * 2 / (4 - 2) * h;
             orc_sw2d_rhs(g, W0, L);
             for (size_t q = 0; q < n; ++q) W0[q] = a3 * U[q] + b3 * L[q] + c3 * W0[q];
+            g_src_t = t + (1.0 * 3 - 2) / (4 - 2) * h;
             orc_sw2d_rhs(g, W0, L);
             for (size_t q = 0; q < n; ++q) U[q] = W0[q] + dtr * L[q];
         }

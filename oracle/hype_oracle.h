@@ -184,6 +184,15 @@ typedef struct {
 int orc_h2d_rhs(const orc_h2d_cfg* e, const double* U, double* RHS, double* dt_out);
 int orc_h2d_run(const orc_h2d_cfg* e, int nsteps, double* U, double* t_out, double* dt_out);
 
+/* point source + receiver of 3d/weno4/point_source and 2d/weno4/line_source for the
+ * acoustic FV paths above (the source cell's u_t equation gains Source(t) / h^dim, the
+ * receiver records u at every RHS call); the RHS at time t; the trace buffer */
+void orc_set_point_source(int on, int isx, int isy, int isz, double f0, int rec_on, int irx, int iry, int irz);
+void orc_set_trace_buffer(double* t, double* p, int max);
+int orc_trace_count(void);
+int orc_acoustic_rhs_at(const orc_acoustic_cfg* g, double t, const double* U, double* RHS);
+int orc_sw2d_rhs_at(const orc_sw2d_cfg* g, double t, const double* U, double* RHS);
+
 /* OpenMP threads the restatement runs with */
 int orc_threads(void);
 

@@ -114,6 +114,14 @@ def lib():
         L.orc_rusanov.argtypes = [D, D, C.c_int, C.c_double, D, C.POINTER(C.c_int)]
         L.orc_rusanov.restype = C.c_double
         L.orc_threads.restype = C.c_int
+        L.orc_set_point_source.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
+                                           C.c_int]
+        L.orc_set_point_source.restype = None
+        L.orc_set_trace_buffer.argtypes = [D, D, C.c_int]
+        L.orc_set_trace_buffer.restype = None
+        L.orc_trace_count.restype = C.c_int
+        L.orc_acoustic_rhs_at.argtypes = [C.POINTER(AcousticCfg), C.c_double, D, D]
+        L.orc_sw2d_rhs_at.argtypes = [C.POINTER(Sw2dCfg), C.c_double, D, D]
         L.orc_positivity_fallbacks.argtypes = [C.c_int]
         L.orc_positivity_fallbacks.restype = C.c_long
         _lib = L
@@ -597,6 +605,146 @@ def ref_sw2d_program(N):
     l2, li = C.c_double(), C.c_double()
     _ref_sw2d_lib().ref_sw2d_program(int(N), C.byref(l2), C.byref(li), _dp(U0), _dp(U1))
     return l2.value, li.value, U0, U1
+
+
+# ---------------------------------------------------------------- point / line source
+class _Source:
+    """the point source and receiver of 3d/weno4/point_source / 2d/weno4/line_source set
+    on the restatement for the duration of a with-block; ``trace()`` then gives the (t, u)
+    the receiver recorded at each RHS evaluation (at most ``capacity``) and the count"""
+
+    def __init__(self, src, f0, rec, capacity):
+        self.src = tuple(src) + (0,) * (3 - len(src)) if src is not None else None
+        self.rec = tuple(rec) + (0,) * (3 - len(rec)) if rec is not None else None
+        self.f0, self.capacity = f0, int(capacity)
+        self._t = np.zeros(max(self.capacity, 1))
+        self._u = np.zeros(max(self.capacity, 1))
+
+    def __enter__(self):
+        sx, sy, sz = self.src if self.src else (0, 0, 0)
+        rx, ry, rz = self.rec if self.rec else (0, 0, 0)
+        lib().orc_set_point_source(int(self.src is not None), sx, sy, sz, float(self.f0), int(self.rec is not None),
+                                   rx, ry, rz)
+        lib().orc_set_trace_buffer(_dp(self._t), _dp(self._u), self.capacity)
+        return self
+
+    def __exit__(self, *exc):
+        lib().orc_set_point_source(0, 0, 0, 0, 1.0, 0, 0, 0, 0)
+        self.count = lib().orc_trace_count()
+        lib().orc_set_trace_buffer(None, None, 0)
+        return False
+
+    def trace(self):
+        m = min(self.count, self.capacity)
+        return self._t[:m].copy(), self._u[:m].copy(), self.count
+
+
+def point_source(src, f0, rec, capacity=100000):
+    return _Source(src, f0, rec, capacity)
+
+
+def acoustic_rhs_at(cfg, t, U):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    lib().orc_acoustic_rhs_at(C.byref(cfg), float(t), _dp(U), _dp(R))
+    return R
+
+
+def sw2d_rhs_at(cfg, t, U):
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    lib().orc_sw2d_rhs_at(C.byref(cfg), float(t), _dp(U), _dp(R))
+    return R
+
+
+# the programs' compiled-in constants: wave_speed (hype.h:39 / :38) and Source's f0
+# (source.c:13 / :14)
+PSRC3D_C, PSRC3D_F0 = 250.0, 100.0
+LSRC2D_C, LSRC2D_F0 = 580.0, 65.0
+
+_ref_psrc = None
+_ref_lsrc = None
+
+
+def _read_pdat(d):
+    path = os.path.join(d, "results", "p.dat")
+    if not os.path.exists(path):
+        return np.zeros((0, 2))
+    return np.loadtxt(path, ndmin=2)
+
+
+def _ref_psrc_lib():
+    global _ref_psrc
+    if _ref_psrc is None:
+        L = C.CDLL(os.path.join(HERE, "_ref", "libref_psrc3d.so"))
+        IP = C.POINTER(C.c_int)
+        L.ref_psrc3d_rhs.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, IP, IP, IP, C.c_double, D, D, C.c_char_p]
+        L.ref_psrc3d_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, IP, IP, IP, C.c_int, C.c_int, C.c_double,
+                                     C.c_double, D, D, C.c_char_p]
+        _ref_psrc = L
+    return _ref_psrc
+
+
+def _ref_lsrc_lib():
+    global _ref_lsrc
+    if _ref_lsrc is None:
+        L = C.CDLL(os.path.join(HERE, "_ref", "libref_lsrc2d.so"))
+        IP = C.POINTER(C.c_int)
+        L.ref_lsrc2d_rhs.argtypes = [C.c_int, C.c_int, C.c_double, IP, IP, IP, C.c_double, D, D, C.c_char_p]
+        L.ref_lsrc2d_run.argtypes = [C.c_int, C.c_int, C.c_double, IP, IP, IP, C.c_int, C.c_int, C.c_double,
+                                     C.c_double, D, D, C.c_char_p]
+        _ref_lsrc = L
+    return _ref_lsrc
+
+
+def ref_psrc3d_rhs(cfg, src, rec, t, U):
+    """the RHS of 3d/weno4/point_source at time t and its receiver line (results/p.dat)"""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    with tempfile.TemporaryDirectory() as d:
+        os.makedirs(os.path.join(d, "results"))
+        rc = _ref_psrc_lib().ref_psrc3d_rhs(cfg.nx, cfg.ny, cfg.nz, cfg.h, (C.c_int * 6)(*cfg.bc), (C.c_int * 3)(*src),
+                                            (C.c_int * 3)(*rec), float(t), _dp(U), _dp(R), d.encode())
+        assert rc == 0
+        return R, _read_pdat(d)
+
+
+def ref_psrc3d_run(cfg, src, rec, U, nsteps, dt, t_final=0.0, initial_rhs=False):
+    """TSSolve of 3d/weno4/point_source from U (t = 0): (U, t, receiver lines (t, u))"""
+    U = np.array(U, dtype=np.float64, order="C", copy=True)
+    t = C.c_double(0.0)
+    with tempfile.TemporaryDirectory() as d:
+        os.makedirs(os.path.join(d, "results"))
+        rc = _ref_psrc_lib().ref_psrc3d_run(cfg.nx, cfg.ny, cfg.nz, cfg.h, (C.c_int * 6)(*cfg.bc), (C.c_int * 3)(*src),
+                                            (C.c_int * 3)(*rec), int(initial_rhs), int(nsteps), float(dt),
+                                            float(t_final), _dp(U), C.byref(t), d.encode())
+        assert rc == 0
+        return U, t.value, _read_pdat(d)
+
+
+def ref_lsrc2d_rhs(cfg, src, rec, t, U):
+    """the RHS of 2d/weno4/line_source at time t and its receiver line"""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    R = np.zeros_like(U)
+    with tempfile.TemporaryDirectory() as d:
+        os.makedirs(os.path.join(d, "results"))
+        rc = _ref_lsrc_lib().ref_lsrc2d_rhs(cfg.nx, cfg.ny, cfg.h, (C.c_int * 4)(*cfg.bc), (C.c_int * 2)(*src),
+                                            (C.c_int * 2)(*rec), float(t), _dp(U), _dp(R), d.encode())
+        assert rc == 0
+        return R, _read_pdat(d)
+
+
+def ref_lsrc2d_run(cfg, src, rec, U, nsteps, dt, t_final=0.0, stepper=1):
+    """TSSolve of 2d/weno4/line_source from U (t = 0): (U, t, receiver lines (t, u))"""
+    U = np.array(U, dtype=np.float64, order="C", copy=True)
+    t = C.c_double(0.0)
+    with tempfile.TemporaryDirectory() as d:
+        os.makedirs(os.path.join(d, "results"))
+        rc = _ref_lsrc_lib().ref_lsrc2d_run(cfg.nx, cfg.ny, cfg.h, (C.c_int * 4)(*cfg.bc), (C.c_int * 2)(*src),
+                                            (C.c_int * 2)(*rec), int(stepper), int(nsteps), float(dt), float(t_final),
+                                            _dp(U), C.byref(t), d.encode())
+        assert rc == 0
+        return U, t.value, _read_pdat(d)
 
 
 def ref_ctcs2d_run(p_old, p, h, c0, dt, zero_bc, nsteps):

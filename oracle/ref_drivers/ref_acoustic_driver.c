@@ -89,3 +89,57 @@ int ref_acoustic_run(int nx, int ny, int nz, double h, const int* bc, int nsteps
     teardown(&R);
     return 0;
 }
+
+#ifdef REF_POINT_SOURCE
+#include <unistd.h>
+/* 3d/weno4/point_source: the same set-up plus its source and receiver cells (AppCtx
+ * isx..irz, hype.c:59-64).  Its RHSFunction appends the receiver to results/p.dat under the
+ * working directory (rhs_function.c:342-346), so the run switches to dir (which holds a
+ * results/ folder) while it lasts.  initial_rhs: the program's RHSFunction call at the
+ * initial time before TSSolve (hype.c:160), which prints one receiver line. */
+static void set_points(RefAcoustic* R, const int* src, const int* rec) {
+    R->ctx.isx = src[0]; R->ctx.isy = src[1]; R->ctx.isz = src[2];
+    R->ctx.irx = rec[0]; R->ctx.iry = rec[1]; R->ctx.irz = rec[2];
+}
+
+int ref_psrc3d_rhs(int nx, int ny, int nz, double h, const int* bc, const int* src, const int* rec, double t,
+                   const double* U_aos, double* RHS_aos, const char* dir) {
+    char old[4096];
+    if (!getcwd(old, sizeof old) || chdir(dir)) return 1;
+    RefAcoustic R;
+    setup(&R, nx, ny, nz, h, bc);
+    set_points(&R, src, rec);
+    memcpy(R.U->a, U_aos, sizeof(double) * (size_t)R.U->n);
+    RHSFunction(R.ts, t, R.U, R.RHS, &R.ctx);
+    memcpy(RHS_aos, R.RHS->a, sizeof(double) * (size_t)R.U->n);
+    teardown(&R);
+    return chdir(old) ? 1 : 0;
+}
+
+int ref_psrc3d_run(int nx, int ny, int nz, double h, const int* bc, const int* src, const int* rec, int initial_rhs,
+                   int nsteps, double dt, double t_final, double* U_aos, double* t_out, const char* dir) {
+    char old[4096];
+    if (!getcwd(old, sizeof old) || chdir(dir)) return 1;
+    RefAcoustic R;
+    setup(&R, nx, ny, nz, h, bc);
+    set_points(&R, src, rec);
+    memcpy(R.U->a, U_aos, sizeof(double) * (size_t)R.U->n);
+    R.ctx.dt = dt;
+    if (initial_rhs) RHSFunction(R.ts, 0.0, R.U, R.RHS, &R.ctx);
+    TSSetRHSFunction(R.ts, NULL, RHSFunction, &R.ctx);
+    TSSetStepNumber(R.ts, 0);
+    TSSetTime(R.ts, 0.0);
+    TSSetTimeStep(R.ts, dt);
+    TSSetMaxTime(R.ts, t_final > 0.0 ? t_final : 1e300);
+    TSSetMaxSteps(R.ts, nsteps);
+    TSSetExactFinalTime(R.ts, TS_EXACTFINALTIME_MATCHSTEP);
+    TSSetType(R.ts, TSSSP);
+    TSSSPSetType(R.ts, TSSSPRKS3);
+    TSSSPSetNumStages(R.ts, 4);
+    TSSolve(R.ts, R.U);
+    memcpy(U_aos, R.U->a, sizeof(double) * (size_t)R.U->n);
+    if (t_out) *t_out = R.ts->t;
+    teardown(&R);
+    return chdir(old) ? 1 : 0;
+}
+#endif

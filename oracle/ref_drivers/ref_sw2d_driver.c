@@ -114,6 +114,40 @@ int ref_sw2d_run(int nx, int ny, double xmin, double ymin, double h, const int* 
     return 0;
 }
 
+#ifdef REF_LINE_SOURCE
+#include <unistd.h>
+/* 2d/weno4/line_source: the same set-up plus its source and receiver cells (AppCtx isx,
+ * isy, irx, iry, hype.c:52-55); its RHSFunction appends the receiver to results/p.dat under
+ * the working directory (rhs_function.c:249-253), so the run switches to dir meanwhile. */
+int ref_lsrc2d_rhs(int nx, int ny, double h, const int* bc, const int* src, const int* rec, double t,
+                   const double* U_aos, double* RHS_aos, const char* dir) {
+    char old[4096];
+    if (!getcwd(old, sizeof old) || chdir(dir)) return 1;
+    RefSW R;
+    setup(&R, nx, ny, 0.0, 0.0, nx * h, ny * h, h, bc);
+    R.ctx.isx = src[0]; R.ctx.isy = src[1]; R.ctx.irx = rec[0]; R.ctx.iry = rec[1];
+    memcpy(R.U->a, U_aos, sizeof(double) * (size_t)R.U->n);
+    RHSFunction(R.ts, t, R.U, R.RHS, &R.ctx);
+    memcpy(RHS_aos, R.RHS->a, sizeof(double) * (size_t)R.U->n);
+    teardown(&R);
+    return chdir(old) ? 1 : 0;
+}
+
+int ref_lsrc2d_run(int nx, int ny, double h, const int* bc, const int* src, const int* rec, int stepper, int nsteps,
+                   double dt, double t_final, double* U_aos, double* t_out, const char* dir) {
+    char old[4096];
+    if (!getcwd(old, sizeof old) || chdir(dir)) return 1;
+    RefSW R;
+    setup(&R, nx, ny, 0.0, 0.0, nx * h, ny * h, h, bc);
+    R.ctx.isx = src[0]; R.ctx.isy = src[1]; R.ctx.irx = rec[0]; R.ctx.iry = rec[1];
+    memcpy(R.U->a, U_aos, sizeof(double) * (size_t)R.U->n);
+    solve(&R, stepper, nsteps, dt, t_final);
+    memcpy(U_aos, R.U->a, sizeof(double) * (size_t)R.U->n);
+    if (t_out) *t_out = R.ts->t;
+    teardown(&R);
+    return chdir(old) ? 1 : 0;
+}
+#else
 /* the program of hype.c at N x N cells: [-1,1]^2, adiabatic walls, CFL 0.5, dt = h CFL / 2,
  * RK104 to FinalTime 1.0, then ErrorNorms (post_process.c); U0/U1 (optional) receive the
  * initial and final states */
@@ -133,3 +167,4 @@ int ref_sw2d_program(int N, double* l2, double* linf, double* U0, double* U1) {
     teardown(&R);
     return 0;
 }
+#endif

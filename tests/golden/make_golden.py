@@ -158,6 +158,30 @@ def h2d_fixtures():
                                 N=N, nx=nx, ny=ny, h=h, cfl=0.9, bc=np.array(bc), eos=np.array(O.H2D_EOS))
 
 
+def source_fixtures():
+    """3d/weno4/point_source and 2d/weno4/line_source: the RHS at a time t of a random state
+    and a run from rest (the program's initial condition) with the receiver's p.dat lines"""
+    rng = np.random.default_rng(81)
+    for name, bc in (("periodic", (0,) * 6), ("mixed", (4, 4, 0, 0, 4, 4))):
+        n, h, dt, src, rec = 16, 0.5, 0.0005, (8, 8, 8), (11, 10, 9)
+        cfg = O.acoustic_cfg(n, h, bc=bc, c=O.PSRC3D_C)
+        U = 1e-3 * rng.standard_normal((n, n, n, 2))
+        R, line = O.ref_psrc3d_rhs(cfg, src, rec, 0.037, U)
+        Un, tn, pdat = O.ref_psrc3d_run(cfg, src, rec, np.zeros_like(U), 24, dt, initial_rhs=True)
+        np.savez_compressed(os.path.join(HERE, f"ref_psrc3d_{name}.npz"), U=U, RHS=R, t_rhs=0.037, line=line, Un=Un,
+                            tn=tn, pdat=pdat, steps=24, dt=dt, h=h, n=n, bc=np.array(bc), src=np.array(src),
+                            rec=np.array(rec), c=O.PSRC3D_C, f0=O.PSRC3D_F0)
+    for name, bc, stepper in (("periodic", (0,) * 4, 1), ("mixed", (4, 4, 0, 0), 0)):
+        n, h, dt, src, rec = 48, 1.0, 0.001, (24, 24), (30, 28)
+        cfg = O.sw2d_cfg(n, n, h, bc=bc, c=O.LSRC2D_C)
+        U = 1e-3 * rng.standard_normal((n, n, 2))
+        R, line = O.ref_lsrc2d_rhs(cfg, src, rec, 0.05, U)
+        Un, tn, pdat = O.ref_lsrc2d_run(cfg, src, rec, np.zeros_like(U), 30, dt, stepper=stepper)
+        np.savez_compressed(os.path.join(HERE, f"ref_lsrc2d_{name}.npz"), U=U, RHS=R, t_rhs=0.05, line=line, Un=Un,
+                            tn=tn, pdat=pdat, steps=30, dt=dt, h=h, n=n, bc=np.array(bc), src=np.array(src),
+                            rec=np.array(rec), c=O.LSRC2D_C, f0=O.LSRC2D_F0, stepper=stepper)
+
+
 def main():
     O.build(REF)
     src = os.path.join(REF, "3d/ctcs/point_source/results/p.dat")
@@ -205,6 +229,7 @@ def main():
     sw2d_fixtures()
     mp3d_fixtures()
     h2d_fixtures()
+    source_fixtures()
     n = 32
     x = -1 + np.arange(n) * (2.0 / n)
     Xg, Yg = np.meshgrid(x, x)

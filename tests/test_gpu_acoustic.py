@@ -59,3 +59,60 @@ def test_published_convergence_table(hype, oracle):
         l2, linf = oracle.plane_wave_errors(cfg, s.get_state(), s.t)
         print(f"plane wave N={n}: L2 {l2:.4e} (table {table[n][0]:.2e}), Linf {linf:.4e} (table {table[n][1]:.2e})")
         assert abs(l2 - table[n][0]) <= 2e-3 * table[n][0] and abs(linf - table[n][1]) <= 2e-3 * table[n][1]
+
+
+# ---------------------------------------------------------------- 3d/weno4/point_source
+@pytest.mark.parametrize("name", ["periodic", "mixed"])
+def test_point_source_vs_reference(hype, oracle, name):
+    """the RHS with Source(t)/h^3 at the source cell, and the program's run from rest (its
+    RHSFunction call at t = 0, hype.c:160, then TSSolve): state against the reference's,
+    receiver trace against its p.dat lines and, sample by sample, the CPU checker's"""
+    z = np.load(os.path.join(GOLDEN, f"ref_psrc3d_{name}.npz"))
+    n, h, dt, f0 = int(z["n"]), float(z["h"]), float(z["dt"]), float(z["f0"])
+    src, rec = tuple(int(v) for v in z["src"]), tuple(int(v) for v in z["rec"])
+    bc = tuple(int(b) for b in z["bc"])
+    s = hype.AcousticFV3D(n, n, n, h, dt, c=float(z["c"]), boundaries=bc)
+    s.set_point_source(src, f0, rec, capacity=1000)
+    assert rel(s.RHSFunction(float(z["t_rhs"]), z["U"]), z["RHS"]) <= 1e-12
+    t, u, cnt = s.receiver_trace()
+    assert cnt == 1 and t[0] == float(z["t_rhs"]) and u[0] == z["U"][rec[2], rec[1], rec[0], 0]
+    s.set_point_source(src, f0, rec, capacity=1000)
+    U0 = np.zeros_like(z["U"])
+    s.RHSFunction(0.0, U0)
+    s.set_state(U0)
+    assert s.step(int(z["steps"])) == int(z["steps"])
+    assert rel(s.get_state(), z["Un"]) <= 1e-12 and s.t == float(z["tn"])
+    t, u, cnt = s.receiver_trace()
+    pdat = z["pdat"]
+    assert cnt == len(pdat) == 1 + 4 * int(z["steps"])
+    assert np.all(np.abs(pdat[:, 0] - t) <= 1e-5 * np.abs(t) + 1e-300)
+    assert np.abs(pdat[:, 1] - u).max() <= 1e-11 * np.abs(u).max()
+    cfg = oracle.acoustic_cfg(n, h, bc=bc, c=float(z["c"]))
+    with oracle.point_source(src, f0, rec) as S:
+        oracle.acoustic_rhs_at(cfg, 0.0, U0)
+        oracle.acoustic_run(cfg, U0, int(z["steps"]), dt)
+    to, uo, co = S.trace()
+    assert co == cnt and np.array_equal(to, t) and rel(u, uo) <= 1e-12
+
+
+def test_point_source_program_matches_greens_function(hype):
+    """the whole 3d/weno4/point_source program (100^3 cells of h = 0.5, c = 250, dt = 5e-4,
+    251 steps, source at (50,50,50), receiver at (57,57,57)) against the analytic receiver
+    signal S(t - r/c) / (4 pi c^2 r): relative L2 misfit below 0.5 % (0.29 % measured with
+    the CPU checker)"""
+    from acoustic_petsc_gb300 import analytic
+
+    n, h, dt, c, f0 = 100, 0.5, 0.0005, 250.0, 100.0
+    s = hype.AcousticFV3D(n, n, n, h, dt, c=c)
+    s.set_point_source((50, 50, 50), f0, (57, 57, 57), capacity=4 * 251 + 1)
+    U0 = np.zeros((n, n, n, 2))
+    s.RHSFunction(0.0, U0)
+    s.set_state(U0)
+    assert s.step(10**6, t_final=251 * dt) == 251
+    t, u, cnt = s.receiver_trace()
+    assert cnt == 1 + 4 * 251
+    ts, us = t[1::4], u[1::4]  # the first stage of every step: t = step * dt
+    ua = analytic.point_source_receiver_3d(ts, 7 * math.sqrt(3.0) * h, c, f0)
+    misfit = analytic.relative_l2_misfit(us, ua)
+    print(f"point source 100^3: receiver misfit {misfit:.3e}")
+    assert misfit < 5e-3

@@ -255,3 +255,63 @@ def test_h2d_rhs_and_steps_match_reference_bitwise(oracle, name):
     assert rc == 0
     assert np.array_equal(U3, z["U3"]) and t3 == float(z["t3"])
 
+
+
+# ---------------------------------------------------------------- 3d/weno4/point_source, 2d/weno4/line_source
+def _pdat_close(t, u, pdat, t_digits):
+    """receiver samples against the program's p.dat lines: u printed with 13 significant
+    digits (%.12e), t with 6 (%e / %g)"""
+    assert pdat.shape == (len(t), 2)
+    assert np.all(np.abs(pdat[:, 0] - t) <= 10.0 ** (1 - t_digits) * np.maximum(np.abs(t), 1e-300) + 1e-300)
+    scale = max(np.abs(u).max(), 1e-300)
+    assert np.abs(pdat[:, 1] - u).max() <= 1e-12 * scale
+
+
+def _src_case(oracle, z, dim):
+    bc = tuple(int(b) for b in z["bc"])
+    n, h, c = int(z["n"]), float(z["h"]), float(z["c"])
+    cfg = oracle.acoustic_cfg(n, h, bc=bc, c=c) if dim == 3 else oracle.sw2d_cfg(n, n, h, bc=bc, c=c)
+    src = tuple(int(v) for v in z["src"])
+    rec = tuple(int(v) for v in z["rec"])
+    return cfg, src, rec, float(z["f0"])
+
+
+@pytest.mark.parametrize("name", ["periodic", "mixed"])
+def test_point_source_3d_matches_reference(oracle, name):
+    """3d/weno4/point_source: Source(t)/h^3 added at the source cell at the RHS time
+    (rhs_function.c:337-339), SSP RKS3 stage times t + (0, 1/2, 1, 1/2) dt, the receiver
+    line printed at every RHS evaluation (hype.c:160's initial call included)"""
+    z = np.load(os.path.join(GOLDEN, f"ref_psrc3d_{name}.npz"))
+    cfg, src, rec, f0 = _src_case(oracle, z, 3)
+    with oracle.point_source(src, f0, rec) as S:
+        R = oracle.acoustic_rhs_at(cfg, float(z["t_rhs"]), z["U"])
+    assert np.array_equal(R, z["RHS"])
+    t, u, cnt = S.trace()
+    _pdat_close(t, u, z["line"], 6)
+    with oracle.point_source(src, f0, rec) as S:
+        U0 = np.zeros_like(z["U"])
+        oracle.acoustic_rhs_at(cfg, 0.0, U0)
+        U, tn, steps = oracle.acoustic_run(cfg, U0, int(z["steps"]), float(z["dt"]))
+    assert np.array_equal(U, z["Un"]) and tn == float(z["tn"])
+    t, u, cnt = S.trace()
+    assert cnt == 1 + 4 * int(z["steps"]) and np.abs(u).max() > 0
+    _pdat_close(t, u, z["pdat"], 6)
+
+
+@pytest.mark.parametrize("name", ["periodic", "mixed"])
+def test_line_source_2d_matches_reference(oracle, name):
+    """2d/weno4/line_source: Source(t)/h^2 at the source cell (rhs_function.c:244-246),
+    RK104 stage times t + (0,1,2,3,4,2,3,4,5,6)/6 dt (or RKS3's), receiver at every RHS"""
+    z = np.load(os.path.join(GOLDEN, f"ref_lsrc2d_{name}.npz"))
+    cfg, src, rec, f0 = _src_case(oracle, z, 2)
+    with oracle.point_source(src, f0, rec) as S:
+        R = oracle.sw2d_rhs_at(cfg, float(z["t_rhs"]), z["U"])
+    assert np.array_equal(R, z["RHS"])
+    _pdat_close(*S.trace()[:2], z["line"], 6)
+    stepper = int(z["stepper"])
+    with oracle.point_source(src, f0, rec) as S:
+        U, tn, steps = oracle.sw2d_run(cfg, np.zeros_like(z["U"]), int(z["steps"]), float(z["dt"]), stepper=stepper)
+    assert np.array_equal(U, z["Un"]) and tn == float(z["tn"])
+    t, u, cnt = S.trace()
+    assert cnt == (10 if stepper == 1 else 4) * int(z["steps"]) and np.abs(u).max() > 0
+    _pdat_close(t, u, z["pdat"], 6)

@@ -210,3 +210,43 @@ def test_h2d_rhs_and_run_bitwise(oracle, N, bc):
         assert r1 == r2 == 0
         assert np.array_equal(U1, U2) and t1 == t2
 
+
+
+@pytest.mark.parametrize("bc", [(0,) * 6, (4, 4, 4, 4, 0, 0)])
+def test_point_source_3d_bitwise(oracle, bc):
+    """3d/weno4/point_source on a fresh grid: RHS at a time t, a run from rest through the
+    wavelet's peak (t0 = 4/f0 = 0.04) with a shortened final step"""
+    _need_ref(oracle)
+    cfg = oracle.acoustic_cfg((12, 10, 9), 0.5, bc=bc, c=oracle.PSRC3D_C)
+    src, rec = (5, 4, 6), (8, 2, 3)
+    U = 1e-3 * np.random.default_rng(91).standard_normal((9, 10, 12, 2))
+    R, line = oracle.ref_psrc3d_rhs(cfg, src, rec, 0.0403, U)
+    with oracle.point_source(src, oracle.PSRC3D_F0, rec):
+        assert np.array_equal(oracle.acoustic_rhs_at(cfg, 0.0403, U), R)
+    Ur, tr, pdat = oracle.ref_psrc3d_run(cfg, src, rec, np.zeros_like(U), 10**6, 0.0005, t_final=0.04512)
+    with oracle.point_source(src, oracle.PSRC3D_F0, rec) as S:
+        Uo, to, n = oracle.acoustic_run(cfg, np.zeros_like(U), 10**6, 0.0005, t_final=0.04512)
+    assert np.array_equal(Uo, Ur) and to == tr
+    t, u, cnt = S.trace()
+    assert cnt == len(pdat) == 4 * n
+    assert np.abs(pdat[:, 1] - u).max() <= 1e-12 * np.abs(u).max()
+
+
+@pytest.mark.parametrize("stepper", [1, 0])
+def test_line_source_2d_bitwise(oracle, stepper):
+    """2d/weno4/line_source on a fresh grid, RK104 (the program's) and RKS3/4"""
+    _need_ref(oracle)
+    cfg = oracle.sw2d_cfg(40, 36, 1.0, bc=(0, 0, 4, 4), c=oracle.LSRC2D_C)
+    src, rec = (20, 17), (26, 21)
+    U = 1e-3 * np.random.default_rng(92).standard_normal((36, 40, 2))
+    R, line = oracle.ref_lsrc2d_rhs(cfg, src, rec, 0.061, U)
+    with oracle.point_source(src, oracle.LSRC2D_F0, rec):
+        assert np.array_equal(oracle.sw2d_rhs_at(cfg, 0.061, U), R)
+    Ur, tr, pdat = oracle.ref_lsrc2d_run(cfg, src, rec, np.zeros_like(U), 10**6, 0.001, t_final=0.0705,
+                                         stepper=stepper)
+    with oracle.point_source(src, oracle.LSRC2D_F0, rec) as S:
+        Uo, to, n = oracle.sw2d_run(cfg, np.zeros_like(U), 10**6, 0.001, t_final=0.0705, stepper=stepper)
+    assert np.array_equal(Uo, Ur) and to == tr
+    t, u, cnt = S.trace()
+    assert cnt == len(pdat) == (10 if stepper == 1 else 4) * n
+    assert np.abs(pdat[:, 1] - u).max() <= 1e-12 * np.abs(u).max()
