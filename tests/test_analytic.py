@@ -33,3 +33,16 @@ def test_point_source_signal_delay_and_amplitude():
     shift = int(round((r / c) / (t[1] - t[0])))
     assert np.allclose(u[shift:], s[: len(t) - shift] / (4 * np.pi * c * c * r), rtol=0, atol=1e-9 * np.abs(u).max())
     assert abs(np.abs(u).max() - np.abs(s).max() / (4 * np.pi * c * c * r)) <= 1e-6 * np.abs(u).max()
+
+
+def test_reference_ctcs_point_source_trace_matches_analytic_signal():
+    """the reference's own receiver trace of 3d/ctcs/point_source (results/p.dat, the same
+    source, receiver and grid as 3d/weno4/point_source: h = 0.5, c = 250, f0 = 100, 7 cells
+    apart on the diagonal) against S(t - r/c) / (4 pi c^2 r): 0.27 % relative L2"""
+    import os
+
+    from conftest import GOLDEN
+
+    d = np.loadtxt(os.path.join(GOLDEN, "point_source_p.dat"))
+    ua = analytic.point_source_receiver_3d(d[:, 0], 7 * np.sqrt(3.0) * 0.5, 250.0, 100.0)
+    assert analytic.relative_l2_misfit(d[:, 1], ua) < 5e-3
