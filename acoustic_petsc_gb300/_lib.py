@@ -19,7 +19,7 @@ F = C.POINTER(C.c_float)
 HYPE_OK, HYPE_ERR_ARG, HYPE_ERR_STATE, HYPE_ERR_CUDA, HYPE_ERR_NOMEM, HYPE_ERR_UNSUPPORTED = range(6)
 BC_PERIODIC, BC_REFLECTIVE, BC_TRANSMISSIVE, BC_ZERO, BC_ADIABATIC = range(5)
 RECON_CWENO4, RECON_LINEAR4, RECON_LEARNED, RECON_WENO3 = 0, 1, 2, 3
-PREC_FP64, PREC_FP32 = 0, 1
+PREC_FP64, PREC_FP32, PREC_DF64 = 0, 1, 2
 DT_MONITOR, DT_FROZEN, DT_FIXED = 0, 1, 2
 FLUX_RUSANOV, FLUX_HLLC, FLUX_ROTHLLC = 0, 1, 2
 MP_DI4, MP_KAPILA5 = 0, 1

@@ -1,0 +1,97 @@
+// df64.cuh -- double-float arithmetic: a value is the unevaluated sum hi + lo of two
+// FP32 numbers with |lo| <= ulp(hi)/2, a 48-bit significand with the FP32 exponent range.
+//
+// Why on GB300: its FP64 pipe issues 1/64 of the FP32 rate, so a reconstruction that is
+// bound by FP64 instruction issue runs several times faster on FP32 pairs, where an add
+// costs ~11 and a multiply ~6 FP32 instructions.  The building blocks are the classical
+// error-free transformations: Knuth's TwoSum, Dekker's FastTwoSum and the FMA-based
+// TwoProduct (exact a*b = p + e); the operations follow the double-double algorithms of
+// Dekker (1971) and Hida, Li & Bailey's QD library report (2001), "sloppy" addition
+// (error ~2^-48 (|x| + |y|)).  Every FP32 operation goes through an _rn intrinsic, which the
+// compiler never contracts into an FMA or reorders: the transformations rely on the
+// rounding of each individual operation.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace hype {
+
+struct __align__(8) df64 {
+    float hi, lo;
+};
+
+// exact split of an FP64 value: hi = fl32(x), lo = fl32(x - hi) (x - hi is exact in FP64)
+__device__ __forceinline__ df64 df_from_double(double x) {
+    const float h = __double2float_rn(x);
+    return df64{h, __double2float_rn(x - (double)h)};
+}
+
+__device__ __forceinline__ double df_to_double(df64 a) { return (double)a.hi + (double)a.lo; }
+
+// a compile-time constant c as a pair (folded by the compiler for literal arguments)
+__host__ __device__ constexpr df64 dfc(double c) {
+    return df64{(float)c, (float)(c - (double)(float)c)};
+}
+
+__device__ __forceinline__ df64 df_fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+    const float s = __fadd_rn(a, b);
+    return df64{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ df64 df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bp = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+    return df64{s, e};
+}
+
+__device__ __forceinline__ df64 operator+(df64 x, df64 y) {
+    const df64 s = df_two_sum(x.hi, y.hi);
+    return df_fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+
+__device__ __forceinline__ df64 operator-(df64 x) { return df64{-x.hi, -x.lo}; }
+
+__device__ __forceinline__ df64 operator-(df64 x, df64 y) {
+    const df64 s = df_two_sum(x.hi, -y.hi);
+    return df_fast_two_sum(s.hi, __fadd_rn(s.lo, __fsub_rn(x.lo, y.lo)));
+}
+
+__device__ __forceinline__ df64 operator*(df64 x, df64 y) {
+    const float p = __fmul_rn(x.hi, y.hi);
+    float e = __fmaf_rn(x.hi, y.hi, -p);
+    e = __fmaf_rn(x.hi, y.lo, e);
+    e = __fmaf_rn(x.lo, y.hi, e);
+    return df_fast_two_sum(p, e);
+}
+
+// times an FP32 number
+__device__ __forceinline__ df64 df_mul(df64 x, float c) {
+    const float p = __fmul_rn(x.hi, c);
+    const float e = __fmaf_rn(x.lo, c, __fmaf_rn(x.hi, c, -p));
+    return df_fast_two_sum(p, e);
+}
+
+// times a power of two (exact)
+__device__ __forceinline__ df64 df_scale(df64 x, float two_pow) { return df64{__fmul_rn(x.hi, two_pow), __fmul_rn(x.lo, two_pow)}; }
+
+__device__ __forceinline__ df64 df_sqr(df64 x) {
+    const float p = __fmul_rn(x.hi, x.hi);
+    float e = __fmaf_rn(x.hi, x.hi, -p);
+    e = __fmaf_rn(__fadd_rn(x.hi, x.hi), x.lo, e);
+    return df_fast_two_sum(p, e);
+}
+
+// x / y: the FP32 quotient q1 = x.hi / y.hi, the remainder x - q1 y in double-float, and
+// its quotient as the correction
+__device__ __forceinline__ df64 df_div(df64 x, df64 y) {
+    const float q1 = __fdiv_rn(x.hi, y.hi);
+    const df64 r = x - df_mul(y, q1);
+    const float q2 = __fdiv_rn(r.hi, y.hi);
+    return df_fast_two_sum(q1, q2);
+}
+
+__device__ __forceinline__ bool df_lt(df64 a, df64 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ df64 df_min(df64 a, df64 b) { return df_lt(b, a) ? b : a; }
+
+}  // namespace hype

@@ -24,6 +24,7 @@
 
 #include <vector>
 
+#include "euler_df64.cuh"
 #include "euler_kernels.cuh"
 #include "mlp_kernels.cuh"
 
@@ -315,6 +316,97 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1)
     }
     if (pad && !(f32 ? ck.ok : traces_admissible<R>(T, g, e, gm1))) {
         store_first_order_g<R>(G, T, g, ge, e);
+        if (!gi && !gj && !gk) atomicAdd(&counters[1], 1ull);
+    }
+}
+
+// HYPE_PREC_DF64: the per-variable reference value r_c of one stage, the stage input's
+// value at cell 0 rounded to FP32 (the deviations u - r_c are formed in FP64, the traces
+// r_c + deviation are rounded once in FP64)
+__device__ __forceinline__ double df_ref(const double* __restrict__ W, const Geo& g, int c) {
+    return (double)__double2float_rn(__ldg(W + (long long)c * g.N));
+}
+
+// ghost fill as k_ghost, storing the deviation from r_c as a double-float pair
+__global__ void __launch_bounds__(128) k_ghost_df(const double* __restrict__ W, df64* __restrict__ G, Geo g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - GW;
+    const int j = blockIdx.y - GW, k = blockIdx.z - GW;
+    if (i >= g.nx + GW) return;
+    int fi = 0, fj = 0, fk = 0;
+    const int mi = bmap(i, g.nx, g.bc[0], g.bc[1], &fi);
+    const int mj = bmap(j, g.ny, g.bc[2], g.bc[3], &fj);
+    const int mk = bmap(k, g.nz, g.bc[4], g.bc[5], &fk);
+    const long long src = ((long long)mk * g.ny + mj) * g.nx + mi;
+    const long long dst = ghost_index(g, i, j, k);
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        double v = __ldg(W + (long long)c * g.N + src);
+        if ((c == 1 && fi) || (c == 2 && fj) || (c == 3 && fk)) v = -v;
+        G[(long long)c * g.GN + dst] = df_from_double(v - df_ref(W, g, c));
+    }
+}
+
+// CWENO4 / R4 reconstruction in double-float on the deviations (euler_df64.cuh); the
+// traces go out as FP64 values r_c + deviation, the same array the FP64 faces consume
+__global__ void __launch_bounds__(128, 1)
+    k_recon_df(const df64* __restrict__ G, double* __restrict__ T, const double* __restrict__ W, Geo g, int recon,
+               int pad, double gm1, unsigned long long* __restrict__ counters) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+    const int k = blockIdx.z - 1;
+    if (i > g.nx || j > g.ny) return;
+    const int gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny), gk = (k < 0 || k >= g.nz);
+    if (gi + gj + gk > 1) return;
+    const long long e = ext_index(g, i, j, k), ge = ghost_index(g, i, j, k);
+    const int sy = g.gx, sz = g.gx * g.gy;
+#pragma unroll 1
+    for (int c = 0; c < NV; ++c) {
+        df64 s[33], cf[20];
+        {
+            const df64* p = G + (long long)c * g.GN + ge;
+            s[0] = p[0];
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                const int off = (o == 0) ? -2 : (o == 1) ? -1 : (o == 2) ? 1 : 2;
+                s[S1(0, off)] = p[off];
+                s[S1(1, off)] = p[off * sy];
+                s[S1(2, off)] = p[off * sz];
+            }
+#pragma unroll
+            for (int sa = 0; sa < 2; ++sa)
+#pragma unroll
+                for (int sb = 0; sb < 2; ++sb) {
+                    s[SQ(0, sa, 1, sb)] = p[(2 * sa - 1) + (2 * sb - 1) * sy];
+                    s[SQ(1, sa, 2, sb)] = p[(2 * sa - 1) * sy + (2 * sb - 1) * sz];
+                    s[SQ(0, sa, 2, sb)] = p[(2 * sa - 1) + (2 * sb - 1) * sz];
+                }
+#pragma unroll
+            for (int a = 0; a < 2; ++a)
+#pragma unroll
+                for (int b = 0; b < 2; ++b)
+#pragma unroll
+                    for (int d = 0; d < 2; ++d) s[SO(a, b, d)] = p[(2 * a - 1) + (2 * b - 1) * sy + (2 * d - 1) * sz];
+        }
+        cweno4_df(s, recon == HYPE_RECON_LINEAR4, cf);
+        const double r = df_ref(W, g, c);
+        double* Tc = T + (long long)c * NTR * g.NE + e;
+        df64 tr[8];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            if (d == 0) face_traces_df<0>(cf, tr);
+            else if (d == 1) face_traces_df<1>(cf, tr);
+            else face_traces_df<2>(cf, tr);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) Tc[(long long)(8 * d + q) * g.NE] = r + df_to_double(tr[q]);
+        }
+    }
+    if (pad && !traces_admissible<double>(T, g, e, gm1)) {
+#pragma unroll 1
+        for (int c = 0; c < NV; ++c) {
+            const double v = df_ref(W, g, c) + df_to_double(G[(long long)c * g.GN + ge]);
+            double* Tc = T + (long long)c * NTR * g.NE + e;
+            for (int q = 0; q < NTR; ++q) Tc[(long long)q * g.NE] = v;
+        }
         if (!gi && !gj && !gk) atomicAdd(&counters[1], 1ull);
     }
 }
@@ -833,10 +925,12 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
     const Geo& g = e->g;
     const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2);
     const bool f32 = e->p.precision == HYPE_PREC_FP32;
+    const bool df = e->p.precision == HYPE_PREC_DF64;
     const int rec = e->p.recon;
     prof_mark(e, 0, true);
     const dim3 bgh(128), ggh(cdiv(g.gx, 128), g.gy, g.nz + 2 * GW);
     if (f32) k_ghost<float><<<ggh, bgh, 0, e->stream>>>(Win, (float*)e->G, g);
+    else if (df) k_ghost_df<<<ggh, bgh, 0, e->stream>>>(Win, (df64*)e->G, g);
     else k_ghost<double><<<ggh, bgh, 0, e->stream>>>(Win, (double*)e->G, g);
     HYPE_LAUNCHED(1);
     const double gm1 = e->p.gamma - 1.0;
@@ -849,6 +943,9 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
         else
             k_recon_learned<double><<<gr, br, 0, e->stream>>>((const double*)e->G, (double*)e->T, g, e->mlp, e->logit_thr,
                                                               gm1, e->p.positivity, e->mlp_cnt);
+    } else if (df) {
+        k_recon_df<<<gr, br, 0, e->stream>>>((const df64*)e->G, (double*)e->T, Win, g, rec, e->p.positivity, gm1,
+                                             e->mlp_cnt);
     } else if (f32) {
         k_recon<float><<<gr, br, ck_bytes, e->stream>>>((const float*)e->G, (float*)e->T, g, rec, e->p.positivity, gm1,
                                                         e->mlp_cnt);
@@ -893,7 +990,11 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
     for (int d = 0; d < 3; ++d)
         if ((p->bc[2 * d] == HYPE_BC_PERIODIC) != (p->bc[2 * d + 1] == HYPE_BC_PERIODIC)) return HYPE_ERR_ARG;
     if (p->recon < HYPE_RECON_CWENO4 || p->recon > HYPE_RECON_WENO3) return HYPE_ERR_ARG;
-    if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32) return HYPE_ERR_ARG;
+    if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32 && p->precision != HYPE_PREC_DF64)
+        return HYPE_ERR_ARG;
+    // the double-float form covers CWENO4 and R4 (no WENO3, indicator or viscous fluxes)
+    if (p->precision == HYPE_PREC_DF64 && p->recon != HYPE_RECON_CWENO4 && p->recon != HYPE_RECON_LINEAR4)
+        return HYPE_ERR_UNSUPPORTED;
     if (p->dt_mode < HYPE_DT_MONITOR || p->dt_mode > HYPE_DT_FIXED) return HYPE_ERR_ARG;
     if (p->flux < HYPE_FLUX_RUSANOV || p->flux > HYPE_FLUX_ROTHLLC) return HYPE_ERR_ARG;
     if (p->positivity != 0 && p->positivity != 1) return HYPE_ERR_ARG;
@@ -1167,6 +1268,8 @@ extern "C" int hype_euler_indicator_stats(hype_euler* e, long long* flagged, lon
 extern "C" int hype_euler_set_recon(hype_euler* e, int recon) {
     if (!e || recon < HYPE_RECON_CWENO4 || recon > HYPE_RECON_WENO3) return HYPE_ERR_ARG;
     if (e->C4 && recon == HYPE_RECON_LEARNED) return HYPE_ERR_ARG;  // the viscous path keeps the R4 coefficients
+    if (e->p.precision == HYPE_PREC_DF64 && recon != HYPE_RECON_CWENO4 && recon != HYPE_RECON_LINEAR4)
+        return HYPE_ERR_UNSUPPORTED;
     HYPE_CK(cudaStreamSynchronize(e->stream));
     e->p.recon = recon;
     return HYPE_OK;

@@ -9,7 +9,8 @@ cell-updates/s (cells x steps / s).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl reference]
 
 Other workloads (--workload): euler256_fp32 (FP32 reconstruction/flux, FP64
-state), euler256_linear (optimal-weight linear reconstruction), euler256_weno3,
+state), euler256_df64 (double-float reconstruction on the FP32 pipe, FP64 state and
+flux, held to the FP64 error bars), euler256_linear (optimal-weight linear reconstruction), euler256_weno3,
 euler256_hllc, ns256_tgv (viscous Taylor-Green), acoustic256 (3D acoustic FV),
 sw2d4096 (2D standing wave, RK104), mp3d256 (3D primitive multiphase), pc2d2048 (2d/HyPE-2D path-conservative
 Kapila, order 3), kapila1024[_fp32|_learned], blast256/512,
@@ -214,6 +215,10 @@ FLUX_TAG = {0: "rusanov", 1: "hllc", 2: "rothllc"}
 FLUX_NAME = {0: "Rusanov", 1: "HLLC", 2: "rotated HLLC"}
 
 
+EULER_DTYPE = {0: "f64", 1: "f64 state / f32 recon+flux",
+               2: "f64 state+flux / df64 recon (FP32 pairs, 48-bit significand, on deviations)"}
+
+
 def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscous=False):
     import torch
 
@@ -263,12 +268,13 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
     bytes_stage = EULER_BYTES_PER_CELL_STAGE + (NS_COEF_BYTES_PER_CELL_STAGE if viscous else 0.0)
     achieved_gbs = bytes_stage * cells / t_stage / 1e9
     peak, peak_kind = _peaks()
-    tag = {0: "fp64", 1: "fp32"}[precision] + ("_linear" if recon else "") + ("_ns" if viscous else "")
+    tag = {0: "fp64", 1: "fp32", 2: "df64"}[precision] + ("_linear" if recon else "") + ("_ns" if viscous else "")
     prof_file = "ns3d_tgv_stage_fp64.txt" if viscous else f"euler_stage_{tag}.txt"
     traffic = _profile_figure(prof_file, "dram_bytes_per_cell_stage")
     flops_cell = _profile_figure(prof_file, "fp_flops_per_cell_stage")
     fpeak = C.c_double()
-    H._lib.check(L.hype_probe_fma_peak(precision, C.byref(fpeak)), "probe")
+    # the double-float form runs its reconstruction on the FP32 pipe
+    H._lib.check(L.hype_probe_fma_peak(1 if precision == 2 else precision, C.byref(fpeak)), "probe")
     roof = {"kernel": "RK stage = k_recon + k_faces x3 + k_update (per-stage average)", "bound": "hbm",
             "achieved": achieved_gbs, "peak": peak, "unit": "GB/s", "frac": achieved_gbs / peak,
             "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
@@ -310,7 +316,7 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
     out = {
         "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == 0 else "f64 state / f32 recon+flux",
+        "scaling": "weak", "vs_baseline": None, "dtype": EULER_DTYPE[precision],
         "data": ("synthetic: Taylor-Green vortex of initial_condition.c at the cell centres" if viscous else
                  "synthetic: Gaussian acoustic pulse dp = 1e-3 exp(-r^2/(2*0.04^2)), 5^3-Gauss cell averages"),
         "config": {"workload": (f"ns3d_tgv_{RECON_TAG[recon]}_{FLUX_TAG[flux]}_ssprk43_{n}" if viscous else
@@ -881,6 +887,9 @@ WORKLOADS = {
     "euler256_hllc": lambda a, *r: run_euler(a, *r, precision=0, recon=0, flux=1),
     "euler256": lambda a, *r: run_euler(a, *r, precision=0, recon=0),
     "euler256_fp32": lambda a, *r: run_euler(a, *r, precision=1, recon=0),
+    "euler256_df64": lambda a, *r: run_euler(a, *r, precision=2, recon=0),
+    "euler256_df64_linear": lambda a, *r: run_euler(a, *r, precision=2, recon=1),
+    "euler128_df64": lambda a, *r: run_euler(a, *r, precision=2, recon=0, n=128),
     "euler256_linear": lambda a, *r: run_euler(a, *r, precision=0, recon=1),
     "euler256_fp32_linear": lambda a, *r: run_euler(a, *r, precision=1, recon=1),
     "euler256_weno3": lambda a, *r: run_euler(a, *r, precision=0, recon=3),

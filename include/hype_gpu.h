@@ -63,6 +63,11 @@ extern "C" {
 /* arithmetic of reconstruction + flux (the state and the RK accumulation are always FP64) */
 #define HYPE_PREC_FP64 0
 #define HYPE_PREC_FP32 1
+/* 3D Euler (CWENO4 / R4): state, flux and stage accumulation in FP64, reconstruction in
+ * double-float arithmetic (pairs of FP32 numbers, 48-bit significand, on the FP32 pipe,
+ * which issues 64x the FP64 rate on GB300) on deviations from a per-variable reference
+ * value; traces rounded once in FP64 */
+#define HYPE_PREC_DF64 2
 
 /* dt semantics */
 #define HYPE_DT_MONITOR 0 /* dt of step n+1 = CFL h / (3 s_max) of the last stage RHS of step n
