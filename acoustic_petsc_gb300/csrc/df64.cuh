@@ -26,7 +26,21 @@ __device__ __forceinline__ df64 df_from_double(double x) {
     return df64{h, __double2float_rn(x - (double)h)};
 }
 
-__device__ __forceinline__ double df_to_double(df64 a) { return (double)a.hi + (double)a.lo; }
+// exact FP32 -> FP64 conversion by assembling the bits on the integer pipe (GB300 runs the
+// F2F conversion on its narrow FP64 pipe): sign, exponent rebased from 127 to 1023, the 23
+// significand bits shifted into the top of the 52; zero, subnormal, infinite and NaN inputs
+// take the ordinary conversion
+__device__ __forceinline__ double df_f2d(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned ex = (b >> 23) & 0xFFu;
+    if (ex - 1u >= 254u) return (double)x;
+    const unsigned hi = (b & 0x80000000u) | ((ex + 896u) << 20) | ((b >> 3) & 0xFFFFFu);
+    return __hiloint2double((int)hi, (int)(b << 29));
+}
+
+// hi + lo in FP64: exact unless lo lies more than 29 bits below hi's last bit, and then
+// rounded once
+__device__ __forceinline__ double df_to_double(df64 a) { return df_f2d(a.hi) + df_f2d(a.lo); }
 
 // a compile-time constant c as a pair (folded by the compiler for literal arguments)
 __host__ __device__ constexpr df64 dfc(double c) {

@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(128) k_ghost_df(const double* __restrict__ W, 
 
 // CWENO4 / R4 reconstruction in double-float on the deviations (euler_df64.cuh); the
 // traces go out as FP64 values r_c + deviation, the same array the FP64 faces consume
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128, 3)
     k_recon_df(const df64* __restrict__ G, double* __restrict__ T, const double* __restrict__ W, Geo g, int recon,
                int pad, double gm1, unsigned long long* __restrict__ counters) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
