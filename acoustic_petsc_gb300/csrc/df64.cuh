@@ -71,19 +71,21 @@ __device__ __forceinline__ df64 operator-(df64 x, df64 y) {
     return df_fast_two_sum(s.hi, __fadd_rn(s.lo, __fsub_rn(x.lo, y.lo)));
 }
 
+// Products are left unnormalised (p + e with |e| up to ~2^-22 |p| instead of ulp(p)/2):
+// every operation below takes such inputs at full accuracy, and the next addition
+// normalises again.
 __device__ __forceinline__ df64 operator*(df64 x, df64 y) {
     const float p = __fmul_rn(x.hi, y.hi);
     float e = __fmaf_rn(x.hi, y.hi, -p);
     e = __fmaf_rn(x.hi, y.lo, e);
     e = __fmaf_rn(x.lo, y.hi, e);
-    return df_fast_two_sum(p, e);
+    return df64{p, e};
 }
 
 // times an FP32 number
 __device__ __forceinline__ df64 df_mul(df64 x, float c) {
     const float p = __fmul_rn(x.hi, c);
-    const float e = __fmaf_rn(x.lo, c, __fmaf_rn(x.hi, c, -p));
-    return df_fast_two_sum(p, e);
+    return df64{p, __fmaf_rn(x.lo, c, __fmaf_rn(x.hi, c, -p))};
 }
 
 // times a power of two (exact)
@@ -92,8 +94,7 @@ __device__ __forceinline__ df64 df_scale(df64 x, float two_pow) { return df64{__
 __device__ __forceinline__ df64 df_sqr(df64 x) {
     const float p = __fmul_rn(x.hi, x.hi);
     float e = __fmaf_rn(x.hi, x.hi, -p);
-    e = __fmaf_rn(__fadd_rn(x.hi, x.hi), x.lo, e);
-    return df_fast_two_sum(p, e);
+    return df64{p, __fmaf_rn(__fadd_rn(x.hi, x.hi), x.lo, e)};
 }
 
 // x / y: the FP32 quotient q1 = x.hi / y.hi, the remainder x - q1 y in double-float, and
@@ -105,6 +106,7 @@ __device__ __forceinline__ df64 df_div(df64 x, df64 y) {
     return df_fast_two_sum(q1, q2);
 }
 
+// (normalised operands: results of + or -)
 __device__ __forceinline__ bool df_lt(df64 a, df64 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 __device__ __forceinline__ df64 df_min(df64 a, df64 b) { return df_lt(b, a) ? b : a; }
 

@@ -608,10 +608,13 @@ __global__ void __launch_bounds__(128) k_faces(const R* __restrict__ T, double* 
                 QL[c] = T[((long long)c * NTR + (2 * D + 1) * 4 + gp) * g.NE + eL];
                 QR[c] = T[((long long)c * NTR + (2 * D) * 4 + gp) * g.NE + eR];
             }
-            const R s = face_solver<R, D, FLUX>(QL, QR, gm, gm1, fl, bad);
+            // Rusanov's 1/2 goes into the Gauss weight 1/4
+            const R s = FLUX == HYPE_FLUX_RUSANOV ? rusanov<R, D, false>(QL, QR, gm, gm1, fl, bad)
+                                                  : face_solver<R, D, FLUX>(QL, QR, gm, gm1, fl, bad);
             smax = fmax(smax, (double)s);
+            const R wq = FLUX == HYPE_FLUX_RUSANOV ? R(0.125) : R(0.25);
 #pragma unroll
-            for (int c = 0; c < NV; ++c) acc[c] += R(0.25) * fl[c];
+            for (int c = 0; c < NV; ++c) acc[c] += wq * fl[c];
         }
         if constexpr (VISC) {
             // PDEViscRiemannSolver (Navier-Stokes-3D/pde.c:386-404): 0.5 (F_v(L) + F_v(R)) at

@@ -71,11 +71,14 @@ __device__ __forceinline__ void cweno4_df(const df64* __restrict__ s, bool linea
     }
     const df64 r13_3 = dfc(13. / 3.), r7_6 = dfc(7. / 6.);
     const df64 common = (ddsq[0] + ddsq[1] + ddsq[2]) * r13_3 + (cxsq[0] + cxsq[1] + cxsq[2]) * r7_6;
-    const df64 IS4 = d4[0] * (d4[0] + ddd4[0] * dfc(0.2)) + d4[1] * (d4[1] + ddd4[1] * dfc(0.2)) +
-                     d4[2] * (d4[2] + ddd4[2] * dfc(0.2)) + common +
-                     (df_sqr(aab[0]) + df_sqr(abb[0]) + df_sqr(aab[1]) + df_sqr(abb[1]) + df_sqr(aab[2]) + df_sqr(abb[2])) *
-                         dfc(4.7) +
-                     (df_sqr(ddd4[0]) + df_sqr(ddd4[1]) + df_sqr(ddd4[2])) * dfc(39.06) + df_sqr(xyz) * dfc(61. / 48.);
+    // sums as balanced trees: a double-float addition is a chain of ~9 dependent FP32
+    // operations, so independent partial sums keep more of them in flight
+    const df64 lin = (d4[0] * (d4[0] + ddd4[0] * dfc(0.2)) + d4[1] * (d4[1] + ddd4[1] * dfc(0.2))) +
+                     (d4[2] * (d4[2] + ddd4[2] * dfc(0.2)) + common);
+    const df64 mixed = ((df_sqr(aab[0]) + df_sqr(abb[0])) + (df_sqr(aab[1]) + df_sqr(abb[1]))) +
+                       (df_sqr(aab[2]) + df_sqr(abb[2]));
+    const df64 cubic = (df_sqr(ddd4[0]) + df_sqr(ddd4[1])) + df_sqr(ddd4[2]);
+    const df64 IS4 = (lin + mixed * dfc(4.7)) + (cubic * dfc(39.06) + df_sqr(xyz) * dfc(61. / 48.));
     const df64 IS0 = (c1sq[0] + c1sq[1] + c1sq[2]) + common;
     df64 sd1[6], sd2[6], sx1[6], sx2[6], IS3[6];
 #pragma unroll
@@ -116,13 +119,12 @@ __device__ __forceinline__ void cweno4_df(const df64* __restrict__ s, bool linea
     for (int k = 1; k < 8; ++k) mn = df_min(mn, q[k]);
     df64 w[8];
     const df64 gk[3] = {dfc(0.85), dfc((1.0 - 0.85) * 0.85), dfc((1. / 6.) * (1 - 0.85) * (1 - 0.85))};
-    df64 total = df64{0.0f, 0.0f};
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         const df64 r2 = df_sqr(df_div(mn, q[k]));
         w[k] = df_sqr(r2) * gk[k == 0 ? 0 : k == 1 ? 1 : 2];
-        total = total + w[k];
     }
+    const df64 total = ((w[0] + w[1]) + (w[2] + w[3])) + ((w[4] + w[5]) + (w[6] + w[7]));
     const df64 rt = df_div(dfc(1.0), total);
 #pragma unroll
     for (int k = 0; k < 8; ++k) w[k] = w[k] * rt;
@@ -135,12 +137,12 @@ __device__ __forceinline__ void cweno4_df(const df64* __restrict__ s, bool linea
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const df64 okeep = o0 + ((d == 0) ? oy + oz : (d == 1) ? ox + oz : ox + oy);
-        cf[CLIN(d)] = wr * d4[d] + okeep * c1[d] + os[2 * d] * sd1[2 * d] + os[2 * d + 1] * sd1[2 * d + 1];
-        cf[CSQ(d)] = (wr + okeep) * dd4[d] + os[2 * d] * sd2[2 * d] + os[2 * d + 1] * sd2[2 * d + 1];
+        cf[CLIN(d)] = (wr * d4[d] + okeep * c1[d]) + (os[2 * d] * sd1[2 * d] + os[2 * d + 1] * sd1[2 * d + 1]);
+        cf[CSQ(d)] = (wr + okeep) * dd4[d] + (os[2 * d] * sd2[2 * d] + os[2 * d + 1] * sd2[2 * d + 1]);
     }
-    cf[7] = (wr + o0 + oz) * cx[0] + os[0] * sx1[0] + os[1] * sx1[1] + os[2] * sx1[2] + os[3] * sx1[3];
-    cf[8] = (wr + o0 + ox) * cx[1] + os[2] * sx2[2] + os[3] * sx2[3] + os[4] * sx2[4] + os[5] * sx2[5];
-    cf[9] = (wr + o0 + oy) * cx[2] + os[0] * sx2[0] + os[1] * sx2[1] + os[4] * sx1[4] + os[5] * sx1[5];
+    cf[7] = (wr + o0 + oz) * cx[0] + ((os[0] * sx1[0] + os[1] * sx1[1]) + (os[2] * sx1[2] + os[3] * sx1[3]));
+    cf[8] = (wr + o0 + ox) * cx[1] + ((os[2] * sx2[2] + os[3] * sx2[3]) + (os[4] * sx2[4] + os[5] * sx2[5]));
+    cf[9] = (wr + o0 + oy) * cx[2] + ((os[0] * sx2[0] + os[1] * sx2[1]) + (os[4] * sx1[4] + os[5] * sx1[5]));
 #pragma unroll
     for (int d = 0; d < 3; ++d) cf[CCUBE(d)] = wr * ddd4[d];
     cf[13] = wr * aab[0]; cf[14] = wr * abb[0]; cf[15] = wr * aab[1]; cf[16] = wr * abb[1];

@@ -11,10 +11,32 @@
 // template parameter (double: the FP64 path; float: the FP32 recon/flux form).
 #pragma once
 
+#include "df64.cuh"
 #include "hype_common.cuh"
 
 namespace hype {
 namespace euler {
+
+// 1/x for the face solvers: the approximate FP32 reciprocal (rcp.approx, ~1 ulp of FP32)
+// of x's leading bits, refined by two Newton steps r <- r + r (1 - x r) in FP64 (the
+// relative error squares at each: 2^-23, 2^-46, then FP64 rounding), four FP64 operations
+// against the longer correctly rounded division; the bits move between the formats on the
+// integer pipe.  x outside [2^-126, 2^126) in magnitude, zero or not finite: the division.
+template <typename R>
+__device__ __forceinline__ R recip(R x) {
+    if (sizeof(R) != sizeof(double)) return R(1) / x;
+    const double xd = (double)x;
+    const unsigned hi = (unsigned)__double2hiint(xd);
+    const unsigned ex = (hi >> 20) & 0x7FFu;
+    if (ex - 897u > 251u) return R(1.0 / xd);
+    const float xf = __uint_as_float((hi & 0x80000000u) | ((ex - 896u) << 23) | ((hi & 0xFFFFFu) << 3));
+    float rf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(xf));
+    double r = df_f2d(rf);
+    r = fma(r, fma(-xd, r, 1.0), r);
+    r = fma(r, fma(-xd, r, 1.0), r);
+    return (R)r;
+}
 
 constexpr int NV = 5;
 constexpr int NTR = 24;  // traces per cell and variable: face (0..5: -x,+x,-y,+y,-z,+z) x Gauss point (0..3)
@@ -397,7 +419,8 @@ __device__ __forceinline__ void face_traces(const R* __restrict__ c, R* __restri
 
 // Rusanov (LLF) flux across an axis face of normal D; returns the max wave
 // speed and flags an inadmissible state (rho < 1e-14 or p < 1e-12).
-template <typename R, int D>
+// HALF = false leaves out the factor 1/2 (the caller folds it into its quadrature weight)
+template <typename R, int D, bool HALF = true>
 __device__ __forceinline__ R rusanov(const R* QL, const R* QR, R gamma, R gm1, R* F, bool& bad) {
     R FL[NV], FR[NV], sL, sR;
 #pragma unroll
@@ -405,7 +428,7 @@ __device__ __forceinline__ R rusanov(const R* QL, const R* QR, R gamma, R gm1, R
         const R* Q = side ? QR : QL;
         R* Fo = side ? FR : FL;
         const R rho = Q[0];
-        const R ir = R(1) / rho;
+        const R ir = recip(rho);
         const R u = ir * Q[1], v = ir * Q[2], w = ir * Q[3];
         const R E = Q[4];
         // 0.5 rho |u|^2 as 0.5 (m . u); the floors rho >= 1e-14, p >= 1e-12 (a NaN fails both)
@@ -426,7 +449,10 @@ __device__ __forceinline__ R rusanov(const R* QL, const R* QR, R gamma, R gm1, R
     }
     const R s = sL < sR ? sR : sL;
 #pragma unroll
-    for (int c = 0; c < NV; ++c) F[c] = R(0.5) * (FR[c] + FL[c] - s * (QR[c] - QL[c]));
+    for (int c = 0; c < NV; ++c) {
+        const R f = FR[c] + FL[c] - s * (QR[c] - QL[c]);
+        F[c] = HALF ? R(0.5) * f : f;
+    }
     return s;
 }
 
