@@ -20,22 +20,46 @@ struct __align__(8) df64 {
     float hi, lo;
 };
 
-// exact split of an FP64 value: hi = fl32(x), lo = fl32(x - hi) (x - hi is exact in FP64)
-__device__ __forceinline__ df64 df_from_double(double x) {
-    const float h = __double2float_rn(x);
-    return df64{h, __double2float_rn(x - (double)h)};
+// x rounded to a 24-bit significand, as FP32 (f) and as FP64 (fd), on the bit pattern:
+// adding half a unit of the 24th bit and clearing the 29 bits below rounds to nearest
+// (ties away from zero) and carries into the exponent where needed; values outside the
+// FP32 normal range take the F2F conversion
+__device__ __forceinline__ float df_round24(double x, double& fd) {
+    const unsigned long long r = ((unsigned long long)__double_as_longlong(x) + 0x10000000ull) & ~0x1FFFFFFFull;
+    const unsigned hi = (unsigned)(r >> 32);
+    const unsigned ex = (hi >> 20) & 0x7FFu;
+    if (ex - 897u <= 253u) {
+        fd = __longlong_as_double((long long)r);
+        return __uint_as_float((hi & 0x80000000u) | ((ex - 896u) << 23) | ((unsigned)(r >> 29) & 0x7FFFFFu));
+    }
+    if ((r & 0x7FFFFFFFFFFFFFFFull) == 0ull) {
+        fd = __longlong_as_double((long long)r);
+        return __uint_as_float(hi & 0x80000000u);
+    }
+    const float f = __double2float_rn(x);
+    fd = (double)f;
+    return f;
 }
 
-// exact FP32 -> FP64 conversion by assembling the bits on the integer pipe (GB300 runs the
-// F2F conversion on its narrow FP64 pipe): sign, exponent rebased from 127 to 1023, the 23
-// significand bits shifted into the top of the 52; zero, subnormal, infinite and NaN inputs
-// take the ordinary conversion
+// split of an FP64 value: hi = x rounded to 24 bits, lo = (x - hi, exact in FP64) rounded
+// likewise; one FP64 subtraction, the rest on the integer pipe
+__device__ __forceinline__ df64 df_from_double(double x) {
+    double hd, ld;
+    const float h = df_round24(x, hd);
+    return df64{h, df_round24(x - hd, ld)};
+}
+
+// FP32 -> FP64 conversion by assembling the bits on the integer pipe (GB300 runs the F2F
+// conversion on its narrow FP64 pipe), without branches: sign, exponent rebased from 127
+// to 1023 (255, infinity or NaN, to 2047), the 23 significand bits shifted into the top of
+// the 52.  Exact for normal numbers, zeros and infinities, NaN stays NaN; FP32 subnormals
+// (below 1.2e-38) become zeros of their sign.
 __device__ __forceinline__ double df_f2d(float x) {
     const unsigned b = __float_as_uint(x);
     const unsigned ex = (b >> 23) & 0xFFu;
-    if (ex - 1u >= 254u) return (double)x;
-    const unsigned hi = (b & 0x80000000u) | ((ex + 896u) << 20) | ((b >> 3) & 0xFFFFFu);
-    return __hiloint2double((int)hi, (int)(b << 29));
+    const unsigned exd = ex == 0u ? 0u : ex == 255u ? 0x7FFu : ex + 896u;
+    const unsigned man = ex == 0u ? 0u : b & 0x7FFFFFu;
+    return __hiloint2double((int)((b & 0x80000000u) | (exd << 20) | (man >> 3)), (int)(man << 29));
 }
 
 // hi + lo in FP64: exact unless lo lies more than 29 bits below hi's last bit, and then
