@@ -44,7 +44,7 @@ SYMBOLS = [
     "hype_euler_read_restart", "hype_euler_write_vtk", "hype_mp2d_write_restart", "hype_mp2d_read_restart",
     "hype_mp2d_write_vtk", "hype_acoustic_create", "hype_acoustic_destroy", "hype_acoustic_upload",
     "hype_acoustic_download", "hype_acoustic_rhs", "hype_acoustic_step", "hype_acoustic_sync", "hype_acoustic_stream",
-    "hype_acoustic_rhs_t", "hype_acoustic_set_point_source", "hype_acoustic_trace", "hype_acoustic2d_rhs_t",
+    "hype_acoustic_rhs_t", "hype_df64_probe", "hype_acoustic_set_point_source", "hype_acoustic_trace", "hype_acoustic2d_rhs_t",
     "hype_acoustic2d_set_point_source", "hype_acoustic2d_trace",
     "hype_euler_set_mlp", "hype_euler_set_recon", "hype_euler_indicator_stats", "hype_euler_sample_features",
     "hype_mlp_nparam", "hype_mlp_score", "hype_mlp_grad", "hype_mlp_train", "hype_euler_shadow_step",
@@ -209,6 +209,7 @@ def lib():
         "hype_acoustic_sync": ([V], C.c_int),
         "hype_acoustic_stream": ([V], C.c_void_p),
         "hype_acoustic_rhs_t": ([V, C.c_double, D, D], C.c_int),
+        "hype_df64_probe": ([D, D, C.c_longlong, D], C.c_int),
         "hype_acoustic_set_point_source": ([V, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
                                             C.c_int], C.c_int),
         "hype_acoustic_trace": ([V, D, D, C.c_int, P(C.c_longlong)], C.c_int),

@@ -512,6 +512,10 @@ int hype_device_count(int* n);
 /* Measured FMA issue ceiling of the FP64 (HYPE_PREC_FP64) or FP32 pipe of the
  * current device, in TFLOP/s (about 20 ms of GPU time). */
 int hype_probe_fma_peak(int precision, double* tflops);
+/* Test support for HYPE_PREC_DF64: for each x[q], y[q] (|x|, |y| in the FP32 normal range),
+ * out[7q..7q+6] = the FP32 pair (hi, lo) of x as FP64 values, hi + lo, and x + y, x - y,
+ * x * y, x / y in double-float arithmetic, each converted back to FP64. */
+int hype_df64_probe(const double* x, const double* y, long long n, double* out);
 const char* hype_strerror(int code);
 /* message of the last CUDA error seen by the library (thread-local) */
 const char* hype_last_error(void);
