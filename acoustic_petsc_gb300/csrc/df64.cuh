@@ -1,6 +1,9 @@
 // df64.cuh -- double-float arithmetic: a value is the unevaluated sum hi + lo of two
 // FP32 numbers with |lo| <= ulp(hi)/2, a 48-bit significand with the FP32 exponent range.
 //
+// The 48 bits hold for |x| >= 2^-74, where a non-zero lo is an FP32 normal number; below,
+// lo may flush to zero (absolute error < 2^-126); |x| must stay below 2^128.
+//
 // Why on GB300: its FP64 pipe issues 1/64 of the FP32 rate, so a reconstruction that is
 // bound by FP64 instruction issue runs several times faster on FP32 pairs, where an add
 // costs ~11 and a multiply ~6 FP32 instructions.  The building blocks are the classical

@@ -35,15 +35,22 @@ def test_split_and_arithmetic(hype):
     assert np.mean(hi == x.astype(np.float32).astype(np.float64)) > 0.9999
     assert np.all(hi.astype(np.float32) == hi) and np.all(lo.astype(np.float32) == lo)
     assert np.all(np.abs(lo) <= np.abs(np.spacing(hi.astype(np.float32)).astype(np.float64)) / 2 * (1 + 1e-7))
-    # hi + lo carries 48 bits of x
-    assert np.all(np.abs(back - x) <= 2.0**-48 * np.abs(x))
+    # hi + lo carries 48 bits of x, except that a remainder x - hi below the FP32 normal
+    # range (possible for |x| < 2^-74) flushes to zero: absolute error < 2^-126
+    assert np.all(np.abs(back - x) <= np.maximum(2.0**-48 * np.abs(x), 2.0**-126))
     assert back[1000] == 0.0 and back[1001] == 0.0
     xs, ys = back, _probe(hype, y, y)[:, 2]  # the values the pair arithmetic actually saw
-    tol = 2.0**-46
-    assert np.all(np.abs(o[:, 3] - (xs + ys)) <= tol * (np.abs(xs) + np.abs(ys)))
-    assert np.all(np.abs(o[:, 4] - (xs - ys)) <= tol * (np.abs(xs) + np.abs(ys)))
-    prod_ok = (np.abs(xs * ys) > 1e-36) & (np.abs(xs * ys) < 1e36)  # products inside the FP32 normal range
-    assert np.all(np.abs(o[prod_ok, 5] - xs[prod_ok] * ys[prod_ok]) <= tol * np.abs(xs[prod_ok] * ys[prod_ok]))
-    q = xs / ys
-    quot_ok = (np.abs(q) > 1e-36) & (np.abs(q) < 1e36)
-    assert np.all(np.abs(o[quot_ok, 6] - q[quot_ok]) <= tol * np.abs(q[quot_ok]))
+    # full accuracy (~2^-46) where operands and results lie in [2^-70, 2^100] (every lo part
+    # an FP32 normal number); smaller magnitudes lose a flushed lo part
+    tol = 2.0**-45
+
+    def inrange(v):
+        return (np.abs(v) >= 2.0**-70) & (np.abs(v) <= 2.0**100)
+
+    ops = inrange(xs) & inrange(ys)
+    for col, ref, scale in ((3, xs + ys, np.abs(xs) + np.abs(ys)), (4, xs - ys, np.abs(xs) + np.abs(ys)),
+                            (5, xs * ys, np.abs(xs * ys)), (6, xs / ys, np.abs(xs / ys))):
+        ok = ops & inrange(ref)
+        assert ok.sum() > n // 4
+        err = np.abs(o[:, col] - ref)
+        assert np.all(err[ok] <= tol * scale[ok]), (col, float(np.max(err[ok] / scale[ok])))
