@@ -321,10 +321,12 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1)
 }
 
 // HYPE_PREC_DF64: the per-variable reference value r_c of one stage, the stage input's
-// value at cell 0 rounded to FP32 (the deviations u - r_c are formed in FP64, the traces
-// r_c + deviation are rounded once in FP64)
+// value at cell 0 rounded to a 24-bit significand (the deviations u - r_c are formed in
+// FP64, the traces r_c + deviation are rounded once in FP64)
 __device__ __forceinline__ double df_ref(const double* __restrict__ W, const Geo& g, int c) {
-    return (double)__double2float_rn(__ldg(W + (long long)c * g.N));
+    double r;
+    df_round24(__ldg(W + (long long)c * g.N), r);
+    return r;
 }
 
 // ghost fill as k_ghost, storing the deviation from r_c as a double-float pair

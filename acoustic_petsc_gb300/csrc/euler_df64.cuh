@@ -2,7 +2,7 @@
 // double-float arithmetic (df64.cuh), for the HYPE_PREC_DF64 form of the 3D Euler RHS.
 //
 // The stencil values arrive as deviations from a per-variable reference value r (the
-// stage input's value at cell 0, rounded to FP32), so every polynomial coefficient but
+// stage input's value at cell 0 rounded to a 24-bit significand), so every coefficient but
 // the constant one is formed from differences of small numbers, and the 48-bit
 // significand is spent on the deviation: the absolute error of a trace is ~2^-48 |u - r|
 // plus the final FP64 rounding of r + trace, against ~2^-53 |u| for the FP64 form.  The
