@@ -154,9 +154,10 @@ struct Stage {
 };
 
 // U, W, out: SoA [2][N]; L = (v, (1/h^2) sum of face-flux differences)
+// U, W and out may be one array (in-place stages), so they carry no __restrict__
 __global__ void __launch_bounds__(256) k_ac_update(const double* __restrict__ Fx, const double* __restrict__ Fy,
-                                                   const double* __restrict__ Fz, const double* __restrict__ U,
-                                                   const double* __restrict__ W, double* __restrict__ out, Geo g,
+                                                   const double* __restrict__ Fz, const double* U,
+                                                   const double* W, double* out, Geo g,
                                                    double r1_h2, Stage st, double dt, SourceArgs src) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;

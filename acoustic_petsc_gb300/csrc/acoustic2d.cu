@@ -161,9 +161,10 @@ __device__ __forceinline__ double sw_edge(double c2, double gL0, double gR0, dou
 
 // W: the stage input (v = W[1] is the first RHS component); X, Y: the states the stage
 // combines; all SoA [2][ny][nx]
-__global__ void __launch_bounds__(256) k_sw_update(const double* __restrict__ T, const double* __restrict__ W,
-                                                   const double* __restrict__ X, const double* __restrict__ Y,
-                                                   double* __restrict__ out, Geo g, double c2, double r1_h, Stage st,
+// W, X, Y and out may be one array (in-place stages), so they carry no __restrict__
+__global__ void __launch_bounds__(256) k_sw_update(const double* __restrict__ T, const double* W,
+                                                   const double* X, const double* Y,
+                                                   double* out, Geo g, double c2, double r1_h, Stage st,
                                                    double dt, SourceArgs src) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;

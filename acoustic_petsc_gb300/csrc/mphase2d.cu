@@ -346,9 +346,10 @@ struct Stage {
     int rhs_only;
 };
 
+// Win, X, Y and out may be one array (in-place stages), so they carry no __restrict__
 __global__ void __launch_bounds__(256) k_mp_update(const double* __restrict__ F, const double* __restrict__ G,
-                                                   const double* __restrict__ Win, const double* __restrict__ X,
-                                                   const double* __restrict__ Y, double* __restrict__ out, Geo g,
+                                                   const double* Win, const double* X,
+                                                   const double* Y, double* out, Geo g,
                                                    double r1_h, Stage st, const DevScalars* __restrict__ ds) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;

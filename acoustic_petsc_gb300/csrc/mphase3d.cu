@@ -492,10 +492,11 @@ struct Stage {
 
 // RHS (rhs_function.c:507-552) and the stage combination; Win: the stage input, whose
 // volume fraction multiplies the normal-velocity flux in the phi equation
+// Win, U, W and out may be one array (in-place stages), so they carry no __restrict__
 __global__ void __launch_bounds__(256) k_m3_update(const double* __restrict__ Fx, const double* __restrict__ Fy,
-                                                   const double* __restrict__ Fz, const double* __restrict__ Win,
-                                                   const double* __restrict__ U, const double* __restrict__ W,
-                                                   double* __restrict__ out, Geo g, double r1_h, Stage st,
+                                                   const double* __restrict__ Fz, const double* Win,
+                                                   const double* U, const double* W,
+                                                   double* out, Geo g, double r1_h, Stage st,
                                                    const DevScalars* __restrict__ ds) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;

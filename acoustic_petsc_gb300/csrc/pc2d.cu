@@ -393,10 +393,11 @@ struct Stage {
     int rhs_only;
 };
 
+// X, Y and out may be one array (in-place stages), so they carry no __restrict__
 __global__ void __launch_bounds__(256) k_pc_update(const double* __restrict__ Fx, const double* __restrict__ Fy,
                                                    const double* __restrict__ Dx, const double* __restrict__ Dy,
-                                                   const double* __restrict__ V5, const double* __restrict__ X,
-                                                   const double* __restrict__ Y, double* __restrict__ out, Geo g,
+                                                   const double* __restrict__ V5, const double* X,
+                                                   const double* Y, double* out, Geo g,
                                                    double r1_h, Stage st, const DevScalars* __restrict__ ds) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;

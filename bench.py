@@ -287,6 +287,12 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
         alu = {"bound": "fp64" if precision == 0 else "fp32", "achieved": ach, "peak": fpeak.value, "unit": "TFLOP/s",
                "frac": ach / fpeak.value, "flops_per_cell_stage": flops_cell,
                "peak_kind": "measured FMA issue ceiling (hype_probe_fma_peak)"}
+        instr_cell = _profile_figure(prof_file, "fp64_instructions_per_cell_stage") if precision == 0 else None
+        if instr_cell:
+            # an FMA counts two flops, an add or multiply one: against the issue ceiling
+            # (peak / 2 instructions per second) the FP64 pipe's occupancy shows directly
+            alu["fp64_instructions_per_cell_stage"] = instr_cell
+            alu["instruction_issue_frac"] = instr_cell * cells / t_stage / (fpeak.value * 1e12 / 2)
     # ---- end to end through the public API with host buffers (pinned)
     e2e = None
     if rank == 0 or ws > 1:
