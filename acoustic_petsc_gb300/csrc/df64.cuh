@@ -133,6 +133,19 @@ __device__ __forceinline__ df64 df_div(df64 x, df64 y) {
     return df_fast_two_sum(q1, q2);
 }
 
+// sqrt(x) for x > 0: the FP32 root s and one Heron correction (x - s^2) / (2 s), with s^2
+// formed exactly by TwoProduct; x <= 0 (or not finite in hi) gives the FP32 root alone
+__device__ __forceinline__ df64 df_sqrt(df64 x) {
+    const float s = __fsqrt_rn(x.hi);
+    if (!(x.hi > 0.0f) || !(s < 3.0e38f)) return df64{s, 0.0f};
+    const float p = __fmul_rn(s, s);
+    const float e = __fmaf_rn(s, s, -p);
+    const df64 r = x - df64{p, e};
+    return df_fast_two_sum(s, __fdiv_rn(r.hi, __fadd_rn(s, s)));
+}
+
+__device__ __forceinline__ df64 df_abs(df64 x) { return x.hi < 0.0f ? df64{-x.hi, -x.lo} : x; }
+
 // (normalised operands: results of + or -)
 __device__ __forceinline__ bool df_lt(df64 a, df64 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 __device__ __forceinline__ df64 df_min(df64 a, df64 b) { return df_lt(b, a) ? b : a; }

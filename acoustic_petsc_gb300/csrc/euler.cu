@@ -348,11 +348,81 @@ __global__ void __launch_bounds__(128) k_ghost_df(const double* __restrict__ W, 
     }
 }
 
-// CWENO4 / R4 reconstruction in double-float on the deviations (euler_df64.cuh); the
-// traces go out as FP64 values r_c + deviation, the same array the FP64 faces consume
+// The stage's reference state r in double-float (its components are the rounded cell-0
+// values, exact FP32 numbers) and the pieces of F(r) the deviation form of the flux uses
+struct DfRef {
+    df64 rho, m[3], E, u[3], p, H;  // u = m / rho, p = (gamma - 1)(E - m.u / 2), H = E + p
+};
+
+__device__ __forceinline__ DfRef df_refstate(const double* __restrict__ W, const Geo& g, df64 gm1) {
+    DfRef R;
+    double fd;
+    R.rho = df64{df_round24(__ldg(W), fd), 0.0f};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) R.m[i] = df64{df_round24(__ldg(W + (long long)(1 + i) * g.N), fd), 0.0f};
+    R.E = df64{df_round24(__ldg(W + 4LL * g.N), fd), 0.0f};
+    const df64 ir = df_div(dfc(1.0), R.rho);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) R.u[i] = R.m[i] * ir;
+    R.p = (R.E - df_scale((R.m[0] * R.u[0] + R.m[1] * R.u[1]) + R.m[2] * R.u[2], 0.5f)) * gm1;
+    R.H = R.E + R.p;
+    return R;
+}
+
+// One side of a face in deviation form: for the trace r + d, the flux deviation
+// dF = F(r + d) - F(r) along D (PDEConsFlux, Navier-Stokes-3D/pde.c:40-88) built only from
+// deviation-sized terms -- du = (d_m - u_r d_rho) / rho, d(m.u) = sum m_r du + d_m u,
+// dp = (gamma - 1)(d_E - d(m.u) / 2), dF_m = m_r du_n + d_m u_n (+ dp), dF_E = H_r du_n +
+// (d_E + dp) u_n -- and the wave speed |u_n| + sqrt(gamma p / rho); the floors of pde.c:56-66
+template <int D>
+__device__ __forceinline__ void dev_side(const DfRef& R, const df64* d, df64 gm1, df64 gam, df64* dF, df64& sp,
+                                         bool& bad) {
+    const df64 rho = R.rho + d[0];
+    const df64 ir = df_div(dfc(1.0), rho);
+    df64 du[3], u[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        du[i] = (d[1 + i] - R.u[i] * d[0]) * ir;
+        u[i] = R.u[i] + du[i];
+    }
+    const df64 dmu = (R.m[0] * du[0] + d[1] * u[0]) + ((R.m[1] * du[1] + d[2] * u[1]) + (R.m[2] * du[2] + d[3] * u[2]));
+    const df64 dp = (d[4] - df_scale(dmu, 0.5f)) * gm1;
+    const df64 p = R.p + dp;
+    bad |= !(rho.hi >= 1.0e-14f && p.hi >= 1.0e-12f);
+    dF[0] = d[1 + D];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const df64 f = R.m[i] * du[D] + d[1 + i] * u[D];
+        dF[1 + i] = (i == D) ? f + dp : f;
+    }
+    dF[4] = R.H * du[D] + (d[4] + dp) * u[D];
+    sp = df_abs(u[D]) + df_sqrt(gam * p * ir);
+}
+
+// density and pressure of the 24 double-float deviation traces against the floors
+__device__ __forceinline__ bool traces_admissible_df(const df64* __restrict__ T, const Geo& g, long long e,
+                                                     const DfRef& R, df64 gm1) {
+    for (int q = 0; q < NTR; ++q) {
+        df64 d[NV];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) d[c] = T[((long long)c * NTR + q) * g.NE + e];
+        const df64 rho = R.rho + d[0];
+        const df64 mx = R.m[0] + d[1], my = R.m[1] + d[2], mz = R.m[2] + d[3];
+        const df64 p = ((R.E + d[4]) - df_scale(df_div((mx * mx + my * my) + mz * mz, rho), 0.5f)) * gm1;
+        if (!(rho.hi >= 1.0e-14f) || !(p.hi >= 1.0e-12f)) return false;
+    }
+    return true;
+}
+
+// CWENO4 / R4 reconstruction in double-float on the deviations (euler_df64.cuh).  DFT: the
+// traces stay double-float deviations for k_faces_df (Rusanov); otherwise they go out as FP64
+// values r_c + deviation, the array the FP64 face solvers consume.
+template <bool DFT>
 __global__ void __launch_bounds__(128, 3)
-    k_recon_df(const df64* __restrict__ G, double* __restrict__ T, const double* __restrict__ W, Geo g, int recon,
+    k_recon_df(const df64* __restrict__ G, void* __restrict__ Tv, const double* __restrict__ W, Geo g, int recon,
                int pad, double gm1, unsigned long long* __restrict__ counters) {
+    double* T = (double*)Tv;
+    df64* Td = (df64*)Tv;
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
     const int k = blockIdx.z - 1;
@@ -390,28 +460,52 @@ __global__ void __launch_bounds__(128, 3)
                     for (int d = 0; d < 2; ++d) s[SO(a, b, d)] = p[(2 * a - 1) + (2 * b - 1) * sy + (2 * d - 1) * sz];
         }
         cweno4_df(s, recon == HYPE_RECON_LINEAR4, cf);
-        const double r = df_ref(W, g, c);
-        double* Tc = T + (long long)c * NTR * g.NE + e;
         df64 tr[8];
+        if constexpr (DFT) {
+            df64* Tc = Td + (long long)c * NTR * g.NE + e;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            if (d == 0) face_traces_df<0>(cf, tr);
-            else if (d == 1) face_traces_df<1>(cf, tr);
-            else face_traces_df<2>(cf, tr);
+            for (int d = 0; d < 3; ++d) {
+                if (d == 0) face_traces_df<0>(cf, tr);
+                else if (d == 1) face_traces_df<1>(cf, tr);
+                else face_traces_df<2>(cf, tr);
 #pragma unroll
-            for (int q = 0; q < 8; ++q) Tc[(long long)(8 * d + q) * g.NE] = r + df_to_double(tr[q]);
+                for (int q = 0; q < 8; ++q) Tc[(long long)(8 * d + q) * g.NE] = tr[q];
+            }
+        } else {
+            const double r = df_ref(W, g, c);
+            double* Tc = T + (long long)c * NTR * g.NE + e;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                if (d == 0) face_traces_df<0>(cf, tr);
+                else if (d == 1) face_traces_df<1>(cf, tr);
+                else face_traces_df<2>(cf, tr);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) Tc[(long long)(8 * d + q) * g.NE] = r + df_to_double(tr[q]);
+            }
         }
     }
-    if (pad && !traces_admissible<double>(T, g, e, gm1)) {
+    if (!pad) return;
+    bool ok;
+    if constexpr (DFT) {
+        const df64 gm1d = df_from_double(gm1);
+        ok = traces_admissible_df(Td, g, e, df_refstate(W, g, gm1d), gm1d);
+    } else {
+        ok = traces_admissible<double>(T, g, e, gm1);
+    }
+    if (!ok) {
 #pragma unroll 1
         for (int c = 0; c < NV; ++c) {
-            const double v = df_ref(W, g, c) + df_to_double(G[(long long)c * g.GN + ge]);
-            double* Tc = T + (long long)c * NTR * g.NE + e;
-            for (int q = 0; q < NTR; ++q) Tc[(long long)q * g.NE] = v;
+            const df64 dv = G[(long long)c * g.GN + ge];
+            const double v = df_ref(W, g, c) + df_to_double(dv);
+            for (int q = 0; q < NTR; ++q) {
+                if constexpr (DFT) Td[((long long)c * NTR + q) * g.NE + e] = dv;
+                else T[((long long)c * NTR + q) * g.NE + e] = v;
+            }
         }
         if (!gi && !gj && !gk) atomicAdd(&counters[1], 1ull);
     }
 }
+
 
 // Indicator-gated reconstruction: the network scores the cell from its three
 // directional 5-point stencils; flagged or low-confidence cells take the full
@@ -584,6 +678,58 @@ __device__ __forceinline__ double visc_side(const double* __restrict__ T, const 
 
 // Face fluxes of direction D.  Face index (i,j,k) is the face on the low side of
 // cell (i,j,k); along D it runs to n (the high face of the last cell).
+// Rusanov faces of the double-float form in deviation form: with F(r) dropped (it is the
+// same at every face, so the divergence does not see it), the stored flux is
+// 1/2 (dF_L + dF_R) - 1/2 s (d_R - d_L) at each Gauss point, weight 1/4, where s is the
+// larger wave speed (pde.c:164-187); every term has the size of the deviations, so the
+// 48-bit significand meets the FP64 form's error bars with the face solver on the FP32 pipe.
+template <int D>
+__global__ void __launch_bounds__(128) k_faces_df(const df64* __restrict__ T, double* __restrict__ F,
+                                                  const double* __restrict__ W, Geo g, double gamma,
+                                                  DevScalars* __restrict__ ds, int slot) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    const int fx = g.nx + (D == 0), fy = g.ny + (D == 1);
+    double smax = 0.0;
+    bool bad = false;
+    if (i < fx && j < fy) {
+        const long long eR = ext_index(g, i, j, k);
+        const long long eL = ext_index(g, i - (D == 0), j - (D == 1), k - (D == 2));
+        const df64 gm1 = df_from_double(gamma - 1.0), gam = df_from_double(gamma);
+        const DfRef R = df_refstate(W, g, gm1);
+        df64 acc[NV];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) acc[c] = df64{0.0f, 0.0f};
+#pragma unroll 1
+        for (int gp = 0; gp < 4; ++gp) {
+            df64 dL[NV], dR[NV], fL[NV], fR[NV], sL, sR;
+#pragma unroll
+            for (int c = 0; c < NV; ++c) {
+                dL[c] = T[((long long)c * NTR + (2 * D + 1) * 4 + gp) * g.NE + eL];
+                dR[c] = T[((long long)c * NTR + (2 * D) * 4 + gp) * g.NE + eR];
+            }
+            dev_side<D>(R, dL, gm1, gam, fL, sL, bad);
+            dev_side<D>(R, dR, gm1, gam, fR, sR, bad);
+            const df64 sm = df_lt(sL, sR) ? sR : sL;
+            smax = fmax(smax, df_to_double(sm));
+#pragma unroll
+            for (int c = 0; c < NV; ++c) acc[c] = acc[c] + df_scale((fL[c] + fR[c]) - sm * (dR[c] - dL[c]), 0.125f);
+        }
+        const long long nf = (long long)fx * fy * (g.nz + (D == 2));
+        const long long f = ((long long)k * fy + j) * fx + i;
+#pragma unroll
+        for (int c = 0; c < NV; ++c) F[c * nf + f] = df_to_double(acc[c]);
+        if (bad) {
+            const int ci = i < g.nx ? i : g.nx - 1, cj = j < g.ny ? j : g.ny - 1, ck = k < g.nz ? k : g.nz - 1;
+            atomicMin(&ds->bad, (unsigned long long)(((long long)ck * g.ny + cj) * g.nx + ci));
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, o));
+    if ((threadIdx.x & 31) == 0 && smax > 0.0) atomic_max_pos(&ds->smax_bits[slot], smax);
+}
+
 template <typename R, int D, int FLUX, bool VISC = false>
 __global__ void __launch_bounds__(128) k_faces(const R* __restrict__ T, double* __restrict__ F, Geo g, double gamma,
                                                DevScalars* __restrict__ ds, int slot, const double* __restrict__ C4 = nullptr,
@@ -950,8 +1096,12 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
             k_recon_learned<double><<<gr, br, 0, e->stream>>>((const double*)e->G, (double*)e->T, g, e->mlp, e->logit_thr,
                                                               gm1, e->p.positivity, e->mlp_cnt);
     } else if (df) {
-        k_recon_df<<<gr, br, 0, e->stream>>>((const df64*)e->G, (double*)e->T, Win, g, rec, e->p.positivity, gm1,
-                                             e->mlp_cnt);
+        if (e->p.flux == HYPE_FLUX_RUSANOV)
+            k_recon_df<true><<<gr, br, 0, e->stream>>>((const df64*)e->G, e->T, Win, g, rec, e->p.positivity, gm1,
+                                                       e->mlp_cnt);
+        else
+            k_recon_df<false><<<gr, br, 0, e->stream>>>((const df64*)e->G, e->T, Win, g, rec, e->p.positivity, gm1,
+                                                        e->mlp_cnt);
     } else if (f32) {
         k_recon<float><<<gr, br, ck_bytes, e->stream>>>((const float*)e->G, (float*)e->T, g, rec, e->p.positivity, gm1,
                                                         e->mlp_cnt);
@@ -969,6 +1119,14 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
                         : e->p.flux == HYPE_FLUX_ROTHLLC ? launch_faces_t<double, HYPE_FLUX_ROTHLLC, true>
                                                          : launch_faces_t<double, HYPE_FLUX_RUSANOV, true>;
         lf(e->g, e->T, e->Fx, e->Fy, e->Fz, e->p.gamma, e->ds, slot, e->stream, e->C4, vp);
+    } else if (df && e->p.flux == HYPE_FLUX_RUSANOV) {
+        const dim3 bf(32, 4);
+        const dim3 fgx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4), g.nz), fgy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4), g.nz),
+            fgz(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz + 1);
+        const df64* Td = (const df64*)e->T;
+        k_faces_df<0><<<fgx, bf, 0, e->stream>>>(Td, e->Fx, Win, g, e->p.gamma, e->ds, slot);
+        k_faces_df<1><<<fgy, bf, 0, e->stream>>>(Td, e->Fy, Win, g, e->p.gamma, e->ds, slot);
+        k_faces_df<2><<<fgz, bf, 0, e->stream>>>(Td, e->Fz, Win, g, e->p.gamma, e->ds, slot);
     } else {
         launch_faces(e->g, e->T, e->Fx, e->Fy, e->Fz, e->p.gamma, e->ds, slot, f32, e->p.flux, e->stream);
     }
