@@ -216,7 +216,8 @@ FLUX_NAME = {0: "Rusanov", 1: "HLLC", 2: "rotated HLLC"}
 
 
 EULER_DTYPE = {0: "f64", 1: "f64 state / f32 recon+flux",
-               2: "f64 state+flux / df64 recon (FP32 pairs, 48-bit significand, on deviations)"}
+               2: "f64 state and stage accumulation / df64 recon+Rusanov flux (FP32 pairs, 48-bit significand, "
+                  "on deviations from a reference state)"}
 
 
 def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscous=False):
@@ -255,6 +256,13 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
     launches = H.launches() - l0
     ms = e0.elapsed_time(e1)
     ms_max = _max_over_ranks(ws, ms)
+    # the double-float form beside the FP64 one (same state, same steps), for the default workload
+    alt = None
+    if precision == 0 and recon == 0 and flux == 0 and not viscous and not args.no_alt_forms:
+        U_fp64 = s.get_state()
+        alt = _euler_df64_beside(args, ws, n, U0, U_fp64, stream_of=lambda h: torch.cuda.ExternalStream(
+            L.hype_euler_stream(h)))
+        del U_fp64
     prof_ms = (C.c_double * 3)()
     prof_n = (C.c_longlong * 3)()
     H._lib.check(L.hype_euler_profile_read(s._h, prof_ms, prof_n), "profile_read")
@@ -338,7 +346,49 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
     }
     if alu:
         out["roofline_alu"] = alu
+    if alt:
+        out["alt_forms"] = alt
     return out
+
+
+def _euler_df64_beside(args, ws, n, U0, U_fp64, stream_of):
+    """the HYPE_PREC_DF64 form of the same workload: state, face fluxes and stage accumulation
+    in FP64, reconstruction and Rusanov flux in FP32 pairs on deviations; the same warm-up and
+    timed steps from the same state, and its largest state difference from the FP64 run"""
+    import torch
+
+    import acoustic_petsc_gb300 as H
+
+    L = H.lib()
+    ctx = H.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, precision=H._lib.PREC_DF64)
+    d = H.EulerSolver(ctx)
+    d.set_state(U0)
+    d.step(max(args.warmup, 3))
+    stream = stream_of(d._h)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    H._lib.check(L.hype_euler_profile(d._h, 1), "profile")
+    _barrier(ws)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    d.step(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = _max_over_ranks(ws, e0.elapsed_time(e1))
+    prof_ms = (C.c_double * 3)()
+    prof_n = (C.c_longlong * 3)()
+    H._lib.check(L.hype_euler_profile_read(d._h, prof_ms, prof_n), "profile_read")
+    H._lib.check(L.hype_euler_profile(d._h, 0), "profile")
+    stages = max(prof_n[0], 1)
+    diff = float(np.abs(d.get_state() - U_fp64).max() / np.abs(U_fp64).max())
+    d.close()
+    return {"df64": {"value": ws * n**3 * args.steps / (ms * 1e-3), "unit": "cell-updates/s",
+                     "ms_per_step": ms / args.steps,
+                     "dtype": EULER_DTYPE[2],
+                     "per_kernel_ms": {"recon": prof_ms[0] / stages, "faces": prof_ms[1] / stages,
+                                       "update": prof_ms[2] / stages},
+                     "state_rel_linf_diff_vs_fp64": diff,
+                     "steps_compared": max(args.warmup, 3) + args.steps,
+                     "profile": "profiles/euler_stage_df64.txt"}}
 
 
 def run_ctcs(args, ws, rank, local, n=512):
@@ -961,6 +1011,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="euler256", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-alt-forms", action="store_true",
+                    help="skip the double-float form measured beside the default FP64 Euler workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=0,
                     help="cells per axis of the 3D Euler / Navier-Stokes workloads (default 256; smaller for profiling)")
