@@ -124,13 +124,17 @@ __device__ __forceinline__ df64 df_sqr(df64 x) {
     return df64{p, __fmaf_rn(__fadd_rn(x.hi, x.hi), x.lo, e)};
 }
 
-// x / y: the FP32 quotient q1 = x.hi / y.hi, the remainder x - q1 y in double-float, and
-// its quotient as the correction
+// x / y: q1 = x.hi / y.hi from the approximate FP32 reciprocal (rcp.approx, ~1 ulp) after
+// one Newton step, the remainder x - q1 y in double-float, and its quotient as the
+// correction (~2^-47 relative accuracy); y.hi must be a nonzero normal number with
+// |y.hi| < 2^126 (the FP32 reciprocal of larger values flushes to zero)
 __device__ __forceinline__ df64 df_div(df64 x, df64 y) {
-    const float q1 = __fdiv_rn(x.hi, y.hi);
+    float ry;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(ry) : "f"(y.hi));
+    ry = __fmaf_rn(ry, __fmaf_rn(-y.hi, ry, 1.0f), ry);
+    const float q1 = __fmul_rn(x.hi, ry);
     const df64 r = x - df_mul(y, q1);
-    const float q2 = __fdiv_rn(r.hi, y.hi);
-    return df_fast_two_sum(q1, q2);
+    return df_fast_two_sum(q1, __fmul_rn(r.hi, ry));
 }
 
 // sqrt(x) for x > 0: the FP32 root s and one Heron correction (x - s^2) / (2 s), with s^2

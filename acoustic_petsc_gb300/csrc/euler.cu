@@ -417,8 +417,10 @@ __device__ __forceinline__ bool traces_admissible_df(const df64* __restrict__ T,
 // CWENO4 / R4 reconstruction in double-float on the deviations (euler_df64.cuh).  DFT: the
 // traces stay double-float deviations for k_faces_df (Rusanov); otherwise they go out as FP64
 // values r_c + deviation, the array the FP64 face solvers consume.
+// (two blocks per SM: with more warps in flight over this long unrolled body the
+// instruction-cache misses cost more than the latency they hide)
 template <bool DFT>
-__global__ void __launch_bounds__(128, 3)
+__global__ void __launch_bounds__(128, 2)
     k_recon_df(const df64* __restrict__ G, void* __restrict__ Tv, const double* __restrict__ W, Geo g, int recon,
                int pad, double gm1, unsigned long long* __restrict__ counters) {
     double* T = (double*)Tv;
