@@ -595,6 +595,139 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1)
     }
 }
 
+// Indicator-gated reconstruction of the double-float form: the network reads the FP32 leading
+// parts of the deviations (its normalised stencils are shift-invariant; the magnitude floors
+// take the density and energy as r + deviation), flagged or low-confidence cells take the
+// double-float CWENO4 and the others its R4 limit, with the positivity redo of k_recon_learned.
+// DFT as for k_recon_df.
+template <bool DFT>
+__global__ void __launch_bounds__(128, 2)
+    k_recon_learned_df(const df64* __restrict__ G, void* __restrict__ Tv, const double* __restrict__ W, Geo g,
+                       const mlp::MmaWeights* __restrict__ wts, float logit_thr, double gm1, int pad,
+                       unsigned long long* __restrict__ counters) {
+    __shared__ __align__(16) __nv_bfloat16 rows[4][mlp::ROWS * mlp::RSTRIDE];
+    __shared__ float lg[4][mlp::ROWS];
+    __shared__ unsigned cnt[2];
+    if (threadIdx.x == 0 && threadIdx.y == 0) cnt[0] = cnt[1] = 0;
+    double* T = (double*)Tv;
+    df64* Td = (df64*)Tv;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+    const int k = blockIdx.z - 1;
+    bool active = !(i > g.nx || j > g.ny);
+    const int gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny), gk = (k < 0 || k >= g.nz);
+    active = active && (gi + gj + gk <= 1);
+    const long long ge = active ? ghost_index(g, i, j, k) : 0;
+    const int sy = g.gx, sz = g.gx * g.gy;
+    __nv_bfloat16* my_rows = rows[threadIdx.y] + threadIdx.x * 3 * mlp::RSTRIDE;
+    float sc[NV];
+    if (active) {
+        double fd;
+        const float rho = df_round24(__ldg(W), fd) + G[ge].hi;
+        const float E = df_round24(__ldg(W + 4LL * g.N), fd) + G[4 * g.GN + ge].hi;
+#pragma unroll
+        for (int c = 0; c < NV; ++c) sc[c] = mlp::var_scale<float>(c, rho, E);
+    }
+#pragma unroll 1
+    for (int d = 0; d < 3; ++d) {
+        float x[mlp::NIN];
+        const int st = d == 0 ? 1 : d == 1 ? sy : sz;
+        if (active) {
+#pragma unroll
+            for (int c = 0; c < NV; ++c) {
+                const df64* p = G + (long long)c * g.GN + ge;
+                float s5[5];
+#pragma unroll
+                for (int o = 0; o < 5; ++o) s5[o] = p[(o - 2) * st].hi;
+                mlp::normalise5(s5, sc[c], x + c * 5);
+            }
+        }
+        mlp::stage_row(my_rows + d * mlp::RSTRIDE, x, active);
+    }
+    __syncthreads();
+    mlp::warp_logits(wts, rows[threadIdx.y], lg[threadIdx.y]);
+    __syncwarp();
+    const float best = fmaxf(lg[threadIdx.y][threadIdx.x * 3], fmaxf(lg[threadIdx.y][threadIdx.x * 3 + 1],
+                                                                       lg[threadIdx.y][threadIdx.x * 3 + 2]));
+    if (active) {
+        const long long e = ext_index(g, i, j, k);
+        const df64 gm1d = df_from_double(gm1);
+        bool full = best > logit_thr;
+#pragma unroll 1
+        for (int pass = 0; pass < 2; ++pass) {
+#pragma unroll 1
+            for (int c = 0; c < NV; ++c) {
+                df64 s[33], cf[20];
+                const df64* p = G + (long long)c * g.GN + ge;
+                s[0] = p[0];
+#pragma unroll
+                for (int o = 0; o < 4; ++o) {
+                    const int off = (o == 0) ? -2 : (o == 1) ? -1 : (o == 2) ? 1 : 2;
+                    s[S1(0, off)] = p[off];
+                    s[S1(1, off)] = p[off * sy];
+                    s[S1(2, off)] = p[off * sz];
+                }
+#pragma unroll
+                for (int sa = 0; sa < 2; ++sa)
+#pragma unroll
+                    for (int sb = 0; sb < 2; ++sb) {
+                        s[SQ(0, sa, 1, sb)] = p[(2 * sa - 1) + (2 * sb - 1) * sy];
+                        s[SQ(1, sa, 2, sb)] = p[(2 * sa - 1) * sy + (2 * sb - 1) * sz];
+                        s[SQ(0, sa, 2, sb)] = p[(2 * sa - 1) + (2 * sb - 1) * sz];
+                    }
+#pragma unroll
+                for (int a = 0; a < 2; ++a)
+#pragma unroll
+                    for (int b = 0; b < 2; ++b)
+#pragma unroll
+                        for (int dd = 0; dd < 2; ++dd)
+                            s[SO(a, b, dd)] = p[(2 * a - 1) + (2 * b - 1) * sy + (2 * dd - 1) * sz];
+                cweno4_df(s, !full, cf);
+                df64 tr[8];
+                const double r = df_ref(W, g, c);
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    if (d == 0) face_traces_df<0>(cf, tr);
+                    else if (d == 1) face_traces_df<1>(cf, tr);
+                    else face_traces_df<2>(cf, tr);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const long long at = ((long long)c * NTR + 8 * d + q) * g.NE + e;
+                        if constexpr (DFT) Td[at] = tr[q];
+                        else T[at] = r + df_to_double(tr[q]);
+                    }
+                }
+            }
+            bool ok;
+            if constexpr (DFT) ok = traces_admissible_df(Td, g, e, df_refstate(W, g, gm1d), gm1d);
+            else ok = traces_admissible<double>(T, g, e, gm1);
+            if (ok) break;
+            if (full) {  // CWENO4 itself inadmissible: first order (when enabled)
+                if (pad) {
+#pragma unroll 1
+                    for (int c = 0; c < NV; ++c) {
+                        const df64 dv = G[(long long)c * g.GN + ge];
+                        const double v = df_ref(W, g, c) + df_to_double(dv);
+                        for (int q = 0; q < NTR; ++q) {
+                            if constexpr (DFT) Td[((long long)c * NTR + q) * g.NE + e] = dv;
+                            else T[((long long)c * NTR + q) * g.NE + e] = v;
+                        }
+                    }
+                    if (!gi && !gj && !gk) atomicAdd(&cnt[1], 1u);
+                }
+                break;
+            }
+            full = true;  // the R4 traces broke positivity: redo the cell with CWENO4
+        }
+        if (full && !gi && !gj && !gk && best > logit_thr) atomicAdd(&cnt[0], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        if (cnt[0]) atomicAdd(&counters[0], (unsigned long long)cnt[0]);
+        if (cnt[1]) atomicAdd(&counters[1], (unsigned long long)cnt[1]);
+    }
+}
+
 // Indicator training data: for every stride-th owned cell, the three directional
 // normalised stencils (X[s][3][25]) and D[s], the largest change that the nonlinear
 // CWENO4 weights make to a face trace relative to the linear R4 polynomial, over the
@@ -1091,7 +1224,13 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
     const size_t ck_bytes = (f32 && e->p.positivity) ? sizeof(float) * 4 * 2 * NTR * 32 : 0;
     if (e->p.recon == HYPE_RECON_LEARNED) {
         if (!e->mlp) return HYPE_ERR_ARG;  // hype_euler_set_mlp first
-        if (f32)
+        if (df && e->p.flux == HYPE_FLUX_RUSANOV)
+            k_recon_learned_df<true><<<gr, br, 0, e->stream>>>((const df64*)e->G, e->T, Win, g, e->mlp, e->logit_thr, gm1,
+                                                               e->p.positivity, e->mlp_cnt);
+        else if (df)
+            k_recon_learned_df<false><<<gr, br, 0, e->stream>>>((const df64*)e->G, e->T, Win, g, e->mlp, e->logit_thr,
+                                                                gm1, e->p.positivity, e->mlp_cnt);
+        else if (f32)
             k_recon_learned<float><<<gr, br, 0, e->stream>>>((const float*)e->G, (float*)e->T, g, e->mlp, e->logit_thr, gm1,
                                                              e->p.positivity, e->mlp_cnt);
         else
@@ -1158,9 +1297,9 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
     if (p->recon < HYPE_RECON_CWENO4 || p->recon > HYPE_RECON_WENO3) return HYPE_ERR_ARG;
     if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32 && p->precision != HYPE_PREC_DF64)
         return HYPE_ERR_ARG;
-    // the double-float form covers CWENO4 and R4 (no WENO3, indicator or viscous fluxes)
-    if (p->precision == HYPE_PREC_DF64 && p->recon != HYPE_RECON_CWENO4 && p->recon != HYPE_RECON_LINEAR4)
-        return HYPE_ERR_UNSUPPORTED;
+    // the double-float form covers CWENO4, R4 and the indicator gate between them (no WENO3, no
+    // viscous fluxes)
+    if (p->precision == HYPE_PREC_DF64 && p->recon == HYPE_RECON_WENO3) return HYPE_ERR_UNSUPPORTED;
     if (p->dt_mode < HYPE_DT_MONITOR || p->dt_mode > HYPE_DT_FIXED) return HYPE_ERR_ARG;
     if (p->flux < HYPE_FLUX_RUSANOV || p->flux > HYPE_FLUX_ROTHLLC) return HYPE_ERR_ARG;
     if (p->positivity != 0 && p->positivity != 1) return HYPE_ERR_ARG;
@@ -1434,8 +1573,7 @@ extern "C" int hype_euler_indicator_stats(hype_euler* e, long long* flagged, lon
 extern "C" int hype_euler_set_recon(hype_euler* e, int recon) {
     if (!e || recon < HYPE_RECON_CWENO4 || recon > HYPE_RECON_WENO3) return HYPE_ERR_ARG;
     if (e->C4 && recon == HYPE_RECON_LEARNED) return HYPE_ERR_ARG;  // the viscous path keeps the R4 coefficients
-    if (e->p.precision == HYPE_PREC_DF64 && recon != HYPE_RECON_CWENO4 && recon != HYPE_RECON_LINEAR4)
-        return HYPE_ERR_UNSUPPORTED;
+    if (e->p.precision == HYPE_PREC_DF64 && recon == HYPE_RECON_WENO3) return HYPE_ERR_UNSUPPORTED;
     HYPE_CK(cudaStreamSynchronize(e->stream));
     e->p.recon = recon;
     return HYPE_OK;

@@ -607,8 +607,31 @@ def run_blast(args, ws, rank, local, n=512, ntrain=64, tau=0.01, prob=0.2):
                      "flagged_per_cell_stage": flagged / (4.0 * cells) if form == "learned_fp64" else None}
         rho64[form] = s64.get_state()[..., 0]
     s64.close()
-    l1_64 = float(np.abs(rho64["learned_fp64"] - rho64["plain_fp64"]).mean() / np.abs(rho64["plain_fp64"]).mean())
-    del rho64
+    # 4. the same two forms with the double-float reconstruction and flux (FP64 error bars)
+    sdf = H.EulerSolver(H.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, positivity=1,
+                                 precision=H._lib.PREC_DF64))
+    sdf.set_mlp(params, prob)
+    stream = torch.cuda.ExternalStream(L.hype_euler_stream(sdf._h))
+    for form, recon in (("plain_df64", H._lib.RECON_CWENO4), ("learned_df64", H._lib.RECON_LEARNED)):
+        sdf.set_recon(recon)
+        sdf.set_state(U0)
+        sdf.t, sdf.next_dt = 0.0, 0.0
+        sdf.step(1)
+        sdf.indicator_stats(reset=True)
+        e0.record(stream)
+        sdf.step(1)
+        e1.record(stream)
+        e1.synchronize()
+        msdf = _max_over_ranks(ws, e0.elapsed_time(e1))
+        flagged, fb = sdf.indicator_stats(reset=True)
+        res[form] = {"value": ws * cells / (msdf * 1e-3), "ms_per_step": msdf,
+                     "flagged_per_cell_stage": flagged / (4.0 * cells) if form == "learned_df64" else None}
+        rho64[form] = sdf.get_state()[..., 0]
+    sdf.close()
+    ref64 = rho64["plain_fp64"]
+    l1_64 = float(np.abs(rho64["learned_fp64"] - ref64).mean() / np.abs(ref64).mean())
+    l1_df = {f: float(np.abs(rho64[f] - ref64).mean() / np.abs(ref64).mean()) for f in ("plain_df64", "learned_df64")}
+    del rho64, ref64
     v = res["learned_fp32"]["value"]
     peak, kind = _peaks()
     ach = EULER_BYTES_PER_CELL_UPDATE * v / ws / 1e9
@@ -627,6 +650,10 @@ def run_blast(args, ws, rank, local, n=512, ntrain=64, tau=0.01, prob=0.2):
             "l1_rho_learned_vs_plain_fp32": l1,
             "speedup_learned_fp64_vs_plain_fp64": res["learned_fp64"]["value"] / res["plain_fp64"]["value"],
             "l1_rho_learned_fp64_vs_plain_fp64_after_2_steps": l1_64,
+            "speedup_learned_df64_vs_plain_fp64": res["learned_df64"]["value"] / res["plain_fp64"]["value"],
+            "l1_rho_vs_plain_fp64_after_2_steps": {"plain_df64": l1_df["plain_df64"],
+                                                   "learned_df64": l1_df["learned_df64"],
+                                                   "learned_fp64": l1_64},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                          "traffic": None},
             "gpu_launches": launches, "clocks": clocks}

@@ -143,3 +143,59 @@ def test_df64_rejects_what_it_does_not_cover(hype):
     s = _solver(hype, 8)
     with pytest.raises(Exception):
         s.set_recon(L.RECON_WENO3)
+
+
+def _gated(hype, n, prob, positivity=0, seed=3):
+    from acoustic_petsc_gb300 import indicator, workloads
+
+    s = _solver(hype, n, recon=hype._lib.RECON_LEARNED, positivity=positivity)
+    s.set_mlp(indicator.init_params(seed), prob)
+    s.set_state(workloads.euler_blast(n, p_ratio=3.0, rho_ratio=2.0))
+    return s
+
+
+@pytest.mark.parametrize("prob,recon", [(1e-30, 0), (1.0 - 1e-7, 1)])
+def test_df64_indicator_gate_limits(hype, prob, recon):
+    """the indicator-gated double-float reconstruction: a gate that flags every cell is the
+    double-float CWENO4, one that flags none its R4 limit, bit for bit"""
+    from acoustic_petsc_gb300 import workloads
+
+    n = 16
+    g = _gated(hype, n, prob)
+    g.step(3)
+    p = _solver(hype, n, recon=recon, positivity=0)
+    p.set_state(workloads.euler_blast(n, p_ratio=3.0, rho_ratio=2.0))
+    p.step(3)
+    assert np.array_equal(g.get_state(), p.get_state())
+    flagged, _ = g.indicator_stats()
+    assert (flagged > 0) == (recon == 0)
+
+
+def test_df64_indicator_gate_matches_fp64_gate(hype, oracle):
+    """the same network gating the FP64 and the double-float reconstructions on a blast: the
+    networks see the FP64 form's stencils rounded to FP32 and the double-float form's deviations,
+    so a cell whose logit sits within rounding of the threshold may go the other way; the
+    flagged counts agree within 1 %, and the states to the FP64 bar unless a cell flipped"""
+    from acoustic_petsc_gb300 import indicator, workloads
+
+    n = 16
+    params = indicator.init_params(5)
+    # a threshold that flags about a fifth of the cells of this state
+    probe = _solver(hype, n, precision=hype._lib.PREC_FP64)
+    probe.set_state(workloads.euler_blast(n, p_ratio=3.0, rho_ratio=2.0))
+    X, _ = indicator.sample(probe)
+    thr = float(np.quantile(indicator.score(X, params), 0.8))
+    prob = 1.0 / (1.0 + np.exp(-thr))
+    states, flags = [], []
+    for prec in (hype._lib.PREC_FP64, hype._lib.PREC_DF64):
+        s = _solver(hype, n, precision=prec, recon=hype._lib.RECON_LEARNED, positivity=1)
+        s.set_mlp(params, prob)
+        s.set_state(workloads.euler_blast(n, p_ratio=3.0, rho_ratio=2.0))
+        s.step(3)
+        states.append(s.get_state())
+        flags.append(s.indicator_stats())
+    assert flags[0][0] > 0 and abs(flags[0][0] - flags[1][0]) <= 0.01 * flags[0][0]
+    err = rel(states[1], states[0])
+    print(f"gate fp64 vs df64: flagged {flags[0][0]} / {flags[1][0]}, state difference {err:.2e}")
+    # a flipped cell next to the blast takes R4 in one run and CWENO4 in the other (1.6e-6 seen)
+    assert err <= (1e-12 if flags[0] == flags[1] else 1e-4)
