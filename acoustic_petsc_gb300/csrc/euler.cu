@@ -399,13 +399,25 @@ __device__ __forceinline__ void dev_side(const DfRef& R, const df64* d, df64 gm1
     sp = df_abs(u[D]) + df_sqrt(gam * p * ir);
 }
 
-// density and pressure of the 24 double-float deviation traces against the floors
+// density and pressure of the 24 double-float deviation traces against the floors: an FP32
+// estimate from the leading parts settles every point whose density and pressure lie clear
+// of the floors by more than its rounding (1e-5 of the magnitudes involved, NaN never
+// clear); the rest are decided in double-float
 __device__ __forceinline__ bool traces_admissible_df(const df64* __restrict__ T, const Geo& g, long long e,
                                                      const DfRef& R, df64 gm1) {
     for (int q = 0; q < NTR; ++q) {
         df64 d[NV];
 #pragma unroll
         for (int c = 0; c < NV; ++c) d[c] = T[((long long)c * NTR + q) * g.NE + e];
+        const float rf = R.rho.hi + d[0].hi, Ef = R.E.hi + d[4].hi;
+        const float mxf = R.m[0].hi + d[1].hi, myf = R.m[1].hi + d[2].hi, mzf = R.m[2].hi + d[3].hi;
+        const float m2 = mxf * mxf + myf * myf + mzf * mzf;
+        const float kef = 0.5f * m2 / rf;
+        const float pf = gm1.hi * (Ef - kef);
+        const float tr = 1.0e-5f * (fabsf(R.rho.hi) + fabsf(d[0].hi)) + 1.0e-14f;
+        const float tp = 1.0e-5f * gm1.hi * (fabsf(Ef) + fabsf(kef)) + 1.0e-12f;
+        if (rf > 1.0e-14f + tr && pf > 1.0e-12f + tp) continue;  // clearly admissible
+        if (rf < 1.0e-14f - tr || pf < 1.0e-12f - tp) return false;  // clearly not
         const df64 rho = R.rho + d[0];
         const df64 mx = R.m[0] + d[1], my = R.m[1] + d[2], mz = R.m[2] + d[3];
         const df64 p = ((R.E + d[4]) - df_scale(df_div((mx * mx + my * my) + mz * mz, rho), 0.5f)) * gm1;
