@@ -78,6 +78,40 @@ __device__ __forceinline__ double grad_poly(const double* c, double x, double y,
            2.0 * c[16] * y * z + c[17] * (x * x - r1_12) + 2.0 * c[18] * x * z + c[19] * x * y;
 }
 
+// grad_poly<D> at the 8 Gauss points of the two faces normal to D at once.  On a face
+// x_D = +-1/2 with tangential coordinates (t1, t2) = +-GPT (t1^2 = t2^2 = GPT^2) the normal
+// derivative is A + B1 t1 + B2 t2 + B12 t1 t2 with
+//   A   = c_D + 0.6 c_DDD + (c_t1t1D + c_t2t2D)(GPT^2 - 1/12) +- c_DD     (3 x^2 - 3/20 = 0.6, 2x = +-1)
+//   B1  = c_Dt1 +- c_DDt1,  B2 = c_Dt2 +- c_DDt2,  B12 = c_xyz,
+// about 14 operations per face instead of 4 evaluations of the 10-term gradient.
+template <int D>
+__device__ __forceinline__ void face_normal_grads(const double* c, double* __restrict__ T, long long NE, long long e) {
+    constexpr double gp = euler::GPT, g2 = euler::GPT * euler::GPT, q = euler::GPT * euler::GPT - 1. / 12.;
+    // coefficient slots of the 20-term basis (grad_poly above): linear, square, cube of D; the
+    // cross x_D t; x_D^2 t; t^2 x_D for both tangential axes
+    constexpr int LIN = 1 + D, SQ = 4 + D, CUBE = 10 + D;
+    constexpr int X1 = D == 0 ? 7 : D == 1 ? 7 : 9;    // c * x_D * t1
+    constexpr int X2 = D == 0 ? 9 : D == 1 ? 8 : 8;    // c * x_D * t2
+    constexpr int DD1 = D == 0 ? 13 : D == 1 ? 14 : 18;  // c * x_D^2 * t1 term (derivative 2 x_D t1)
+    constexpr int DD2 = D == 0 ? 17 : D == 1 ? 15 : 16;  // c * x_D^2 * t2 term
+    constexpr int TT1 = D == 0 ? 14 : D == 1 ? 13 : 17;  // c * (t1^2 - 1/12) x_D
+    constexpr int TT2 = D == 0 ? 18 : D == 1 ? 16 : 15;  // c * (t2^2 - 1/12) x_D
+    const double E = c[LIN] + 0.6 * c[CUBE] + (c[TT1] + c[TT2]) * q;
+    const double w = g2 * c[19];
+#pragma unroll
+    for (int sn = 0; sn < 2; ++sn) {
+        const double A = sn ? E + c[SQ] : E - c[SQ];
+        const double u = gp * (sn ? c[X1] + c[DD1] : c[X1] - c[DD1]);
+        const double v = gp * (sn ? c[X2] + c[DD2] : c[X2] - c[DD2]);
+        const double Ap = A + w, Am = A - w, s = u + v, d = u - v;
+        double* Tq = T + (long long)((2 * D + sn) * 4) * NE + e;
+        Tq[0 * NE] = Ap - s;  // (t1 -, t2 -)
+        Tq[1 * NE] = Am - d;  // (t1 -, t2 +)
+        Tq[2 * NE] = Am + d;  // (t1 +, t2 -)
+        Tq[3 * NE] = Ap + s;  // (t1 +, t2 +)
+    }
+}
+
 // T[face][gp][extended cell]: the face-normal gradient (times h) at the 4 Gauss points
 // of the 6 faces; Gauss point q = 2 (t1 > 0) + (t2 > 0), (t1, t2) the remaining axes
 __global__ void __launch_bounds__(128) k_ac_recon(const double* __restrict__ G, double* __restrict__ T, Geo g, int linear) {
@@ -114,17 +148,9 @@ __global__ void __launch_bounds__(128) k_ac_recon(const double* __restrict__ G, 
             for (int d = 0; d < 2; ++d) s[euler::SO(a, b, d)] = __ldg(p + (2 * a - 1) + (2 * b - 1) * sy + (2 * d - 1) * sz);
     euler::cweno4<double>(s, linear != 0, cf);
     const long long e = ext_index(g, i, j, k);
-    constexpr double gp = euler::GPT;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const double t1 = (q & 2) ? gp : -gp, t2 = (q & 1) ? gp : -gp;
-        T[(long long)(0 * 4 + q) * g.NE + e] = grad_poly<0>(cf, -0.5, t1, t2);
-        T[(long long)(1 * 4 + q) * g.NE + e] = grad_poly<0>(cf, 0.5, t1, t2);
-        T[(long long)(2 * 4 + q) * g.NE + e] = grad_poly<1>(cf, t1, -0.5, t2);
-        T[(long long)(3 * 4 + q) * g.NE + e] = grad_poly<1>(cf, t1, 0.5, t2);
-        T[(long long)(4 * 4 + q) * g.NE + e] = grad_poly<2>(cf, t1, t2, -0.5);
-        T[(long long)(5 * 4 + q) * g.NE + e] = grad_poly<2>(cf, t1, t2, 0.5);
-    }
+    face_normal_grads<0>(cf, T, g.NE, e);
+    face_normal_grads<1>(cf, T, g.NE, e);
+    face_normal_grads<2>(cf, T, g.NE, e);
 }
 
 // face flux sum_q w_q c^2 (gL + gR) / 2, w_q = 1/4 (the gradients carry a factor h
