@@ -93,3 +93,22 @@ def test_point_source_2d_bitwise(hype, oracle, order, bc):
     a, b, r = oracle.ctcs_pointsrc(cfg, z, z, 95, receiver=True)
     ga, gb = lf.get()
     assert np.array_equal(gb, b) and np.array_equal(rec, r)
+
+
+def test_line_source_2d_program_matches_greens_function(hype):
+    """2d/ctcs/line_source's program (500^2 nodes of h = 1, 4th-order stencil, c0 = 580,
+    dt = 1e-3, 502 steps, periodic, source (250,250), receiver (330,330)) against its
+    results/green.py comparison, the 2D Green's function convolved with the wavelet: 1.5 %
+    relative L2 misfit with the CPU checker (second order in time), bound 3 %"""
+    from acoustic_petsc_gb300 import analytic
+
+    n = 500
+    z = np.zeros((n, n))
+    lf = hype.Leapfrog(z.shape, dx=1.0, dt=0.001, c0=580.0, form=1, order=4, bc=0, f0=65.0, src=(250, 250),
+                       rec=(330, 330))
+    lf.set(z, z)
+    rec = lf.UpdatePressure(502)
+    t = np.arange(502) * 0.001
+    misfit = analytic.relative_l2_misfit(rec, analytic.line_source_receiver_2d(t, 80 * np.sqrt(2.0), 580.0, 65.0))
+    print(f"CTCS line source 500^2: receiver misfit {misfit:.3e}")
+    assert misfit < 0.03
