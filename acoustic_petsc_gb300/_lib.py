@@ -84,7 +84,7 @@ class Mp2dParams(C.Structure):
 class AcousticParams(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("x_min", C.c_double), ("y_min", C.c_double),
                 ("z_min", C.c_double), ("h", C.c_double), ("c", C.c_double), ("dt", C.c_double), ("bc", C.c_int * 6),
-                ("recon", C.c_int)]
+                ("recon", C.c_int), ("precision", C.c_int)]
 
 
 class Status(C.Structure):

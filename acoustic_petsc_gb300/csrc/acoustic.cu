@@ -19,6 +19,7 @@
 #include <math.h>
 #include <string.h>
 
+#include "euler_df64.cuh"
 #include "euler_kernels.cuh"
 #include "point_source.cuh"
 
@@ -52,7 +53,12 @@ __device__ __forceinline__ int amap(int i, int n, int blo, int bhi, int* flip) {
                 bhi == HYPE_BC_PERIODIC ? HYPE_BC_PERIODIC : HYPE_BC_REFLECTIVE, flip);
 }
 
-__global__ void __launch_bounds__(128) k_ac_ghost(const double* __restrict__ U, double* __restrict__ G, Geo g) {
+__device__ __forceinline__ void put_g(double* p, double v) { *p = v; }
+__device__ __forceinline__ void put_g(df64* p, double v) { *p = df_from_double(v); }
+
+// G: the ghosted u in FP64, or (HYPE_PREC_DF64) as double-float pairs
+template <typename GT>
+__global__ void __launch_bounds__(128) k_ac_ghost(const double* __restrict__ U, GT* __restrict__ G, Geo g) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x - GW;
     const int j = blockIdx.y - GW, k = blockIdx.z - GW;
     if (i >= g.nx + GW) return;
@@ -60,8 +66,9 @@ __global__ void __launch_bounds__(128) k_ac_ghost(const double* __restrict__ U, 
     const int mi = amap(i, g.nx, g.bc[0], g.bc[1], &fi);
     const int mj = amap(j, g.ny, g.bc[2], g.bc[3], &fj);
     const int mk = amap(k, g.nz, g.bc[4], g.bc[5], &fk);
-    const double v = __ldg(U + ((long long)mk * g.ny + mj) * g.nx + mi);  // component u
-    G[ghost_index(g, i, j, k)] = ((fi + fj + fk) & 1) ? -v : v;
+    double v = __ldg(U + ((long long)mk * g.ny + mj) * g.nx + mi);  // component u
+    if ((fi + fj + fk) & 1) v = -v;
+    put_g(G + ghost_index(g, i, j, k), v);
 }
 
 // gradient component D of the 20-term polynomial at (x, y, z), times h
@@ -153,6 +160,93 @@ __global__ void __launch_bounds__(128) k_ac_recon(const double* __restrict__ G, 
     face_normal_grads<2>(cf, T, g.NE, e);
 }
 
+// the double-float form: face_normal_grads in pairs of FP32 numbers
+template <int D>
+__device__ __forceinline__ void face_normal_grads_df(const df64* c, df64* __restrict__ T, long long NE, long long e) {
+    constexpr double gp = euler::GPT, g2 = euler::GPT * euler::GPT, q = euler::GPT * euler::GPT - 1. / 12.;
+    constexpr int LIN = 1 + D, SQ = 4 + D, CUBE = 10 + D;
+    constexpr int X1 = D == 0 ? 7 : D == 1 ? 7 : 9;
+    constexpr int X2 = D == 0 ? 9 : D == 1 ? 8 : 8;
+    constexpr int DD1 = D == 0 ? 13 : D == 1 ? 14 : 18;
+    constexpr int DD2 = D == 0 ? 17 : D == 1 ? 15 : 16;
+    constexpr int TT1 = D == 0 ? 14 : D == 1 ? 13 : 17;
+    constexpr int TT2 = D == 0 ? 18 : D == 1 ? 16 : 15;
+    const df64 E = c[LIN] + (c[CUBE] * dfc(0.6) + (c[TT1] + c[TT2]) * dfc(q));
+    const df64 w = c[19] * dfc(g2);
+#pragma unroll
+    for (int sn = 0; sn < 2; ++sn) {
+        const df64 A = sn ? E + c[SQ] : E - c[SQ];
+        const df64 u = (sn ? c[X1] + c[DD1] : c[X1] - c[DD1]) * dfc(gp);
+        const df64 v = (sn ? c[X2] + c[DD2] : c[X2] - c[DD2]) * dfc(gp);
+        const df64 Ap = A + w, Am = A - w, s = u + v, d = u - v;
+        df64* Tq = T + (long long)((2 * D + sn) * 4) * NE + e;
+        Tq[0 * NE] = Ap - s;
+        Tq[1 * NE] = Am - d;
+        Tq[2 * NE] = Am + d;
+        Tq[3 * NE] = Ap + s;
+    }
+}
+
+// k_ac_recon in double-float: the R4 / CWENO4 coefficients (euler_df64.cuh) and the 24 face-
+// normal gradients, kept as pairs for k_ac_faces_df
+__global__ void __launch_bounds__(128, 2) k_ac_recon_df(const df64* __restrict__ G, df64* __restrict__ T, Geo g,
+                                                        int linear) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+    const int k = blockIdx.z - 1;
+    if (i > g.nx || j > g.ny) return;
+    const int gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny), gk = (k < 0 || k >= g.nz);
+    if (gi + gj + gk > 1) return;
+    const df64* p = G + ghost_index(g, i, j, k);
+    const int sy = g.gx, sz = g.gx * g.gy;
+    df64 s[33], cf[20];
+    s[0] = p[0];
+#pragma unroll
+    for (int o = 0; o < 4; ++o) {
+        const int off = (o == 0) ? -2 : (o == 1) ? -1 : (o == 2) ? 1 : 2;
+        s[euler::S1(0, off)] = p[off];
+        s[euler::S1(1, off)] = p[off * sy];
+        s[euler::S1(2, off)] = p[off * sz];
+    }
+#pragma unroll
+    for (int sa = 0; sa < 2; ++sa)
+#pragma unroll
+        for (int sb = 0; sb < 2; ++sb) {
+            s[euler::SQ(0, sa, 1, sb)] = p[(2 * sa - 1) + (2 * sb - 1) * sy];
+            s[euler::SQ(1, sa, 2, sb)] = p[(2 * sa - 1) * sy + (2 * sb - 1) * sz];
+            s[euler::SQ(0, sa, 2, sb)] = p[(2 * sa - 1) + (2 * sb - 1) * sz];
+        }
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int d = 0; d < 2; ++d) s[euler::SO(a, b, d)] = p[(2 * a - 1) + (2 * b - 1) * sy + (2 * d - 1) * sz];
+    euler::cweno4_df(s, linear != 0, cf);
+    const long long e = ext_index(g, i, j, k);
+    face_normal_grads_df<0>(cf, T, g.NE, e);
+    face_normal_grads_df<1>(cf, T, g.NE, e);
+    face_normal_grads_df<2>(cf, T, g.NE, e);
+}
+
+// k_ac_faces in double-float: 1/8 c^2 sum_q (gL + gR), rounded once to FP64
+template <int D>
+__global__ void __launch_bounds__(128) k_ac_faces_df(const df64* __restrict__ T, double* __restrict__ F, Geo g,
+                                                     double c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    const int fx = g.nx + (D == 0), fy = g.ny + (D == 1);
+    if (i >= fx || j >= fy) return;
+    const long long eR = ext_index(g, i, j, k);
+    const long long eL = ext_index(g, i - (D == 0), j - (D == 1), k - (D == 2));
+    df64 sum = df64{0.0f, 0.0f};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        sum = sum + (T[(long long)((2 * D + 1) * 4 + q) * g.NE + eL] + T[(long long)((2 * D) * 4 + q) * g.NE + eR]);
+    F[((long long)k * fy + j) * fx + i] = df_to_double(df_scale(sum * df_from_double(c2), 0.125f));
+}
+
 // face flux sum_q w_q c^2 (gL + gR) / 2, w_q = 1/4 (the gradients carry a factor h
 // that the divergence's 1/h^2 removes)
 template <int D>
@@ -239,7 +333,20 @@ struct hype_acoustic {
 
 static int ac_rhs(hype_acoustic* a, const double* Win) {
     const Geo& g = a->g;
-    k_ac_ghost<<<dim3(cdiv(g.gx, 128), g.gy, g.nz + 2 * GW), 128, 0, a->stream>>>(Win, a->Gh, g);
+    if (a->p.precision == HYPE_PREC_DF64) {
+        k_ac_ghost<df64><<<dim3(cdiv(g.gx, 128), g.gy, g.nz + 2 * GW), 128, 0, a->stream>>>(Win, (df64*)a->Gh, g);
+        k_ac_recon_df<<<dim3(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2), dim3(32, 4), 0, a->stream>>>(
+            (const df64*)a->Gh, (df64*)a->T, g, a->p.recon == HYPE_RECON_LINEAR4);
+        const double c2 = a->p.c * a->p.c;
+        const dim3 bf(32, 4);
+        const df64* T = (const df64*)a->T;
+        k_ac_faces_df<0><<<dim3(cdiv(g.nx + 1, 32), cdiv(g.ny, 4), g.nz), bf, 0, a->stream>>>(T, a->Fx, g, c2);
+        k_ac_faces_df<1><<<dim3(cdiv(g.nx, 32), cdiv(g.ny + 1, 4), g.nz), bf, 0, a->stream>>>(T, a->Fy, g, c2);
+        k_ac_faces_df<2><<<dim3(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz + 1), bf, 0, a->stream>>>(T, a->Fz, g, c2);
+        HYPE_LAUNCHED(5);
+        return HYPE_OK;
+    }
+    k_ac_ghost<double><<<dim3(cdiv(g.gx, 128), g.gy, g.nz + 2 * GW), 128, 0, a->stream>>>(Win, a->Gh, g);
     k_ac_recon<<<dim3(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2), dim3(32, 4), 0, a->stream>>>(
         a->Gh, a->T, g, a->p.recon == HYPE_RECON_LINEAR4);
     const double c2 = a->p.c * a->p.c;
@@ -269,6 +376,7 @@ extern "C" int hype_acoustic_create(const hype_acoustic_params* p, hype_acoustic
     for (int d = 0; d < 3; ++d)
         if ((p->bc[2 * d] == HYPE_BC_PERIODIC) != (p->bc[2 * d + 1] == HYPE_BC_PERIODIC)) return HYPE_ERR_ARG;
     if (p->recon != HYPE_RECON_LINEAR4 && p->recon != HYPE_RECON_CWENO4) return HYPE_ERR_ARG;
+    if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_DF64) return HYPE_ERR_ARG;
     hype_acoustic* a = new hype_acoustic();
     a->p = *p;
     Geo& g = a->g;

@@ -456,8 +456,9 @@ class AcousticFV3D:
     face-normal gradients, a central flux and SSPRK(4,3) with a fixed dt."""
 
     def __init__(self, N_x, N_y, N_z, h, dt, c=1.0, x_min=0.0, y_min=0.0, z_min=0.0,
-                 boundaries=(L.BC_PERIODIC,) * 6, recon=L.RECON_LINEAR4):
+                 boundaries=(L.BC_PERIODIC,) * 6, recon=L.RECON_LINEAR4, precision=L.PREC_FP64):
         p = L.AcousticParams()
+        p.precision = precision
         p.nx, p.ny, p.nz = N_x, N_y, N_z
         p.x_min, p.y_min, p.z_min, p.h, p.c, p.dt = x_min, y_min, z_min, h, c, dt
         for q in range(6):

@@ -736,7 +736,7 @@ def run_mp2d_learned(args, ws, rank, local, n=1024, ntrain=256, tau=1e-4, prob=0
             "gpu_launches": launches, "clocks": clocks}
 
 
-def run_acoustic(args, ws, rank, local, n=256):
+def run_acoustic(args, ws, rank, local, n=256, precision=0):
     """acoustic FV path of 3d/weno4/plane_wave: the plane wave k = (1,1,1) on [0, 2 pi]^3,
     periodic, R4 face gradients + central flux, SSPRK(4,3) with dt = h CFL / 3, CFL 0.5"""
     import math
@@ -749,7 +749,7 @@ def run_acoustic(args, ws, rank, local, n=256):
     H._lib.check(L.hype_set_device(local), "hype_set_device")
     torch.cuda.set_device(local)
     h = 2 * math.pi / n
-    s = H.AcousticFV3D(n, n, n, h, h * 0.5 / 3.0)
+    s = H.AcousticFV3D(n, n, n, h, h * 0.5 / 3.0, precision=precision)
     x = (np.arange(n) + 0.5) * h
     ph = x[:, None, None] + x[None, :, None] + x[None, None, :]
     U0 = np.stack([np.sin(ph), -math.sqrt(3.0) * np.cos(ph)], -1)
@@ -775,8 +775,11 @@ def run_acoustic(args, ws, rank, local, n=256):
     s.close()
     return {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic plane wave sin(x+y+z), exact cell-centre values",
-            "config": {"workload": f"acoustic_fv_plane_wave_{n}", "grid": [n, n, n], "cfl": 0.5,
+            "vs_baseline": None,
+            "dtype": "f64" if precision == 0 else "f64 state / df64 (FP32 pairs) gradients and fluxes",
+            "data": "synthetic plane wave sin(x+y+z), exact cell-centre values",
+            "config": {"workload": f"acoustic_fv_plane_wave_{n}" + ("_df64" if precision else ""), "grid": [n, n, n],
+                       "cfl": 0.5,
                        "scheme": "R4 face gradients + central flux + SSPRK(4,3), 3d/weno4/plane_wave"},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                          "traffic": None},
@@ -981,6 +984,7 @@ WORKLOADS = {
     "kapila1024": lambda a, *r: run_mp2d(a, *r, precision=0),
     "kapila1024_learned": run_mp2d_learned,
     "acoustic256": run_acoustic,
+    "acoustic256_df64": lambda a, *r: run_acoustic(a, *r, precision=2),
     "kapila1024_fp32": lambda a, *r: run_mp2d(a, *r, precision=1),
     "euler256_hllc": lambda a, *r: run_euler(a, *r, precision=0, recon=0, flux=1),
     "euler256": lambda a, *r: run_euler(a, *r, precision=0, recon=0),

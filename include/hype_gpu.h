@@ -274,6 +274,8 @@ typedef struct {
     double dt;  /* fixed time step (hype.c:56: h CFL / (3 c)) */
     int bc[6];  /* HYPE_BC_PERIODIC or HYPE_BC_ADIABATIC */
     int recon;  /* HYPE_RECON_LINEAR4 (the reference's setting) or HYPE_RECON_CWENO4 */
+    int precision; /* HYPE_PREC_FP64, or HYPE_PREC_DF64: reconstruction, gradients and face fluxes in double-float
+                      (FP32 pairs), state and stage accumulation in FP64 */
 } hype_acoustic_params;
 
 int hype_acoustic_create(const hype_acoustic_params* p, hype_acoustic** out);

@@ -116,3 +116,53 @@ def test_point_source_program_matches_greens_function(hype):
     misfit = analytic.relative_l2_misfit(us, ua)
     print(f"point source 100^3: receiver misfit {misfit:.3e}")
     assert misfit < 5e-3
+
+
+# ---------------------------------------------------------------- the double-float form
+@pytest.mark.parametrize("name", ["periodic", "adiabatic", "mixed"])
+def test_df64_rhs_and_steps_vs_reference(hype, name):
+    """HYPE_PREC_DF64 (R4, gradients and face fluxes in FP32 pairs, FP64 state and stages)
+    at the FP64 form's bars against the reference fixtures"""
+    from acoustic_petsc_gb300 import _lib as L
+
+    z = np.load(os.path.join(GOLDEN, f"ref_acoustic_{name}.npz"))
+    nx, ny, nz = (int(v) for v in z["shape"])
+    mk = lambda: hype.AcousticFV3D(nx, ny, nz, float(z["h"]), float(z["dt"]), boundaries=tuple(int(b) for b in z["bc"]),
+                                   precision=L.PREC_DF64)
+    s = mk()
+    e_rhs = rel(s.RHSFunction(0.0, z["U"]), z["RHS"])
+    s.set_state(z["U"])
+    assert s.step(3) == 3
+    e3 = rel(s.get_state(), z["U3"])
+    print(f"acoustic df64 {name}: RHS {e_rhs:.2e}, 3 steps {e3:.2e}")
+    assert e_rhs <= 1e-12 and e3 <= 1e-12
+
+
+def test_df64_convergence_table_and_point_source(hype, oracle):
+    """the published convergence table (N = 16, 32, 64) and the 100^3 point-source receiver with
+    the double-float form, as the FP64 form reproduces them"""
+    from acoustic_petsc_gb300 import _lib as L
+    from acoustic_petsc_gb300 import analytic
+
+    with open(os.path.join(GOLDEN, "accuracy_tables.json")) as f:
+        table = {int(r[0]): (r[1], r[2]) for r in json.load(f)["plane_wave_3d_main_tex"]}
+    for n in (16, 32, 64):
+        h = 2 * math.pi / n
+        cfg = oracle.acoustic_cfg(n, h)
+        s = hype.AcousticFV3D(n, n, n, h, h * 0.5 / 3.0, precision=L.PREC_DF64)
+        s.set_state(oracle.plane_wave_ic(cfg))
+        s.step(10**6, t_final=1.0)
+        l2, linf = oracle.plane_wave_errors(cfg, s.get_state(), s.t)
+        assert abs(l2 - table[n][0]) <= 2e-3 * table[n][0] and abs(linf - table[n][1]) <= 2e-3 * table[n][1]
+    n, h, dt = 100, 0.5, 0.0005
+    s = hype.AcousticFV3D(n, n, n, h, dt, c=250.0, precision=L.PREC_DF64)
+    s.set_point_source((50, 50, 50), 100.0, (57, 57, 57), capacity=4 * 251 + 1)
+    U0 = np.zeros((n, n, n, 2))
+    s.RHSFunction(0.0, U0)
+    s.set_state(U0)
+    s.step(251)
+    t, u, cnt = s.receiver_trace()
+    misfit = analytic.relative_l2_misfit(u[1::4], analytic.point_source_receiver_3d(t[1::4], 7 * math.sqrt(3.0) * h,
+                                                                                      250.0, 100.0))
+    print(f"acoustic df64 point source 100^3: receiver misfit {misfit:.3e}")
+    assert misfit < 5e-3
