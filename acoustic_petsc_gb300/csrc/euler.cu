@@ -434,7 +434,8 @@ __device__ __forceinline__ bool traces_admissible_df(const df64* __restrict__ T,
 template <bool DFT>
 __global__ void __launch_bounds__(128, 2)
     k_recon_df(const df64* __restrict__ G, void* __restrict__ Tv, const double* __restrict__ W, Geo g, int recon,
-               int pad, double gm1, unsigned long long* __restrict__ counters) {
+               int pad, double gm1, unsigned long long* __restrict__ counters, df64* __restrict__ C4 = nullptr,
+               double c4_scale = 1.0) {
     double* T = (double*)Tv;
     df64* Td = (df64*)Tv;
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
@@ -474,6 +475,18 @@ __global__ void __launch_bounds__(128, 2)
                     for (int d = 0; d < 2; ++d) s[SO(a, b, d)] = p[(2 * a - 1) + (2 * b - 1) * sy + (2 * d - 1) * sz];
         }
         cweno4_df(s, recon == HYPE_RECON_LINEAR4, cf);
+        if (C4) {  // the R4 polynomial (times 1/h) of the deviations, for the viscous face gradients
+            const df64 sc = df_from_double(c4_scale);
+            df64 r4[20];
+            if (recon == HYPE_RECON_LINEAR4) {
+#pragma unroll
+                for (int q = 0; q < 20; ++q) r4[q] = cf[q];
+            } else {
+                cweno4_df(s, true, r4);
+            }
+#pragma unroll
+            for (int q = 1; q < 20; ++q) C4[((long long)c * 20 + q) * g.NE + e] = r4[q] * sc;
+        }
         df64 tr[8];
         if constexpr (DFT) {
             df64* Tc = Td + (long long)c * NTR * g.NE + e;
@@ -830,15 +843,58 @@ __device__ __forceinline__ double visc_side(const double* __restrict__ T, const 
 // 1/2 (dF_L + dF_R) - 1/2 s (d_R - d_L) at each Gauss point, weight 1/4, where s is the
 // larger wave speed (pde.c:164-187); every term has the size of the deviations, so the
 // 48-bit significand meets the FP64 form's error bars with the face solver on the FP32 pipe.
-template <int D>
+// one side's share of PDEViscRiemannSolver (Navier-Stokes-3D/pde.c:386-404) in double-float:
+// 1/8 F_v at each of the 4 Gauss points of the side's face, from its traces (r + deviation)
+// and the R4 gradients of the deviations; returns the largest viscous speed
+template <int D, int NS>
+__device__ __forceinline__ double visc_side_df(const df64* __restrict__ T, const df64* __restrict__ C4, const Geo& g,
+                                               long long e, const DfRef& R, df64 gm1, df64 mu, df64 kc, df64 vmax,
+                                               df64* av) {
+    FaceGradDf fg[NV][3];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        const df64* p = C4 + (long long)c * 20 * g.NE + e;
+        fg[c][0] = face_grad_df<D, NS, 0>(p, g.NE);
+        fg[c][1] = face_grad_df<D, NS, 1>(p, g.NE);
+        fg[c][2] = face_grad_df<D, NS, 2>(p, g.NE);
+    }
+    constexpr int face = 2 * D + (NS > 0 ? 1 : 0);
+    double sv = 0.0;
+    auto at = [&](auto gpc) {
+        constexpr int gp = decltype(gpc)::value;
+        df64 Q[NV], Gq[NV][3], Fv[NV];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            Q[c] = T[((long long)c * NTR + face * 4 + gp) * g.NE + e];
+#pragma unroll
+            for (int b = 0; b < 3; ++b) Gq[c][b] = fg_eval_df<gp>(fg[c][b]);
+        }
+        Q[0] = R.rho + Q[0];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) Q[1 + i] = R.m[i] + Q[1 + i];
+        Q[4] = R.E + Q[4];
+        sv = fmax(sv, df_to_double(visc_flux_df<D>(Q, Gq, gm1, mu, kc, vmax, Fv)));
+#pragma unroll
+        for (int c = 0; c < NV; ++c) av[c] = av[c] + df_scale(Fv[c], 0.125f);
+    };
+    at(std::integral_constant<int, 0>{});
+    at(std::integral_constant<int, 1>{});
+    at(std::integral_constant<int, 2>{});
+    at(std::integral_constant<int, 3>{});
+    return sv;
+}
+
+template <int D, bool VISC = false>
 __global__ void __launch_bounds__(128) k_faces_df(const df64* __restrict__ T, double* __restrict__ F,
                                                   const double* __restrict__ W, Geo g, double gamma,
-                                                  DevScalars* __restrict__ ds, int slot) {
+                                                  DevScalars* __restrict__ ds, int slot,
+                                                  const df64* __restrict__ C4 = nullptr,
+                                                  Visc vp = Visc{0.0, 0.0, 0.0, 0.0}) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
     const int fx = g.nx + (D == 0), fy = g.ny + (D == 1);
-    double smax = 0.0;
+    double smax = 0.0, smaxv = 0.0;
     bool bad = false;
     if (i < fx && j < fy) {
         const long long eR = ext_index(g, i, j, k);
@@ -863,6 +919,11 @@ __global__ void __launch_bounds__(128) k_faces_df(const df64* __restrict__ T, do
 #pragma unroll
             for (int c = 0; c < NV; ++c) acc[c] = acc[c] + df_scale((fL[c] + fR[c]) - sm * (dR[c] - dL[c]), 0.125f);
         }
+        if constexpr (VISC) {
+            const df64 mu = df_from_double(vp.mu), kc = df_from_double(vp.kc), vmax = df_from_double(vp.vmax);
+            smaxv = visc_side_df<D, 1>(T, C4, g, eL, R, gm1, mu, kc, vmax, acc);
+            smaxv = fmax(smaxv, visc_side_df<D, -1>(T, C4, g, eR, R, gm1, mu, kc, vmax, acc));
+        }
         const long long nf = (long long)fx * fy * (g.nz + (D == 2));
         const long long f = ((long long)k * fy + j) * fx + i;
 #pragma unroll
@@ -875,6 +936,11 @@ __global__ void __launch_bounds__(128) k_faces_df(const df64* __restrict__ T, do
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, o));
     if ((threadIdx.x & 31) == 0 && smax > 0.0) atomic_max_pos(&ds->smax_bits[slot], smax);
+    if constexpr (VISC) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) smaxv = fmax(smaxv, __shfl_xor_sync(0xffffffffu, smaxv, o));
+        if ((threadIdx.x & 31) == 0 && smaxv > 0.0) atomic_max_pos(&ds->smaxv_bits[slot], smaxv);
+    }
 }
 
 template <typename R, int D, int FLUX, bool VISC = false>
@@ -1251,7 +1317,7 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
     } else if (df) {
         if (e->p.flux == HYPE_FLUX_RUSANOV)
             k_recon_df<true><<<gr, br, 0, e->stream>>>((const df64*)e->G, e->T, Win, g, rec, e->p.positivity, gm1,
-                                                       e->mlp_cnt);
+                                                       e->mlp_cnt, (df64*)e->C4, 1.0 / e->p.h);
         else
             k_recon_df<false><<<gr, br, 0, e->stream>>>((const df64*)e->G, e->T, Win, g, rec, e->p.positivity, gm1,
                                                         e->mlp_cnt);
@@ -1264,7 +1330,20 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
     }
     prof_mark(e, 0, false);
     prof_mark(e, 1, true);
-    if (e->C4) {
+    if (e->C4 && df) {
+        // Navier-Stokes in double-float: Rusanov in deviation form plus both sides' viscous fluxes
+        const double mu = e->p.mu, gm = e->p.gamma;
+        const Visc vp{mu, e->p.cv * mu * gm / e->p.prandtl, std::max((4. / 3.) * mu, gm * mu / e->p.prandtl),
+                      1.0 / e->p.h};
+        const dim3 bf(32, 4);
+        const dim3 fgx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4), g.nz), fgy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4), g.nz),
+            fgz(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz + 1);
+        const df64* Td = (const df64*)e->T;
+        const df64* C4 = (const df64*)e->C4;
+        k_faces_df<0, true><<<fgx, bf, 0, e->stream>>>(Td, e->Fx, Win, g, e->p.gamma, e->ds, slot, C4, vp);
+        k_faces_df<1, true><<<fgy, bf, 0, e->stream>>>(Td, e->Fy, Win, g, e->p.gamma, e->ds, slot, C4, vp);
+        k_faces_df<2, true><<<fgz, bf, 0, e->stream>>>(Td, e->Fz, Win, g, e->p.gamma, e->ds, slot, C4, vp);
+    } else if (e->C4) {
         // Navier-Stokes: the inviscid flux plus the average of both sides' viscous fluxes
         const double mu = e->p.mu, g = e->p.gamma;
         const Visc vp{mu, e->p.cv * mu * g / e->p.prandtl, std::max((4. / 3.) * mu, g * mu / e->p.prandtl), 1.0 / e->p.h};
@@ -1315,11 +1394,13 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
     if (p->dt_mode < HYPE_DT_MONITOR || p->dt_mode > HYPE_DT_FIXED) return HYPE_ERR_ARG;
     if (p->flux < HYPE_FLUX_RUSANOV || p->flux > HYPE_FLUX_ROTHLLC) return HYPE_ERR_ARG;
     if (p->positivity != 0 && p->positivity != 1) return HYPE_ERR_ARG;
-    // viscosity: FP64 only, with the CWENO4 / R4 / WENO3 traces (the gradients always come from R4)
+    // viscosity: FP64 (with the CWENO4 / R4 / WENO3 traces) or the double-float form with the Rusanov
+    // flux; the gradients always come from R4
     const bool visc = p->mu != 0.0;
-    if (visc && (!(p->mu > 0.0) || !(p->prandtl > 0.0) || !(p->cv > 0.0) || p->precision != HYPE_PREC_FP64 ||
+    if (visc && (!(p->mu > 0.0) || !(p->prandtl > 0.0) || !(p->cv > 0.0) || p->precision == HYPE_PREC_FP32 ||
                  p->recon == HYPE_RECON_LEARNED))
         return HYPE_ERR_ARG;
+    if (visc && p->precision == HYPE_PREC_DF64 && p->flux != HYPE_FLUX_RUSANOV) return HYPE_ERR_UNSUPPORTED;
     hype_euler* e = new hype_euler();
     e->p = *p;
     Geo& g = e->g;

@@ -179,5 +179,120 @@ __device__ __forceinline__ void face_traces_df(const df64* __restrict__ c, df64*
     }
 }
 
+// ---------------------------------------------------------------- viscous fluxes in double-float
+// face_grad / fg_eval / visc_flux of euler_kernels.cuh on pairs: the gradient of the R4
+// polynomial (coefficients of the deviations, times 1/h) on a face side as P + Q t1 + R t2 + S t1 t2
+struct FaceGradDf {
+    df64 p, q, r, s;
+};
+
+template <int D, int NS, int EX, int EY, int EZ>
+__device__ __forceinline__ void fg_term_df(FaceGradDf& f, df64 c, double k) {
+    constexpr int eD = D == 0 ? EX : (D == 1 ? EY : EZ);
+    constexpr int e1 = D == 0 ? EY : EX, e2 = D == 2 ? EY : EZ;
+    constexpr double n = 0.5 * NS;
+    constexpr double nf = eD == 0 ? 1.0 : (eD == 1 ? n : n * n);
+    if constexpr (e1 == 2 || e2 == 2) f.p = f.p + c * dfc(k * (nf * G2));
+    else if constexpr (e1 == 0 && e2 == 0) f.p = f.p + c * dfc(k * nf);
+    else if constexpr (e1 == 1 && e2 == 0) f.q = f.q + c * dfc(k * nf);
+    else if constexpr (e1 == 0 && e2 == 1) f.r = f.r + c * dfc(k * nf);
+    else f.s = f.s + c * dfc(k * nf);
+}
+
+template <int D, int NS, int B>
+__device__ __forceinline__ FaceGradDf face_grad_df(const df64* __restrict__ p, long long st) {
+    auto C = [&](int q) { return p[q * st]; };
+    const df64 z{0.0f, 0.0f};
+    FaceGradDf f{z, z, z, z};
+    if constexpr (B == 0) {
+        fg_term_df<D, NS, 0, 0, 0>(f, C(1), 1.0);
+        fg_term_df<D, NS, 1, 0, 0>(f, C(4), 2.0);
+        fg_term_df<D, NS, 0, 1, 0>(f, C(7), 1.0);
+        fg_term_df<D, NS, 0, 0, 1>(f, C(9), 1.0);
+        const df64 c10 = C(10), c14 = C(14), c18 = C(18);
+        fg_term_df<D, NS, 2, 0, 0>(f, c10, 3.0);
+        fg_term_df<D, NS, 0, 0, 0>(f, c10, -R3_20);
+        fg_term_df<D, NS, 1, 1, 0>(f, C(13), 2.0);
+        fg_term_df<D, NS, 0, 2, 0>(f, c14, 1.0);
+        fg_term_df<D, NS, 0, 0, 0>(f, c14, -R1_12);
+        fg_term_df<D, NS, 1, 0, 1>(f, C(17), 2.0);
+        fg_term_df<D, NS, 0, 0, 2>(f, c18, 1.0);
+        fg_term_df<D, NS, 0, 0, 0>(f, c18, -R1_12);
+        fg_term_df<D, NS, 0, 1, 1>(f, C(19), 1.0);
+    } else if constexpr (B == 1) {
+        fg_term_df<D, NS, 0, 0, 0>(f, C(2), 1.0);
+        fg_term_df<D, NS, 0, 1, 0>(f, C(5), 2.0);
+        fg_term_df<D, NS, 1, 0, 0>(f, C(7), 1.0);
+        fg_term_df<D, NS, 0, 0, 1>(f, C(8), 1.0);
+        const df64 c11 = C(11), c13 = C(13), c16 = C(16);
+        fg_term_df<D, NS, 0, 2, 0>(f, c11, 3.0);
+        fg_term_df<D, NS, 0, 0, 0>(f, c11, -R3_20);
+        fg_term_df<D, NS, 2, 0, 0>(f, c13, 1.0);
+        fg_term_df<D, NS, 0, 0, 0>(f, c13, -R1_12);
+        fg_term_df<D, NS, 1, 1, 0>(f, C(14), 2.0);
+        fg_term_df<D, NS, 0, 1, 1>(f, C(15), 2.0);
+        fg_term_df<D, NS, 0, 0, 2>(f, c16, 1.0);
+        fg_term_df<D, NS, 0, 0, 0>(f, c16, -R1_12);
+        fg_term_df<D, NS, 1, 0, 1>(f, C(19), 1.0);
+    } else {
+        fg_term_df<D, NS, 0, 0, 0>(f, C(3), 1.0);
+        fg_term_df<D, NS, 0, 0, 1>(f, C(6), 2.0);
+        fg_term_df<D, NS, 0, 1, 0>(f, C(8), 1.0);
+        fg_term_df<D, NS, 1, 0, 0>(f, C(9), 1.0);
+        const df64 c12 = C(12), c15 = C(15), c17 = C(17);
+        fg_term_df<D, NS, 0, 0, 2>(f, c12, 3.0);
+        fg_term_df<D, NS, 0, 0, 0>(f, c12, -R3_20);
+        fg_term_df<D, NS, 0, 2, 0>(f, c15, 1.0);
+        fg_term_df<D, NS, 0, 0, 0>(f, c15, -R1_12);
+        fg_term_df<D, NS, 0, 1, 1>(f, C(16), 2.0);
+        fg_term_df<D, NS, 2, 0, 0>(f, c17, 1.0);
+        fg_term_df<D, NS, 0, 0, 0>(f, c17, -R1_12);
+        fg_term_df<D, NS, 1, 0, 1>(f, C(18), 2.0);
+        fg_term_df<D, NS, 1, 1, 0>(f, C(19), 1.0);
+    }
+    return f;
+}
+
+template <int GP>
+__device__ __forceinline__ df64 fg_eval_df(const FaceGradDf& f) {
+    constexpr double s1 = (GP & 2) ? GPT : -GPT, s2 = (GP & 1) ? GPT : -GPT;
+    return (f.p + f.q * dfc(s1)) + (f.r * dfc(s2) + f.s * dfc(s1 * s2));
+}
+
+// PDEViscFlux (Navier-Stokes-3D/pde.c:90-162) as visc_flux: Q the full state (r + deviation),
+// G its gradients; every flux term is a product with a gradient, so the flux has the size of
+// the deviations and F(r) = 0; returns vmax / rho
+template <int D>
+__device__ __forceinline__ df64 visc_flux_df(const df64* Q, const df64 (*G)[3], df64 gm1, df64 mu, df64 kc, df64 vmax,
+                                             df64* F) {
+    const df64 irho = df_div(dfc(1.0), Q[0]);
+    const df64 u = irho * Q[1], v = irho * Q[2], w = irho * Q[3];
+    const df64 m2 = (Q[1] * Q[1] + Q[2] * Q[2]) + Q[3] * Q[3];
+    const df64 em = Q[4] - m2 * irho;  // E - |m|^2 / rho
+    df64 vg[3][3], T[3];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+        const df64 rb = G[0][b] * irho;
+        vg[0][b] = G[1][b] - u * rb;
+        vg[1][b] = G[2][b] - v * rb;
+        vg[2][b] = G[3][b] - w * rb;
+        // the temperature gradient (times c_v) of pde.c:118-130, regrouped:
+        // (gamma - 1)/rho (E_b - u.m_b - rho_b/rho (E - |m|^2 / rho))
+        const df64 um = (u * G[1][b] + v * G[2][b]) + w * G[3][b];
+        T[b] = ((G[4][b] - um) - rb * em) * (gm1 * irho);
+    }
+    const df64 div_v = ((vg[0][0] + vg[1][1]) + vg[2][2]) * (mu * dfc(-2.0 / 3.0));
+    const df64 tdd = div_v + df_scale(mu * vg[D][D], 2.0f);
+    const df64 t0 = D == 0 ? tdd : mu * (vg[0][D] + vg[D][0]);
+    const df64 t1 = D == 1 ? tdd : mu * (vg[1][D] + vg[D][1]);
+    const df64 t2 = D == 2 ? tdd : mu * (vg[2][D] + vg[D][2]);
+    F[0] = df64{0.0f, 0.0f};
+    F[1] = -t0;
+    F[2] = -t1;
+    F[3] = -t2;
+    F[4] = -(((u * t0 + v * t1) + w * t2) + kc * T[D]);
+    return vmax * irho;
+}
+
 }  // namespace euler
 }  // namespace hype

@@ -277,7 +277,8 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
     achieved_gbs = bytes_stage * cells / t_stage / 1e9
     peak, peak_kind = _peaks()
     tag = {0: "fp64", 1: "fp32", 2: "df64"}[precision] + ("_linear" if recon else "") + ("_ns" if viscous else "")
-    prof_file = "ns3d_tgv_stage_fp64.txt" if viscous else f"euler_stage_{tag}.txt"
+    prof_file = ("ns3d_tgv_stage_fp64.txt" if precision == 0 else f"ns3d_tgv_stage_{tag}.txt") if viscous else \
+        f"euler_stage_{tag}.txt"
     traffic = _profile_figure(prof_file, "dram_bytes_per_cell_stage")
     flops_cell = _profile_figure(prof_file, "fp_flops_per_cell_stage")
     fpeak = C.c_double()
@@ -996,6 +997,7 @@ WORKLOADS = {
     "euler256_fp32_linear": lambda a, *r: run_euler(a, *r, precision=1, recon=1),
     "euler256_weno3": lambda a, *r: run_euler(a, *r, precision=0, recon=3),
     "ns256_tgv": lambda a, *r: run_euler(a, *r, precision=0, recon=1, viscous=True),
+    "ns256_tgv_df64": lambda a, *r: run_euler(a, *r, precision=2, recon=1, viscous=True),
     "euler64": lambda a, *r: run_euler(a, *r, precision=0, recon=0, n=64),
     "euler128": lambda a, *r: run_euler(a, *r, precision=0, recon=0, n=128),
     "euler128_fp32": lambda a, *r: run_euler(a, *r, precision=1, recon=0, n=128),

@@ -138,8 +138,8 @@ def test_df64_rejects_what_it_does_not_cover(hype):
 
     with pytest.raises(Exception):
         _solver(hype, 8, recon=L.RECON_WENO3)
-    with pytest.raises(Exception):
-        _solver(hype, 8, mu=0.01, prandtl=0.71, cv=1.0)
+    with pytest.raises(Exception):  # viscous: Rusanov only
+        _solver(hype, 8, mu=0.01, prandtl=0.71, cv=1.0, flux=L.FLUX_HLLC)
     s = _solver(hype, 8)
     with pytest.raises(Exception):
         s.set_recon(L.RECON_WENO3)
