@@ -70,6 +70,9 @@ class AppCtx:
     gamma: float = 1.4
     boundaries: tuple = (L.BC_PERIODIC,) * 6  # left,right,bottom,top,back,front
     recon: int = L.RECON_CWENO4
+    # PREC_FP64 (the reference's arithmetic), PREC_FP32 (reconstruction and flux in FP32), or
+    # PREC_DF64 (reconstruction and Rusanov / viscous fluxes in FP32 pairs on deviations from a
+    # reference state, state and stages in FP64: the FP64 form's error bars at about 4x its speed)
     precision: int = L.PREC_FP64
     dt_mode: int = L.DT_MONITOR
     flux: int = L.FLUX_RUSANOV
