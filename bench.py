@@ -698,8 +698,10 @@ def run_mp2d_learned(args, ws, rank, local, n=1024, ntrain=256, tau=1e-4, prob=0
     res = {}
     clocks, launches = None, 0
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    rho = {}
     for form, prec, recon in (("plain_fp32", Lc.PREC_FP32, Lc.RECON_CWENO4), ("learned_fp32", Lc.PREC_FP32, Lc.RECON_LEARNED),
-                              ("plain_fp64", Lc.PREC_FP64, Lc.RECON_CWENO4)):
+                              ("plain_fp64", Lc.PREC_FP64, Lc.RECON_CWENO4),
+                              ("learned_fp64", Lc.PREC_FP64, Lc.RECON_LEARNED)):
         m, _ = solver(n, prec, recon)
         if recon == Lc.RECON_LEARNED:
             m.set_mlp(params, prob)
@@ -719,7 +721,11 @@ def run_mp2d_learned(args, ws, rank, local, n=1024, ntrain=256, tau=1e-4, prob=0
                      "minmod_fallback_cells": m.fallback_cells}
         if form == "learned_fp32":
             clocks, launches = clk.summary(), H.launches() - l0
+        if form.endswith("fp64"):
+            q = m.get_state()
+            rho[form] = q[..., 0] + q[..., 1]  # alpha1 rho1 + alpha2 rho2
         m.close()
+    l1_64 = float(np.abs(rho["learned_fp64"] - rho["plain_fp64"]).mean() / np.abs(rho["plain_fp64"]).mean())
     v = res["learned_fp32"]["value"]
     peak, kind = _peaks()
     return {"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
@@ -733,6 +739,8 @@ def run_mp2d_learned(args, ws, rank, local, n=1024, ntrain=256, tau=1e-4, prob=0
                                      "recall": recall, "precision": precision, "flagged_train": flagged_train}},
             "forms": res, "speedup_vs_plain_fp32": v / res["plain_fp32"]["value"],
             "speedup_vs_plain_fp64": v / res["plain_fp64"]["value"],
+            "speedup_learned_fp64_vs_plain_fp64": res["learned_fp64"]["value"] / res["plain_fp64"]["value"],
+            "l1_rho_learned_fp64_vs_plain_fp64": l1_64,
             "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None, "traffic": None},
             "gpu_launches": launches, "clocks": clocks}
 
