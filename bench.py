@@ -994,6 +994,8 @@ WORKLOADS = {
     "kapila1024_learned": run_mp2d_learned,
     "acoustic256": run_acoustic,
     "acoustic256_df64": lambda a, *r: run_acoustic(a, *r, precision=2),
+    "acoustic128": lambda a, *r: run_acoustic(a, *r, n=128),
+    "acoustic128_df64": lambda a, *r: run_acoustic(a, *r, n=128, precision=2),
     "kapila1024_fp32": lambda a, *r: run_mp2d(a, *r, precision=1),
     "euler256_hllc": lambda a, *r: run_euler(a, *r, precision=0, recon=0, flux=1),
     "euler256": lambda a, *r: run_euler(a, *r, precision=0, recon=0),
