@@ -199,3 +199,26 @@ def test_df64_indicator_gate_matches_fp64_gate(hype, oracle):
     print(f"gate fp64 vs df64: flagged {flags[0][0]} / {flags[1][0]}, state difference {err:.2e}")
     # a flipped cell next to the blast takes R4 in one run and CWENO4 in the other (1.6e-6 seen)
     assert err <= (1e-12 if flags[0] == flags[1] else 1e-4)
+
+
+@pytest.mark.parametrize("shape,bc", [((3, 5, 4), (0, 0, 1, 1, 2, 2)), ((4, 3, 3), (1, 2, 0, 0, 0, 0))])
+def test_smallest_grids_both_forms(hype, oracle, shape, bc):
+    """the smallest grids the library takes (3 cells on an axis: the periodic ghost fill wraps
+    more than once, reflective and transmissive ghosts reach past the opposite wall's mirror)
+    in the FP64 and the double-float forms against the CPU checker"""
+    nx, ny, nz = shape
+    rng = np.random.default_rng(7 + nx)
+    U = np.zeros((nz, ny, nx, 5))
+    U[..., 0] = 1.0 + 0.1 * rng.random((nz, ny, nx))
+    U[..., 1:4] = 0.1 * rng.standard_normal((nz, ny, nx, 3))
+    U[..., 4] = (1 / 1.4 + 0.1 * rng.random((nz, ny, nx))) / 0.4 + 0.5 * (U[..., 1:4] ** 2).sum(-1) / U[..., 0]
+    cfg = oracle.euler_cfg(shape, 1.0 / nx, cfl=0.4, bc=bc)
+    Ro, smax, rc, _ = oracle.euler_rhs(cfg, U)
+    assert rc == 0
+    Uo, t, dt, rc = oracle.euler_run(cfg, U, 2)
+    for prec in (hype._lib.PREC_FP64, hype._lib.PREC_DF64):
+        s = _solver(hype, shape, bc, precision=prec)
+        assert rel(s.RHSFunction(0.0, U), Ro) <= TOL_STEP
+        s.set_state(U)
+        s.step(2)
+        assert rel(s.get_state(), Uo) <= TOL_STEP
