@@ -623,56 +623,62 @@ __device__ __forceinline__ void mc_tangents(R nx, R ny, R nz, bool fixed, R* t1,
 // frame and rotated back with the inverse frame matrix
 template <typename R>
 __device__ __forceinline__ R hllc(const R* QL, const R* QR, R nx, R ny, R nz, R gamma, R gm1, R* Flux, bool& bad) {
-    R FL[NV], FR[NV];
-    const R sl = cons_flux_n<R>(QL, nx, ny, nz, gamma, gm1, FL, bad);
-    const R sr = cons_flux_n<R>(QR, nx, ny, nz, gamma, gm1, FR, bad);
     R t1[3], t2[3];
     mc_tangents<R>(nx, ny, nz, false, t1, t2);
-    // inverse of the frame matrix [n; t1; t2] by cofactors (pde.c:189-205)
+    // inverse of the frame matrix [n; t1; t2] by cofactors (pde.c:189-205; constant for an axis normal)
     const R M00 = nx, M01 = ny, M02 = nz, M10 = t1[0], M11 = t1[1], M12 = t1[2], M20 = t2[0], M21 = t2[1], M22 = t2[2];
     const R idet = R(1) / (M00 * (M11 * M22 - M12 * M21) - M01 * (M10 * M22 - M12 * M20) + M02 * (M10 * M21 - M11 * M20));
     const R i00 = (M11 * M22 - M12 * M21) * idet, i01 = -(M01 * M22 - M02 * M21) * idet, i02 = (M01 * M12 - M02 * M11) * idet;
     const R i10 = -(M10 * M22 - M12 * M20) * idet, i11 = (M00 * M22 - M02 * M20) * idet, i12 = -(M00 * M12 - M02 * M10) * idet;
     const R i20 = (M10 * M21 - M11 * M20) * idet, i21 = -(M00 * M21 - M01 * M20) * idet, i22 = (M00 * M11 - M01 * M10) * idet;
-    R S[2], un[2], ut1[2], ut2[2], rho[2], P[2], E[2], c[2];
+    // per side, once: 1/rho, the velocity, the pressure (PDEConsFlux, pde.c:40-88), the physical
+    // flux, the frame velocities and the sound speed (the divisions of pde.c:207-322 become
+    // products with a few reciprocals)
+    R F[2][NV], un[2], ut1[2], ut2[2], P[2], c[2], ir[2];
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
         const R* Q = side ? QR : QL;
-        const R ir = R(1) / Q[0];
-        const R u = ir * Q[1], v = ir * Q[2], w = ir * Q[3];
-        rho[side] = Q[0];
-        P[side] = gm1 * (Q[4] - R(0.5) * ir * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]));
-        E[side] = Q[4];
-        un[side] = u * nx + v * ny + w * nz;
+        ir[side] = recip(Q[0]);
+        const R u = ir[side] * Q[1], v = ir[side] * Q[2], w = ir[side] * Q[3];
+        const R p = gm1 * (Q[4] - R(0.5) * Q[0] * (u * u + v * v + w * w));
+        bad |= (Q[0] < R(1.0e-14)) || (p < R(1.0e-12)) || !(Q[0] == Q[0]);
+        P[side] = p;
+        un[side] = nx * u + ny * v + nz * w;
         ut1[side] = u * t1[0] + v * t1[1] + w * t1[2];
         ut2[side] = u * t2[0] + v * t2[1] + w * t2[2];
-        c[side] = sqrt(gamma * P[side] / rho[side]);
+        const R mun = Q[0] * un[side];
+        F[side][0] = mun;
+        F[side][1] = mun * u + nx * p;
+        F[side][2] = mun * v + ny * p;
+        F[side][3] = mun * w + nz * p;
+        F[side][4] = (Q[4] + p) * un[side];
+        c[side] = sqrt(ir[side] * gamma * p);
     }
     const R SL = fmin(un[1] - c[1], un[0] - c[0]);
     const R SR = fmax(un[0] + c[0], un[1] + c[1]);
-    S[0] = SL;
-    S[1] = SR;
-    const R Ss = (P[1] - P[0] + rho[0] * un[0] * (SL - un[0]) - rho[1] * un[1] * (SR - un[1])) /
-                 (rho[0] * (SL - un[0]) - rho[1] * (SR - un[1]));
+    const R S[2] = {SL, SR};
+    const R Ss = (P[1] - P[0] + QL[0] * un[0] * (SL - un[0]) - QR[0] * un[1] * (SR - un[1])) *
+                 recip(QL[0] * (SL - un[0]) - QR[0] * (SR - un[1]));
     R Fs[2][NV];
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
         const R* Q = side ? QR : QL;
-        const R* Fo = side ? FR : FL;
         const R d = S[side] - un[side];
-        const R q0 = rho[side] * d / (S[side] - Ss);
+        const R rd = Q[0] * d;
+        const R q0 = rd * recip(S[side] - Ss);
         R Qs[NV];
         Qs[0] = q0;
         Qs[1] = q0 * (Ss * i00 + ut1[side] * i01 + ut2[side] * i02);
         Qs[2] = q0 * (Ss * i10 + ut1[side] * i11 + ut2[side] * i12);
         Qs[3] = q0 * (Ss * i20 + ut1[side] * i21 + ut2[side] * i22);
-        Qs[4] = q0 * ((E[side] / rho[side]) + (Ss - un[side]) * (Ss + P[side] / (rho[side] * d)));
+        Qs[4] = q0 * (Q[4] * ir[side] + (Ss - un[side]) * (Ss + P[side] * recip(rd)));
 #pragma unroll
-        for (int k = 0; k < NV; ++k) Fs[side][k] = Fo[k] + S[side] * (Qs[k] - Q[k]);
+        for (int k = 0; k < NV; ++k) Fs[side][k] = F[side][k] + S[side] * (Qs[k] - Q[k]);
     }
 #pragma unroll
     for (int k = 0; k < NV; ++k)
-        Flux[k] = (SL > R(0)) ? FL[k] : (Ss >= R(0)) ? Fs[0][k] : (SR >= R(0)) ? Fs[1][k] : FR[k];
+        Flux[k] = (SL > R(0)) ? F[0][k] : (Ss >= R(0)) ? Fs[0][k] : (SR >= R(0)) ? Fs[1][k] : F[1][k];
+    const R sl = fabs(un[0]) + c[0], sr = fabs(un[1]) + c[1];
     return sl < sr ? sr : sl;
 }
 
