@@ -86,7 +86,7 @@ __device__ __forceinline__ void cons2prim(const Eos& e, const double* Q, double*
 // P_inf, total energy, sound speed.  Computed once per trace instead of once per HLLC
 // evaluation (the rotated solver makes three).
 struct Side {
-    double rho, u, v, w, p, phi, E, a;
+    double rho, u, v, w, p, phi, E, a, irho;
 };
 
 __device__ __forceinline__ Side make_side(const Eos& e, const double* V, bool& bad) {
@@ -96,7 +96,8 @@ __device__ __forceinline__ Side make_side(const Eos& e, const double* V, bool& b
     const double P_inf = mix_pinf(e, g, s.phi);
     s.E = 0.5 * s.rho * (s.u * s.u + s.v * s.v + s.w * s.w) + (s.p + g * P_inf) / (g - 1.0);
     if (s.rho < RHO_FLOOR || (s.p + P_inf) < PRS_FLOOR) bad = true;
-    s.a = sqrt(g * (s.p + P_inf) / s.rho);
+    s.irho = euler::recip(s.rho);
+    s.a = sqrt(g * (s.p + P_inf) * s.irho);
     return s;
 }
 
@@ -110,8 +111,8 @@ __device__ __forceinline__ double hllc7(const Side& L, const Side& R, double nx,
     const double un_L = L.u * nx + L.v * ny + L.w * nz, un_R = R.u * nx + R.v * ny + R.w * nz;
     const double S_L = fmin(un_R - R.a, un_L - L.a);
     const double S_R = fmax(un_L + L.a, un_R + R.a);
-    const double S_star = (R.p - L.p + L.rho * un_L * (S_L - un_L) - R.rho * un_R * (S_R - un_R)) /
-                          (L.rho * (S_L - un_L) - R.rho * (S_R - un_R));
+    const double S_star = (R.p - L.p + L.rho * un_L * (S_L - un_L) - R.rho * un_R * (S_R - un_R)) *
+                          euler::recip(L.rho * (S_L - un_L) - R.rho * (S_R - un_R));
     // the reference's branch order (pde.c:368-376); with S_L == 0 and S_star >= 0 it leaves
     // the flux unset, here zero
     const int sel = (S_L > 0.0) ? 0 : (S_star >= 0.0 && S_L < 0.0) ? 1 : (S_star < 0.0 && S_R >= 0.0) ? 2
@@ -137,26 +138,26 @@ __device__ __forceinline__ double hllc7(const Side& L, const Side& R, double nx,
         // the frame of pde.c:290-312 and the first column of its inverse
         double t1x, t1y, t1z, t2x, t2y, t2z;
         if (fabs(ny + nz) > fabs(ny - nz)) {
-            const double il = 1.0 / sqrt(2.0 * (1.0 + nz * (ny - nx) + nx * ny));
+            const double il = rsqrt(2.0 * (1.0 + nz * (ny - nx) + nx * ny));
             t1x = (ny + nz) * il; t1y = (nz - nx) * il; t1z = -(nx + ny) * il;
             t2x = (nx * (nz - ny) - ny * ny - nz * nz) * il;
             t2y = (ny * (nx + nz) + nx * nx + nz * nz) * il;
             t2z = (nz * (nx - nz) - nx * nx - ny * ny) * il;
         } else {
-            const double il = 1.0 / sqrt(2.0 * (1.0 - nx * ny - nx * nz - ny * nz));
+            const double il = rsqrt(2.0 * (1.0 - nx * ny - nx * nz - ny * nz));
             t1x = (ny - nz) * il; t1y = (nz - nx) * il; t1z = (nx - ny) * il;
             t2x = (nx * (ny + nz) - ny * ny - nz * nz) * il;
             t2y = (ny * (nx + nz) - nx * nx - nz * nz) * il;
             t2z = (nz * (nx + ny) - nx * nx - ny * ny) * il;
         }
         const double cx = t1y * t2z - t1z * t2y, cy = t1z * t2x - t1x * t2z, cz = t1x * t2y - t1y * t2x;
-        const double idet = 1.0 / (nx * cx + ny * cy + nz * cz);
+        const double idet = euler::recip(nx * cx + ny * cy + nz * cz);
         const double S = left ? S_L : S_R;
-        const double isd = 1.0 / (S - S_star);
+        const double isd = euler::recip(S - S_star);
         const double q0 = K.rho * (S - un) * isd;
         const double dn = (S_star - un) * idet;
         const double Qs[MV] = {q0, q0 * (K.u + dn * cx), q0 * (K.v + dn * cy), q0 * (K.w + dn * cz),
-                               q0 * ((K.E / K.rho) + (S_star - un) * (S_star + K.p / (K.rho * (S - un)))),
+                               q0 * ((K.E * K.irho) + (S_star - un) * (S_star + K.p * K.irho * euler::recip(S - un))),
                                K.phi * (S - un) * isd};
         const double Q[MV] = {K.rho, K.rho * K.u, K.rho * K.v, K.rho * K.w, K.E, K.phi};
 #pragma unroll
@@ -172,12 +173,12 @@ __device__ __forceinline__ double hllc7(const Side& L, const Side& R, double nx,
 // its two Miller-Colella tangents, weighted by their projections on the face normal
 __device__ __forceinline__ double rot_hllc7(const Side& L, const Side& R, double nx, double ny, double nz, double* Flux) {
     const double du = R.u - L.u, dv = R.v - L.v, dw = R.w - L.w;
-    const double dq = sqrt(du * du + dv * dv + dw * dw);
+    const double dq2 = du * du + dv * dv + dw * dw;
     double n1x, n1y, n1z;
-    if (dq < 1.0E-10) {
+    if (dq2 < 1.0E-20) {  // |du| < 1e-10 (pde.c:391)
         n1x = nx; n1y = ny; n1z = nz;
     } else {
-        const double idq = 1.0 / dq;
+        const double idq = rsqrt(dq2);
         n1x = du * idq; n1y = dv * idq; n1z = dw * idq;
     }
     double a1 = n1x * nx + n1y * ny + n1z * nz;
@@ -186,13 +187,13 @@ __device__ __forceinline__ double rot_hllc7(const Side& L, const Side& R, double
     }
     double t1x, t1y, t1z, t2x, t2y, t2z;
     if (fabs(n1y + n1z) > fabs(n1y - n1z)) {
-        const double il = 1.0 / sqrt(2.0 * (1.0 + n1z * (n1y - n1x) + n1x * n1y));
+        const double il = rsqrt(2.0 * (1.0 + n1z * (n1y - n1x) + n1x * n1y));
         t1x = (n1y + n1z) * il; t1y = (n1z - n1x) * il; t1z = -(n1x + n1y) * il;
         t2x = (n1x * (n1z - n1y) - n1y * n1y - n1z * n1z) * il;
         t2y = (n1y * (n1x + n1z) + n1x * n1x + n1z * n1z) * il;
         t2z = (n1z * (n1x - n1y) - n1x * n1x - n1y * n1y) * il;
     } else {
-        const double il = 1.0 / sqrt(2.0 * (1.0 - n1x * n1y - n1x * n1z - n1y * n1z));
+        const double il = rsqrt(2.0 * (1.0 - n1x * n1y - n1x * n1z - n1y * n1z));
         t1x = (n1y - n1z) * il; t1y = (n1z - n1x) * il; t1z = (n1x - n1y) * il;
         t2x = (n1x * (n1y + n1z) - n1y * n1y - n1z * n1z) * il;
         t2y = (n1y * (n1x + n1z) - n1x * n1x - n1z * n1z) * il;
