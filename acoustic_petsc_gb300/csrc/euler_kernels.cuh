@@ -582,36 +582,19 @@ __device__ __forceinline__ double visc_flux(const double* Q, const double (*G)[3
 }
 
 // ---------------------------------------------------------------- HLLC family
-// PDEConsFlux with a general unit normal (Navier-Stokes-3D/pde.c:40-88)
-template <typename R>
-__device__ __forceinline__ R cons_flux_n(const R* Q, R nx, R ny, R nz, R gamma, R gm1, R* F, bool& bad) {
-    const R rho = Q[0];
-    const R ir = R(1) / rho;
-    const R u = ir * Q[1], v = ir * Q[2], w = ir * Q[3];
-    const R E = Q[4];
-    const R p = gm1 * (E - R(0.5) * rho * (u * u + v * v + w * w));
-    bad |= (rho < R(1.0e-14)) || (p < R(1.0e-12)) || !(rho == rho);
-    const R un = nx * u + ny * v + nz * w;
-    const R mun = rho * un;
-    F[0] = mun;
-    F[1] = mun * u + nx * p;
-    F[2] = mun * v + ny * p;
-    F[3] = mun * w + nz * p;
-    F[4] = (E + p) * un;
-    return fabs(un) + sqrt(ir * gamma * p);
-}
-
-// Miller-Colella tangents (pde.c:236-251; 'fixed' = the corrected t2z of pde.c:348)
-template <typename R>
+// Miller-Colella tangents (pde.c:236-251; 'fixed' = the corrected t2z of pde.c:348).  RT: the
+// normal is data (rsqrt); otherwise a compile-time axis, for which 1/sqrt folds to a constant.
+template <typename R, bool RT = false>
 __device__ __forceinline__ void mc_tangents(R nx, R ny, R nz, bool fixed, R* t1, R* t2) {
+    auto inv_sqrt = [](R x) { return RT ? rsqrt(x) : R(1) / sqrt(x); };
     if (fabs(ny + nz) > fabs(ny - nz)) {
-        const R iL = R(1) / sqrt(R(2) * (R(1) + nz * (ny - nx) + nx * ny));
+        const R iL = inv_sqrt(R(2) * (R(1) + nz * (ny - nx) + nx * ny));
         t1[0] = (ny + nz) * iL; t1[1] = (nz - nx) * iL; t1[2] = -(nx + ny) * iL;
         t2[0] = (nx * (nz - ny) - ny * ny - nz * nz) * iL;
         t2[1] = (ny * (nx + nz) + nx * nx + nz * nz) * iL;
         t2[2] = (fixed ? (nz * (nx - ny) - nx * nx - ny * ny) : (nz * (nx - nz) - nx * nx - ny * ny)) * iL;
     } else {
-        const R iL = R(1) / sqrt(R(2) * (R(1) - nx * ny - nx * nz - ny * nz));
+        const R iL = inv_sqrt(R(2) * (R(1) - nx * ny - nx * nz - ny * nz));
         t1[0] = (ny - nz) * iL; t1[1] = (nz - nx) * iL; t1[2] = (nx - ny) * iL;
         t2[0] = (nx * (ny + nz) - ny * ny - nz * nz) * iL;
         t2[1] = (ny * (nx + nz) - nx * nx - nz * nz) * iL;
@@ -621,6 +604,82 @@ __device__ __forceinline__ void mc_tangents(R nx, R ny, R nz, bool fixed, R* t1,
 
 // PDEHLLCRiemannSolver (pde.c:207-322): star states built in the (n, t1, t2)
 // frame and rotated back with the inverse frame matrix
+// One side of a face for the HLLC family: what PDEConsFlux derives from the conserved
+// trace that does not depend on the normal -- 1/rho, velocity, pressure, sound speed --
+// formed once per trace (the rotated solver makes three HLLC evaluations)
+template <typename R>
+struct HSide {
+    R rho, u, v, w, p, E, ir, c;
+};
+
+template <typename R>
+__device__ __forceinline__ HSide<R> hllc_side(const R* Q, R gamma, R gm1, bool& bad) {
+    HSide<R> s;
+    s.rho = Q[0];
+    s.ir = recip(Q[0]);
+    s.u = s.ir * Q[1]; s.v = s.ir * Q[2]; s.w = s.ir * Q[3];
+    s.E = Q[4];
+    s.p = gm1 * (Q[4] - R(0.5) * Q[0] * (s.u * s.u + s.v * s.v + s.w * s.w));
+    bad |= (Q[0] < R(1.0e-14)) || (s.p < R(1.0e-12)) || !(Q[0] == Q[0]);
+    s.c = sqrt(s.ir * gamma * s.p);
+    return s;
+}
+
+// PDEHLLCRiemannSolver (pde.c:207-322) for the unit normal n from the two sides: star states
+// built in the (n, t1, t2) frame and rotated back with the inverse frame matrix
+template <typename R, bool RT = false>
+__device__ __forceinline__ R hllc_sides(const HSide<R>* side, const R* QL, const R* QR, R nx, R ny, R nz, R* Flux) {
+    R t1[3], t2[3];
+    mc_tangents<R, RT>(nx, ny, nz, false, t1, t2);
+    // inverse of the frame matrix [n; t1; t2] by cofactors (pde.c:189-205; constant for an axis normal)
+    const R M00 = nx, M01 = ny, M02 = nz, M10 = t1[0], M11 = t1[1], M12 = t1[2], M20 = t2[0], M21 = t2[1], M22 = t2[2];
+    const R idet = recip(M00 * (M11 * M22 - M12 * M21) - M01 * (M10 * M22 - M12 * M20) + M02 * (M10 * M21 - M11 * M20));
+    const R i00 = (M11 * M22 - M12 * M21) * idet, i01 = -(M01 * M22 - M02 * M21) * idet, i02 = (M01 * M12 - M02 * M11) * idet;
+    const R i10 = -(M10 * M22 - M12 * M20) * idet, i11 = (M00 * M22 - M02 * M20) * idet, i12 = -(M00 * M12 - M02 * M10) * idet;
+    const R i20 = (M10 * M21 - M11 * M20) * idet, i21 = -(M00 * M21 - M01 * M20) * idet, i22 = (M00 * M11 - M01 * M10) * idet;
+    R F[2][NV], un[2], ut1[2], ut2[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const HSide<R>& s = side[k];
+        un[k] = nx * s.u + ny * s.v + nz * s.w;
+        ut1[k] = s.u * t1[0] + s.v * t1[1] + s.w * t1[2];
+        ut2[k] = s.u * t2[0] + s.v * t2[1] + s.w * t2[2];
+        const R mun = s.rho * un[k];
+        F[k][0] = mun;
+        F[k][1] = mun * s.u + nx * s.p;
+        F[k][2] = mun * s.v + ny * s.p;
+        F[k][3] = mun * s.w + nz * s.p;
+        F[k][4] = (s.E + s.p) * un[k];
+    }
+    const R SL = fmin(un[1] - side[1].c, un[0] - side[0].c);
+    const R SR = fmax(un[0] + side[0].c, un[1] + side[1].c);
+    const R S[2] = {SL, SR};
+    const R Ss = (side[1].p - side[0].p + side[0].rho * un[0] * (SL - un[0]) - side[1].rho * un[1] * (SR - un[1])) *
+                 recip(side[0].rho * (SL - un[0]) - side[1].rho * (SR - un[1]));
+    R Fs[2][NV];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const R* Q = k ? QR : QL;
+        const HSide<R>& s = side[k];
+        const R d = S[k] - un[k];
+        const R rd = s.rho * d;
+        const R q0 = rd * recip(S[k] - Ss);
+        R Qs[NV];
+        Qs[0] = q0;
+        Qs[1] = q0 * (Ss * i00 + ut1[k] * i01 + ut2[k] * i02);
+        Qs[2] = q0 * (Ss * i10 + ut1[k] * i11 + ut2[k] * i12);
+        Qs[3] = q0 * (Ss * i20 + ut1[k] * i21 + ut2[k] * i22);
+        Qs[4] = q0 * (s.E * s.ir + (Ss - un[k]) * (Ss + s.p * recip(rd)));
+#pragma unroll
+        for (int c = 0; c < NV; ++c) Fs[k][c] = F[k][c] + S[k] * (Qs[c] - Q[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < NV; ++c)
+        Flux[c] = (SL > R(0)) ? F[0][c] : (Ss >= R(0)) ? Fs[0][c] : (SR >= R(0)) ? Fs[1][c] : F[1][c];
+    const R sl = fabs(un[0]) + side[0].c, sr = fabs(un[1]) + side[1].c;
+    return sl < sr ? sr : sl;
+}
+
 template <typename R>
 __device__ __forceinline__ R hllc(const R* QL, const R* QR, R nx, R ny, R nz, R gamma, R gm1, R* Flux, bool& bad) {
     R t1[3], t2[3];
@@ -686,16 +745,14 @@ __device__ __forceinline__ R hllc(const R* QL, const R* QR, R nx, R ny, R nz, R 
 // direction n1 and its two tangents, weighted by their projections on n
 template <typename R>
 __device__ __forceinline__ R rot_hllc(const R* QL, const R* QR, R nx, R ny, R nz, R gamma, R gm1, R* Flux, bool& bad) {
-    R irho = R(1) / QL[0];
-    const R uL = irho * QL[1], vL = irho * QL[2], wL = irho * QL[3];
-    irho = R(1) / QR[0];
-    const R du = irho * QR[1] - uL, dv = irho * QR[2] - vL, dw = irho * QR[3] - wL;
-    const R dq = sqrt(du * du + dv * dv + dw * dw);
+    const HSide<R> side[2] = {hllc_side<R>(QL, gamma, gm1, bad), hllc_side<R>(QR, gamma, gm1, bad)};
+    const R du = side[1].u - side[0].u, dv = side[1].v - side[0].v, dw = side[1].w - side[0].w;
+    const R dq2 = du * du + dv * dv + dw * dw;
     R n1[3];
-    if (dq < R(1.0E-10)) {
+    if (dq2 < R(1.0E-20)) {  // |du| < 1e-10
         n1[0] = nx; n1[1] = ny; n1[2] = nz;
     } else {
-        const R idq = R(1) / dq;
+        const R idq = rsqrt(dq2);
         n1[0] = du * idq; n1[1] = dv * idq; n1[2] = dw * idq;
     }
     R a1 = n1[0] * nx + n1[1] * ny + n1[2] * nz;
@@ -704,7 +761,7 @@ __device__ __forceinline__ R rot_hllc(const R* QL, const R* QR, R nx, R ny, R nz
         a1 = -a1;
     }
     R t1[3], t2[3];
-    mc_tangents<R>(n1[0], n1[1], n1[2], true, t1, t2);
+    mc_tangents<R, true>(n1[0], n1[1], n1[2], true, t1, t2);
     R a2 = t1[0] * nx + t1[1] * ny + t1[2] * nz;
     if (a2 < R(0)) {
         t1[0] = -t1[0]; t1[1] = -t1[1]; t1[2] = -t1[2];
@@ -716,9 +773,9 @@ __device__ __forceinline__ R rot_hllc(const R* QL, const R* QR, R nx, R ny, R nz
         a3 = -a3;
     }
     R F1[NV], F2[NV], F3[NV];
-    const R s1 = hllc<R>(QL, QR, n1[0], n1[1], n1[2], gamma, gm1, F1, bad);
-    const R s2 = hllc<R>(QL, QR, t1[0], t1[1], t1[2], gamma, gm1, F2, bad);
-    const R s3 = hllc<R>(QL, QR, t2[0], t2[1], t2[2], gamma, gm1, F3, bad);
+    const R s1 = hllc_sides<R, true>(side, QL, QR, n1[0], n1[1], n1[2], F1);
+    const R s2 = hllc_sides<R, true>(side, QL, QR, t1[0], t1[1], t1[2], F2);
+    const R s3 = hllc_sides<R, true>(side, QL, QR, t2[0], t2[1], t2[2], F3);
 #pragma unroll
     for (int k = 0; k < NV; ++k) Flux[k] = a1 * F1[k] + a2 * F2[k] + a3 * F3[k];
     return fmax(s1, fmax(s2, s3));

@@ -998,6 +998,7 @@ WORKLOADS = {
     "acoustic128_df64": lambda a, *r: run_acoustic(a, *r, n=128, precision=2),
     "kapila1024_fp32": lambda a, *r: run_mp2d(a, *r, precision=1),
     "euler256_hllc": lambda a, *r: run_euler(a, *r, precision=0, recon=0, flux=1),
+    "euler256_rothllc": lambda a, *r: run_euler(a, *r, precision=0, recon=0, flux=2),
     "euler256": lambda a, *r: run_euler(a, *r, precision=0, recon=0),
     "euler256_fp32": lambda a, *r: run_euler(a, *r, precision=1, recon=0),
     "euler256_df64": lambda a, *r: run_euler(a, *r, precision=2, recon=0),
