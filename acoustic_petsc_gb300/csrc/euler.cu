@@ -1237,6 +1237,11 @@ struct hype_euler {
     unsigned long long* mlp_cnt = nullptr;
     // per-kernel event timing inside a timed region (hype_euler_profile)
     bool prof = false;
+    // the steady-state step (every step after the first of a call) captured as a CUDA graph,
+    // with the launch choices it was captured under and the kernels it launches
+    cudaGraphExec_t step_graph = nullptr;
+    long long graph_key[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    long long graph_launches = 0;
     std::vector<cudaEvent_t> ev;  // pairs (start, end)
     std::vector<int> ev_kind;     // 0 recon, 1 faces (3 directions), 2 update
     size_t ev_used = 0;
@@ -1474,6 +1479,7 @@ extern "C" void hype_euler_destroy(hype_euler* e) {
     cudaFree(e->mlp); cudaFree(e->mlp_cnt); cudaFree(e->C4); cudaFree(e->mon);
     if (e->hs) cudaFreeHost(e->hs);
     for (auto x : e->ev) cudaEventDestroy(x);
+    if (e->step_graph) cudaGraphExecDestroy(e->step_graph);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
 }
@@ -1564,6 +1570,67 @@ extern "C" int hype_euler_sync(hype_euler* e) {
     return HYPE_OK;
 }
 
+// One SSPRK(4,3) step after the first of a call: dt from the previous step (MONITOR) or as
+// set, then the four stages (the device scalars carry everything that changes between steps)
+static int launch_steady_step(hype_euler* e, int mode, double cfl_h) {
+    const Stage s12{0.0, 1.0, 0.5, 0};
+    const Stage s3{2.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 0};
+    int rc;
+    k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 3, mode == HYPE_DT_MONITOR, 1, cfl_h, e->p.recon, 1.0 / e->p.h,
+                                         e->C4 != nullptr);
+    HYPE_LAUNCHED(1);
+    if ((rc = launch_rhs(e, e->U, 0))) return rc;
+    if ((rc = launch_update(e, e->U, e->U, e->W, s12))) return rc;
+    if ((rc = launch_rhs(e, e->W, 1))) return rc;
+    if ((rc = launch_update(e, e->U, e->W, e->W, s12))) return rc;
+    if ((rc = launch_rhs(e, e->W, 2))) return rc;
+    if ((rc = launch_update(e, e->U, e->W, e->W, s3))) return rc;
+    if ((rc = launch_rhs(e, e->W, 3))) return rc;
+    return launch_update(e, e->U, e->W, e->U, s12);
+}
+
+// The steady-state step as a CUDA graph (replayed instead of ~25 launches per step; what
+// matters on small grids), recaptured when a launch choice changes; falls back to launching
+// (returns false) while profiling or if the capture fails.
+static bool steady_step_graph(hype_euler* e, int mode, double cfl_h) {
+    if (e->prof) return false;
+    long long lt;
+    memcpy(&lt, &e->logit_thr, sizeof(float));
+    const long long key[8] = {mode, e->p.recon, e->p.flux, e->p.precision, e->p.positivity, (long long)(size_t)e->mlp,
+                              lt, (long long)(cfl_h * 1e15)};
+    if (e->step_graph && memcmp(key, e->graph_key, sizeof(key)) == 0) return true;
+    if (e->step_graph) {
+        cudaGraphExecDestroy(e->step_graph);
+        e->step_graph = nullptr;
+    }
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    const long long l0 = hype_launch_count();
+    const int rc = launch_steady_step(e, mode, cfl_h);
+    const cudaError_t ce = cudaStreamEndCapture(e->stream, &graph);
+    const long long nl = hype_launch_count() - l0;
+    count_launch(-nl);  // captured, not launched
+    if (rc != HYPE_OK || ce != cudaSuccess || !graph) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return false;
+    }
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    e->step_graph = exec;
+    memcpy(e->graph_key, key, sizeof(key));
+    e->graph_launches = nl;
+    return true;
+}
+
 extern "C" int hype_euler_step(hype_euler* e, int nsteps, double* t_inout, double* dt_inout, hype_status* st) {
     if (!e || nsteps < 0 || !t_inout || !dt_inout) return HYPE_ERR_ARG;
     const int mode = e->p.dt_mode;
@@ -1583,6 +1650,13 @@ extern "C" int hype_euler_step(hype_euler* e, int nsteps, double* t_inout, doubl
     const Stage s12{0.0, 1.0, 0.5, 0};
     const Stage s3{2.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 0};
     for (int s = 0; s < nsteps; ++s) {
+        if (s == 1 && nsteps > 2 && steady_step_graph(e, mode, cfl_h)) {
+            for (; s < nsteps; ++s) {
+                HYPE_CK(cudaGraphLaunch(e->step_graph, e->stream));
+                count_launch(e->graph_launches);
+            }
+            break;
+        }
         if (s == 0 && first_from_rhs) {
             // the initial RHS call of hype.c:175 is this step's first stage RHS
             if ((rc = launch_rhs(e, e->U, 0))) return rc;

@@ -301,3 +301,29 @@ def test_restart_file_resumes_bit_for_bit(hype, tmp_path):
     assert lines[4] == f"DIMENSIONS {n} {n} {n}" and lines[8] == "SCALARS density double 1"
     rho = np.array([float(t) for t in lines[10:10 + n**3]])
     assert np.array_equal(rho, a.get_state()[..., 0].ravel())
+
+
+@pytest.mark.parametrize("precision,flux", [(0, 0), (2, 0), (0, 1)])
+def test_graph_replayed_steps_equal_launched_steps(hype, precision, flux):
+    """Steps after the first of a call replay a captured CUDA graph; with per-kernel profiling
+    on they are launched one by one.  Same kernels, same arguments: bit-identical states, times
+    and next dt, and the replayed kernels are counted as launches."""
+    from acoustic_petsc_gb300 import _lib as L
+
+    n = 20
+    U0 = _pulse(n, amp=0.2)
+    out = []
+    for prof in (0, 1):
+        s = solver(hype, n, precision=precision, flux=flux)
+        s.set_state(U0)
+        L.lib().hype_euler_profile(s._h, prof)
+        l0 = L.launches()
+        s.step(7)
+        out.append((s.get_state(), s.t, s.next_dt, L.launches() - l0))
+        s.step(3)  # a second call reuses the captured graph
+        out.append((s.get_state(), s.t, s.next_dt, None))
+        s.close()
+    (Ug, tg, dg, lg), (Ug2, tg2, dg2, _), (Ue, te, de, le), (Ue2, te2, de2, _) = out
+    assert np.array_equal(Ug, Ue) and tg == te and dg == de
+    assert np.array_equal(Ug2, Ue2) and tg2 == te2 and dg2 == de2
+    assert lg == le > 0
