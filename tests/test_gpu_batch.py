@@ -47,3 +47,20 @@ def test_graph_and_tiles_do_not_change_results(hype):
     for r in res[1:]:
         for x, y in zip(res[0], r):
             assert np.array_equal(x, y)
+
+
+def test_full_batch_workload_vs_oracle(hype, oracle):
+    """the batched-acoustics workload at its full size: 256 instances with sides drawn
+    log-uniformly in [64, 1024] (seed 7), one persistent launch per step, the step graph-captured;
+    every instance after 150 steps against the checker's run of that instance alone."""
+    inst = _instances(256, seed=7, nmin=64, nmax=1024)
+    b = hype.BatchLeapfrog([hype.Monopole(**m) for m in inst])
+    b.step(150)
+    worst = 0.0
+    for q, m in enumerate(inst):
+        a, p = b.get(q)
+        ao, po = _oracle_run(oracle, m, 150)
+        worst = max(worst, np.abs(p - po).max() / np.abs(po).max(), np.abs(a - ao).max() / np.abs(ao).max())
+    b.close()
+    print(f"256 instances, 150 steps: worst relative L-inf {worst:.2e}")
+    assert worst <= TOL
