@@ -154,3 +154,22 @@ def test_multiphase_restart_round_trip(hype, tmp_path):
     m.write_vtk(tmp_path / "sol.vtk")
     assert (tmp_path / "sol.vtk").read_text().splitlines()[4] == "DIMENSIONS 40 40 1"
     assert L.MP_KAPILA5 == 1
+
+
+def test_kapila_full_workload_vs_oracle(hype, oracle):
+    """the Kapila workload at its full size (1024^2 cells, 1e8 Pa step driving the air bubble):
+    RHS and two SSPRK(4,3) steps bit-identical to the multi-threaded checker (the FP64 form keeps
+    the checker's operation order and is compiled without contractions)"""
+    m, cfg, U = _kapila(hype, oracle, 1024, 1)
+    R = m.RHSFunction(0.0, U)
+    Ro, smax, rc, fb = oracle.mp2d_rhs(cfg, U)
+    assert rc == 0
+    e_rhs = rel(R, Ro)
+    m.set_state(U)
+    m.step(2)
+    Uo, t, dt, rc = oracle.mp2d_run(cfg, U, 2, stepper=0)
+    assert rc == 0
+    e_run = rel(m.get_state(), Uo)
+    print(f"Kapila 1024^2: RHS {e_rhs:.2e}, two steps {e_run:.2e}")
+    assert np.array_equal(R, Ro) and np.array_equal(m.get_state(), Uo)
+    assert m.t == t
