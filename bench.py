@@ -256,13 +256,9 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
     launches = H.launches() - l0
     ms = e0.elapsed_time(e1)
     ms_max = _max_over_ranks(ws, ms)
-    # the double-float form beside the FP64 one (same state, same steps), for the default workload
-    alt = None
-    if precision == 0 and recon == 0 and flux == 0 and not viscous and not args.no_alt_forms:
-        U_fp64 = s.get_state()
-        alt = _euler_df64_beside(args, ws, n, U0, U_fp64, stream_of=lambda h: torch.cuda.ExternalStream(
-            L.hype_euler_stream(h)))
-        del U_fp64
+    # the state after the timed steps, for the double-float form beside this one (default workload)
+    with_alt = precision == 0 and recon == 0 and flux == 0 and not viscous and not args.no_alt_forms
+    U_fp64 = s.get_state() if with_alt else None
     prof_ms = (C.c_double * 3)()
     prof_n = (C.c_longlong * 3)()
     H._lib.check(L.hype_euler_profile_read(s._h, prof_ms, prof_n), "profile_read")
@@ -326,6 +322,12 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
         e2e = {"value": ws * cells * ke / (ms_e2e * 1e-3), "unit": "cell-updates/s", "h2d_bytes_per_step": nb,
                "d2h_bytes_per_step": nb, "steps": ke,
                "path": "EulerSolver.set_state -> step(1) -> get_state (hype_euler_upload/step/download)"}
+    # the double-float form (same initial state and steps), timed after the FP64 form's legs
+    alt = None
+    if with_alt:
+        alt = _euler_df64_beside(args, ws, n, U0, U_fp64, stream_of=lambda h: torch.cuda.ExternalStream(
+            L.hype_euler_stream(h)))
+    del U_fp64
     clocks = clk.summary()
     s.close()
     out = {
