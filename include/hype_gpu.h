@@ -132,7 +132,10 @@ double* hype_euler_state_device(hype_euler* e);
 
 /* nsteps of SSPRK(4,3) on the resident state -- replaces TSSolve with
  * TSSSP/TSSSPRKS3/4 stages (3d/weno4/Navier-Stokes-3D/hype.c:185-188).  The
- * whole step (4 fused stages, device-side dt) runs without host round trips.
+ * whole step (4 fused stages, device-side dt) runs without host round trips;
+ * with nsteps > 2 the steps after the first replay one CUDA graph of the step,
+ * captured on first use and again after a reconstruction, flux, precision,
+ * positivity, indicator or dt-mode change (not while hype_euler_profile is on).
  * *t_inout advances by the dts used; *dt_inout is the dt the next step will use
  * (input for HYPE_DT_FIXED; for the other modes pass the value of a previous
  * call, or <= 0 to start from the RHS of the current state as hype.c does). */
