@@ -36,7 +36,7 @@ SYMBOLS = [
     "hype_batch_step", "hype_batch_sync",
     "hype_strerror", "hype_last_error", "hype_launch_count", "hype_version",
     "hype_euler_stream", "hype_euler_profile", "hype_euler_profile_read", "hype_set_device", "hype_device_count",
-    "hype_probe_fma_peak", "hype_euler_rhs_noalloc", "hype_euler_noalloc_max_ext",
+    "hype_euler_rhs_noalloc", "hype_euler_noalloc_max_ext",
     "hype_mp2d_create", "hype_mp2d_destroy", "hype_mp2d_rhs", "hype_mp2d_upload", "hype_mp2d_download",
     "hype_mp2d_step", "hype_mp2d_sync", "hype_mp2d_stream", "hype_mp2d_set_mlp", "hype_mp2d_set_recon",
     "hype_mp2d_indicator_stats", "hype_mp2d_sample_features", "hype_euler_get_params", "hype_mp2d_get_params",
@@ -44,7 +44,7 @@ SYMBOLS = [
     "hype_euler_read_restart", "hype_euler_write_vtk", "hype_mp2d_write_restart", "hype_mp2d_read_restart",
     "hype_mp2d_write_vtk", "hype_acoustic_create", "hype_acoustic_destroy", "hype_acoustic_upload",
     "hype_acoustic_download", "hype_acoustic_rhs", "hype_acoustic_step", "hype_acoustic_sync", "hype_acoustic_stream",
-    "hype_acoustic_rhs_t", "hype_df64_probe", "hype_acoustic_set_point_source", "hype_acoustic_trace", "hype_acoustic2d_rhs_t",
+    "hype_acoustic_rhs_t", "hype_acoustic_set_point_source", "hype_acoustic_trace", "hype_acoustic2d_rhs_t",
     "hype_acoustic2d_set_point_source", "hype_acoustic2d_trace",
     "hype_euler_set_mlp", "hype_euler_set_recon", "hype_euler_indicator_stats", "hype_euler_sample_features",
     "hype_mlp_nparam", "hype_mlp_score", "hype_mlp_grad", "hype_mlp_train", "hype_euler_shadow_step",
@@ -173,7 +173,6 @@ def lib():
         "hype_euler_profile_read": ([V, D, P(C.c_longlong)], C.c_int),
         "hype_set_device": ([C.c_int], C.c_int),
         "hype_device_count": ([P(C.c_int)], C.c_int),
-        "hype_probe_fma_peak": ([C.c_int, D], C.c_int),
         "hype_euler_rhs_noalloc": ([P(EulerParams), V, V, D, V], C.c_int),
         "hype_euler_noalloc_max_ext": ([], C.c_longlong),
         "hype_mp2d_create": ([P(Mp2dParams), P(V)], C.c_int),
@@ -209,7 +208,6 @@ def lib():
         "hype_acoustic_sync": ([V], C.c_int),
         "hype_acoustic_stream": ([V], C.c_void_p),
         "hype_acoustic_rhs_t": ([V, C.c_double, D, D], C.c_int),
-        "hype_df64_probe": ([D, D, C.c_longlong, D], C.c_int),
         "hype_acoustic_set_point_source": ([V, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
                                             C.c_int], C.c_int),
         "hype_acoustic_trace": ([V, D, D, C.c_int, P(C.c_longlong)], C.c_int),
@@ -258,6 +256,25 @@ def lib():
         f.restype = res
     _L = L
     return L
+
+
+_P = None
+
+
+def probes():
+    """The test and measurement library (libhype_probes.so: the FMA issue ceiling and the
+    double-float primitive probe), kept out of the public C ABI; loaded after lib()."""
+    global _P
+    if _P is not None:
+        return _P
+    lib()
+    if not os.path.exists(_build.PROBE_LIB):
+        _build.build()
+    P = C.CDLL(_build.PROBE_LIB)
+    P.hype_probe_fma_peak.argtypes, P.hype_probe_fma_peak.restype = [C.c_int, D], C.c_int
+    P.hype_df64_probe.argtypes, P.hype_df64_probe.restype = [D, D, C.c_longlong, D], C.c_int
+    _P = P
+    return P
 
 
 def errstr(code: int) -> str:

@@ -1814,11 +1814,13 @@ constexpr size_t align_up(size_t b) { return (b + kAlign - 1) / kAlign * kAlign;
 constexpr size_t kNoAllocTraceBytes = align_up(sizeof(double) * NV * NTR * kNoAllocMaxExt);
 constexpr size_t kNoAllocFluxBytes = align_up(sizeof(double) * NV * kNoAllocMaxExt);  // one direction
 constexpr size_t kNoAllocScalarBytes = align_up(sizeof(DevScalars));
+// the reconstruction's two event counters (indicator, positivity fallback): written, never read here
+constexpr size_t kNoAllocCounterBytes = align_up(2 * sizeof(unsigned long long));
 // ghosted stage input: (nx+6)(ny+6)(nz+6) <= (9/5)^3 (nx+2)(ny+2)(nz+2) for n >= 3
 constexpr long long kNoAllocMaxGhost = kNoAllocMaxExt * 729 / 125 + 1;
 constexpr size_t kNoAllocGhostBytes = align_up(sizeof(double) * NV * kNoAllocMaxGhost);
-constexpr size_t kNoAllocBytes =
-    kNoAllocTraceBytes + 3 * kNoAllocFluxBytes + kNoAllocScalarBytes + kNoAllocGhostBytes;  // ~7.7 MB
+constexpr size_t kNoAllocBytes = kNoAllocTraceBytes + 3 * kNoAllocFluxBytes + kNoAllocScalarBytes +
+                                 kNoAllocCounterBytes + kNoAllocGhostBytes;  // ~7.7 MB
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -1843,6 +1845,7 @@ extern "C" int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* 
     if (p->recon != HYPE_RECON_CWENO4 && p->recon != HYPE_RECON_LINEAR4 && p->recon != HYPE_RECON_WENO3) return HYPE_ERR_ARG;
     if (p->precision != HYPE_PREC_FP64 && p->precision != HYPE_PREC_FP32) return HYPE_ERR_ARG;
     if (p->flux < HYPE_FLUX_RUSANOV || p->flux > HYPE_FLUX_ROTHLLC) return HYPE_ERR_ARG;
+    if (p->positivity != 0 && p->positivity != 1) return HYPE_ERR_ARG;
     if (p->mu != 0.0) {
         set_last_error("hype_euler_rhs_noalloc: the viscous terms need a context (hype_euler_create)", cudaErrorInvalidValue);
         return HYPE_ERR_UNSUPPORTED;
@@ -1885,20 +1888,27 @@ extern "C" int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* 
     double* Fy = (double*)(base + kNoAllocTraceBytes + kNoAllocFluxBytes);
     double* Fz = (double*)(base + kNoAllocTraceBytes + 2 * kNoAllocFluxBytes);
     DevScalars* ds = (DevScalars*)(base + kNoAllocTraceBytes + 3 * kNoAllocFluxBytes);
-    void* G = base + kNoAllocTraceBytes + 3 * kNoAllocFluxBytes + kNoAllocScalarBytes;
+    unsigned long long* counters =
+        (unsigned long long*)(base + kNoAllocTraceBytes + 3 * kNoAllocFluxBytes + kNoAllocScalarBytes);
+    void* G = base + kNoAllocTraceBytes + 3 * kNoAllocFluxBytes + kNoAllocScalarBytes + kNoAllocCounterBytes;
     cudaStream_t s = (cudaStream_t)stream;
     // the scratch keeps the previous call's contents: the wave-speed maximum and the
     // admissibility word must start cleared; traces and fluxes are fully rewritten
     k_reset_slot<<<1, 1, 0, s>>>(ds, 4);
+    HYPE_CK(cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), s));
     const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2);
     const int rec = p->recon;
+    const int pad = p->positivity;
     const dim3 bgh(128), ggh(cdiv(g.gx, 128), g.gy, g.nz + 2 * GW);
     if (p->precision == HYPE_PREC_FP32) {
+        // the FP32 admissibility check of the positivity fallback keeps its per-warp columns in
+        // dynamic shared memory, as in the context path
+        const size_t ck_bytes = pad ? sizeof(float) * 4 * 2 * NTR * 32 : 0;
         k_ghost<float><<<ggh, bgh, 0, s>>>(dU, (float*)G, g);
-        k_recon<float><<<gr, br, 0, s>>>((const float*)G, (float*)T, g, rec, 0, p->gamma - 1.0, nullptr);
+        k_recon<float><<<gr, br, ck_bytes, s>>>((const float*)G, (float*)T, g, rec, pad, p->gamma - 1.0, counters);
     } else {
         k_ghost<double><<<ggh, bgh, 0, s>>>(dU, (double*)G, g);
-        k_recon<double><<<gr, br, 0, s>>>((const double*)G, (double*)T, g, rec, 0, p->gamma - 1.0, nullptr);
+        k_recon<double><<<gr, br, 0, s>>>((const double*)G, (double*)T, g, rec, pad, p->gamma - 1.0, counters);
     }
     launch_faces(g, T, Fx, Fy, Fz, p->gamma, ds, 4, p->precision == HYPE_PREC_FP32, p->flux, s);
     const Stage st{0.0, 0.0, 0.0, 1};

@@ -1,9 +1,11 @@
 // df64_probe.cu -- elementwise probe of the double-float primitives of df64.cuh, for the
 // tests: the split of an FP64 value into its FP32 pair and back, and the pair arithmetic.
+// Built into libhype_probes.so (test use only), not part of the library's C ABI.
 #include <cuda_runtime.h>
 
 #include "df64.cuh"
 #include "hype_common.cuh"
+#include "probes.h"
 
 namespace hype {
 

@@ -175,8 +175,7 @@ def cpu_euler_rate(n: int, steps: int, use_ref: bool = True):
     from acoustic_petsc_gb300 import workloads
     from oracle import pyoracle as O
 
-    O.build(os.environ.get("HYPE_REF_DIR", "/root/reference") if os.path.isdir(
-        os.environ.get("HYPE_REF_DIR", "/root/reference")) else None)
+    O.build(O.ref_dir())
     U = workloads.euler_pulse(n)
     cfg = O.euler_cfg(n, 1.0 / n, cfl=0.4, nthreads=os.cpu_count() or 1)
     kind = "port"
@@ -279,7 +278,7 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
     flops_cell = _profile_figure(prof_file, "fp_flops_per_cell_stage")
     fpeak = C.c_double()
     # the double-float form runs its reconstruction on the FP32 pipe
-    H._lib.check(L.hype_probe_fma_peak(1 if precision == 2 else precision, C.byref(fpeak)), "probe")
+    H._lib.check(H._lib.probes().hype_probe_fma_peak(1 if precision == 2 else precision, C.byref(fpeak)), "probe")
     roof = {"kernel": "RK stage = k_recon + k_faces x3 + k_update (per-stage average)", "bound": "hbm",
             "achieved": achieved_gbs, "peak": peak, "unit": "GB/s", "frac": achieved_gbs / peak,
             "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,

@@ -195,9 +195,15 @@ int hype_euler_shadow_step(hype_euler* e, double* t_inout, double* dt_inout, dou
  * which loads the library holds until the process exits.
  *   - Limit: (nx+2)(ny+2)(nz+2) <= 5832 (e.g. 16^3 cells; hype_euler_noalloc_max_ext
  *     returns the bound); larger grids return HYPE_ERR_ARG.
+ *   - Options: CWENO4, R4 or WENO3; FP64 or FP32 reconstruction and flux; any flux;
+ *     the positivity fallback (p->positivity 0 or 1) as in the context path.  No
+ *     viscous terms (p->mu != 0 returns HYPE_ERR_UNSUPPORTED), no double-float form
+ *     and no learned indicator (both need per-context state).
  *   - The first call on a device looks up the array's device address (once per
- *     device, with that device current); make that first call before any stream
- *     capture.
+ *     device, with that device current) and keeps it for the life of the process;
+ *     make that first call before any stream capture.  cudaDeviceReset (or any
+ *     other teardown of the device's primary context) after the first call is not
+ *     supported: the kept address would be stale.
  *   - Every call shares the one array: calls that overlap on the GPU (other
  *     streams, other host threads on the same device) race and corrupt each
  *     other's results; serialise them.
@@ -514,13 +520,6 @@ int hype_mlp_train(const float* X, const float* y, int n, float* params, int epo
 /* Select the CUDA device that later hype_*_create calls of this thread use. */
 int hype_set_device(int device);
 int hype_device_count(int* n);
-/* Measured FMA issue ceiling of the FP64 (HYPE_PREC_FP64) or FP32 pipe of the
- * current device, in TFLOP/s (about 20 ms of GPU time). */
-int hype_probe_fma_peak(int precision, double* tflops);
-/* Test support for HYPE_PREC_DF64: for each x[q], y[q] (|x|, |y| in the FP32 normal range),
- * out[7q..7q+6] = the FP32 pair (hi, lo) of x as FP64 values, hi + lo, and x + y, x - y,
- * x * y, x / y in double-float arithmetic, each converted back to FP64. */
-int hype_df64_probe(const double* x, const double* y, long long n, double* out);
 const char* hype_strerror(int code);
 /* message of the last CUDA error seen by the library (thread-local) */
 const char* hype_last_error(void);

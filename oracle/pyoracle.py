@@ -30,12 +30,24 @@ def _dp(a: np.ndarray):
     return a.ctypes.data_as(D)
 
 
-def build(ref_dir: str | None = None, quiet: bool = True) -> None:
+# where this recipe looks for the reference tree when HYPE_REF_DIR is not set (the
+# container that builds the checker); the GPU machine has no reference tree
+_REF_DEFAULT = "/root/reference"
+
+
+def ref_dir() -> str | None:
+    """The reference tree the checker compiles in place: HYPE_REF_DIR, else the recipe's
+    default location; None where neither exists (then only the restatement is built)."""
+    d = os.environ.get("HYPE_REF_DIR") or _REF_DEFAULT
+    return d if os.path.isdir(d) else None
+
+
+def build(ref: str | None = None, quiet: bool = True) -> None:
     """make the restatement; also the reference checker when the tree exists."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-s", "-C", HERE, "liboracle"], check=True, stdout=out)
-    ref_dir = ref_dir or "/root/reference"
-    if os.path.isdir(ref_dir):
+    ref_dir = ref or globals()["ref_dir"]()
+    if ref_dir and os.path.isdir(ref_dir):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={ref_dir}"], check=True, stdout=out)
 
 

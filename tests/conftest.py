@@ -18,8 +18,7 @@ def pytest_configure(config):
 def oracle():
     from oracle import pyoracle
 
-    pyoracle.build(os.environ.get("HYPE_REF_DIR", "/root/reference") if os.path.isdir(
-        os.environ.get("HYPE_REF_DIR", "/root/reference")) else None)
+    pyoracle.build(pyoracle.ref_dir())
     return pyoracle
 
 

@@ -13,7 +13,7 @@ def _probe(hype, x, y):
     x = np.ascontiguousarray(x, dtype=np.float64)
     y = np.ascontiguousarray(y, dtype=np.float64)
     out = np.empty((len(x), 7))
-    L.check(L.lib().hype_df64_probe(x.ctypes.data_as(L.D), y.ctypes.data_as(L.D), len(x),
+    L.check(L.probes().hype_df64_probe(x.ctypes.data_as(L.D), y.ctypes.data_as(L.D), len(x),
                                     out.ctypes.data_as(L.D)), "hype_df64_probe")
     return out
 
