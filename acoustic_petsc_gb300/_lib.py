@@ -24,6 +24,7 @@ DT_MONITOR, DT_FROZEN, DT_FIXED = 0, 1, 2
 FLUX_RUSANOV, FLUX_HLLC, FLUX_ROTHLLC = 0, 1, 2
 MP_DI4, MP_KAPILA5 = 0, 1
 STEP_SSPRK43, STEP_SSPRK104 = 0, 1
+STAGE_AUTO, STAGE_UNFUSED = 0, 1
 
 # every entry point the header declares (checked by the CPU test suite)
 SYMBOLS = [
@@ -36,7 +37,7 @@ SYMBOLS = [
     "hype_batch_step", "hype_batch_sync",
     "hype_strerror", "hype_last_error", "hype_launch_count", "hype_version",
     "hype_euler_stream", "hype_euler_profile", "hype_euler_profile_read", "hype_set_device", "hype_device_count",
-    "hype_euler_rhs_noalloc", "hype_euler_noalloc_max_ext",
+    "hype_euler_rhs_noalloc", "hype_euler_noalloc_max_ext", "hype_euler_set_stage_kernel",
     "hype_mp2d_create", "hype_mp2d_destroy", "hype_mp2d_rhs", "hype_mp2d_upload", "hype_mp2d_download",
     "hype_mp2d_step", "hype_mp2d_sync", "hype_mp2d_stream", "hype_mp2d_set_mlp", "hype_mp2d_set_recon",
     "hype_mp2d_indicator_stats", "hype_mp2d_sample_features", "hype_euler_get_params", "hype_mp2d_get_params",
@@ -141,6 +142,7 @@ def lib():
         "hype_euler_create": ([P(EulerParams), P(V)], C.c_int),
         "hype_euler_destroy": ([V], None),
         "hype_euler_rhs": ([V, C.c_double, D, D, D], C.c_int),
+        "hype_euler_set_stage_kernel": ([V, C.c_int], C.c_int),
         "hype_euler_rhs_device": ([V, C.c_double, V, V, D], C.c_int),
         "hype_euler_upload": ([V, D], C.c_int),
         "hype_euler_download": ([V, D], C.c_int),

@@ -147,18 +147,26 @@ struct TraceCheck {
     bool ok;
 };
 
+// The FP32 admissibility test of one trace point from its density, squared momentum
+// |m|^2 (accumulated x, y, z in that order: m2 = mx*mx, then fma(my, my, m2), fma(mz, mz, m2))
+// and energy; every operation is an explicitly rounded intrinsic, so the unfused and the fused
+// stage kernels take the same decision bit for bit.
+__device__ __forceinline__ bool adm_f32(float rho, float m2, float E, float g1) {
+    return (rho >= 1.0e-14f) &&
+           (__fmul_rn(g1, __fmaf_rn(E, rho, __fmul_rn(-0.5f, m2))) >= __fmul_rn(1.0e-12f, rho));
+}
+
 __device__ __forceinline__ void trace_check(TraceCheck* ck, int c, int q, float v) {
     float* r = ck->col + q * 32;
     float* m = ck->col + (NTR + q) * 32;
     if (c == 0) {
         *r = v;
     } else if (c == 1) {
-        *m = v * v;
+        *m = __fmul_rn(v, v);
     } else if (c < 4) {
-        *m += v * v;
+        *m = __fmaf_rn(v, v, *m);
     } else {
-        const float rho = *r;
-        ck->ok = ck->ok && (rho >= 1.0e-14f) && (ck->g1 * (v * rho - 0.5f * *m) >= 1.0e-12f * rho);
+        ck->ok = ck->ok && adm_f32(*r, *m, v, ck->g1);
     }
 }
 
@@ -1014,6 +1022,21 @@ struct Stage {
     int rhs_only;
 };
 
+// The flux divergence of one cell from its six face fluxes, -(1/h)(dx + dy + dz) with
+// dx = F(i+1/2) - F(i-1/2) etc., as explicitly rounded operations in a fixed order: the x and y
+// part first, then the z difference (the fused stage kernel forms the two parts one plane apart).
+__device__ __forceinline__ double div_xy(double dx, double dy, double r1_h) {
+    return __fma_rn(-r1_h, dy, __dmul_rn(-r1_h, dx));
+}
+__device__ __forceinline__ double div_z(double pxy, double dz, double r1_h) { return __fma_rn(-r1_h, dz, pxy); }
+
+// the SSP stage value a U + b W + (c dt) L (b = 1 when a = 0), explicitly rounded
+__device__ __forceinline__ double stage_value(const Stage& st, double cdt, double u, double w, double L) {
+    if (st.rhs_only) return L;
+    if (st.a == 0.0) return __fma_rn(cdt, L, w);
+    return __fma_rn(cdt, L, __fma_rn(st.b, w, __dmul_rn(st.a, u)));
+}
+
 // U, W and out may be one array (in-place stages), so they carry no __restrict__
 __global__ void __launch_bounds__(256) k_update(const double* __restrict__ Fx, const double* __restrict__ Fy,
                                                 const double* __restrict__ Fz, const double* U,
@@ -1032,17 +1055,233 @@ __global__ void __launch_bounds__(256) k_update(const double* __restrict__ Fx, c
     const double cdt = st.rhs_only ? 0.0 : st.c * ds->dt;
 #pragma unroll
     for (int c = 0; c < NV; ++c) {
-        const double L = -r1_h * (Fx[c * nfx + ix + 1] - Fx[c * nfx + ix]) - r1_h * (Fy[c * nfy + iy + g.nx] - Fy[c * nfy + iy]) -
-                         r1_h * (Fz[c * nfz + iz + (long long)g.nx * g.ny] - Fz[c * nfz + iz]);
-        double v;
-        if (st.rhs_only) {
-            v = L;
-        } else {
-            v = W[c * g.N + cell] + cdt * L;
-            if (st.a != 0.0) v = st.a * U[c * g.N + cell] + st.b * W[c * g.N + cell] + cdt * L;
-        }
-        out[c * g.N + cell] = v;
+        const double pxy = div_xy(Fx[c * nfx + ix + 1] - Fx[c * nfx + ix], Fy[c * nfy + iy + g.nx] - Fy[c * nfy + iy], r1_h);
+        const double L = div_z(pxy, Fz[c * nfz + iz + (long long)g.nx * g.ny] - Fz[c * nfz + iz], r1_h);
+        const double u = (!st.rhs_only && st.a != 0.0) ? U[c * g.N + cell] : 0.0;
+        const double w = st.rhs_only ? 0.0 : W[c * g.N + cell];
+        out[c * g.N + cell] = stage_value(st, cdt, u, w, L);
     }
+}
+
+// ---------------------------------------------------------------- fused FP32 stage
+// One pass per RK stage for the FP32 reconstruction + Rusanov flux form: reconstruction of
+// every variable, the 24 face traces, the Rusanov solves at the face Gauss points, the flux
+// divergence, the wave-speed maximum, the admissibility word and the SSP stage combination,
+// with the face traces kept in shared memory (the unfused kernels write 120 traces per cell to
+// HBM and read them back: 960 B per cell-stage of FP32 traffic).  It follows the loop
+// structure of 3d/weno4/Navier-Stokes-3D/rhs_function.c:183-433 (reconstruct, evaluate the
+// face traces, solve per face Gauss point, difference) over tiles instead of the whole box.
+//
+// Layout: a block is FS_TW warps of 32 lanes.  Lane l of warp w holds cell
+// (i0 + l - 1, j0 + w - 1) of an x-y tile: lanes 1..30 and warps 1..FS_TW-2 are the owned
+// cells, lane 0 / 31 and warp 0 / FS_TW-1 the one-cell ring whose traces the tile's boundary
+// faces need (the ring is reconstructed again by the neighbouring tile: 2(30 + 12) of 360
+// cells per plane).  The block marches its tile along z; the +z traces of a plane stay in the
+// thread's registers as the -z side of the next plane's z faces, and each cell's divergence
+// is completed one plane later, when its +z face flux exists.  Blocks are persistent, one per
+// SM (the trace and flux arrays take 215 KB of shared memory), and split the tiles' planes into equal
+// contiguous runs: a run re-reconstructs one plane below and one above it.
+// Every arithmetic step is the unfused kernels' (cweno4 / weno3, face_traces, rusanov, the
+// admissibility test and the divergence use the same device functions and explicit roundings),
+// so both paths give bit-identical results.
+constexpr int FS_TW = 12;                        // warps per block (at most 168 registers per thread)
+constexpr int FS_NT = 32 * FS_TW;                // 384 threads
+constexpr int FS_OX = 30, FS_OY = FS_TW - 2;     // owned tile: 30 x 10 cells
+constexpr int FS_NQ = NV * NTR;                  // traces per cell
+// traces [c][q][thread] (FP32) and the x / y face fluxes [2][c][thread] (FP64): 215,040 B
+constexpr size_t FS_SMEM = sizeof(float) * FS_NQ * FS_NT + sizeof(double) * 2 * NV * FS_NT;
+
+__host__ __device__ inline long long fs_tiles_x(int nx) { return (nx + FS_OX - 1) / FS_OX; }
+__host__ __device__ inline long long fs_tiles_y(int ny) { return (ny + FS_OY - 1) / FS_OY; }
+
+// one Rusanov face (weight 1/8 per Gauss point, as k_faces): L side trace q0L.., R side q0R..
+// read from the shared trace array (columns tL, tR) or, for the z faces' low side, from registers
+__device__ __forceinline__ void fs_face(const float* __restrict__ S, int tL, int tR, int qL, int qR,
+                                        const float (*zl)[4], float gm, float gm1, double* Fd, double& smax,
+                                        bool& bad, int D) {
+    float acc[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) acc[c] = 0.0f;
+#pragma unroll
+    for (int gp = 0; gp < 4; ++gp) {
+        float QL[NV], QR[NV], fl[NV];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            QL[c] = zl ? zl[c][gp] : S[(c * NTR + qL + gp) * FS_NT + tL];
+            QR[c] = S[(c * NTR + qR + gp) * FS_NT + tR];
+        }
+        float s;
+        if (D == 0) s = rusanov<float, 0, false>(QL, QR, gm, gm1, fl, bad);
+        else if (D == 1) s = rusanov<float, 1, false>(QL, QR, gm, gm1, fl, bad);
+        else s = rusanov<float, 2, false>(QL, QR, gm, gm1, fl, bad);
+        smax = fmax(smax, (double)s);
+#pragma unroll
+        for (int c = 0; c < NV; ++c) acc[c] += 0.125f * fl[c];
+    }
+#pragma unroll
+    for (int c = 0; c < NV; ++c) Fd[c] = (double)acc[c];
+}
+
+__device__ __forceinline__ void fs_bad(DevScalars* ds, const Geo& g, int i, int j, int k) {
+    const int ci = i < g.nx ? i : g.nx - 1, cj = j < g.ny ? j : g.ny - 1, ck = k < g.nz ? k : g.nz - 1;
+    atomicMin(&ds->bad, (unsigned long long)(((long long)ck * g.ny + cj) * g.nx + ci));
+}
+
+__global__ void __launch_bounds__(FS_NT, 1)
+    k_stage_f32(const float* __restrict__ G, const double* U, const double* W, double* out, Geo g, int recon, int pad,
+                double gamma, double r1_h, Stage st, DevScalars* __restrict__ ds, int slot,
+                unsigned long long* __restrict__ counters) {
+    extern __shared__ float S[];  // traces [c][q][thread], then the x / y face fluxes [2][c][thread]
+    double* SF = reinterpret_cast<double*>(S + FS_NQ * FS_NT);
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const float gm = (float)gamma, gm1 = (float)(gamma - 1.0);
+    const int sy = g.gx, sz = g.gx * g.gy;
+    const long long tiles_x = fs_tiles_x(g.nx);
+    const long long total = tiles_x * fs_tiles_y(g.ny) * g.nz;  // plane-units
+    const long long b0 = (long long)blockIdx.x * total / gridDim.x, b1 = (long long)(blockIdx.x + 1) * total / gridDim.x;
+    const double cdt = st.rhs_only ? 0.0 : st.c * ds->dt;
+    double smax = 0.0;
+    unsigned nfall = 0;
+    for (long long pos = b0; pos < b1;) {
+        const long long tile = pos / g.nz;
+        const int kb = (int)(pos - tile * g.nz);
+        const int ke = (int)min((long long)g.nz, kb + (b1 - pos));
+        pos += ke - kb;
+        const int i0 = (int)(tile % tiles_x) * FS_OX, j0 = (int)(tile / tiles_x) * FS_OY;
+        const int i = i0 + lane - 1, j = j0 + w - 1;
+        const int ihi = min(i0 + FS_OX, g.nx), jhi = min(j0 + FS_OY, g.ny);  // owned: [i0, ihi) x [j0, jhi)
+        const bool own_x = i >= i0 && i < ihi, own_y = j >= j0 && j < jhi;
+        const bool ring_x = (i == i0 - 1 || i == ihi), ring_y = (j == j0 - 1 || j == jhi);
+        const bool owned = own_x && own_y;
+        const bool ring = (ring_x && own_y) || (own_x && ring_y);
+        float zp[NV][4];    // +z traces of the previous plane
+        double Fzp[NV];     // flux of the previous plane's -z face
+        double Pp[NV];      // x/y part of the previous plane's divergence
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            Fzp[c] = Pp[c] = 0.0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) zp[c][q] = 0.0f;
+        }
+#pragma unroll 1
+        for (int k = kb - 1; k <= ke; ++k) {
+            const bool edge = (k == kb - 1) || (k == ke);  // only the z traces of owned columns are used
+            const bool active = owned || (ring && !edge);
+            // ---- reconstruction: all 24 traces of each variable into the shared array
+            if (active) {
+                const long long ge = ghost_index(g, i, j, k);
+#pragma unroll 1
+                for (int c = 0; c < NV; ++c) {
+                    float s[33], cf[20], tr[8];
+                    gather33g<float>(G + (long long)c * g.GN + ge, sy, sz, s);
+                    if (recon == HYPE_RECON_WENO3) weno3<float>(s, cf);
+                    else cweno4<float>(s, recon == HYPE_RECON_LINEAR4, cf);
+                    float* Sc = S + (c * NTR) * FS_NT + t;
+                    face_traces<float, 0>(cf, tr);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) Sc[q * FS_NT] = tr[q];
+                    face_traces<float, 1>(cf, tr);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) Sc[(8 + q) * FS_NT] = tr[q];
+                    face_traces<float, 2>(cf, tr);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) Sc[(16 + q) * FS_NT] = tr[q];
+                }
+                // positivity fallback: the cell's 24 traces against the floors, first order if any fails
+                if (pad) {
+                    bool ok = true;
+#pragma unroll 4
+                    for (int q = 0; q < NTR; ++q) {
+                        const float rho = S[(0 * NTR + q) * FS_NT + t];
+                        float m2 = __fmul_rn(S[(1 * NTR + q) * FS_NT + t], S[(1 * NTR + q) * FS_NT + t]);
+                        m2 = __fmaf_rn(S[(2 * NTR + q) * FS_NT + t], S[(2 * NTR + q) * FS_NT + t], m2);
+                        m2 = __fmaf_rn(S[(3 * NTR + q) * FS_NT + t], S[(3 * NTR + q) * FS_NT + t], m2);
+                        ok = ok && adm_f32(rho, m2, S[(4 * NTR + q) * FS_NT + t], gm1);
+                    }
+                    if (!ok) {
+#pragma unroll 1
+                        for (int c = 0; c < NV; ++c) {
+                            const float v = __ldg(G + (long long)c * g.GN + ge);
+                            for (int q = 0; q < NTR; ++q) S[(c * NTR + q) * FS_NT + t] = v;
+                        }
+                        if (owned && !edge) ++nfall;
+                    }
+                }
+            }
+            __syncthreads();
+            // ---- Rusanov fluxes: each cell's -x, -y and -z faces (ring lanes / rows at the high side
+            // give the owned cells' +x / +y faces); x / y fluxes into the shared flux array
+            const bool plane = (k >= kb) && (k < ke);
+            if (plane && own_y && (own_x || i == ihi)) {
+                bool b = false;
+                double F[NV];
+                fs_face(S, t - 1, t, 4, 0, nullptr, gm, gm1, F, smax, b, 0);
+                if (b) fs_bad(ds, g, i, j, k);
+#pragma unroll
+                for (int c = 0; c < NV; ++c) SF[c * FS_NT + t] = F[c];
+            }
+            if (plane && own_x && (own_y || j == jhi)) {
+                bool b = false;
+                double F[NV];
+                fs_face(S, t - 32, t, 12, 8, nullptr, gm, gm1, F, smax, b, 1);
+                if (b) fs_bad(ds, g, i, j, k);
+#pragma unroll
+                for (int c = 0; c < NV; ++c) SF[(NV + c) * FS_NT + t] = F[c];
+            }
+            double Fz[NV];
+            if (k >= kb && owned) {
+                bool b = false;
+                fs_face(S, t, t, 0, 16, zp, gm, gm1, Fz, smax, b, 2);  // L: registers (zl), R: own -z (q 16..19)
+                if (b) fs_bad(ds, g, i, j, k);
+            }
+            if (owned && k < ke) {
+#pragma unroll
+                for (int c = 0; c < NV; ++c)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) zp[c][q] = S[(c * NTR + 20 + q) * FS_NT + t];
+            }
+            __syncthreads();  // traces read (the next plane may overwrite them), x / y fluxes written
+            if (owned && k >= kb) {
+                if (k > kb) {  // the previous plane's divergence is complete: its stage value
+                    const long long cell = ((long long)(k - 1) * g.ny + j) * g.nx + i;
+#pragma unroll
+                    for (int c = 0; c < NV; ++c) {
+                        const double L = div_z(Pp[c], Fz[c] - Fzp[c], r1_h);
+                        const double u = (!st.rhs_only && st.a != 0.0) ? U[c * g.N + cell] : 0.0;
+                        const double wv = st.rhs_only ? 0.0 : W[c * g.N + cell];
+                        out[c * g.N + cell] = stage_value(st, cdt, u, wv, L);
+                    }
+                }
+                if (k < ke) {
+#pragma unroll
+                    for (int c = 0; c < NV; ++c)
+                        Pp[c] = div_xy(SF[c * FS_NT + t + 1] - SF[c * FS_NT + t],
+                                       SF[(NV + c) * FS_NT + t + 32] - SF[(NV + c) * FS_NT + t], r1_h);
+                }
+#pragma unroll
+                for (int c = 0; c < NV; ++c) Fzp[c] = Fz[c];
+            }
+            // the next plane's traces are written after this plane's flux array is read: its sync
+            // (after the reconstruction) orders them before the next x / y flux writes
+        }
+    }
+    if (pad && nfall) atomicAdd(&counters[1], (unsigned long long)nfall);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, o));
+    if (lane == 0 && smax > 0.0) atomic_max_pos(&ds->smax_bits[slot], smax);
+}
+
+// the stage combination alone, from an RHS already in L (the first stage of a step whose dt
+// comes from that stage's own RHS): the same explicitly rounded value as the fused kernel's
+__global__ void __launch_bounds__(256) k_stage_combine(const double* U, const double* W, const double* __restrict__ L,
+                                                       double* out, long long n, Stage st,
+                                                       const DevScalars* __restrict__ ds) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const double cdt = st.rhs_only ? 0.0 : st.c * ds->dt;
+    const double u = (!st.rhs_only && st.a != 0.0) ? U[q] : 0.0;
+    const double w = st.rhs_only ? 0.0 : W[q];
+    out[q] = stage_value(st, cdt, u, w, L[q]);
 }
 
 // dt from the largest wave speed, rounded as each reference program does:
@@ -1242,6 +1481,11 @@ struct hype_euler {
     cudaGraphExec_t step_graph = nullptr;
     long long graph_key[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     long long graph_launches = 0;
+    // stage kernels: HYPE_STAGE_AUTO takes the fused FP32 stage where it applies; the unfused
+    // kernels' trace and face-flux buffers are allocated when first needed
+    int stage_mode = HYPE_STAGE_AUTO;
+    int nsm = 1;
+    double* acc = nullptr;  // two doubles: k_l1's sums
     std::vector<cudaEvent_t> ev;  // pairs (start, end)
     std::vector<int> ev_kind;     // 0 recon, 1 faces (3 directions), 2 update
     size_t ev_used = 0;
@@ -1382,6 +1626,81 @@ static int launch_update(hype_euler* e, const double* U, const double* W, double
     return HYPE_OK;
 }
 
+// whether the context's current options run the fused FP32 stage kernel
+static bool uses_fused(const hype_euler* e) {
+    return e->stage_mode == HYPE_STAGE_AUTO && e->p.precision == HYPE_PREC_FP32 && e->p.flux == HYPE_FLUX_RUSANOV &&
+           !e->C4 && (e->p.recon == HYPE_RECON_CWENO4 || e->p.recon == HYPE_RECON_LINEAR4 ||
+                      e->p.recon == HYPE_RECON_WENO3);
+}
+
+// the unfused kernels' face traces and face fluxes, allocated on first use (never inside a
+// stream capture: every entry point that may launch them calls this first)
+static int ensure_unfused(hype_euler* e) {
+    if (e->T) return HYPE_OK;
+    const Geo& g = e->g;
+    const hype_euler_params* p = &e->p;
+    const size_t tsz = (p->precision == HYPE_PREC_FP32 ? sizeof(float) : sizeof(double)) * NV * NTR * (size_t)g.NE;
+    cudaError_t ce = cudaMalloc(&e->T, tsz);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&e->Fx, sizeof(double) * NV * (size_t)(p->nx + 1) * p->ny * p->nz);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&e->Fy, sizeof(double) * NV * (size_t)p->nx * (p->ny + 1) * p->nz);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&e->Fz, sizeof(double) * NV * (size_t)p->nx * p->ny * (p->nz + 1));
+    if (ce != cudaSuccess) {
+        cudaFree(e->T); cudaFree(e->Fx); cudaFree(e->Fy); cudaFree(e->Fz);
+        e->T = nullptr; e->Fx = e->Fy = e->Fz = nullptr;
+        set_last_error("cudaMalloc (face traces)", ce);
+        return HYPE_ERR_NOMEM;
+    }
+    return HYPE_OK;
+}
+
+static int prepare(hype_euler* e) { return uses_fused(e) ? HYPE_OK : ensure_unfused(e); }
+
+// One RK stage: out = a U + b W + (c dt) L(Win) (or out = L(Win) for RHS-only calls), with the
+// wave-speed maximum into slot.  The fused FP32 stage is the device ghost fill plus one kernel;
+// every other form is ghost fill, reconstruction, three face-flux kernels and the update.
+static int launch_stage(hype_euler* e, const double* Win, const double* U, const double* W, double* out, Stage st,
+                        int slot) {
+    if (!uses_fused(e)) {
+        int rc = launch_rhs(e, Win, slot);
+        if (rc) return rc;
+        return launch_update(e, U, W, out, st);
+    }
+    const Geo& g = e->g;
+    prof_mark(e, 0, true);
+    const dim3 bgh(128), ggh(cdiv(g.gx, 128), g.gy, g.nz + 2 * GW);
+    k_ghost<float><<<ggh, bgh, 0, e->stream>>>(Win, (float*)e->G, g);
+    prof_mark(e, 0, false);
+    prof_mark(e, 1, true);
+    const long long units = fs_tiles_x(g.nx) * fs_tiles_y(g.ny) * g.nz;
+    const unsigned blocks = (unsigned)std::min<long long>(e->nsm, units);
+    k_stage_f32<<<blocks, FS_NT, FS_SMEM, e->stream>>>((const float*)e->G, U, W, out, g, e->p.recon, e->p.positivity,
+                                                      e->p.gamma, 1.0 / e->p.h, st, e->ds, slot, e->mlp_cnt);
+    prof_mark(e, 1, false);
+    HYPE_LAUNCHED(2);
+    return HYPE_OK;
+}
+
+// the first stage of a step whose dt comes from that stage's own RHS: RHS into L, dt, then the
+// stage combination (fused form) or the update kernel (unfused)
+static int launch_first_stage_from_rhs(hype_euler* e, int mode, double cfl_h, Stage s12) {
+    int rc;
+    if (uses_fused(e)) {
+        const Stage rhs{0.0, 0.0, 0.0, 1};
+        if ((rc = launch_stage(e, e->U, nullptr, nullptr, e->L, rhs, 0))) return rc;
+    } else if ((rc = launch_rhs(e, e->U, 0))) {
+        return rc;
+    }
+    k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 0, 1, 0, cfl_h, e->p.recon, 1.0 / e->p.h, e->C4 != nullptr);
+    HYPE_LAUNCHED(1);
+    if (!uses_fused(e)) return launch_update(e, e->U, e->U, e->W, s12);
+    const long long n = NV * e->g.N;
+    prof_mark(e, 2, true);
+    k_stage_combine<<<cdiv(n, 256), 256, 0, e->stream>>>(e->U, e->U, e->L, e->W, n, s12, e->ds);
+    prof_mark(e, 2, false);
+    HYPE_LAUNCHED(1);
+    return HYPE_OK;
+}
+
 extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
     if (!p || !out) return HYPE_ERR_ARG;
     *out = nullptr;
@@ -1417,7 +1736,6 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
     g.ey = p->ny + 2;
     set_ghost_extents(g);
     const size_t sN = sizeof(double) * NV * (size_t)g.N;
-    const size_t tsz = (p->precision == HYPE_PREC_FP32 ? sizeof(float) : sizeof(double)) * NV * NTR * (size_t)g.NE;
     int rc = HYPE_OK;
     auto fail = [&](int code) {
         hype_euler_destroy(e);
@@ -1439,16 +1757,25 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
     ALLOC(e->W, sN);
     ALLOC(e->L, sN);
     ALLOC(e->S, sN);
-    ALLOC(e->T, tsz);
-    ALLOC(e->Fx, sizeof(double) * NV * (size_t)(p->nx + 1) * p->ny * p->nz);
-    ALLOC(e->Fy, sizeof(double) * NV * (size_t)p->nx * (p->ny + 1) * p->nz);
-    ALLOC(e->Fz, sizeof(double) * NV * (size_t)p->nx * p->ny * (p->nz + 1));
     ALLOC(e->stage_aos, sN);
+    ALLOC(e->acc, 2 * sizeof(double));
     ALLOC(e->ds, sizeof(DevScalars));
     ALLOC(e->mlp_cnt, 2 * sizeof(unsigned long long));
     ALLOC(e->G, (p->precision == HYPE_PREC_FP32 ? sizeof(float) : sizeof(double)) * NV * (size_t)g.GN);
     if (visc) ALLOC(e->C4, sizeof(double) * NV * 20 * (size_t)g.NE);
 #undef ALLOC
+    {
+        int dev = 0;
+        ce = cudaGetDevice(&dev);
+        if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (ce == cudaSuccess)
+            ce = cudaFuncSetAttribute(k_stage_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FS_SMEM);
+        if (ce != cudaSuccess) {
+            set_last_error("hype_euler_create (device attributes)", ce);
+            return fail(HYPE_ERR_CUDA);
+        }
+        if ((rc = prepare(e))) return fail(rc);
+    }
     ce = cudaMemset(e->mlp_cnt, 0, 2 * sizeof(unsigned long long));
     if (ce != cudaSuccess) {
         set_last_error("cudaMemset", ce);
@@ -1476,7 +1803,7 @@ extern "C" void hype_euler_destroy(hype_euler* e) {
     if (e->stream) cudaStreamSynchronize(e->stream);
     cudaFree(e->U); cudaFree(e->W); cudaFree(e->L); cudaFree(e->S); cudaFree(e->T);
     cudaFree(e->Fx); cudaFree(e->Fy); cudaFree(e->Fz); cudaFree(e->stage_aos); cudaFree(e->ds); cudaFree(e->G);
-    cudaFree(e->mlp); cudaFree(e->mlp_cnt); cudaFree(e->C4); cudaFree(e->mon);
+    cudaFree(e->mlp); cudaFree(e->mlp_cnt); cudaFree(e->C4); cudaFree(e->mon); cudaFree(e->acc);
     if (e->hs) cudaFreeHost(e->hs);
     for (auto x : e->ev) cudaEventDestroy(x);
     if (e->step_graph) cudaGraphExecDestroy(e->step_graph);
@@ -1508,11 +1835,11 @@ static int read_scalars(hype_euler* e) {
 
 static int rhs_core(hype_euler* e, const double* dU, double* dRHS, double* dt_out) {
     int rc;
+    if ((rc = prepare(e))) return rc;
     k_reset_slot<<<1, 1, 0, e->stream>>>(e->ds, 4);
     HYPE_LAUNCHED(1);
-    if ((rc = launch_rhs(e, dU, 4))) return rc;
     Stage st{0.0, 0.0, 0.0, 1};
-    if ((rc = launch_update(e, nullptr, nullptr, dRHS, st))) return rc;
+    if ((rc = launch_stage(e, dU, nullptr, nullptr, dRHS, st, 4))) return rc;
     if ((rc = read_scalars(e))) return rc;
     const double smax = bits_to_double(e->hs->smax_bits[4]);
     const double smaxv = bits_to_double(e->hs->smaxv_bits[4]);
@@ -1579,14 +1906,10 @@ static int launch_steady_step(hype_euler* e, int mode, double cfl_h) {
     k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 3, mode == HYPE_DT_MONITOR, 1, cfl_h, e->p.recon, 1.0 / e->p.h,
                                          e->C4 != nullptr);
     HYPE_LAUNCHED(1);
-    if ((rc = launch_rhs(e, e->U, 0))) return rc;
-    if ((rc = launch_update(e, e->U, e->U, e->W, s12))) return rc;
-    if ((rc = launch_rhs(e, e->W, 1))) return rc;
-    if ((rc = launch_update(e, e->U, e->W, e->W, s12))) return rc;
-    if ((rc = launch_rhs(e, e->W, 2))) return rc;
-    if ((rc = launch_update(e, e->U, e->W, e->W, s3))) return rc;
-    if ((rc = launch_rhs(e, e->W, 3))) return rc;
-    return launch_update(e, e->U, e->W, e->U, s12);
+    if ((rc = launch_stage(e, e->U, e->U, e->U, e->W, s12, 0))) return rc;
+    if ((rc = launch_stage(e, e->W, e->U, e->W, e->W, s12, 1))) return rc;
+    if ((rc = launch_stage(e, e->W, e->U, e->W, e->W, s3, 2))) return rc;
+    return launch_stage(e, e->W, e->U, e->W, e->U, s12, 3);
 }
 
 // The steady-state step as a CUDA graph (replayed instead of ~25 launches per step; what
@@ -1596,8 +1919,8 @@ static bool steady_step_graph(hype_euler* e, int mode, double cfl_h) {
     if (e->prof) return false;
     long long lt;
     memcpy(&lt, &e->logit_thr, sizeof(float));
-    const long long key[8] = {mode, e->p.recon, e->p.flux, e->p.precision, e->p.positivity, (long long)(size_t)e->mlp,
-                              lt, (long long)(cfl_h * 1e15)};
+    const long long key[8] = {mode, e->p.recon, e->p.flux, e->p.precision, e->p.positivity + 2 * e->stage_mode,
+                              (long long)(size_t)e->mlp, lt, (long long)(cfl_h * 1e15)};
     if (e->step_graph && memcmp(key, e->graph_key, sizeof(key)) == 0) return true;
     if (e->step_graph) {
         cudaGraphExecDestroy(e->step_graph);
@@ -1637,6 +1960,7 @@ extern "C" int hype_euler_step(hype_euler* e, int nsteps, double* t_inout, doubl
     if (mode == HYPE_DT_FIXED && !(*dt_inout > 0)) return HYPE_ERR_ARG;
     const double cfl_h = e->p.cfl * e->p.h;
     int rc;
+    if ((rc = prepare(e))) return rc;
     // host-side initial values of t, dt, flags
     DevScalars init;
     memset(&init, 0, sizeof(init));
@@ -1659,24 +1983,18 @@ extern "C" int hype_euler_step(hype_euler* e, int nsteps, double* t_inout, doubl
         }
         if (s == 0 && first_from_rhs) {
             // the initial RHS call of hype.c:175 is this step's first stage RHS
-            if ((rc = launch_rhs(e, e->U, 0))) return rc;
-            k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 0, 1, 0, cfl_h, e->p.recon, 1.0 / e->p.h, e->C4 != nullptr);
-            HYPE_LAUNCHED(1);
+            if ((rc = launch_first_stage_from_rhs(e, mode, cfl_h, s12))) return rc;
         } else {
             // dt: MONITOR refreshes it from the last stage of the previous step
             const int use_src = (mode == HYPE_DT_MONITOR) && s > 0;
             k_begin_step<<<1, 1, 0, e->stream>>>(e->ds, mode, 3, use_src, 1, cfl_h, e->p.recon, 1.0 / e->p.h,
                                                  e->C4 != nullptr);
             HYPE_LAUNCHED(1);
-            if ((rc = launch_rhs(e, e->U, 0))) return rc;
+            if ((rc = launch_stage(e, e->U, e->U, e->U, e->W, s12, 0))) return rc;
         }
-        if ((rc = launch_update(e, e->U, e->U, e->W, s12))) return rc;
-        if ((rc = launch_rhs(e, e->W, 1))) return rc;
-        if ((rc = launch_update(e, e->U, e->W, e->W, s12))) return rc;
-        if ((rc = launch_rhs(e, e->W, 2))) return rc;
-        if ((rc = launch_update(e, e->U, e->W, e->W, s3))) return rc;
-        if ((rc = launch_rhs(e, e->W, 3))) return rc;
-        if ((rc = launch_update(e, e->U, e->W, e->U, s12))) return rc;
+        if ((rc = launch_stage(e, e->W, e->U, e->W, e->W, s12, 1))) return rc;
+        if ((rc = launch_stage(e, e->W, e->U, e->W, e->W, s3, 2))) return rc;
+        if ((rc = launch_stage(e, e->W, e->U, e->W, e->U, s12, 3))) return rc;
     }
     if ((rc = read_scalars(e))) return rc;
     *t_inout = e->hs->t;
@@ -1768,6 +2086,13 @@ extern "C" int hype_euler_sample_features(hype_euler* e, long long stride, float
     }
     if (ns_out) *ns_out = ns;
     return HYPE_OK;
+}
+
+extern "C" int hype_euler_set_stage_kernel(hype_euler* e, int mode) {
+    if (!e || (mode != HYPE_STAGE_AUTO && mode != HYPE_STAGE_UNFUSED)) return HYPE_ERR_ARG;
+    HYPE_CK(cudaStreamSynchronize(e->stream));
+    e->stage_mode = mode;
+    return prepare(e);
 }
 
 extern "C" int hype_euler_profile(hype_euler* e, int enable) {
@@ -1944,7 +2269,7 @@ extern "C" int hype_euler_shadow_step(hype_euler* e, double* t_inout, double* dt
     *t_inout = t0;
     *dt_inout = dt0;
     if ((rc = hype_euler_step(e, 1, t_inout, dt_inout, nullptr))) return rc;
-    double* acc = (double*)e->Fx;  // scratch: the face fluxes are rebuilt by the next RHS
+    double* acc = e->acc;
     HYPE_CK(cudaMemsetAsync(acc, 0, 2 * sizeof(double), e->stream));
     k_l1<<<608, 256, 0, e->stream>>>(e->U, e->L, e->g.N, acc);
     HYPE_LAUNCHED(1);

@@ -183,6 +183,10 @@ class EulerSolver:
         check(L.lib().hype_euler_set_recon(self._h, int(recon)), "hype_euler_set_recon")
         self.ctx.recon = recon
 
+    def set_stage_kernel(self, mode: int) -> None:
+        """L.STAGE_AUTO: the fused FP32 stage where it applies; L.STAGE_UNFUSED: separate kernels"""
+        check(L.lib().hype_euler_set_stage_kernel(self._h, int(mode)), "hype_euler_set_stage_kernel")
+
     def indicator_stats(self, reset: bool = True):
         f, b = C.c_longlong(), C.c_longlong()
         check(L.lib().hype_euler_indicator_stats(self._h, C.byref(f), C.byref(b), int(reset)), "indicator_stats")

@@ -158,10 +158,24 @@ int hype_euler_monitor(hype_euler* e, double* ke, double* dissipation);
 
 /* Per-kernel timing: while enabled, every kernel the context launches is
  * bracketed by CUDA events on its stream; read returns the summed milliseconds
- * and launch counts of [0] reconstruction, [1] face fluxes (3 directions),
- * [2] divergence + stage update since the last enable. */
+ * and launch counts of [0] ghost fill + reconstruction, [1] face fluxes (3
+ * directions) or, for the fused stage, the fused stage kernel, [2] divergence +
+ * stage update (fused stage: only the combination of a first stage whose dt
+ * comes from its own RHS) since the last enable. */
 int hype_euler_profile(hype_euler* e, int enable);
 int hype_euler_profile_read(hype_euler* e, double* ms, long long* count);
+
+/* Stage kernels.  HYPE_STAGE_AUTO (the default) runs the FP32 reconstruction +
+ * Rusanov form (CWENO4, R4 or WENO3, inviscid) as one fused kernel per RK stage
+ * after the device ghost fill: face traces stay in shared memory, there is no
+ * trace or face-flux buffer, and the results are bit-identical to the unfused
+ * kernels.  Every other form, and HYPE_STAGE_UNFUSED, runs ghost fill,
+ * reconstruction into a face-trace buffer, three face-flux kernels and the
+ * update.  No counterpart in the reference (its RHSFunction is one CPU pass,
+ * 3d/weno4/Navier-Stokes-3D/rhs_function.c:183-433). */
+#define HYPE_STAGE_AUTO 0
+#define HYPE_STAGE_UNFUSED 1
+int hype_euler_set_stage_kernel(hype_euler* e, int mode);
 
 /* ---- learned troubled-cell indicator (no counterpart in the reference) ----
  * Network 25 -> 32 -> 32 -> 1 (ReLU), BF16 weights, FP32 accumulation; params are
