@@ -1079,7 +1079,7 @@ __global__ void __launch_bounds__(256) k_update(const double* __restrict__ Fx, c
 // cells per plane).  The block marches its tile along z; the +z traces of a plane stay in the
 // thread's registers as the -z side of the next plane's z faces, and each cell's divergence
 // is completed one plane later, when its +z face flux exists.  Blocks are persistent, one per
-// SM (the trace and flux arrays take 215 KB of shared memory), and split the tiles' planes into equal
+// SM (the trace array takes 180 KB of shared memory), and split the tiles' planes into equal
 // contiguous runs: a run re-reconstructs one plane below and one above it.
 // Every arithmetic step is the unfused kernels' (cweno4 / weno3, face_traces, rusanov, the
 // admissibility test and the divergence use the same device functions and explicit roundings),
@@ -1088,8 +1088,8 @@ constexpr int FS_TW = 12;                        // warps per block (at most 168
 constexpr int FS_NT = 32 * FS_TW;                // 384 threads
 constexpr int FS_OX = 30, FS_OY = FS_TW - 2;     // owned tile: 30 x 10 cells
 constexpr int FS_NQ = NV * NTR;                  // traces per cell
-// traces [c][q][thread] (FP32) and the x / y face fluxes [2][c][thread] (FP64): 215,040 B
-constexpr size_t FS_SMEM = sizeof(float) * FS_NQ * FS_NT + sizeof(double) * 2 * NV * FS_NT;
+// traces [c][q][thread] (FP32): 184,320 B, which leaves 60 KB of the SM's L1 for the stencil gathers
+constexpr size_t FS_SMEM = sizeof(float) * FS_NQ * FS_NT;
 
 __host__ __device__ inline long long fs_tiles_x(int nx) { return (nx + FS_OX - 1) / FS_OX; }
 __host__ __device__ inline long long fs_tiles_y(int ny) { return (ny + FS_OY - 1) / FS_OY; }
@@ -1131,8 +1131,7 @@ __global__ void __launch_bounds__(FS_NT, 1)
     k_stage_f32(const float* __restrict__ G, const double* U, const double* W, double* out, Geo g, int recon, int pad,
                 double gamma, double r1_h, Stage st, DevScalars* __restrict__ ds, int slot,
                 unsigned long long* __restrict__ counters) {
-    extern __shared__ float S[];  // traces [c][q][thread], then the x / y face fluxes [2][c][thread]
-    double* SF = reinterpret_cast<double*>(S + FS_NQ * FS_NT);
+    extern __shared__ float S[];  // traces [c][q][thread]
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const float gm = (float)gamma, gm1 = (float)(gamma - 1.0);
     const int sy = g.gx, sz = g.gx * g.gy;
@@ -1209,40 +1208,18 @@ __global__ void __launch_bounds__(FS_NT, 1)
                 }
             }
             __syncthreads();
-            // ---- Rusanov fluxes: each cell's -x, -y and -z faces (ring lanes / rows at the high side
-            // give the owned cells' +x / +y faces); x / y fluxes into the shared flux array
+            // ---- Rusanov fluxes of the owned cells' faces: -x (the ring lane at the high side gives
+            // the last cell's +x; the +x flux of every cell comes from its right neighbour lane by a
+            // shuffle), -y and +y (each y face is solved by both of its cells: no exchange between
+            // warps), -z (low side from registers)
             const bool plane = (k >= kb) && (k < ke);
-            if (plane && own_y && (own_x || i == ihi)) {
-                bool b = false;
-                double F[NV];
-                fs_face(S, t - 1, t, 4, 0, nullptr, gm, gm1, F, smax, b, 0);
-                if (b) fs_bad(ds, g, i, j, k);
-#pragma unroll
-                for (int c = 0; c < NV; ++c) SF[c * FS_NT + t] = F[c];
-            }
-            if (plane && own_x && (own_y || j == jhi)) {
-                bool b = false;
-                double F[NV];
-                fs_face(S, t - 32, t, 12, 8, nullptr, gm, gm1, F, smax, b, 1);
-                if (b) fs_bad(ds, g, i, j, k);
-#pragma unroll
-                for (int c = 0; c < NV; ++c) SF[(NV + c) * FS_NT + t] = F[c];
-            }
-            double Fz[NV];
+            // z face first: it completes the previous plane (its stage value), then frees zp
             if (k >= kb && owned) {
+                double Fz[NV];
                 bool b = false;
                 fs_face(S, t, t, 0, 16, zp, gm, gm1, Fz, smax, b, 2);  // L: registers (zl), R: own -z (q 16..19)
                 if (b) fs_bad(ds, g, i, j, k);
-            }
-            if (owned && k < ke) {
-#pragma unroll
-                for (int c = 0; c < NV; ++c)
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) zp[c][q] = S[(c * NTR + 20 + q) * FS_NT + t];
-            }
-            __syncthreads();  // traces read (the next plane may overwrite them), x / y fluxes written
-            if (owned && k >= kb) {
-                if (k > kb) {  // the previous plane's divergence is complete: its stage value
+                if (k > kb) {
                     const long long cell = ((long long)(k - 1) * g.ny + j) * g.nx + i;
 #pragma unroll
                     for (int c = 0; c < NV; ++c) {
@@ -1252,17 +1229,44 @@ __global__ void __launch_bounds__(FS_NT, 1)
                         out[c * g.N + cell] = stage_value(st, cdt, u, wv, L);
                     }
                 }
-                if (k < ke) {
-#pragma unroll
-                    for (int c = 0; c < NV; ++c)
-                        Pp[c] = div_xy(SF[c * FS_NT + t + 1] - SF[c * FS_NT + t],
-                                       SF[(NV + c) * FS_NT + t + 32] - SF[(NV + c) * FS_NT + t], r1_h);
-                }
 #pragma unroll
                 for (int c = 0; c < NV; ++c) Fzp[c] = Fz[c];
             }
-            // the next plane's traces are written after this plane's flux array is read: its sync
-            // (after the reconstruction) orders them before the next x / y flux writes
+            if (owned && k < ke) {
+#pragma unroll
+                for (int c = 0; c < NV; ++c)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) zp[c][q] = S[(c * NTR + 20 + q) * FS_NT + t];
+            }
+            // x faces: every lane its -x face (the ring lane at the high side gives the last cell's +x),
+            // the +x flux from the right neighbour lane
+            double dF[NV];
+            {
+                double Fxl[NV];
+#pragma unroll
+                for (int c = 0; c < NV; ++c) Fxl[c] = 0.0;
+                if (plane && own_y && (own_x || i == ihi)) {
+                    bool b = false;
+                    fs_face(S, t - 1, t, 4, 0, nullptr, gm, gm1, Fxl, smax, b, 0);
+                    if (b) fs_bad(ds, g, i, j, k);
+                }
+#pragma unroll
+                for (int c = 0; c < NV; ++c) dF[c] = __shfl_down_sync(0xffffffffu, Fxl[c], 1) - Fxl[c];
+            }
+            // y faces: each owned cell solves its -y and +y faces (both of its neighbours' rows are in
+            // the shared array; no flux exchange between warps)
+            if (plane && owned) {
+                double Fl[NV], Fh[NV];
+                bool b = false;
+                fs_face(S, t - 32, t, 12, 8, nullptr, gm, gm1, Fl, smax, b, 1);
+                if (b) fs_bad(ds, g, i, j, k);
+                b = false;
+                fs_face(S, t, t + 32, 12, 8, nullptr, gm, gm1, Fh, smax, b, 1);
+                if (b) fs_bad(ds, g, i, j + 1, k);
+#pragma unroll
+                for (int c = 0; c < NV; ++c) Pp[c] = div_xy(dF[c], Fh[c] - Fl[c], r1_h);
+            }
+            __syncthreads();  // every trace of the plane read before the next plane's are written
         }
     }
     if (pad && nfall) atomicAdd(&counters[1], (unsigned long long)nfall);

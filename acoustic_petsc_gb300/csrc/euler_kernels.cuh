@@ -24,7 +24,7 @@ namespace euler {
 // integer pipe.  x outside [2^-126, 2^126) in magnitude, zero or not finite: the division.
 template <typename R>
 __device__ __forceinline__ R recip(R x) {
-    if (sizeof(R) != sizeof(double)) return R(1) / x;
+    if (sizeof(R) != sizeof(double)) return (R)__frcp_rn((float)x);  // 1 / x correctly rounded, as the division
     const double xd = (double)x;
     const unsigned hi = (unsigned)__double2hiint(xd);
     const unsigned ex = (hi >> 20) & 0x7FFu;
