@@ -34,7 +34,8 @@ SYMBOLS = [
     "hype_ctcs_step", "hype_ctcs_level_device", "hype_ctcs_sync",
     "hype_batch_create", "hype_batch_destroy", "hype_batch_set_tile", "hype_batch_get_tile", "hype_batch_set",
     "hype_batch_get",
-    "hype_batch_step", "hype_batch_sync",
+    "hype_batch_step", "hype_batch_sync", "hype_batch_set_classes", "hype_batch_get_classes",
+    "hype_batch_instance_times",
     "hype_strerror", "hype_last_error", "hype_launch_count", "hype_version",
     "hype_euler_stream", "hype_euler_profile", "hype_euler_profile_read", "hype_set_device", "hype_device_count",
     "hype_euler_rhs_noalloc", "hype_euler_noalloc_max_ext", "hype_euler_set_stage_kernel",
@@ -164,6 +165,9 @@ def lib():
         "hype_batch_set": ([V, C.c_int, D, D], C.c_int),
         "hype_batch_get": ([V, C.c_int, D, D], C.c_int),
         "hype_batch_step": ([V, C.c_int, C.c_int], C.c_int),
+        "hype_batch_set_classes": ([V, C.c_int], C.c_int),
+        "hype_batch_get_classes": ([V, I, I], C.c_int),
+        "hype_batch_instance_times": ([V, D], C.c_int),
         "hype_batch_sync": ([V], C.c_int),
         "hype_strerror": ([C.c_int], C.c_char_p),
         "hype_last_error": ([], C.c_char_p),

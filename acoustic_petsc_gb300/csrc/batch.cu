@@ -12,6 +12,14 @@
 // launch is sized to the GPU (a multiple of the SM count), not to the batch.
 // A chunk of steps is captured once as a CUDA graph and replayed; the tile
 // shape is chosen by timing candidates and cached per grid-shape signature.
+//
+// Scheduling: the instances are split by size into classes (equal counts, smallest
+// first), each with its own stream, work-list and step counter; the classes' kernels
+// carry descending launch priorities, smallest class highest, so the block scheduler
+// serves the small instances' steps first and fills the SMs they leave idle with the
+// larger classes' tiles.  Every instance's arithmetic is unchanged (the classes touch
+// disjoint parts of the level pools), small instances finish early, and the
+// completion time of each class is an event on the device timeline.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdlib.h>
@@ -49,12 +57,14 @@ struct Work {
 //   p^{n+1} = (2 - 4a) p - p^{n-1} + a ((e + w) + (n + s)) + (k2 sin gx) gy,
 // a = (c0 dt/h)^2, the same update as 2p - p^{n-1} + c0^2 dt^2 (lap_h p + s) up to
 // rounding.
+// the step index is the class's counter (advanced once per graph chunk) plus s_off
 template <int TX, int TY, int R>
 __global__ void __launch_bounds__(TX* TY) k_batch(const Inst* __restrict__ inst, const Work* __restrict__ work, int nwork,
                                                   const double* __restrict__ pold, const double* __restrict__ p,
                                                   double* __restrict__ pnew, const double* __restrict__ gauss,
-                                                  const double* __restrict__ sinv, int ninst, const int* __restrict__ step) {
-    const int s = *step;
+                                                  const double* __restrict__ sinv, int ninst, const int* __restrict__ step,
+                                                  int s_off) {
+    const int s = *step + s_off;
     for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
         const Work wk = work[w];
         const Inst I = inst[wk.q];
@@ -85,7 +95,9 @@ __global__ void __launch_bounds__(TX* TY) k_batch(const Inst* __restrict__ inst,
     }
 }
 
-__global__ void k_tick(int* step) { *step += 1; }
+__global__ void k_tick(int* step, int inc) { *step += inc; }
+
+constexpr int kMaxClasses = 8;
 
 }  // namespace batch
 }  // namespace hype
@@ -105,18 +117,26 @@ struct hype_batch {
     double* sinv = nullptr;
     int sin_cap = 0;
     long long it = 0;  // global step counter of the instances (time t = it*dt)
-    int* d_step = nullptr;
-    int tx = 0, ty = 0;  // chosen tile
-    Work* d_work = nullptr;
-    int nwork = 0;
-    int grid = 0;
-    cudaGraphExec_t chunk[3] = {nullptr, nullptr, nullptr};
+    int* d_step = nullptr;  // one step counter per class
+    int tx = 0, ty = 0;     // chosen tile
+    // size classes: instance -> class, per class its stream, priority, work-list and graphs
+    int ncls = 1;
+    std::vector<int> cls;
+    cudaStream_t cs[kMaxClasses] = {};
+    int prio[kMaxClasses] = {};
+    Work* d_work[kMaxClasses] = {};
+    int nwork[kMaxClasses] = {};
+    int grid[kMaxClasses] = {};
+    cudaGraphExec_t chunk[kMaxClasses][3] = {};
+    cudaEvent_t ev_start = nullptr;
+    cudaEvent_t ev_done[kMaxClasses] = {};
+    bool timed = false;  // the events hold the last hype_batch_step call
 };
 
 static const int kBatchChunk = 30;
 
 typedef void (*BatchKernel)(const Inst*, const Work*, int, const double*, const double*, double*, const double*,
-                            const double*, int, const int*);
+                            const double*, int, const int*, int);
 
 // tile shapes (width x height in nodes) and their thread blocks: TX x TY threads,
 // R rows per thread
@@ -138,61 +158,100 @@ static const TileCfg* pick_tile(int tx, int ty) {
 }
 
 static void drop_graphs(hype_batch* b) {
-    for (int q = 0; q < 3; ++q)
-        if (b->chunk[q]) {
-            cudaGraphExecDestroy(b->chunk[q]);
-            b->chunk[q] = nullptr;
-        }
+    for (int c = 0; c < kMaxClasses; ++c)
+        for (int q = 0; q < 3; ++q)
+            if (b->chunk[c][q]) {
+                cudaGraphExecDestroy(b->chunk[c][q]);
+                b->chunk[c][q] = nullptr;
+            }
 }
 
 static int build_worklist(hype_batch* b, int tx, int ty) {
     const TileCfg* tc = pick_tile(tx, ty);
     if (!tc) return HYPE_ERR_ARG;
-    std::vector<Work> w;
-    for (size_t q = 0; q < b->inst.size(); ++q)
-        for (int j0 = 0; j0 < b->inst[q].ny; j0 += ty)
-            for (int i0 = 0; i0 < b->inst[q].nx; i0 += tx) w.push_back(Work{(int)q, i0, j0, 0});
-    cudaFree(b->d_work);
-    b->d_work = nullptr;
-    HYPE_CK(cudaMalloc((void**)&b->d_work, sizeof(Work) * w.size()));
-    HYPE_CK(cudaMemcpy(b->d_work, w.data(), sizeof(Work) * w.size(), cudaMemcpyHostToDevice));
-    b->nwork = (int)w.size();
     int dev = 0, sms = 0, per_sm = 0;
     HYPE_CK(cudaGetDevice(&dev));
     HYPE_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     HYPE_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc->k, tx * tc->threads_y, 0));
     if (per_sm < 1) per_sm = 1;
-    b->grid = std::min<long long>((long long)sms * per_sm, (long long)b->nwork);
+    for (int c = 0; c < b->ncls; ++c) {
+        std::vector<Work> w;
+        for (size_t q = 0; q < b->inst.size(); ++q) {
+            if (b->cls[q] != c) continue;
+            for (int j0 = 0; j0 < b->inst[q].ny; j0 += ty)
+                for (int i0 = 0; i0 < b->inst[q].nx; i0 += tx) w.push_back(Work{(int)q, i0, j0, 0});
+        }
+        cudaFree(b->d_work[c]);
+        b->d_work[c] = nullptr;
+        b->nwork[c] = (int)w.size();
+        if (w.empty()) continue;
+        HYPE_CK(cudaMalloc((void**)&b->d_work[c], sizeof(Work) * w.size()));
+        HYPE_CK(cudaMemcpy(b->d_work[c], w.data(), sizeof(Work) * w.size(), cudaMemcpyHostToDevice));
+        b->grid[c] = (int)std::min<long long>((long long)sms * per_sm, (long long)w.size());
+    }
     b->tx = tx;
     b->ty = ty;
     drop_graphs(b);
     return HYPE_OK;
 }
 
-static int batch_launch(hype_batch* b, int phase) {
+// class c's kernel for one step (step index = its counter + s_off), at the class's priority
+static int class_launch(hype_batch* b, int c, int phase, int s_off) {
     const TileCfg* tc = pick_tile(b->tx, b->ty);
-    double* po = b->lv[(phase + 2) % 3];
-    double* pc = b->lv[phase];
+    const double* po = b->lv[(phase + 2) % 3];
+    const double* pc = b->lv[phase];
     double* pn = b->lv[(phase + 1) % 3];
-    tc->k<<<b->grid, dim3(b->tx, tc->threads_y), 0, b->stream>>>(b->d_inst, b->d_work, b->nwork, po, pc, pn, b->gauss,
-                                                                 b->sinv, (int)b->inst.size(), b->d_step);
-    k_tick<<<1, 1, 0, b->stream>>>(b->d_step);
-    HYPE_LAUNCHED(2);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(b->grid[c]);
+    cfg.blockDim = dim3(b->tx, tc->threads_y);
+    cfg.stream = b->cs[c];
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributePriority;
+    attr.val.priority = b->prio[c];
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    const Inst* di = b->d_inst;
+    const Work* dw = b->d_work[c];
+    const int nw = b->nwork[c], ni = (int)b->inst.size();
+    const double* ga = b->gauss;
+    const double* sv = b->sinv;
+    const int* st = b->d_step + c;
+    HYPE_CK(cudaLaunchKernelEx(&cfg, tc->k, di, dw, nw, po, pc, pn, ga, sv, ni, st, s_off));
+    count_launch(1);
     return HYPE_OK;
 }
 
-static int build_chunk(hype_batch* b, int phase) {
+static int class_tick(hype_batch* b, int c, int inc) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(1);
+    cfg.blockDim = dim3(1);
+    cfg.stream = b->cs[c];
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributePriority;
+    attr.val.priority = b->prio[c];
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    HYPE_CK(cudaLaunchKernelEx(&cfg, k_tick, b->d_step + c, inc));
+    count_launch(1);
+    return HYPE_OK;
+}
+
+// a chunk of kBatchChunk steps of class c starting at level phase, one graph
+static int build_chunk(hype_batch* b, int c, int phase) {
     cudaGraph_t g;
-    HYPE_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    HYPE_CK(cudaStreamBeginCapture(b->cs[c], cudaStreamCaptureModeThreadLocal));
+    const long long l0 = hype_launch_count();
     int rc = HYPE_OK;
-    for (int s = 0; s < kBatchChunk && rc == HYPE_OK; ++s) rc = batch_launch(b, (phase + s) % 3);
-    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    for (int s = 0; s < kBatchChunk && rc == HYPE_OK; ++s) rc = class_launch(b, c, (phase + s) % 3, s);
+    if (rc == HYPE_OK) rc = class_tick(b, c, kBatchChunk);
+    cudaError_t e = cudaStreamEndCapture(b->cs[c], &g);
+    count_launch(-(hype_launch_count() - l0));  // captured, not launched
     if (rc) return rc;
     if (e != cudaSuccess) {
         set_last_error("cudaStreamEndCapture", e);
         return HYPE_ERR_CUDA;
     }
-    e = cudaGraphInstantiate(&b->chunk[phase], g, 0);
+    e = cudaGraphInstantiate(&b->chunk[c][phase], g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) {
         set_last_error("cudaGraphInstantiate", e);
@@ -219,32 +278,73 @@ static int fill_sin(hype_batch* b, int nsteps) {
             h[(size_t)s * ni + q] = sin(two_pi * b->hi[q].freq * t);
         }
     HYPE_CK(cudaMemcpyAsync(b->sinv, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, b->stream));
-    int zero = 0;
-    HYPE_CK(cudaMemcpyAsync(b->d_step, &zero, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    HYPE_CK(cudaMemsetAsync(b->d_step, 0, sizeof(int) * kMaxClasses, b->stream));
     HYPE_CK(cudaStreamSynchronize(b->stream));
     return HYPE_OK;
 }
 
+// every class advances nsteps: the classes' streams start together after the call's start
+// event and the library stream waits for all of them
 static int run_steps(hype_batch* b, int nsteps, int graph) {
     int rc;
     if ((rc = fill_sin(b, nsteps))) return rc;
-    int s = 0;
-    if (graph) {
-        while (nsteps - s >= kBatchChunk) {
-            const int phase = b->cur;
-            if (!b->chunk[phase] && (rc = build_chunk(b, phase))) return rc;
-            HYPE_CK(cudaGraphLaunch(b->chunk[phase], b->stream));
-            count_launch(2 * kBatchChunk);
-            b->cur = (b->cur + kBatchChunk) % 3;
-            s += kBatchChunk;
+    HYPE_CK(cudaEventRecord(b->ev_start, b->stream));
+    for (int c = 0; c < b->ncls; ++c) {
+        HYPE_CK(cudaStreamWaitEvent(b->cs[c], b->ev_start, 0));
+        if (b->nwork[c] > 0) {
+            int s = 0, phase = b->cur;
+            if (graph) {
+                while (nsteps - s >= kBatchChunk) {
+                    if (!b->chunk[c][phase] && (rc = build_chunk(b, c, phase))) return rc;
+                    HYPE_CK(cudaGraphLaunch(b->chunk[c][phase], b->cs[c]));
+                    count_launch(kBatchChunk + 1);
+                    phase = (phase + kBatchChunk) % 3;
+                    s += kBatchChunk;
+                }
+            }
+            for (; s < nsteps; ++s) {
+                if ((rc = class_launch(b, c, phase, 0))) return rc;
+                if ((rc = class_tick(b, c, 1))) return rc;
+                phase = (phase + 1) % 3;
+            }
         }
+        HYPE_CK(cudaEventRecord(b->ev_done[c], b->cs[c]));
+        HYPE_CK(cudaStreamWaitEvent(b->stream, b->ev_done[c], 0));
     }
-    for (; s < nsteps; ++s) {
-        if ((rc = batch_launch(b, b->cur))) return rc;
-        b->cur = (b->cur + 1) % 3;
-    }
+    b->cur = (int)((b->cur + nsteps) % 3);
     b->it += nsteps;
+    b->timed = true;
     return HYPE_OK;
+}
+
+// instances into nclasses size classes of equal count (ties by index), smallest first;
+// class c runs at the c-th highest stream priority the device offers
+static int set_classes(hype_batch* b, int nclasses) {
+    int least = 0, greatest = 0;
+    HYPE_CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    const int levels = least - greatest + 1;
+    const int ni = (int)b->inst.size();
+    int n = nclasses > 0 ? nclasses : std::min(levels, kMaxClasses);
+    n = std::max(1, std::min(std::min(n, kMaxClasses), ni));
+    HYPE_CK(cudaStreamSynchronize(b->stream));
+    for (int c = 0; c < kMaxClasses; ++c)
+        if (b->cs[c]) HYPE_CK(cudaStreamSynchronize(b->cs[c]));
+    std::vector<int> order(ni);
+    for (int q = 0; q < ni; ++q) order[q] = q;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return (long long)b->inst[x].nx * b->inst[x].ny < (long long)b->inst[y].nx * b->inst[y].ny;
+    });
+    b->cls.assign(ni, 0);
+    for (int r = 0; r < ni; ++r) b->cls[order[r]] = (int)((long long)r * n / ni);
+    b->ncls = n;
+    for (int c = 0; c < n; ++c) {
+        // smallest class: the greatest priority (numerically lowest); the rest spread over the range
+        b->prio[c] = n == 1 ? least : greatest + (int)((long long)c * (levels - 1) / (n - 1));
+        if (!b->cs[c]) HYPE_CK(cudaStreamCreateWithPriority(&b->cs[c], cudaStreamNonBlocking, b->prio[c]));
+        if (!b->ev_done[c]) HYPE_CK(cudaEventCreate(&b->ev_done[c]));
+    }
+    b->timed = false;
+    return b->tx ? build_worklist(b, b->tx, b->ty) : HYPE_OK;
 }
 
 // ------------------------------------------------------------------ autotuner
@@ -374,7 +474,8 @@ extern "C" int hype_batch_create(int ninst, const hype_mono_instance* in, hype_b
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_inst, sizeof(Inst) * ninst);
     if (e == cudaSuccess) e = cudaMemcpy(b->d_inst, b->inst.data(), sizeof(Inst) * ninst, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->gauss, sizeof(double) * goff);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_step, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_step, sizeof(int) * kMaxClasses);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev_start);
     if (e == cudaSuccess) {
         // separable Gaussian factors exp(-(x-xs)^2/(2 sig^2)), exp(-(y-ys)^2/(2 sig^2))
         std::vector<double> g(goff);
@@ -397,7 +498,8 @@ extern "C" int hype_batch_create(int ninst, const hype_mono_instance* in, hype_b
         hype_batch_destroy(b);
         return e == cudaErrorMemoryAllocation ? HYPE_ERR_NOMEM : HYPE_ERR_CUDA;
     }
-    int rc = build_worklist(b, 32, 32);
+    int rc = set_classes(b, 0);
+    if (rc == HYPE_OK) rc = build_worklist(b, 32, 32);
     if (rc) {
         hype_batch_destroy(b);
         return rc;
@@ -415,7 +517,13 @@ extern "C" void hype_batch_destroy(hype_batch* b) {
     cudaFree(b->gauss);
     cudaFree(b->sinv);
     cudaFree(b->d_step);
-    cudaFree(b->d_work);
+    for (int c = 0; c < kMaxClasses; ++c) {
+        if (b->cs[c]) cudaStreamSynchronize(b->cs[c]);
+        cudaFree(b->d_work[c]);
+        if (b->cs[c]) cudaStreamDestroy(b->cs[c]);
+        if (b->ev_done[c]) cudaEventDestroy(b->ev_done[c]);
+    }
+    if (b->ev_start) cudaEventDestroy(b->ev_start);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
@@ -456,6 +564,32 @@ extern "C" int hype_batch_get(hype_batch* b, int q, double* p_old, double* p) {
 extern "C" int hype_batch_step(hype_batch* b, int nsteps, int graph) {
     if (!b || nsteps < 0) return HYPE_ERR_ARG;
     return run_steps(b, nsteps, graph);
+}
+
+extern "C" int hype_batch_set_classes(hype_batch* b, int nclasses) {
+    if (!b || nclasses < 0) return HYPE_ERR_ARG;
+    return set_classes(b, nclasses);
+}
+
+extern "C" int hype_batch_get_classes(const hype_batch* b, int* nclasses, int* cls) {
+    if (!b || !nclasses) return HYPE_ERR_ARG;
+    *nclasses = b->ncls;
+    if (cls)
+        for (size_t q = 0; q < b->cls.size(); ++q) cls[q] = b->cls[q];
+    return HYPE_OK;
+}
+
+extern "C" int hype_batch_instance_times(hype_batch* b, double* seconds) {
+    if (!b || !seconds || !b->timed) return HYPE_ERR_ARG;
+    HYPE_CK(cudaStreamSynchronize(b->stream));
+    double t[kMaxClasses];
+    for (int c = 0; c < b->ncls; ++c) {
+        float ms = 0.0f;
+        HYPE_CK(cudaEventElapsedTime(&ms, b->ev_start, b->ev_done[c]));
+        t[c] = 1e-3 * ms;
+    }
+    for (size_t q = 0; q < b->inst.size(); ++q) seconds[q] = t[b->cls[q]];
+    return HYPE_OK;
 }
 
 extern "C" int hype_batch_sync(hype_batch* b) {

@@ -1030,6 +1030,14 @@ __device__ __forceinline__ double div_xy(double dx, double dy, double r1_h) {
 }
 __device__ __forceinline__ double div_z(double pxy, double dz, double r1_h) { return __fma_rn(-r1_h, dz, pxy); }
 
+// the FP32 form's divergence: its face fluxes are FP32 values, differenced and scaled in FP32
+// (neighbouring fluxes lie within a factor 2 of each other in smooth flow, where the FP32
+// differences are exact); only the stage combination is FP64
+__device__ __forceinline__ float div_xy_f(float dx, float dy, float r1_h) {
+    return __fmaf_rn(-r1_h, dy, __fmul_rn(-r1_h, dx));
+}
+__device__ __forceinline__ float div_z_f(float pxy, float dz, float r1_h) { return __fmaf_rn(-r1_h, dz, pxy); }
+
 // the SSP stage value a U + b W + (c dt) L (b = 1 when a = 0), explicitly rounded
 __device__ __forceinline__ double stage_value(const Stage& st, double cdt, double u, double w, double L) {
     if (st.rhs_only) return L;
@@ -1037,7 +1045,9 @@ __device__ __forceinline__ double stage_value(const Stage& st, double cdt, doubl
     return __fma_rn(cdt, L, __fma_rn(st.b, w, __dmul_rn(st.a, u)));
 }
 
-// U, W and out may be one array (in-place stages), so they carry no __restrict__
+// U, W and out may be one array (in-place stages), so they carry no __restrict__.
+// F32: the face fluxes hold FP32 values (the FP32 form); the divergence is formed in FP32
+template <bool F32 = false>
 __global__ void __launch_bounds__(256) k_update(const double* __restrict__ Fx, const double* __restrict__ Fy,
                                                 const double* __restrict__ Fz, const double* U,
                                                 const double* W, double* out, Geo g, double r1_h,
@@ -1055,8 +1065,17 @@ __global__ void __launch_bounds__(256) k_update(const double* __restrict__ Fx, c
     const double cdt = st.rhs_only ? 0.0 : st.c * ds->dt;
 #pragma unroll
     for (int c = 0; c < NV; ++c) {
-        const double pxy = div_xy(Fx[c * nfx + ix + 1] - Fx[c * nfx + ix], Fy[c * nfy + iy + g.nx] - Fy[c * nfy + iy], r1_h);
-        const double L = div_z(pxy, Fz[c * nfz + iz + (long long)g.nx * g.ny] - Fz[c * nfz + iz], r1_h);
+        double L;
+        if constexpr (F32) {
+            const float r1hf = (float)r1_h;
+            const float pxy = div_xy_f((float)Fx[c * nfx + ix + 1] - (float)Fx[c * nfx + ix],
+                                       (float)Fy[c * nfy + iy + g.nx] - (float)Fy[c * nfy + iy], r1hf);
+            L = df_f2d(div_z_f(pxy, (float)Fz[c * nfz + iz + (long long)g.nx * g.ny] - (float)Fz[c * nfz + iz], r1hf));
+        } else {
+            const double pxy =
+                div_xy(Fx[c * nfx + ix + 1] - Fx[c * nfx + ix], Fy[c * nfy + iy + g.nx] - Fy[c * nfy + iy], r1_h);
+            L = div_z(pxy, Fz[c * nfz + iz + (long long)g.nx * g.ny] - Fz[c * nfz + iz], r1_h);
+        }
         const double u = (!st.rhs_only && st.a != 0.0) ? U[c * g.N + cell] : 0.0;
         const double w = st.rhs_only ? 0.0 : W[c * g.N + cell];
         out[c * g.N + cell] = stage_value(st, cdt, u, w, L);
@@ -1079,7 +1098,7 @@ __global__ void __launch_bounds__(256) k_update(const double* __restrict__ Fx, c
 // cells per plane).  The block marches its tile along z; the +z traces of a plane stay in the
 // thread's registers as the -z side of the next plane's z faces, and each cell's divergence
 // is completed one plane later, when its +z face flux exists.  Blocks are persistent, one per
-// SM (the trace array takes 180 KB of shared memory), and split the tiles' planes into equal
+// SM (the trace and flux arrays take 188 KB of shared memory), and split the tiles' planes into equal
 // contiguous runs: a run re-reconstructs one plane below and one above it.
 // Every arithmetic step is the unfused kernels' (cweno4 / weno3, face_traces, rusanov, the
 // admissibility test and the divergence use the same device functions and explicit roundings),
@@ -1088,8 +1107,9 @@ constexpr int FS_TW = 12;                        // warps per block (at most 168
 constexpr int FS_NT = 32 * FS_TW;                // 384 threads
 constexpr int FS_OX = 30, FS_OY = FS_TW - 2;     // owned tile: 30 x 10 cells
 constexpr int FS_NQ = NV * NTR;                  // traces per cell
-// traces [c][q][thread] (FP32): 184,320 B, which leaves 60 KB of the SM's L1 for the stencil gathers
-constexpr size_t FS_SMEM = sizeof(float) * FS_NQ * FS_NT;
+// traces [c][q][thread] and the -y face fluxes [c][thread] (FP32): 192,000 B, which leaves 60 KB of
+// the SM's L1 for the stencil gathers
+constexpr size_t FS_SMEM = sizeof(float) * (FS_NQ + NV) * FS_NT;
 
 __host__ __device__ inline long long fs_tiles_x(int nx) { return (nx + FS_OX - 1) / FS_OX; }
 __host__ __device__ inline long long fs_tiles_y(int ny) { return (ny + FS_OY - 1) / FS_OY; }
@@ -1097,7 +1117,7 @@ __host__ __device__ inline long long fs_tiles_y(int ny) { return (ny + FS_OY - 1
 // one Rusanov face (weight 1/8 per Gauss point, as k_faces): L side trace q0L.., R side q0R..
 // read from the shared trace array (columns tL, tR) or, for the z faces' low side, from registers
 __device__ __forceinline__ void fs_face(const float* __restrict__ S, int tL, int tR, int qL, int qR,
-                                        const float (*zl)[4], float gm, float gm1, double* Fd, double& smax,
+                                        const float (*zl)[4], float gm, float gm1, float* Fd, float& smax,
                                         bool& bad, int D) {
     float acc[NV];
 #pragma unroll
@@ -1114,12 +1134,12 @@ __device__ __forceinline__ void fs_face(const float* __restrict__ S, int tL, int
         if (D == 0) s = rusanov<float, 0, false>(QL, QR, gm, gm1, fl, bad);
         else if (D == 1) s = rusanov<float, 1, false>(QL, QR, gm, gm1, fl, bad);
         else s = rusanov<float, 2, false>(QL, QR, gm, gm1, fl, bad);
-        smax = fmax(smax, (double)s);
+        smax = fmaxf(smax, s);
 #pragma unroll
         for (int c = 0; c < NV; ++c) acc[c] += 0.125f * fl[c];
     }
 #pragma unroll
-    for (int c = 0; c < NV; ++c) Fd[c] = (double)acc[c];
+    for (int c = 0; c < NV; ++c) Fd[c] = acc[c];
 }
 
 __device__ __forceinline__ void fs_bad(DevScalars* ds, const Geo& g, int i, int j, int k) {
@@ -1127,20 +1147,69 @@ __device__ __forceinline__ void fs_bad(DevScalars* ds, const Geo& g, int i, int 
     atomicMin(&ds->bad, (unsigned long long)(((long long)ck * g.ny + cj) * g.nx + ci));
 }
 
+// one cell's 24 traces of every variable into its column of the shared array (linear: R4)
+__device__ __forceinline__ void fs_recon_cell(float* __restrict__ S, const float* __restrict__ G, const Geo& g,
+                                              long long ge, int t, bool linear, bool weno) {
+    const int sy = g.gx, sz = g.gx * g.gy;
+#pragma unroll 1
+    for (int c = 0; c < NV; ++c) {
+        float s[33], cf[20], tr[8];
+        gather33g<float>(G + (long long)c * g.GN + ge, sy, sz, s);
+        if (weno) weno3<float>(s, cf);
+        else cweno4<float>(s, linear, cf);
+        float* Sc = S + (c * NTR) * FS_NT + t;
+        face_traces<float, 0>(cf, tr);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) Sc[q * FS_NT] = tr[q];
+        face_traces<float, 1>(cf, tr);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) Sc[(8 + q) * FS_NT] = tr[q];
+        face_traces<float, 2>(cf, tr);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) Sc[(16 + q) * FS_NT] = tr[q];
+    }
+}
+
+// the cell's 24 traces (its own column) against the density / pressure floors
+__device__ __forceinline__ bool fs_admissible(const float* __restrict__ S, int t, float gm1) {
+    bool ok = true;
+#pragma unroll 4
+    for (int q = 0; q < NTR; ++q) {
+        const float rho = S[(0 * NTR + q) * FS_NT + t];
+        float m2 = __fmul_rn(S[(1 * NTR + q) * FS_NT + t], S[(1 * NTR + q) * FS_NT + t]);
+        m2 = __fmaf_rn(S[(2 * NTR + q) * FS_NT + t], S[(2 * NTR + q) * FS_NT + t], m2);
+        m2 = __fmaf_rn(S[(3 * NTR + q) * FS_NT + t], S[(3 * NTR + q) * FS_NT + t], m2);
+        ok = ok && adm_f32(rho, m2, S[(4 * NTR + q) * FS_NT + t], gm1);
+    }
+    return ok;
+}
+
+// per warp, the network inputs (96 BF16 rows) and logits while the learned gate scores a plane
+constexpr int FS_STAGE_FLOATS = (mlp::ROWS * mlp::RSTRIDE * 2 + mlp::ROWS * 4) / 4;  // 2016
+static_assert(FS_STAGE_FLOATS * FS_TW <= FS_NQ * FS_NT, "gate staging fits the trace array");
+static_assert((FS_STAGE_FLOATS * 4) % 16 == 0, "staging rows stay 16-byte aligned");
+
+// LEARNED: the indicator gate of k_recon_learned folded in -- the network scores each cell from
+// its three directional 5-point stencils on the tensor cores (mma.sync BF16, FP32 accumulation);
+// flagged or low-confidence cells take CWENO4, the others R4, and a cell whose R4 traces break the
+// floors is redone with CWENO4 (then first order with the positivity fallback)
+template <bool LEARNED>
 __global__ void __launch_bounds__(FS_NT, 1)
     k_stage_f32(const float* __restrict__ G, const double* U, const double* W, double* out, Geo g, int recon, int pad,
                 double gamma, double r1_h, Stage st, DevScalars* __restrict__ ds, int slot,
-                unsigned long long* __restrict__ counters) {
-    extern __shared__ float S[];  // traces [c][q][thread]
+                unsigned long long* __restrict__ counters, const mlp::MmaWeights* __restrict__ wts = nullptr,
+                float logit_thr = 0.0f) {
+    extern __shared__ float S[];  // traces [c][q][thread], then the -y face fluxes [c][thread]
+    float* SFy = S + FS_NQ * FS_NT;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const float gm = (float)gamma, gm1 = (float)(gamma - 1.0);
-    const int sy = g.gx, sz = g.gx * g.gy;
     const long long tiles_x = fs_tiles_x(g.nx);
     const long long total = tiles_x * fs_tiles_y(g.ny) * g.nz;  // plane-units
     const long long b0 = (long long)blockIdx.x * total / gridDim.x, b1 = (long long)(blockIdx.x + 1) * total / gridDim.x;
     const double cdt = st.rhs_only ? 0.0 : st.c * ds->dt;
-    double smax = 0.0;
-    unsigned nfall = 0;
+    const float r1h = (float)r1_h;
+    float smax = 0.0f;
+    unsigned nfall = 0, nflag = 0;
     for (long long pos = b0; pos < b1;) {
         const long long tile = pos / g.nz;
         const int kb = (int)(pos - tile * g.nz);
@@ -1154,11 +1223,11 @@ __global__ void __launch_bounds__(FS_NT, 1)
         const bool owned = own_x && own_y;
         const bool ring = (ring_x && own_y) || (own_x && ring_y);
         float zp[NV][4];    // +z traces of the previous plane
-        double Fzp[NV];     // flux of the previous plane's -z face
-        double Pp[NV];      // x/y part of the previous plane's divergence
+        float Fzp[NV];      // flux of the previous plane's -z face
+        float Pp[NV];       // x/y part of the previous plane's divergence
 #pragma unroll
         for (int c = 0; c < NV; ++c) {
-            Fzp[c] = Pp[c] = 0.0;
+            Fzp[c] = Pp[c] = 0.0f;
 #pragma unroll
             for (int q = 0; q < 4; ++q) zp[c][q] = 0.0f;
         }
@@ -1166,46 +1235,63 @@ __global__ void __launch_bounds__(FS_NT, 1)
         for (int k = kb - 1; k <= ke; ++k) {
             const bool edge = (k == kb - 1) || (k == ke);  // only the z traces of owned columns are used
             const bool active = owned || (ring && !edge);
+            const long long ge = active ? ghost_index(g, i, j, k) : 0;
+            bool full = false;
+            float best = 0.0f;
+            if constexpr (LEARNED) {
+                // the warp's 32 cells x 3 directions staged as BF16 rows in the (free) trace array
+                __nv_bfloat16* rows = reinterpret_cast<__nv_bfloat16*>(S + w * FS_STAGE_FLOATS);
+                float* lg = reinterpret_cast<float*>(rows + mlp::ROWS * mlp::RSTRIDE);
+                __nv_bfloat16* my_rows = rows + lane * 3 * mlp::RSTRIDE;
+                float sc[NV];
+                if (active) {
+                    const float rho = __ldg(G + ge), E = __ldg(G + 4 * g.GN + ge);
+#pragma unroll
+                    for (int c = 0; c < NV; ++c) sc[c] = mlp::var_scale<float>(c, rho, E);
+                }
+#pragma unroll 1
+                for (int d = 0; d < 3; ++d) {
+                    float x[mlp::NIN];
+                    const int stp = d == 0 ? 1 : d == 1 ? g.gx : g.gx * g.gy;
+                    if (active) {
+#pragma unroll
+                        for (int c = 0; c < NV; ++c) {
+                            const float* p = G + (long long)c * g.GN + ge;
+                            float s5[5];
+#pragma unroll
+                            for (int o = 0; o < 5; ++o) s5[o] = __ldg(p + (o - 2) * stp);
+                            mlp::normalise5(s5, sc[c], x + c * 5);
+                        }
+                    }
+                    mlp::stage_row(my_rows + d * mlp::RSTRIDE, x, active);
+                }
+                __syncwarp();
+                mlp::warp_logits(wts, rows, lg);
+                __syncwarp();
+                best = fmaxf(lg[lane * 3], fmaxf(lg[lane * 3 + 1], lg[lane * 3 + 2]));
+                full = best > logit_thr;
+                __syncthreads();  // every warp's rows read before the traces overwrite the array
+            }
             // ---- reconstruction: all 24 traces of each variable into the shared array
             if (active) {
-                const long long ge = ghost_index(g, i, j, k);
-#pragma unroll 1
-                for (int c = 0; c < NV; ++c) {
-                    float s[33], cf[20], tr[8];
-                    gather33g<float>(G + (long long)c * g.GN + ge, sy, sz, s);
-                    if (recon == HYPE_RECON_WENO3) weno3<float>(s, cf);
-                    else cweno4<float>(s, recon == HYPE_RECON_LINEAR4, cf);
-                    float* Sc = S + (c * NTR) * FS_NT + t;
-                    face_traces<float, 0>(cf, tr);
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) Sc[q * FS_NT] = tr[q];
-                    face_traces<float, 1>(cf, tr);
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) Sc[(8 + q) * FS_NT] = tr[q];
-                    face_traces<float, 2>(cf, tr);
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) Sc[(16 + q) * FS_NT] = tr[q];
+                const bool weno = !LEARNED && recon == HYPE_RECON_WENO3;
+                fs_recon_cell(S, G, g, ge, t, LEARNED ? !full : recon == HYPE_RECON_LINEAR4, weno);
+                bool ok = (LEARNED || pad) ? fs_admissible(S, t, gm1) : true;
+                if (LEARNED && !ok && !full) {  // the R4 traces broke positivity: the cell with CWENO4
+                    full = true;
+                    fs_recon_cell(S, G, g, ge, t, false, false);
+                    ok = fs_admissible(S, t, gm1);
                 }
-                // positivity fallback: the cell's 24 traces against the floors, first order if any fails
-                if (pad) {
-                    bool ok = true;
-#pragma unroll 4
-                    for (int q = 0; q < NTR; ++q) {
-                        const float rho = S[(0 * NTR + q) * FS_NT + t];
-                        float m2 = __fmul_rn(S[(1 * NTR + q) * FS_NT + t], S[(1 * NTR + q) * FS_NT + t]);
-                        m2 = __fmaf_rn(S[(2 * NTR + q) * FS_NT + t], S[(2 * NTR + q) * FS_NT + t], m2);
-                        m2 = __fmaf_rn(S[(3 * NTR + q) * FS_NT + t], S[(3 * NTR + q) * FS_NT + t], m2);
-                        ok = ok && adm_f32(rho, m2, S[(4 * NTR + q) * FS_NT + t], gm1);
-                    }
-                    if (!ok) {
+                // positivity fallback: first order when the traces still break the floors
+                if (!ok && pad) {
 #pragma unroll 1
-                        for (int c = 0; c < NV; ++c) {
-                            const float v = __ldg(G + (long long)c * g.GN + ge);
-                            for (int q = 0; q < NTR; ++q) S[(c * NTR + q) * FS_NT + t] = v;
-                        }
-                        if (owned && !edge) ++nfall;
+                    for (int c = 0; c < NV; ++c) {
+                        const float v = __ldg(G + (long long)c * g.GN + ge);
+                        for (int q = 0; q < NTR; ++q) S[(c * NTR + q) * FS_NT + t] = v;
                     }
+                    if (owned && !edge) ++nfall;
                 }
+                if (LEARNED && full && owned && !edge && best > logit_thr) ++nflag;
             }
             __syncthreads();
             // ---- Rusanov fluxes of the owned cells' faces: -x (the ring lane at the high side gives
@@ -1215,7 +1301,7 @@ __global__ void __launch_bounds__(FS_NT, 1)
             const bool plane = (k >= kb) && (k < ke);
             // z face first: it completes the previous plane (its stage value), then frees zp
             if (k >= kb && owned) {
-                double Fz[NV];
+                float Fz[NV];
                 bool b = false;
                 fs_face(S, t, t, 0, 16, zp, gm, gm1, Fz, smax, b, 2);  // L: registers (zl), R: own -z (q 16..19)
                 if (b) fs_bad(ds, g, i, j, k);
@@ -1223,7 +1309,7 @@ __global__ void __launch_bounds__(FS_NT, 1)
                     const long long cell = ((long long)(k - 1) * g.ny + j) * g.nx + i;
 #pragma unroll
                     for (int c = 0; c < NV; ++c) {
-                        const double L = div_z(Pp[c], Fz[c] - Fzp[c], r1_h);
+                        const double L = df_f2d(div_z_f(Pp[c], Fz[c] - Fzp[c], r1h));
                         const double u = (!st.rhs_only && st.a != 0.0) ? U[c * g.N + cell] : 0.0;
                         const double wv = st.rhs_only ? 0.0 : W[c * g.N + cell];
                         out[c * g.N + cell] = stage_value(st, cdt, u, wv, L);
@@ -1240,11 +1326,11 @@ __global__ void __launch_bounds__(FS_NT, 1)
             }
             // x faces: every lane its -x face (the ring lane at the high side gives the last cell's +x),
             // the +x flux from the right neighbour lane
-            double dF[NV];
+            float dF[NV];
             {
-                double Fxl[NV];
+                float Fxl[NV];
 #pragma unroll
-                for (int c = 0; c < NV; ++c) Fxl[c] = 0.0;
+                for (int c = 0; c < NV; ++c) Fxl[c] = 0.0f;
                 if (plane && own_y && (own_x || i == ihi)) {
                     bool b = false;
                     fs_face(S, t - 1, t, 4, 0, nullptr, gm, gm1, Fxl, smax, b, 0);
@@ -1253,26 +1339,30 @@ __global__ void __launch_bounds__(FS_NT, 1)
 #pragma unroll
                 for (int c = 0; c < NV; ++c) dF[c] = __shfl_down_sync(0xffffffffu, Fxl[c], 1) - Fxl[c];
             }
-            // y faces: each owned cell solves its -y and +y faces (both of its neighbours' rows are in
-            // the shared array; no flux exchange between warps)
-            if (plane && owned) {
-                double Fl[NV], Fh[NV];
+            // y faces: each owned cell and the ring row at the high side its -y face, shared through
+            // the flux array (the row above gives each owned cell its +y face)
+            float Fyl[NV];
+            if (plane && own_x && (own_y || j == jhi)) {
                 bool b = false;
-                fs_face(S, t - 32, t, 12, 8, nullptr, gm, gm1, Fl, smax, b, 1);
+                fs_face(S, t - 32, t, 12, 8, nullptr, gm, gm1, Fyl, smax, b, 1);
                 if (b) fs_bad(ds, g, i, j, k);
-                b = false;
-                fs_face(S, t, t + 32, 12, 8, nullptr, gm, gm1, Fh, smax, b, 1);
-                if (b) fs_bad(ds, g, i, j + 1, k);
 #pragma unroll
-                for (int c = 0; c < NV; ++c) Pp[c] = div_xy(dF[c], Fh[c] - Fl[c], r1_h);
+                for (int c = 0; c < NV; ++c) SFy[c * FS_NT + t] = Fyl[c];
             }
-            __syncthreads();  // every trace of the plane read before the next plane's are written
+            __syncthreads();  // every trace read (the next plane may overwrite them), -y fluxes written
+            if (plane && owned) {
+#pragma unroll
+                for (int c = 0; c < NV; ++c) Pp[c] = div_xy_f(dF[c], SFy[c * FS_NT + t + 32] - Fyl[c], r1h);
+            }
+            // the flux array is next written after the next plane's first barrier, when every
+            // thread has read it
         }
     }
-    if (pad && nfall) atomicAdd(&counters[1], (unsigned long long)nfall);
+    if (nfall) atomicAdd(&counters[1], (unsigned long long)nfall);
+    if (LEARNED && nflag) atomicAdd(&counters[0], (unsigned long long)nflag);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, o));
-    if (lane == 0 && smax > 0.0) atomic_max_pos(&ds->smax_bits[slot], smax);
+    for (int o = 16; o > 0; o >>= 1) smax = fmaxf(smax, __shfl_xor_sync(0xffffffffu, smax, o));
+    if (lane == 0 && smax > 0.0f) atomic_max_pos(&ds->smax_bits[slot], (double)smax);
 }
 
 // the stage combination alone, from an RHS already in L (the first stage of a step whose dt
@@ -1624,7 +1714,10 @@ static int launch_update(hype_euler* e, const double* U, const double* W, double
     const Geo& g = e->g;
     const dim3 b(32, 8), gr(cdiv(g.nx, 32), cdiv(g.ny, 8), g.nz);
     prof_mark(e, 2, true);
-    k_update<<<gr, b, 0, e->stream>>>(e->Fx, e->Fy, e->Fz, U, W, out, g, 1.0 / e->p.h, st, e->ds);
+    if (e->p.precision == HYPE_PREC_FP32)
+        k_update<true><<<gr, b, 0, e->stream>>>(e->Fx, e->Fy, e->Fz, U, W, out, g, 1.0 / e->p.h, st, e->ds);
+    else
+        k_update<false><<<gr, b, 0, e->stream>>>(e->Fx, e->Fy, e->Fz, U, W, out, g, 1.0 / e->p.h, st, e->ds);
     prof_mark(e, 2, false);
     HYPE_LAUNCHED(1);
     return HYPE_OK;
@@ -1634,7 +1727,7 @@ static int launch_update(hype_euler* e, const double* U, const double* W, double
 static bool uses_fused(const hype_euler* e) {
     return e->stage_mode == HYPE_STAGE_AUTO && e->p.precision == HYPE_PREC_FP32 && e->p.flux == HYPE_FLUX_RUSANOV &&
            !e->C4 && (e->p.recon == HYPE_RECON_CWENO4 || e->p.recon == HYPE_RECON_LINEAR4 ||
-                      e->p.recon == HYPE_RECON_WENO3);
+                      e->p.recon == HYPE_RECON_WENO3 || (e->p.recon == HYPE_RECON_LEARNED && e->mlp));
 }
 
 // the unfused kernels' face traces and face fluxes, allocated on first use (never inside a
@@ -1677,8 +1770,14 @@ static int launch_stage(hype_euler* e, const double* Win, const double* U, const
     prof_mark(e, 1, true);
     const long long units = fs_tiles_x(g.nx) * fs_tiles_y(g.ny) * g.nz;
     const unsigned blocks = (unsigned)std::min<long long>(e->nsm, units);
-    k_stage_f32<<<blocks, FS_NT, FS_SMEM, e->stream>>>((const float*)e->G, U, W, out, g, e->p.recon, e->p.positivity,
-                                                      e->p.gamma, 1.0 / e->p.h, st, e->ds, slot, e->mlp_cnt);
+    if (e->p.recon == HYPE_RECON_LEARNED)
+        k_stage_f32<true><<<blocks, FS_NT, FS_SMEM, e->stream>>>((const float*)e->G, U, W, out, g, e->p.recon,
+                                                                e->p.positivity, e->p.gamma, 1.0 / e->p.h, st, e->ds,
+                                                                slot, e->mlp_cnt, e->mlp, e->logit_thr);
+    else
+        k_stage_f32<false><<<blocks, FS_NT, FS_SMEM, e->stream>>>((const float*)e->G, U, W, out, g, e->p.recon,
+                                                                 e->p.positivity, e->p.gamma, 1.0 / e->p.h, st, e->ds,
+                                                                 slot, e->mlp_cnt);
     prof_mark(e, 1, false);
     HYPE_LAUNCHED(2);
     return HYPE_OK;
@@ -1773,12 +1872,17 @@ extern "C" int hype_euler_create(const hype_euler_params* p, hype_euler** out) {
         ce = cudaGetDevice(&dev);
         if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, dev);
         if (ce == cudaSuccess)
-            ce = cudaFuncSetAttribute(k_stage_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FS_SMEM);
+            ce = cudaFuncSetAttribute(k_stage_f32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FS_SMEM);
+        if (ce == cudaSuccess)
+            ce = cudaFuncSetAttribute(k_stage_f32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FS_SMEM);
         if (ce != cudaSuccess) {
             set_last_error("hype_euler_create (device attributes)", ce);
             return fail(HYPE_ERR_CUDA);
         }
-        if ((rc = prepare(e))) return fail(rc);
+        // the FP32 Rusanov form runs fused (the learned gate too, once its network is set): no trace
+        // buffers up front; every other form allocates them now
+        const bool fusable = p->precision == HYPE_PREC_FP32 && p->flux == HYPE_FLUX_RUSANOV && !visc;
+        if (!fusable && (rc = prepare(e))) return fail(rc);
     }
     ce = cudaMemset(e->mlp_cnt, 0, 2 * sizeof(unsigned long long));
     if (ce != cudaSuccess) {
@@ -2242,7 +2346,10 @@ extern "C" int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* 
     launch_faces(g, T, Fx, Fy, Fz, p->gamma, ds, 4, p->precision == HYPE_PREC_FP32, p->flux, s);
     const Stage st{0.0, 0.0, 0.0, 1};
     const dim3 bu(32, 8), gu(cdiv(g.nx, 32), cdiv(g.ny, 8), g.nz);
-    k_update<<<gu, bu, 0, s>>>(Fx, Fy, Fz, nullptr, nullptr, dRHS, g, 1.0 / p->h, st, ds);
+    if (p->precision == HYPE_PREC_FP32)
+        k_update<true><<<gu, bu, 0, s>>>(Fx, Fy, Fz, nullptr, nullptr, dRHS, g, 1.0 / p->h, st, ds);
+    else
+        k_update<false><<<gu, bu, 0, s>>>(Fx, Fy, Fz, nullptr, nullptr, dRHS, g, 1.0 / p->h, st, ds);
     HYPE_LAUNCHED(7);
     if (dt_out) {
         unsigned long long w[2];

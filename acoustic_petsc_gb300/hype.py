@@ -340,6 +340,23 @@ class BatchLeapfrog:
     def step(self, nsteps: int, graph: bool = True):
         check(L.lib().hype_batch_step(self._h, int(nsteps), int(bool(graph))), "hype_batch_step")
 
+    def set_classes(self, nclasses: int = 0):
+        """size classes on prioritised streams (0: one per device priority level; 1: none)"""
+        check(L.lib().hype_batch_set_classes(self._h, int(nclasses)), "hype_batch_set_classes")
+
+    def classes(self):
+        """(number of classes, each instance's class)"""
+        n = C.c_int()
+        cls = (C.c_int * len(self.instances))()
+        check(L.lib().hype_batch_get_classes(self._h, C.byref(n), cls), "hype_batch_get_classes")
+        return n.value, np.array(cls[:], dtype=np.int64)
+
+    def instance_times(self):
+        """seconds from the start of the last step() call to each instance's completion (device events)"""
+        t = np.empty(len(self.instances))
+        check(L.lib().hype_batch_instance_times(self._h, _dp(t)), "hype_batch_instance_times")
+        return t
+
     def sync(self):
         check(L.lib().hype_batch_sync(self._h), "hype_batch_sync")
 

@@ -516,9 +516,23 @@ int hype_batch_get_tile(const hype_batch* b, int* tile_x, int* tile_y);
 /* initial levels of instance q (host arrays ny*nx) */
 int hype_batch_set(hype_batch* b, int q, const double* p_old, const double* p);
 int hype_batch_get(hype_batch* b, int q, double* p_old, double* p);
-/* nsteps of every instance; graph=1 replays a captured CUDA graph of the step */
+/* nsteps of every instance; graph=1 replays captured CUDA graphs of 30-step chunks */
 int hype_batch_step(hype_batch* b, int nsteps, int graph);
 int hype_batch_sync(hype_batch* b);
+/* Scheduling (no counterpart in the reference, whose instances are separate runs of
+ * 2d/ctcs/line_source/wave.c:98-111): the instances are split by node count into
+ * nclasses classes of equal size, smallest first; each class runs on its own stream
+ * and its kernels carry a launch priority, the smallest class the highest, so small
+ * instances finish early while the larger ones fill the rest of the GPU.  nclasses = 0:
+ * as many classes as the device has stream priority levels (at most 8); 1: all
+ * instances advance together.  Results do not depend on it. */
+int hype_batch_set_classes(hype_batch* b, int nclasses);
+/* the number of classes and, when cls is not NULL, each instance's class */
+int hype_batch_get_classes(const hype_batch* b, int* nclasses, int* cls);
+/* completion time of every instance in the last hype_batch_step call, in seconds from
+ * the call's start on the device timeline (CUDA events; an instance completes with its
+ * class); waits for the call */
+int hype_batch_instance_times(hype_batch* b, double* seconds);
 
 /* ============================================================ indicator training */
 int hype_mlp_nparam(void);

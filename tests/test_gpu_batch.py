@@ -64,3 +64,40 @@ def test_full_batch_workload_vs_oracle(hype, oracle):
     b.close()
     print(f"256 instances, 150 steps: worst relative L-inf {worst:.2e}")
     assert worst <= TOL
+
+
+def test_size_classes_do_not_change_results(hype):
+    """the size classes (own streams, launch priorities) touch disjoint parts of the level
+    pools: any number of classes gives bit-identical instances"""
+    inst = _instances(9, seed=13)
+    res = []
+    for ncls in (1, 0, 3, 9):
+        b = hype.BatchLeapfrog([hype.Monopole(**m) for m in inst], tile=(32, 32))
+        b.set_classes(ncls)
+        b.step(47)
+        b.step(31)
+        res.append([b.get(q) for q in range(len(inst))])
+        b.close()
+    for r in res[1:]:
+        for (a0, p0), (a1, p1) in zip(res[0], r):
+            assert np.array_equal(a0, a1) and np.array_equal(p0, p1)
+
+
+def test_instance_completion_times(hype):
+    """each instance's completion time of a call: positive, equal within a class, and the
+    smallest class (highest priority) done no later than the largest"""
+    inst = _instances(24, seed=17, nmin=40, nmax=400)
+    b = hype.BatchLeapfrog([hype.Monopole(**m) for m in inst], tile=(32, 32))
+    b.set_classes(0)
+    n, cls = b.classes()
+    b.step(120)
+    t = b.instance_times()
+    assert n >= 1 and cls.min() == 0 and cls.max() == n - 1
+    assert (t > 0).all()
+    for c in range(n):
+        assert np.ptp(t[cls == c]) == 0.0
+    sizes = np.array([m["nx"] * m["ny"] for m in inst])
+    assert sizes[cls == 0].max() <= sizes[cls == n - 1].min()
+    assert t[cls == 0][0] <= t[cls == n - 1][0]
+    print(f"{n} classes; completion times {sorted(set(np.round(t * 1e3, 3)))} ms")
+    b.close()

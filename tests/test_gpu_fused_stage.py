@@ -126,3 +126,30 @@ def test_fused_256_three_steps(hype):
         s.close()
     assert np.array_equal(res[0][0], res[1][0])
     assert res[0][1] == res[1][1] and res[0][2] == res[1][2]
+
+
+def test_fused_learned_gate_equals_unfused(hype):
+    """the indicator gate folded into the fused stage (scoring on the tensor cores, R4 or CWENO4
+    per cell, CWENO4 redo on an R4 positivity break, first order after that) against the
+    unfused k_recon_learned path: bit-identical states and the same flagged / fallback counts"""
+    from test_gpu_indicator import _train_on_blast
+
+    from acoustic_petsc_gb300 import workloads
+
+    p, _, _, _ = _train_on_blast(hype)
+    n = 40
+    U = workloads.euler_blast(n)
+    a, b = _pair(hype, (n, n, n), recon=hype._lib.RECON_LEARNED, positivity=1)
+    stats = []
+    for s in (a, b):
+        s.set_mlp(p, 0.2)
+        s.set_state(U)
+        s.indicator_stats(reset=True)
+        s.step(1)
+        s.step(9)
+        stats.append(s.indicator_stats())
+    assert np.array_equal(a.get_state(), b.get_state())
+    assert a.t == b.t and a.next_dt == b.next_dt
+    assert stats[0] == stats[1]
+    assert stats[0][0] > 0
+    print(f"learned blast {n}^3 FP32, 10 steps: flagged {stats[0][0]}, fallbacks {stats[0][1]} in both forms")
