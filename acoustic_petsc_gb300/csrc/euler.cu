@@ -1142,6 +1142,9 @@ __device__ __forceinline__ void fs_face(const float* __restrict__ S, int tL, int
     for (int c = 0; c < NV; ++c) Fd[c] = acc[c];
 }
 
+// a hint that the line holding *a will be read soon (into L2); a must lie inside its array
+__device__ __forceinline__ void prefetch_l2(const void* a) { asm volatile("prefetch.global.L2 [%0];" ::"l"(a)); }
+
 __device__ __forceinline__ void fs_bad(DevScalars* ds, const Geo& g, int i, int j, int k) {
     const int ci = i < g.nx ? i : g.nx - 1, cj = j < g.ny ? j : g.ny - 1, ck = k < g.nz ? k : g.nz - 1;
     atomicMin(&ds->bad, (unsigned long long)(((long long)ck * g.ny + cj) * g.nx + ci));
@@ -1271,6 +1274,32 @@ __global__ void __launch_bounds__(FS_NT, 1)
                 best = fmaxf(lg[lane * 3], fmaxf(lg[lane * 3 + 1], lg[lane * 3 + 2]));
                 full = best > logit_thr;
                 __syncthreads();  // every warp's rows read before the traces overwrite the array
+            }
+            // ---- L2 prefetch, one plane ahead of use: the ghosted input three planes up (the leading
+            // plane of the next plane's stencils; the ring rows' warps also take the two rows beyond
+            // them), and the stage inputs of this plane, read by the update at the next plane
+            if (k + 3 <= g.nz + GW - 1 && (active || (ring_x && own_y) || (own_x && ring_y))) {
+                const long long gp = ghost_index(g, i, j, k + 3);
+#pragma unroll
+                for (int c = 0; c < NV; ++c) {
+                    const float* a = G + (long long)c * g.GN + gp;
+                    prefetch_l2(a);
+                    if (w == 0 && own_x) {
+                        prefetch_l2(a - g.gx);
+                        prefetch_l2(a - 2 * g.gx);
+                    } else if (j == jhi && own_x) {
+                        prefetch_l2(a + g.gx);
+                        prefetch_l2(a + 2 * g.gx);
+                    }
+                }
+            }
+            if (owned && k >= kb && k < ke && !st.rhs_only) {
+                const long long cell = ((long long)k * g.ny + j) * g.nx + i;
+#pragma unroll
+                for (int c = 0; c < NV; ++c) {
+                    prefetch_l2(W + c * g.N + cell);
+                    if (st.a != 0.0) prefetch_l2(U + c * g.N + cell);
+                }
             }
             // ---- reconstruction: all 24 traces of each variable into the shared array
             if (active) {
