@@ -700,6 +700,135 @@ def run_blast(args, ws, rank, local, n=512, ntrain=64, tau=0.01, prob=0.2):
             "gpu_launches": launches, "clocks": clocks}
 
 
+def _train_blast_indicator(H, ntrain=64, tau=0.01, prob=0.2):
+    """the troubled-cell network trained on the GPU from solver labels of a small blast run"""
+    from acoustic_petsc_gb300 import indicator, workloads
+
+    tr = H.EulerSolver(H.AppCtx(N_x=ntrain, N_y=ntrain, N_z=ntrain, h=1.0 / ntrain, CFL=0.4, positivity=1,
+                                precision=H._lib.PREC_FP32))
+    tr.set_state(workloads.euler_blast(ntrain))
+    Xs, Ds = [], []
+    for _ in range(6):
+        tr.step(4)
+        X, D = indicator.sample(tr)
+        Xs.append(X)
+        Ds.append(D)
+    tr.close()
+    X, D = np.concatenate(Xs), np.concatenate(Ds)
+    y = indicator.labels(D, tau)
+    t0 = time.perf_counter()
+    params, loss = indicator.train(X, y, epochs=10, batch=4096, lr=3e-3, seed=0)
+    t_train = time.perf_counter() - t0
+    recall, precision, flagged = indicator.recall_precision(indicator.score(X, params), y, prob)
+    meta = {"train_grid": ntrain, "samples": int(X.shape[0]), "tau": tau, "prob_threshold": prob,
+            "train_s": t_train, "final_loss": loss, "recall": recall, "precision": precision,
+            "flagged_train": flagged}
+    return params, meta
+
+
+def _blast_form(H, n, U0, precision, recon, params, prob, dt, nsteps):
+    """one form of the blast run with a fixed dt; returns its density and timing / counts"""
+    import torch
+
+    L = H.lib()
+    ctx = H.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, positivity=1, precision=precision, recon=recon,
+                   dt_mode=H._lib.DT_FIXED)
+    s = H.EulerSolver(ctx)
+    if recon == H._lib.RECON_LEARNED:
+        s.set_mlp(params, prob)
+    s.set_state(U0)
+    s.indicator_stats(reset=True)
+    stream = torch.cuda.ExternalStream(L.hype_euler_stream(s._h))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    s.step(nsteps, dt=dt)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    flagged, fb = s.indicator_stats()
+    rho = np.ascontiguousarray(s.get_state()[..., 0])
+    t = s.t
+    s.close()
+    cells = n**3
+    return rho, {"value": cells * nsteps / (ms * 1e-3), "ms_per_step": ms / nsteps, "steps": nsteps, "t_final": t,
+                 "flagged_per_cell_stage": flagged / (4.0 * cells * nsteps) if recon == H._lib.RECON_LEARNED else None,
+                 "positivity_fallback_rate": fb / (4.0 * cells * nsteps)}
+
+
+def run_blast_horizon(args, ws, rank, local, n=512, nsteps=500, prob=0.2, smax_bound=3.0):
+    """The blast workload to its full length: 512^3, 500 SSPRK(4,3) steps at a fixed dt
+    (CFL 0.4 against a wave-speed bound of 3), every form timed and compared.
+    (a) distance from the FP64-bar reference at 512^3: L1(rho) of each form against the plain
+        double-float run (the plain FP64 run is too slow to take 500 steps here; the two agree to
+        round-off, shown over the first 50 steps);
+    (b) accuracy: the same problem at 256^3 (initial state = the 512^3 one averaged over 2^3 cells,
+        250 steps of twice the dt) in every form, L1(rho) against the 512^3 reference averaged to
+        256^3, and each form's error over plain CWENO4's in the same arithmetic (the 1.05 bar)."""
+    import torch
+
+    import acoustic_petsc_gb300 as H
+    from acoustic_petsc_gb300 import workloads
+
+    L = H.lib()
+    H._lib.check(L.hype_set_device(local), "hype_set_device")
+    torch.cuda.set_device(local)
+    P = H._lib
+    params, meta = _train_blast_indicator(H, prob=prob)
+    U0 = workloads.euler_blast(n)
+    dt = 0.4 * (1.0 / n) / (3.0 * smax_bound)
+    l1 = lambda a, b: float(np.abs(a - b).sum() / np.abs(b).sum())  # noqa: E731
+    forms512 = {}
+    with Clocks(_gpu_index(local)) as clk:
+        ref, forms512["plain_df64"] = _blast_form(H, n, U0, P.PREC_DF64, P.RECON_CWENO4, params, prob, dt, nsteps)
+        for name, prec, recon in (("plain_fp32", P.PREC_FP32, P.RECON_CWENO4),
+                                  ("learned_fp32", P.PREC_FP32, P.RECON_LEARNED),
+                                  ("learned_df64", P.PREC_DF64, P.RECON_LEARNED)):
+            rho, forms512[name] = _blast_form(H, n, U0, prec, recon, params, prob, dt, nsteps)
+            forms512[name]["l1_rho_vs_plain_df64"] = l1(rho, ref)
+            del rho
+        # the double-float reference against plain FP64 over the first 50 steps
+        r64, f64 = _blast_form(H, n, U0, P.PREC_FP64, P.RECON_CWENO4, params, prob, dt, 50)
+        rdf, _ = _blast_form(H, n, U0, P.PREC_DF64, P.RECON_CWENO4, params, prob, dt, 50)
+        f64["l1_rho_vs_plain_df64_after_50_steps"] = l1(rdf, r64)
+        forms512["plain_fp64_50_steps"] = f64
+        del r64, rdf
+        # (b) 256^3 from the averaged initial state, against the averaged 512^3 reference
+        m = n // 2
+        U1 = U0.reshape(m, 2, m, 2, m, 2, 5).mean(axis=(1, 3, 5))
+        del U0
+        ref_c = ref.reshape(m, 2, m, 2, m, 2).mean(axis=(1, 3, 5))
+        del ref
+        forms256 = {}
+        for name, prec, recon in (("plain_fp64", P.PREC_FP64, P.RECON_CWENO4),
+                                  ("learned_fp64", P.PREC_FP64, P.RECON_LEARNED),
+                                  ("plain_fp32", P.PREC_FP32, P.RECON_CWENO4),
+                                  ("learned_fp32", P.PREC_FP32, P.RECON_LEARNED),
+                                  ("plain_df64", P.PREC_DF64, P.RECON_CWENO4),
+                                  ("learned_df64", P.PREC_DF64, P.RECON_LEARNED)):
+            rho, forms256[name] = _blast_form(H, m, U1, prec, recon, params, prob, 2.0 * dt, nsteps // 2)
+            forms256[name]["l1_rho_error_vs_512_reference"] = l1(rho, ref_c)
+            del rho
+    for name in forms256:
+        base = "plain_" + name.split("_")[1]
+        forms256[name]["error_over_plain_same_arithmetic"] = (forms256[name]["l1_rho_error_vs_512_reference"] /
+                                                              forms256[base]["l1_rho_error_vs_512_reference"])
+        forms256[name]["error_over_plain_fp64"] = (forms256[name]["l1_rho_error_vs_512_reference"] /
+                                                   forms256["plain_fp64"]["l1_rho_error_vs_512_reference"])
+    v = forms512["learned_fp32"]["value"]
+    return {"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "n_gpus": ws, "steps": nsteps,
+            "warmup": 0, "ms_per_step": forms512["learned_fp32"]["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 state / f32 recon+flux, bf16 indicator",
+            "data": "synthetic: spherical blast p ratio 10, rho ratio 8, r0 0.1, seeded 1e-3 pressure noise",
+            "config": {"workload": f"euler3d_blast_{n}_{nsteps}_steps", "grid": [n, n, n], "dt": dt,
+                       "dt_rule": f"fixed: CFL 0.4 h / (3 x {smax_bound})", "positivity_fallback": "first order",
+                       "indicator": meta},
+            "forms_512": forms512, "forms_256_vs_512_reference": forms256,
+            "speedup_learned_fp32_vs_plain_fp32": v / forms512["plain_fp32"]["value"],
+            "speedup_learned_fp32_vs_plain_fp64": v / forms512["plain_fp64_50_steps"]["value"],
+            "gpu_launches": None, "clocks": clk.summary()}
+
+
 def run_mp2d_learned(args, ws, rank, local, n=1024, ntrain=256, tau=1e-4, prob=0.2):
     """Config 3 with the learned indicator: Kapila 1024^2 shock-bubble, FP64 state, FP32
     reconstruction/flux; plain CWENO4 vs the indicator-gated form (network trained on the
@@ -1030,6 +1159,8 @@ def run_pc2d(args, ws, rank, local, n=2048, order=3):
 WORKLOADS = {
     "blast512": run_blast,
     "blast256": lambda a, *r: run_blast(a, *r, n=256),
+    "blast512_horizon": run_blast_horizon,
+    "blast128_horizon": lambda a, *r: run_blast_horizon(a, *r, n=128, nsteps=40),
     "kapila1024": lambda a, *r: run_mp2d(a, *r, precision=0),
     "kapila1024_learned": run_mp2d_learned,
     "acoustic256": run_acoustic,
