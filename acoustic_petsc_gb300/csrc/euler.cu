@@ -1187,10 +1187,8 @@ __device__ __forceinline__ bool fs_admissible(const float* __restrict__ S, int t
     return ok;
 }
 
-// per warp, the network inputs (96 BF16 rows) and logits while the learned gate scores a plane
-constexpr int FS_STAGE_FLOATS = (mlp::ROWS * mlp::RSTRIDE * 2 + mlp::ROWS * 4) / 4;  // 2016
-static_assert(FS_STAGE_FLOATS * FS_TW <= FS_NQ * FS_NT, "gate staging fits the trace array");
-static_assert((FS_STAGE_FLOATS * 4) % 16 == 0, "staging rows stay 16-byte aligned");
+// the learned gate stages 3 x 16 BF16 pairs and 3 logits per cell in the cell's warp columns
+static_assert(3 * (mlp::KP / 2) + 3 <= FS_NQ, "gate staging fits the trace columns");
 
 // LEARNED: the indicator gate of k_recon_learned folded in -- the network scores each cell from
 // its three directional 5-point stencils on the tensor cores (mma.sync BF16, FP32 accumulation);
@@ -1242,10 +1240,10 @@ __global__ void __launch_bounds__(FS_NT, 1)
             bool full = false;
             float best = 0.0f;
             if constexpr (LEARNED) {
-                // the warp's 32 cells x 3 directions staged as BF16 rows in the (free) trace array
-                __nv_bfloat16* rows = reinterpret_cast<__nv_bfloat16*>(S + w * FS_STAGE_FLOATS);
-                float* lg = reinterpret_cast<float*>(rows + mlp::ROWS * mlp::RSTRIDE);
-                __nv_bfloat16* my_rows = rows + lane * 3 * mlp::RSTRIDE;
+                // the warp's 32 cells x 3 directions staged as BF16 rows in the warp's own columns of
+                // the trace array (free until this plane's traces: no block barrier, only the warp's)
+                unsigned* cols = reinterpret_cast<unsigned*>(S) + w * 32;
+                float* lgo = S + 3 * (mlp::KP / 2) * FS_NT + w * 32;
                 float sc[NV];
                 if (active) {
                     const float rho = __ldg(G + ge), E = __ldg(G + 4 * g.GN + ge);
@@ -1266,40 +1264,14 @@ __global__ void __launch_bounds__(FS_NT, 1)
                             mlp::normalise5(s5, sc[c], x + c * 5);
                         }
                     }
-                    mlp::stage_row(my_rows + d * mlp::RSTRIDE, x, active);
+                    mlp::stage_row_cols(cols, FS_NT, d, lane, x, active);
                 }
                 __syncwarp();
-                mlp::warp_logits(wts, rows, lg);
+                mlp::warp_logits_cols(wts, cols, FS_NT, lgo);
                 __syncwarp();
-                best = fmaxf(lg[lane * 3], fmaxf(lg[lane * 3 + 1], lg[lane * 3 + 2]));
+                best = fmaxf(lgo[lane], fmaxf(lgo[FS_NT + lane], lgo[2 * FS_NT + lane]));
                 full = best > logit_thr;
-                __syncthreads();  // every warp's rows read before the traces overwrite the array
-            }
-            // ---- L2 prefetch, one plane ahead of use: the ghosted input three planes up (the leading
-            // plane of the next plane's stencils; the ring rows' warps also take the two rows beyond
-            // them), and the stage inputs of this plane, read by the update at the next plane
-            if (k + 3 <= g.nz + GW - 1 && (active || (ring_x && own_y) || (own_x && ring_y))) {
-                const long long gp = ghost_index(g, i, j, k + 3);
-#pragma unroll
-                for (int c = 0; c < NV; ++c) {
-                    const float* a = G + (long long)c * g.GN + gp;
-                    prefetch_l2(a);
-                    if (w == 0 && own_x) {
-                        prefetch_l2(a - g.gx);
-                        prefetch_l2(a - 2 * g.gx);
-                    } else if (j == jhi && own_x) {
-                        prefetch_l2(a + g.gx);
-                        prefetch_l2(a + 2 * g.gx);
-                    }
-                }
-            }
-            if (owned && k >= kb && k < ke && !st.rhs_only) {
-                const long long cell = ((long long)k * g.ny + j) * g.nx + i;
-#pragma unroll
-                for (int c = 0; c < NV; ++c) {
-                    prefetch_l2(W + c * g.N + cell);
-                    if (st.a != 0.0) prefetch_l2(U + c * g.N + cell);
-                }
+                __syncwarp();  // the rows and logits read before this warp's traces overwrite its columns
             }
             // ---- reconstruction: all 24 traces of each variable into the shared array
             if (active) {

@@ -296,6 +296,15 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
         alu = {"bound": "fp64" if precision == 0 else "fp32", "achieved": ach, "peak": fpeak.value, "unit": "TFLOP/s",
                "frac": ach / fpeak.value, "flops_per_cell_stage": flops_cell,
                "peak_kind": "measured FMA issue ceiling (hype_probe_fma_peak)"}
+        # the reference algorithm's own operation count (oracle/flopcount.py on its expression trees):
+        # the work the GPU form does with fewer operations, as a rate against the same peak
+        alg = (_profile_figure("flops_euler_cweno4_rusanov.txt", "algorithmic_flops_per_cell_stage")
+               if recon == 0 and flux == 0 and not viscous else None)
+        if alg:
+            alu["algorithmic_flops_per_cell_stage"] = alg
+            alu["algorithmic_achieved"] = alg * cells / t_stage / 1e12
+            alu["algorithmic_frac"] = alu["algorithmic_achieved"] / fpeak.value
+            alu["algorithmic_source"] = "profiles/flops_euler_cweno4_rusanov.txt (reference expression trees)"
         instr_cell = _profile_figure(prof_file, "fp64_instructions_per_cell_stage") if precision == 0 else None
         if instr_cell:
             # an FMA counts two flops, an add or multiply one: against the issue ceiling
@@ -1191,11 +1200,29 @@ WORKLOADS = {
 }
 
 
+# one CPU sample of the 3D Euler workload for the reference arm and the GPU line's cpu_baseline:
+# the 256^3 pulse's physics on 128^3 cells (the per-cell rate of the restatement grows with the
+# grid up to about this size; the whole 256^3 grid would take minutes per step)
+EULER_CPU_SAMPLE_N = 128
+
+
+def _reference_program_figures():
+    """the reference program's own per-core rate, measured where its sources are (the GPU machine has
+    none): profiles/cpu_reference_euler.txt"""
+    if not os.path.exists(os.path.join(ROOT, "profiles", "cpu_reference_euler.txt")):
+        return None
+    keys = ("reference_cweno4_per_core_cell_updates_per_s", "restatement_over_reference_per_core_cweno4",
+            "reference_weno3_per_core_cell_updates_per_s", "restatement_over_reference_per_core_weno3")
+    out = {k: _profile_figure("cpu_reference_euler.txt", k) for k in keys}
+    out["source"] = "profiles/cpu_reference_euler.txt (python oracle/time_reference.py 32, x86_64 host, 1 core)"
+    return out
+
+
 def reference_arm(args, ws, rank):
     """CPU implementation of the path on all host cores, bounded sample per step."""
     if rank != 0:
         return None
-    n = int(os.environ.get("HYPE_REF_SAMPLE_N", "64"))
+    n = int(os.environ.get("HYPE_REF_SAMPLE_N", str(EULER_CPU_SAMPLE_N)))
     if args.workload.startswith("euler"):
         rates = []
         for _ in range(max(args.warmup, 0)):
@@ -1206,7 +1233,9 @@ def reference_arm(args, ws, rank):
             rates.append(r)
             t_all += d
         value = n**3 * args.steps / t_all
-        sample = f"1 SSPRK(4,3) step of a {n}^3 periodic pulse grid per bench step (same physics as 256^3)"
+        sample = (f"1 SSPRK(4,3) step of a {n}^3 periodic pulse grid per bench step (same physics as 256^3); "
+                  "the C restatement of the reference's RHS (bit-identical to the reference compiled in place), "
+                  "all host threads")
         cfg_w = "euler3d_cweno4_rusanov_ssprk43_256"
     else:
         r, cores, kind, d = cpu_ctcs_rate(512, 200)
@@ -1216,6 +1245,7 @@ def reference_arm(args, ws, rank):
             "config": {"workload": cfg_w},
             "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": cores, "kind": kind,
                              "sample": sample},
+            "reference_program": _reference_program_figures() if args.workload.startswith("euler") else None,
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -1312,10 +1342,14 @@ def main():
             out["cpu_baseline"] = {"value": n**3 * 2 / d, "unit": "cell-updates/s", "cores": O.threads(),
                                    "kind": "port", "sample": f"2 SSPRK(4,3) steps of the {n}^3 Taylor-Green run ({d:.1f} s)"}
         elif args.workload.startswith("euler"):
-            n = 160 if args.workload != "euler64" else 48
-            r, cores, kind, d = cpu_euler_rate(n, 3, use_ref=False)
+            n = EULER_CPU_SAMPLE_N if args.workload != "euler64" else 48
+            r, cores, kind, d = cpu_euler_rate(n, 2, use_ref=False)
             out["cpu_baseline"] = {"value": r, "unit": "cell-updates/s", "cores": cores, "kind": kind,
-                                   "sample": f"3 SSPRK(4,3) steps of a {n}^3 periodic pulse grid ({d:.1f} s wall)"}
+                                   "sample": f"2 SSPRK(4,3) steps of a {n}^3 periodic pulse grid ({d:.1f} s wall), "
+                                             "the same sample as the reference arm"}
+            ref = _reference_program_figures()
+            if ref:
+                out["cpu_baseline"]["reference_program"] = ref
         else:
             r, cores, kind, d = cpu_ctcs_rate(512, 300)
             out["cpu_baseline"] = {"value": r, "unit": "cell-updates/s", "cores": cores, "kind": kind,

@@ -315,3 +315,17 @@ def test_line_source_2d_matches_reference(oracle, name):
     t, u, cnt = S.trace()
     assert cnt == (10 if stepper == 1 else 4) * int(z["steps"]) and np.abs(u).max() > 0
     _pdat_close(t, u, z["pdat"], 6)
+
+
+def test_reference_flop_count_transcription():
+    """the counting-scalar transcription of the reference's CWENO4 weno() reproduces the C
+    restatement's coefficients bit for bit, and its per-cell-stage total is the committed figure"""
+    import re
+
+    from oracle import flopcount
+
+    out = flopcount.main()
+    assert out["transcription_vs_restatement_max_abs_diff"] == 0.0
+    txt = open(os.path.join(os.path.dirname(GOLDEN), "..", "profiles", "flops_euler_cweno4_rusanov.txt")).read()
+    committed = float(re.search(r"algorithmic_flops_per_cell_stage = ([0-9.]+)", txt).group(1))
+    assert out["flops_per_cell_stage"] == committed
