@@ -1250,19 +1250,20 @@ __global__ void __launch_bounds__(FS_NT, 1)
 #pragma unroll
                     for (int c = 0; c < NV; ++c) sc[c] = mlp::var_scale<float>(c, rho, E);
                 }
-#pragma unroll 1
+                // the x stencils of the 5 variables, then y, then z: each direction's 25 loads are issued
+                // together, and the next direction's are in flight while one is normalised and staged
+#pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     float x[mlp::NIN];
                     const int stp = d == 0 ? 1 : d == 1 ? g.gx : g.gx * g.gy;
                     if (active) {
+                        float s5[NV][5];
 #pragma unroll
-                        for (int c = 0; c < NV; ++c) {
-                            const float* p = G + (long long)c * g.GN + ge;
-                            float s5[5];
+                        for (int c = 0; c < NV; ++c)
 #pragma unroll
-                            for (int o = 0; o < 5; ++o) s5[o] = __ldg(p + (o - 2) * stp);
-                            mlp::normalise5(s5, sc[c], x + c * 5);
-                        }
+                            for (int o = 0; o < 5; ++o) s5[c][o] = __ldg(G + (long long)c * g.GN + ge + (o - 2) * stp);
+#pragma unroll
+                        for (int c = 0; c < NV; ++c) mlp::normalise5(s5[c], sc[c], x + c * 5);
                     }
                     mlp::stage_row_cols(cols, FS_NT, d, lane, x, active);
                 }

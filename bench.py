@@ -291,7 +291,22 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
             "traffic": traffic * cells if traffic else None, "algorithmic_bytes": bytes_stage * cells,
             "per_kernel_ms": per_kernel}
     alu = None
-    if flops_cell:
+    instr32 = _profile_figure(prof_file, "issued_thread_instructions_per_cell_stage") if precision == 1 else None
+    if instr32:
+        # the fused FP32 stage: every issued thread instruction against the FP32 pipe's issue ceiling
+        # (the FMA probe's rate / 2: an FMA is two flops, one instruction)
+        ach_i = instr32 * cells / t_stage
+        alu = {"bound": "fp32 issue", "issued_thread_instructions_per_cell_stage": instr32,
+               "achieved_instr_per_s": ach_i, "peak_instr_per_s": fpeak.value * 1e12 / 2,
+               "frac": ach_i / (fpeak.value * 1e12 / 2),
+               "peak_kind": "measured FMA issue ceiling (hype_probe_fma_peak)"}
+        alg = _profile_figure("flops_euler_cweno4_rusanov.txt", "algorithmic_flops_per_cell_stage") \
+            if recon == 0 and flux == 0 and not viscous else None
+        if alg:
+            alu["algorithmic_flops_per_cell_stage"] = alg
+            alu["algorithmic_achieved_tflops"] = alg * cells / t_stage / 1e12
+            alu["algorithmic_frac"] = alu["algorithmic_achieved_tflops"] / fpeak.value
+    elif flops_cell:
         ach = flops_cell * cells / t_stage / 1e12
         alu = {"bound": "fp64" if precision == 0 else "fp32", "achieved": ach, "peak": fpeak.value, "unit": "TFLOP/s",
                "frac": ach / fpeak.value, "flops_per_cell_stage": flops_cell,
@@ -1341,7 +1356,7 @@ def main():
             d = time.perf_counter() - t0
             out["cpu_baseline"] = {"value": n**3 * 2 / d, "unit": "cell-updates/s", "cores": O.threads(),
                                    "kind": "port", "sample": f"2 SSPRK(4,3) steps of the {n}^3 Taylor-Green run ({d:.1f} s)"}
-        elif args.workload.startswith("euler"):
+        elif args.workload.startswith("euler") or args.workload.startswith("blast"):
             n = EULER_CPU_SAMPLE_N if args.workload != "euler64" else 48
             r, cores, kind, d = cpu_euler_rate(n, 2, use_ref=False)
             out["cpu_baseline"] = {"value": r, "unit": "cell-updates/s", "cores": cores, "kind": kind,
