@@ -17,6 +17,19 @@
 namespace hype {
 namespace euler {
 
+// 1/x to about 1 ulp of FP32 (one MUFU instruction): the FP32 form's weight ratios and face-solver
+// reciprocals, where the correctly rounded division's longer instruction sequence would cost more
+// than the form's own rounding; x positive and in the normal range (on the host: the division)
+__host__ __device__ __forceinline__ float rcp_fast(float x) {
+#ifdef __CUDA_ARCH__
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return 1.0f / x;
+#endif
+}
+
 // 1/x for the face solvers: the approximate FP32 reciprocal (rcp.approx, ~1 ulp of FP32)
 // of x's leading bits, refined by two Newton steps r <- r + r (1 - x r) in FP64 (the
 // relative error squares at each: 2^-23, 2^-46, then FP64 rounding), four FP64 operations
@@ -24,7 +37,7 @@ namespace euler {
 // integer pipe.  x outside [2^-126, 2^126) in magnitude, zero or not finite: the division.
 template <typename R>
 __device__ __forceinline__ R recip(R x) {
-    if (sizeof(R) != sizeof(double)) return (R)__frcp_rn((float)x);  // 1 / x correctly rounded, as the division
+    if (sizeof(R) != sizeof(double)) return (R)rcp_fast((float)x);
     const double xd = (double)x;
     const unsigned hi = (unsigned)__double2hiint(xd);
     const unsigned ex = (hi >> 20) & 0x7FFu;
@@ -75,6 +88,8 @@ constexpr double G2 = GPT * GPT;
 
 template <typename R>
 struct Weights;
+
+
 
 // CWENO4 coefficients (20) of one variable from its 33-point stencil.
 // linear: the R4 polynomial (the limit in which all nonlinear weights equal the linear ones).
@@ -188,7 +203,8 @@ __host__ __device__ __forceinline__ void cweno4(const R* __restrict__ s, bool li
     const R gH = R(0.85), g0 = R((1.0 - 0.85) * 0.85), gs = R((1. / 6.) * (1 - 0.85) * (1 - 0.85));
     R w4, w0, ws[6];
     Weights<R>::compute(IS4, IS0, IS3, gH, g0, gs, w4, w0, ws);
-    const R wr = w4 / gH;
+    // 1/gammaHi as a constant: a product, not a division (the FP64 form keeps the division)
+    const R wr = sizeof(R) == sizeof(float) ? w4 * R(1.0 / 0.85) : w4 / gH;
     if (wdev) {  // largest departure of a nonlinear weight from its linear value (indicator labels)
         R d = fmax(fabs(w4 - gH), fabs(w0 - g0));
 #pragma unroll
@@ -279,21 +295,21 @@ struct Weights<float> {
             ss[m] = IS3[m] + 1.0e-12f;
             mn = fminf(mn, ss[m]);
         }
-        float r = mn / s4;
+        float r = mn * rcp_fast(s4);
         r *= r;
         w4 = gH * r * r;
-        r = mn / s0;
+        r = mn * rcp_fast(s0);
         r *= r;
         w0 = g0 * r * r;
         float total = w4 + w0;
 #pragma unroll
         for (int m = 0; m < 6; ++m) {
-            r = mn / ss[m];
+            r = mn * rcp_fast(ss[m]);
             r *= r;
             ws[m] = gs * r * r;
             total += ws[m];
         }
-        const float inv = 1.0f / total;
+        const float inv = rcp_fast(total);
         w4 *= inv;
         w0 *= inv;
 #pragma unroll
