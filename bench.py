@@ -356,8 +356,9 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
     # the double-float form (same initial state and steps), timed after the FP64 form's legs
     alt = None
     if with_alt:
-        alt = _euler_df64_beside(args, ws, n, U0, U_fp64, stream_of=lambda h: torch.cuda.ExternalStream(
-            L.hype_euler_stream(h)))
+        so = lambda h: torch.cuda.ExternalStream(L.hype_euler_stream(h))  # noqa: E731
+        alt = _euler_df64_beside(args, ws, n, U0, U_fp64, stream_of=so)
+        alt.update(_euler_df64_beside(args, ws, n, U0, U_fp64, stream_of=so, precision=1))
     del U_fp64
     clocks = clk.summary()
     s.close()
@@ -385,16 +386,17 @@ def run_euler(args, ws, rank, local, precision=0, recon=0, n=256, flux=0, viscou
     return out
 
 
-def _euler_df64_beside(args, ws, n, U0, U_fp64, stream_of):
-    """the HYPE_PREC_DF64 form of the same workload: state, face fluxes and stage accumulation
-    in FP64, reconstruction and Rusanov flux in FP32 pairs on deviations; the same warm-up and
-    timed steps from the same state, and its largest state difference from the FP64 run"""
+def _euler_df64_beside(args, ws, n, U0, U_fp64, stream_of, precision=2):
+    """another precision form of the same workload (default: HYPE_PREC_DF64, state, face fluxes and
+    stage accumulation in FP64, reconstruction and Rusanov flux in FP32 pairs on deviations; 1: the
+    fused FP32 stage), the same warm-up and timed steps from the same state, and its largest state
+    difference from the FP64 run"""
     import torch
 
     import acoustic_petsc_gb300 as H
 
     L = H.lib()
-    ctx = H.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, precision=H._lib.PREC_DF64)
+    ctx = H.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, precision=precision)
     d = H.EulerSolver(ctx)
     d.set_state(U0)
     d.step(max(args.warmup, 3))
@@ -415,14 +417,16 @@ def _euler_df64_beside(args, ws, n, U0, U_fp64, stream_of):
     stages = max(prof_n[0], 1)
     diff = float(np.abs(d.get_state() - U_fp64).max() / np.abs(U_fp64).max())
     d.close()
-    return {"df64": {"value": ws * n**3 * args.steps / (ms * 1e-3), "unit": "cell-updates/s",
-                     "ms_per_step": ms / args.steps,
-                     "dtype": EULER_DTYPE[2],
-                     "per_kernel_ms": {"recon": prof_ms[0] / stages, "faces": prof_ms[1] / stages,
-                                       "update": prof_ms[2] / stages},
-                     "state_rel_linf_diff_vs_fp64": diff,
-                     "steps_compared": max(args.warmup, 3) + args.steps,
-                     "profile": "profiles/euler_stage_df64.txt"}}
+    tag = "df64" if precision == 2 else "fp32"
+    per = ({"recon": prof_ms[0] / stages, "faces": prof_ms[1] / stages, "update": prof_ms[2] / stages}
+           if precision == 2 else {"ghost": prof_ms[0] / stages, "stage_fused": prof_ms[1] / stages})
+    return {tag: {"value": ws * n**3 * args.steps / (ms * 1e-3), "unit": "cell-updates/s",
+                  "ms_per_step": ms / args.steps,
+                  "dtype": EULER_DTYPE[precision],
+                  "per_kernel_ms": per,
+                  "state_rel_linf_diff_vs_fp64": diff,
+                  "steps_compared": max(args.warmup, 3) + args.steps,
+                  "profile": f"profiles/euler_stage_{tag}.txt"}}
 
 
 def run_ctcs(args, ws, rank, local, n=512):
