@@ -1,5 +1,5 @@
 """3D Euler CWENO4 + Rusanov on the GPU against the reference's outputs and the
-CPU checker.  Tolerance (spec bar for the FP64 path): relative L-inf
+CPU checker.  Tolerance (the bar of the FP64 path): relative L-inf
 max|gpu - ref| / max|ref| <= 1e-12 after one step, <= 1e-10 after a run."""
 import os
 

@@ -1,5 +1,5 @@
 """Learned troubled-cell indicator (no counterpart in the reference: parity is
-unpinned; it is judged by its gradients against a CPU FP64 restatement and by
+unpinned; it is checked by its gradients against a CPU FP64 restatement and by
 the accuracy of the gated solver against full CWENO4)."""
 import numpy as np
 import pytest
