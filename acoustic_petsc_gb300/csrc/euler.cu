@@ -1094,8 +1094,8 @@ __global__ void __launch_bounds__(256) k_update(const double* __restrict__ Fx, c
 // Layout: a block is FS_TW warps of 32 lanes.  Lane l of warp w holds cell
 // (i0 + l - 1, j0 + w - 1) of an x-y tile: lanes 1..30 and warps 1..FS_TW-2 are the owned
 // cells, lane 0 / 31 and warp 0 / FS_TW-1 the one-cell ring whose traces the tile's boundary
-// faces need (the ring is reconstructed again by the neighbouring tile: 2(30 + 12) of 360
-// cells per plane).  The block marches its tile along z; the +z traces of a plane stay in the
+// faces need (the ring is reconstructed again by the neighbouring tile: 80 ring cells beside
+// the 300 owned ones per plane).  The block marches its tile along z; the +z traces of a plane stay in the
 // thread's registers as the -z side of the next plane's z faces, and each cell's divergence
 // is completed one plane later, when its +z face flux exists.  Blocks are persistent, one per
 // SM (the trace and flux arrays take 188 KB of shared memory), and split the tiles' planes into equal

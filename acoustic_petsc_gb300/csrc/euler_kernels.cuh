@@ -30,6 +30,30 @@ __host__ __device__ __forceinline__ float rcp_fast(float x) {
 #endif
 }
 
+// 1/x for the FP64 CWENO4 weights, whose magnitudes (products of (IS + 1e-12)^2, sums of their inverse
+// squares) lie far outside the FP32 range: x is rebased to [1, 2), the approximate FP32 reciprocal of its
+// leading bits is scaled back by 2^(1023 - e) on the integer pipe and refined by two FP64 Newton steps
+// (relative error 2^-23, 2^-46, then FP64 rounding: within an ulp of the quotient), four FP64 operations
+// against the correctly rounded division's longer sequence.  Biased exponent outside [2, 2044] (zero,
+// subnormal, a reciprocal that would be subnormal, infinities, NaN): the division.  On the host: the division.
+__host__ __device__ __forceinline__ double recip_wide(double x) {
+#ifdef __CUDA_ARCH__
+    const unsigned hi = (unsigned)__double2hiint(x);
+    const unsigned ex = (hi >> 20) & 0x7FFu;
+    if (ex - 2u > 2042u) return 1.0 / x;
+    const float mf = __uint_as_float((hi & 0x80000000u) | (127u << 23) | ((hi & 0xFFFFFu) << 3));
+    float rf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(mf));
+    double r = df_f2d(rf);
+    r = __hiloint2double(__double2hiint(r) - ((int)ex - 1023) * (1 << 20), __double2loint(r));
+    r = fma(r, fma(-x, r, 1.0), r);
+    r = fma(r, fma(-x, r, 1.0), r);
+    return r;
+#else
+    return 1.0 / x;
+#endif
+}
+
 // 1/x for the face solvers: the approximate FP32 reciprocal (rcp.approx, ~1 ulp of FP32)
 // of x's leading bits, refined by two Newton steps r <- r + r (1 - x r) in FP64 (the
 // relative error squares at each: 2^-23, 2^-46, then FP64 rounding), four FP64 operations
@@ -203,8 +227,8 @@ __host__ __device__ __forceinline__ void cweno4(const R* __restrict__ s, bool li
     const R gH = R(0.85), g0 = R((1.0 - 0.85) * 0.85), gs = R((1. / 6.) * (1 - 0.85) * (1 - 0.85));
     R w4, w0, ws[6];
     Weights<R>::compute(IS4, IS0, IS3, gH, g0, gs, w4, w0, ws);
-    // 1/gammaHi as a constant: a product, not a division (the FP64 form keeps the division)
-    const R wr = sizeof(R) == sizeof(float) ? w4 * R(1.0 / 0.85) : w4 / gH;
+    // 1/gammaHi as a constant: a product, not a division
+    const R wr = w4 * R(1.0 / 0.85);
     if (wdev) {  // largest departure of a nonlinear weight from its linear value (indicator labels)
         R d = fmax(fabs(w4 - gH), fabs(w0 - g0));
 #pragma unroll
@@ -237,9 +261,10 @@ __host__ __device__ __forceinline__ void cweno4(const R* __restrict__ s, bool li
 }
 
 // w = gamma / (IS + eps)^4, normalised.  FP64: the eight reciprocals 1/(IS + eps)^2
-// come from one division by their product (prefix products, then back-substitution:
+// come from one reciprocal of their product (prefix products, then back-substitution:
 // 21 multiplications instead of 7 more reciprocals); a product outside the normal
-// range (IS beyond ~1e36) takes the plain reciprocals instead.
+// range (IS beyond ~1e36) takes the plain reciprocals instead.  Reciprocals by recip_wide
+// (within an ulp of the division, on a fraction of its FP64 instructions).
 template <>
 struct Weights<double> {
     __host__ __device__ __forceinline__ static void compute(double IS4, double IS0, const double* IS3, double gH, double g0, double gs,
@@ -255,7 +280,7 @@ struct Weights<double> {
 #pragma unroll
         for (int k = 1; k < 8; ++k) P[k] = P[k - 1] * q[k];
         if (P[7] > 1.0e-290 && P[7] < 1.0e290) {
-            double inv = 1.0 / P[7];
+            double inv = recip_wide(P[7]);
 #pragma unroll
             for (int k = 7; k > 0; --k) {
                 r[k] = inv * P[k - 1];
@@ -264,7 +289,7 @@ struct Weights<double> {
             r[0] = inv;
         } else {
 #pragma unroll
-            for (int k = 0; k < 8; ++k) r[k] = 1.0 / q[k];
+            for (int k = 0; k < 8; ++k) r[k] = recip_wide(q[k]);
         }
         w4 = gH * (r[0] * r[0]);
         w0 = g0 * (r[1] * r[1]);
@@ -274,7 +299,7 @@ struct Weights<double> {
             ws[m] = gs * (r[2 + m] * r[2 + m]);
             total += ws[m];
         }
-        const double rt = 1.0 / total;
+        const double rt = recip_wide(total);
         w4 *= rt;
         w0 *= rt;
 #pragma unroll
