@@ -225,11 +225,15 @@ __device__ __forceinline__ bool traces_admissible(const R* __restrict__ T, const
 // its per-axis boundary map picks (periodic wrap, reflective mirror, transmissive
 // copy) and a reflective ghost's wall-normal momentum negated; G is in the
 // reconstruction's precision, so the FP32 form converts each value once per stage.
+// One thread per ghosted cell of an x-y plane (flat index over the plane, so no block is left
+// mostly idle at the end of a row), one grid row per plane.
+constexpr int kGhostThreads = 256;
+
 template <typename R>
-__global__ void __launch_bounds__(128) k_ghost(const double* __restrict__ W, R* __restrict__ G, Geo g) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x - GW;
-    const int j = blockIdx.y - GW, k = blockIdx.z - GW;
-    if (i >= g.nx + GW) return;
+__global__ void __launch_bounds__(kGhostThreads) k_ghost(const double* __restrict__ W, R* __restrict__ G, Geo g) {
+    const int q = blockIdx.x * kGhostThreads + threadIdx.x;
+    if (q >= g.gx * g.gy) return;
+    const int i = q % g.gx - GW, j = q / g.gx - GW, k = blockIdx.y - GW;
     int fi = 0, fj = 0, fk = 0;
     const int mi = bmap(i, g.nx, g.bc[0], g.bc[1], &fi);
     const int mj = bmap(j, g.ny, g.bc[2], g.bc[3], &fj);
@@ -243,6 +247,8 @@ __global__ void __launch_bounds__(128) k_ghost(const double* __restrict__ W, R* 
         G[(long long)c * g.GN + dst] = (R)v;
     }
 }
+
+inline dim3 ghost_grid(const Geo& g) { return dim3(cdiv((long long)g.gx * g.gy, kGhostThreads), g.nz + 2 * GW); }
 
 // the 33-point stencil (index map of euler_kernels.cuh) of one variable about p = &G[cell]
 template <typename R>
@@ -1312,9 +1318,11 @@ __global__ void __launch_bounds__(FS_NT, 1)
 #pragma unroll
                     for (int c = 0; c < NV; ++c) {
                         const double L = df_f2d(div_z_f(Pp[c], Fz[c] - Fzp[c], r1h));
-                        const double u = (!st.rhs_only && st.a != 0.0) ? U[c * g.N + cell] : 0.0;
-                        const double wv = st.rhs_only ? 0.0 : W[c * g.N + cell];
-                        out[c * g.N + cell] = stage_value(st, cdt, u, wv, L);
+                        // read once and written once: streaming accesses, which leave L1 to the
+                        // stencil planes of the ghosted input
+                        const double u = (!st.rhs_only && st.a != 0.0) ? __ldcs(U + c * g.N + cell) : 0.0;
+                        const double wv = st.rhs_only ? 0.0 : __ldcs(W + c * g.N + cell);
+                        __stcs(out + c * g.N + cell, stage_value(st, cdt, u, wv, L));
                     }
                 }
 #pragma unroll
@@ -1639,9 +1647,9 @@ static int launch_rhs(hype_euler* e, const double* Win, int slot) {
     const int rec = e->p.recon;
     prof_mark(e, 0, true);
     const dim3 bgh(128), ggh(cdiv(g.gx, 128), g.gy, g.nz + 2 * GW);
-    if (f32) k_ghost<float><<<ggh, bgh, 0, e->stream>>>(Win, (float*)e->G, g);
+    if (f32) k_ghost<float><<<ghost_grid(g), kGhostThreads, 0, e->stream>>>(Win, (float*)e->G, g);
     else if (df) k_ghost_df<<<ggh, bgh, 0, e->stream>>>(Win, (df64*)e->G, g);
-    else k_ghost<double><<<ggh, bgh, 0, e->stream>>>(Win, (double*)e->G, g);
+    else k_ghost<double><<<ghost_grid(g), kGhostThreads, 0, e->stream>>>(Win, (double*)e->G, g);
     HYPE_LAUNCHED(1);
     const double gm1 = e->p.gamma - 1.0;
     const size_t ck_bytes = (f32 && e->p.positivity) ? sizeof(float) * 4 * 2 * NTR * 32 : 0;
@@ -1766,8 +1774,7 @@ static int launch_stage(hype_euler* e, const double* Win, const double* U, const
     }
     const Geo& g = e->g;
     prof_mark(e, 0, true);
-    const dim3 bgh(128), ggh(cdiv(g.gx, 128), g.gy, g.nz + 2 * GW);
-    k_ghost<float><<<ggh, bgh, 0, e->stream>>>(Win, (float*)e->G, g);
+    k_ghost<float><<<ghost_grid(g), kGhostThreads, 0, e->stream>>>(Win, (float*)e->G, g);
     prof_mark(e, 0, false);
     prof_mark(e, 1, true);
     const long long units = fs_tiles_x(g.nx) * fs_tiles_y(g.ny) * g.nz;
@@ -2334,15 +2341,14 @@ extern "C" int hype_euler_rhs_noalloc(const hype_euler_params* p, const double* 
     const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2);
     const int rec = p->recon;
     const int pad = p->positivity;
-    const dim3 bgh(128), ggh(cdiv(g.gx, 128), g.gy, g.nz + 2 * GW);
     if (p->precision == HYPE_PREC_FP32) {
         // the FP32 admissibility check of the positivity fallback keeps its per-warp columns in
         // dynamic shared memory, as in the context path
         const size_t ck_bytes = pad ? sizeof(float) * 4 * 2 * NTR * 32 : 0;
-        k_ghost<float><<<ggh, bgh, 0, s>>>(dU, (float*)G, g);
+        k_ghost<float><<<ghost_grid(g), kGhostThreads, 0, s>>>(dU, (float*)G, g);
         k_recon<float><<<gr, br, ck_bytes, s>>>((const float*)G, (float*)T, g, rec, pad, p->gamma - 1.0, counters);
     } else {
-        k_ghost<double><<<ggh, bgh, 0, s>>>(dU, (double*)G, g);
+        k_ghost<double><<<ghost_grid(g), kGhostThreads, 0, s>>>(dU, (double*)G, g);
         k_recon<double><<<gr, br, 0, s>>>((const double*)G, (double*)T, g, rec, pad, p->gamma - 1.0, counters);
     }
     launch_faces(g, T, Fx, Fy, Fz, p->gamma, ds, 4, p->precision == HYPE_PREC_FP32, p->flux, s);

@@ -594,7 +594,7 @@ __device__ __forceinline__ double visc_flux(const double* Q, const double (*G)[3
                                             double vmax, double* F) {
     // kc = cv mu gamma / Pr (heat conductivity), vmax = max(4 mu / 3, gamma mu / Pr); the
     // divisions by rho of the reference's expressions are products with 1/rho here
-    const double irho = 1.0 / Q[0], irho2 = irho * irho;
+    const double irho = 1.0 / Q[0];
     const double u = irho * Q[1], v = irho * Q[2], w = irho * Q[3];
     const double rhou = Q[1], rhov = Q[2], rhow = Q[3], e = Q[4];
     const double m2 = rhou * rhou + rhov * rhov + rhow * rhow;
