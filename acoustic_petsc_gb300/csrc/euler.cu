@@ -1318,11 +1318,9 @@ __global__ void __launch_bounds__(FS_NT, 1)
 #pragma unroll
                     for (int c = 0; c < NV; ++c) {
                         const double L = df_f2d(div_z_f(Pp[c], Fz[c] - Fzp[c], r1h));
-                        // read once and written once: streaming accesses, which leave L1 to the
-                        // stencil planes of the ghosted input
-                        const double u = (!st.rhs_only && st.a != 0.0) ? __ldcs(U + c * g.N + cell) : 0.0;
-                        const double wv = st.rhs_only ? 0.0 : __ldcs(W + c * g.N + cell);
-                        __stcs(out + c * g.N + cell, stage_value(st, cdt, u, wv, L));
+                        const double u = (!st.rhs_only && st.a != 0.0) ? U[c * g.N + cell] : 0.0;
+                        const double wv = st.rhs_only ? 0.0 : W[c * g.N + cell];
+                        out[c * g.N + cell] = stage_value(st, cdt, u, wv, L);
                     }
                 }
 #pragma unroll
