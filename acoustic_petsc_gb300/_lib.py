@@ -48,7 +48,8 @@ SYMBOLS = [
     "hype_acoustic_download", "hype_acoustic_rhs", "hype_acoustic_step", "hype_acoustic_sync", "hype_acoustic_stream",
     "hype_acoustic_rhs_t", "hype_acoustic_set_point_source", "hype_acoustic_trace", "hype_acoustic2d_rhs_t",
     "hype_acoustic2d_set_point_source", "hype_acoustic2d_trace",
-    "hype_euler_set_mlp", "hype_euler_set_recon", "hype_euler_indicator_stats", "hype_euler_sample_features",
+    "hype_euler_set_mlp", "hype_euler_set_recon", "hype_euler_indicator_stats", "hype_euler_set_gate_per_step",
+    "hype_euler_gate_flags", "hype_euler_sample_features",
     "hype_mlp_nparam", "hype_mlp_score", "hype_mlp_grad", "hype_mlp_train", "hype_euler_shadow_step",
     "hype_euler_monitor", "hype_acoustic2d_create", "hype_acoustic2d_destroy", "hype_acoustic2d_upload",
     "hype_acoustic2d_download", "hype_acoustic2d_rhs", "hype_acoustic2d_step", "hype_acoustic2d_sync",
@@ -249,6 +250,8 @@ def lib():
         "hype_euler_set_mlp": ([V, F, C.c_float], C.c_int),
         "hype_euler_set_recon": ([V, C.c_int], C.c_int),
         "hype_euler_indicator_stats": ([V, P(C.c_longlong), P(C.c_longlong), C.c_int], C.c_int),
+        "hype_euler_set_gate_per_step": ([V, C.c_int], C.c_int),
+        "hype_euler_gate_flags": ([V, C.c_void_p, C.c_int], C.c_int),
         "hype_euler_sample_features": ([V, C.c_longlong, F, F, P(C.c_longlong)], C.c_int),
         "hype_euler_shadow_step": ([V, D, D, D], C.c_int),
         "hype_mlp_nparam": ([], C.c_int),

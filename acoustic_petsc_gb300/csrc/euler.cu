@@ -1193,19 +1193,93 @@ __device__ __forceinline__ bool fs_admissible(const float* __restrict__ S, int t
     return ok;
 }
 
-// the learned gate stages 3 x 16 BF16 pairs and 3 logits per cell in the cell's warp columns
-static_assert(3 * (mlp::KP / 2) + 3 <= FS_NQ, "gate staging fits the trace columns");
+// The learned gate of the fused FP32 stage, scored ahead of it from the ghosted FP32 copy: one
+// byte per extended cell, 1 where the network's largest directional logit exceeds the threshold.
+// Scored are the cells the stage reconstructs (the owned cells and the one-cell frame without its
+// edges and corners, which keep the zero the array is created with).  The features, their BF16
+// rounding and the tensor-core scoring are k_recon_learned's, so the flags are that kernel's
+// decisions bit for bit.  Block: 32 x 4 cells of one x-y plane, as k_recon_learned.
+__global__ void __launch_bounds__(128) k_gate_f32(const float* __restrict__ G, unsigned char* __restrict__ flag, Geo g,
+                                                  const mlp::MmaWeights* __restrict__ wts, float logit_thr) {
+    __shared__ __align__(16) __nv_bfloat16 rows[4][mlp::ROWS * mlp::RSTRIDE];
+    __shared__ float lg[4][mlp::ROWS];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+    const int k = blockIdx.z - 1;
+    const int gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny), gk = (k < 0 || k >= g.nz);
+    const bool active = i <= g.nx && j <= g.ny && gi + gj + gk <= 1;
+    const long long ge = active ? ghost_index(g, i, j, k) : 0;
+    __nv_bfloat16* my_rows = rows[threadIdx.y] + threadIdx.x * 3 * mlp::RSTRIDE;
+    const float* Gc = G + ge;  // variable c at Gc[c * GN + offset]
+    float sc[NV];
+    if (active) {
+        const float rho = __ldg(Gc), E = __ldg(Gc + 4 * g.GN);
+#pragma unroll
+        for (int c = 0; c < NV; ++c) sc[c] = mlp::var_scale<float>(c, rho, E);
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        float x[mlp::NIN];
+#pragma unroll
+        for (int q = 0; q < mlp::NIN; ++q) x[q] = 0.0f;  // the row of an inactive lane is never read
+        const int stp = d == 0 ? 1 : d == 1 ? g.gx : g.gx * g.gy;
+        if (active) {
+            float s5[NV][5];
+#pragma unroll
+            for (int c = 0; c < NV; ++c) {
+                const float* p = Gc + (long long)c * g.GN;
+#pragma unroll
+                for (int o = 0; o < 5; ++o) s5[c][o] = __ldg(p + (o - 2) * stp);
+            }
+#pragma unroll
+            for (int c = 0; c < NV; ++c) mlp::normalise5(s5[c], sc[c], x + c * 5);
+        }
+        mlp::stage_row(my_rows + d * mlp::RSTRIDE, x, true);
+    }
+    __syncwarp();  // the warp's rows staged
+    mlp::warp_logits(wts, rows[threadIdx.y], lg[threadIdx.y]);
+    __syncwarp();
+    if (active) {
+        const float* l3 = lg[threadIdx.y] + threadIdx.x * 3;
+        flag[ext_index(g, i, j, k)] = fmaxf(l3[0], fmaxf(l3[1], l3[2])) > logit_thr ? 1 : 0;
+    }
+}
 
-// LEARNED: the indicator gate of k_recon_learned folded in -- the network scores each cell from
-// its three directional 5-point stencils on the tensor cores (mma.sync BF16, FP32 accumulation);
-// flagged or low-confidence cells take CWENO4, the others R4, and a cell whose R4 traces break the
+// The gate's flags widened to each cell's 3 x 3 x 3 neighbourhood (a cell is flagged when any cell
+// around it is), for the cells the fused stage reconstructs.  Flags scored on a step's first stage
+// and reused by its later stages then still cover a discontinuity that moves by less than a cell
+// over the step (the CFL number bounds the wave speed x dt by the cell width).
+__global__ void __launch_bounds__(128) k_gate_dilate(const unsigned char* __restrict__ f, unsigned char* __restrict__ o,
+                                                     Geo g) {
+    const int i = blockIdx.x * 128 + threadIdx.x, j = blockIdx.y, k = blockIdx.z;  // extended coordinates
+    if (i >= g.ex) return;
+    const int ey = g.ny + 2, ez = g.nz + 2;
+    unsigned m = 0;
+#pragma unroll
+    for (int dk = -1; dk <= 1; ++dk) {
+        const int kk = k + dk;
+        if (kk < 0 || kk >= ez) continue;
+#pragma unroll
+        for (int dj = -1; dj <= 1; ++dj) {
+            const int jj = j + dj;
+            if (jj < 0 || jj >= ey) continue;
+            const unsigned char* row = f + ((long long)kk * ey + jj) * g.ex;
+            m |= __ldg(row + i);
+            if (i > 0) m |= __ldg(row + i - 1);
+            if (i + 1 < g.ex) m |= __ldg(row + i + 1);
+        }
+    }
+    o[((long long)k * ey + j) * g.ex + i] = (unsigned char)m;
+}
+
+// LEARNED: the indicator gate of k_recon_learned, read from the flags k_gate_f32 wrote for this
+// stage's input: flagged cells take CWENO4, the others R4, and a cell whose R4 traces break the
 // floors is redone with CWENO4 (then first order with the positivity fallback)
 template <bool LEARNED>
 __global__ void __launch_bounds__(FS_NT, 1)
     k_stage_f32(const float* __restrict__ G, const double* U, const double* W, double* out, Geo g, int recon, int pad,
                 double gamma, double r1_h, Stage st, DevScalars* __restrict__ ds, int slot,
-                unsigned long long* __restrict__ counters, const mlp::MmaWeights* __restrict__ wts = nullptr,
-                float logit_thr = 0.0f) {
+                unsigned long long* __restrict__ counters, const unsigned char* __restrict__ gate = nullptr) {
     extern __shared__ float S[];  // traces [c][q][thread], then the -y face fluxes [c][thread]
     float* SFy = S + FS_NQ * FS_NT;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -1229,6 +1303,9 @@ __global__ void __launch_bounds__(FS_NT, 1)
         const bool ring_x = (i == i0 - 1 || i == ihi), ring_y = (j == j0 - 1 || j == jhi);
         const bool owned = own_x && own_y;
         const bool ring = (ring_x && own_y) || (own_x && ring_y);
+        // the gate's flag of the next plane, loaded a plane ahead (cells in [-1, n] along x and y)
+        unsigned char fnext = 0;
+        if (LEARNED && (owned || ring)) fnext = gate[ext_index(g, i, j, kb - 1)];
         float zp[NV][4];    // +z traces of the previous plane
         float Fzp[NV];      // flux of the previous plane's -z face
         float Pp[NV];       // x/y part of the previous plane's divergence
@@ -1244,41 +1321,10 @@ __global__ void __launch_bounds__(FS_NT, 1)
             const bool active = owned || (ring && !edge);
             const long long ge = active ? ghost_index(g, i, j, k) : 0;
             bool full = false;
-            float best = 0.0f;
             if constexpr (LEARNED) {
-                // the warp's 32 cells x 3 directions staged as BF16 rows in the warp's own columns of
-                // the trace array (free until this plane's traces: no block barrier, only the warp's)
-                unsigned* cols = reinterpret_cast<unsigned*>(S) + w * 32;
-                float* lgo = S + 3 * (mlp::KP / 2) * FS_NT + w * 32;
-                float sc[NV];
-                if (active) {
-                    const float rho = __ldg(G + ge), E = __ldg(G + 4 * g.GN + ge);
-#pragma unroll
-                    for (int c = 0; c < NV; ++c) sc[c] = mlp::var_scale<float>(c, rho, E);
-                }
-                // the x stencils of the 5 variables, then y, then z: each direction's 25 loads are issued
-                // together, and the next direction's are in flight while one is normalised and staged
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    float x[mlp::NIN];
-                    const int stp = d == 0 ? 1 : d == 1 ? g.gx : g.gx * g.gy;
-                    if (active) {
-                        float s5[NV][5];
-#pragma unroll
-                        for (int c = 0; c < NV; ++c)
-#pragma unroll
-                            for (int o = 0; o < 5; ++o) s5[c][o] = __ldg(G + (long long)c * g.GN + ge + (o - 2) * stp);
-#pragma unroll
-                        for (int c = 0; c < NV; ++c) mlp::normalise5(s5[c], sc[c], x + c * 5);
-                    }
-                    mlp::stage_row_cols(cols, FS_NT, d, lane, x, active);
-                }
-                __syncwarp();
-                mlp::warp_logits_cols(wts, cols, FS_NT, lgo);
-                __syncwarp();
-                best = fmaxf(lgo[lane], fmaxf(lgo[FS_NT + lane], lgo[2 * FS_NT + lane]));
-                full = best > logit_thr;
-                __syncwarp();  // the rows and logits read before this warp's traces overwrite its columns
+                full = active && fnext != 0;
+                if (full && owned && !edge) ++nflag;
+                if ((owned || ring) && k < ke) fnext = gate[ext_index(g, i, j, k + 1)];
             }
             // ---- reconstruction: all 24 traces of each variable into the shared array
             if (active) {
@@ -1299,7 +1345,6 @@ __global__ void __launch_bounds__(FS_NT, 1)
                     }
                     if (owned && !edge) ++nfall;
                 }
-                if (LEARNED && full && owned && !edge && best > logit_thr) ++nflag;
             }
             __syncthreads();
             // ---- Rusanov fluxes of the owned cells' faces: -x (the ring lane at the high side gives
@@ -1574,6 +1619,11 @@ struct hype_euler {
     double* pin = nullptr;     // pinned host staging for AoS transfers
     // learned indicator: BF16 parameters, logit threshold, counters (flagged, positivity fallbacks)
     mlp::MmaWeights* mlp = nullptr;  // packed for the tensor-core inference
+    // fused FP32 stage: the gate's flags (one byte per extended cell) and, when the gate is scored
+    // once per step, their one-cell widening that the step's stages read
+    unsigned char* gate = nullptr;
+    unsigned char* gate_wide = nullptr;
+    int gate_per_step = 0;
     float logit_thr = 0.0f;
     unsigned long long* mlp_cnt = nullptr;
     // per-kernel event timing inside a timed region (hype_euler_profile)
@@ -1735,7 +1785,7 @@ static int launch_update(hype_euler* e, const double* U, const double* W, double
 static bool uses_fused(const hype_euler* e) {
     return e->stage_mode == HYPE_STAGE_AUTO && e->p.precision == HYPE_PREC_FP32 && e->p.flux == HYPE_FLUX_RUSANOV &&
            !e->C4 && (e->p.recon == HYPE_RECON_CWENO4 || e->p.recon == HYPE_RECON_LINEAR4 ||
-                      e->p.recon == HYPE_RECON_WENO3 || (e->p.recon == HYPE_RECON_LEARNED && e->mlp));
+                      e->p.recon == HYPE_RECON_WENO3 || (e->p.recon == HYPE_RECON_LEARNED && e->mlp && e->gate));
 }
 
 // the unfused kernels' face traces and face fluxes, allocated on first use (never inside a
@@ -1773,20 +1823,31 @@ static int launch_stage(hype_euler* e, const double* Win, const double* U, const
     const Geo& g = e->g;
     prof_mark(e, 0, true);
     k_ghost<float><<<ghost_grid(g), kGhostThreads, 0, e->stream>>>(Win, (float*)e->G, g);
+    const bool learned = e->p.recon == HYPE_RECON_LEARNED;
+    // the gate's flags for this stage's input; scored once per step, on the first stage's input
+    // (slot 0) and for RHS-only calls (slot 4), then widened by a cell for the step's later stages
+    const bool score = learned && (!e->gate_per_step || slot == 0 || slot == 4);
+    if (score) {
+        const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4), g.nz + 2);
+        k_gate_f32<<<gr, br, 0, e->stream>>>((const float*)e->G, e->gate, g, e->mlp, e->logit_thr);
+        if (e->gate_per_step)
+            k_gate_dilate<<<dim3(cdiv(g.ex, 128), g.ny + 2, g.nz + 2), 128, 0, e->stream>>>(e->gate, e->gate_wide, g);
+    }
     prof_mark(e, 0, false);
     prof_mark(e, 1, true);
     const long long units = fs_tiles_x(g.nx) * fs_tiles_y(g.ny) * g.nz;
     const unsigned blocks = (unsigned)std::min<long long>(e->nsm, units);
-    if (e->p.recon == HYPE_RECON_LEARNED)
+    if (learned)
         k_stage_f32<true><<<blocks, FS_NT, FS_SMEM, e->stream>>>((const float*)e->G, U, W, out, g, e->p.recon,
                                                                 e->p.positivity, e->p.gamma, 1.0 / e->p.h, st, e->ds,
-                                                                slot, e->mlp_cnt, e->mlp, e->logit_thr);
+                                                                slot, e->mlp_cnt,
+                                                                e->gate_per_step ? e->gate_wide : e->gate);
     else
         k_stage_f32<false><<<blocks, FS_NT, FS_SMEM, e->stream>>>((const float*)e->G, U, W, out, g, e->p.recon,
                                                                  e->p.positivity, e->p.gamma, 1.0 / e->p.h, st, e->ds,
                                                                  slot, e->mlp_cnt);
     prof_mark(e, 1, false);
-    HYPE_LAUNCHED(2);
+    HYPE_LAUNCHED(2 + (score ? 1 + (e->gate_per_step ? 1 : 0) : 0));
     return HYPE_OK;
 }
 
@@ -1918,7 +1979,7 @@ extern "C" void hype_euler_destroy(hype_euler* e) {
     if (e->stream) cudaStreamSynchronize(e->stream);
     cudaFree(e->U); cudaFree(e->W); cudaFree(e->L); cudaFree(e->S); cudaFree(e->T);
     cudaFree(e->Fx); cudaFree(e->Fy); cudaFree(e->Fz); cudaFree(e->stage_aos); cudaFree(e->ds); cudaFree(e->G);
-    cudaFree(e->mlp); cudaFree(e->mlp_cnt); cudaFree(e->C4); cudaFree(e->mon); cudaFree(e->acc);
+    cudaFree(e->mlp); cudaFree(e->gate); cudaFree(e->gate_wide); cudaFree(e->mlp_cnt); cudaFree(e->C4); cudaFree(e->mon); cudaFree(e->acc);
     if (e->hs) cudaFreeHost(e->hs);
     for (auto x : e->ev) cudaEventDestroy(x);
     if (e->step_graph) cudaGraphExecDestroy(e->step_graph);
@@ -2034,7 +2095,8 @@ static bool steady_step_graph(hype_euler* e, int mode, double cfl_h) {
     if (e->prof) return false;
     long long lt;
     memcpy(&lt, &e->logit_thr, sizeof(float));
-    const long long key[8] = {mode, e->p.recon, e->p.flux, e->p.precision, e->p.positivity + 2 * e->stage_mode,
+    const long long key[8] = {mode, e->p.recon, e->p.flux, e->p.precision,
+                              e->p.positivity + 2 * e->stage_mode + 8 * e->gate_per_step,
                               (long long)(size_t)e->mlp, lt, (long long)(cfl_h * 1e15)};
     if (e->step_graph && memcmp(key, e->graph_key, sizeof(key)) == 0) return true;
     if (e->step_graph) {
@@ -2153,9 +2215,30 @@ extern "C" int hype_euler_set_mlp(hype_euler* e, const float* params, float prob
     mlp::MmaWeights hw;  // host staging, copied before the stream synchronisation below
     mlp::pack_weights(h.data(), hw);
     if (!e->mlp) HYPE_CK(cudaMalloc((void**)&e->mlp, sizeof(mlp::MmaWeights)));
+    if (!e->gate && e->p.precision == HYPE_PREC_FP32) {
+        HYPE_CK(cudaMalloc((void**)&e->gate, (size_t)e->g.NE));
+        HYPE_CK(cudaMalloc((void**)&e->gate_wide, (size_t)e->g.NE));
+        HYPE_CK(cudaMemsetAsync(e->gate, 0, (size_t)e->g.NE, e->stream));
+        HYPE_CK(cudaMemsetAsync(e->gate_wide, 0, (size_t)e->g.NE, e->stream));
+    }
     HYPE_CK(cudaMemcpyAsync(e->mlp, &hw, sizeof(mlp::MmaWeights), cudaMemcpyHostToDevice, e->stream));
     HYPE_CK(cudaStreamSynchronize(e->stream));
     e->logit_thr = logf(prob_threshold / (1.0f - prob_threshold));
+    return HYPE_OK;
+}
+
+extern "C" int hype_euler_set_gate_per_step(hype_euler* e, int per_step) {
+    if (!e || (per_step != 0 && per_step != 1)) return HYPE_ERR_ARG;
+    HYPE_CK(cudaStreamSynchronize(e->stream));
+    e->gate_per_step = per_step;  // part of the step graph's key: the next step recaptures
+    return HYPE_OK;
+}
+
+extern "C" int hype_euler_gate_flags(hype_euler* e, unsigned char* out, int widened) {
+    if (!e || !out || (widened != 0 && widened != 1)) return HYPE_ERR_ARG;
+    if (!e->gate) return HYPE_ERR_UNSUPPORTED;
+    HYPE_CK(cudaMemcpyAsync(out, widened ? e->gate_wide : e->gate, (size_t)e->g.NE, cudaMemcpyDeviceToHost, e->stream));
+    HYPE_CK(cudaStreamSynchronize(e->stream));
     return HYPE_OK;
 }
 

@@ -30,11 +30,21 @@ __host__ __device__ __forceinline__ T var_scale(int c, T rho, T E) {
 // (grid noise, weak acoustics) read as flat, a jump of the order of the state as O(1)
 __host__ __device__ __forceinline__ void normalise5(const float* s, float scale, float* out) {
     const float mu = 0.2f * (s[0] + s[1] + s[2] + s[3] + s[4]);
+#ifdef __CUDA_ARCH__
+    // three-input min / max (the same extremes for finite values; a signed zero they may pick
+    // differently cancels in hi - lo + floor)
+    float lo, hi;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(lo) : "f"(s[0]), "f"(s[1]), "f"(s[2]));
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(lo) : "f"(lo), "f"(s[3]), "f"(s[4]));
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(hi) : "f"(s[0]), "f"(s[1]), "f"(s[2]));
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(hi) : "f"(hi), "f"(s[3]), "f"(s[4]));
+#else
     float lo = s[0], hi = s[0];
     for (int k = 1; k < 5; ++k) {
         lo = s[k] < lo ? s[k] : lo;
         hi = s[k] > hi ? s[k] : hi;
     }
+#endif
 #ifdef __CUDA_ARCH__
     const float inv = __frcp_rn((hi - lo) + (1e-2f * scale + 1e-30f));  // = 1 / x, correctly rounded
 #else
@@ -181,91 +191,6 @@ __device__ __forceinline__ void warp_logits(const MmaWeights* __restrict__ w, co
         if (tg == 0) {
             lg[mt * 16 + g] = o0 + b3;
             lg[mt * 16 + g + 8] = o1 + b3;
-        }
-    }
-}
-
-// ---- the same scoring with the rows staged in columns (the fused stage kernel keeps them in the
-// warp's 32 columns of its shared trace array, stride words apart): row d*32 + l is direction d of
-// lane l's cell; its 16 BF16 pairs kw sit at word (d*16 + kw) * stride + col(l, kw), with the
-// column skewed by 8 (kw mod 4) so that the fragment loads of the 8 rows x 4 words a warp
-// instruction reads hit 32 distinct banks.
-__device__ __forceinline__ int skew_col(int l, int kw) { return (l + 8 * (kw & 3)) & 31; }
-
-// lane l's row of direction d: 25 features, the bias input 1, zeros
-__device__ __forceinline__ void stage_row_cols(unsigned* base, int stride, int d, int l, const float* x, bool valid) {
-#pragma unroll
-    for (int kw = 0; kw < KP / 2; ++kw) {
-        const int k = 2 * kw;
-        const float lo = !valid ? 0.0f : k < NIN ? x[k] : (k == NIN ? 1.0f : 0.0f);
-        const float hi = !valid ? 0.0f : k + 1 < NIN ? x[k + 1] : (k + 1 == NIN ? 1.0f : 0.0f);
-        __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-        base[(d * (KP / 2) + kw) * stride + skew_col(l, kw)] = *reinterpret_cast<unsigned*>(&v);
-    }
-}
-
-// logits of the warp's 96 column-staged rows: row d*32 + l to lgo[d * stride + l]; every lane calls it
-__device__ __forceinline__ void warp_logits_cols(const MmaWeights* __restrict__ w, const unsigned* base, int stride,
-                                                 float* lgo) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, tg = lane & 3;
-    unsigned bw1[4][2][2], bw2[4][2][2];
-#pragma unroll
-    for (int n = 0; n < 4; ++n)
-#pragma unroll
-        for (int kt = 0; kt < 2; ++kt) {
-            const int o = (n * 8 + g) * (KP / 2) + kt * 8 + tg;
-            bw1[n][kt][0] = __ldg(&w->w1[o]);
-            bw1[n][kt][1] = __ldg(&w->w1[o + 4]);
-            bw2[n][kt][0] = __ldg(&w->w2[o]);
-            bw2[n][kt][1] = __ldg(&w->w2[o + 4]);
-        }
-    const float b3 = __ldg(&w->b3);
-#pragma unroll 1
-    for (int mt = 0; mt < 6; ++mt) {
-        const int d = mt >> 1, l0 = (mt & 1) * 16;
-        unsigned a[2][4];
-#pragma unroll
-        for (int kt = 0; kt < 2; ++kt) {
-            const int k0 = kt * 8 + tg, k1 = k0 + 4;
-            a[kt][0] = base[(d * (KP / 2) + k0) * stride + skew_col(l0 + g, k0)];
-            a[kt][1] = base[(d * (KP / 2) + k0) * stride + skew_col(l0 + g + 8, k0)];
-            a[kt][2] = base[(d * (KP / 2) + k1) * stride + skew_col(l0 + g, k1)];
-            a[kt][3] = base[(d * (KP / 2) + k1) * stride + skew_col(l0 + g + 8, k1)];
-        }
-        float c1[4][4];
-#pragma unroll
-        for (int n = 0; n < 4; ++n) {
-            c1[n][0] = c1[n][1] = c1[n][2] = c1[n][3] = 0.0f;
-            mma_bf16(c1[n], a[0], bw1[n][0][0], bw1[n][0][1]);
-            mma_bf16(c1[n], a[1], bw1[n][1][0], bw1[n][1][1]);
-        }
-        unsigned h[2][4];
-#pragma unroll
-        for (int kt = 0; kt < 2; ++kt) {
-            h[kt][0] = pack_relu(c1[2 * kt][0], c1[2 * kt][1]);
-            h[kt][1] = pack_relu(c1[2 * kt][2], c1[2 * kt][3]);
-            h[kt][2] = pack_relu(c1[2 * kt + 1][0], c1[2 * kt + 1][1]);
-            h[kt][3] = pack_relu(c1[2 * kt + 1][2], c1[2 * kt + 1][3]);
-        }
-        float o0 = 0.0f, o1 = 0.0f;
-#pragma unroll
-        for (int n = 0; n < 4; ++n) {
-            const int col = n * 8 + tg * 2;
-            const float b20 = __ldg(&w->b2[col]), b21 = __ldg(&w->b2[col + 1]);
-            const float w30 = __ldg(&w->w3[col]), w31 = __ldg(&w->w3[col + 1]);
-            float c2[4] = {b20, b21, b20, b21};
-            mma_bf16(c2, h[0], bw2[n][0][0], bw2[n][0][1]);
-            mma_bf16(c2, h[1], bw2[n][1][0], bw2[n][1][1]);
-            o0 = fmaf(w30, fmaxf(c2[0], 0.0f), fmaf(w31, fmaxf(c2[1], 0.0f), o0));
-            o1 = fmaf(w30, fmaxf(c2[2], 0.0f), fmaf(w31, fmaxf(c2[3], 0.0f), o1));
-        }
-        o0 += __shfl_xor_sync(0xffffffffu, o0, 1);
-        o0 += __shfl_xor_sync(0xffffffffu, o0, 2);
-        o1 += __shfl_xor_sync(0xffffffffu, o1, 1);
-        o1 += __shfl_xor_sync(0xffffffffu, o1, 2);
-        if (tg == 0) {
-            lgo[d * stride + l0 + g] = o0 + b3;
-            lgo[d * stride + l0 + g + 8] = o1 + b3;
         }
     }
 }

@@ -187,6 +187,19 @@ class EulerSolver:
         """L.STAGE_AUTO: the fused FP32 stage where it applies; L.STAGE_UNFUSED: separate kernels"""
         check(L.lib().hype_euler_set_stage_kernel(self._h, int(mode)), "hype_euler_set_stage_kernel")
 
+    def set_gate_per_step(self, per_step: bool) -> None:
+        """fused FP32 stage: score the gate once per step (flags widened by a cell, read by the
+        step's four stages) instead of on every stage's input"""
+        check(L.lib().hype_euler_set_gate_per_step(self._h, int(bool(per_step))), "hype_euler_set_gate_per_step")
+
+    def gate_flags(self, widened: bool = False) -> np.ndarray:
+        """the fused FP32 stage's gate flags of the last scoring, shape (nz+2, ny+2, nx+2), frame included"""
+        c = self.ctx
+        out = np.zeros((c.N_z + 2, c.N_y + 2, c.N_x + 2), dtype=np.uint8)
+        check(L.lib().hype_euler_gate_flags(self._h, out.ctypes.data_as(C.c_void_p), int(bool(widened))),
+              "hype_euler_gate_flags")
+        return out
+
     def indicator_stats(self, reset: bool = True):
         f, b = C.c_longlong(), C.c_longlong()
         check(L.lib().hype_euler_indicator_stats(self._h, C.byref(f), C.byref(b), int(reset)), "indicator_stats")

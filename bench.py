@@ -628,8 +628,13 @@ def run_blast(args, ws, rank, local, n=512, ntrain=64, tau=0.01, prob=0.2):
     rho = {}
     clocks = None
     launches = 0
-    for form, recon in (("plain_fp32", H._lib.RECON_CWENO4), ("learned_fp32", H._lib.RECON_LEARNED)):
+    # the learned FP32 form twice: the gate scored on every stage's input (what the unfused kernels
+    # do), and scored once per step with its flags widened by a cell for the step's four stages
+    for form, recon, per_step in (("plain_fp32", H._lib.RECON_CWENO4, False),
+                                  ("learned_fp32", H._lib.RECON_LEARNED, False),
+                                  ("learned_fp32_per_step", H._lib.RECON_LEARNED, True)):
         s.set_recon(recon)
+        s.set_gate_per_step(per_step)
         s.set_state(U0)
         s.t, s.next_dt = 0.0, 0.0
         s.step(max(args.warmup, 3))
@@ -647,10 +652,11 @@ def run_blast(args, ws, rank, local, n=512, ntrain=64, tau=0.01, prob=0.2):
                      "flagged_per_cell_stage": flagged / (4.0 * cells * args.steps),
                      "positivity_fallback_rate": fb / (4.0 * cells * args.steps)}
         rho[form] = s.get_state()[..., 0]
-        if form == "learned_fp32":
+        if form == "learned_fp32_per_step":
             clocks = clk.summary()
             launches = H.launches() - l0
     l1 = float(np.abs(rho["learned_fp32"] - rho["plain_fp32"]).mean() / np.abs(rho["plain_fp32"]).mean())
+    l1_step = float(np.abs(rho["learned_fp32_per_step"] - rho["plain_fp32"]).mean() / np.abs(rho["plain_fp32"]).mean())
     s.close()
     del rho
     # 3. the plain and the indicator-gated FP64 forms (FP64 traces: 130 GB of scratch at 512^3), two steps
@@ -701,11 +707,12 @@ def run_blast(args, ws, rank, local, n=512, ntrain=64, tau=0.01, prob=0.2):
     l1_64 = float(np.abs(rho64["learned_fp64"] - ref64).mean() / np.abs(ref64).mean())
     l1_df = {f: float(np.abs(rho64[f] - ref64).mean() / np.abs(ref64).mean()) for f in ("plain_df64", "learned_df64")}
     del rho64, ref64
-    v = res["learned_fp32"]["value"]
+    v = res["learned_fp32_per_step"]["value"]
     peak, kind = _peaks()
     ach = EULER_BYTES_PER_CELL_UPDATE * v / ws / 1e9
     return {"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": max(args.warmup, 3), "ms_per_step": res["learned_fp32"]["ms_per_step"], "higher_is_better": True,
+            "warmup": max(args.warmup, 3), "ms_per_step": res["learned_fp32_per_step"]["ms_per_step"],
+            "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64 state / f32 recon+flux, bf16 indicator",
             "data": "synthetic: spherical blast p ratio 10, rho ratio 8, r0 0.1, seeded 1e-3 pressure noise",
             "config": {"workload": f"euler3d_blast_{n}_learned_indicator", "grid": [n, n, n], "cfl": 0.4,
@@ -714,9 +721,12 @@ def run_blast(args, ws, rank, local, n=512, ntrain=64, tau=0.01, prob=0.2):
                                      "prob_threshold": prob, "train_s": t_train, "final_loss": loss,
                                      "recall": recall, "precision": precision, "flagged_train": flagged_train}},
             "forms": res,
+            "value_form": "learned_fp32_per_step",
             "speedup_vs_plain_fp32": v / res["plain_fp32"]["value"],
+            "speedup_per_stage_gate_vs_plain_fp32": res["learned_fp32"]["value"] / res["plain_fp32"]["value"],
             "speedup_vs_plain_fp64": v / res["plain_fp64"]["value"],
             "l1_rho_learned_vs_plain_fp32": l1,
+            "l1_rho_learned_per_step_vs_plain_fp32": l1_step,
             "speedup_learned_fp64_vs_plain_fp64": res["learned_fp64"]["value"] / res["plain_fp64"]["value"],
             "l1_rho_learned_fp64_vs_plain_fp64_after_2_steps": l1_64,
             "speedup_learned_df64_vs_plain_fp64": res["learned_df64"]["value"] / res["plain_fp64"]["value"],
@@ -754,8 +764,9 @@ def _train_blast_indicator(H, ntrain=64, tau=0.01, prob=0.2):
     return params, meta
 
 
-def _blast_form(H, n, U0, precision, recon, params, prob, dt, nsteps):
-    """one form of the blast run with a fixed dt; returns its density and timing / counts"""
+def _blast_form(H, n, U0, precision, recon, params, prob, dt, nsteps, per_step=False):
+    """one form of the blast run with a fixed dt; returns its density and timing / counts
+    (per_step: the fused FP32 stage's gate scored once per step)"""
     import torch
 
     L = H.lib()
@@ -764,6 +775,8 @@ def _blast_form(H, n, U0, precision, recon, params, prob, dt, nsteps):
     s = H.EulerSolver(ctx)
     if recon == H._lib.RECON_LEARNED:
         s.set_mlp(params, prob)
+        if per_step:
+            s.set_gate_per_step(True)
     s.set_state(U0)
     s.indicator_stats(reset=True)
     stream = torch.cuda.ExternalStream(L.hype_euler_stream(s._h))
@@ -784,7 +797,7 @@ def _blast_form(H, n, U0, precision, recon, params, prob, dt, nsteps):
                  "positivity_fallback_rate": fb / (4.0 * cells * nsteps)}
 
 
-def run_blast_horizon(args, ws, rank, local, n=512, nsteps=500, prob=0.2, smax_bound=3.0):
+def run_blast_horizon(args, ws, rank, local, n=512, nsteps=500, prob=0.2, smax_bound=3.0, fp32_only=False):
     """The blast workload to its full length: 512^3, 500 SSPRK(4,3) steps at a fixed dt
     (CFL 0.4 against a wave-speed bound of 3), every form timed and compared.
     (a) distance from the FP64-bar reference at 512^3: L1(rho) of each form against the plain
@@ -792,7 +805,9 @@ def run_blast_horizon(args, ws, rank, local, n=512, nsteps=500, prob=0.2, smax_b
         round-off, shown over the first 50 steps);
     (b) accuracy: the same problem at 256^3 (initial state = the 512^3 one averaged over 2^3 cells,
         250 steps of twice the dt) in every form, L1(rho) against the 512^3 reference averaged to
-        256^3, and each form's error over plain CWENO4's in the same arithmetic (the 1.05 bar)."""
+        256^3, and each form's error over plain CWENO4's in the same arithmetic (the 1.05 bar).
+    fp32_only: the FP32 forms alone, against the plain FP32 run at 512^3 as the reference (1.2e-8 in
+    L1(rho) from the double-float one after the 500 steps; a few minutes instead of half an hour)."""
     import torch
 
     import acoustic_petsc_gb300 as H
@@ -807,12 +822,16 @@ def run_blast_horizon(args, ws, rank, local, n=512, nsteps=500, prob=0.2, smax_b
     dt = 0.4 * (1.0 / n) / (3.0 * smax_bound)
     l1 = lambda a, b: float(np.abs(a - b).sum() / np.abs(b).sum())  # noqa: E731
     forms512 = {}
+    if fp32_only:
+        return _blast_horizon_fp32(H, n, nsteps, prob, dt, params, meta, U0, l1, ws, local)
     with Clocks(_gpu_index(local)) as clk:
         ref, forms512["plain_df64"] = _blast_form(H, n, U0, P.PREC_DF64, P.RECON_CWENO4, params, prob, dt, nsteps)
         for name, prec, recon in (("plain_fp32", P.PREC_FP32, P.RECON_CWENO4),
                                   ("learned_fp32", P.PREC_FP32, P.RECON_LEARNED),
+                                  ("learned_fp32_per_step", P.PREC_FP32, P.RECON_LEARNED),
                                   ("learned_df64", P.PREC_DF64, P.RECON_LEARNED)):
-            rho, forms512[name] = _blast_form(H, n, U0, prec, recon, params, prob, dt, nsteps)
+            rho, forms512[name] = _blast_form(H, n, U0, prec, recon, params, prob, dt, nsteps,
+                                              per_step=name.endswith("per_step"))
             forms512[name]["l1_rho_vs_plain_df64"] = l1(rho, ref)
             del rho
         # the double-float reference against plain FP64 over the first 50 steps
@@ -832,9 +851,11 @@ def run_blast_horizon(args, ws, rank, local, n=512, nsteps=500, prob=0.2, smax_b
                                   ("learned_fp64", P.PREC_FP64, P.RECON_LEARNED),
                                   ("plain_fp32", P.PREC_FP32, P.RECON_CWENO4),
                                   ("learned_fp32", P.PREC_FP32, P.RECON_LEARNED),
+                                  ("learned_fp32_per_step", P.PREC_FP32, P.RECON_LEARNED),
                                   ("plain_df64", P.PREC_DF64, P.RECON_CWENO4),
                                   ("learned_df64", P.PREC_DF64, P.RECON_LEARNED)):
-            rho, forms256[name] = _blast_form(H, m, U1, prec, recon, params, prob, 2.0 * dt, nsteps // 2)
+            rho, forms256[name] = _blast_form(H, m, U1, prec, recon, params, prob, 2.0 * dt, nsteps // 2,
+                                              per_step=name.endswith("per_step"))
             forms256[name]["l1_rho_error_vs_512_reference"] = l1(rho, ref_c)
             del rho
     for name in forms256:
@@ -853,7 +874,48 @@ def run_blast_horizon(args, ws, rank, local, n=512, nsteps=500, prob=0.2, smax_b
                        "indicator": meta},
             "forms_512": forms512, "forms_256_vs_512_reference": forms256,
             "speedup_learned_fp32_vs_plain_fp32": v / forms512["plain_fp32"]["value"],
+            "speedup_learned_fp32_per_step_vs_plain_fp32": (forms512["learned_fp32_per_step"]["value"] /
+                                                            forms512["plain_fp32"]["value"]),
             "speedup_learned_fp32_vs_plain_fp64": v / forms512["plain_fp64_50_steps"]["value"],
+            "gpu_launches": None, "clocks": clk.summary()}
+
+
+def _blast_horizon_fp32(H, n, nsteps, prob, dt, params, meta, U0, l1, ws, local):
+    """run_blast_horizon's FP32 forms: the plain FP32 run at n^3 is the reference"""
+    P = H._lib
+    forms512 = {}
+    with Clocks(_gpu_index(local)) as clk:
+        ref, forms512["plain_fp32"] = _blast_form(H, n, U0, P.PREC_FP32, P.RECON_CWENO4, params, prob, dt, nsteps)
+        for name in ("learned_fp32", "learned_fp32_per_step"):
+            rho, forms512[name] = _blast_form(H, n, U0, P.PREC_FP32, P.RECON_LEARNED, params, prob, dt, nsteps,
+                                              per_step=name.endswith("per_step"))
+            forms512[name]["l1_rho_vs_plain_fp32"] = l1(rho, ref)
+            del rho
+        m = n // 2
+        U1 = U0.reshape(m, 2, m, 2, m, 2, 5).mean(axis=(1, 3, 5))
+        ref_c = ref.reshape(m, 2, m, 2, m, 2).mean(axis=(1, 3, 5))
+        del ref
+        forms256 = {}
+        for name, recon in (("plain_fp32", P.RECON_CWENO4), ("learned_fp32", P.RECON_LEARNED),
+                            ("learned_fp32_per_step", P.RECON_LEARNED)):
+            rho, forms256[name] = _blast_form(H, m, U1, P.PREC_FP32, recon, params, prob, 2.0 * dt, nsteps // 2,
+                                              per_step=name.endswith("per_step"))
+            forms256[name]["l1_rho_error_vs_512_reference"] = l1(rho, ref_c)
+            del rho
+    for name in forms256:
+        forms256[name]["error_over_plain_same_arithmetic"] = (forms256[name]["l1_rho_error_vs_512_reference"] /
+                                                              forms256["plain_fp32"]["l1_rho_error_vs_512_reference"])
+    v = forms512["learned_fp32_per_step"]["value"]
+    return {"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "n_gpus": ws, "steps": nsteps,
+            "warmup": 0, "ms_per_step": forms512["learned_fp32_per_step"]["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 state / f32 recon+flux, bf16 indicator",
+            "data": "synthetic: spherical blast p ratio 10, rho ratio 8, r0 0.1, seeded 1e-3 pressure noise",
+            "config": {"workload": f"euler3d_blast_{n}_{nsteps}_steps_fp32_forms", "grid": [n, n, n], "dt": dt,
+                       "reference": f"plain FP32 CWENO4 at {n}^3", "positivity_fallback": "first order",
+                       "indicator": meta},
+            "forms_512": forms512, "forms_256_vs_512_reference": forms256,
+            "speedup_learned_fp32_per_step_vs_plain_fp32": v / forms512["plain_fp32"]["value"],
+            "speedup_learned_fp32_vs_plain_fp32": forms512["learned_fp32"]["value"] / forms512["plain_fp32"]["value"],
             "gpu_launches": None, "clocks": clk.summary()}
 
 
@@ -1189,6 +1251,7 @@ WORKLOADS = {
     "blast256": lambda a, *r: run_blast(a, *r, n=256),
     "blast512_horizon": run_blast_horizon,
     "blast128_horizon": lambda a, *r: run_blast_horizon(a, *r, n=128, nsteps=40),
+    "blast512_horizon_fp32": lambda a, *r: run_blast_horizon(a, *r, fp32_only=True),
     "kapila1024": lambda a, *r: run_mp2d(a, *r, precision=0),
     "kapila1024_learned": run_mp2d_learned,
     "acoustic256": run_acoustic,

@@ -158,7 +158,8 @@ int hype_euler_monitor(hype_euler* e, double* ke, double* dissipation);
 
 /* Per-kernel timing: while enabled, every kernel the context launches is
  * bracketed by CUDA events on its stream; read returns the summed milliseconds
- * and launch counts of [0] ghost fill + reconstruction, [1] face fluxes (3
+ * and launch counts of [0] ghost fill + reconstruction (fused stage: ghost fill,
+ * and the indicator gate's scoring pass when the gate is on), [1] face fluxes (3
  * directions) or, for the fused stage, the fused stage kernel, [2] divergence +
  * stage update (fused stage: only the combination of a first stage whose dt
  * comes from its own RHS) since the last enable. */
@@ -185,8 +186,21 @@ int hype_euler_set_stage_kernel(hype_euler* e, int mode);
 int hype_euler_set_mlp(hype_euler* e, const float* params, float prob_threshold);
 /* switch the reconstruction (HYPE_RECON_*) of an existing context, e.g. for a full-WENO shadow step */
 int hype_euler_set_recon(hype_euler* e, int recon);
-/* counts of owned cells sent to CWENO4 by the network / by the positivity fallback since the last reset */
+/* counts of owned cells sent to CWENO4 by the network / by the positivity fallback since the last reset
+ * (per RK stage: a cell counts once in every stage that reconstructs it with CWENO4) */
 int hype_euler_indicator_stats(hype_euler* e, long long* flagged, long long* positivity_fallbacks, int reset);
+/* Fused FP32 stage only (HYPE_PREC_FP32, Rusanov, HYPE_STAGE_AUTO): per_step = 1 scores the
+ * network once per step, on the first stage's input (and on every RHS-only call), widens the flags
+ * to each cell's 3x3x3 neighbourhood and lets the step's four stages read them; per_step = 0 (the
+ * default, and what every other form does) scores every stage's input, bit-identical to the
+ * unfused kernels.  A discontinuity moves by less than a cell per step at CFL <= 1, so the
+ * widened flags of the step's start cover it in the later stages. */
+int hype_euler_set_gate_per_step(hype_euler* e, int per_step);
+/* the fused FP32 stage's gate flags of the last scoring, one byte per extended cell
+ * ((nx+2)(ny+2)(nz+2), x fastest, cell (i, j, k) at ((k+1)(ny+2) + j+1)(nx+2) + i+1): widened = 0
+ * the network's flags, 1 their 3x3x3 widening (per-step scoring only); HYPE_ERR_UNSUPPORTED
+ * before the network of an FP32 context is set */
+int hype_euler_gate_flags(hype_euler* e, unsigned char* out, int widened);
 /* training samples from the resident state: every stride-th owned cell, its three
  * directional normalised stencils X[s][3][25] and D[s], the largest change the CWENO4
  * nonlinear weights make to one of its 24 face traces relative to the linear R4

@@ -129,9 +129,10 @@ def test_fused_256_three_steps(hype):
 
 
 def test_fused_learned_gate_equals_unfused(hype):
-    """the indicator gate folded into the fused stage (scoring on the tensor cores, R4 or CWENO4
-    per cell, CWENO4 redo on an R4 positivity break, first order after that) against the
-    unfused k_recon_learned path: bit-identical states and the same flagged / fallback counts"""
+    """the indicator gate of the fused stage (a scoring pass on the tensor cores writing one flag
+    per cell, then R4 or CWENO4 per cell in the fused kernel, CWENO4 redo on an R4 positivity
+    break, first order after that) against the unfused k_recon_learned path: bit-identical states
+    and the same flagged / fallback counts"""
     from test_gpu_indicator import _train_on_blast
 
     from acoustic_petsc_gb300 import workloads
@@ -153,3 +154,111 @@ def test_fused_learned_gate_equals_unfused(hype):
     assert stats[0] == stats[1]
     assert stats[0][0] > 0
     print(f"learned blast {n}^3 FP32, 10 steps: flagged {stats[0][0]}, fallbacks {stats[0][1]} in both forms")
+
+
+@pytest.fixture(scope="module")
+def blast_net(hype):
+    from test_gpu_indicator import _train_on_blast
+
+    p, _, _, _ = _train_on_blast(hype)
+    return p
+
+
+def _widen(f):
+    """the 3 x 3 x 3 maximum of a flag array (x fastest, zero outside it)"""
+    pad = np.pad(f, 1)
+    out = np.zeros_like(f)
+    nz, ny, nx = f.shape
+    for dk in range(3):
+        for dj in range(3):
+            for di in range(3):
+                out |= pad[dk:dk + nz, dj:dj + ny, di:di + nx]
+    return out
+
+
+def test_gate_per_step_widens_the_first_stage_flags(hype, blast_net):
+    """gate scored once per step: after a step, the widened flags are the 3x3x3 maximum of the
+    network's flags, the network's flags equal the per-stage gate's on the same input (an
+    RHS-only call scores its input in both modes), and the flagged count is the widened owned
+    cells once in each of the step's four stages"""
+    from acoustic_petsc_gb300 import workloads
+
+    n = 40
+    U = workloads.euler_blast(n)
+    per_stage, per_step = (hype.EulerSolver(hype.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, positivity=1,
+                                                        precision=hype._lib.PREC_FP32,
+                                                        recon=hype._lib.RECON_LEARNED)) for _ in range(2))
+    for s in (per_stage, per_step):
+        s.set_mlp(blast_net, 0.2)
+    per_step.set_gate_per_step(True)
+    per_step.set_state(U)
+    per_step.indicator_stats(reset=True)
+    per_step.step(1)
+    flagged, _ = per_step.indicator_stats()
+    raw, wide = per_step.gate_flags(False), per_step.gate_flags(True)
+    assert raw.any()
+    assert np.array_equal(wide, _widen(raw))
+    assert flagged == 4 * int(wide[1:-1, 1:-1, 1:-1].sum())
+    per_step.RHSFunction(0.0, U)
+    per_stage.RHSFunction(0.0, U)
+    assert np.array_equal(per_step.gate_flags(False), per_stage.gate_flags(False))
+    print(f"blast {n}^3: {int(raw[1:-1, 1:-1, 1:-1].sum())} cells flagged, {int(wide[1:-1, 1:-1, 1:-1].sum())} "
+          "after widening")
+    per_stage.close()
+    per_step.close()
+
+
+@pytest.mark.parametrize("bias", [1000.0, -1000.0], ids=["all", "none"])
+def test_gate_per_step_limits(hype, blast_net, bias):
+    """a network that flags every cell makes the per-step gated stage plain CWENO4 bit for bit; one
+    that flags none makes it the per-stage gate's R4 with the CWENO4 redo, bit for bit"""
+    from acoustic_petsc_gb300 import workloads
+
+    n = 24
+    U = workloads.euler_blast(n)
+    p = np.array(blast_net, dtype=np.float32)
+    p[-1] = bias
+    out = []
+    for recon, per_step in ((hype._lib.RECON_LEARNED, True),
+                            (hype._lib.RECON_CWENO4 if bias > 0 else hype._lib.RECON_LEARNED, False)):
+        s = hype.EulerSolver(hype.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, positivity=1,
+                                         precision=hype._lib.PREC_FP32, recon=recon))
+        if recon == hype._lib.RECON_LEARNED:
+            s.set_mlp(p, 0.2)
+            s.set_gate_per_step(per_step)
+        s.set_state(U)
+        s.indicator_stats(reset=True)
+        s.step(1)
+        s.step(4)
+        out.append((s.get_state(), s.t, s.indicator_stats()))
+        s.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert out[0][1] == out[1][1]
+    assert out[0][2][0] == (5 * 4 * n**3 if bias > 0 else 0)
+
+
+def test_gate_per_step_accuracy(hype, blast_net):
+    """the per-step gate keeps the learned form's distance from plain CWENO4: blast 48^3, 20 steps,
+    relative L1 of the density against the plain FP32 form no larger than the per-stage gate's
+    (within 50 %) and below 1e-3"""
+    from acoustic_petsc_gb300 import workloads
+
+    n = 48
+    U = workloads.euler_blast(n)
+    rho = {}
+    for name, recon, per_step in (("plain", hype._lib.RECON_CWENO4, False), ("stage", hype._lib.RECON_LEARNED, False),
+                                  ("step", hype._lib.RECON_LEARNED, True)):
+        s = hype.EulerSolver(hype.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, positivity=1,
+                                         precision=hype._lib.PREC_FP32, recon=recon, dt_mode=hype._lib.DT_FIXED))
+        if recon == hype._lib.RECON_LEARNED:
+            s.set_mlp(blast_net, 0.2)
+            s.set_gate_per_step(per_step)
+        s.set_state(U)
+        s.step(20, dt=0.25 / n)
+        rho[name] = s.get_state()[..., 0]
+        s.close()
+    d_stage = float(np.abs(rho["stage"] - rho["plain"]).sum() / np.abs(rho["plain"]).sum())
+    d_step = float(np.abs(rho["step"] - rho["plain"]).sum() / np.abs(rho["plain"]).sum())
+    print(f"blast {n}^3, 20 steps: L1(rho) from plain CWENO4: per-stage gate {d_stage:.3e}, per-step gate {d_step:.3e}")
+    assert d_step <= 1.5 * d_stage + 1e-7
+    assert d_step < 1e-3
