@@ -235,19 +235,17 @@ __device__ __forceinline__ bool pad_ok(const Eos& e, const R* V) {
     return !((double)V[0] < 1.0e-14 || (double)V[1] < 1.0e-14 || ((double)V[4] + pi) < 1.0e-12 || a1 < 0.0 || a1 > 1.0);
 }
 
-// conserved state of a primitive state (PDEPrim2Cons, pde.c:24-36; kapila_5eqn.c:44-60)
+// conserved state of a primitive state (PDEPrim2Cons, pde.c:24-36; kapila_5eqn.c:44-60); (gd, pid) is
+// the state's mixture, mix(e, V[NV - 1]), formed once per face point by the caller
 template <typename R, int MODEL>
-__device__ __forceinline__ void prim2cons(const Eos& e, const R* V, R* Q) {
-    double gd, pid;
+__device__ __forceinline__ void prim2cons(const R* V, double gd, double pid, R* Q) {
     if (MODEL == HYPE_MP_DI4) {
-        mix(e, (double)V[4], gd, pid);
         const R g = (R)gd, pi = (R)pid;
         const R en = (V[3] + g * pi) / (g - R(1.0));
         const R k = R(0.5) * V[0] * (V[1] * V[1] + V[2] * V[2]);
         Q[0] = V[0]; Q[1] = V[0] * V[1]; Q[2] = V[0] * V[2]; Q[3] = k + en; Q[4] = V[4];
     } else {
         const R a1 = V[5], a2 = R(1.0) - a1;
-        mix(e, (double)a1, gd, pid);
         const R g = (R)gd, pi = (R)pid;
         const R rho = a1 * V[0] + a2 * V[1];
         Q[0] = a1 * V[0]; Q[1] = a2 * V[1]; Q[2] = rho * V[2]; Q[3] = rho * V[3];
@@ -256,13 +254,12 @@ __device__ __forceinline__ void prim2cons(const Eos& e, const R* V, R* Q) {
     }
 }
 
-// physical flux of a primitive state and its wave speed (PDEFluxPrim, pde.c:62-97)
+// physical flux of a primitive state and its wave speed (PDEFluxPrim, pde.c:62-97); (gd, pid) as for
+// prim2cons
 template <typename R, int MODEL>
-__device__ __forceinline__ R flux_prim(const Eos& e, const R* V, R nx, R ny, R* F, bool& bad) {
-    double gd, pid;
+__device__ __forceinline__ R flux_prim(const R* V, double gd, double pid, R nx, R ny, R* F, bool& bad) {
     if (MODEL == HYPE_MP_DI4) {
         const R phi = V[4];
-        mix(e, (double)phi, gd, pid);
         const R g = (R)gd, pi = (R)pid;
         const R rho = V[0], u = V[1], v = V[2], p = V[3];
         const R E = (p + g * pi) / (g - R(1.0)) + R(0.5) * rho * (u * u + v * v);
@@ -273,7 +270,6 @@ __device__ __forceinline__ R flux_prim(const Eos& e, const R* V, R nx, R ny, R* 
         return fabs(un) + sqrt(g * (p + pi) / rho);
     }
     const R a1 = V[5], a2 = R(1.0) - a1;
-    mix(e, (double)a1, gd, pid);
     const R g = (R)gd, pi = (R)pid;
     const R r1 = V[0], r2 = V[1], u = V[2], v = V[3], p = V[4];
     const R rho = a1 * r1 + a2 * r2;
@@ -286,18 +282,19 @@ __device__ __forceinline__ R flux_prim(const Eos& e, const R* V, R nx, R ny, R* 
 }
 
 // HLLC with the interface velocity as the last component (HLLCRiemannSolver, pde.c:131-232);
-// star partial densities of the five-equation model a_k r_k (S - u_n)/(S - S*)
+// star partial densities of the five-equation model a_k r_k (S - u_n)/(S - S*).  The reference
+// re-forms each side's mixture in every EOS call; it depends on the side's state alone, so the
+// caller forms it once per face point (gLd, piLd / gRd, piRd): the same values, a twelfth of the
+// FP64 divisions
 template <typename R, int MODEL>
-__device__ __forceinline__ R hllc2(const Eos& e, const R* VL, const R* VR, R nx, R ny, R* Flux, bool& bad) {
+__device__ __forceinline__ R hllc2(const R* VL, const R* VR, double gLd, double piLd, double gRd, double piRd, R nx,
+                                   R ny, R* Flux, bool& bad) {
     constexpr int NV = MODEL == HYPE_MP_DI4 ? 5 : 6;
     R QL[MAXV], QR[MAXV], FL[MAXV + 1], FR[MAXV + 1];
-    prim2cons<R, MODEL>(e, VL, QL);
-    prim2cons<R, MODEL>(e, VR, QR);
-    const R sl = flux_prim<R, MODEL>(e, VL, nx, ny, FL, bad);
-    const R sr = flux_prim<R, MODEL>(e, VR, nx, ny, FR, bad);
-    double gLd, piLd, gRd, piRd;
-    mix(e, (double)VL[NV - 1], gLd, piLd);
-    mix(e, (double)VR[NV - 1], gRd, piRd);
+    prim2cons<R, MODEL>(VL, gLd, piLd, QL);
+    prim2cons<R, MODEL>(VR, gRd, piRd, QR);
+    const R sl = flux_prim<R, MODEL>(VL, gLd, piLd, nx, ny, FL, bad);
+    const R sr = flux_prim<R, MODEL>(VR, gRd, piRd, nx, ny, FR, bad);
     const R gL = (R)gLd, piL = (R)piLd, gR = (R)gRd, piR = (R)piRd;
     R rL, rR, uL, uR, vL, vR, PL, PR;
     if (MODEL == HYPE_MP_DI4) {
@@ -382,9 +379,12 @@ __device__ __forceinline__ R rot_hllc2(const Eos& e, const R* VL, const R* VR, R
     if (a2 < R(0)) {
         n2x = -n2x; n2y = -n2y; a2 = -a2;
     }
+    double gLd, piLd, gRd, piRd;  // each side's mixture, once for both solves
+    mix(e, (double)VL[NV - 1], gLd, piLd);
+    mix(e, (double)VR[NV - 1], gRd, piRd);
     R f1[MAXV + 1], f2[MAXV + 1];
-    const R s1 = hllc2<R, MODEL>(e, VL, VR, n1x, n1y, f1, bad);
-    const R s2 = hllc2<R, MODEL>(e, VL, VR, n2x, n2y, f2, bad);
+    const R s1 = hllc2<R, MODEL>(VL, VR, gLd, piLd, gRd, piRd, n1x, n1y, f1, bad);
+    const R s2 = hllc2<R, MODEL>(VL, VR, gLd, piLd, gRd, piRd, n2x, n2y, f2, bad);
 #pragma unroll
     for (int k = 0; k <= NV; ++k) Flux[k] = a1 * f1[k] + a2 * f2[k];
     return (s1 < s2) ? s2 : s1;

@@ -797,6 +797,63 @@ def _blast_form(H, n, U0, precision, recon, params, prob, dt, nsteps, per_step=F
                  "positivity_fallback_rate": fb / (4.0 * cells * nsteps)}
 
 
+def run_blast_stage_kernels(args, ws, rank, local, n=256, prob=0.2):
+    """Per-stage kernel times of the fused FP32 forms on the blast (positivity fallback on): plain
+    CWENO4, plain R4 (the floor any gate can reach), the learned gate scored on every stage's input
+    and scored once per step; from the context's per-kernel CUDA events ([0] ghost fill plus the
+    gate's scoring / widening passes, [1] the fused stage kernel), averaged over the timed stages."""
+    import ctypes as C
+
+    import torch
+
+    import acoustic_petsc_gb300 as H
+    from acoustic_petsc_gb300 import workloads
+
+    L = H.lib()
+    H._lib.check(L.hype_set_device(local), "hype_set_device")
+    torch.cuda.set_device(local)
+    P = H._lib
+    params, meta = _train_blast_indicator(H, prob=prob)
+    U0 = workloads.euler_blast(n)
+    out = {}
+    with Clocks(_gpu_index(local)) as clk:
+        for name, recon, per_step in (("plain_cweno4", P.RECON_CWENO4, False), ("plain_r4", P.RECON_LINEAR4, False),
+                                      ("learned", P.RECON_LEARNED, False),
+                                      ("learned_per_step", P.RECON_LEARNED, True)):
+            s = H.EulerSolver(H.AppCtx(N_x=n, N_y=n, N_z=n, h=1.0 / n, CFL=0.4, positivity=1,
+                                       precision=P.PREC_FP32, recon=recon))
+            if recon == P.RECON_LEARNED:
+                s.set_mlp(params, prob)
+                s.set_gate_per_step(per_step)
+            s.set_state(U0)
+            s.step(max(args.warmup, 3))
+            s.indicator_stats(reset=True)
+            H._lib.check(L.hype_euler_profile(s._h, 1), "profile")
+            s.step(args.steps)
+            ms = (C.c_double * 3)()
+            cnt = (C.c_longlong * 3)()
+            H._lib.check(L.hype_euler_profile_read(s._h, ms, cnt), "profile_read")
+            H._lib.check(L.hype_euler_profile(s._h, 0), "profile")
+            flagged, fb = s.indicator_stats()
+            stages = max(cnt[1], 1)
+            out[name] = {"ghost_and_gate_ms": ms[0] / stages, "stage_fused_ms": ms[1] / stages,
+                         "total_ms": (ms[0] + ms[1] + ms[2]) / stages,
+                         "flagged_per_cell_stage": flagged / (stages * n**3), "positivity_fallbacks": fb}
+            s.close()
+    base = out["plain_cweno4"]["total_ms"]
+    for v in out.values():
+        v["speedup_vs_plain_cweno4"] = base / v["total_ms"]
+    v = n**3 / (out["learned_per_step"]["total_ms"] * 4e-3)
+    return {"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": 4 * out["learned_per_step"]["total_ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 state / f32 recon+flux, bf16 indicator",
+            "data": "synthetic: spherical blast p ratio 10, rho ratio 8, r0 0.1, seeded 1e-3 pressure noise",
+            "config": {"workload": f"euler3d_blast_{n}_fp32_stage_kernels", "grid": [n, n, n], "indicator": meta,
+                       "timing": "per-kernel CUDA events (hype_euler_profile), per RK stage"},
+            "stage_kernels": out, "gpu_launches": None, "clocks": clk.summary()}
+
+
 def run_blast_horizon(args, ws, rank, local, n=512, nsteps=500, prob=0.2, smax_bound=3.0, fp32_only=False):
     """The blast workload to its full length: 512^3, 500 SSPRK(4,3) steps at a fixed dt
     (CFL 0.4 against a wave-speed bound of 3), every form timed and compared.
@@ -1252,6 +1309,7 @@ WORKLOADS = {
     "blast512_horizon": run_blast_horizon,
     "blast128_horizon": lambda a, *r: run_blast_horizon(a, *r, n=128, nsteps=40),
     "blast512_horizon_fp32": lambda a, *r: run_blast_horizon(a, *r, fp32_only=True),
+    "blast256_stage_kernels": run_blast_stage_kernels,
     "kapila1024": lambda a, *r: run_mp2d(a, *r, precision=0),
     "kapila1024_learned": run_mp2d_learned,
     "acoustic256": run_acoustic,
