@@ -195,6 +195,26 @@ __device__ __forceinline__ void mix(const Eos& e, double a, double& g, double& p
     }
 }
 
+// the mixture in the face solver's arithmetic: FP64 for the FP64 form (mix, the reference's
+// rounding); FP32 for the FP32 form, whose solver works on FP32 values of g and pi anyway (every
+// term of the mixture rules is positive for gamma > 1 and non-negative stiffnesses: nothing
+// cancels, and the FP32 pair is within a few ulp of the rounded FP64 one)
+template <typename R>
+__device__ __forceinline__ void mix_r(const Eos& e, R a, R& g, R& pi) {
+    if constexpr (sizeof(R) == sizeof(double)) {
+        double gd, pd;
+        mix(e, (double)a, gd, pd);
+        g = (R)gd;
+        pi = (R)pd;
+    } else {
+        const float g1 = (float)e.g1, g2 = (float)e.g2, p1 = (float)e.p1, p2 = (float)e.p2;
+        const float a2 = 1.0f - a;
+        if (e.model == HYPE_MP_DI4) g = 1.0f + (g1 - 1.0f) * (g2 - 1.0f) / (a2 * (g1 - 1.0f) + a * (g2 - 1.0f));
+        else g = 1.0f + ((g1 - 1.0f) * (g2 - 1.0f)) / ((g2 - 1.0f) * a + (g1 - 1.0f) * a2);
+        pi = ((g - 1.0f) / g) * (g1 * p1 * a / (g1 - 1.0f) + g2 * p2 * a2 / (g2 - 1.0f));
+    }
+}
+
 // conserved -> primitive (FP64): DI4 (rho,u,v,p,phi), KAPILA5 (rho1,rho2,u,v,p,a1)
 __device__ __forceinline__ void cons2prim(const Eos& e, const double* Q, double* V) {
     double g, pi;
@@ -221,32 +241,39 @@ __device__ __forceinline__ void cons2prim(const Eos& e, const double* Q, double*
     }
 }
 
-// admissibility of a reconstructed primitive state (pde.c:99-129)
+// admissibility of a reconstructed primitive state (pde.c:99-129).  The mixture's stiffness pi is
+// formed only when the pressure test needs it: with both gases' gamma > 1, non-negative
+// stiffnesses and the volume fraction in [0, 1] (outside it the state fails anyway), pi >= 0, so
+// p + pi rounds to at least p and p >= 1e-12 passes the test whatever pi is (a NaN p fails
+// neither form of the test).
 template <typename R>
 __device__ __forceinline__ bool pad_ok(const Eos& e, const R* V) {
     double g, pi;
+    const bool stiff_nonneg = e.p1 >= 0.0 && e.p2 >= 0.0 && e.g1 > 1.0 && e.g2 > 1.0;
     if (e.model == HYPE_MP_DI4) {
-        const double phi = (double)V[4];
+        const double phi = (double)V[4], p = (double)V[3];
+        if ((double)V[0] < 1.0e-14 || phi < 0.0 || phi > 1.0) return false;
+        if (stiff_nonneg && !(p < 1.0e-12)) return true;
         mix(e, phi, g, pi);
-        return !((double)V[0] < 1.0e-14 || ((double)V[3] + pi) < 1.0e-12 || phi < 0.0 || phi > 1.0);
+        return !((p + pi) < 1.0e-12);
     }
-    const double a1 = (double)V[5];
+    const double a1 = (double)V[5], p = (double)V[4];
+    if ((double)V[0] < 1.0e-14 || (double)V[1] < 1.0e-14 || a1 < 0.0 || a1 > 1.0) return false;
+    if (stiff_nonneg && !(p < 1.0e-12)) return true;
     mix(e, a1, g, pi);
-    return !((double)V[0] < 1.0e-14 || (double)V[1] < 1.0e-14 || ((double)V[4] + pi) < 1.0e-12 || a1 < 0.0 || a1 > 1.0);
+    return !((p + pi) < 1.0e-12);
 }
 
-// conserved state of a primitive state (PDEPrim2Cons, pde.c:24-36; kapila_5eqn.c:44-60); (gd, pid) is
-// the state's mixture, mix(e, V[NV - 1]), formed once per face point by the caller
+// conserved state of a primitive state (PDEPrim2Cons, pde.c:24-36; kapila_5eqn.c:44-60); (g, pi) is
+// the state's mixture, mix_r(e, V[NV - 1]), formed once per face point by the caller
 template <typename R, int MODEL>
-__device__ __forceinline__ void prim2cons(const R* V, double gd, double pid, R* Q) {
+__device__ __forceinline__ void prim2cons(const R* V, R g, R pi, R* Q) {
     if (MODEL == HYPE_MP_DI4) {
-        const R g = (R)gd, pi = (R)pid;
         const R en = (V[3] + g * pi) / (g - R(1.0));
         const R k = R(0.5) * V[0] * (V[1] * V[1] + V[2] * V[2]);
         Q[0] = V[0]; Q[1] = V[0] * V[1]; Q[2] = V[0] * V[2]; Q[3] = k + en; Q[4] = V[4];
     } else {
         const R a1 = V[5], a2 = R(1.0) - a1;
-        const R g = (R)gd, pi = (R)pid;
         const R rho = a1 * V[0] + a2 * V[1];
         Q[0] = a1 * V[0]; Q[1] = a2 * V[1]; Q[2] = rho * V[2]; Q[3] = rho * V[3];
         Q[4] = (V[4] + g * pi) / (g - R(1.0)) + R(0.5) * rho * (V[2] * V[2] + V[3] * V[3]);
@@ -254,13 +281,12 @@ __device__ __forceinline__ void prim2cons(const R* V, double gd, double pid, R* 
     }
 }
 
-// physical flux of a primitive state and its wave speed (PDEFluxPrim, pde.c:62-97); (gd, pid) as for
+// physical flux of a primitive state and its wave speed (PDEFluxPrim, pde.c:62-97); (g, pi) as for
 // prim2cons
 template <typename R, int MODEL>
-__device__ __forceinline__ R flux_prim(const R* V, double gd, double pid, R nx, R ny, R* F, bool& bad) {
+__device__ __forceinline__ R flux_prim(const R* V, R g, R pi, R nx, R ny, R* F, bool& bad) {
     if (MODEL == HYPE_MP_DI4) {
         const R phi = V[4];
-        const R g = (R)gd, pi = (R)pid;
         const R rho = V[0], u = V[1], v = V[2], p = V[3];
         const R E = (p + g * pi) / (g - R(1.0)) + R(0.5) * rho * (u * u + v * v);
         const R un = u * nx + v * ny;
@@ -270,7 +296,6 @@ __device__ __forceinline__ R flux_prim(const R* V, double gd, double pid, R nx, 
         return fabs(un) + sqrt(g * (p + pi) / rho);
     }
     const R a1 = V[5], a2 = R(1.0) - a1;
-    const R g = (R)gd, pi = (R)pid;
     const R r1 = V[0], r2 = V[1], u = V[2], v = V[3], p = V[4];
     const R rho = a1 * r1 + a2 * r2;
     const R E = (p + g * pi) / (g - R(1.0)) + R(0.5) * rho * (u * u + v * v);
@@ -284,18 +309,17 @@ __device__ __forceinline__ R flux_prim(const R* V, double gd, double pid, R nx, 
 // HLLC with the interface velocity as the last component (HLLCRiemannSolver, pde.c:131-232);
 // star partial densities of the five-equation model a_k r_k (S - u_n)/(S - S*).  The reference
 // re-forms each side's mixture in every EOS call; it depends on the side's state alone, so the
-// caller forms it once per face point (gLd, piLd / gRd, piRd): the same values, a twelfth of the
-// FP64 divisions
+// caller forms it once per face point (gL, piL / gR, piR): the same values, a twelfth of the
+// mixture evaluations
 template <typename R, int MODEL>
-__device__ __forceinline__ R hllc2(const R* VL, const R* VR, double gLd, double piLd, double gRd, double piRd, R nx,
-                                   R ny, R* Flux, bool& bad) {
+__device__ __forceinline__ R hllc2(const R* VL, const R* VR, R gL, R piL, R gR, R piR, R nx, R ny, R* Flux,
+                                   bool& bad) {
     constexpr int NV = MODEL == HYPE_MP_DI4 ? 5 : 6;
     R QL[MAXV], QR[MAXV], FL[MAXV + 1], FR[MAXV + 1];
-    prim2cons<R, MODEL>(VL, gLd, piLd, QL);
-    prim2cons<R, MODEL>(VR, gRd, piRd, QR);
-    const R sl = flux_prim<R, MODEL>(VL, gLd, piLd, nx, ny, FL, bad);
-    const R sr = flux_prim<R, MODEL>(VR, gRd, piRd, nx, ny, FR, bad);
-    const R gL = (R)gLd, piL = (R)piLd, gR = (R)gRd, piR = (R)piRd;
+    prim2cons<R, MODEL>(VL, gL, piL, QL);
+    prim2cons<R, MODEL>(VR, gR, piR, QR);
+    const R sl = flux_prim<R, MODEL>(VL, gL, piL, nx, ny, FL, bad);
+    const R sr = flux_prim<R, MODEL>(VR, gR, piR, nx, ny, FR, bad);
     R rL, rR, uL, uR, vL, vR, PL, PR;
     if (MODEL == HYPE_MP_DI4) {
         rL = VL[0]; uL = VL[1]; vL = VL[2]; PL = VL[3];
@@ -379,12 +403,12 @@ __device__ __forceinline__ R rot_hllc2(const Eos& e, const R* VL, const R* VR, R
     if (a2 < R(0)) {
         n2x = -n2x; n2y = -n2y; a2 = -a2;
     }
-    double gLd, piLd, gRd, piRd;  // each side's mixture, once for both solves
-    mix(e, (double)VL[NV - 1], gLd, piLd);
-    mix(e, (double)VR[NV - 1], gRd, piRd);
+    R gL, piL, gR, piR;  // each side's mixture, once for both solves
+    mix_r<R>(e, VL[NV - 1], gL, piL);
+    mix_r<R>(e, VR[NV - 1], gR, piR);
     R f1[MAXV + 1], f2[MAXV + 1];
-    const R s1 = hllc2<R, MODEL>(VL, VR, gLd, piLd, gRd, piRd, n1x, n1y, f1, bad);
-    const R s2 = hllc2<R, MODEL>(VL, VR, gLd, piLd, gRd, piRd, n2x, n2y, f2, bad);
+    const R s1 = hllc2<R, MODEL>(VL, VR, gL, piL, gR, piR, n1x, n1y, f1, bad);
+    const R s2 = hllc2<R, MODEL>(VL, VR, gL, piL, gR, piR, n2x, n2y, f2, bad);
 #pragma unroll
     for (int k = 0; k <= NV; ++k) Flux[k] = a1 * f1[k] + a2 * f2[k];
     return (s1 < s2) ? s2 : s1;

@@ -1310,6 +1310,7 @@ WORKLOADS = {
     "blast128_horizon": lambda a, *r: run_blast_horizon(a, *r, n=128, nsteps=40),
     "blast512_horizon_fp32": lambda a, *r: run_blast_horizon(a, *r, fp32_only=True),
     "blast256_stage_kernels": run_blast_stage_kernels,
+    "blast128_stage_kernels": lambda a, *r: run_blast_stage_kernels(a, *r, n=128),
     "kapila1024": lambda a, *r: run_mp2d(a, *r, precision=0),
     "kapila1024_learned": run_mp2d_learned,
     "acoustic256": run_acoustic,
