@@ -23,9 +23,11 @@
 namespace hype {
 namespace mp2d {
 
-int launch_rhs_f32(int model, bool learned, const double* P, void* T, double* F, double* G, const Geo& g, const Eos& e,
-                   DevScalars* ds, int slot, const mlp::MmaWeights* mlp, float logit_thr, unsigned long long* flagged,
-                   cudaStream_t st);
+int launch_rhs_f32(int model, bool learned, const double* Win, float* Pf, void* T, float* F, float* G, const Geo& g,
+                   const Eos& e, DevScalars* ds, int slot, const mlp::MmaWeights* mlp, float logit_thr,
+                   unsigned long long* flagged, cudaStream_t st);
+void launch_update_f32(const float* F, const float* G, const double* Win, const double* X, const double* Y, double* out,
+                       const Geo& g, double r1_h, Stage st, const DevScalars* ds, cudaStream_t stream);
 
 __global__ void k_mp_prim(const double* __restrict__ U, double* __restrict__ P, Eos e, long long N, int nv) {
     const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -35,12 +37,6 @@ __global__ void k_mp_prim(const double* __restrict__ U, double* __restrict__ P, 
     cons2prim(e, Q, V);
     for (int c = 0; c < nv; ++c) P[c * N + q] = V[c];
 }
-
-// out = a*X + b*Y + (c*dt)*L, L the divergence with the volume-fraction term
-struct Stage {
-    double a, b, c, d;  // c*dt/d: the stage's dt fraction formed as the reference forms dt/r
-    int rhs_only;
-};
 
 // Win, X, Y and out may be one array (in-place stages), so they carry no __restrict__
 __global__ void __launch_bounds__(256) k_mp_update(const double* __restrict__ F, const double* __restrict__ G,
@@ -126,6 +122,7 @@ struct hype_mp2d {
     Eos e;
     cudaStream_t stream = nullptr;
     double *U = nullptr, *W0 = nullptr, *W1 = nullptr, *L = nullptr, *S = nullptr, *P = nullptr;
+    float* Pf = nullptr;  // the FP32 form's primitives
     void* T = nullptr;
     double *F = nullptr, *G = nullptr, *stage_aos = nullptr;
     DevScalars* ds = nullptr;
@@ -138,7 +135,6 @@ struct hype_mp2d {
 
 static int mp_rhs(hype_mp2d* m, const double* Win, int slot) {
     const Geo& g = m->g;
-    k_mp_prim<<<cdiv(g.N, 256), 256, 0, m->stream>>>(Win, m->P, m->e, g.N, g.nv);
     const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4));
     const dim3 gx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4)), gy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4));
     const bool f32 = m->p.precision == HYPE_PREC_FP32;
@@ -156,12 +152,12 @@ static int mp_rhs(hype_mp2d* m, const double* Win, int slot) {
         k_mp_faces<R, M, 1><<<gy, br, 0, m->stream>>>((const R*)m->T, Gf, g, m->e, m->ds, slot);               \
     } while (0)
     if (f32) {  // the FP32 form lives in mphase2d_f32.cu (compiled with FMA contraction)
-        launch_rhs_f32(m->e.model, learned, m->P, m->T, m->F, Gf, g, m->e, m->ds, slot, m->mlp, m->logit_thr, m->flagged,
-                       m->stream);
-    } else if (m->e.model == HYPE_MP_DI4) {
-        MP_LAUNCH(double, HYPE_MP_DI4);
+        launch_rhs_f32(m->e.model, learned, Win, m->Pf, m->T, (float*)m->F, (float*)Gf, g, m->e, m->ds, slot, m->mlp,
+                       m->logit_thr, m->flagged, m->stream);
     } else {
-        MP_LAUNCH(double, HYPE_MP_KAPILA5);
+        k_mp_prim<<<cdiv(g.N, 256), 256, 0, m->stream>>>(Win, m->P, m->e, g.N, g.nv);
+        if (m->e.model == HYPE_MP_DI4) MP_LAUNCH(double, HYPE_MP_DI4);
+        else MP_LAUNCH(double, HYPE_MP_KAPILA5);
     }
 #undef MP_LAUNCH
     HYPE_LAUNCHED(4);
@@ -171,7 +167,10 @@ static int mp_rhs(hype_mp2d* m, const double* Win, int slot) {
 static int mp_update(hype_mp2d* m, const double* Win, const double* X, const double* Y, double* out, Stage st) {
     const Geo& g = m->g;
     const dim3 b(32, 8), gr(cdiv(g.nx, 32), cdiv(g.ny, 8));
-    k_mp_update<<<gr, b, 0, m->stream>>>(m->F, m->G, Win, X, Y, out, g, 1.0 / m->p.h, st, m->ds);
+    if (m->p.precision == HYPE_PREC_FP32)  // FP32 face fluxes (mphase2d_f32.cu)
+        launch_update_f32((const float*)m->F, (const float*)m->G, Win, X, Y, out, g, 1.0 / m->p.h, st, m->ds, m->stream);
+    else
+        k_mp_update<<<gr, b, 0, m->stream>>>(m->F, m->G, Win, X, Y, out, g, 1.0 / m->p.h, st, m->ds);
     HYPE_LAUNCHED(1);
     return HYPE_OK;
 }
@@ -205,6 +204,8 @@ extern "C" int hype_mp2d_create(const hype_mp2d_params* p, hype_mp2d** out) {
     for (auto b : bufs)
         if (ce == cudaSuccess) ce = cudaMalloc((void**)b, sN);
     if (ce == cudaSuccess) ce = cudaMalloc(&m->T, tsz);
+    if (ce == cudaSuccess && p->precision == HYPE_PREC_FP32)
+        ce = cudaMalloc((void**)&m->Pf, sizeof(float) * g.nv * (size_t)g.N);
     if (ce == cudaSuccess) ce = cudaMalloc((void**)&m->F, sizeof(double) * (g.nv + 1) * (size_t)(p->nx + 1) * p->ny);
     if (ce == cudaSuccess) ce = cudaMalloc((void**)&m->G, sizeof(double) * (g.nv + 1) * (size_t)p->nx * (p->ny + 1));
     if (ce == cudaSuccess) ce = cudaMalloc((void**)&m->ds, sizeof(DevScalars));
@@ -230,7 +231,7 @@ extern "C" void hype_mp2d_destroy(hype_mp2d* m) {
     if (!m) return;
     if (m->stream) cudaStreamSynchronize(m->stream);
     cudaFree(m->U); cudaFree(m->W0); cudaFree(m->W1); cudaFree(m->L); cudaFree(m->S); cudaFree(m->P);
-    cudaFree(m->stage_aos); cudaFree(m->T); cudaFree(m->F); cudaFree(m->G); cudaFree(m->ds);
+    cudaFree(m->stage_aos); cudaFree(m->T); cudaFree(m->Pf); cudaFree(m->F); cudaFree(m->G); cudaFree(m->ds);
     cudaFree(m->mlp); cudaFree(m->flagged);
     if (m->hs) cudaFreeHost(m->hs);
     if (m->stream) cudaStreamDestroy(m->stream);

@@ -19,6 +19,12 @@ struct Geo {
     long long N, NE;  // owned cells, extended cells (nx+2)(ny+2)
 };
 
+// out = a*X + b*Y + (c*dt)*L, L the divergence with the volume-fraction term
+struct Stage {
+    double a, b, c, d;  // c*dt/d: the stage's dt fraction formed as the reference forms dt/r
+    int rhs_only;
+};
+
 struct DevScalars {
     unsigned long long smax_bits[12];  // per stage (10 max) + RHS-only slot 11
     double dt, t;
@@ -64,12 +70,12 @@ __device__ __forceinline__ void cell_map(const Geo& g, int i, int j, CellMap& cm
     cm.e = (long long)(j + 1) * (g.nx + 2) + (i + 1);
 }
 
-// primitive variable c at offset (oi, oj); a reflective ghost negates the velocity
-// normal to its wall (x: u, y: v)
-template <int MODEL>
-__device__ __forceinline__ double ldp(const double* __restrict__ P, const Geo& g, const CellMap& cm, int c, int oi, int oj) {
+// primitive variable c at offset (oi, oj) of the FP64 primitives or of the FP32 form's FP32 copy
+// (PT); a reflective ghost negates the velocity normal to its wall (x: u, y: v)
+template <int MODEL, typename PT>
+__device__ __forceinline__ PT ldp(const PT* __restrict__ P, const Geo& g, const CellMap& cm, int c, int oi, int oj) {
     constexpr int IU = MODEL == HYPE_MP_DI4 ? 1 : 2;
-    double v = __ldg(P + (long long)c * g.N + (long long)cm.mj[oj + 2] * g.nx + cm.mi[oi + 2]);
+    PT v = __ldg(P + (long long)c * g.N + (long long)cm.mj[oj + 2] * g.nx + cm.mi[oi + 2]);
     if (c == IU && ((cm.fi >> (oi + 2)) & 1)) v = -v;
     if (c == IU + 1 && ((cm.fj >> (oj + 2)) & 1)) v = -v;
     return v;
@@ -77,8 +83,8 @@ __device__ __forceinline__ double ldp(const double* __restrict__ P, const Geo& g
 
 // one cell: 2D CWENO4 (or its optimal-weight R4 limit) of every primitive variable,
 // its 8 face traces; returns whether the 8 admissibility nodes pass (rhs_function.c:173-250)
-template <typename R, int MODEL>
-__device__ __forceinline__ bool mp_cell_recon(const double* __restrict__ P, R* __restrict__ T, const Geo& g, const Eos& e,
+template <typename R, int MODEL, typename PT>
+__device__ __forceinline__ bool mp_cell_recon(const PT* __restrict__ P, R* __restrict__ T, const Geo& g, const Eos& e,
                                               const CellMap& cm, bool linear) {
     constexpr int NV = MODEL == HYPE_MP_DI4 ? 5 : 6;
     R VN[8][NV];
@@ -117,8 +123,8 @@ __device__ __forceinline__ bool mp_cell_recon(const double* __restrict__ P, R* _
 }
 
 // physically inadmissible somewhere in the cell: first order + minmod slopes (rhs_function.c:239-250)
-template <typename R, int MODEL>
-__device__ __forceinline__ void mp_cell_fallback(const double* __restrict__ P, R* __restrict__ T, const Geo& g,
+template <typename R, int MODEL, typename PT>
+__device__ __forceinline__ void mp_cell_fallback(const PT* __restrict__ P, R* __restrict__ T, const Geo& g,
                                                  const CellMap& cm) {
     constexpr int NV = MODEL == HYPE_MP_DI4 ? 5 : 6;
 #pragma unroll 1
@@ -135,8 +141,9 @@ __device__ __forceinline__ void mp_cell_fallback(const double* __restrict__ P, R
     }
 }
 
-template <typename R, int MODEL>
-__global__ void __launch_bounds__(128) k_mp_recon(const double* __restrict__ P, R* __restrict__ T, Geo g, Eos e,
+// PT: the primitives' type (FP64; the FP32 form reads its FP32 copy)
+template <typename R, int MODEL, typename PT = double>
+__global__ void __launch_bounds__(128) k_mp_recon(const PT* __restrict__ P, R* __restrict__ T, Geo g, Eos e,
                                                   DevScalars* __restrict__ ds) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
@@ -145,17 +152,19 @@ __global__ void __launch_bounds__(128) k_mp_recon(const double* __restrict__ P, 
     if (gi && gj) return;
     CellMap cm;
     cell_map(g, i, j, cm);
-    if (mp_cell_recon<R, MODEL>(P, T, g, e, cm, false)) return;
+    if (mp_cell_recon<R, MODEL, PT>(P, T, g, e, cm, false)) return;
     if (!gi && !gj) atomicAdd(&ds->fallback, 1ull);
-    mp_cell_fallback<R, MODEL>(P, T, g, cm);
+    mp_cell_fallback<R, MODEL, PT>(P, T, g, cm);
 }
 
 // Network inputs of one cell along direction d (0: x, 1: y): the normalised 5-point
 // stencils of the mixture density, the normal and tangential velocity, the pressure
 // and the volume fraction, each against a floor of 1 % of its magnitude in the cell
 // (density |rho|, velocities sqrt((|p| + pi)/rho), pressure |p| + pi, volume fraction 1).
-template <int MODEL>
-__device__ __forceinline__ void mp_features(const double* __restrict__ P, const Geo& g, const Eos& e, const CellMap& cm,
+// From the FP64 primitives (PT = double) or, in the FP32 form, from its FP32 copy (the mixture
+// density and the floor's pi then in FP32).
+template <int MODEL, typename PT = double>
+__device__ __forceinline__ void mp_features(const PT* __restrict__ P, const Geo& g, const Eos& e, const CellMap& cm,
                                             int d, float* x) {
     constexpr int IU = MODEL == HYPE_MP_DI4 ? 1 : 2;
     constexpr int IP = MODEL == HYPE_MP_DI4 ? 3 : 4;
@@ -164,21 +173,28 @@ __device__ __forceinline__ void mp_features(const double* __restrict__ P, const 
 #pragma unroll
     for (int o = 0; o < 5; ++o) {
         const int oi = d == 0 ? o - 2 : 0, oj = d == 1 ? o - 2 : 0;
-        const double a = ldp<MODEL>(P, g, cm, IA, oi, oj);
-        const double rho = MODEL == HYPE_MP_DI4
-                               ? ldp<MODEL>(P, g, cm, 0, oi, oj)
-                               : a * ldp<MODEL>(P, g, cm, 0, oi, oj) + (1.0 - a) * ldp<MODEL>(P, g, cm, 1, oi, oj);
-        const double u = ldp<MODEL>(P, g, cm, IU, oi, oj), v = ldp<MODEL>(P, g, cm, IU + 1, oi, oj);
+        const PT a = ldp<MODEL>(P, g, cm, IA, oi, oj);
+        const PT rho = MODEL == HYPE_MP_DI4
+                           ? ldp<MODEL>(P, g, cm, 0, oi, oj)
+                           : a * ldp<MODEL>(P, g, cm, 0, oi, oj) + (PT(1.0) - a) * ldp<MODEL>(P, g, cm, 1, oi, oj);
+        const PT u = ldp<MODEL>(P, g, cm, IU, oi, oj), v = ldp<MODEL>(P, g, cm, IU + 1, oi, oj);
         q[0][o] = (float)rho;
         q[1][o] = (float)(d == 0 ? u : v);
         q[2][o] = (float)(d == 0 ? v : u);
         q[3][o] = (float)ldp<MODEL>(P, g, cm, IP, oi, oj);
         q[4][o] = (float)a;
     }
-    double gm, pi;
-    mix(e, (double)q[4][2], gm, pi);
+    float pif;
+    if constexpr (sizeof(PT) == sizeof(double)) {
+        double gm, pi;
+        mix(e, (double)q[4][2], gm, pi);
+        pif = (float)pi;
+    } else {
+        float gm;
+        mix_r<float>(e, q[4][2], gm, pif);
+    }
     const float srho = fabsf(q[0][2]) + 1e-30f;
-    const float sp = fabsf(q[3][2]) + (float)pi;
+    const float sp = fabsf(q[3][2]) + pif;
     const float svel = sqrtf(sp / srho);
     const float sc[5] = {srho, svel, svel, sp, 1.0f};
 #pragma unroll
@@ -189,8 +205,8 @@ __device__ __forceinline__ void mp_features(const double* __restrict__ P, const 
 // each cell from its two directional stencils on the tensor cores; flagged cells take
 // the full CWENO4, the others its R4 limit; R4 traces that fail the admissibility
 // nodes are redone with CWENO4, and the minmod fallback stays the last resort.
-template <typename R, int MODEL>
-__global__ void __launch_bounds__(128) k_mp_recon_learned(const double* __restrict__ P, R* __restrict__ T, Geo g, Eos e,
+template <typename R, int MODEL, typename PT = double>
+__global__ void __launch_bounds__(128) k_mp_recon_learned(const PT* __restrict__ P, R* __restrict__ T, Geo g, Eos e,
                                                           DevScalars* __restrict__ ds,
                                                           const mlp::MmaWeights* __restrict__ wts, float logit_thr,
                                                           unsigned long long* __restrict__ flagged) {
@@ -208,7 +224,7 @@ __global__ void __launch_bounds__(128) k_mp_recon_learned(const double* __restri
 #pragma unroll 1
     for (int d = 0; d < 2; ++d) {
         float x[mlp::NIN];
-        if (active) mp_features<MODEL>(P, g, e, cm, d, x);
+        if (active) mp_features<MODEL, PT>(P, g, e, cm, d, x);
         mlp::stage_row(rows[threadIdx.y] + (threadIdx.x * 2 + d) * mlp::RSTRIDE, x, active);
     }
     __syncthreads();  // counter cleared, rows staged
@@ -217,14 +233,14 @@ __global__ void __launch_bounds__(128) k_mp_recon_learned(const double* __restri
     const float best = fmaxf(lg[threadIdx.y][threadIdx.x * 2], lg[threadIdx.y][threadIdx.x * 2 + 1]);
     if (active) {
         bool full = best > logit_thr;
-        bool ok = mp_cell_recon<R, MODEL>(P, T, g, e, cm, !full);
+        bool ok = mp_cell_recon<R, MODEL, PT>(P, T, g, e, cm, !full);
         if (!ok && !full) {
             full = true;
-            ok = mp_cell_recon<R, MODEL>(P, T, g, e, cm, false);
+            ok = mp_cell_recon<R, MODEL, PT>(P, T, g, e, cm, false);
         }
         if (!ok) {
             if (!gi && !gj) atomicAdd(&ds->fallback, 1ull);
-            mp_cell_fallback<R, MODEL>(P, T, g, cm);
+            mp_cell_fallback<R, MODEL, PT>(P, T, g, cm);
         }
         if (full && best > logit_thr && !gi && !gj) atomicAdd(&cnt, 1u);
     }
@@ -282,8 +298,9 @@ __global__ void __launch_bounds__(128) k_mp_features(const double* __restrict__ 
     D[s] = (float)dmax;
 }
 
+// face fluxes stored in the solver's type (FP64; the FP32 form keeps them in FP32 for its update)
 template <typename R, int MODEL, int D>
-__global__ void __launch_bounds__(128) k_mp_faces(const R* __restrict__ T, double* __restrict__ F, Geo g, Eos e,
+__global__ void __launch_bounds__(128) k_mp_faces(const R* __restrict__ T, R* __restrict__ F, Geo g, Eos e,
                                                   DevScalars* __restrict__ ds, int slot) {
     constexpr int NV = MODEL == HYPE_MP_DI4 ? 5 : 6;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -313,7 +330,7 @@ __global__ void __launch_bounds__(128) k_mp_faces(const R* __restrict__ T, doubl
         const long long nf = (long long)fx * fy;
         const long long f = (long long)j * fx + i;
 #pragma unroll
-        for (int c = 0; c <= NV; ++c) F[c * nf + f] = (double)acc[c];
+        for (int c = 0; c <= NV; ++c) F[c * nf + f] = acc[c];
         if (bad) atomicMin(&ds->bad, (unsigned long long)((long long)(j < g.ny ? j : g.ny - 1) * g.nx + (i < g.nx ? i : g.nx - 1)));
     }
 #pragma unroll

@@ -250,6 +250,17 @@ template <typename R>
 __device__ __forceinline__ bool pad_ok(const Eos& e, const R* V) {
     double g, pi;
     const bool stiff_nonneg = e.p1 >= 0.0 && e.p2 >= 0.0 && e.g1 > 1.0 && e.g2 > 1.0;
+    if constexpr (sizeof(R) == sizeof(float)) {
+        // the same tests on the FP32 values without converting them: for a float x, (double)x < c
+        // exactly when x < c rounded up to a float
+        const float rho_floor = __double2float_ru(1.0e-14), p_floor = __double2float_ru(1.0e-12);
+        const int ia = e.model == HYPE_MP_DI4 ? 4 : 5, ip = ia - 1;
+        const float a = V[ia], p = V[ip];
+        if (V[0] < rho_floor || (e.model != HYPE_MP_DI4 && V[1] < rho_floor) || a < 0.0f || a > 1.0f) return false;
+        if (stiff_nonneg && !(p < p_floor)) return true;
+        mix(e, (double)a, g, pi);
+        return !(((double)p + pi) < 1.0e-12);
+    }
     if (e.model == HYPE_MP_DI4) {
         const double phi = (double)V[4], p = (double)V[3];
         if ((double)V[0] < 1.0e-14 || phi < 0.0 || phi > 1.0) return false;
