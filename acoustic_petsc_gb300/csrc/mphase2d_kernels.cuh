@@ -292,60 +292,82 @@ __device__ __forceinline__ void prim2cons(const R* V, R g, R pi, R* Q) {
     }
 }
 
-// physical flux of a primitive state and its wave speed (PDEFluxPrim, pde.c:62-97); (g, pi) as for
-// prim2cons
+// What one side of a face point gives independently of the normal (pde.c:24-129, HLLC :131-232):
+// its conserved state (PDEPrim2Cons), mixture density, sound speed sqrt(g (p + pi) / rho) (the
+// same expression in PDEFluxPrim and in the HLLC speeds), HLLC's own energy expression, and the
+// admissibility flag of PDEFluxPrim.  The rotated solver makes two HLLC evaluations per face point;
+// the reference forms these in each, here once per side: the same expressions, the same values.
+template <typename R>
+struct Side2 {
+    R Q[MAXV];
+    R rho, c, Eh;
+};
+
 template <typename R, int MODEL>
-__device__ __forceinline__ R flux_prim(const R* V, R g, R pi, R nx, R ny, R* F, bool& bad) {
+__device__ __forceinline__ void make_side2(const R* V, R g, R pi, Side2<R>& s, bool& bad) {
+    prim2cons<R, MODEL>(V, g, pi, s.Q);
+    R u, v, p;
+    if (MODEL == HYPE_MP_DI4) {
+        s.rho = V[0]; u = V[1]; v = V[2]; p = V[3];
+    } else {
+        s.rho = V[5] * V[0] + (R(1.0) - V[5]) * V[1];  // a1 r1 + a2 r2
+        u = V[2]; v = V[3]; p = V[4];
+    }
+    bad |= (s.rho < R(1.0e-14)) || ((p + pi) < R(1.0e-12)) || !(s.rho == s.rho);
+    s.c = sqrt(g * (p + pi) / s.rho);
+    s.Eh = (p + g * pi) / (g - R(1.0)) + R(0.5) * s.rho * u * u + R(0.5) * s.rho * v * v;
+}
+
+// physical flux of a primitive state along (nx, ny) and its wave speed (PDEFluxPrim, pde.c:62-97);
+// its energy (p + g pi)/(g - 1) + rho |u|^2 / 2 is the conserved energy of the side
+template <typename R, int MODEL>
+__device__ __forceinline__ R flux_prim(const R* V, const Side2<R>& s, R nx, R ny, R* F) {
     if (MODEL == HYPE_MP_DI4) {
         const R phi = V[4];
         const R rho = V[0], u = V[1], v = V[2], p = V[3];
-        const R E = (p + g * pi) / (g - R(1.0)) + R(0.5) * rho * (u * u + v * v);
+        const R E = s.Q[3];
         const R un = u * nx + v * ny;
         const R rhoun = rho * un;
-        bad |= (rho < R(1.0e-14)) || ((p + pi) < R(1.0e-12)) || !(rho == rho);
         F[0] = rhoun; F[1] = rhoun * u + p * nx; F[2] = rhoun * v + p * ny; F[3] = un * (E + p); F[4] = phi * un;
-        return fabs(un) + sqrt(g * (p + pi) / rho);
+        return fabs(un) + s.c;
     }
     const R a1 = V[5], a2 = R(1.0) - a1;
     const R r1 = V[0], r2 = V[1], u = V[2], v = V[3], p = V[4];
-    const R rho = a1 * r1 + a2 * r2;
-    const R E = (p + g * pi) / (g - R(1.0)) + R(0.5) * rho * (u * u + v * v);
+    const R rho = s.rho;
+    const R E = s.Q[4];
     const R un = u * nx + v * ny;
-    bad |= (rho < R(1.0e-14)) || ((p + pi) < R(1.0e-12)) || !(rho == rho);
     F[0] = a1 * r1 * un; F[1] = a2 * r2 * un; F[2] = rho * u * un + p * nx; F[3] = rho * v * un + p * ny;
     F[4] = (E + p) * un; F[5] = a1 * un;
-    return fabs(un) + sqrt(g * (p + pi) / rho);
+    return fabs(un) + s.c;
 }
 
 // HLLC with the interface velocity as the last component (HLLCRiemannSolver, pde.c:131-232);
 // star partial densities of the five-equation model a_k r_k (S - u_n)/(S - S*).  The reference
-// re-forms each side's mixture in every EOS call; it depends on the side's state alone, so the
-// caller forms it once per face point (gL, piL / gR, piR): the same values, a twelfth of the
-// mixture evaluations
+// re-forms each side's mixture and EOS quantities in every EOS call; they depend on the side's
+// state alone, so the caller forms them once per face point (sides L, R): the same values, a
+// fraction of the divisions and square roots
 template <typename R, int MODEL>
-__device__ __forceinline__ R hllc2(const R* VL, const R* VR, R gL, R piL, R gR, R piR, R nx, R ny, R* Flux,
-                                   bool& bad) {
+__device__ __forceinline__ R hllc2(const R* VL, const R* VR, const Side2<R>& sL, const Side2<R>& sR, R nx, R ny,
+                                   R* Flux) {
     constexpr int NV = MODEL == HYPE_MP_DI4 ? 5 : 6;
-    R QL[MAXV], QR[MAXV], FL[MAXV + 1], FR[MAXV + 1];
-    prim2cons<R, MODEL>(VL, gL, piL, QL);
-    prim2cons<R, MODEL>(VR, gR, piR, QR);
-    const R sl = flux_prim<R, MODEL>(VL, gL, piL, nx, ny, FL, bad);
-    const R sr = flux_prim<R, MODEL>(VR, gR, piR, nx, ny, FR, bad);
-    R rL, rR, uL, uR, vL, vR, PL, PR;
+    R FL[MAXV + 1], FR[MAXV + 1];
+    const R* QL = sL.Q;
+    const R* QR = sR.Q;
+    const R sl = flux_prim<R, MODEL>(VL, sL, nx, ny, FL);
+    const R sr = flux_prim<R, MODEL>(VR, sR, nx, ny, FR);
+    R uL, uR, vL, vR, PL, PR;
     if (MODEL == HYPE_MP_DI4) {
-        rL = VL[0]; uL = VL[1]; vL = VL[2]; PL = VL[3];
-        rR = VR[0]; uR = VR[1]; vR = VR[2]; PR = VR[3];
+        uL = VL[1]; vL = VL[2]; PL = VL[3];
+        uR = VR[1]; vR = VR[2]; PR = VR[3];
     } else {
-        rL = VL[5] * VL[0] + (R(1.0) - VL[5]) * VL[1];
-        rR = VR[5] * VR[0] + (R(1.0) - VR[5]) * VR[1];
         uL = VL[2]; vL = VL[3]; PL = VL[4];
         uR = VR[2]; vR = VR[3]; PR = VR[4];
     }
+    const R rL = sL.rho, rR = sR.rho;
     const R unL = uL * nx + vL * ny, utL = -uL * ny + vL * nx;
     const R unR = uR * nx + vR * ny, utR = -uR * ny + vR * nx;
-    const R cL = sqrt(gL * (PL + piL) / rL), cR = sqrt(gR * (PR + piR) / rR);
-    const R EL = (PL + gL * piL) / (gL - R(1.0)) + R(0.5) * rL * uL * uL + R(0.5) * rL * vL * vL;
-    const R ER = (PR + gR * piR) / (gR - R(1.0)) + R(0.5) * rR * uR * uR + R(0.5) * rR * vR * vR;
+    const R cL = sL.c, cR = sR.c;
+    const R EL = sL.Eh, ER = sR.Eh;
     const R a1 = unR - cR, b1 = unL - cL;
     const R SL = (a1 < b1) ? a1 : b1;
     const R a2 = unL + cL, b2 = unR + cR;
@@ -414,12 +436,15 @@ __device__ __forceinline__ R rot_hllc2(const Eos& e, const R* VL, const R* VR, R
     if (a2 < R(0)) {
         n2x = -n2x; n2y = -n2y; a2 = -a2;
     }
-    R gL, piL, gR, piR;  // each side's mixture, once for both solves
+    R gL, piL, gR, piR;  // each side's mixture and EOS quantities, once for both solves
     mix_r<R>(e, VL[NV - 1], gL, piL);
     mix_r<R>(e, VR[NV - 1], gR, piR);
+    Side2<R> sL, sR;
+    make_side2<R, MODEL>(VL, gL, piL, sL, bad);
+    make_side2<R, MODEL>(VR, gR, piR, sR, bad);
     R f1[MAXV + 1], f2[MAXV + 1];
-    const R s1 = hllc2<R, MODEL>(VL, VR, gL, piL, gR, piR, n1x, n1y, f1, bad);
-    const R s2 = hllc2<R, MODEL>(VL, VR, gL, piL, gR, piR, n2x, n2y, f2, bad);
+    const R s1 = hllc2<R, MODEL>(VL, VR, sL, sR, n1x, n1y, f1);
+    const R s2 = hllc2<R, MODEL>(VL, VR, sL, sR, n2x, n2y, f2);
 #pragma unroll
     for (int k = 0; k <= NV; ++k) Flux[k] = a1 * f1[k] + a2 * f2[k];
     return (s1 < s2) ? s2 : s1;
