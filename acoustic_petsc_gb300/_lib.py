@@ -41,7 +41,8 @@ SYMBOLS = [
     "hype_euler_rhs_noalloc", "hype_euler_noalloc_max_ext", "hype_euler_set_stage_kernel",
     "hype_mp2d_create", "hype_mp2d_destroy", "hype_mp2d_rhs", "hype_mp2d_upload", "hype_mp2d_download",
     "hype_mp2d_step", "hype_mp2d_sync", "hype_mp2d_stream", "hype_mp2d_set_mlp", "hype_mp2d_set_recon",
-    "hype_mp2d_indicator_stats", "hype_mp2d_sample_features", "hype_euler_get_params", "hype_mp2d_get_params",
+    "hype_mp2d_indicator_stats", "hype_mp2d_set_gate_per_step", "hype_mp2d_gate_flags", "hype_mp2d_sample_features",
+    "hype_euler_get_params", "hype_mp2d_get_params",
     "hype_write_petsc_vec", "hype_read_petsc_vec", "hype_write_vtk", "hype_euler_write_restart",
     "hype_euler_read_restart", "hype_euler_write_vtk", "hype_mp2d_write_restart", "hype_mp2d_read_restart",
     "hype_mp2d_write_vtk", "hype_acoustic_create", "hype_acoustic_destroy", "hype_acoustic_upload",
@@ -193,6 +194,8 @@ def lib():
         "hype_mp2d_set_mlp": ([V, F, C.c_float], C.c_int),
         "hype_mp2d_set_recon": ([V, C.c_int], C.c_int),
         "hype_mp2d_indicator_stats": ([V, P(C.c_longlong), C.c_int], C.c_int),
+        "hype_mp2d_set_gate_per_step": ([V, C.c_int], C.c_int),
+        "hype_mp2d_gate_flags": ([V, C.c_void_p, C.c_int], C.c_int),
         "hype_mp2d_sample_features": ([V, C.c_longlong, F, F, P(C.c_longlong)], C.c_int),
         "hype_euler_get_params": ([V, P(EulerParams)], C.c_int),
         "hype_mp2d_get_params": ([V, P(Mp2dParams)], C.c_int),

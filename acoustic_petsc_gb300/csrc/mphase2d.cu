@@ -25,7 +25,7 @@ namespace mp2d {
 
 int launch_rhs_f32(int model, bool learned, const double* Win, float* Pf, void* T, float* F, float* G, const Geo& g,
                    const Eos& e, DevScalars* ds, int slot, const mlp::MmaWeights* mlp, float logit_thr,
-                   unsigned long long* flagged, cudaStream_t st);
+                   unsigned long long* flagged, const GateStep& gs, cudaStream_t st);
 void launch_update_f32(const float* F, const float* G, const double* Win, const double* X, const double* Y, double* out,
                        const Geo& g, double r1_h, Stage st, const DevScalars* ds, cudaStream_t stream);
 
@@ -131,6 +131,10 @@ struct hype_mp2d {
     mlp::MmaWeights* mlp = nullptr;
     float logit_thr = 0.0f;
     unsigned long long* flagged = nullptr;
+    // the gate scored once per step: the network's flags and their 3 x 3 widening, one byte per
+    // extended cell (allocated with the network)
+    unsigned char *gate = nullptr, *gate_wide = nullptr;
+    int gate_per_step = 0;
 };
 
 static int mp_rhs(hype_mp2d* m, const double* Win, int slot) {
@@ -141,9 +145,15 @@ static int mp_rhs(hype_mp2d* m, const double* Win, int slot) {
     const bool learned = m->p.recon == HYPE_RECON_LEARNED;
     if (learned && !m->mlp) return HYPE_ERR_ARG;  // hype_mp2d_set_mlp first
     double* Gf = m->G;
+    // gate scored once per step: on the step's first stage (slot 0) and on RHS-only calls (slot 11)
+    const bool per_step = learned && m->gate_per_step != 0;
+    const GateStep gs{per_step, per_step && (slot == 0 || slot == 11), m->gate, m->gate_wide};
 #define MP_LAUNCH(R, M)                                                                                        \
     do {                                                                                                       \
-        if (learned)                                                                                           \
+        if (gs.on)                                                                                             \
+            launch_gated_recon<R, M, double>(m->P, (R*)m->T, g, m->e, m->ds, m->mlp, m->logit_thr, m->flagged, \
+                                             gs, m->stream);                                                   \
+        else if (learned)                                                                                      \
             k_mp_recon_learned<R, M><<<gr, br, 0, m->stream>>>(m->P, (R*)m->T, g, m->e, m->ds, m->mlp,         \
                                                                m->logit_thr, m->flagged);                      \
         else                                                                                                   \
@@ -153,14 +163,14 @@ static int mp_rhs(hype_mp2d* m, const double* Win, int slot) {
     } while (0)
     if (f32) {  // the FP32 form lives in mphase2d_f32.cu (compiled with FMA contraction)
         launch_rhs_f32(m->e.model, learned, Win, m->Pf, m->T, (float*)m->F, (float*)Gf, g, m->e, m->ds, slot, m->mlp,
-                       m->logit_thr, m->flagged, m->stream);
+                       m->logit_thr, m->flagged, gs, m->stream);
     } else {
         k_mp_prim<<<cdiv(g.N, 256), 256, 0, m->stream>>>(Win, m->P, m->e, g.N, g.nv);
         if (m->e.model == HYPE_MP_DI4) MP_LAUNCH(double, HYPE_MP_DI4);
         else MP_LAUNCH(double, HYPE_MP_KAPILA5);
     }
 #undef MP_LAUNCH
-    HYPE_LAUNCHED(4);
+    HYPE_LAUNCHED(4 + (gs.score ? 2 : 0));
     return HYPE_OK;
 }
 
@@ -232,7 +242,7 @@ extern "C" void hype_mp2d_destroy(hype_mp2d* m) {
     if (m->stream) cudaStreamSynchronize(m->stream);
     cudaFree(m->U); cudaFree(m->W0); cudaFree(m->W1); cudaFree(m->L); cudaFree(m->S); cudaFree(m->P);
     cudaFree(m->stage_aos); cudaFree(m->T); cudaFree(m->Pf); cudaFree(m->F); cudaFree(m->G); cudaFree(m->ds);
-    cudaFree(m->mlp); cudaFree(m->flagged);
+    cudaFree(m->mlp); cudaFree(m->flagged); cudaFree(m->gate); cudaFree(m->gate_wide);
     if (m->hs) cudaFreeHost(m->hs);
     if (m->stream) cudaStreamDestroy(m->stream);
     delete m;
@@ -370,6 +380,12 @@ extern "C" int hype_mp2d_set_mlp(hype_mp2d* m, const float* params, float prob_t
     mlp::MmaWeights hw;  // host staging, copied before the stream synchronisation below
     mlp::pack_weights(h.data(), hw);
     if (!m->mlp) HYPE_CK(cudaMalloc((void**)&m->mlp, sizeof(mlp::MmaWeights)));
+    if (!m->gate) {
+        HYPE_CK(cudaMalloc((void**)&m->gate, (size_t)m->g.NE));
+        HYPE_CK(cudaMalloc((void**)&m->gate_wide, (size_t)m->g.NE));
+        HYPE_CK(cudaMemsetAsync(m->gate, 0, (size_t)m->g.NE, m->stream));
+        HYPE_CK(cudaMemsetAsync(m->gate_wide, 0, (size_t)m->g.NE, m->stream));
+    }
     HYPE_CK(cudaMemcpyAsync(m->mlp, &hw, sizeof(mlp::MmaWeights), cudaMemcpyHostToDevice, m->stream));
     HYPE_CK(cudaStreamSynchronize(m->stream));
     m->logit_thr = logf(prob_threshold / (1.0f - prob_threshold));
@@ -380,6 +396,21 @@ extern "C" int hype_mp2d_set_recon(hype_mp2d* m, int recon) {
     if (!m || (recon != HYPE_RECON_CWENO4 && recon != HYPE_RECON_LEARNED)) return HYPE_ERR_ARG;
     HYPE_CK(cudaStreamSynchronize(m->stream));
     m->p.recon = recon;
+    return HYPE_OK;
+}
+
+extern "C" int hype_mp2d_set_gate_per_step(hype_mp2d* m, int per_step) {
+    if (!m || (per_step != 0 && per_step != 1)) return HYPE_ERR_ARG;
+    HYPE_CK(cudaStreamSynchronize(m->stream));
+    m->gate_per_step = per_step;
+    return HYPE_OK;
+}
+
+extern "C" int hype_mp2d_gate_flags(hype_mp2d* m, unsigned char* out, int widened) {
+    if (!m || !out || (widened != 0 && widened != 1)) return HYPE_ERR_ARG;
+    if (!m->gate) return HYPE_ERR_UNSUPPORTED;
+    HYPE_CK(cudaMemcpyAsync(out, widened ? m->gate_wide : m->gate, (size_t)m->g.NE, cudaMemcpyDeviceToHost, m->stream));
+    HYPE_CK(cudaStreamSynchronize(m->stream));
     return HYPE_OK;
 }
 

@@ -248,6 +248,99 @@ __global__ void __launch_bounds__(128) k_mp_recon_learned(const PT* __restrict__
     if (threadIdx.x == 0 && threadIdx.y == 0 && cnt) atomicAdd(flagged, (unsigned long long)cnt);
 }
 
+// The gate scored on its own pass (hype_mp2d_set_gate_per_step: a step's first stage): one flag byte
+// per extended cell the reconstruction covers (the frame's corners keep the zero the array is created
+// with), with k_mp_recon_learned's features and tensor-core scoring
+template <int MODEL, typename PT = double>
+__global__ void __launch_bounds__(128) k_mp_gate(const PT* __restrict__ P, unsigned char* __restrict__ flag, Geo g,
+                                                 Eos e, const mlp::MmaWeights* __restrict__ wts, float logit_thr) {
+    constexpr int NR = 64;  // 32 cells x 2 directions per warp
+    __shared__ __align__(16) __nv_bfloat16 rows[4][NR * mlp::RSTRIDE];
+    __shared__ float lg[4][NR];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+    const bool gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny);
+    const bool active = !(i > g.nx || j > g.ny) && !(gi && gj);
+    CellMap cm;
+    if (active) cell_map(g, i, j, cm);
+#pragma unroll 1
+    for (int d = 0; d < 2; ++d) {
+        float x[mlp::NIN];
+        if (active) mp_features<MODEL, PT>(P, g, e, cm, d, x);
+        mlp::stage_row(rows[threadIdx.y] + (threadIdx.x * 2 + d) * mlp::RSTRIDE, x, active);
+    }
+    __syncwarp();  // the warp's rows staged
+    mlp::warp_logits<NR>(wts, rows[threadIdx.y], lg[threadIdx.y]);
+    __syncwarp();
+    if (active) flag[cm.e] = fmaxf(lg[threadIdx.y][threadIdx.x * 2], lg[threadIdx.y][threadIdx.x * 2 + 1]) > logit_thr;
+}
+
+// the gate's flags widened to each cell's 3 x 3 neighbourhood over the extended grid: flags scored
+// on a step's first stage still cover a discontinuity that moves by less than a cell in the step
+static __global__ void __launch_bounds__(128) k_mp_gate_dilate(const unsigned char* __restrict__ f, unsigned char* __restrict__ o,
+                                                        Geo g) {
+    const int ex = g.nx + 2, ey = g.ny + 2;
+    const int i = blockIdx.x * 128 + threadIdx.x, j = blockIdx.y;
+    if (i >= ex) return;
+    unsigned m = 0;
+#pragma unroll
+    for (int dj = -1; dj <= 1; ++dj) {
+        const int jj = j + dj;
+        if (jj < 0 || jj >= ey) continue;
+        const unsigned char* row = f + (long long)jj * ex;
+        m |= __ldg(row + i);
+        if (i > 0) m |= __ldg(row + i - 1);
+        if (i + 1 < ex) m |= __ldg(row + i + 1);
+    }
+    o[(long long)j * ex + i] = (unsigned char)m;
+}
+
+// k_mp_recon_learned's reconstruction on flags the gate wrote: flagged cells take CWENO4, the others
+// its R4 limit, R4 traces that fail the admissibility nodes are redone with CWENO4, the minmod
+// fallback stays the last resort; counts the owned cells the flags send to CWENO4
+template <typename R, int MODEL, typename PT = double>
+__global__ void __launch_bounds__(128) k_mp_recon_flags(const PT* __restrict__ P, R* __restrict__ T, Geo g, Eos e,
+                                                        DevScalars* __restrict__ ds,
+                                                        const unsigned char* __restrict__ flags,
+                                                        unsigned long long* __restrict__ flagged) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+    if (i > g.nx || j > g.ny) return;
+    const bool gi = (i < 0 || i >= g.nx), gj = (j < 0 || j >= g.ny);
+    if (gi && gj) return;
+    CellMap cm;
+    cell_map(g, i, j, cm);
+    bool full = flags[cm.e] != 0;
+    if (full && !gi && !gj) atomicAdd(flagged, 1ull);
+    bool ok = mp_cell_recon<R, MODEL, PT>(P, T, g, e, cm, !full);
+    if (!ok && !full) ok = mp_cell_recon<R, MODEL, PT>(P, T, g, e, cm, false);
+    if (!ok) {
+        if (!gi && !gj) atomicAdd(&ds->fallback, 1ull);
+        mp_cell_fallback<R, MODEL, PT>(P, T, g, cm);
+    }
+}
+
+// the gate passes of one RHS when the gate is scored once per step: score (and widen) on the step's
+// first stage or an RHS-only call, then every stage reconstructs from the widened flags
+struct GateStep {
+    bool on;               // hype_mp2d_set_gate_per_step
+    bool score;            // this stage scores
+    unsigned char* raw;    // the network's flags
+    unsigned char* wide;   // their 3 x 3 widening
+};
+
+template <typename R, int MODEL, typename PT>
+inline void launch_gated_recon(const PT* P, R* T, const Geo& g, const Eos& e, DevScalars* ds,
+                               const mlp::MmaWeights* wts, float logit_thr, unsigned long long* flagged,
+                               const GateStep& gs, cudaStream_t st) {
+    const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4));
+    if (gs.score) {
+        k_mp_gate<MODEL, PT><<<gr, br, 0, st>>>(P, gs.raw, g, e, wts, logit_thr);
+        k_mp_gate_dilate<<<dim3(cdiv(g.nx + 2, 128), g.ny + 2), 128, 0, st>>>(gs.raw, gs.wide, g);
+    }
+    k_mp_recon_flags<R, MODEL, PT><<<gr, br, 0, st>>>(P, T, g, e, ds, gs.wide, flagged);
+}
+
 // Training data: for every stride-th owned cell its features X[s][3][25] (x, y, and y
 // again: the training kernels take three directions and the max over a repeated row
 // is the max over the two) and D[s], the largest change that the nonlinear CWENO4

@@ -48,14 +48,16 @@ __global__ void __launch_bounds__(256) k_mp_prim_f32(const double* __restrict__ 
 // RHS of the FP32 form (Pf: its FP32 primitives)
 int launch_rhs_f32(int model, bool learned, const double* Win, float* Pf, void* T, float* F, float* G, const Geo& g,
                    const Eos& e, DevScalars* ds, int slot, const mlp::MmaWeights* mlp, float logit_thr,
-                   unsigned long long* flagged, cudaStream_t st) {
+                   unsigned long long* flagged, const GateStep& gs, cudaStream_t st) {
     const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4));
     const dim3 gx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4)), gy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4));
     k_mp_prim_f32<<<cdiv(g.N, 256), 256, 0, st>>>(Win, Pf, e, g.N);
     const float* P = Pf;
 #define MP_LAUNCH_F32(M)                                                                                       \
     do {                                                                                                       \
-        if (learned)                                                                                           \
+        if (gs.on)                                                                                             \
+            launch_gated_recon<float, M, float>(P, (float*)T, g, e, ds, mlp, logit_thr, flagged, gs, st);      \
+        else if (learned)                                                                                      \
             k_mp_recon_learned<float, M, float><<<gr, br, 0, st>>>(P, (float*)T, g, e, ds, mlp, logit_thr,     \
                                                                    flagged);                                   \
         else                                                                                                   \

@@ -459,6 +459,17 @@ class Multiphase2D:
     def set_recon(self, recon):
         check(L.lib().hype_mp2d_set_recon(self._h, int(recon)), "hype_mp2d_set_recon")
 
+    def set_gate_per_step(self, per_step):
+        """score the gate once per step (flags widened by a cell, read by the step's stages)"""
+        check(L.lib().hype_mp2d_set_gate_per_step(self._h, int(bool(per_step))), "hype_mp2d_set_gate_per_step")
+
+    def gate_flags(self, widened=False):
+        """the per-step gate's last flags, shape (ny+2, nx+2), frame included"""
+        out = np.zeros((self.ny + 2, self.nx + 2), dtype=np.uint8)
+        check(L.lib().hype_mp2d_gate_flags(self._h, out.ctypes.data_as(C.c_void_p), int(bool(widened))),
+              "hype_mp2d_gate_flags")
+        return out
+
     def indicator_stats(self, reset=False):
         """owned-cell reconstructions flagged by the network since the last reset"""
         f = C.c_longlong()

@@ -287,8 +287,17 @@ void* hype_mp2d_stream(hype_mp2d* m);
  * pressure and volume fraction along x and along y) */
 int hype_mp2d_set_mlp(hype_mp2d* m, const float* params, float prob_threshold);
 int hype_mp2d_set_recon(hype_mp2d* m, int recon);
-/* owned-cell reconstructions the network flagged (full CWENO4) since the last reset */
+/* owned-cell reconstructions the network flagged (full CWENO4) since the last reset (with the gate
+ * scored once per step: those its widened flags send to CWENO4, counted in every stage) */
 int hype_mp2d_indicator_stats(hype_mp2d* m, long long* flagged, int reset);
+/* per_step = 1: the gate is scored on each step's first stage (and on RHS-only calls) in its own
+ * pass, its flags widened to each cell's 3x3 neighbourhood and read by every stage of the step;
+ * per_step = 0 (default): scored inside every stage's reconstruction.  Both precision forms. */
+int hype_mp2d_set_gate_per_step(hype_mp2d* m, int per_step);
+/* the last flags of the per-step gate, one byte per extended cell ((nx+2)(ny+2), x fastest, cell
+ * (i, j) at (j+1)(nx+2) + i+1): widened = 0 the network's, 1 their 3x3 widening;
+ * HYPE_ERR_UNSUPPORTED before hype_mp2d_set_mlp */
+int hype_mp2d_gate_flags(hype_mp2d* m, unsigned char* out, int widened);
 /* training samples from the resident state: every stride-th owned cell, its features
  * X[s][3][25] (x, y, y: the training kernels take three directions) and D[s], the
  * largest change the nonlinear CWENO4 weights make to one of its 8 face traces relative

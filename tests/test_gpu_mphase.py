@@ -142,6 +142,100 @@ def test_kapila_learned_gain_at_equal_error(hype):
     assert frac < 0.5
 
 
+@pytest.fixture(scope="module")
+def kapila_net(hype):
+    p, _, _ = _kapila_training(hype)
+    return p
+
+
+def _widen2(f):
+    pad = np.pad(f, 1)
+    ny, nx = f.shape
+    out = np.zeros_like(f)
+    for dj in range(3):
+        for di in range(3):
+            out |= pad[dj:dj + ny, di:di + nx]
+    return out
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+def test_kapila_gate_per_step_flags(hype, kapila_net, precision):
+    """gate scored once per step: the widened flags are the 3x3 maximum of the network's flags, the
+    network's flags on an RHS-only call are the cells the per-stage gate flags on the same state
+    (its counter), and a step counts the widened owned cells in each of its four stages"""
+    L = hype._lib
+    n = 64
+    per_stage = _kapila_solver(hype, n, precision=precision, recon=L.RECON_LEARNED)
+    per_step = _kapila_solver(hype, n, precision=precision, recon=L.RECON_LEARNED)
+    for m in (per_stage, per_step):
+        m.set_mlp(kapila_net, 0.2)
+        m.step(20)  # the shock into the domain: some cells to flag
+    per_step.set_gate_per_step(True)
+    U = per_stage.get_state()
+    per_step.set_state(U)
+    per_step.indicator_stats(reset=True)
+    per_step.step(1)
+    flagged = per_step.indicator_stats(reset=True)
+    raw, wide = per_step.gate_flags(False), per_step.gate_flags(True)
+    assert raw.any()
+    assert np.array_equal(wide, _widen2(raw))
+    assert flagged == 4 * int(wide[1:-1, 1:-1].sum())
+    per_step.set_state(U)
+    per_step.RHSFunction(0.0, U)
+    per_stage.indicator_stats(reset=True)
+    per_stage.RHSFunction(0.0, U)
+    assert int(per_step.gate_flags(False)[1:-1, 1:-1].sum()) == per_stage.indicator_stats(reset=True)
+    print(f"Kapila {n}^2: {int(raw[1:-1, 1:-1].sum())} cells flagged, {int(wide[1:-1, 1:-1].sum())} after widening")
+    per_stage.close()
+    per_step.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("bias", [1000.0, -1000.0], ids=["all", "none"])
+def test_kapila_gate_per_step_limits(hype, kapila_net, precision, bias):
+    """a network that flags every cell makes the per-step gated form plain CWENO4 bit for bit; one
+    that flags none makes it the per-stage gate's R4 with the CWENO4 redo, bit for bit"""
+    L = hype._lib
+    n = 48
+    p = np.array(kapila_net, dtype=np.float32)
+    p[-1] = bias
+    out = []
+    for recon, per_step in ((L.RECON_LEARNED, True), (L.RECON_CWENO4 if bias > 0 else L.RECON_LEARNED, False)):
+        m = _kapila_solver(hype, n, precision=precision, recon=recon)
+        if recon == L.RECON_LEARNED:
+            m.set_mlp(p, 0.2)
+            m.set_gate_per_step(per_step)
+        m.step(6)
+        out.append((m.get_state(), m.t))
+        m.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert out[0][1] == out[1][1]
+
+
+def test_kapila_gate_per_step_gain_at_equal_error(hype, kapila_net):
+    """the per-step gate on the 64^2 shock-bubble problem against a 128^2 FP64 run: within 1.05x of
+    plain FP32 CWENO4's L1 error, as the per-stage gate"""
+    L = hype._lib
+    n = 64
+    ref = _kapila_solver(hype, 2 * n)
+    plain = _kapila_solver(hype, n, precision=L.PREC_FP32)
+    learned = _kapila_solver(hype, n, precision=L.PREC_FP32, recon=L.RECON_LEARNED)
+    learned.set_mlp(kapila_net, 0.2)
+    learned.set_gate_per_step(True)
+    T = 2.0e-4
+    for m in (ref, plain, learned):
+        while m.t < T:
+            m.step(1)
+    rho = lambda U: U[..., 0] + U[..., 1]  # noqa: E731
+    r_ref = rho(ref.get_state()).reshape(n, 2, n, 2).mean(axis=(1, 3))
+    e_plain = np.abs(rho(plain.get_state()) - r_ref).mean() / np.abs(r_ref).mean()
+    e_learn = np.abs(rho(learned.get_state()) - r_ref).mean() / np.abs(r_ref).mean()
+    print(f"Kapila L1(rho) vs 2x FP64: plain FP32 {e_plain:.3e}, per-step gated FP32 {e_learn:.3e}")
+    assert e_learn <= 1.05 * e_plain
+    for m in (ref, plain, learned):
+        m.close()
+
+
 def test_multiphase_restart_round_trip(hype, tmp_path):
     L = hype._lib
     m = _kapila_solver(hype, 40)
