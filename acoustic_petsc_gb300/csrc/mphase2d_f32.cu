@@ -12,12 +12,16 @@ namespace mp2d {
 // where the stiffness term cancels most of E) and every other value formed in FP64 as cons2prim
 // does, with its divisions as FP64 reciprocals within an ulp (the values are rounded to FP32 next),
 // written as the FP32 copy the reconstruction reads
+// the mixture rules' constants, formed once on the host: (g1 - 1)(g2 - 1), g_k p_k / (g_k - 1)
+struct MixConst {
+    double c, s1, s2;
+};
+
 __global__ void __launch_bounds__(256) k_mp_prim_f32(const double* __restrict__ U, float* __restrict__ P, Eos e,
-                                                     long long N) {
+                                                     MixConst mc, long long N) {
     const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (q >= N) return;
-    const double r1 = euler::recip_wide(e.g1 - 1.0), r2 = euler::recip_wide(e.g2 - 1.0);
-    const double c = (e.g1 - 1.0) * (e.g2 - 1.0), s1 = e.g1 * e.p1 * r1, s2 = e.g2 * e.p2 * r2;
+    const double c = mc.c, s1 = mc.s1, s2 = mc.s2;
     if (e.model == HYPE_MP_DI4) {
         const double Q0 = U[q], Q1 = U[N + q], Q2 = U[2 * N + q], Q3 = U[3 * N + q], phi = U[4 * N + q];
         const double g = 1.0 + c * euler::recip_wide((1.0 - phi) * (e.g1 - 1.0) + phi * (e.g2 - 1.0));
@@ -51,7 +55,8 @@ int launch_rhs_f32(int model, bool learned, const double* Win, float* Pf, void* 
                    unsigned long long* flagged, const GateStep& gs, cudaStream_t st) {
     const dim3 br(32, 4), gr(cdiv(g.nx + 2, 32), cdiv(g.ny + 2, 4));
     const dim3 gx(cdiv(g.nx + 1, 32), cdiv(g.ny, 4)), gy(cdiv(g.nx, 32), cdiv(g.ny + 1, 4));
-    k_mp_prim_f32<<<cdiv(g.N, 256), 256, 0, st>>>(Win, Pf, e, g.N);
+    const MixConst mc{(e.g1 - 1.0) * (e.g2 - 1.0), e.g1 * e.p1 / (e.g1 - 1.0), e.g2 * e.p2 / (e.g2 - 1.0)};
+    k_mp_prim_f32<<<cdiv(g.N, 256), 256, 0, st>>>(Win, Pf, e, mc, g.N);
     const float* P = Pf;
 #define MP_LAUNCH_F32(M)                                                                                       \
     do {                                                                                                       \
