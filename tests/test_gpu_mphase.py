@@ -59,16 +59,21 @@ def test_kapila_workload_rhs_and_steps_vs_oracle(hype, oracle, model):
     assert abs(m.t - t) <= 1e-12 * t
 
 
-def test_kapila_fp32_recon_flux_error_stated(hype, oracle):
-    m, cfg, U = _kapila(hype, oracle, 96, 1, precision=1)
+@pytest.mark.parametrize("model", [0, 1], ids=["diffuse_interface", "kapila"])
+def test_kapila_fp32_recon_flux_error_stated(hype, oracle, model):
+    """the FP32 recon/flux form (FP32 primitives, mixture, fluxes; FP64 pressure, volume-fraction term
+    and stage combination) against the FP64 checker after 12 steps, both 2D models"""
+    m, cfg, U = _kapila(hype, oracle, 96, model, precision=1)
     m.set_state(U)
     m.step(12)
     Uo, t, dt, rc = oracle.mp2d_run(cfg, U, 12, stepper=0)
-    rho = m.get_state()[..., 0] + m.get_state()[..., 1]
-    rho_o = Uo[..., 0] + Uo[..., 1]
+    assert rc == 0
+    density = (lambda Q: Q[..., 0]) if model == 0 else (lambda Q: Q[..., 0] + Q[..., 1])
+    rho, rho_o = density(m.get_state()), density(Uo)
     l1 = float(np.abs(rho - rho_o).mean() / np.abs(rho_o).mean())
-    print(f"Kapila FP32 recon/flux: L1(rho) rel err {l1:.2e} after 12 steps, state rel {rel(m.get_state(), Uo):.2e}")
+    print(f"model {model} FP32 recon/flux: L1(rho) rel err {l1:.2e} after 12 steps, state rel {rel(m.get_state(), Uo):.2e}")
     assert l1 <= 1e-3
+    assert np.isfinite(m.get_state()).all()
 
 
 def _kapila_solver(hype, n, precision=0, recon=0):
