@@ -1329,12 +1329,16 @@ __global__ void __launch_bounds__(FS_NT, 1)
             // ---- reconstruction: all 24 traces of each variable into the shared array
             if (active) {
                 const bool weno = !LEARNED && recon == HYPE_RECON_WENO3;
-                fs_recon_cell(S, G, g, ge, t, LEARNED ? !full : recon == HYPE_RECON_LINEAR4, weno);
-                bool ok = (LEARNED || pad) ? fs_admissible(S, t, gm1) : true;
-                if (LEARNED && !ok && !full) {  // the R4 traces broke positivity: the cell with CWENO4
-                    full = true;
-                    fs_recon_cell(S, G, g, ge, t, false, false);
-                    ok = fs_admissible(S, t, gm1);
+                bool linear = LEARNED ? !full : recon == HYPE_RECON_LINEAR4;
+                bool ok = true;
+                // one copy of the reconstruction in the code: with the gate, R4 traces that break
+                // the floors are redone with CWENO4 on a second pass
+#pragma unroll 1
+                for (int pass = 0; pass < 2; ++pass) {
+                    fs_recon_cell(S, G, g, ge, t, linear, weno);
+                    ok = (LEARNED || pad) ? fs_admissible(S, t, gm1) : true;
+                    if (!LEARNED || ok || !linear) break;
+                    linear = false;
                 }
                 // positivity fallback: first order when the traces still break the floors
                 if (!ok && pad) {
