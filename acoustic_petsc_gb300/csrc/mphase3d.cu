@@ -67,6 +67,8 @@ __device__ __forceinline__ double mix_g(const Eos& e, double phi) {
     return 1.0 + (e.g1 - 1.0) * (e.g2 - 1.0) / ((1.0 - phi) * (e.g1 - 1.0) + phi * (e.g2 - 1.0));
 }
 __device__ __forceinline__ double mix_pinf(const Eos& e, double g, double phi) {
+    // with no stiffness in either gas both terms vanish, and so does the product: no divisions
+    if (e.p1 == 0.0 && e.p2 == 0.0) return 0.0;
     return ((g - 1.0) / g) * (e.g1 * e.p1 * phi / (e.g1 - 1.0) + e.g2 * e.p2 * (1.0 - phi) / (e.g2 - 1.0));
 }
 __device__ __forceinline__ void cons2prim(const Eos& e, const double* Q, double* V) {
