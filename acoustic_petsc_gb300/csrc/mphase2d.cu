@@ -206,7 +206,7 @@ extern "C" int hype_mp2d_create(const hype_mp2d_params* p, hype_mp2d** out) {
     for (int f = 0; f < 4; ++f) g.bc[f] = p->bc[f];
     g.N = (long long)p->nx * p->ny;
     g.NE = (long long)(p->nx + 2) * (p->ny + 2);
-    m->e = Eos{p->model, p->g1, p->p1, p->g2, p->p2};
+    m->e = make_eos(p->model, p->g1, p->p1, p->g2, p->p2);
     const size_t sN = sizeof(double) * g.nv * (size_t)g.N;
     const size_t tsz = (p->precision == HYPE_PREC_FP32 ? 4 : 8) * (size_t)g.nv * 8 * g.NE;
     cudaError_t ce = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);

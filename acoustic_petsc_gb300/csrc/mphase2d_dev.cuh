@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(128) k_mp_faces(const R* __restrict__ T, R* __
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int fx = g.nx + (D == 0), fy = g.ny + (D == 1);
-    double smax = 0.0;
+    R smax_r = R(0);  // in the solver's type: the maximum of FP32 speeds is the same taken in FP32
     bool bad = false;
     if (i < fx && j < fy) {
         const long long eR = (long long)(j + 1) * (g.nx + 2) + (i + 1);
@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(128) k_mp_faces(const R* __restrict__ T, R* __
                 VR[c] = T[((long long)c * 8 + (2 * D) * 2 + q) * g.NE + eR];
             }
             const R s = rot_hllc2<R, MODEL>(e, VL, VR, R(D == 0), R(D == 1), fl, bad);
-            smax = fmax(smax, (double)s);
+            smax_r = fmax(smax_r, s);
 #pragma unroll
             for (int c = 0; c <= NV; ++c) acc[c] += R(0.5) * fl[c];
         }
@@ -427,7 +427,8 @@ __global__ void __launch_bounds__(128) k_mp_faces(const R* __restrict__ T, R* __
         if (bad) atomicMin(&ds->bad, (unsigned long long)((long long)(j < g.ny ? j : g.ny - 1) * g.nx + (i < g.nx ? i : g.nx - 1)));
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) smax = fmax(smax, __shfl_xor_sync(0xffffffffu, smax, o));
+    for (int o = 16; o > 0; o >>= 1) smax_r = fmax(smax_r, __shfl_xor_sync(0xffffffffu, smax_r, o));
+    const double smax = (double)smax_r;
     if ((threadIdx.x & 31) == 0 && smax > 0.0) atomicMax(&ds->smax_bits[slot], (unsigned long long)__double_as_longlong(smax));
 }
 

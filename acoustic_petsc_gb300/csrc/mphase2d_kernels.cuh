@@ -23,7 +23,12 @@ constexpr int MAXV = 6;
 struct Eos {
     int model;  // HYPE_MP_DI4 or HYPE_MP_KAPILA5
     double g1, p1, g2, p2;
+    float g1f, p1f, g2f, p2f;  // the same rounded to FP32 (the FP32 form's mixture)
 };
+
+inline Eos make_eos(int model, double g1, double p1, double g2, double p2) {
+    return Eos{model, g1, p1, g2, p2, (float)g1, (float)p1, (float)g2, (float)p2};
+}
 
 // basis of the 10-term polynomial (reconstruction.c:11-48)
 __host__ __device__ inline double basis2(double x, double y, int n) {
@@ -207,7 +212,7 @@ __device__ __forceinline__ void mix_r(const Eos& e, R a, R& g, R& pi) {
         g = (R)gd;
         pi = (R)pd;
     } else {
-        const float g1 = (float)e.g1, g2 = (float)e.g2, p1 = (float)e.p1, p2 = (float)e.p2;
+        const float g1 = e.g1f, g2 = e.g2f, p1 = e.p1f, p2 = e.p2f;
         const float a2 = 1.0f - a;
         if (e.model == HYPE_MP_DI4) g = 1.0f + (g1 - 1.0f) * (g2 - 1.0f) / (a2 * (g1 - 1.0f) + a * (g2 - 1.0f));
         else g = 1.0f + ((g1 - 1.0f) * (g2 - 1.0f)) / ((g2 - 1.0f) * a + (g1 - 1.0f) * a2);
