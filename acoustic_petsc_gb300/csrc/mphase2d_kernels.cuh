@@ -24,10 +24,20 @@ struct Eos {
     int model;  // HYPE_MP_DI4 or HYPE_MP_KAPILA5
     double g1, p1, g2, p2;
     float g1f, p1f, g2f, p2f;  // the same rounded to FP32 (the FP32 form's mixture)
+    int stiff_nonneg;          // both gamma > 1 and both stiffnesses >= 0: the mixture's pi >= 0
+    float rho_floor_f, p_floor_f;  // 1e-14 and 1e-12 rounded up to FP32: for a float x, (double)x < c iff x < c_f
 };
 
+inline float float_at_or_above(double c) {
+    float f = (float)c;
+    if ((double)f < c) f = nextafterf(f, INFINITY);
+    return f;
+}
+
 inline Eos make_eos(int model, double g1, double p1, double g2, double p2) {
-    return Eos{model, g1, p1, g2, p2, (float)g1, (float)p1, (float)g2, (float)p2};
+    return Eos{model, g1, p1, g2, p2, (float)g1, (float)p1, (float)g2, (float)p2,
+               (p1 >= 0.0 && p2 >= 0.0 && g1 > 1.0 && g2 > 1.0) ? 1 : 0, float_at_or_above(1.0e-14),
+               float_at_or_above(1.0e-12)};
 }
 
 // basis of the 10-term polynomial (reconstruction.c:11-48)
@@ -254,11 +264,11 @@ __device__ __forceinline__ void cons2prim(const Eos& e, const double* Q, double*
 template <typename R>
 __device__ __forceinline__ bool pad_ok(const Eos& e, const R* V) {
     double g, pi;
-    const bool stiff_nonneg = e.p1 >= 0.0 && e.p2 >= 0.0 && e.g1 > 1.0 && e.g2 > 1.0;
+    const bool stiff_nonneg = e.stiff_nonneg != 0;
     if constexpr (sizeof(R) == sizeof(float)) {
         // the same tests on the FP32 values without converting them: for a float x, (double)x < c
         // exactly when x < c rounded up to a float
-        const float rho_floor = __double2float_ru(1.0e-14), p_floor = __double2float_ru(1.0e-12);
+        const float rho_floor = e.rho_floor_f, p_floor = e.p_floor_f;
         const int ia = e.model == HYPE_MP_DI4 ? 4 : 5, ip = ia - 1;
         const float a = V[ia], p = V[ip];
         if (V[0] < rho_floor || (e.model != HYPE_MP_DI4 && V[1] < rho_floor) || a < 0.0f || a > 1.0f) return false;
