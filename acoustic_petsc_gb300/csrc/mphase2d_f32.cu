@@ -76,10 +76,10 @@ int launch_rhs_f32(int model, bool learned, const double* Win, float* Pf, void* 
     return HYPE_OK;
 }
 
-// The FP32 form's stage update from its FP32 face fluxes: each flux difference of the conserved
-// variables is taken in FP32 (exact where the two fluxes lie within a factor 2, i.e. in smooth flow)
-// and scaled in FP64; the volume-fraction term (a u)' - a u', which cancels, and the stage
-// combination are formed in FP64 as k_mp_update does.
+// The FP32 form's stage update from its FP32 face fluxes: the divergence of each conserved variable
+// in FP32 (the flux differences exact where the two fluxes lie within a factor 2, i.e. in smooth
+// flow); the volume-fraction term (a u)' - a u', which cancels, and the stage combination are
+// formed in FP64 as k_mp_update does.
 // Win, X, Y and out may be one array (in-place stages), so they carry no __restrict__
 __global__ void __launch_bounds__(256) k_mp_update_f32(const float* __restrict__ F, const float* __restrict__ G,
                                                        const double* Win, const double* X, const double* Y, double* out,
@@ -93,6 +93,7 @@ __global__ void __launch_bounds__(256) k_mp_update_f32(const float* __restrict__
     const long long cell = (long long)j * g.nx + i;
     const double a = Win[ia * g.N + cell];
     const double cdt = st.rhs_only ? 0.0 : st.c * ds->dt / st.d;
+    const float r1hf = (float)r1_h;
     for (int c = 0; c < nv; ++c) {
         double L;
         if (c == ia) {
@@ -104,7 +105,7 @@ __global__ void __launch_bounds__(256) k_mp_update_f32(const float* __restrict__
         } else {
             const float dx = F[c * nfx + fxl + 1] - F[c * nfx + fxl];
             const float dy = G[c * nfy + fyl + g.nx] - G[c * nfy + fyl];
-            L = -r1_h * (double)dx - r1_h * (double)dy;
+            L = (double)(-r1hf * (dx + dy));
         }
         double v;
         if (st.rhs_only) {
