@@ -47,6 +47,12 @@ def test_invalid_arguments_rejected_without_gpu(hype):
     m[0].nx = 2
     assert L.hype_batch_create(1, m, C.byref(h)) == H.HYPE_ERR_ARG
     assert L.hype_euler_step(None, 1, None, None, None) == H.HYPE_ERR_ARG
+    # the learned gate's per-step option and flag readback, 3D and 2D
+    buf = (C.c_ubyte * 8)()
+    assert L.hype_euler_set_gate_per_step(None, 1) == H.HYPE_ERR_ARG
+    assert L.hype_euler_gate_flags(None, buf, 0) == H.HYPE_ERR_ARG
+    assert L.hype_mp2d_set_gate_per_step(None, 1) == H.HYPE_ERR_ARG
+    assert L.hype_mp2d_gate_flags(None, buf, 1) == H.HYPE_ERR_ARG
 
 
 def test_library_is_in_tree(hype):
